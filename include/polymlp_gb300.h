@@ -1,0 +1,163 @@
+/*
+ * polymlp_gb300.h - C ABI of libpolymlp_gb300.so, the GB300 (sm_103a) hot path
+ * of the polynomial machine-learning potential (pypolymlp).
+ *
+ * Every entry point returns 0 on success and a non-zero status on failure;
+ * pg_last_error() returns the message of the last failure on this thread.
+ * No entry point calls exit(), and none takes or returns torch types.
+ * Buffers are caller-owned; host pointers unless a function says otherwise.
+ *
+ * Reference interfaces that these entry points replace are cited per
+ * function (paths inside sekocha/pypolymlp).
+ */
+#ifndef POLYMLP_GB300_H
+#define POLYMLP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/*
+ * Model settings.  Mirrors struct feature_params
+ * (src/pypolymlp/cxx/src/polymlp/polymlp_mlpcpp.h:55), which the reference
+ * fills from params.as_dict() in convert_params_dict_to_feature_params
+ * (src/pypolymlp/cxx/src/compute/py_params.cpp:11).
+ */
+typedef struct pg_feature_params {
+    int n_type;
+    int feature_type;          /* 0 = "pair", 1 = "gtinv" */
+    int model_type;            /* 1..4 */
+    int max_p;                 /* 1..3 */
+    int max_l;
+    double cutoff;
+    int n_fn;                  /* number of radial functions */
+    const double* pair_params; /* n_fn x 2, row-major (beta, mu) */
+    const int* cond_offsets;   /* n_type*n_type + 1 offsets; entry (i, j), i <= j, row-major */
+    const int* cond_values;    /* active radial indices of each type pair */
+    int n_lcomb;               /* gtinv: number of l combinations */
+    const int* lcomb_offsets;  /* n_lcomb + 1 */
+    const int* lcomb_values;   /* l values of each combination */
+    const int* lmseq_offsets;  /* n_lcomb + 1, cumulative number of m-combinations */
+    const int* lmseq_values;   /* per m-combination: order entries, each l*l+l+m */
+    const double* lm_coeffs;   /* one coefficient per m-combination */
+} pg_feature_params;
+
+/*
+ * A batch of periodic structures.  axis: n_st x 3 x 3 row-major, columns are
+ * the lattice vectors (as PolymlpStructure.axis).  positions: Cartesian,
+ * atom-major (sum(n_atoms) x 3).  types: sum(n_atoms) type indices.
+ */
+typedef struct pg_structures {
+    int n_st;
+    const int* n_atoms;
+    const double* axis;
+    const double* positions;
+    const int* types;
+} pg_structures;
+
+typedef struct pg_model pg_model;
+typedef struct pg_gram pg_gram;
+typedef struct pg_eval pg_eval;
+
+enum { PG_FP64 = 0, PG_MIXED = 1 };
+
+/* Message of the last failure on the calling thread (truncated to len). */
+int pg_last_error(char* buf, size_t len);
+
+/* Number of visible CUDA devices (0 when none); fails if the runtime is unusable. */
+int pg_device_count(int* count);
+
+/*
+ * Model tables.  Replaces Model(fp) / PolymlpAPI::set_features
+ * (src/pypolymlp/cxx/src/compute/model.cpp:11,
+ *  src/pypolymlp/cxx/src/polymlp/polymlp_api.cpp:44).
+ */
+int pg_model_create(const pg_feature_params* fp, pg_model** out);
+int pg_model_destroy(pg_model* m);
+int pg_model_n_features(const pg_model* m, int* n_features);
+
+/*
+ * Feature attributes, as FeaturesAttr
+ * (src/pypolymlp/cxx/src/compute/py_features_attr.cpp:11).  Sizes are written
+ * to *n_linear (radial/gtinv/tcomb entries), *n_tcomb_values (flattened type
+ * combinations) and *n_poly_values (flattened polynomial ids); pass NULL
+ * arrays to query sizes.
+ */
+int pg_model_feature_attrs(const pg_model* m, int* n_linear, int* radial_ids, int* gtinv_ids,
+                           int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values,
+                           int* n_poly, int* n_poly_values, int* poly_offsets, int* poly_values);
+
+/*
+ * X rows of a batch of structures, as PotentialModel
+ * (src/pypolymlp/cxx/src/compute/py_model.cpp:10-56 with Model::run,
+ *  src/pypolymlp/cxx/src/compute/model.cpp:39).  For structure s, the energy
+ * row is e_row[s]; if f_row[s] >= 0 the 3*n_atoms force rows start there
+ * (atom-major x, y, z) and the 6 stress rows (xx, yy, zz, xy, yz, zx) start at
+ * s_row[s].  x is column-major with leading dimension ld (>= every row used);
+ * rows of this batch are overwritten, other rows are untouched.
+ * precision: PG_FP64 or PG_MIXED (FP32 features, FP64 sums over neighbours).
+ */
+int pg_features_x(pg_model* m, const pg_structures* st, const int64_t* e_row,
+                  const int64_t* f_row, const int64_t* s_row, double* x, int64_t ld,
+                  int precision);
+
+/*
+ * Fused regression assembly: X rows are generated on the device, weighted,
+ * and summed into X^T X, X^T y, y^T y and the column sums of the (unweighted)
+ * energy rows, without X leaving the GPU.  Replaces the sequential loop of
+ * calc_xtx_xty (src/pypolymlp/mlp_dev/core/data_sequential.py:25-152) with its
+ * numpy x.T @ x (src/pypolymlp/mlp_dev/core/utils_sequential.py:94).
+ * w and y are per-row weights and weighted targets of this batch in the row
+ * layout given by e_row/f_row/s_row (relative to the batch, ld = n_rows).
+ */
+int pg_gram_create(pg_model* m, int precision, pg_gram** out);
+int pg_gram_destroy(pg_gram* g);
+int pg_gram_accumulate(pg_gram* g, const pg_structures* st, const int64_t* e_row,
+                       const int64_t* f_row, const int64_t* s_row, int64_t n_rows,
+                       const double* w, const double* y);
+/* Results (host): xtx F x F (full symmetric), xty F, yty, xe_sum F, xe_sq_sum F, n_rows. */
+int pg_gram_result(pg_gram* g, double* xtx, double* xty, double* yty, double* xe_sum,
+                   double* xe_sq_sum, int64_t* n_rows_total);
+
+/*
+ * Ridge solve over alphas in ascending order on the device, as solver_ridge
+ * (src/pypolymlp/mlp_dev/standard/solvers.py:48-84) with LAPACK posv: for each
+ * alpha, Cholesky of xtx + alpha*I and two triangular solves.  xtx (F x F) and
+ * xty (F) are host arrays; coefs is F x n_alpha column-major.  info[i] != 0
+ * marks a failed factorisation, for which the column is filled with 1e30.
+ */
+int pg_solve_ridge(int n_features, const double* xtx, const double* xty, const double* alphas,
+                   int n_alpha, double* coefs, int* info);
+
+/*
+ * Energy / force / stress evaluation, as PotentialPropertiesFast
+ * (src/pypolymlp/cxx/src/compute/py_properties_fast.cpp:10-77 with
+ *  PolymlpEval::eval, src/pypolymlp/cxx/src/compute/polymlp_eval.cpp:24).
+ * coeffs are already divided by the column scales (as in polymlp.yaml).
+ * energy: n_st; forces: sum(n_atoms) x 3 (atom-major); stress: n_st x 6 in
+ * eV per cell (xx, yy, zz, xy, yz, zx).
+ */
+int pg_eval_create(const pg_feature_params* fp, const double* coeffs, int n_coeffs, int precision,
+                   pg_eval** out);
+int pg_eval_destroy(pg_eval* e);
+int pg_eval_run(pg_eval* e, const pg_structures* st, double* energy, double* forces,
+                double* stress);
+
+/*
+ * Neighbour lists (test surface, as NeighborFull / NeighborHalf,
+ * src/pypolymlp/cxx/src/compute/neighbor_full.cpp:10,
+ * src/pypolymlp/cxx/src/compute/neighbor_half.cpp:10).  For one structure:
+ * offsets (n_atoms + 1), neighbour index and displacement pos[j] - pos[i] + t
+ * (3 per entry).  Pass NULL arrays to query *n_entries first.
+ */
+int pg_neighbor_list(const pg_structures* st, int structure, double cutoff, int half,
+                     int64_t* n_entries, int* offsets, int* neighbors, double* diffs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POLYMLP_GB300_H */

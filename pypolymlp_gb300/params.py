@@ -1,0 +1,132 @@
+"""Model-parameter dictionaries in the reference's FFI format.
+
+`make_params_dict` builds the dictionary that ``PolymlpParamsSingle.as_dict()``
+produces (src/pypolymlp/core/data_format.py:268) for the settings of
+``set_all_params`` (src/pypolymlp/core/params_utils.py:141): Gaussian radial
+parameters as ``set_gaussian_params`` makes them (product of two linspaces,
+plus the constant (0, 0) function appended at the end, params_utils.py:69-93),
+and every radial function active for every type pair.  The gtinv tables
+(l_comb, lm_seq, lm_coeffs) are the reference's invariant tables for the
+chosen order and l_max; they are loaded from JSON files written from the
+reference's Readgtinv (tests/golden/gtinv/).
+"""
+
+from __future__ import annotations
+
+import itertools
+import json
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GTINV_DIR = os.path.join(_REPO, "tests", "golden", "gtinv")
+
+
+def gtinv_file(order: int, maxl: Sequence[int], version: int = 1) -> str:
+    tag = "_".join(str(int(v)) for v in list(maxl)[: max(order - 1, 0)])
+    return os.path.join(GTINV_DIR, f"gtinv_v{version}_order{order}_maxl{tag}.json")
+
+
+def load_gtinv(order: int, maxl: Sequence[int], version: int = 1):
+    path = gtinv_file(order, maxl, version)
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"gtinv tables for order={order} maxl={tuple(maxl)} not found at {path}; "
+            "generate them with tests/golden/make_golden.py where the reference is available"
+        )
+    with open(path) as f:
+        d = json.load(f)
+    return d["l_comb"], d["lm_seq"], d["lm_coeffs"]
+
+
+def gaussian_params(params1=(1.0, 1.0, 1), params2=(0.0, 5.0, 7)):
+    g1 = np.linspace(float(params1[0]), float(params1[1]), int(params1[2]))
+    g2 = np.linspace(float(params2[0]), float(params2[1]), int(params2[2]))
+    pp = [[float(a), float(b)] for a, b in itertools.product(g1, g2)]
+    pp.append([0.0, 0.0])
+    return pp
+
+
+def make_params_dict(
+    n_type: int,
+    cutoff: float,
+    model_type: int,
+    max_p: int,
+    feature_type: str = "gtinv",
+    gaussian_params1=(1.0, 1.0, 1),
+    gaussian_params2=(0.0, 5.0, 7),
+    gtinv_order: int = 3,
+    gtinv_maxl: Sequence[int] = (4, 4, 2, 1, 1),
+    gtinv_tables: Optional[tuple] = None,
+    elements: Optional[Sequence[str]] = None,
+    include_force: bool = True,
+    include_stress: bool = True,
+    alphas: Optional[Sequence[float]] = None,
+) -> dict:
+    pair_params = gaussian_params(gaussian_params1, gaussian_params2)
+    cond = {}
+    for i in range(n_type):
+        for j in range(i, n_type):
+            cond[(i, j)] = list(range(len(pair_params)))
+    if feature_type == "gtinv":
+        if gtinv_tables is None:
+            gtinv_tables = load_gtinv(gtinv_order, gtinv_maxl)
+        l_comb, lm_seq, lm_coeffs = gtinv_tables
+        max_l = int(max(gtinv_maxl[: max(gtinv_order - 1, 1)])) if gtinv_order > 1 else 0
+        gtinv = {
+            "order": gtinv_order,
+            "max_l": list(gtinv_maxl),
+            "n_type": n_type,
+            "lm_seq": lm_seq,
+            "l_comb": l_comb,
+            "lm_coeffs": lm_coeffs,
+            "version": 1,
+        }
+    else:
+        max_l = 0
+        gtinv = {"order": 0, "max_l": [], "n_type": n_type, "lm_seq": [], "l_comb": [],
+                 "lm_coeffs": [], "version": 1}
+    if elements is None:
+        elements = [f"E{i}" for i in range(n_type)]
+    return {
+        "n_type": n_type,
+        "elements": list(elements),
+        "model": {
+            "cutoff": float(cutoff),
+            "model_type": int(model_type),
+            "max_p": int(max_p),
+            "max_l": max_l,
+            "feature_type": feature_type,
+            "gtinv": gtinv,
+            "pair_type": "gaussian",
+            "pair_conditional": False,
+            "pair_params": pair_params,
+            "pair_params_conditional": cond,
+        },
+        "include_force": include_force,
+        "include_stress": include_stress,
+        "print_memory": False,
+        "alphas": list(alphas) if alphas is not None else None,
+    }
+
+
+def to_json(params_dict: dict) -> str:
+    """JSON form (tuple keys become "i,j")."""
+    d = json.loads(json.dumps(params_dict, default=lambda o: o.tolist() if hasattr(o, "tolist") else str(o)))
+    model = dict(params_dict["model"])
+    cond = model.get("pair_params_conditional") or {}
+    d["model"]["pair_params_conditional"] = {
+        (f"{k[0]},{k[1]}" if isinstance(k, tuple) else str(k)): list(v) for k, v in cond.items()
+    }
+    return json.dumps(d)
+
+
+def from_json(text: str) -> dict:
+    d = json.loads(text)
+    cond = d["model"].get("pair_params_conditional") or {}
+    d["model"]["pair_params_conditional"] = {
+        tuple(int(a) for a in k.split(",")): v for k, v in cond.items()
+    }
+    return d
