@@ -1,0 +1,165 @@
+"""ctypes binding of libpolymlp_gb300.so (include/polymlp_gb300.h).
+
+The library is built in-tree by `pypolymlp_gb300.build.build()`.  There is no
+CPU fallback: if the library or a CUDA device is missing, every entry point
+raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from .abi import FeatureParams, Structures
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libpolymlp_gb300.so")
+_lib = None
+_lock = threading.Lock()
+
+PG_FP64 = 0
+PG_MIXED = 1
+
+_i64p = C.POINTER(C.c_int64)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+
+class GB300Error(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise GB300Error(
+                    f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                    "(there is no CPU fallback)"
+                )
+            L = C.CDLL(LIB_PATH)
+            L.pg_last_error.argtypes = [C.c_char_p, C.c_size_t]
+            L.pg_device_count.argtypes = [_ip]
+            L.pg_model_create.argtypes = [_vp, C.POINTER(_vp)]
+            L.pg_model_destroy.argtypes = [_vp]
+            L.pg_model_n_features.argtypes = [_vp, _ip]
+            L.pg_model_feature_attrs.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip]
+            L.pg_features_x.argtypes = [_vp, _vp, _i64p, _i64p, _i64p, _dp, C.c_int64, C.c_int]
+            L.pg_neighbor_list.argtypes = [_vp, C.c_int, C.c_double, C.c_int, _i64p, _ip, _ip, _dp]
+            for name, args in [
+                ("pg_gram_create", [_vp, C.c_int, C.POINTER(_vp)]),
+                ("pg_gram_destroy", [_vp]),
+                ("pg_gram_accumulate", [_vp, _vp, _i64p, _i64p, _i64p, C.c_int64, _dp, _dp]),
+                ("pg_gram_result", [_vp, _dp, _dp, _dp, _dp, _dp, _i64p]),
+                ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
+                ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
+                ("pg_eval_destroy", [_vp]),
+                ("pg_eval_run", [_vp, _vp, _dp, _dp, _dp]),
+            ]:
+                if hasattr(L, name):
+                    getattr(L, name).argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != 0:
+        buf = C.create_string_buffer(4096)
+        lib().pg_last_error(buf, 4096)
+        raise GB300Error(buf.value.decode(errors="replace"))
+
+
+def device_count() -> int:
+    n = C.c_int()
+    check(lib().pg_device_count(C.byref(n)))
+    return n.value
+
+
+def require_device():
+    if device_count() < 1:
+        raise GB300Error("no CUDA device is visible: the GB300 hot path has no CPU fallback")
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Model:
+    """Handle of pg_model (model tables uploaded to the device)."""
+
+    def __init__(self, params_dict: dict):
+        require_device()
+        self.fp = FeatureParams(params_dict)
+        self.params_dict = params_dict
+        h = _vp()
+        check(lib().pg_model_create(C.cast(self.fp.ref(), _vp), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.pg_model_destroy(h)
+            self._h = None
+
+    @property
+    def n_features(self) -> int:
+        n = C.c_int()
+        check(lib().pg_model_n_features(self._h, C.byref(n)))
+        return n.value
+
+    def features_x(self, st: Structures, e_row, f_row, s_row, n_rows: int, precision: int = PG_FP64, out=None):
+        nf = self.n_features
+        if out is None:
+            out = np.zeros((n_rows, nf), dtype=np.float64, order="F")
+        if out.dtype != np.float64 or not out.flags["F_CONTIGUOUS"] or out.shape[1] != nf:
+            raise ValueError("out must be a Fortran-ordered float64 array with n_features columns")
+        e_row = np.ascontiguousarray(e_row, dtype=np.int64)
+        f_row = np.ascontiguousarray(f_row, dtype=np.int64)
+        s_row = np.ascontiguousarray(s_row, dtype=np.int64)
+        check(lib().pg_features_x(self._h, C.cast(st.ref(), _vp), _p(e_row, C.c_int64), _p(f_row, C.c_int64),
+                                  _p(s_row, C.c_int64), _p(out, C.c_double), C.c_int64(out.shape[0]),
+                                  int(precision)))
+        return out
+
+    def feature_attrs(self):
+        L = lib()
+        nl, ntv, npoly, npv = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        null = C.POINTER(C.c_int)()
+        check(L.pg_model_feature_attrs(self._h, C.byref(nl), null, null, C.byref(ntv), null, null, C.byref(npoly),
+                                       C.byref(npv), null, null))
+        rad = np.zeros(max(nl.value, 1), np.int32)
+        gt = np.zeros(max(nl.value, 1), np.int32)
+        tco = np.zeros(nl.value + 1, np.int32)
+        tcv = np.zeros(max(ntv.value, 1), np.int32)
+        po = np.zeros(npoly.value + 1, np.int32)
+        pv = np.zeros(max(npv.value, 1), np.int32)
+        check(L.pg_model_feature_attrs(self._h, C.byref(nl), _p(rad, C.c_int), _p(gt, C.c_int), C.byref(ntv),
+                                       _p(tco, C.c_int), _p(tcv, C.c_int), C.byref(npoly), C.byref(npv),
+                                       _p(po, C.c_int), _p(pv, C.c_int)))
+        tcomb = [tcv[tco[i]:tco[i + 1]].tolist() for i in range(nl.value)]
+        poly = [pv[po[i]:po[i + 1]].tolist() for i in range(npoly.value)]
+        return rad[:nl.value].tolist(), gt[:nl.value].tolist(), tcomb, poly
+
+
+def neighbor_list(st: Structures, s: int, cutoff: float):
+    L = lib()
+    n = C.c_int64()
+    null_i = C.POINTER(C.c_int)()
+    check(L.pg_neighbor_list(C.cast(st.ref(), _vp), s, cutoff, 0, C.byref(n), null_i, null_i,
+                             C.POINTER(C.c_double)()))
+    na = int(st.n_atoms[s])
+    offs = np.zeros(na + 1, np.int32)
+    nb = np.zeros(max(n.value, 1), np.int32)
+    d = np.zeros((max(n.value, 1), 3))
+    check(L.pg_neighbor_list(C.cast(st.ref(), _vp), s, cutoff, 0, C.byref(n), _p(offs, C.c_int), _p(nb, C.c_int),
+                             _p(d, C.c_double)))
+    return offs, nb[:n.value], d[:n.value]

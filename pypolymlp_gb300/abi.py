@@ -146,6 +146,9 @@ class FeatureParams:
         s.lmseq_offsets = _ip_of(self._lm_offs)
         s.lmseq_values = _ip_of(self._lm_vals)
         s.lm_coeffs = _dp_of(self._coeffs)
+        # the struct keeps its buffers alive even if this owner is dropped
+        s._keep = (self._pair, self._cond_offs, self._cond_vals, self._lc_offs, self._lc_vals,
+                   self._lm_offs, self._lm_vals, self._coeffs)
         self.struct = s
         self.n_type = n_type
         self.cutoff = s.cutoff
@@ -189,6 +192,7 @@ class Structures:
         s.axis = _dp_of(self.axis)
         s.positions = _dp_of(self.positions)
         s.types = _ip_of(self.types)
+        s._keep = (self.n_atoms, self.axis, self.positions, self.types)
         self.struct = s
 
     @classmethod

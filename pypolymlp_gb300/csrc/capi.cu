@@ -1,0 +1,502 @@
+// C ABI of libpolymlp_gb300.so (declared in include/polymlp_gb300.h): model
+// creation, X rows, neighbour lists.  The regression assembly, solver and
+// evaluator entry points live in gram.cu, solve.cu and eval.cu.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "host/cell.h"
+#include "host/params.h"
+#include "kernels.h"
+#include "model.h"
+
+namespace pg {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+// ------------------------------------------------------------ DeviceModel
+void DeviceModel::build(const FlatModel& fm, int chunk_width) {
+    if (fm.n_type > kMaxTypes) throw std::runtime_error("at most 8 atom types are supported on the device");
+    bufs.clear();
+    bufs.reserve(64 * kMaxTypes);
+    auto up = [&](const auto& v) -> const void* {
+        bufs.emplace_back();
+        upload(bufs.back(), v);
+        return bufs.back().template as<void>();
+    };
+    chunk = chunk_width;
+    n_chunks = (fm.n_features + chunk - 1) / chunk;
+    dm = DevModel{};
+    dm.n_type = fm.n_type;
+    dm.n_tp = fm.n_tp;
+    dm.F = fm.n_features;
+    dm.n_fn_max = fm.n_fn_max;
+    dm.maxl = fm.maxl;
+    dm.n_ylm = fm.n_ylm;
+    dm.gtinv = fm.gtinv ? 1 : 0;
+    dm.cutoff = fm.cutoff;
+    dm.type_pairs = (const int*)up(fm.type_pairs);
+    dm.tp_nfn = (const int*)up(fm.tp_nfn);
+    dm.tp_beta = (const double*)up(fm.tp_beta);
+    dm.tp_mu = (const double*)up(fm.tp_mu);
+    chunk_cap_ent = 1;
+    for (int t = 0; t < fm.n_type; ++t) {
+        const FlatType& ft = fm.types[t];
+        DevType& d = dm.types[t];
+        d.K = ft.K;
+        d.K0 = ft.K0;
+        d.n_lin = ft.n_lin;
+        d.n_ent = (int)ft.ent_head.size();
+        d.head_tp = (const int*)up(ft.head_tp);
+        d.head_nid = (const int*)up(ft.head_nid);
+        d.head_key = (const int*)up(ft.head_key);
+        d.head_m = (const int*)up(ft.head_m);
+        d.head_full = (const int*)up(ft.head_full);
+        d.head_jloc = (const int*)up(ft.head_jloc);
+        d.head_signj = (const double*)up(ft.head_signj);
+        d.full_src = (const int*)up(ft.full_src);
+        d.full_is_conj = (const int*)up(ft.full_is_conj);
+        d.full_cc = (const double*)up(ft.full_cc);
+        d.val_off = (const int*)up(ft.val_off);
+        d.val_terms = (const FlatTerm*)up(ft.val_terms);
+        d.ent_off = (const int*)up(ft.ent_off);
+        d.ent_head = (const int*)up(ft.ent_head);
+        d.term_off = (const int*)up(ft.term_off);
+        d.g_terms = (const FlatTerm*)up(ft.g_terms);
+        d.col_ncomp = (const int*)up(ft.col_ncomp);
+        d.comp_k = (const int*)up(ft.comp_k);
+        d.comp_w = (const int*)up(ft.comp_w);
+        d.col_nent = (const int*)up(ft.col_nent);
+        std::vector<int> coff(fm.n_features, 0);
+        for (int c0 = 0; c0 < fm.n_features; c0 += chunk) {
+            int acc = 0;
+            for (int c = c0; c < std::min(fm.n_features, c0 + chunk); ++c) {
+                coff[c] = acc;
+                acc += ft.col_nent[c];
+            }
+            chunk_cap_ent = std::max(chunk_cap_ent, acc);
+        }
+        d.col_ent_off = (const int*)up(coff);
+        std::vector<int> meta(ft.ent_head.size());
+        for (size_t e = 0; e < ft.ent_head.size(); ++e) {
+            const int h = ft.ent_head[e];
+            if (ft.head_tp[h] > 255 || ft.head_nid[h] > 255 || ft.head_key[h] > 32767)
+                throw std::runtime_error("model too large for the packed entry metadata");
+            meta[e] = ft.head_tp[h] | (ft.head_nid[h] << 8) | (ft.head_key[h] << 16);
+        }
+        d.ent_meta = (const int*)up(meta);
+    }
+}
+
+// ------------------------------------------------------------ DeviceBatch
+void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
+    n_st = s_end - s_begin;
+    long long off0 = 0;
+    for (int s = 0; s < s_begin; ++s) off0 += st->n_atoms[s];
+    st_atom_off.assign(1, 0);
+    st_trans_off.assign(1, 0);
+    types.clear();
+    atom_st.clear();
+    trans.clear();
+    pos.clear();
+    long long a = off0;
+    for (int s = s_begin; s < s_end; ++s) {
+        const int n = st->n_atoms[s];
+        if (n < 0) throw std::runtime_error("negative atom count");
+        const CellTranslations ct = cell_translations(st->axis + 9 * (size_t)s, st->positions + 3 * a, n, cutoff);
+        for (const auto& t : ct.trans) trans.insert(trans.end(), t.begin(), t.end());
+        for (int i = 0; i < n; ++i) {
+            pos.insert(pos.end(), ct.pos[i].begin(), ct.pos[i].end());
+            types.push_back(st->types[a + i]);
+            atom_st.push_back(s - s_begin);
+        }
+        st_atom_off.push_back(st_atom_off.back() + n);
+        st_trans_off.push_back((int)(trans.size() / 3));
+        a += n;
+    }
+    n_atoms = st_atom_off.back();
+    upload(d_st_atom_off, st_atom_off);
+    upload(d_st_trans_off, st_trans_off);
+    upload(d_trans, trans);
+    upload(d_pos, pos);
+    upload(d_types, types);
+    upload(d_atom_st, atom_st);
+    DevBatch B = view(cutoff);
+    d_counts.reserve(sizeof(int) * std::max(1, n_atoms));
+    if (n_atoms > 0) launch_nb_count(B, d_counts.as<int>(), stream);
+    std::vector<int> counts(n_atoms);
+    if (n_atoms > 0)
+        PG_CUDA(cudaMemcpyAsync(counts.data(), d_counts.as<int>(), sizeof(int) * n_atoms, cudaMemcpyDeviceToHost,
+                                stream));
+    PG_CUDA(cudaStreamSynchronize(stream));
+    nb_off.assign(n_atoms + 1, 0);
+    for (int i = 0; i < n_atoms; ++i) nb_off[i + 1] = nb_off[i] + counts[i];
+    n_pairs = nb_off[n_atoms];
+    upload(d_nb_off, nb_off);
+    d_nb_j.reserve(sizeof(int) * std::max<long long>(1, n_pairs));
+    d_nb_d.reserve(sizeof(double) * 3 * std::max<long long>(1, n_pairs));
+    if (n_atoms > 0) launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), stream);
+}
+
+DevBatch DeviceBatch::view(double cutoff) const {
+    DevBatch B;
+    B.n_st = n_st;
+    B.n_atoms = n_atoms;
+    B.st_atom_off = d_st_atom_off.as<int>();
+    B.st_trans_off = d_st_trans_off.as<int>();
+    B.trans = d_trans.as<double>();
+    B.pos = d_pos.as<double>();
+    B.types = d_types.as<int>();
+    B.atom_st = d_atom_st.as<int>();
+    B.cutoff = cutoff;
+    return B;
+}
+
+// ------------------------------------------------------------ Model
+Model::Model(const pg_feature_params* p)
+    : tables(build_model_tables(feature_params_from_abi(p))), flat(flatten_model(tables)) {
+    int dev = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    dev64.build(flat, 128);
+    dev32.build(flat, 256);
+    max_k = max_k0 = 1;
+    for (const auto& ft : flat.types) {
+        max_k = std::max(max_k, ft.K);
+        max_k0 = std::max(max_k0, ft.K0);
+    }
+}
+
+// Per-atom storage offsets (a_nlm, features, adjoint entries) of a staged batch.
+void Model::atom_offsets(const DeviceBatch& b, size_t t_size, std::vector<long long>& a_off,
+                         std::vector<long long>& d_off, std::vector<long long>& g_off, long long& a_tot,
+                         long long& d_tot, long long& g_tot) const {
+    a_off.resize(b.n_atoms);
+    d_off.resize(b.n_atoms);
+    g_off.resize(b.n_atoms);
+    a_tot = d_tot = g_tot = 0;
+    for (int i = 0; i < b.n_atoms; ++i) {
+        const auto& ft = flat.types[b.types[i]];
+        a_off[i] = a_tot;
+        d_off[i] = d_tot;
+        g_off[i] = g_tot;
+        a_tot += ft.K0;
+        d_tot += ft.n_lin;
+        g_tot += (long long)ft.ent_head.size();
+    }
+    (void)t_size;
+}
+
+size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
+    size_t mx = 0;
+    for (const auto& ft : flat.types) {
+        const size_t ts = fp64 ? 8 : 4;
+        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts + ft.ent_head.size() * 2 * ts;
+        mx = std::max(mx, b);
+    }
+    return mx + (size_t)(mean_pairs * 28.0) + (size_t)flat.n_features * 3 * (fp64 ? 8 : 4);
+}
+
+// Rows of one staged batch into Xd (device, column-major, leading dim ld), in
+// the batch-local row layout given by e_row/f_row/s_row (device arrays).
+template <typename T>
+void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row,
+                       const long long* d_s_row, const std::vector<long long>& f_row_host, T* Xd, long long ld,
+                       cudaStream_t stream) {
+    const bool fp64 = sizeof(T) == 8;
+    const DeviceModel& dmod = fp64 ? dev64 : dev32;
+    const DevBatch B = b.view(flat.cutoff);
+    std::vector<long long> a_off, d_off, g_off;
+    long long a_tot, d_tot, g_tot;
+    atom_offsets(b, sizeof(T), a_off, d_off, g_off, a_tot, d_tot, g_tot);
+    upload(d_a_off, a_off);
+    upload(d_d_off, d_off);
+    upload(d_g_off, g_off);
+    s_A.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
+    s_D.reserve(sizeof(T) * std::max<long long>(1, d_tot));
+    s_G.reserve(2 * sizeof(T) * std::max<long long>(1, g_tot));
+    if (b.n_atoms > 0) {
+        launch_anlm<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                       d_a_off.as<long long>(), s_A.as<double2>(), max_k0, stream);
+        launch_features_adjoint<T>(dmod.dm, B, d_a_off.as<long long>(), s_A.as<double2>(),
+                                   d_d_off.as<long long>(), s_D.as<T>(), d_g_off.as<long long>(), s_G.as<void>(),
+                                   max_k, stream);
+    }
+    // work items: blocks of kRowsTR target atoms per structure
+    std::vector<RowItem> items;
+    std::vector<int> item_off(1, 0);
+    for (int s = 0; s < b.n_st; ++s) {
+        const int n = b.st_atom_off[s + 1] - b.st_atom_off[s];
+        const bool force = f_row_host[s] >= 0;
+        const int nblk = force ? std::max(1, (n + kRowsTR - 1) / kRowsTR) : 1;
+        for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * kRowsTR});
+        item_off.push_back((int)items.size());
+    }
+    upload(d_items, items);
+    upload(d_item_off, item_off);
+    s_partial.reserve(sizeof(double) * 7 * (size_t)flat.n_features * std::max<size_t>(1, items.size()));
+    if (!items.empty()) {
+        launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                       d_d_off.as<long long>(), s_D.as<T>(), d_g_off.as<long long>(), s_G.as<void>(),
+                       d_items.as<RowItem>(), (int)items.size(), d_f_row, dmod.chunk, dmod.n_chunks,
+                       dmod.chunk_cap_ent, Xd, ld, s_partial.as<double>(), stream);
+        launch_rows_reduce<T>(flat.n_features, b.n_st, d_item_off.as<int>(), s_partial.as<double>(), d_e_row,
+                              d_s_row, Xd, ld, stream);
+    }
+    PG_CUDA(cudaGetLastError());
+}
+
+template void Model::batch_rows<double>(DeviceBatch&, const long long*, const long long*, const long long*,
+                                        const std::vector<long long>&, double*, long long, cudaStream_t);
+template void Model::batch_rows<float>(DeviceBatch&, const long long*, const long long*, const long long*,
+                                       const std::vector<long long>&, float*, long long, cudaStream_t);
+
+// Split [0, n_st) into batches whose staged data fits the device budget.
+std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bool fp64, size_t budget) const {
+    std::vector<std::pair<int, int>> out;
+    const size_t per_atom = bytes_per_atom(fp64, 300.0);
+    const long long max_atoms = std::max<long long>(1, (long long)(budget / std::max<size_t>(1, per_atom)));
+    int s0 = 0;
+    long long acc = 0;
+    for (int s = 0; s < st->n_st; ++s) {
+        if (s > s0 && acc + st->n_atoms[s] > max_atoms) {
+            out.push_back({s0, s});
+            s0 = s;
+            acc = 0;
+        }
+        acc += st->n_atoms[s];
+    }
+    if (s0 < st->n_st) out.push_back({s0, st->n_st});
+    return out;
+}
+
+size_t device_budget_bytes() {
+    if (const char* e = std::getenv("PG_BATCH_BYTES")) return (size_t)std::atoll(e);
+    size_t free_b = 0, total_b = 0;
+    PG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    return std::min<size_t>(free_b / 3, (size_t)16 << 30);
+}
+
+__global__ void pg_f32_to_f64(const float* src, double* dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+struct pg_model {
+    std::unique_ptr<Model> m;
+};
+
+extern "C" {
+
+int pg_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        std::strncpy(buf, g_last_error.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return 0;
+}
+
+int pg_device_count(int* count) {
+    return guarded([&] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) n = 0;
+        else if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+        *count = n;
+    });
+}
+
+int pg_model_create(const pg_feature_params* fp, pg_model** out) {
+    return guarded([&] {
+        if (!out) throw std::runtime_error("null output handle");
+        auto h = new pg_model;
+        try {
+            h->m = std::make_unique<Model>(fp);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int pg_model_destroy(pg_model* m) {
+    return guarded([&] { delete m; });
+}
+
+int pg_model_n_features(const pg_model* m, int* n) {
+    return guarded([&] {
+        if (!m) throw std::runtime_error("null model");
+        *n = m->m->flat.n_features;
+    });
+}
+
+int pg_model_feature_attrs(const pg_model* m, int* n_linear, int* radial_ids, int* gtinv_ids, int* n_tcomb_values,
+                           int* tcomb_offsets, int* tcomb_values, int* n_poly, int* n_poly_values,
+                           int* poly_offsets, int* poly_values) {
+    return guarded([&] {
+        if (!m) throw std::runtime_error("null model");
+        const ModelTables& mt = m->m->tables;
+        std::vector<int> rad, gt;
+        std::vector<std::vector<int>> tc, poly;
+        if (!mt.fp.gtinv) {
+            // ntp attributes in global order (py_features_attr.cpp:23-28)
+            for (int tp = 0; tp < mt.n_type_pairs; ++tp)
+                for (int n : mt.tp_to_n[tp]) {
+                    rad.push_back(n);
+                    tc.push_back({tp});
+                }
+        } else {
+            for (const auto& lt : mt.linear_terms) {
+                rad.push_back(lt.n);
+                gt.push_back(lt.lm_comb_id);
+                tc.push_back(mt.tp_combs[lt.order][lt.tp_comb_id]);
+            }
+        }
+        for (const auto& c : mt.comb2) poly.push_back(c);
+        for (const auto& c : mt.comb3) poly.push_back(c);
+        int ntv = 0, npv = 0;
+        for (const auto& v : tc) ntv += (int)v.size();
+        for (const auto& v : poly) npv += (int)v.size();
+        *n_linear = (int)rad.size();
+        *n_tcomb_values = ntv;
+        *n_poly = (int)poly.size();
+        *n_poly_values = npv;
+        if (!radial_ids) return;
+        int k = 0;
+        tcomb_offsets[0] = 0;
+        for (size_t i = 0; i < rad.size(); ++i) {
+            radial_ids[i] = rad[i];
+            if (gtinv_ids) gtinv_ids[i] = gt.empty() ? -1 : gt[i];
+            for (int v : tc[i]) tcomb_values[k++] = v;
+            tcomb_offsets[i + 1] = k;
+        }
+        k = 0;
+        poly_offsets[0] = 0;
+        for (size_t i = 0; i < poly.size(); ++i) {
+            for (int v : poly[i]) poly_values[k++] = v;
+            poly_offsets[i + 1] = k;
+        }
+    });
+}
+
+int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, const int64_t* f_row,
+                  const int64_t* s_row, double* x, int64_t ld, int precision) {
+    return guarded([&] {
+        if (!mh || !st || !x) throw std::runtime_error("null argument");
+        if (precision != PG_FP64 && precision != PG_MIXED) throw std::runtime_error("unknown precision");
+        Model& m = *mh->m;
+        const bool fp64 = precision == PG_FP64;
+        const int F = m.flat.n_features;
+        cudaStream_t stream = 0;
+        const auto batches = m.plan_batches(st, fp64, device_budget_bytes());
+        DeviceBatch b;
+        DevBuf Xd, X64, d_e, d_f, d_s;
+        for (const auto& bt : batches) {
+            const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
+            b.stage(st, s0, s1, m.flat.cutoff, stream);
+            // batch-local row layout: energies, stresses, forces
+            std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);
+            long long r = nb;
+            for (int q = 0; q < nb; ++q) le[q] = q;
+            for (int q = 0; q < nb; ++q)
+                if (f_row[s0 + q] >= 0) {
+                    ls[q] = r;
+                    r += 6;
+                }
+            for (int q = 0; q < nb; ++q)
+                if (f_row[s0 + q] >= 0) {
+                    lf[q] = r;
+                    r += 3LL * st->n_atoms[s0 + q];
+                }
+            const long long rows = r;
+            upload(d_e, le);
+            upload(d_f, lf);
+            upload(d_s, ls);
+            Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
+            double* X64p;
+            if (fp64) {
+                m.batch_rows<double>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf,
+                                     Xd.as<double>(), rows, stream);
+                X64p = Xd.as<double>();
+            } else {
+                m.batch_rows<float>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf,
+                                    Xd.as<float>(), rows, stream);
+                X64.reserve((size_t)rows * F * 8);
+                pg_f32_to_f64<<<1024, 256, 0, stream>>>(Xd.as<float>(), X64.as<double>(), (size_t)rows * F);
+                X64p = X64.as<double>();
+            }
+            PG_CUDA(cudaGetLastError());
+            // copy each local row range to the caller's rows (column-major)
+            auto copy_rows = [&](long long src_row, long long dst_row, long long n_rows) {
+                if (n_rows <= 0) return;
+                PG_CUDA(cudaMemcpy2DAsync(x + dst_row, (size_t)ld * sizeof(double), X64p + src_row,
+                                          (size_t)rows * sizeof(double), (size_t)n_rows * sizeof(double), F,
+                                          cudaMemcpyDeviceToHost, stream));
+            };
+            auto contiguous = [&](const int64_t* rr, int width_kind) {
+                long long expect = -1;
+                for (int q = 0; q < nb; ++q) {
+                    const long long w = width_kind == 0 ? 1 : (width_kind == 1 ? 6 : 3LL * st->n_atoms[s0 + q]);
+                    if (width_kind != 0 && f_row[s0 + q] < 0) continue;
+                    if (expect >= 0 && rr[s0 + q] != expect) return false;
+                    expect = rr[s0 + q] + w;
+                }
+                return true;
+            };
+            if (contiguous(e_row, 0)) {
+                copy_rows(0, e_row[s0], nb);
+            } else {
+                for (int q = 0; q < nb; ++q) copy_rows(le[q], e_row[s0 + q], 1);
+            }
+            const bool cs = contiguous(s_row, 1), cf = contiguous(f_row, 2);
+            long long ns = 0, nfr = 0, first_s = -1, first_f = -1;
+            for (int q = 0; q < nb; ++q)
+                if (f_row[s0 + q] >= 0) {
+                    if (first_s < 0) {
+                        first_s = q;
+                        first_f = q;
+                    }
+                    ns += 6;
+                    nfr += 3LL * st->n_atoms[s0 + q];
+                }
+            if (first_s >= 0) {
+                if (cs) copy_rows(ls[first_s], s_row[s0 + first_s], ns);
+                else
+                    for (int q = 0; q < nb; ++q)
+                        if (f_row[s0 + q] >= 0) copy_rows(ls[q], s_row[s0 + q], 6);
+                if (cf) copy_rows(lf[first_f], f_row[s0 + first_f], nfr);
+                else
+                    for (int q = 0; q < nb; ++q)
+                        if (f_row[s0 + q] >= 0) copy_rows(lf[q], f_row[s0 + q], 3LL * st->n_atoms[s0 + q]);
+            }
+            PG_CUDA(cudaStreamSynchronize(stream));
+        }
+    });
+}
+
+int pg_neighbor_list(const pg_structures* st, int structure, double cutoff, int half, int64_t* n_entries,
+                     int* offsets, int* neighbors, double* diffs) {
+    return guarded([&] {
+        if (half) throw std::runtime_error("half lists are built by the evaluator; use half = 0");
+        if (structure < 0 || structure >= st->n_st) throw std::runtime_error("structure index out of range");
+        DeviceBatch b;
+        b.stage(st, structure, structure + 1, cutoff, 0);
+        *n_entries = b.n_pairs;
+        if (!offsets) return;
+        for (int i = 0; i <= b.n_atoms; ++i) offsets[i] = (int)b.nb_off[i];
+        std::vector<int> nj(b.n_pairs);
+        if (b.n_pairs) {
+            PG_CUDA(cudaMemcpy(nj.data(), b.d_nb_j.as<int>(), sizeof(int) * b.n_pairs, cudaMemcpyDeviceToHost));
+            PG_CUDA(cudaMemcpy(diffs, b.d_nb_d.as<double>(), sizeof(double) * 3 * b.n_pairs, cudaMemcpyDeviceToHost));
+        }
+        for (long long k = 0; k < b.n_pairs; ++k) neighbors[k] = nj[k];  // batch holds one structure: local ids
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,232 @@
+// Device-side views of the model tables and of a batch of structures, and the
+// warp-cooperative pair basis (radial functions, Y_lm for m <= 0 and their
+// gradients) shared by the training and evaluation kernels.
+#pragma once
+
+#include <cstdint>
+
+#include "host/flat_tables.h"
+
+namespace pg {
+
+constexpr int kMaxTypes = 8;
+constexpr double kPiD = 3.1415926535897932384626433832795;
+
+template <typename T>
+struct cplx {
+    T re, im;
+};
+template <typename T>
+__device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T>
+__device__ __forceinline__ T creal_mul(cplx<T> a, cplx<T> b) {
+    return a.re * b.re - a.im * b.im;
+}
+
+struct DevType {
+    int K, K0, n_lin, n_ent;
+    const int *head_tp, *head_nid, *head_key, *head_m, *head_full, *head_jloc;
+    const double* head_signj;
+    const int *full_src, *full_is_conj;
+    const double* full_cc;
+    const int* val_off;
+    const FlatTerm* val_terms;
+    const int *ent_off, *ent_head, *term_off;
+    const FlatTerm* g_terms;
+    const int *col_ncomp, *comp_k, *comp_w, *col_nent, *col_ent_off;
+    const int* ent_meta;  // per G entry: tp | nid << 8 | key << 16
+};
+
+struct DevModel {
+    int n_type, n_tp, F, n_fn_max, maxl, n_ylm, gtinv;
+    double cutoff;
+    const int* type_pairs;
+    const int* tp_nfn;
+    const double *tp_beta, *tp_mu;
+    DevType types[kMaxTypes];
+};
+
+// Basis of one pair image, in shared memory, computed by one warp.
+template <typename T>
+struct BasisView {
+    T* fn;         // [n_fn_max]
+    T* fnd;        // [n_fn_max]
+    cplx<T>* Y;    // [n_ylm]
+    cplx<T>* dY;   // [3][n_ylm]
+    T* P;          // [n_ylm + 2] scratch
+    T* Q;          // [n_ylm + 2] scratch
+    T* cs;         // [maxl + 1] cos(m phi)
+    T* sn;         // [maxl + 1] sin(m phi)
+};
+
+template <typename T>
+__host__ __device__ inline size_t basis_slot_elems(int n_fn_max, int n_ylm, int maxl) {
+    // counted in units of T
+    return (size_t)2 * n_fn_max + 2 * (size_t)n_ylm * 4 + 2 * ((size_t)n_ylm + 2) + 2 * ((size_t)maxl + 1);
+}
+
+template <typename T>
+__device__ inline BasisView<T> basis_view(T* base, int n_fn_max, int n_ylm, int maxl) {
+    BasisView<T> v;
+    v.fn = base;
+    v.fnd = base + n_fn_max;
+    v.Y = reinterpret_cast<cplx<T>*>(base + 2 * n_fn_max);
+    v.dY = v.Y + n_ylm;
+    v.P = base + 2 * n_fn_max + 2 * (size_t)n_ylm * 4;
+    v.Q = v.P + n_ylm + 2;
+    v.cs = v.Q + n_ylm + 2;
+    v.sn = v.cs + maxl + 1;
+    return v;
+}
+
+__device__ __forceinline__ int lmi(int l, int m) { return l * (l + 1) / 2 + m; }
+
+// Radial functions of one type pair at distance dis
+// (polymlp_basis_function.h:16-43, polymlp_functions_interface.cpp:41-62).
+template <typename T, bool DERIV>
+__device__ inline void warp_radial(const DevModel& M, int tp, double dis, BasisView<T>& B, int lane) {
+    const int nfn = M.tp_nfn[tp];
+    const T r = (T)dis;
+    const T rc = (T)M.cutoff;
+    const T v1 = (T)kPiD / rc;
+    const T v2 = v1 * r;
+    T fc, fcd = 0;
+    if (DERIV) {
+        fc = (T)0.5 * (cos(v2) + (T)1.0);
+        fcd = (T)-0.5 * v1 * sin(v2);
+    } else {
+        fc = (T)0.5 * (cos((T)kPiD * r / rc) + (T)1.0);
+    }
+    for (int q = lane; q < nfn; q += 32) {
+        const T beta = (T)M.tp_beta[tp * M.n_fn_max + q];
+        const T mu = (T)M.tp_mu[tp * M.n_fn_max + q];
+        const T x = r - mu;
+        const T bf = exp(-beta * x * x);
+        B.fn[q] = bf * fc;
+        if (DERIV) B.fnd[q] = (T)-2.0 * beta * x * bf * fc + bf * fcd;
+    }
+}
+
+// Y_lm (m <= 0, index l(l+1)/2 + l + m) and gradients of the unit vector
+// (x, y, z)/r, following the normalised associated Legendre recursion of
+// polymlp_spherical_harmonics.cpp:27-209 (Limpanuparb & Milthorpe,
+// arXiv:1410.1748).  Lane m computes the Legendre column m; lanes then fill
+// the (l, m) table.  Caller must __syncwarp() before reading B.
+template <typename T, bool DERIV>
+__device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, double zd, double rd, BasisView<T>& B,
+                                int lane) {
+    const T x = (T)xd, y = (T)yd, z = (T)zd, r = (T)rd;
+    const T ct = z / r;
+    const T rho = hypot(x, y);
+    const T cp = rho > (T)0 ? x / rho : (T)1;
+    const T sp = rho > (T)0 ? y / rho : (T)0;
+    const T st = sqrt((T)1 - ct * ct);
+    const T s2pi = (T)0.39894228040143267794;
+    const T sq3 = (T)1.7320508075688772935, sq32 = (T)1.2247448713915890491;
+    const int L = maxl;
+    if (lane <= L) {
+        const int m = lane;
+        T pmm, qmm;
+        if (m == 0) {
+            pmm = s2pi;
+            qmm = 0;
+        } else {
+            pmm = -st * sq32 * s2pi;
+            qmm = -sq32 * s2pi;
+            for (int l = 2; l <= m; ++l) {
+                const T c1 = -sqrt((T)1.0 + (T)0.5 / (T)l) * st;
+                pmm = c1 * pmm;
+                qmm = c1 * qmm;
+            }
+        }
+        B.P[lmi(m, m)] = pmm;
+        B.Q[lmi(m, m)] = qmm;
+        if (m + 1 <= L) {
+            T p1, q1;
+            if (m == 0) {
+                p1 = ct * sq3 * s2pi;
+                q1 = 0;
+            } else {
+                const T c2 = sqrt((T)2.0 * (T)m + (T)3.0) * ct;
+                p1 = c2 * pmm;
+                q1 = c2 * qmm;
+            }
+            B.P[lmi(m + 1, m)] = p1;
+            B.Q[lmi(m + 1, m)] = q1;
+            T p2 = pmm, q2 = qmm;
+            for (int l = m + 2; l <= L; ++l) {
+                const T ls = (T)(l * l), lm1s = (T)((l - 1) * (l - 1)), ms = (T)(m * m);
+                const T alm = sqrt(((T)4.0 * ls - (T)1.0) / (ls - ms));
+                const T blm = -sqrt((lm1s - ms) / ((T)4.0 * lm1s - (T)1.0));
+                const T p = alm * (ct * p1 + blm * p2);
+                const T q = alm * (ct * q1 + blm * q2);
+                B.P[lmi(l, m)] = p;
+                B.Q[lmi(l, m)] = q;
+                p2 = p1;
+                q2 = q1;
+                p1 = p;
+                q1 = q;
+            }
+        }
+        // cos(m phi), sin(m phi) by the Chebyshev recurrence
+        T c1 = 1, c2 = cp, s1 = 0, s2 = -sp;
+        const T tc = (T)2 * c2;
+        for (int mp = 1; mp <= m; ++mp) {
+            const T s = tc * s1 - s2, c = tc * c1 - c2;
+            c2 = c1;
+            c1 = c;
+            s2 = s1;
+            s1 = s;
+        }
+        B.cs[m] = c1;
+        B.sn[m] = s1;
+    }
+    if (lane == 0) {
+        // Q_{l}^{1} for l = 0 reads index 1 (= Q_1^0 = 0); keep the slot past the end zero
+        B.P[n_ylm] = 0;
+        B.Q[n_ylm] = 0;
+        B.P[n_ylm + 1] = 0;
+        B.Q[n_ylm + 1] = 0;
+    }
+    __syncwarp();
+    const T h = (T)0.5 * (T)1.41421356237309504880;
+    const T invr = (T)1 / r;
+    for (int idx = lane; idx < n_ylm; idx += 32) {
+        int l = 0;
+        while ((l + 1) * (l + 2) / 2 <= idx) ++l;
+        const int mp = lmi(l, 0) + l - idx;  // m = -mp
+        if (mp == 0) {
+            B.Y[idx] = {B.P[lmi(l, 0)] * h, (T)0};
+            if (DERIV) {
+                const T qv = (l == 0) ? B.Q[1] : B.Q[lmi(l, 1)];
+                const T common = qv * st * invr * sqrt((T)0.5 * (T)l * (T)(l + 1));
+                B.dY[idx] = {common * ct * cp, (T)0};
+                B.dY[n_ylm + idx] = {common * ct * sp, (T)0};
+                B.dY[2 * n_ylm + idx] = {-common * st, (T)0};
+            }
+        } else {
+            const T sign = (mp & 1) ? (T)-1 : (T)1;
+            const T c = B.cs[mp], s = B.sn[mp];
+            const T tmp = sign * B.P[lmi(l, mp)] * h;
+            B.Y[idx] = {tmp * c, -(tmp * s)};
+            if (DERIV) {
+                const cplx<T> common = {c * h * invr, s * h * invr};
+                const T qlm = B.Q[lmi(l, mp)];
+                T dth = (T)mp * ct * qlm;
+                if (mp != l) dth += sqrt((T)((l - mp) * (l + mp + 1))) * B.Q[lmi(l, mp + 1)] * st;
+                const T dph = (T)mp * qlm;  // imaginary
+                // common * (dth*ct*cp - i*dph*sp)
+                cplx<T> ax = cmul(common, cplx<T>{dth * ct * cp, -dph * sp});
+                cplx<T> ay = cmul(common, cplx<T>{dth * ct * sp, dph * cp});
+                cplx<T> az = {-common.re * dth * st, -common.im * dth * st};
+                B.dY[idx] = {sign * ax.re, -sign * ax.im};
+                B.dY[n_ylm + idx] = {sign * ay.re, -sign * ay.im};
+                B.dY[2 * n_ylm + idx] = {sign * az.re, -sign * az.im};
+            }
+        }
+    }
+}
+
+}  // namespace pg

@@ -1,0 +1,157 @@
+// Flattening of ModelTables for device upload (see flat_tables.h).
+#include "flat_tables.h"
+
+#include <algorithm>
+#include <map>
+#include <stdexcept>
+
+namespace pg {
+namespace {
+
+FlatTerm make_term(double coeff, const std::vector<int>& ids, int conj) {
+    if ((int)ids.size() > kMaxOrder) throw std::runtime_error("product order exceeds the supported maximum (6)");
+    FlatTerm t{};
+    t.coeff = coeff;
+    t.n = (int)ids.size();
+    t.conj = conj;
+    for (int i = 0; i < kMaxOrder; ++i) t.ids[i] = i < t.n ? ids[i] : 0;
+    return t;
+}
+
+}  // namespace
+
+FlatModel flatten_model(const ModelTables& mt) {
+    FlatModel fm;
+    const auto& fp = mt.fp;
+    fm.n_type = fp.n_type;
+    fm.n_tp = mt.n_type_pairs;
+    fm.n_features = mt.n_features;
+    fm.gtinv = fp.gtinv;
+    fm.cutoff = fp.cutoff;
+    fm.maxl = fp.gtinv ? fp.maxl : 0;
+    fm.n_ylm = fp.gtinv ? (fp.maxl + 1) * (fp.maxl + 2) / 2 : 1;
+    for (int i = 0; i < fp.n_type; ++i)
+        for (int j = 0; j < fp.n_type; ++j) fm.type_pairs.push_back(mt.type_pairs[i][j]);
+    fm.n_fn_max = 1;
+    for (const auto& ns : mt.tp_to_n) fm.n_fn_max = std::max<int>(fm.n_fn_max, (int)ns.size());
+    fm.tp_beta.assign((size_t)fm.n_tp * fm.n_fn_max, 0.0);
+    fm.tp_mu.assign((size_t)fm.n_tp * fm.n_fn_max, 0.0);
+    for (int tp = 0; tp < fm.n_tp; ++tp) {
+        fm.tp_nfn.push_back((int)mt.tp_to_n[tp].size());
+        for (size_t q = 0; q < mt.tp_to_n[tp].size(); ++q) {
+            fm.tp_beta[(size_t)tp * fm.n_fn_max + q] = fp.params[mt.tp_to_n[tp][q]][0];
+            fm.tp_mu[(size_t)tp * fm.n_fn_max + q] = fp.params[mt.tp_to_n[tp][q]][1];
+        }
+    }
+    const int F = mt.n_features;
+    fm.types.resize(fp.n_type);
+    for (int t = 0; t < fp.n_type; ++t) {
+        const auto& tt = mt.types[t];
+        auto& ft = fm.types[t];
+        ft.n_lin = (int)tt.lin_index.size();
+        // heads and conj completion
+        if (fp.gtinv) {
+            ft.K = (int)tt.full.size();
+            ft.K0 = (int)tt.noconj.size();
+            for (const auto& e : tt.noconj) {
+                ft.head_tp.push_back(e.tp);
+                ft.head_nid.push_back(e.n_id);
+                ft.head_key.push_back(e.ylm_key);
+                ft.head_m.push_back(e.m);
+                ft.head_l.push_back(e.l);
+                ft.head_full.push_back(e.ilocal_id);
+                ft.head_jloc.push_back(e.jlocal_noconj_id);
+                ft.head_signj.push_back(e.sign_j);
+            }
+            ft.full_src.assign(ft.K, 0);
+            ft.full_cc.assign(ft.K, 1.0);
+            ft.full_is_conj.assign(ft.K, 0);
+            std::vector<int> full_to_head(ft.K, -1);
+            for (int h = 0; h < ft.K0; ++h) full_to_head[tt.noconj[h].ilocal_id] = h;
+            for (const auto& e : tt.full) {
+                if (e.conj) {
+                    ft.full_src[e.ilocal_id] = full_to_head.at(e.ilocal_conj_id);
+                    ft.full_cc[e.ilocal_id] = e.cc;
+                    ft.full_is_conj[e.ilocal_id] = 1;
+                } else {
+                    ft.full_src[e.ilocal_id] = full_to_head.at(e.ilocal_id);
+                }
+            }
+            // value terms
+            ft.val_off.push_back(0);
+            for (int k = 0; k < ft.n_lin; ++k) {
+                for (const auto& s : tt.value_terms[k]) ft.val_terms.push_back(make_term(s.coeff, s.ids, 0));
+                ft.val_off.push_back((int)ft.val_terms.size());
+            }
+            // G entries: per feature, group deriv terms by folded head
+            ft.ent_off.push_back(0);
+            ft.term_off.push_back(0);
+            for (int k = 0; k < ft.n_lin; ++k) {
+                std::map<int, std::vector<FlatTerm>> by_head;
+                for (const auto& d : tt.deriv_terms[k]) {
+                    const auto& fe = tt.full[d.head];
+                    if (fe.conj) {
+                        by_head[full_to_head.at(fe.ilocal_conj_id)].push_back(make_term(d.coeff, d.rest, 1));
+                    } else {
+                        by_head[full_to_head.at(d.head)].push_back(make_term(d.coeff, d.rest, 0));
+                    }
+                }
+                for (auto& kv : by_head) {
+                    ft.ent_head.push_back(kv.first);
+                    for (auto& term : kv.second) ft.g_terms.push_back(term);
+                    ft.term_off.push_back((int)ft.g_terms.size());
+                }
+                ft.ent_off.push_back((int)ft.ent_head.size());
+            }
+        } else {
+            ft.K = ft.K0 = (int)tt.ntp.size();
+            for (const auto& e : tt.ntp) {
+                ft.head_tp.push_back(e.tp);
+                ft.head_nid.push_back(e.n_id);
+                ft.head_key.push_back(0);
+                ft.head_m.push_back(0);
+                ft.head_l.push_back(0);
+                ft.head_full.push_back(e.ilocal_id);
+                ft.head_jloc.push_back(e.jlocal_id);
+                ft.head_signj.push_back(1.0);
+            }
+            ft.full_src.resize(ft.K);
+            for (int h = 0; h < ft.K; ++h) ft.full_src[h] = h;
+            ft.full_cc.assign(ft.K, 1.0);
+            ft.full_is_conj.assign(ft.K, 0);
+            ft.val_off.push_back(0);
+            ft.ent_off.push_back(0);
+            ft.term_off.push_back(0);
+            for (int k = 0; k < ft.n_lin; ++k) {
+                const int h = tt.value_terms[k][0].ids[0];
+                ft.val_terms.push_back(make_term(1.0, {h}, 0));
+                ft.val_off.push_back((int)ft.val_terms.size());
+                ft.ent_head.push_back(h);
+                ft.g_terms.push_back(make_term(1.0, {}, 0));
+                ft.term_off.push_back((int)ft.g_terms.size());
+                ft.ent_off.push_back((int)ft.ent_head.size());
+            }
+        }
+        // column recipes over all F columns
+        ft.col_ncomp.assign(F, 0);
+        ft.comp_k.assign((size_t)F * 3, -1);
+        ft.comp_w.assign((size_t)F * 6, -1);
+        ft.col_nent.assign(F, 0);
+        for (const auto& p : tt.poly) {
+            const int n = (int)p.local_ids.size();
+            ft.col_ncomp[p.col] = n;
+            for (int c = 0; c < n; ++c) {
+                ft.comp_k[(size_t)p.col * 3 + c] = p.local_ids[c];
+                int q = 0;
+                for (int o = 0; o < n; ++o)
+                    if (o != c) ft.comp_w[((size_t)p.col * 3 + c) * 2 + q++] = p.local_ids[o];
+                const int k = p.local_ids[c];
+                ft.col_nent[p.col] += ft.ent_off[k + 1] - ft.ent_off[k];
+            }
+        }
+        for (int c = 0; c < F; ++c) fm.max_nent_col = std::max(fm.max_nent_col, ft.col_nent[c]);
+    }
+    return fm;
+}
+
+}  // namespace pg

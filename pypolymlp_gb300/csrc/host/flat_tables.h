@@ -1,0 +1,63 @@
+// Flat (device-uploadable) form of the model tables.
+//
+// Naming: K = full a_nlm entries of a centre type, K0 = no-conjugate entries
+// (m <= 0), "head" = a no-conjugate entry.  For each linear feature k of a
+// type the adjoint vector G_k[h] = d(feature k)/d(a_h) (conjugate heads folded
+// into their m <= 0 partner) is stored sparsely as "G entries".
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "model_tables.h"
+
+namespace pg {
+
+constexpr int kMaxOrder = 6;  // gtinv order supported by the reference tables
+
+// One product term: coeff * prod(a[ids[0..n)]) (ids: full local ids).
+struct FlatTerm {
+    double coeff;
+    int n;
+    int conj;  // G terms: 1 if the term's head is the conjugate of the entry's head
+    int ids[kMaxOrder];
+};
+
+struct FlatType {
+    int K = 0, K0 = 0, n_lin = 0;
+    // heads (K0): meta for basis lookup and the evaluator
+    std::vector<int> head_tp, head_nid, head_key, head_m, head_l, head_full, head_jloc;
+    std::vector<double> head_signj;
+    // conj completion of full entries: src head index and cc (cc = 0 for heads)
+    std::vector<int> full_src;
+    std::vector<double> full_cc;
+    std::vector<int> full_is_conj;
+    // value terms per linear feature (CSR)
+    std::vector<int> val_off;
+    std::vector<FlatTerm> val_terms;
+    // G entries per linear feature (CSR over features), head per entry, terms per entry (CSR)
+    std::vector<int> ent_off, ent_head, term_off;
+    std::vector<FlatTerm> g_terms;
+    // per column (all F columns): recipe components.  comp_k[col*3+c] is the
+    // local linear feature (-1 = unused); comp_w[(col*3+c)*2+q] are the
+    // feature indices whose product weights the component (-1 = none).
+    std::vector<int> col_ncomp, comp_k, comp_w;
+    // per column: number of G entries (sum over its components), for smem sizing
+    std::vector<int> col_nent;
+    // evaluator: per head, the potential terms grouped (CSR) - built separately
+};
+
+struct FlatModel {
+    int n_type = 0, n_tp = 0, n_features = 0, n_fn_max = 0, maxl = 0, n_ylm = 0;
+    bool gtinv = true;
+    double cutoff = 0.0;
+    std::vector<int> type_pairs;        // n_type*n_type
+    std::vector<int> tp_nfn;            // radial functions per type pair
+    std::vector<double> tp_beta, tp_mu; // [tp*n_fn_max + n_id]
+    std::vector<FlatType> types;
+    int max_nent_col = 0;               // max G entries of a single column (any type)
+};
+
+FlatModel flatten_model(const ModelTables& mt);
+
+}  // namespace pg

@@ -126,8 +126,8 @@ struct Builder {
                 if (type_in_all_pairs({a.tp}, mt.type_pairs, t)) comb1_indices[t].push_back(a.global_id);
         for (const auto& a : global) {
             const int t1 = mt.tp_to_types[a.tp][0], t2 = mt.tp_to_types[a.tp][1];
-            for (int t : {t1, t2}) {
-                if (t == t2 && t1 == t2) break;
+            for (int q = 0; q < (t1 == t2 ? 1 : 2); ++q) {
+                const int t = q == 0 ? t1 : t2;
                 auto& tt = mt.types[t];
                 const int loc = global_to_local[{a.global_id, t}];
                 tt.value_terms.push_back({Term{1.0, {loc}}});

@@ -1,0 +1,51 @@
+// Device-side batch view and host launchers of the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_model.cuh"
+#include "runtime.h"
+
+namespace pg {
+
+// --------------------------------------------------------------- batch view
+struct DevBatch {
+    int n_st;
+    int n_atoms;
+    const int* st_atom_off;    // n_st + 1
+    const int* st_trans_off;   // n_st + 1
+    const double* trans;       // 3 per translation
+    const double* pos;         // 3 per atom (wrapped as NeighborCell does)
+    const int* types;          // per atom
+    const int* atom_st;        // per atom: structure index
+    double cutoff;
+};
+
+// Work item: (structure, first target atom of a block of TR atoms).
+struct RowItem {
+    int st;
+    int a0;
+};
+
+constexpr int kRowsTR = 32;  // target atoms per pg_rows block
+
+void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st);
+void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, cudaStream_t st);
+template <typename T>
+void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
+                 const long long* a_off, double2* A, int max_k0, cudaStream_t st);
+template <typename T>
+void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
+                             const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
+                             cudaStream_t st);
+size_t rows_smem_bytes(const DevModel& M, int chunk, int cap_ent, bool fp64);
+template <typename T>
+void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
+                 const long long* d_off, const T* D, const long long* g_off, const void* G, const RowItem* items,
+                 int n_items, const long long* f_row, int chunk, int n_chunks, int cap_ent, T* X, long long ld,
+                 double* partial, cudaStream_t st);
+template <typename T>
+void launch_rows_reduce(int F, int n_st, const int* item_off, const double* partial, const long long* e_row,
+                        const long long* s_row, T* X, long long ld, cudaStream_t st);
+
+}  // namespace pg

@@ -1,0 +1,35 @@
+// Uploaded model (tables + device views) and the per-batch X-row pipeline.
+#pragma once
+
+#include <utility>
+#include <vector>
+
+#include "kernels.h"
+#include "runtime.h"
+
+namespace pg {
+
+struct Model {
+    ModelTables tables;
+    FlatModel flat;
+    DeviceModel dev64, dev32;   // pg_rows column chunk of 128 (FP64) and 256 (FP32)
+    int max_k = 1, max_k0 = 1;
+    // per-batch scratch (grow-only)
+    DevBuf d_a_off, d_d_off, d_g_off, s_A, s_D, s_G, d_items, d_item_off, s_partial;
+
+    explicit Model(const pg_feature_params* p);
+
+    void atom_offsets(const DeviceBatch& b, size_t t_size, std::vector<long long>& a_off,
+                      std::vector<long long>& d_off, std::vector<long long>& g_off, long long& a_tot,
+                      long long& d_tot, long long& g_tot) const;
+    size_t bytes_per_atom(bool fp64, double mean_pairs) const;
+    std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
+
+    template <typename T>
+    void batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row, const long long* d_s_row,
+                    const std::vector<long long>& f_row_host, T* Xd, long long ld, cudaStream_t stream);
+};
+
+size_t device_budget_bytes();
+
+}  // namespace pg

@@ -1,0 +1,119 @@
+// Host runtime shared by the C ABI translation units: error reporting,
+// device buffers, the uploaded model and batch staging.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "device_model.cuh"
+#include "host/flat_tables.h"
+#include "host/model_tables.h"
+#include "polymlp_gb300.h"
+
+namespace pg {
+
+void set_last_error(const std::string& msg);
+
+#define PG_CUDA(call)                                                                                     \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call); \
+    } while (0)
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+    } catch (...) {
+        set_last_error("unknown error");
+    }
+    return 1;
+}
+
+// Owning device buffer (cudaMalloc/cudaFree).
+class DevBuf {
+  public:
+    DevBuf() = default;
+    explicit DevBuf(size_t bytes) { alloc(bytes); }
+    ~DevBuf() { release(); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p_(o.p_), n_(o.n_) {
+        o.p_ = nullptr;
+        o.n_ = 0;
+    }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p_ = o.p_;
+            n_ = o.n_;
+            o.p_ = nullptr;
+            o.n_ = 0;
+        }
+        return *this;
+    }
+    void alloc(size_t bytes) {
+        release();
+        if (bytes == 0) bytes = 16;
+        PG_CUDA(cudaMalloc(&p_, bytes));
+        n_ = bytes;
+    }
+    // grow-only reservation
+    void reserve(size_t bytes) {
+        if (bytes > n_) alloc(bytes);
+    }
+    void release() {
+        if (p_) cudaFree(p_);
+        p_ = nullptr;
+        n_ = 0;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p_);
+    }
+    size_t bytes() const { return n_; }
+
+  private:
+    void* p_ = nullptr;
+    size_t n_ = 0;
+};
+
+template <class V>
+void upload(DevBuf& b, const std::vector<V>& v) {
+    b.alloc(v.size() * sizeof(V));
+    if (!v.empty()) PG_CUDA(cudaMemcpy(b.as<void>(), v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+}
+
+// Model uploaded to the device for one column-chunk width.
+struct DeviceModel {
+    DevModel dm{};
+    int chunk = 0;            // columns per pg_rows block
+    int n_chunks = 0;
+    int chunk_cap_ent = 0;    // max G entries of a chunk (shared-memory sizing)
+    std::vector<DevBuf> bufs;
+    void build(const FlatModel& fm, int chunk_width);
+};
+
+// Batch of structures staged on the device with neighbour lists and per-atom data.
+struct DeviceBatch {
+    int n_st = 0, n_atoms = 0;
+    long long n_pairs = 0;
+    std::vector<int> st_atom_off, st_trans_off, types, atom_st;
+    std::vector<double> trans, pos;
+    DevBuf d_st_atom_off, d_st_trans_off, d_trans, d_pos, d_types, d_atom_st;
+    DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d;
+    std::vector<long long> nb_off;
+    // Build translations on the host and the full neighbour list on the device.
+    void stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream);
+    struct DevBatch view(double cutoff) const;
+};
+
+}  // namespace pg

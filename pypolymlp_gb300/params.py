@@ -114,13 +114,13 @@ def make_params_dict(
 
 def to_json(params_dict: dict) -> str:
     """JSON form (tuple keys become "i,j")."""
-    d = json.loads(json.dumps(params_dict, default=lambda o: o.tolist() if hasattr(o, "tolist") else str(o)))
-    model = dict(params_dict["model"])
-    cond = model.get("pair_params_conditional") or {}
+    d = dict(params_dict)
+    d["model"] = dict(params_dict["model"])
+    cond = d["model"].get("pair_params_conditional") or {}
     d["model"]["pair_params_conditional"] = {
-        (f"{k[0]},{k[1]}" if isinstance(k, tuple) else str(k)): list(v) for k, v in cond.items()
+        (f"{k[0]},{k[1]}" if isinstance(k, tuple) else str(k)): [int(a) for a in v] for k, v in cond.items()
     }
-    return json.dumps(d)
+    return json.dumps(d, default=lambda o: o.tolist() if hasattr(o, "tolist") else str(o))
 
 
 def from_json(text: str) -> dict:

@@ -1,0 +1,115 @@
+"""GPU X rows (pg_features_x through the C ABI) against the oracle and the
+reference's golden signatures.
+
+Tolerances: FP64 path 1e-10 relative to the column magnitude (the bar for
+features and derivatives); mixed path (FP32 features, FP64 neighbour sums)
+1e-4 relative to the column magnitude.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import assert_signature, load_golden
+from oracle import oracle
+from pypolymlp_gb300 import synthetic as syn
+from pypolymlp_gb300.abi import Structures, row_layout
+from pypolymlp_gb300.params import make_params_dict
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+MIXED_RTOL = 1e-4
+
+
+def _model(p):
+    from pypolymlp_gb300 import _ffi
+
+    return _ffi.Model(p)
+
+
+def _colrel(x, ref):
+    scale = np.maximum(np.abs(ref).max(axis=0), 1e-300)
+    return float((np.abs(x - ref) / scale).max())
+
+
+@pytest.mark.parametrize("name", ["x_cfg1.npz", "x_cfg2.npz", "x_cfg3.npz", "x_pair_mt2_p3.npz"])
+def test_fp64_rows_match_reference_signature(name):
+    from pypolymlp_gb300 import _ffi
+
+    params, st, gold = load_golden(name)
+    e, f, s, n = row_layout(st.n_atoms, [True] * st.n_st)
+    x = _model(params).features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
+    assert_signature(x, gold, rtol=FP64_RTOL)
+
+
+CASES = {
+    "binary_mt3": (dict(n_type=2, cutoff=7.0, model_type=3, max_p=2, gaussian_params2=(0, 5, 10), gtinv_order=3,
+                        gtinv_maxl=(8, 4)), lambda: syn.binary_set(3, seed=31)),
+    "ternary_mt4_p3": (dict(n_type=3, cutoff=5.0, model_type=4, max_p=3, gaussian_params2=(0, 4, 4), gtinv_order=3,
+                            gtinv_maxl=(6, 4)), lambda: syn.ternary_set(3, seed=32, n_range=(8, 70))),
+    "unary_order4": (dict(n_type=1, cutoff=6.0, model_type=2, max_p=2, gaussian_params2=(0, 5, 5), gtinv_order=4,
+                          gtinv_maxl=(8, 8, 2)), lambda: syn.fcc_set(2, seed=33)),
+    "pair_mt2_p3": (dict(n_type=2, cutoff=6.0, model_type=2, max_p=3, feature_type="pair",
+                         gaussian_params2=(0, 5, 6)), lambda: syn.binary_set(2, seed=34, n_min=16, n_max=40)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_rows_match_oracle(case):
+    from pypolymlp_gb300 import _ffi
+
+    kw, gen = CASES[case]
+    p = make_params_dict(**kw)
+    ss = gen()
+    st = Structures(ss.axis, ss.positions, ss.types)
+    force = [i % 3 != 1 for i in range(st.n_st)]  # mix energy-only structures in
+    e, f, s, n = row_layout(st.n_atoms, force)
+    ref = oracle.features_x(p, st, e, f, s, n)
+    m = _model(p)
+    x64 = m.features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
+    assert _colrel(x64, ref) < FP64_RTOL
+    x32 = m.features_x(st, e, f, s, n, precision=_ffi.PG_MIXED)
+    assert _colrel(x32, ref) < MIXED_RTOL
+
+
+def test_rows_deterministic():
+    from pypolymlp_gb300 import _ffi
+
+    kw, gen = CASES["binary_mt3"]
+    p = make_params_dict(**kw)
+    ss = gen()
+    st = Structures(ss.axis, ss.positions, ss.types)
+    e, f, s, n = row_layout(st.n_atoms, [True] * st.n_st)
+    m = _model(p)
+    a = m.features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
+    b = m.features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_neighbor_list_bit_exact():
+    from pypolymlp_gb300 import _ffi
+
+    ss = syn.ternary_set(8, seed=41)
+    st = Structures(ss.axis, ss.positions, ss.types)
+    for s in range(st.n_st):
+        go, gj, gd = _ffi.neighbor_list(st, s, 6.0)
+        oo, oj, od = oracle.neighbor_list(st, s, 6.0, half=False)
+        np.testing.assert_array_equal(go, oo)
+        np.testing.assert_array_equal(gj, oj)
+        np.testing.assert_array_equal(gd, od)
+
+
+def test_empty_and_single_atom_structures():
+    """A one-atom cell (self images only) and a structure without force rows."""
+    from pypolymlp_gb300 import _ffi
+
+    kw, _ = CASES["binary_mt3"]
+    p = make_params_dict(**kw)
+    axis = [np.eye(3) * 3.1, np.eye(3) * 8.0]
+    pos = [np.zeros((1, 3)), np.array([[0.0, 0.0, 0.0], [1.9, 0.3, 0.2]])]
+    types = [np.array([0]), np.array([0, 1])]
+    st = Structures(axis, pos, types)
+    e, f, s, n = row_layout(st.n_atoms, [True, True])
+    ref = oracle.features_x(p, st, e, f, s, n)
+    x = _model(p).features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
+    assert _colrel(x, ref) < FP64_RTOL
