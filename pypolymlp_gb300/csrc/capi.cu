@@ -228,8 +228,8 @@ void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long
     std::vector<int> item_off(1, 0);
     for (int s = 0; s < b.n_st; ++s) {
         const int n = b.st_atom_off[s + 1] - b.st_atom_off[s];
-        const bool force = f_row_host[s] >= 0;
-        const int nblk = force ? std::max(1, (n + kRowsTR - 1) / kRowsTR) : 1;
+        // every centre belongs to exactly one block (energy rows need all of them)
+        const int nblk = std::max(1, (n + kRowsTR - 1) / kRowsTR);
         for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * kRowsTR});
         item_off.push_back((int)items.size());
     }
@@ -287,9 +287,6 @@ __global__ void pg_f32_to_f64(const float* src, double* dst, size_t n) {
 
 using namespace pg;
 
-struct pg_model {
-    std::unique_ptr<Model> m;
-};
 
 extern "C" {
 

@@ -1,1 +1,417 @@
-// placeholder
+// Regression assembly on the device: X^T X, X^T y, y^T y and the energy-row
+// column statistics, replacing the numpy loop of calc_xtx_xty
+// (src/pypolymlp/mlp_dev/core/data_sequential.py:97-153) with X generated in
+// HBM by pg_rows.
+//
+//   pg_syrk_f64        FP64 judge path: upper-triangle tiles of X^T X on the
+//                      CUDA cores (64x64 tile per block, 4x4 per thread).
+//   pg_gram_bf16x3     mixed path: X (FP32) split into bf16 hi + lo, and
+//                      X^T X ~= hi^T hi + hi^T lo + lo^T hi accumulated in FP32
+//                      on the tensor cores, flushed into the FP64 Gram every
+//                      kFlushRows rows.
+//   helpers            energy-row sums, row weighting, X^T y.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+
+#include "kernels.h"
+#include "model.h"
+
+namespace pg {
+
+// ------------------------------------------------------------ statistics
+// xe_sum[c] += sum_r X[e_rows[r], c], xe_sq_sum[c] += sum X^2 (unweighted energy rows).
+template <typename T>
+__global__ void pg_energy_stats(const T* X, long long ld, int F, const long long* e_rows, int n_e, double* xe_sum,
+                                double* xe_sq) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= F) return;
+    double s = 0, q = 0;
+    for (int r = 0; r < n_e; ++r) {
+        const double v = (double)X[(size_t)c * ld + e_rows[r]];
+        s += v;
+        q += v * v;
+    }
+    xe_sum[c] += s;
+    xe_sq[c] += q;
+}
+
+// X[r, c] *= w[r]
+template <typename T>
+__global__ void pg_scale_rows(T* X, long long ld, long long n_rows, int F, const double* w) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    const T wr = (T)w[r];
+    for (int c = blockIdx.y; c < F; c += gridDim.y) X[(size_t)c * ld + r] *= wr;
+}
+
+// xty[c] += sum_r X[r, c] * y[r]  (one block per column, FP64 accumulation)
+template <typename T>
+__global__ void pg_xty(const T* X, long long ld, long long n_rows, const double* y, double* xty) {
+    const int c = blockIdx.x;
+    double s = 0;
+    for (long long r = threadIdx.x; r < n_rows; r += blockDim.x) s += (double)X[(size_t)c * ld + r] * y[r];
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) xty[c] += red[0];
+}
+
+// ------------------------------------------------------------ FP64 SYRK
+// G (F x F, column-major, upper triangle used) += X^T X over rows [0, n_rows).
+constexpr int kS64 = 64, kK64 = 16;
+
+__global__ void __launch_bounds__(256) pg_syrk_f64(const double* X, long long ld, long long n_rows, int F,
+                                                   const int2* tiles, double* G) {
+    const int2 tl = tiles[blockIdx.x];
+    const int i0 = tl.x * kS64, j0 = tl.y * kS64;
+    __shared__ double As[kK64][kS64 + 1];
+    __shared__ double Bs[kK64][kS64 + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4] = {};
+    for (long long k0 = 0; k0 < n_rows; k0 += kK64) {
+        // load: 16 rows x 64 columns each (row index fastest -> coalesced)
+        for (int q = threadIdx.x; q < kK64 * kS64; q += 256) {
+            const int kk = q % kK64, cc = q / kK64;
+            const long long r = k0 + kk;
+            const int ci = i0 + cc, cj = j0 + cc;
+            As[kk][cc] = (r < n_rows && ci < F) ? X[(size_t)ci * ld + r] : 0.0;
+            Bs[kk][cc] = (r < n_rows && cj < F) ? X[(size_t)cj * ld + r] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kK64; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                a[u] = As[kk][ty * 4 + u];
+                b[u] = Bs[kk][tx * 4 + u];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+            if (i < F && j < F && i <= j) G[(size_t)j * F + i] += acc[u][v];
+        }
+}
+
+// ------------------------------------------------------------ BF16x3 (mma.sync)
+constexpr int kT = 128;        // output tile (features x features)
+constexpr int kKc = 32;        // rows per k-chunk
+constexpr int kPad = 8;        // bf16 padding per smem row (bank spread)
+constexpr long long kFlushRows = 8192;
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x2(unsigned (&r)[2], const void* p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
+
+// 256 threads, 8 warps as 2 (M) x 4 (N); each warp 64 x 32 of the 128 x 128 tile.
+__global__ void __launch_bounds__(256) pg_gram_bf16x3(const float* X, long long ld, long long n_rows, int F,
+                                                      const int2* tiles, double* G) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int RS = kKc + kPad;  // row stride (bf16 elements)
+    __nv_bfloat16* Ah = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+    __nv_bfloat16* Al = Ah + kT * RS;
+    __nv_bfloat16* Bh = Al + kT * RS;
+    __nv_bfloat16* Bl = Bh + kT * RS;
+    const int2 tl = tiles[blockIdx.x];
+    const int i0 = tl.x * kT, j0 = tl.y * kT;
+    const bool diag = tl.x == tl.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp >> 2, wn = warp & 3;  // warp tile origin: (wm*64, wn*32)
+    float acc[4][4][4];                       // [m16 block][n8 block][frag]
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b)
+            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
+    long long since_flush = 0;
+    for (long long k0 = 0; k0 < n_rows; k0 += kKc) {
+        // load 128 columns x 32 rows for A (columns i0..) and B (j0..), split into hi/lo
+        for (int q = threadIdx.x; q < kT * kKc; q += 256) {
+            const int kk = q % kKc, cc = q / kKc;
+            const long long r = k0 + kk;
+            const int ci = i0 + cc;
+            const float va = (r < n_rows && ci < F) ? X[(size_t)ci * ld + r] : 0.f;
+            const __nv_bfloat16 ha = __float2bfloat16_rn(va);
+            Ah[cc * RS + kk] = ha;
+            Al[cc * RS + kk] = __float2bfloat16_rn(va - __bfloat162float(ha));
+            if (!diag) {
+                const int cj = j0 + cc;
+                const float vb = (r < n_rows && cj < F) ? X[(size_t)cj * ld + r] : 0.f;
+                const __nv_bfloat16 hb = __float2bfloat16_rn(vb);
+                Bh[cc * RS + kk] = hb;
+                Bl[cc * RS + kk] = __float2bfloat16_rn(vb - __bfloat162float(hb));
+            }
+        }
+        __syncthreads();
+        const __nv_bfloat16* BH = diag ? Ah : Bh;
+        const __nv_bfloat16* BL = diag ? Al : Bl;
+#pragma unroll
+        for (int ks = 0; ks < kKc; ks += 16) {
+            unsigned ah[4][4], al[4][4], bh[4][2], bl[4][2];
+#pragma unroll
+            for (int mi = 0; mi < 4; ++mi) {
+                const int row = wm * 64 + mi * 16 + (lane & 15);
+                const int col = ks + ((lane >> 4) << 3);
+                ldsm_x4(ah[mi], Ah + row * RS + col);
+                ldsm_x4(al[mi], Al + row * RS + col);
+            }
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni) {
+                const int row = wn * 32 + ni * 8 + (lane & 7);
+                const int col = ks + (((lane >> 3) & 1) << 3);
+                ldsm_x2(bh[ni], BH + row * RS + col);
+                ldsm_x2(bl[ni], BL + row * RS + col);
+            }
+#pragma unroll
+            for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni) {
+                    mma_bf16_16816(acc[mi][ni], al[mi], bh[ni]);
+                    mma_bf16_16816(acc[mi][ni], ah[mi], bl[ni]);
+                    mma_bf16_16816(acc[mi][ni], ah[mi], bh[ni]);
+                }
+        }
+        __syncthreads();
+        since_flush += kKc;
+        const bool last = k0 + kKc >= n_rows;
+        if (since_flush >= kFlushRows || last) {
+            // flush the FP32 partial sums into the FP64 Gram (this block owns the tile)
+#pragma unroll
+            for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+                for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const int i = i0 + wm * 64 + mi * 16 + (lane >> 2) + ((c >> 1) << 3);
+                        const int j = j0 + wn * 32 + ni * 8 + ((lane & 3) << 1) + (c & 1);
+                        if (i < F && j < F && i <= j) G[(size_t)j * F + i] += (double)acc[mi][ni][c];
+                        acc[mi][ni][c] = 0.f;
+                    }
+            since_flush = 0;
+        }
+    }
+}
+
+// Mirror the upper triangle into the lower one.
+__global__ void pg_symmetrize(double* G, int F) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j < F && i < j) G[(size_t)i * F + j] = G[(size_t)j * F + i];
+}
+
+void launch_syrk_f64(const double* X, long long ld, long long n_rows, int F, const int2* tiles, int n_tiles,
+                     double* G, cudaStream_t st) {
+    pg_syrk_f64<<<n_tiles, 256, 0, st>>>(X, ld, n_rows, F, tiles, G);
+}
+
+size_t gram_bf16_smem() { return (size_t)4 * kT * (kKc + kPad) * sizeof(__nv_bfloat16); }
+
+void launch_gram_bf16x3(const float* X, long long ld, long long n_rows, int F, const int2* tiles, int n_tiles,
+                        double* G, cudaStream_t st) {
+    const size_t smem = gram_bf16_smem();
+    PG_CUDA(cudaFuncSetAttribute(pg_gram_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pg_gram_bf16x3<<<n_tiles, 256, smem, st>>>(X, ld, n_rows, F, tiles, G);
+}
+
+// ------------------------------------------------------------ pg_gram object
+struct Gram {
+    Model* m;
+    int precision;
+    int F;
+    DevBuf G, xty, xe_sum, xe_sq, tiles64, tiles128, Xd, d_w, d_y, d_e, d_f, d_s, d_erows;
+    int n_tiles64 = 0, n_tiles128 = 0;
+    double yty = 0;
+    long long n_rows_total = 0;
+    DeviceBatch batch;
+    cudaStream_t stream = 0;
+
+    Gram(Model* mm, int prec) : m(mm), precision(prec), F(mm->flat.n_features) {
+        G.alloc((size_t)F * F * sizeof(double));
+        xty.alloc(F * sizeof(double));
+        xe_sum.alloc(F * sizeof(double));
+        xe_sq.alloc(F * sizeof(double));
+        PG_CUDA(cudaMemset(G.as<void>(), 0, G.bytes()));
+        PG_CUDA(cudaMemset(xty.as<void>(), 0, xty.bytes()));
+        PG_CUDA(cudaMemset(xe_sum.as<void>(), 0, xe_sum.bytes()));
+        PG_CUDA(cudaMemset(xe_sq.as<void>(), 0, xe_sq.bytes()));
+        auto tile_list = [&](int tsz, DevBuf& buf, int& n) {
+            const int nt = (F + tsz - 1) / tsz;
+            std::vector<int2> t;
+            for (int j = 0; j < nt; ++j)
+                for (int i = 0; i <= j; ++i) t.push_back(make_int2(i, j));
+            upload(buf, t);
+            n = (int)t.size();
+        };
+        tile_list(kS64, tiles64, n_tiles64);
+        tile_list(kT, tiles128, n_tiles128);
+    }
+
+    // One sub-batch of structures with its rows in batch-local layout.
+    void accumulate_batch(const pg_structures* st, int s0, int s1, const std::vector<long long>& le,
+                          const std::vector<long long>& lf, const std::vector<long long>& ls, long long rows,
+                          const std::vector<double>& w, const std::vector<double>& y) {
+        const bool fp64 = precision == PG_FP64;
+        batch.stage(st, s0, s1, m->flat.cutoff, stream);
+        upload(d_e, le);
+        upload(d_f, lf);
+        upload(d_s, ls);
+        Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
+        upload(d_w, w);
+        upload(d_y, y);
+        std::vector<long long> erows(le.begin(), le.end());
+        upload(d_erows, erows);
+        const int ne = (int)erows.size();
+        dim3 sg((unsigned)((rows + 255) / 256), (unsigned)std::min(F, 64));
+        if (fp64) {
+            double* X = Xd.as<double>();
+            m->batch_rows<double>(batch, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf, X, rows,
+                                  stream);
+            pg_energy_stats<double><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, d_erows.as<long long>(), ne,
+                                                                        xe_sum.as<double>(), xe_sq.as<double>());
+            pg_scale_rows<double><<<sg, 256, 0, stream>>>(X, rows, rows, F, d_w.as<double>());
+            pg_xty<double><<<F, 256, 0, stream>>>(X, rows, rows, d_y.as<double>(), xty.as<double>());
+            launch_syrk_f64(X, rows, rows, F, tiles64.as<int2>(), n_tiles64, G.as<double>(), stream);
+        } else {
+            float* X = Xd.as<float>();
+            m->batch_rows<float>(batch, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf, X, rows,
+                                 stream);
+            pg_energy_stats<float><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, d_erows.as<long long>(), ne,
+                                                                       xe_sum.as<double>(), xe_sq.as<double>());
+            pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, d_w.as<double>());
+            pg_xty<float><<<F, 256, 0, stream>>>(X, rows, rows, d_y.as<double>(), xty.as<double>());
+            launch_gram_bf16x3(X, rows, rows, F, tiles128.as<int2>(), n_tiles128, G.as<double>(), stream);
+        }
+        PG_CUDA(cudaGetLastError());
+        for (double v : y) yty += v * v;
+        n_rows_total += rows;
+    }
+};
+
+}  // namespace pg
+
+using namespace pg;
+
+struct pg_gram {
+    std::unique_ptr<Gram> g;
+};
+
+extern "C" {
+
+int pg_gram_create(pg_model* m, int precision, pg_gram** out) {
+    return guarded([&] {
+        if (!m || !out) throw std::runtime_error("null argument");
+        if (precision != PG_FP64 && precision != PG_MIXED) throw std::runtime_error("unknown precision");
+        auto h = new pg_gram;
+        try {
+            h->g = std::make_unique<Gram>(m->m.get(), precision);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int pg_gram_destroy(pg_gram* g) {
+    return guarded([&] { delete g; });
+}
+
+int pg_gram_accumulate(pg_gram* gh, const pg_structures* st, const int64_t* e_row, const int64_t* f_row,
+                       const int64_t* s_row, int64_t n_rows, const double* w, const double* y) {
+    return guarded([&] {
+        if (!gh || !st || !e_row || !f_row || !s_row || !w || !y) throw std::runtime_error("null argument");
+        Gram& g = *gh->g;
+        Model& m = *g.m;
+        for (int s = 0; s < st->n_st; ++s) {
+            if (e_row[s] < 0 || e_row[s] >= n_rows) throw std::runtime_error("energy row out of range");
+            if (f_row[s] >= 0 && (f_row[s] + 3LL * st->n_atoms[s] > n_rows || s_row[s] < 0 || s_row[s] + 6 > n_rows))
+                throw std::runtime_error("force/stress rows out of range");
+        }
+        const auto batches = m.plan_batches(st, g.precision == PG_FP64, device_budget_bytes());
+        for (const auto& bt : batches) {
+            const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
+            std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);
+            std::vector<double> wl, yl;
+            long long r = nb;
+            wl.resize(nb);
+            yl.resize(nb);
+            for (int q = 0; q < nb; ++q) {
+                le[q] = q;
+                wl[q] = w[e_row[s0 + q]];
+                yl[q] = y[e_row[s0 + q]];
+            }
+            for (int q = 0; q < nb; ++q)
+                if (f_row[s0 + q] >= 0) {
+                    ls[q] = r;
+                    for (int c = 0; c < 6; ++c) {
+                        wl.push_back(w[s_row[s0 + q] + c]);
+                        yl.push_back(y[s_row[s0 + q] + c]);
+                    }
+                    r += 6;
+                }
+            for (int q = 0; q < nb; ++q)
+                if (f_row[s0 + q] >= 0) {
+                    lf[q] = r;
+                    const long long nr = 3LL * st->n_atoms[s0 + q];
+                    for (long long c = 0; c < nr; ++c) {
+                        wl.push_back(w[f_row[s0 + q] + c]);
+                        yl.push_back(y[f_row[s0 + q] + c]);
+                    }
+                    r += nr;
+                }
+            g.accumulate_batch(st, s0, s1, le, lf, ls, r, wl, yl);
+        }
+    });
+}
+
+int pg_gram_result(pg_gram* gh, double* xtx, double* xty, double* yty, double* xe_sum, double* xe_sq_sum,
+                   int64_t* n_rows_total) {
+    return guarded([&] {
+        if (!gh) throw std::runtime_error("null gram");
+        Gram& g = *gh->g;
+        const int F = g.F;
+        dim3 grid((F + 255) / 256, F);
+        pg_symmetrize<<<grid, 256, 0, g.stream>>>(g.G.as<double>(), F);
+        PG_CUDA(cudaGetLastError());
+        PG_CUDA(cudaStreamSynchronize(g.stream));
+        if (xtx) PG_CUDA(cudaMemcpy(xtx, g.G.as<double>(), (size_t)F * F * sizeof(double), cudaMemcpyDeviceToHost));
+        if (xty) PG_CUDA(cudaMemcpy(xty, g.xty.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
+        if (xe_sum) PG_CUDA(cudaMemcpy(xe_sum, g.xe_sum.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
+        if (xe_sq_sum)
+            PG_CUDA(cudaMemcpy(xe_sq_sum, g.xe_sq.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
+        if (yty) *yty = g.yty;
+        if (n_rows_total) *n_rows_total = g.n_rows_total;
+    });
+}
+
+}  // extern "C"

@@ -1,6 +1,7 @@
 // Uploaded model (tables + device views) and the per-batch X-row pipeline.
 #pragma once
 
+#include <memory>
 #include <utility>
 #include <vector>
 
@@ -33,3 +34,8 @@ struct Model {
 size_t device_budget_bytes();
 
 }  // namespace pg
+
+// Opaque C handle of a model (include/polymlp_gb300.h).
+struct pg_model {
+    std::unique_ptr<pg::Model> m;
+};

@@ -1,1 +1,214 @@
-// placeholder
+// Ridge solve on the device in FP64, replacing solver_ridge
+// (src/pypolymlp/mlp_dev/standard/solvers.py:48-84), which calls LAPACK posv
+// (Cholesky of X^T X + alpha I, two triangular solves) for each alpha and
+// fills the coefficients with 1e30 when the factorisation fails (:40-44).
+//
+// Blocked right-looking Cholesky A = L L^T (lower, column-major, block 64):
+//   pg_chol_diag    factor the diagonal block in shared memory (one block),
+//   pg_chol_panel   panel rows below it: L21 = A21 L11^-T (one thread per row),
+//   pg_chol_update  trailing update A22 -= L21 L21^T (64x64 tiles, lower only).
+// Triangular solves L z = b and L^T x = z run in one block each.
+// A non-positive or non-finite pivot sets info = column + 1 and stops.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "runtime.h"
+
+namespace pg {
+
+constexpr int kCB = 64;
+
+__global__ void pg_add_diag(double* A, const double* A0, int F, double alpha) {
+    const size_t n = (size_t)F * F;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = q % F, j = q / F;
+        A[q] = A0[q] + (i == j ? alpha : 0.0);
+    }
+}
+
+// Factor A[k:k+b, k:k+b] in place (lower).  info[0] != 0 stops all later work.
+__global__ void pg_chol_diag(double* A, int F, int k, int* info) {
+    __shared__ double S[kCB][kCB + 1];
+    __shared__ int bad;
+    const int b = min(kCB, F - k);
+    if (threadIdx.x == 0) bad = 0;
+    if (*info != 0) return;
+    for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
+        const int i = q % b, j = q / b;
+        S[i][j] = A[(size_t)(k + j) * F + k + i];
+    }
+    __syncthreads();
+    for (int j = 0; j < b; ++j) {
+        if (threadIdx.x == 0) {
+            const double d = S[j][j];
+            if (!(d > 0.0) || !isfinite(d)) {
+                bad = k + j + 1;
+            } else {
+                S[j][j] = sqrt(d);
+            }
+        }
+        __syncthreads();
+        if (bad) break;
+        const double djj = S[j][j];
+        for (int i = j + 1 + threadIdx.x; i < b; i += blockDim.x) S[i][j] /= djj;
+        __syncthreads();
+        for (int q = threadIdx.x; q < (b - j - 1) * (b - j - 1); q += blockDim.x) {
+            const int i = j + 1 + q % (b - j - 1), c = j + 1 + q / (b - j - 1);
+            if (c <= i) S[i][c] -= S[i][j] * S[c][j];
+        }
+        __syncthreads();
+    }
+    if (bad) {
+        if (threadIdx.x == 0) *info = bad;
+        return;
+    }
+    for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
+        const int i = q % b, j = q / b;
+        if (j <= i) A[(size_t)(k + j) * F + k + i] = S[i][j];
+    }
+}
+
+// Rows i >= k+b: solve x L11^T = a (forward substitution along the row).
+__global__ void pg_chol_panel(double* A, int F, int k, const int* info) {
+    __shared__ double L[kCB][kCB + 1];
+    if (*info != 0) return;
+    const int b = min(kCB, F - k);
+    for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
+        const int i = q % b, j = q / b;
+        L[i][j] = A[(size_t)(k + j) * F + k + i];
+    }
+    __syncthreads();
+    const int row = k + b + blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= F) return;
+    double x[kCB];
+    for (int j = 0; j < b; ++j) {
+        double v = A[(size_t)(k + j) * F + row];
+        for (int p = 0; p < j; ++p) v -= x[p] * L[j][p];
+        x[j] = v / L[j][j];
+    }
+    for (int j = 0; j < b; ++j) A[(size_t)(k + j) * F + row] = x[j];
+}
+
+// A22 -= L21 L21^T over the lower triangle; tiles listed by (ti, tj), ti >= tj.
+__global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, const int2* tiles, const int* info) {
+    __shared__ double Pi[kCB][kCB + 1];
+    __shared__ double Pj[kCB][kCB + 1];
+    if (*info != 0) return;
+    const int b = min(kCB, F - k);
+    const int s0 = k + b;
+    const int2 t = tiles[blockIdx.x];
+    const int i0 = s0 + t.x * kCB, j0 = s0 + t.y * kCB;
+    for (int q = threadIdx.x; q < kCB * kCB; q += 256) {
+        const int r = q % kCB, p = q / kCB;
+        Pi[r][p] = (i0 + r < F && p < b) ? A[(size_t)(k + p) * F + i0 + r] : 0.0;
+        Pj[r][p] = (j0 + r < F && p < b) ? A[(size_t)(k + p) * F + j0 + r] : 0.0;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4] = {};
+    for (int p = 0; p < b; ++p) {
+        double a[4], c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a[u] = Pi[ty * 4 + u][p];
+            c[u] = Pj[tx * 4 + u][p];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], c[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+            if (i < F && j < F && j <= i) A[(size_t)j * F + i] -= acc[u][v];
+        }
+}
+
+// L z = b, then L^T x = z; one block of 1024 threads.
+__global__ void pg_chol_solve(const double* L, int F, const double* b, double* x, const int* info) {
+    extern __shared__ double v[];  // F entries
+    __shared__ double red[32];
+    if (*info != 0) {
+        for (int i = threadIdx.x; i < F; i += blockDim.x) x[i] = 1e30;
+        return;
+    }
+    for (int i = threadIdx.x; i < F; i += blockDim.x) v[i] = b[i];
+    __syncthreads();
+    for (int j = 0; j < F; ++j) {
+        const double zj = v[j] / L[(size_t)j * F + j];
+        __syncthreads();
+        if (threadIdx.x == 0) v[j] = zj;
+        for (int i = j + 1 + threadIdx.x; i < F; i += blockDim.x) v[i] -= L[(size_t)j * F + i] * zj;
+        __syncthreads();
+    }
+    // backward: x_j = (z_j - sum_{i>j} L[i,j] x_i) / L[j,j]
+    for (int j = F - 1; j >= 0; --j) {
+        double s = 0.0;
+        for (int i = j + 1 + threadIdx.x; i < F; i += blockDim.x) s += L[(size_t)j * F + i] * v[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (threadIdx.x == 0) v[j] = (v[j] - t) / L[(size_t)j * F + j];
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < F; i += blockDim.x) x[i] = v[i];
+}
+
+// Factor A (F x F, column-major, lower used) in place; returns info.
+int cholesky_device(double* A, int F, int* d_info, cudaStream_t st) {
+    std::vector<int2> tiles;
+    DevBuf d_tiles;
+    for (int k = 0; k < F; k += kCB) {
+        pg_chol_diag<<<1, 256, 0, st>>>(A, F, k, d_info);
+        const int b = std::min(kCB, F - k);
+        const int rest = F - k - b;
+        if (rest <= 0) break;
+        pg_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, F, k, d_info);
+        const int nt = (rest + kCB - 1) / kCB;
+        tiles.clear();
+        for (int i = 0; i < nt; ++i)
+            for (int j = 0; j <= i; ++j) tiles.push_back(make_int2(i, j));
+        upload(d_tiles, tiles);
+        pg_chol_update<<<(int)tiles.size(), 256, 0, st>>>(A, F, k, d_tiles.as<int2>(), d_info);
+    }
+    PG_CUDA(cudaGetLastError());
+    int info = 0;
+    PG_CUDA(cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    return info;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+extern "C" int pg_solve_ridge(int F, const double* xtx, const double* xty, const double* alphas, int n_alpha,
+                              double* coefs, int* info) {
+    return guarded([&] {
+        if (F <= 0 || !xtx || !xty || !alphas || !coefs || !info) throw std::runtime_error("bad arguments");
+        if ((size_t)F * sizeof(double) > 200 * 1024) throw std::runtime_error("n_features too large for the solver");
+        cudaStream_t st = 0;
+        DevBuf A0((size_t)F * F * 8), A((size_t)F * F * 8), b(F * 8), x(F * 8), d_info(sizeof(int));
+        PG_CUDA(cudaMemcpy(A0.as<void>(), xtx, (size_t)F * F * 8, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemcpy(b.as<void>(), xty, (size_t)F * 8, cudaMemcpyHostToDevice));
+        const size_t smem = (size_t)F * sizeof(double);
+        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        for (int a = 0; a < n_alpha; ++a) {
+            pg_add_diag<<<1024, 256, 0, st>>>(A.as<double>(), A0.as<double>(), F, alphas[a]);
+            PG_CUDA(cudaMemsetAsync(d_info.as<void>(), 0, sizeof(int), st));
+            info[a] = cholesky_device(A.as<double>(), F, d_info.as<int>(), st);
+            pg_chol_solve<<<1, 1024, smem, st>>>(A.as<double>(), F, b.as<double>(), x.as<double>(), d_info.as<int>());
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaMemcpy(coefs + (size_t)a * F, x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
+        }
+    });
+}

@@ -1,0 +1,287 @@
+"""Regression on the GPU: X^T X assembly, ridge solve and model selection.
+
+The data preparation restates the reference's semantics exactly, since it
+decides the targets and weights that the GPU Gram consumes:
+
+* minimum energy per atom over all datasets (get_min_energy,
+  src/pypolymlp/mlp_dev/core/utils.py:10-21),
+* row weights and weighted targets (apply_weights,
+  src/pypolymlp/mlp_dev/core/utils_weights.py:10-98),
+* column scales from the unweighted energy rows and zeroed columns
+  (compute_scales / round_scales, src/pypolymlp/mlp_dev/core/utils_scales.py:6-40;
+  data_sequential.py:76-90),
+* ridge solve for every alpha (solver_ridge, standard/solvers.py:48-84),
+* RMSE from Gram quantities and selection by test RMSE
+  (compute_rmse_seq / get_best_model, mlp_dev/core/utils_model_selection.py:37-117).
+
+X never leaves the device: pg_gram_accumulate generates the rows of a batch
+of structures, weights them and adds X^T X, X^T y, y^T y and the energy-row
+column sums in one call.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _ffi
+from .abi import Structures, row_layout
+
+
+@dataclass
+class Dataset:
+    """Structures with DFT energies, forces (N, 3 per structure) and stresses
+    (n_st x 6, xx yy zz xy yz zx, eV per cell), as the reference's Dataset
+    holds them after _set_properties (src/pypolymlp/core/dataset_utils.py:200-250)."""
+
+    axis: List[np.ndarray]
+    positions: List[np.ndarray]
+    types: List[np.ndarray]
+    energies: np.ndarray
+    forces: Optional[List[np.ndarray]] = None
+    stresses: Optional[np.ndarray] = None
+    include_force: bool = True
+    include_stress: bool = True
+    weight: float = 1.0
+    name: str = "data"
+
+    @classmethod
+    def from_structure_set(cls, sset, include_force=True, include_stress=True, weight=1.0, name="data"):
+        return cls(list(sset.axis), list(sset.positions), list(sset.types), np.asarray(sset.energies),
+                   sset.forces, sset.stresses, include_force, include_stress, weight, name)
+
+    def __len__(self):
+        return len(self.types)
+
+    @property
+    def total_n_atoms(self):
+        return np.array([len(t) for t in self.types], dtype=np.int64)
+
+    def slice(self, b, e):
+        return Dataset(self.axis[b:e], self.positions[b:e], self.types[b:e], self.energies[b:e],
+                       None if self.forces is None else self.forces[b:e],
+                       None if self.stresses is None else self.stresses[b:e],
+                       self.include_force, self.include_stress, self.weight, self.name)
+
+
+def get_min_energy(datasets: Sequence[Dataset]) -> float:
+    min_e = 1e10
+    for d in datasets:
+        if len(d.energies) == 0:
+            raise RuntimeError("Empty energy data.")
+        m = float(np.min(d.energies / d.total_n_atoms))
+        min_e = min(min_e, m)
+    return min_e
+
+
+def _weight_energy(energy, n_atoms, min_e):
+    e_per_atom = energy / n_atoms
+    e_th1, e_th2 = min_e * 0.75, min_e * 0.50
+    w = np.ones(len(energy))
+    w[e_per_atom > e_th1] = 0.5
+    w[e_per_atom > e_th2] = 0.3
+    w[e_per_atom > 0.0] = 0.1
+    return w
+
+
+def _weight_force(forces, tol=1e-12):
+    w = np.abs(forces)
+    w[w < tol] = tol
+    w = np.reciprocal(w)
+    w[w > 1.0] = 1.0
+    return w
+
+
+def _weight_stress(stress, weight_stress, tol=1e-12):
+    nonzero = np.abs(stress) > tol
+    log1 = np.ones(len(stress)) * np.log10(tol)
+    log1[nonzero] = np.log10(np.abs(stress)[nonzero])
+    w = np.power(5, -log1)
+    w[w > 1.0] = 1.0
+    return w * weight_stress
+
+
+def weights_and_targets(d: Dataset, min_e: float, weight_stress: float = 0.1):
+    """Row layout (energies, stresses, forces) of a dataset with its weights w
+    and weighted targets y (apply_weights)."""
+    n_atoms = d.total_n_atoms
+    force = [d.include_force] * len(d)
+    e_row, f_row, s_row, n_rows = row_layout(n_atoms, force)
+    w = np.ones(n_rows)
+    y = np.zeros(n_rows)
+    we = _weight_energy(np.asarray(d.energies, float), n_atoms, min_e) * d.weight
+    w[e_row] = we
+    y[e_row] = we * d.energies
+    if d.include_force:
+        fvec = np.concatenate([np.asarray(f, float).reshape(-1) for f in d.forces])
+        svec = np.asarray(d.stresses, float).reshape(-1)
+        f0 = int(f_row[0])
+        s0 = int(s_row[0])
+        wf = _weight_force(fvec) * d.weight
+        w[f0:f0 + len(fvec)] = wf
+        y[f0:f0 + len(fvec)] = wf * fvec
+        if d.include_stress:
+            ws = _weight_stress(svec, weight_stress * d.weight)
+            w[s0:s0 + len(svec)] = ws
+            y[s0:s0 + len(svec)] = ws * svec
+        else:
+            # stress rows are zeroed when forces are present without stresses
+            w[s0:s0 + len(svec)] = 0.0
+            y[s0:s0 + len(svec)] = 0.0
+    return e_row, f_row, s_row, n_rows, w, y
+
+
+class GramAccumulator:
+    """Owner of a pg_gram handle."""
+
+    def __init__(self, model: _ffi.Model, precision: int):
+        self.model = model
+        h = _ffi._vp()
+        _ffi.check(_ffi.lib().pg_gram_create(model.handle, int(precision), C.byref(h)))
+        self._h = h
+        self.F = model.n_features
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _ffi._lib is not None:
+            _ffi._lib.pg_gram_destroy(h)
+            self._h = None
+
+    def accumulate(self, st: Structures, e_row, f_row, s_row, n_rows, w, y):
+        e_row = np.ascontiguousarray(e_row, dtype=np.int64)
+        f_row = np.ascontiguousarray(f_row, dtype=np.int64)
+        s_row = np.ascontiguousarray(s_row, dtype=np.int64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        p = _ffi._p
+        _ffi.check(_ffi.lib().pg_gram_accumulate(self._h, C.cast(st.ref(), _ffi._vp), p(e_row, C.c_int64),
+                                                 p(f_row, C.c_int64), p(s_row, C.c_int64), C.c_int64(n_rows),
+                                                 p(w, C.c_double), p(y, C.c_double)))
+
+    def result(self):
+        F = self.F
+        xtx = np.zeros((F, F), order="F")
+        xty = np.zeros(F)
+        xe_sum = np.zeros(F)
+        xe_sq = np.zeros(F)
+        yty = C.c_double()
+        n = C.c_int64()
+        p = _ffi._p
+        _ffi.check(_ffi.lib().pg_gram_result(self._h, p(xtx, C.c_double), p(xty, C.c_double), C.byref(yty),
+                                             p(xe_sum, C.c_double), p(xe_sq, C.c_double), C.byref(n)))
+        return xtx, xty, yty.value, xe_sum, xe_sq, n.value
+
+
+@dataclass
+class DataXY:
+    xtx: np.ndarray
+    xty: np.ndarray
+    y_sq_norm: float
+    total_n_data: int
+    scales: np.ndarray
+    zero_ids: np.ndarray
+    min_energy: float
+    xe_sum: Optional[np.ndarray] = None
+    xe_sq_sum: Optional[np.ndarray] = None
+
+
+def compute_scales(scales, xe_sum, xe_sq_sum, n_data, include_force=True, threshold=1e-10):
+    if scales is None:
+        variance = xe_sq_sum / n_data - np.square(xe_sum / n_data)
+        variance[variance < 0.0] = 1.0
+        scales = np.sqrt(variance)
+    scales = np.array(scales, dtype=float)
+    if include_force:
+        zero_ids = np.abs(scales) < threshold
+    else:
+        zero_ids = np.abs(scales) < threshold * threshold
+    scales[zero_ids] = 1.0
+    return scales, zero_ids
+
+
+def calc_xtx_xty(model: _ffi.Model, datasets: Sequence[Dataset], precision: int = _ffi.PG_MIXED,
+                 scales=None, min_energy=None, weight_stress: float = 0.1, batch_size: int = 2000,
+                 scale_threshold: float = 1e-10) -> DataXY:
+    """GPU counterpart of calc_xtx_xty (data_sequential.py:25-94)."""
+    if min_energy is None:
+        min_energy = get_min_energy(datasets)
+    acc = GramAccumulator(model, precision)
+    for d in datasets:
+        for b in range(0, len(d), batch_size):
+            sub = d.slice(b, min(len(d), b + batch_size))
+            e_row, f_row, s_row, n_rows, w, y = weights_and_targets(sub, min_energy, weight_stress)
+            st = Structures(sub.axis, sub.positions, sub.types)
+            acc.accumulate(st, e_row, f_row, s_row, n_rows, w, y)
+    xtx, xty, yty, xe_sum, xe_sq, n_rows_total = acc.result()
+    n_data = sum(len(d.energies) for d in datasets)
+    include_force = any(d.include_force for d in datasets)
+    scales, zero_ids = compute_scales(scales, xe_sum, xe_sq, n_data, include_force, scale_threshold)
+    xtx[zero_ids] = 0.0
+    xtx[:, zero_ids] = 0.0
+    xty[zero_ids] = 0.0
+    xtx /= scales[:, np.newaxis]
+    xtx /= scales[np.newaxis, :]
+    xty /= scales
+    return DataXY(xtx, xty, yty, int(n_rows_total), scales, zero_ids, min_energy, xe_sum, xe_sq)
+
+
+def solver_ridge(xtx: np.ndarray, xty: np.ndarray, alphas: Sequence[float]) -> np.ndarray:
+    """Coefficients (F x n_alpha); a failed factorisation gives a column of 1e30."""
+    F = xtx.shape[0]
+    a = np.ascontiguousarray(np.asarray(alphas, dtype=np.float64))
+    A = np.asfortranarray(xtx, dtype=np.float64)
+    b = np.ascontiguousarray(xty, dtype=np.float64)
+    coefs = np.zeros((F, len(a)), order="F")
+    info = np.zeros(len(a), dtype=np.int32)
+    p = _ffi._p
+    _ffi.check(_ffi.lib().pg_solve_ridge(F, p(A, C.c_double), p(b, C.c_double), p(a, C.c_double), len(a),
+                                         p(coefs, C.c_double), p(info, C.c_int)))
+    return np.asarray(coefs), info
+
+
+def compute_rmse_seq(coefs_array, data_xy: DataXY, check_singular=False, error_threshold=1e6):
+    out = []
+    for c in coefs_array.T:
+        mse = (c @ (data_xy.xtx @ c) - 2 * c @ data_xy.xty + data_xy.y_sq_norm) / data_xy.total_n_data
+        out.append(np.sqrt(mse) if mse >= 0 else 1e10)
+    out = np.array(out)
+    if check_singular and np.all(out > error_threshold):
+        raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
+                           "This singularity issue might be reduced by increasing "
+                           "the value of alpha (the magnitude of the penalty term).")
+    return out
+
+
+@dataclass
+class FitResult:
+    coeffs: np.ndarray          # scaled coefficients of the best alpha
+    scales: np.ndarray
+    alpha: float
+    rmse_train: float
+    rmse_test: float
+    coefs_array: np.ndarray = field(repr=False, default=None)
+    rmse_train_array: np.ndarray = field(repr=False, default=None)
+    rmse_test_array: np.ndarray = field(repr=False, default=None)
+
+    @property
+    def scaled_coeffs(self):
+        """Coefficients divided by the scales (the polymlp.yaml convention)."""
+        return self.coeffs / self.scales
+
+
+def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
+        precision: int = _ffi.PG_MIXED, batch_size: int = 2000, model: Optional[_ffi.Model] = None) -> FitResult:
+    """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60)."""
+    model = model or _ffi.Model(params_dict)
+    train_xy = calc_xtx_xty(model, train, precision=precision, batch_size=batch_size)
+    coefs, _info = solver_ridge(train_xy.xtx, train_xy.xty, alphas)
+    rmse_train = compute_rmse_seq(coefs, train_xy, check_singular=True)
+    test_xy = calc_xtx_xty(model, test, precision=precision, scales=train_xy.scales,
+                           min_energy=train_xy.min_energy, batch_size=batch_size)
+    rmse_test = compute_rmse_seq(coefs, test_xy)
+    idx = int(np.argmin(rmse_test))
+    return FitResult(coefs[:, idx], train_xy.scales, float(alphas[idx]), float(rmse_train[idx]),
+                     float(rmse_test[idx]), coefs, rmse_train, rmse_test)
