@@ -1,0 +1,326 @@
+"""Benchmark: X^T X assembly throughput (rows/s) on one GB300.
+
+Workload (default): the binary-alloy precision-path configuration - 5,000
+seeded synthetic structures of 64..128 atoms (bcc/fcc supercells, a ~ U(2.8,
+4.2) A, displacements N(0, 0.15 A), random A/B occupancy), Morse labels,
+gtinv order 3, l_max (8, 4), 10 Gaussians + constant, cutoff 7 A,
+model_type 3, max_p 2 (F = 2,618 columns, ~1.3 M rows).
+
+One step = one pass of the hot path over the whole dataset: neighbour lists,
+a_nlm, invariant features and their force/stress derivatives (X rows, FP32
+features with FP64 neighbour sums), row weighting, X^T y, and X^T X on the
+tensor cores (BF16x3 split products, FP32 accumulation flushed into FP64).
+
+  value : rows/s with the structures, weights and targets resident in HBM.
+  e2e   : rows/s through the C ABI with host buffers (pg_gram_accumulate: host
+          cell translations + H2D copies, then pg_gram_result: D2H of X^T X).
+  cpu_baseline : the CPU oracle (the reference algorithm restated in C++,
+          OpenMP over structures) + numpy X^T X on a bounded sample.
+
+`--impl reference` times the reference's CPU algorithm instead (the oracle
+port; the reference's own build is not available on the GPU host) on the
+same workload, metric and unit, one bounded sample per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "X^T X rows/s (mixed BF16x3 Gram + FP32 features)"
+UNIT = "rows/s"
+
+CFG2 = dict(n_type=2, cutoff=7.0, model_type=3, max_p=2, gaussian_params2=(0.0, 5.0, 10), gtinv_order=3,
+            gtinv_maxl=(8, 4))
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_dataset(n_struct, seed, device):
+    from pypolymlp_gb300 import synthetic as syn
+    from pypolymlp_gb300.regression import Dataset
+
+    ss = syn.binary_set(n_struct, seed=seed)
+    t = time.time()
+    syn.morse_labels(ss, syn.morse_D(2), device=device)
+    log(f"labels for {n_struct} structures in {time.time() - t:.1f}s")
+    return Dataset.from_structure_set(ss, name="binary")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) < 9:
+                        continue
+                    try:
+                        sm.append(float(p[1]))
+                        mx.append(float(p[2]))
+                    except ValueError:
+                        continue
+                    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                    for name, v in zip(names, p[5:9]):
+                        if v.lower().startswith("active"):
+                            reasons.add(name)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_baseline(params, data, sample, n_threads):
+    """CPU oracle (reference algorithm) + numpy Gram on the first `sample` structures."""
+    from oracle.pipeline import calc_xtx_xty_cpu
+    from pypolymlp_gb300.regression import get_min_energy
+
+    sub = data.slice(0, sample)
+    t = time.time()
+    xy = calc_xtx_xty_cpu(params, [sub], min_energy=get_min_energy([data]), n_threads=n_threads)
+    dt = time.time() - t
+    return xy.total_n_data / dt, dt, xy.total_n_data
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from pypolymlp_gb300.params import make_params_dict
+
+    params = make_params_dict(**CFG2)
+    data = make_dataset(max(args.ref_sample, 8), seed=2, device=None)
+    n_threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_baseline(params, data, min(4, len(data)), n_threads)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, dt, rows = cpu_baseline(params, data, args.ref_sample, n_threads)
+        rates.append(r)
+        times.append(dt)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "binary alloy, gtinv order 3, l_max (8,4), 10+1 Gaussians, rc 7, model_type 3, "
+                               "max_p 2 (F=2618)", "sample_structures": args.ref_sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
+                         "sample": f"first {args.ref_sample} structures of the 5,000-structure workload per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-struct", type=int, default=5000)
+    ap.add_argument("--cpu-sample", type=int, default=48)
+    ap.add_argument("--ref-sample", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64", action="store_true", help="time the FP64 judge path instead")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank, world, local_rank = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(local_rank)
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.abi import Structures
+    from pypolymlp_gb300.params import make_params_dict
+    from pypolymlp_gb300.regression import DeviceBatch, GramAccumulator, get_min_energy, weights_and_targets
+
+    precision = _ffi.PG_FP64 if args.fp64 else _ffi.PG_MIXED
+    params = make_params_dict(**CFG2)
+    data = make_dataset(args.n_struct, seed=2 + rank, device="cuda")
+    min_e = get_min_energy([data])
+    model = _ffi.Model(params)
+    F = model.n_features
+    t = time.time()
+    batch = DeviceBatch(model, data, min_e, precision)
+    log(f"staged {len(data)} structures, {batch.n_rows} rows in {time.time() - t:.1f}s")
+    gram = GramAccumulator(model, precision)
+
+    def step():
+        gram.reset()
+        gram.accumulate_batch(batch)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        start.record()
+        for _ in range(args.steps):
+            step()
+        end.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = start.elapsed_time(end)
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    rows_per_step = batch.n_rows
+    value = rows_per_step * args.steps * world / (ms / 1e3)
+
+    # per-kernel profile of one more step (events on the launching stream)
+    _ffi.profile_enable(True)
+    _ffi.profile_read()
+    step()
+    prof = _ffi.profile_read()
+    _ffi.profile_enable(False)
+    launches_per_step = sum(v[1] for v in prof.values()) + 4  # + energy stats, row scaling, X^T y, symmetrize
+    # dominant kernel and its roofline
+    hbm_gbs, bf16_tf, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dn) = dom
+    per_launch_s = dms / dn / 1e3
+    if dname.startswith("pg_gram"):
+        flops = F * (F + 1) * rows_per_step / dn
+        achieved = flops / per_launch_s / 1e12
+        peak = bf16_tf / 3.0 if dname == "pg_gram_bf16x3" else None
+        roof = {"kernel": dname, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "note": f"peak = {peak_kind} bf16 dense / 3 (three split products)"}
+    else:
+        bytes_ = F * (4 if precision == _ffi.PG_MIXED else 8) * rows_per_step / dn
+        achieved = bytes_ / per_launch_s / 1e9
+        roof = {"kernel": dname, "bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
+                "frac": achieved / hbm_gbs, "traffic": None,
+                "note": f"algorithmic bytes = F x {4 if precision == _ffi.PG_MIXED else 8} B per X row written; "
+                        f"peak {peak_kind}"}
+    kernels = {k: {"ms_per_step": v[0], "launches": v[1]} for k, v in prof.items()}
+
+    # e2e through the C ABI with host buffers (one pass; host prep + H2D + D2H inside)
+    e_row, f_row, s_row, n_rows, w, y = weights_and_targets(data, min_e)
+    st = Structures(data.axis, data.positions, data.types)
+    gram2 = GramAccumulator(model, precision)
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 2))
+    t0 = time.time()
+    for _ in range(e2e_steps):
+        gram2.reset()
+        gram2.accumulate(st, e_row, f_row, s_row, n_rows, w, y)
+        res = gram2.result()
+    torch.cuda.synchronize()
+    e2e_s = (time.time() - t0) / e2e_steps
+    h2d = st.positions.nbytes + st.axis.nbytes + st.types.nbytes + st.n_atoms.nbytes + 2 * n_rows * 8
+    d2h = F * F * 8 + 3 * F * 8
+    e2e = {"value": n_rows * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+    del res
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n_threads = os.cpu_count() or 1
+        r, dt, rows = cpu_baseline(params, data, args.cpu_sample, n_threads)
+        cpu = {"value": r, "unit": UNIT, "cores": n_threads, "kind": "port",
+               "sample": f"first {args.cpu_sample} structures ({rows} rows), CPU oracle X rows + numpy X^T X, "
+                         f"{dt:.1f}s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.fp64 else "f32+bf16x3", "data": "synthetic",
+            "config": {"workload": "binary alloy, 5000 structures of 64-128 atoms, gtinv order 3, l_max (8,4), "
+                                   "10+1 Gaussians, rc 7 A, model_type 3, max_p 2",
+                       "n_features": F, "rows_per_step": int(rows_per_step), "n_structures": len(data),
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (X is rows x F x 4 B)"},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "roofline": roof,
+            "kernels": kernels,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

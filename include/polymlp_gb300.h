@@ -61,6 +61,7 @@ typedef struct pg_structures {
 typedef struct pg_model pg_model;
 typedef struct pg_gram pg_gram;
 typedef struct pg_eval pg_eval;
+typedef struct pg_batch pg_batch;
 
 enum { PG_FP64 = 0, PG_MIXED = 1 };
 
@@ -118,9 +119,24 @@ int pg_gram_destroy(pg_gram* g);
 int pg_gram_accumulate(pg_gram* g, const pg_structures* st, const int64_t* e_row,
                        const int64_t* f_row, const int64_t* s_row, int64_t n_rows,
                        const double* w, const double* y);
+/* Zero the sums of a pg_gram (same model and precision). */
+int pg_gram_reset(pg_gram* g);
 /* Results (host): xtx F x F (full symmetric), xty F, yty, xe_sum F, xe_sq_sum F, n_rows. */
 int pg_gram_result(pg_gram* g, double* xtx, double* xty, double* yty, double* xe_sum,
                    double* xe_sq_sum, int64_t* n_rows_total);
+
+/*
+ * A batch staged on the device: structures (with translations and wrapped
+ * positions from the host), row layout, weights and weighted targets.  The
+ * same arguments as pg_gram_accumulate; pg_gram_accumulate_batch then does
+ * only device work (neighbour lists, rows, X^T X, ...), so a batch can be
+ * assembled repeatedly with its inputs resident in HBM.
+ */
+int pg_batch_create(pg_model* m, const pg_structures* st, const int64_t* e_row, const int64_t* f_row,
+                    const int64_t* s_row, int64_t n_rows, const double* w, const double* y, int precision,
+                    pg_batch** out);
+int pg_batch_destroy(pg_batch* b);
+int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
 
 /*
  * Ridge solve over alphas in ascending order on the device, as solver_ridge
@@ -145,6 +161,15 @@ int pg_eval_create(const pg_feature_params* fp, const double* coeffs, int n_coef
 int pg_eval_destroy(pg_eval* e);
 int pg_eval_run(pg_eval* e, const pg_structures* st, double* energy, double* forces,
                 double* stress);
+
+/*
+ * Per-kernel timing with CUDA events on the launching stream.  pg_profile_read
+ * synchronises the device and returns, per kernel name, the summed launch
+ * durations (ms) and launch counts recorded since the previous read; names are
+ * NUL-separated in the names buffer.
+ */
+int pg_profile_enable(int on);
+int pg_profile_read(char* names, size_t names_len, double* ms, int* launches, int max_names, int* n_names);
 
 /*
  * Neighbour lists (test surface, as NeighborFull / NeighborHalf,

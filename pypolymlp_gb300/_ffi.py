@@ -56,6 +56,12 @@ def lib():
                 ("pg_gram_destroy", [_vp]),
                 ("pg_gram_accumulate", [_vp, _vp, _i64p, _i64p, _i64p, C.c_int64, _dp, _dp]),
                 ("pg_gram_result", [_vp, _dp, _dp, _dp, _dp, _dp, _i64p]),
+                ("pg_gram_reset", [_vp]),
+                ("pg_batch_create", [_vp, _vp, _i64p, _i64p, _i64p, C.c_int64, _dp, _dp, C.c_int, C.POINTER(_vp)]),
+                ("pg_batch_destroy", [_vp]),
+                ("pg_gram_accumulate_batch", [_vp, _vp]),
+                ("pg_profile_enable", [C.c_int]),
+                ("pg_profile_read", [C.c_char_p, C.c_size_t, _dp, _ip, C.c_int, _ip]),
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),
@@ -163,3 +169,24 @@ def neighbor_list(st: Structures, s: int, cutoff: float):
     check(L.pg_neighbor_list(C.cast(st.ref(), _vp), s, cutoff, 0, C.byref(n), _p(offs, C.c_int), _p(nb, C.c_int),
                              _p(d, C.c_double)))
     return offs, nb[:n.value], d[:n.value]
+
+
+def profile_enable(on: bool = True):
+    check(lib().pg_profile_enable(1 if on else 0))
+
+
+def profile_read():
+    """{kernel name: (total ms, launches)} since the previous read."""
+    names = C.create_string_buffer(8192)
+    ms = np.zeros(64)
+    launches = np.zeros(64, dtype=np.int32)
+    n = C.c_int()
+    check(lib().pg_profile_read(names, 8192, _p(ms, C.c_double), _p(launches, C.c_int), 64, C.byref(n)))
+    out = {}
+    raw = names.raw
+    pos = 0
+    for k in range(n.value):
+        end = raw.index(b"\0", pos)
+        out[raw[pos:end].decode()] = (float(ms[k]), int(launches[k]))
+        pos = end + 1
+    return out

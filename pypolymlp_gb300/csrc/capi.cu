@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <map>
+#include <mutex>
 #include <numeric>
 
 #include "host/cell.h"
@@ -15,6 +17,31 @@ namespace pg {
 
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+// ------------------------------------------------------------ profiler
+namespace {
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = std::getenv("PG_PROFILE") != nullptr;
+std::vector<ProfRec> g_prof;
+}  // namespace
+
+ProfScope::ProfScope(const char* name, cudaStream_t st) : name_(name), st_(st) {
+    if (!g_prof_on) return;
+    cudaEventCreate(&a_);
+    cudaEventCreate(&b_);
+    cudaEventRecord(a_, st_);
+}
+
+ProfScope::~ProfScope() {
+    if (!a_) return;
+    cudaEventRecord(b_, st_);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.push_back(ProfRec{name_, a_, b_});
+}
 
 // ------------------------------------------------------------ DeviceModel
 void DeviceModel::build(const FlatModel& fm, int chunk_width) {
@@ -91,7 +118,7 @@ void DeviceModel::build(const FlatModel& fm, int chunk_width) {
 }
 
 // ------------------------------------------------------------ DeviceBatch
-void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
+void DeviceBatch::upload_structures(const pg_structures* st, int s_begin, int s_end, double cutoff) {
     n_st = s_end - s_begin;
     long long off0 = 0;
     for (int s = 0; s < s_begin; ++s) off0 += st->n_atoms[s];
@@ -105,6 +132,10 @@ void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double 
     for (int s = s_begin; s < s_end; ++s) {
         const int n = st->n_atoms[s];
         if (n < 0) throw std::runtime_error("negative atom count");
+        for (int i = 0; i < n; ++i) {
+            const int t = st->types[a + i];
+            if (t < 0) throw std::runtime_error("negative atom type");
+        }
         const CellTranslations ct = cell_translations(st->axis + 9 * (size_t)s, st->positions + 3 * a, n, cutoff);
         for (const auto& t : ct.trans) trans.insert(trans.end(), t.begin(), t.end());
         for (int i = 0; i < n; ++i) {
@@ -123,21 +154,44 @@ void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double 
     upload(d_pos, pos);
     upload(d_types, types);
     upload(d_atom_st, atom_st);
-    DevBatch B = view(cutoff);
     d_counts.reserve(sizeof(int) * std::max(1, n_atoms));
-    if (n_atoms > 0) launch_nb_count(B, d_counts.as<int>(), stream);
-    std::vector<int> counts(n_atoms);
-    if (n_atoms > 0)
-        PG_CUDA(cudaMemcpyAsync(counts.data(), d_counts.as<int>(), sizeof(int) * n_atoms, cudaMemcpyDeviceToHost,
-                                stream));
+    d_nb_off.reserve(sizeof(long long) * (n_atoms + 1));
+    d_total.reserve(sizeof(long long));
+}
+
+// Count candidates, scan on the device, then fill in the reference's order.
+void DeviceBatch::build_neighbors(double cutoff, cudaStream_t stream) {
+    const DevBatch B = view(cutoff);
+    if (n_atoms == 0) {
+        n_pairs = 0;
+        nb_off.assign(1, 0);
+        PG_CUDA(cudaMemsetAsync(d_nb_off.as<void>(), 0, sizeof(long long), stream));
+        return;
+    }
+    {
+        ProfScope ps("pg_nb_count", stream);
+        launch_nb_count(B, d_counts.as<int>(), stream);
+    }
+    launch_exclusive_scan(d_counts.as<int>(), n_atoms, d_nb_off.as<long long>(), d_total.as<long long>(), stream);
+    long long total = 0;
+    PG_CUDA(cudaMemcpyAsync(&total, d_total.as<long long>(), sizeof(long long), cudaMemcpyDeviceToHost, stream));
     PG_CUDA(cudaStreamSynchronize(stream));
-    nb_off.assign(n_atoms + 1, 0);
-    for (int i = 0; i < n_atoms; ++i) nb_off[i + 1] = nb_off[i] + counts[i];
-    n_pairs = nb_off[n_atoms];
-    upload(d_nb_off, nb_off);
+    n_pairs = total;
     d_nb_j.reserve(sizeof(int) * std::max<long long>(1, n_pairs));
     d_nb_d.reserve(sizeof(double) * 3 * std::max<long long>(1, n_pairs));
-    if (n_atoms > 0) launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), stream);
+    ProfScope ps("pg_nb_fill", stream);
+    launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), stream);
+}
+
+void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
+    upload_structures(st, s_begin, s_end, cutoff);
+    build_neighbors(cutoff, stream);
+}
+
+void DeviceBatch::host_offsets() {
+    nb_off.assign(n_atoms + 1, 0);
+    PG_CUDA(cudaMemcpy(nb_off.data(), d_nb_off.as<long long>(), sizeof(long long) * (n_atoms + 1),
+                       cudaMemcpyDeviceToHost));
 }
 
 DevBatch DeviceBatch::view(double cutoff) const {
@@ -198,32 +252,13 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
     return mx + (size_t)(mean_pairs * 28.0) + (size_t)flat.n_features * 3 * (fp64 ? 8 : 4);
 }
 
-// Rows of one staged batch into Xd (device, column-major, leading dim ld), in
-// the batch-local row layout given by e_row/f_row/s_row (device arrays).
-template <typename T>
-void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row,
-                       const long long* d_s_row, const std::vector<long long>& f_row_host, T* Xd, long long ld,
-                       cudaStream_t stream) {
-    const bool fp64 = sizeof(T) == 8;
-    const DeviceModel& dmod = fp64 ? dev64 : dev32;
-    const DevBatch B = b.view(flat.cutoff);
+// Per-batch plan: per-atom storage offsets and pg_rows work items.
+void Model::plan_rows(const DeviceBatch& b, RowPlan& plan) const {
     std::vector<long long> a_off, d_off, g_off;
-    long long a_tot, d_tot, g_tot;
-    atom_offsets(b, sizeof(T), a_off, d_off, g_off, a_tot, d_tot, g_tot);
-    upload(d_a_off, a_off);
-    upload(d_d_off, d_off);
-    upload(d_g_off, g_off);
-    s_A.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
-    s_D.reserve(sizeof(T) * std::max<long long>(1, d_tot));
-    s_G.reserve(2 * sizeof(T) * std::max<long long>(1, g_tot));
-    if (b.n_atoms > 0) {
-        launch_anlm<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                       d_a_off.as<long long>(), s_A.as<double2>(), max_k0, stream);
-        launch_features_adjoint<T>(dmod.dm, B, d_a_off.as<long long>(), s_A.as<double2>(),
-                                   d_d_off.as<long long>(), s_D.as<T>(), d_g_off.as<long long>(), s_G.as<void>(),
-                                   max_k, stream);
-    }
-    // work items: blocks of kRowsTR target atoms per structure
+    atom_offsets(b, 0, a_off, d_off, g_off, plan.a_tot, plan.d_tot, plan.g_tot);
+    upload(plan.d_a_off, a_off);
+    upload(plan.d_d_off, d_off);
+    upload(plan.d_g_off, g_off);
     std::vector<RowItem> items;
     std::vector<int> item_off(1, 0);
     for (int s = 0; s < b.n_st; ++s) {
@@ -233,24 +268,70 @@ void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long
         for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * kRowsTR});
         item_off.push_back((int)items.size());
     }
-    upload(d_items, items);
-    upload(d_item_off, item_off);
-    s_partial.reserve(sizeof(double) * 7 * (size_t)flat.n_features * std::max<size_t>(1, items.size()));
-    if (!items.empty()) {
-        launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                       d_d_off.as<long long>(), s_D.as<T>(), d_g_off.as<long long>(), s_G.as<void>(),
-                       d_items.as<RowItem>(), (int)items.size(), d_f_row, dmod.chunk, dmod.n_chunks,
-                       dmod.chunk_cap_ent, Xd, ld, s_partial.as<double>(), stream);
-        launch_rows_reduce<T>(flat.n_features, b.n_st, d_item_off.as<int>(), s_partial.as<double>(), d_e_row,
+    plan.n_items = (int)items.size();
+    upload(plan.d_items, items);
+    upload(plan.d_item_off, item_off);
+}
+
+// Rows of one uploaded batch into Xd (device, column-major, leading dim ld), in
+// the batch-local row layout given by e_row/f_row/s_row (device arrays):
+// neighbour lists, a_nlm, features + adjoint, force/stress rows, energy/stress sums.
+template <typename T>
+void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_row, const long long* d_f_row,
+                     const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream) {
+    const bool fp64 = sizeof(T) == 8;
+    const DeviceModel& dmod = fp64 ? dev64 : dev32;
+    b.build_neighbors(flat.cutoff, stream);
+    const DevBatch B = b.view(flat.cutoff);
+    s_A.reserve(sizeof(double2) * std::max<long long>(1, plan.a_tot));
+    s_D.reserve(sizeof(T) * std::max<long long>(1, plan.d_tot));
+    s_G.reserve(2 * sizeof(T) * std::max<long long>(1, plan.g_tot));
+    if (b.n_atoms > 0) {
+        {
+            ProfScope ps("pg_anlm", stream);
+            launch_anlm<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                           plan.d_a_off.as<long long>(), s_A.as<double2>(), max_k0, stream);
+        }
+        {
+            ProfScope ps("pg_features_adjoint", stream);
+            launch_features_adjoint<T>(dmod.dm, B, plan.d_a_off.as<long long>(), s_A.as<double2>(),
+                                       plan.d_d_off.as<long long>(), s_D.as<T>(), plan.d_g_off.as<long long>(),
+                                       s_G.as<void>(), max_k, stream);
+        }
+    }
+    s_partial.reserve(sizeof(double) * 7 * (size_t)flat.n_features * std::max(1, plan.n_items));
+    if (plan.n_items > 0) {
+        {
+            ProfScope ps("pg_rows", stream);
+            launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                           plan.d_d_off.as<long long>(), s_D.as<T>(), plan.d_g_off.as<long long>(), s_G.as<void>(),
+                           plan.d_items.as<RowItem>(), plan.n_items, d_f_row, dmod.chunk, dmod.n_chunks,
+                           dmod.chunk_cap_ent, Xd, ld, s_partial.as<double>(), stream);
+        }
+        ProfScope ps("pg_rows_reduce", stream);
+        launch_rows_reduce<T>(flat.n_features, b.n_st, plan.d_item_off.as<int>(), s_partial.as<double>(), d_e_row,
                               d_s_row, Xd, ld, stream);
     }
     PG_CUDA(cudaGetLastError());
 }
 
-template void Model::batch_rows<double>(DeviceBatch&, const long long*, const long long*, const long long*,
-                                        const std::vector<long long>&, double*, long long, cudaStream_t);
-template void Model::batch_rows<float>(DeviceBatch&, const long long*, const long long*, const long long*,
-                                       const std::vector<long long>&, float*, long long, cudaStream_t);
+template <typename T>
+void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row,
+                       const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream) {
+    RowPlan plan;
+    plan_rows(b, plan);
+    run_rows<T>(b, plan, d_e_row, d_f_row, d_s_row, Xd, ld, stream);
+    PG_CUDA(cudaStreamSynchronize(stream));
+}
+
+template void Model::run_rows<double>(DeviceBatch&, const RowPlan&, const long long*, const long long*,
+                                      const long long*, double*, long long, cudaStream_t);
+template void Model::run_rows<float>(DeviceBatch&, const RowPlan&, const long long*, const long long*,
+                                     const long long*, float*, long long, cudaStream_t);
+template void Model::batch_rows<double>(DeviceBatch&, const long long*, const long long*, const long long*, double*,
+                                        long long, cudaStream_t);
+template void Model::batch_rows<float>(DeviceBatch&, const long long*, const long long*, const long long*, float*,
+                                       long long, cudaStream_t);
 
 // Split [0, n_st) into batches whose staged data fits the device budget.
 std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bool fp64, size_t budget) const {
@@ -275,7 +356,7 @@ size_t device_budget_bytes() {
     if (const char* e = std::getenv("PG_BATCH_BYTES")) return (size_t)std::atoll(e);
     size_t free_b = 0, total_b = 0;
     PG_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    return std::min<size_t>(free_b / 3, (size_t)16 << 30);
+    return (size_t)(0.55 * (double)free_b);
 }
 
 __global__ void pg_f32_to_f64(const float* src, double* dst, size_t n) {
@@ -396,7 +477,7 @@ int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, c
         DevBuf Xd, X64, d_e, d_f, d_s;
         for (const auto& bt : batches) {
             const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
-            b.stage(st, s0, s1, m.flat.cutoff, stream);
+            b.upload_structures(st, s0, s1, m.flat.cutoff);
             // batch-local row layout: energies, stresses, forces
             std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);
             long long r = nb;
@@ -418,11 +499,11 @@ int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, c
             Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
             double* X64p;
             if (fp64) {
-                m.batch_rows<double>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf,
+                m.batch_rows<double>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(),
                                      Xd.as<double>(), rows, stream);
                 X64p = Xd.as<double>();
             } else {
-                m.batch_rows<float>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf,
+                m.batch_rows<float>(b, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(),
                                     Xd.as<float>(), rows, stream);
                 X64.reserve((size_t)rows * F * 8);
                 pg_f32_to_f64<<<1024, 256, 0, stream>>>(Xd.as<float>(), X64.as<double>(), (size_t)rows * F);
@@ -477,6 +558,43 @@ int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, c
     });
 }
 
+int pg_profile_enable(int on) {
+    return guarded([&] { g_prof_on = on != 0; });
+}
+
+// Sum of launch durations per kernel name since the last read: writes up to
+// max_names entries ("name" NUL-separated in names, total ms and launches).
+int pg_profile_read(char* names, size_t names_len, double* ms, int* launches, int max_names, int* n_names) {
+    return guarded([&] {
+        PG_CUDA(cudaDeviceSynchronize());
+        std::map<std::string, std::pair<double, int>> agg;
+        {
+            std::lock_guard<std::mutex> lk(g_prof_mu);
+            for (auto& r : g_prof) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, r.a, r.b);
+                auto& e = agg[r.name];
+                e.first += t;
+                e.second += 1;
+                cudaEventDestroy(r.a);
+                cudaEventDestroy(r.b);
+            }
+            g_prof.clear();
+        }
+        int k = 0;
+        size_t pos = 0;
+        for (auto& kv : agg) {
+            if (k >= max_names || pos + kv.first.size() + 1 > names_len) break;
+            std::memcpy(names + pos, kv.first.c_str(), kv.first.size() + 1);
+            pos += kv.first.size() + 1;
+            ms[k] = kv.second.first;
+            launches[k] = kv.second.second;
+            ++k;
+        }
+        *n_names = k;
+    });
+}
+
 int pg_neighbor_list(const pg_structures* st, int structure, double cutoff, int half, int64_t* n_entries,
                      int* offsets, int* neighbors, double* diffs) {
     return guarded([&] {
@@ -484,6 +602,7 @@ int pg_neighbor_list(const pg_structures* st, int structure, double cutoff, int 
         if (structure < 0 || structure >= st->n_st) throw std::runtime_error("structure index out of range");
         DeviceBatch b;
         b.stage(st, structure, structure + 1, cutoff, 0);
+        b.host_offsets();
         *n_entries = b.n_pairs;
         if (!offsets) return;
         for (int i = 0; i <= b.n_atoms; ++i) offsets[i] = (int)b.nb_off[i];

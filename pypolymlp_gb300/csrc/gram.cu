@@ -243,16 +243,82 @@ void launch_gram_bf16x3(const float* X, long long ld, long long n_rows, int F, c
     pg_gram_bf16x3<<<n_tiles, 256, smem, st>>>(X, ld, n_rows, F, tiles, G);
 }
 
+// ------------------------------------------------------------ batches
+// A batch of structures staged on the device with its row layout, weights and
+// weighted targets: everything the regression assembly reads from HBM.
+struct Prepared {
+    DeviceBatch b;
+    RowPlan plan;
+    long long rows = 0;
+    int n_e = 0;
+    double yty = 0.0;
+    DevBuf d_e, d_f, d_s, d_w, d_y;
+};
+
+// Split a caller's batch into device-sized sub-batches with batch-local rows.
+std::vector<std::unique_ptr<Prepared>> prepare_batches(Model& m, const pg_structures* st, const int64_t* e_row,
+                                                       const int64_t* f_row, const int64_t* s_row, int64_t n_rows,
+                                                       const double* w, const double* y, bool fp64) {
+    for (int s = 0; s < st->n_st; ++s) {
+        if (e_row[s] < 0 || e_row[s] >= n_rows) throw std::runtime_error("energy row out of range");
+        if (f_row[s] >= 0 && (f_row[s] + 3LL * st->n_atoms[s] > n_rows || s_row[s] < 0 || s_row[s] + 6 > n_rows))
+            throw std::runtime_error("force/stress rows out of range");
+    }
+    std::vector<std::unique_ptr<Prepared>> out;
+    for (const auto& bt : m.plan_batches(st, fp64, device_budget_bytes())) {
+        const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
+        auto P = std::make_unique<Prepared>();
+        std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);
+        std::vector<double> wl(nb), yl(nb);
+        long long r = nb;
+        for (int q = 0; q < nb; ++q) {
+            le[q] = q;
+            wl[q] = w[e_row[s0 + q]];
+            yl[q] = y[e_row[s0 + q]];
+        }
+        for (int q = 0; q < nb; ++q)
+            if (f_row[s0 + q] >= 0) {
+                ls[q] = r;
+                for (int c = 0; c < 6; ++c) {
+                    wl.push_back(w[s_row[s0 + q] + c]);
+                    yl.push_back(y[s_row[s0 + q] + c]);
+                }
+                r += 6;
+            }
+        for (int q = 0; q < nb; ++q)
+            if (f_row[s0 + q] >= 0) {
+                lf[q] = r;
+                const long long nr = 3LL * st->n_atoms[s0 + q];
+                for (long long c = 0; c < nr; ++c) {
+                    wl.push_back(w[f_row[s0 + q] + c]);
+                    yl.push_back(y[f_row[s0 + q] + c]);
+                }
+                r += nr;
+            }
+        P->rows = r;
+        P->n_e = nb;
+        for (double v : yl) P->yty += v * v;
+        P->b.upload_structures(st, s0, s1, m.flat.cutoff);
+        m.plan_rows(P->b, P->plan);
+        upload(P->d_e, le);
+        upload(P->d_f, lf);
+        upload(P->d_s, ls);
+        upload(P->d_w, wl);
+        upload(P->d_y, yl);
+        out.push_back(std::move(P));
+    }
+    return out;
+}
+
 // ------------------------------------------------------------ pg_gram object
 struct Gram {
     Model* m;
     int precision;
     int F;
-    DevBuf G, xty, xe_sum, xe_sq, tiles64, tiles128, Xd, d_w, d_y, d_e, d_f, d_s, d_erows;
+    DevBuf G, xty, xe_sum, xe_sq, tiles64, tiles128, Xd;
     int n_tiles64 = 0, n_tiles128 = 0;
     double yty = 0;
     long long n_rows_total = 0;
-    DeviceBatch batch;
     cudaStream_t stream = 0;
 
     Gram(Model* mm, int prec) : m(mm), precision(prec), F(mm->flat.n_features) {
@@ -260,10 +326,7 @@ struct Gram {
         xty.alloc(F * sizeof(double));
         xe_sum.alloc(F * sizeof(double));
         xe_sq.alloc(F * sizeof(double));
-        PG_CUDA(cudaMemset(G.as<void>(), 0, G.bytes()));
-        PG_CUDA(cudaMemset(xty.as<void>(), 0, xty.bytes()));
-        PG_CUDA(cudaMemset(xe_sum.as<void>(), 0, xe_sum.bytes()));
-        PG_CUDA(cudaMemset(xe_sq.as<void>(), 0, xe_sq.bytes()));
+        reset();
         auto tile_list = [&](int tsz, DevBuf& buf, int& n) {
             const int nt = (F + tsz - 1) / tsz;
             std::vector<int2> t;
@@ -276,43 +339,44 @@ struct Gram {
         tile_list(kT, tiles128, n_tiles128);
     }
 
-    // One sub-batch of structures with its rows in batch-local layout.
-    void accumulate_batch(const pg_structures* st, int s0, int s1, const std::vector<long long>& le,
-                          const std::vector<long long>& lf, const std::vector<long long>& ls, long long rows,
-                          const std::vector<double>& w, const std::vector<double>& y) {
+    void reset() {
+        PG_CUDA(cudaMemsetAsync(G.as<void>(), 0, G.bytes(), stream));
+        PG_CUDA(cudaMemsetAsync(xty.as<void>(), 0, xty.bytes(), stream));
+        PG_CUDA(cudaMemsetAsync(xe_sum.as<void>(), 0, xe_sum.bytes(), stream));
+        PG_CUDA(cudaMemsetAsync(xe_sq.as<void>(), 0, xe_sq.bytes(), stream));
+        yty = 0;
+        n_rows_total = 0;
+    }
+
+    // Device work for one prepared batch: neighbours, rows, statistics, weights, X^T y, X^T X.
+    void accumulate(Prepared& P) {
         const bool fp64 = precision == PG_FP64;
-        batch.stage(st, s0, s1, m->flat.cutoff, stream);
-        upload(d_e, le);
-        upload(d_f, lf);
-        upload(d_s, ls);
+        const long long rows = P.rows;
         Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
-        upload(d_w, w);
-        upload(d_y, y);
-        std::vector<long long> erows(le.begin(), le.end());
-        upload(d_erows, erows);
-        const int ne = (int)erows.size();
         dim3 sg((unsigned)((rows + 255) / 256), (unsigned)std::min(F, 64));
         if (fp64) {
             double* X = Xd.as<double>();
-            m->batch_rows<double>(batch, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf, X, rows,
-                                  stream);
-            pg_energy_stats<double><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, d_erows.as<long long>(), ne,
+            m->run_rows<double>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
+                                rows, stream);
+            pg_energy_stats<double><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, P.d_e.as<long long>(), P.n_e,
                                                                         xe_sum.as<double>(), xe_sq.as<double>());
-            pg_scale_rows<double><<<sg, 256, 0, stream>>>(X, rows, rows, F, d_w.as<double>());
-            pg_xty<double><<<F, 256, 0, stream>>>(X, rows, rows, d_y.as<double>(), xty.as<double>());
+            pg_scale_rows<double><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
+            pg_xty<double><<<F, 256, 0, stream>>>(X, rows, rows, P.d_y.as<double>(), xty.as<double>());
+            ProfScope ps("pg_syrk_f64", stream);
             launch_syrk_f64(X, rows, rows, F, tiles64.as<int2>(), n_tiles64, G.as<double>(), stream);
         } else {
             float* X = Xd.as<float>();
-            m->batch_rows<float>(batch, d_e.as<long long>(), d_f.as<long long>(), d_s.as<long long>(), lf, X, rows,
-                                 stream);
-            pg_energy_stats<float><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, d_erows.as<long long>(), ne,
+            m->run_rows<float>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
+                               rows, stream);
+            pg_energy_stats<float><<<(F + 127) / 128, 128, 0, stream>>>(X, rows, F, P.d_e.as<long long>(), P.n_e,
                                                                        xe_sum.as<double>(), xe_sq.as<double>());
-            pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, d_w.as<double>());
-            pg_xty<float><<<F, 256, 0, stream>>>(X, rows, rows, d_y.as<double>(), xty.as<double>());
+            pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
+            pg_xty<float><<<F, 256, 0, stream>>>(X, rows, rows, P.d_y.as<double>(), xty.as<double>());
+            ProfScope ps("pg_gram_bf16x3", stream);
             launch_gram_bf16x3(X, rows, rows, F, tiles128.as<int2>(), n_tiles128, G.as<double>(), stream);
         }
         PG_CUDA(cudaGetLastError());
-        for (double v : y) yty += v * v;
+        yty += P.yty;
         n_rows_total += rows;
     }
 };
@@ -323,6 +387,10 @@ using namespace pg;
 
 struct pg_gram {
     std::unique_ptr<Gram> g;
+};
+struct pg_batch {
+    std::vector<std::unique_ptr<Prepared>> parts;
+    int precision;
 };
 
 extern "C" {
@@ -346,51 +414,50 @@ int pg_gram_destroy(pg_gram* g) {
     return guarded([&] { delete g; });
 }
 
+int pg_gram_reset(pg_gram* g) {
+    return guarded([&] {
+        if (!g) throw std::runtime_error("null gram");
+        g->g->reset();
+    });
+}
+
 int pg_gram_accumulate(pg_gram* gh, const pg_structures* st, const int64_t* e_row, const int64_t* f_row,
                        const int64_t* s_row, int64_t n_rows, const double* w, const double* y) {
     return guarded([&] {
         if (!gh || !st || !e_row || !f_row || !s_row || !w || !y) throw std::runtime_error("null argument");
         Gram& g = *gh->g;
-        Model& m = *g.m;
-        for (int s = 0; s < st->n_st; ++s) {
-            if (e_row[s] < 0 || e_row[s] >= n_rows) throw std::runtime_error("energy row out of range");
-            if (f_row[s] >= 0 && (f_row[s] + 3LL * st->n_atoms[s] > n_rows || s_row[s] < 0 || s_row[s] + 6 > n_rows))
-                throw std::runtime_error("force/stress rows out of range");
+        auto parts = prepare_batches(*g.m, st, e_row, f_row, s_row, n_rows, w, y, g.precision == PG_FP64);
+        for (auto& P : parts) g.accumulate(*P);
+        PG_CUDA(cudaStreamSynchronize(g.stream));
+    });
+}
+
+int pg_batch_create(pg_model* mh, const pg_structures* st, const int64_t* e_row, const int64_t* f_row,
+                    const int64_t* s_row, int64_t n_rows, const double* w, const double* y, int precision,
+                    pg_batch** out) {
+    return guarded([&] {
+        if (!mh || !st || !e_row || !f_row || !s_row || !w || !y || !out) throw std::runtime_error("null argument");
+        auto h = new pg_batch;
+        try {
+            h->parts = prepare_batches(*mh->m, st, e_row, f_row, s_row, n_rows, w, y, precision == PG_FP64);
+            h->precision = precision;
+        } catch (...) {
+            delete h;
+            throw;
         }
-        const auto batches = m.plan_batches(st, g.precision == PG_FP64, device_budget_bytes());
-        for (const auto& bt : batches) {
-            const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
-            std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);
-            std::vector<double> wl, yl;
-            long long r = nb;
-            wl.resize(nb);
-            yl.resize(nb);
-            for (int q = 0; q < nb; ++q) {
-                le[q] = q;
-                wl[q] = w[e_row[s0 + q]];
-                yl[q] = y[e_row[s0 + q]];
-            }
-            for (int q = 0; q < nb; ++q)
-                if (f_row[s0 + q] >= 0) {
-                    ls[q] = r;
-                    for (int c = 0; c < 6; ++c) {
-                        wl.push_back(w[s_row[s0 + q] + c]);
-                        yl.push_back(y[s_row[s0 + q] + c]);
-                    }
-                    r += 6;
-                }
-            for (int q = 0; q < nb; ++q)
-                if (f_row[s0 + q] >= 0) {
-                    lf[q] = r;
-                    const long long nr = 3LL * st->n_atoms[s0 + q];
-                    for (long long c = 0; c < nr; ++c) {
-                        wl.push_back(w[f_row[s0 + q] + c]);
-                        yl.push_back(y[f_row[s0 + q] + c]);
-                    }
-                    r += nr;
-                }
-            g.accumulate_batch(st, s0, s1, le, lf, ls, r, wl, yl);
-        }
+        PG_CUDA(cudaDeviceSynchronize());
+        *out = h;
+    });
+}
+
+int pg_batch_destroy(pg_batch* b) {
+    return guarded([&] { delete b; });
+}
+
+int pg_gram_accumulate_batch(pg_gram* gh, pg_batch* b) {
+    return guarded([&] {
+        if (!gh || !b) throw std::runtime_error("null argument");
+        for (auto& P : b->parts) gh->g->accumulate(*P);
     });
 }
 

@@ -38,6 +38,7 @@ template <typename T>
 void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
+void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
 size_t rows_smem_bytes(const DevModel& M, int chunk, int cap_ent, bool fp64);
 template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,

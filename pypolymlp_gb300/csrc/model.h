@@ -10,13 +10,20 @@
 
 namespace pg {
 
+// Per-batch offsets of per-atom data and the pg_rows work items.
+struct RowPlan {
+    long long a_tot = 0, d_tot = 0, g_tot = 0;
+    int n_items = 0;
+    DevBuf d_a_off, d_d_off, d_g_off, d_items, d_item_off;
+};
+
 struct Model {
     ModelTables tables;
     FlatModel flat;
     DeviceModel dev64, dev32;   // pg_rows column chunk of 128 (FP64) and 256 (FP32)
     int max_k = 1, max_k0 = 1;
     // per-batch scratch (grow-only)
-    DevBuf d_a_off, d_d_off, d_g_off, s_A, s_D, s_G, d_items, d_item_off, s_partial;
+    DevBuf s_A, s_D, s_G, s_partial;
 
     explicit Model(const pg_feature_params* p);
 
@@ -26,9 +33,13 @@ struct Model {
     size_t bytes_per_atom(bool fp64, double mean_pairs) const;
     std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
 
+    void plan_rows(const DeviceBatch& b, RowPlan& plan) const;
+    template <typename T>
+    void run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_row, const long long* d_f_row,
+                  const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream);
     template <typename T>
     void batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row, const long long* d_s_row,
-                    const std::vector<long long>& f_row_host, T* Xd, long long ld, cudaStream_t stream);
+                    T* Xd, long long ld, cudaStream_t stream);
 };
 
 size_t device_budget_bytes();

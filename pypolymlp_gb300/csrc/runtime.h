@@ -109,11 +109,28 @@ struct DeviceBatch {
     std::vector<int> st_atom_off, st_trans_off, types, atom_st;
     std::vector<double> trans, pos;
     DevBuf d_st_atom_off, d_st_trans_off, d_trans, d_pos, d_types, d_atom_st;
-    DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d;
-    std::vector<long long> nb_off;
-    // Build translations on the host and the full neighbour list on the device.
+    DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d, d_total;
+    std::vector<long long> nb_off;  // host copy, only after host_offsets()
+    // Host: translations and wrapped positions (NeighborCell), uploaded to the device.
+    void upload_structures(const pg_structures* st, int s_begin, int s_end, double cutoff);
+    // Device: full neighbour lists (count, scan, fill).
+    void build_neighbors(double cutoff, cudaStream_t stream);
     void stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream);
+    void host_offsets();
     struct DevBatch view(double cutoff) const;
+};
+
+// Per-kernel timing with CUDA events on the launching stream (enabled by
+// pg_profile_enable or PG_PROFILE=1); read back with pg_profile_read.
+class ProfScope {
+  public:
+    ProfScope(const char* name, cudaStream_t st);
+    ~ProfScope();
+
+  private:
+    const char* name_;
+    cudaStream_t st_;
+    cudaEvent_t a_ = nullptr, b_ = nullptr;
 };
 
 }  // namespace pg

@@ -439,7 +439,37 @@ __global__ void pg_rows_reduce(int F, const int* item_off /* n_st+1 */, const do
     }
 }
 
+// ------------------------------------------------------------ prefix sums
+// offsets[0] = 0, offsets[i + 1] = offsets[i] + counts[i]; one block of 1024.
+__global__ void pg_exclusive_scan(const int* counts, int n, long long* offsets, long long* total) {
+    __shared__ long long part[1024];
+    const int t = threadIdx.x;
+    const long long chunk = (n + blockDim.x - 1) / blockDim.x;
+    const long long b = t * chunk, e = min((long long)n, b + chunk);
+    long long s = 0;
+    for (long long i = b; i < e; ++i) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        const long long v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long run = part[t] - s;  // exclusive prefix of this chunk
+    if (t == 0) offsets[0] = 0;
+    for (long long i = b; i < e; ++i) {
+        run += counts[i];
+        offsets[i + 1] = run;
+    }
+    if (t == blockDim.x - 1) *total = part[t];
+}
+
 // ------------------------------------------------------------- launchers
+void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st) {
+    pg_exclusive_scan<<<1, 1024, 0, st>>>(counts, n, offsets, total);
+}
+
 void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st) {
     const int threads = 256, warps = threads / 32;
     pg_nb_count<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, counts);

@@ -161,6 +161,12 @@ class GramAccumulator:
                                                  p(f_row, C.c_int64), p(s_row, C.c_int64), C.c_int64(n_rows),
                                                  p(w, C.c_double), p(y, C.c_double)))
 
+    def reset(self):
+        _ffi.check(_ffi.lib().pg_gram_reset(self._h))
+
+    def accumulate_batch(self, batch: "DeviceBatch"):
+        _ffi.check(_ffi.lib().pg_gram_accumulate_batch(self._h, batch.handle))
+
     def result(self):
         F = self.F
         xtx = np.zeros((F, F), order="F")
@@ -173,6 +179,38 @@ class GramAccumulator:
         _ffi.check(_ffi.lib().pg_gram_result(self._h, p(xtx, C.c_double), p(xty, C.c_double), C.byref(yty),
                                              p(xe_sum, C.c_double), p(xe_sq, C.c_double), C.byref(n)))
         return xtx, xty, yty.value, xe_sum, xe_sq, n.value
+
+
+class DeviceBatch:
+    """A dataset staged in HBM (pg_batch): structures, row layout, weights and
+    weighted targets, ready for repeated pg_gram_accumulate_batch calls."""
+
+    def __init__(self, model: _ffi.Model, d: Dataset, min_energy: float, precision: int,
+                 weight_stress: float = 0.1):
+        e_row, f_row, s_row, n_rows, w, y = weights_and_targets(d, min_energy, weight_stress)
+        st = Structures(d.axis, d.positions, d.types)
+        self.n_rows = int(n_rows)
+        p = _ffi._p
+        e_row = np.ascontiguousarray(e_row, dtype=np.int64)
+        f_row = np.ascontiguousarray(f_row, dtype=np.int64)
+        s_row = np.ascontiguousarray(s_row, dtype=np.int64)
+        w = np.ascontiguousarray(w)
+        y = np.ascontiguousarray(y)
+        h = _ffi._vp()
+        _ffi.check(_ffi.lib().pg_batch_create(model.handle, C.cast(st.ref(), _ffi._vp), p(e_row, C.c_int64),
+                                              p(f_row, C.c_int64), p(s_row, C.c_int64), C.c_int64(n_rows),
+                                              p(w, C.c_double), p(y, C.c_double), int(precision), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _ffi._lib is not None:
+            _ffi._lib.pg_batch_destroy(h)
+            self._h = None
 
 
 @dataclass
