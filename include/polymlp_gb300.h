@@ -137,6 +137,17 @@ int pg_batch_create(pg_model* m, const pg_structures* st, const int64_t* e_row, 
                     pg_batch** out);
 int pg_batch_destroy(pg_batch* b);
 int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
+/*
+ * Weighted residuals R = y - X C of a staged batch for n_coef (<= 16)
+ * coefficient vectors C (F x n_coef, column-major, in X's own column scaling),
+ * with the rows regenerated at the pg_gram's precision and accumulated in
+ * FP64.  Writes X^T R (F x n_coef) and the sums of R^2 over energy, force and
+ * stress rows (3 x n_coef, kind-major).  Used for FP64 iterative refinement
+ * of a mixed-precision fit and for RMSEs from residuals rather than from
+ * c^T A c - 2 c^T b + y^T y.
+ */
+int pg_batch_residual(pg_gram* g, pg_batch* b, const double* coefs, int n_coef, double* xtr, double* sq,
+                      int64_t* n_rows);
 
 /*
  * Ridge solve over alphas in ascending order on the device, as solver_ridge

@@ -60,6 +60,7 @@ def lib():
                 ("pg_batch_create", [_vp, _vp, _i64p, _i64p, _i64p, C.c_int64, _dp, _dp, C.c_int, C.POINTER(_vp)]),
                 ("pg_batch_destroy", [_vp]),
                 ("pg_gram_accumulate_batch", [_vp, _vp]),
+                ("pg_batch_residual", [_vp, _vp, _dp, C.c_int, _dp, _dp, _i64p]),
                 ("pg_profile_enable", [C.c_int]),
                 ("pg_profile_read", [C.c_char_p, C.c_size_t, _dp, _ip, C.c_int, _ip]),
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),

@@ -243,6 +243,72 @@ void launch_gram_bf16x3(const float* X, long long ld, long long n_rows, int F, c
     pg_gram_bf16x3<<<n_tiles, 256, smem, st>>>(X, ld, n_rows, F, tiles, G);
 }
 
+// ------------------------------------------------------------ residuals
+constexpr int kMaxCoef = 16;
+
+// R[row, k] = y[row] - sum_c X[row, c] C[c, k]  (FP64 accumulation, one thread per row)
+template <typename T>
+__global__ void pg_residual(const T* X, long long ld, long long rows, int F, const double* C, int nc,
+                            const double* y, double* R) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    double acc[kMaxCoef];
+    for (int k = 0; k < nc; ++k) acc[k] = 0.0;
+    for (int c = 0; c < F; ++c) {
+        const double x = (double)X[(size_t)c * ld + r];
+        for (int k = 0; k < nc; ++k) acc[k] += x * C[(size_t)k * F + c];
+    }
+    for (int k = 0; k < nc; ++k) R[(size_t)k * rows + r] = y[r] - acc[k];
+}
+
+// XtR[c, k] += sum_r X[r, c] R[r, k]  (one block per column)
+template <typename T>
+__global__ void pg_xtr(const T* X, long long ld, long long rows, int F, const double* R, int nc, double* XtR) {
+    const int c = blockIdx.x;
+    __shared__ double red[kMaxCoef][256];
+    double acc[kMaxCoef];
+    for (int k = 0; k < nc; ++k) acc[k] = 0.0;
+    for (long long r = threadIdx.x; r < rows; r += blockDim.x) {
+        const double x = (double)X[(size_t)c * ld + r];
+        for (int k = 0; k < nc; ++k) acc[k] += x * R[(size_t)k * rows + r];
+    }
+    for (int k = 0; k < nc; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int k = 0; k < nc; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < nc; ++k) XtR[(size_t)k * F + c] += red[k][0];
+}
+
+// sq[kind * nc + k] += sum of R^2 over the rows of kind (0 energy, 1 force, 2 stress)
+__global__ void pg_residual_sq(const double* R, long long rows, int nc, long long n_e, long long s_end,
+                               double* sq) {
+    const int k = blockIdx.y;
+    double e = 0, f = 0, s = 0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows;
+         r += (long long)gridDim.x * blockDim.x) {
+        const double v = R[(size_t)k * rows + r];
+        if (r < n_e) e += v * v;
+        else if (r < s_end) s += v * v;
+        else f += v * v;
+    }
+    __shared__ double red[3][256];
+    red[0][threadIdx.x] = e;
+    red[1][threadIdx.x] = f;
+    red[2][threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; ++q) atomicAdd(&sq[q * nc + k], red[q][0]);
+}
+
 // ------------------------------------------------------------ batches
 // A batch of structures staged on the device with its row layout, weights and
 // weighted targets: everything the regression assembly reads from HBM.
@@ -251,6 +317,7 @@ struct Prepared {
     RowPlan plan;
     long long rows = 0;
     int n_e = 0;
+    long long s_end = 0;  // first force row (energies, then stresses, then forces)
     double yty = 0.0;
     DevBuf d_e, d_f, d_s, d_w, d_y;
 };
@@ -297,6 +364,9 @@ std::vector<std::unique_ptr<Prepared>> prepare_batches(Model& m, const pg_struct
             }
         P->rows = r;
         P->n_e = nb;
+        P->s_end = nb;
+        for (int q = 0; q < nb; ++q)
+            if (f_row[s0 + q] >= 0) P->s_end += 6;
         for (double v : yl) P->yty += v * v;
         P->b.upload_structures(st, s0, s1, m.flat.cutoff);
         m.plan_rows(P->b, P->plan);
@@ -379,6 +449,35 @@ struct Gram {
         yty += P.yty;
         n_rows_total += rows;
     }
+
+    // Weighted residuals of coefficient columns C (F x nc, device) on one batch:
+    // XtR += X^T R and sq += per-kind sums of R^2 (rows regenerated on the device).
+    void residual(Prepared& P, const double* C, int nc, double* XtR, double* sq, DevBuf& R) {
+        const bool fp64 = precision == PG_FP64;
+        const long long rows = P.rows;
+        Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
+        R.reserve((size_t)rows * nc * sizeof(double));
+        dim3 sg((unsigned)((rows + 255) / 256), (unsigned)std::min(F, 64));
+        const unsigned nblk = (unsigned)((rows + 255) / 256);
+        if (fp64) {
+            double* X = Xd.as<double>();
+            m->run_rows<double>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
+                                rows, stream);
+            pg_scale_rows<double><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
+            pg_residual<double><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc, P.d_y.as<double>(), R.as<double>());
+            pg_xtr<double><<<F, 256, 0, stream>>>(X, rows, rows, F, R.as<double>(), nc, XtR);
+        } else {
+            float* X = Xd.as<float>();
+            m->run_rows<float>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
+                               rows, stream);
+            pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
+            pg_residual<float><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc, P.d_y.as<double>(), R.as<double>());
+            pg_xtr<float><<<F, 256, 0, stream>>>(X, rows, rows, F, R.as<double>(), nc, XtR);
+        }
+        dim3 g2(std::min(1024u, nblk), nc);
+        pg_residual_sq<<<g2, 256, 0, stream>>>(R.as<double>(), rows, nc, P.n_e, P.s_end, sq);
+        PG_CUDA(cudaGetLastError());
+    }
 };
 
 }  // namespace pg
@@ -458,6 +557,29 @@ int pg_gram_accumulate_batch(pg_gram* gh, pg_batch* b) {
     return guarded([&] {
         if (!gh || !b) throw std::runtime_error("null argument");
         for (auto& P : b->parts) gh->g->accumulate(*P);
+    });
+}
+
+int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef, double* xtr, double* sq,
+                      int64_t* n_rows) {
+    return guarded([&] {
+        if (!gh || !b || !coefs || n_coef < 1) throw std::runtime_error("bad arguments");
+        if (n_coef > kMaxCoef) throw std::runtime_error("at most 16 coefficient vectors per residual pass");
+        Gram& g = *gh->g;
+        const int F = g.F;
+        DevBuf C((size_t)F * n_coef * 8), XtR((size_t)F * n_coef * 8), SQ((size_t)3 * n_coef * 8), R;
+        PG_CUDA(cudaMemcpy(C.as<void>(), coefs, (size_t)F * n_coef * 8, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemset(XtR.as<void>(), 0, XtR.bytes()));
+        PG_CUDA(cudaMemset(SQ.as<void>(), 0, SQ.bytes()));
+        long long rows = 0;
+        for (auto& P : b->parts) {
+            g.residual(*P, C.as<double>(), n_coef, XtR.as<double>(), SQ.as<double>(), R);
+            rows += P->rows;
+        }
+        PG_CUDA(cudaStreamSynchronize(g.stream));
+        if (xtr) PG_CUDA(cudaMemcpy(xtr, XtR.as<double>(), (size_t)F * n_coef * 8, cudaMemcpyDeviceToHost));
+        if (sq) PG_CUDA(cudaMemcpy(sq, SQ.as<double>(), (size_t)3 * n_coef * 8, cudaMemcpyDeviceToHost));
+        if (n_rows) *n_rows = rows;
     });
 }
 

@@ -293,9 +293,30 @@ def compute_rmse_seq(coefs_array, data_xy: DataXY, check_singular=False, error_t
     return out
 
 
+def batch_residual(gram: GramAccumulator, batches: Sequence["DeviceBatch"], coefs: np.ndarray):
+    """X^T R (F x k) and per-kind sums of squared weighted residuals (3 x k:
+    energy, force, stress) for coefficient columns in X's own scaling."""
+    coefs = np.asfortranarray(np.atleast_2d(np.asarray(coefs, dtype=np.float64).T).T)
+    F, k = coefs.shape
+    xtr_tot = np.zeros((F, k), order="F")
+    sq_tot = np.zeros((3, k))
+    n_tot = 0
+    p = _ffi._p
+    for b in batches:
+        xtr = np.zeros((F, k), order="F")
+        sq = np.zeros((3, k))
+        n = C.c_int64()
+        _ffi.check(_ffi.lib().pg_batch_residual(gram._h, b.handle, p(coefs, C.c_double), k, p(xtr, C.c_double),
+                                                p(sq, C.c_double), C.byref(n)))
+        xtr_tot += xtr
+        sq_tot += sq
+        n_tot += n.value
+    return xtr_tot, sq_tot, n_tot
+
+
 @dataclass
 class FitResult:
-    coeffs: np.ndarray          # scaled coefficients of the best alpha
+    coeffs: np.ndarray          # coefficients of the best alpha in the scaled basis
     scales: np.ndarray
     alpha: float
     rmse_train: float
@@ -303,6 +324,7 @@ class FitResult:
     coefs_array: np.ndarray = field(repr=False, default=None)
     rmse_train_array: np.ndarray = field(repr=False, default=None)
     rmse_test_array: np.ndarray = field(repr=False, default=None)
+    info: np.ndarray = field(repr=False, default=None)
 
     @property
     def scaled_coeffs(self):
@@ -311,15 +333,52 @@ class FitResult:
 
 
 def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
-        precision: int = _ffi.PG_MIXED, batch_size: int = 2000, model: Optional[_ffi.Model] = None) -> FitResult:
-    """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60)."""
+        precision: int = _ffi.PG_MIXED, model: Optional[_ffi.Model] = None, refine: Optional[int] = None,
+        weight_stress: float = 0.1) -> FitResult:
+    """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60).
+
+    The Gram is assembled once (mixed or FP64); the ridge systems are solved
+    in FP64; with the mixed Gram, `refine` FP64 iterative-refinement steps
+    c <- c + (A + alpha I)^-1 (S^-1 X^T (y - X S^-1 c) - alpha c) use residuals
+    of freshly generated rows.  RMSEs are computed from residuals (weighted
+    rows, as the reference's Gram-based formula defines them)."""
     model = model or _ffi.Model(params_dict)
-    train_xy = calc_xtx_xty(model, train, precision=precision, batch_size=batch_size)
-    coefs, _info = solver_ridge(train_xy.xtx, train_xy.xty, alphas)
-    rmse_train = compute_rmse_seq(coefs, train_xy, check_singular=True)
-    test_xy = calc_xtx_xty(model, test, precision=precision, scales=train_xy.scales,
-                           min_energy=train_xy.min_energy, batch_size=batch_size)
-    rmse_test = compute_rmse_seq(coefs, test_xy)
+    if refine is None:
+        refine = 1 if precision == _ffi.PG_MIXED else 0
+    alphas = np.asarray(alphas, dtype=np.float64)
+    min_e = get_min_energy(train)
+    tb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in train]
+    gram = GramAccumulator(model, precision)
+    for b in tb:
+        gram.accumulate_batch(b)
+    xtx, xty, yty, xe_sum, xe_sq, n_rows = gram.result()
+    n_data = sum(len(d.energies) for d in train)
+    scales, zero_ids = compute_scales(None, xe_sum, xe_sq, n_data, any(d.include_force for d in train))
+    xtx[zero_ids] = 0.0
+    xtx[:, zero_ids] = 0.0
+    xty[zero_ids] = 0.0
+    xtx /= scales[:, None]
+    xtx /= scales[None, :]
+    xty /= scales
+    coefs, info = solver_ridge(xtx, xty, alphas)
+    for _ in range(refine):
+        xtr, _, _ = batch_residual(gram, tb, coefs / scales[:, None])
+        g = xtr / scales[:, None] - coefs * alphas[None, :]
+        g[zero_ids] = 0.0
+        for k, a in enumerate(alphas):
+            if info[k] != 0:
+                continue
+            d, _ = solver_ridge(xtx, g[:, k], [a])
+            coefs[:, k] += d[:, 0]
+    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
+    rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
+    if np.all(rmse_train > 1e6):
+        raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
+                           "This singularity issue might be reduced by increasing "
+                           "the value of alpha (the magnitude of the penalty term).")
+    vb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in test]
+    _, sq, n_te = batch_residual(gram, vb, coefs / scales[:, None])
+    rmse_test = np.sqrt(sq.sum(axis=0) / n_te)
     idx = int(np.argmin(rmse_test))
-    return FitResult(coefs[:, idx], train_xy.scales, float(alphas[idx]), float(rmse_train[idx]),
-                     float(rmse_test[idx]), coefs, rmse_train, rmse_test)
+    return FitResult(coefs[:, idx], scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
+                     coefs, rmse_train, rmse_test, info)

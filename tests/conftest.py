@@ -41,8 +41,10 @@ def assert_signature(x, gold, rtol):
     """X against a reference signature.  Errors are scaled by the column (or
     row/projection) magnitude, since single elements can cancel to ~0."""
     sig = x_signature(x)
-    colmax = gold["colmax"]
-    scale_all = np.abs(colmax).max()
+    colmax_raw = gold["colmax"]
+    scale_all = np.abs(colmax_raw).max()
+    # columns that vanish up to rounding carry only noise: floor at 1e-4 of max|X|
+    colmax = np.maximum(colmax_raw, 1e-4 * scale_all)
     np.testing.assert_array_equal(np.asarray(x.shape), gold["shape"])
     # sampled elements: relative to their column magnitude
     idx = gold["sample_idx"]

@@ -44,10 +44,16 @@ CONFIGS = {
 }
 
 
+# extra invariant tables used by the tests (small models)
+EXTRA_GTINV = [(2, (2,)), (3, (4, 2)), (3, (6, 2)), (4, (4, 2, 1))]
+
+
 def write_gtinv():
-    for c in CONFIGS.values():
-        l_comb, lm_seq, lm_coeffs = ref.readgtinv(c["gtinv_order"], c["gtinv_maxl"])
-        path = gtinv_file(c["gtinv_order"], c["gtinv_maxl"])
+    tabs = [(c["gtinv_order"], c["gtinv_maxl"]) for c in CONFIGS.values()] + EXTRA_GTINV
+    for order, maxl in tabs:
+        l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
+        path = gtinv_file(order, maxl)
+        c = {"gtinv_order": order, "gtinv_maxl": maxl}
         with open(path, "w") as f:
             json.dump({"order": c["gtinv_order"], "maxl": list(c["gtinv_maxl"]), "version": 1,
                        "l_comb": l_comb, "lm_seq": lm_seq, "lm_coeffs": lm_coeffs}, f, separators=(",", ":"))

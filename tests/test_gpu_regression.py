@@ -44,7 +44,8 @@ def test_gram_fp64_and_mixed_match_cpu():
     scale = np.abs(ref.xtx).max()
     assert np.abs(g64.xtx - ref.xtx).max() / scale < 1e-12
     assert np.abs(g64.xty - ref.xty).max() / np.abs(ref.xty).max() < 1e-12
-    np.testing.assert_allclose(g64.scales, ref.scales, rtol=1e-12)
+    # scales come from E[x^2] - E[x]^2, which cancels: compare loosely
+    np.testing.assert_allclose(g64.scales, ref.scales, rtol=1e-8)
     assert abs(g64.y_sq_norm - ref.y_sq_norm) <= 1e-12 * ref.y_sq_norm
     assert g64.total_n_data == ref.total_n_data
     g32 = calc_xtx_xty(m, train, precision=_ffi.PG_MIXED, batch_size=7)
@@ -77,8 +78,30 @@ def test_ridge_singular_gives_1e30():
     assert np.all(got == 1e30)
 
 
+def _energy_force_rmse(params, coefs_unscaled, datasets):
+    """Energy RMSE per atom (eV/atom) and force RMSE (eV/A) of a model, with
+    predictions from the CPU oracle's FP64 X rows."""
+    from oracle import oracle
+    from pypolymlp_gb300.abi import Structures, row_layout
+
+    de, df = [], []
+    for d in datasets:
+        st = Structures(d.axis, d.positions, d.types)
+        e, f, s, n = row_layout(st.n_atoms, [True] * st.n_st)
+        x = oracle.features_x(params, st, e, f, s, n)
+        pred = x @ coefs_unscaled
+        de.append((pred[e] - d.energies) / st.n_atoms)
+        fr = np.concatenate([pred[f[k]:f[k] + 3 * st.n_atoms[k]] for k in range(st.n_st)])
+        df.append(fr - np.concatenate([np.asarray(v).reshape(-1) for v in d.forces]))
+    de, df = np.concatenate(de), np.concatenate(df)
+    return float(np.sqrt(np.mean(de ** 2))), float(np.sqrt(np.mean(df ** 2)))
+
+
 def test_fit_mixed_vs_fp64_rmse():
-    """End-to-end fit: mixed-precision RMSE within 0.05 meV/atom of the FP64 CPU fit."""
+    """End-to-end fit.  FP64 GPU path: test RMSEs of every alpha equal the CPU
+    pipeline's (Gram formula, LAPACK posv) to 1e-6.  Mixed path (BF16x3 Gram,
+    FP64 Cholesky + one refinement step): the selected model's energy RMSE
+    within 0.05 meV/atom and force RMSE within 1 meV/A of the FP64 fit."""
     from pypolymlp_gb300 import _ffi
     from pypolymlp_gb300.regression import compute_rmse_seq, fit
 
@@ -90,8 +113,9 @@ def test_fit_mixed_vs_fp64_rmse():
     ref_test = calc_xtx_xty_cpu(p, test, scales=ref_train.scales, min_energy=ref_train.min_energy)
     rmse_ref = compute_rmse_seq(coefs, ref_test)
     r64 = fit(p, train, test, alphas, precision=_ffi.PG_FP64)
-    r32 = fit(p, train, test, alphas, precision=_ffi.PG_MIXED)
     np.testing.assert_allclose(r64.rmse_test_array, rmse_ref, rtol=1e-6)
-    # the RMSE here is over weighted rows (energy per structure, forces, stresses);
-    # compare the selected models' test RMSE
-    assert abs(r32.rmse_test - r64.rmse_test) < 5e-5 * 32
+    r32 = fit(p, train, test, alphas, precision=_ffi.PG_MIXED)
+    e64, f64 = _energy_force_rmse(p, r64.scaled_coeffs, test)
+    e32, f32 = _energy_force_rmse(p, r32.scaled_coeffs, test)
+    assert abs(e32 - e64) < 0.05e-3, (e32, e64)
+    assert abs(f32 - f64) < 1e-3, (f32, f64)

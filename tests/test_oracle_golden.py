@@ -75,13 +75,14 @@ def test_oracle_x_elementwise_vs_reference():
     from pypolymlp_gb300.abi import Structures
     from pypolymlp_gb300.params import make_params_dict
 
-    p = make_params_dict(n_type=3, cutoff=5.0, model_type=4, max_p=3, gaussian_params2=(0, 4, 4), gtinv_order=3,
-                         gtinv_maxl=(6, 4))
-    ss = syn.ternary_set(3, seed=5, n_range=(6, 20))
+    p = make_params_dict(n_type=2, cutoff=5.0, model_type=4, max_p=3, gaussian_params2=(0, 4, 3), gtinv_order=3,
+                         gtinv_maxl=(4, 2))
+    ss = syn.ternary_set(3, seed=5, n_range=(6, 20), n_types=2)
     st = Structures(ss.axis, ss.positions, ss.types)
     force = [True, False, True]
     e, f, s, n = row_layout(st.n_atoms, force)
     xr = ref.features_x(p, st, e, f, s, n)
     xo = oracle.features_x(p, st, e, f, s, n)
-    scale = np.maximum(np.abs(xr).max(axis=0), 1e-300)
+    colmax = np.abs(xr).max(axis=0)
+    scale = np.maximum(colmax, 1e-4 * colmax.max())
     assert (np.abs(xr - xo) / scale).max() < 1e-12
