@@ -66,9 +66,9 @@ _BCC = np.array([[0, 0, 0], [0.5, 0.5, 0.5]], dtype=float)
 def _supercell(basis, reps, a):
     n1, n2, n3 = reps
     grid = np.array([[i, j, k] for i in range(n1) for j in range(n2) for k in range(n3)], dtype=float)
-    frac = (grid[:, None, :] + basis[None, :, :]).reshape(-1, 3)
+    cells = (grid[:, None, :] + basis[None, :, :]).reshape(-1, 3)  # in conventional-cell units
     axis = np.diag([n1 * a, n2 * a, n3 * a]).astype(float)
-    return axis, frac @ axis.T
+    return axis, cells * a
 
 
 def fcc_set(n_struct=200, seed=1):

@@ -50,8 +50,8 @@ def test_gram_fp64_and_mixed_match_cpu():
     assert g64.total_n_data == ref.total_n_data
     g32 = calc_xtx_xty(m, train, precision=_ffi.PG_MIXED, batch_size=7)
     assert np.abs(g32.xtx - ref.xtx).max() / scale < 1e-5
-    # symmetric
-    assert np.array_equal(g64.xtx, g64.xtx.T)
+    # symmetric up to the rounding of the two-sided column scaling
+    assert np.abs(g64.xtx - g64.xtx.T).max() <= 1e-14 * scale
 
 
 def test_ridge_solve_matches_posv():
