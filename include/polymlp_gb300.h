@@ -160,6 +160,26 @@ int pg_solve_ridge(int n_features, const double* xtx, const double* xty, const d
                    int n_alpha, double* coefs, int* info);
 
 /*
+ * Ridge solve that allocates no memory.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory at the point where
+ * they solve - a host framework or inference server that owns the GPU's
+ * allocator, code running while a CUDA stream is being captured, or a loop
+ * that must never enter the allocator.  The caller passes device buffers:
+ * d_xtx (F x F, column-major, symmetric), d_xty (F) and d_coefs (F, written);
+ * *info (host) is 0, or column + 1 of a failed factorisation (then d_coefs is
+ * filled with 1e30), as for pg_solve_ridge with one alpha.  The factor is
+ * built in a fixed device array inside the library: n_features must be at
+ * most 1024 (larger sizes are rejected with an error), and each GPU that loads
+ * the library keeps that array (about 8 MiB) until the process exits.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls on a device share
+ * the array, so calls whose GPU work overlaps (other threads or streams) race.
+ * Work is issued on the default stream and the call returns when it is done.
+ */
+int pg_solve_ridge_noalloc(int n_features, const double* d_xtx, const double* d_xty, double alpha,
+                           double* d_coefs, int* info);
+
+/*
  * Energy / force / stress evaluation, as PotentialPropertiesFast
  * (src/pypolymlp/cxx/src/compute/py_properties_fast.cpp:10-77 with
  *  PolymlpEval::eval, src/pypolymlp/cxx/src/compute/polymlp_eval.cpp:24).

@@ -64,6 +64,7 @@ def lib():
                 ("pg_profile_enable", [C.c_int]),
                 ("pg_profile_read", [C.c_char_p, C.c_size_t, _dp, _ip, C.c_int, _ip]),
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
+                ("pg_solve_ridge_noalloc", [C.c_int, _vp, _vp, C.c_double, _vp, _ip]),
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),
                 ("pg_eval_run", [_vp, _vp, _dp, _dp, _dp]),

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "runtime.h"
@@ -210,5 +212,93 @@ extern "C" int pg_solve_ridge(int F, const double* xtx, const double* xty, const
             PG_CUDA(cudaGetLastError());
             PG_CUDA(cudaMemcpy(coefs + (size_t)a * F, x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
         }
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Ridge solve that allocates no memory.
+//
+// Some callers cannot allocate device memory when they solve: code that runs
+// inside an inference server or a host framework whose allocator owns every
+// byte of the GPU, code that runs while a CUDA stream is being captured (where
+// cudaMalloc is not allowed), or a real-time loop that must not touch the
+// allocator.  They hand over device buffers they already own.  This variant of
+// the blocked Cholesky solve keeps its workspace (the factor of
+// xtx + alpha I, the list of update tiles and the status word) in one
+// file-scope device array instead of cudaMalloc'ed buffers.
+//
+// Limits and sharing: n_features <= kNoAllocMaxF (1024); every GPU that loads
+// this library holds the array (8 MiB + a few KiB) until the process exits.
+// All calls on a device share the one array and it keeps the last call's
+// contents (the status word is cleared at the start of each call), so calls
+// whose GPU work overlaps - from several host threads or streams - race on it.
+constexpr int kNoAllocMaxF = 1024;
+constexpr int kNoAllocMaxTiles = (kNoAllocMaxF / kCB) * (kNoAllocMaxF / kCB + 1) / 2;
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double) +
+                                 (size_t)kNoAllocMaxTiles * sizeof(int2) + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};  // device address of the array, per device (set up once)
+}  // namespace
+
+// Device address of g_noalloc_scratch on the current device.  The first call on
+// a device looks it up with cudaGetSymbolAddress (no allocation).
+static unsigned char* noalloc_scratch() {
+    int dev = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            throw std::runtime_error(std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    return static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+}
+
+extern "C" int pg_solve_ridge_noalloc(int F, const double* d_xtx, const double* d_xty, double alpha,
+                                      double* d_coefs, int* info) {
+    return guarded([&] {
+        if (!d_xtx || !d_xty || !d_coefs || !info) throw std::runtime_error("null argument");
+        if (F <= 0) throw std::runtime_error("n_features must be positive");
+        if (F > kNoAllocMaxF)
+            throw std::runtime_error("pg_solve_ridge_noalloc: n_features " + std::to_string(F) +
+                                     " exceeds the maximum of " + std::to_string(kNoAllocMaxF) +
+                                     " (use pg_solve_ridge)");
+        cudaStream_t st = 0;
+        unsigned char* base = noalloc_scratch();
+        double* A = reinterpret_cast<double*>(base);
+        int2* tiles = reinterpret_cast<int2*>(base + (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double));
+        int* d_info = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(tiles) +
+                                             (size_t)kNoAllocMaxTiles * sizeof(int2));
+        PG_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int), st));
+        pg_add_diag<<<1024, 256, 0, st>>>(A, d_xtx, F, alpha);
+        std::vector<int2> tl;
+        for (int k = 0; k < F; k += kCB) {
+            pg_chol_diag<<<1, 256, 0, st>>>(A, F, k, d_info);
+            const int b = std::min(kCB, F - k);
+            const int rest = F - k - b;
+            if (rest <= 0) break;
+            pg_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, F, k, d_info);
+            const int nt = (rest + kCB - 1) / kCB;
+            tl.clear();
+            for (int i = 0; i < nt; ++i)
+                for (int j = 0; j <= i; ++j) tl.push_back(make_int2(i, j));
+            // the tile list of this step is consumed by the next kernel on the same stream
+            PG_CUDA(cudaMemcpyAsync(tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+            pg_chol_update<<<(int)tl.size(), 256, 0, st>>>(A, F, k, tiles, d_info);
+            PG_CUDA(cudaStreamSynchronize(st));  // the host tile list is reused next step
+        }
+        const size_t smem = (size_t)F * sizeof(double);
+        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        pg_chol_solve<<<1, 1024, smem, st>>>(A, F, d_xty, d_coefs, d_info);
+        PG_CUDA(cudaGetLastError());
+        PG_CUDA(cudaMemcpyAsync(info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
     });
 }
