@@ -44,7 +44,7 @@ ProfScope::~ProfScope() {
 }
 
 // ------------------------------------------------------------ DeviceModel
-void DeviceModel::build(const FlatModel& fm, int chunk_width) {
+void DeviceModel::build(const FlatModel& fm, int max_chunk, bool fp64) {
     if (fm.n_type > kMaxTypes) throw std::runtime_error("at most 8 atom types are supported on the device");
     bufs.clear();
     bufs.reserve(64 * kMaxTypes);
@@ -53,8 +53,6 @@ void DeviceModel::build(const FlatModel& fm, int chunk_width) {
         upload(bufs.back(), v);
         return bufs.back().template as<void>();
     };
-    chunk = chunk_width;
-    n_chunks = (fm.n_features + chunk - 1) / chunk;
     dm = DevModel{};
     dm.n_type = fm.n_type;
     dm.n_tp = fm.n_tp;
@@ -64,11 +62,65 @@ void DeviceModel::build(const FlatModel& fm, int chunk_width) {
     dm.n_ylm = fm.n_ylm;
     dm.gtinv = fm.gtinv ? 1 : 0;
     dm.cutoff = fm.cutoff;
+    // Column chunks: balanced widths (multiples of 32, at most max_chunk) whose
+    // shared-memory footprint, which grows with the G entries of a chunk, fits.
+    const int F = fm.n_features;
+    auto cap_for = [&](int ch) {
+        int cap = 1;
+        for (const auto& ft : fm.types)
+            for (int c0 = 0; c0 < F; c0 += ch) {
+                int acc = 0;
+                for (int c = c0; c < std::min(F, c0 + ch); ++c) acc += ft.col_nent[c];
+                cap = std::max(cap, acc);
+            }
+        return cap;
+    };
+    const size_t smem_limit = 227 * 1024;
+    int nch = (F + max_chunk - 1) / max_chunk;
+    for (;; ++nch) {
+        int ch = (F + nch - 1) / nch;
+        ch = (ch + 31) / 32 * 32;
+        const int cap = cap_for(ch);
+        if (rows_smem_bytes(dm, ch, cap, fp64) <= smem_limit || ch <= 32) {
+            chunk = ch;
+            chunk_cap_ent = cap;
+            break;
+        }
+    }
+    if (rows_smem_bytes(dm, chunk, chunk_cap_ent, fp64) > smem_limit)
+        throw std::runtime_error("model too large for the pg_rows shared-memory layout");
+    n_chunks = (F + chunk - 1) / chunk;
+    // Per centre type, the threads of a chunk take its columns in order of their
+    // adjoint-entry signature (which type pairs have entries, then how many), so
+    // the lanes of a warp mostly share the same loop length for a given pair.
+    std::vector<std::vector<int>> perm(fm.n_type, std::vector<int>(F));
+    for (int t = 0; t < fm.n_type; ++t) {
+        const FlatType& ft = fm.types[t];
+        for (int c0 = 0; c0 < F; c0 += chunk) {
+            const int c1 = std::min(F, c0 + chunk);
+            std::vector<std::pair<std::vector<int>, int>> key;
+            for (int c = c0; c < c1; ++c) {
+                std::vector<int> cnt(fm.n_tp, 0);
+                for (int q = 0; q < ft.col_ncomp[c]; ++q) {
+                    const int k = ft.comp_k[(size_t)c * 3 + q];
+                    for (int tp = 0; tp < fm.n_tp; ++tp)
+                        cnt[tp] += ft.ent_tp_off[(size_t)k * (fm.n_tp + 1) + tp + 1] -
+                                   ft.ent_tp_off[(size_t)k * (fm.n_tp + 1) + tp];
+                }
+                std::vector<int> k2;
+                for (int tp = 0; tp < fm.n_tp; ++tp) k2.push_back(cnt[tp] > 0 ? 0 : 1);
+                for (int tp = 0; tp < fm.n_tp; ++tp) k2.push_back(-cnt[tp]);
+                key.push_back({k2, c});
+            }
+            std::stable_sort(key.begin(), key.end());
+            for (int q = 0; q < c1 - c0; ++q) perm[t][c0 + q] = key[q].second;
+        }
+    }
     dm.type_pairs = (const int*)up(fm.type_pairs);
     dm.tp_nfn = (const int*)up(fm.tp_nfn);
     dm.tp_beta = (const double*)up(fm.tp_beta);
     dm.tp_mu = (const double*)up(fm.tp_mu);
-    chunk_cap_ent = 1;
+    dm.ylm_tab = (const double*)up(fm.ylm_tab);
     for (int t = 0; t < fm.n_type; ++t) {
         const FlatType& ft = fm.types[t];
         DevType& d = dm.types[t];
@@ -96,15 +148,16 @@ void DeviceModel::build(const FlatModel& fm, int chunk_width) {
         d.comp_k = (const int*)up(ft.comp_k);
         d.comp_w = (const int*)up(ft.comp_w);
         d.col_nent = (const int*)up(ft.col_nent);
-        std::vector<int> coff(fm.n_features, 0);
-        for (int c0 = 0; c0 < fm.n_features; c0 += chunk) {
+        std::vector<int> coff(F, 0);
+        for (int c0 = 0; c0 < F; c0 += chunk) {
             int acc = 0;
-            for (int c = c0; c < std::min(fm.n_features, c0 + chunk); ++c) {
+            for (int q = c0; q < std::min(F, c0 + chunk); ++q) {
+                const int c = perm[t][q];
                 coff[c] = acc;
                 acc += ft.col_nent[c];
             }
-            chunk_cap_ent = std::max(chunk_cap_ent, acc);
         }
+        d.col_perm = (const int*)up(perm[t]);
         d.col_ent_off = (const int*)up(coff);
         std::vector<int> meta(ft.ent_head.size());
         for (size_t e = 0; e < ft.ent_head.size(); ++e) {
@@ -114,6 +167,7 @@ void DeviceModel::build(const FlatModel& fm, int chunk_width) {
             meta[e] = ft.head_tp[h] | (ft.head_nid[h] << 8) | (ft.head_key[h] << 16);
         }
         d.ent_meta = (const int*)up(meta);
+        d.ent_tp_off = (const int*)up(ft.ent_tp_off);
     }
 }
 
@@ -213,8 +267,8 @@ Model::Model(const pg_feature_params* p)
     : tables(build_model_tables(feature_params_from_abi(p))), flat(flatten_model(tables)) {
     int dev = 0;
     PG_CUDA(cudaGetDevice(&dev));
-    dev64.build(flat, 128);
-    dev32.build(flat, 256);
+    dev64.build(flat, 256, true);
+    dev32.build(flat, 512, false);
     max_k = max_k0 = 1;
     for (const auto& ft : flat.types) {
         max_k = std::max(max_k, ft.K);

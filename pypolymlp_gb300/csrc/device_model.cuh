@@ -36,7 +36,9 @@ struct DevType {
     const int *ent_off, *ent_head, *term_off;
     const FlatTerm* g_terms;
     const int *col_ncomp, *comp_k, *comp_w, *col_nent, *col_ent_off;
-    const int* ent_meta;  // per G entry: tp | nid << 8 | key << 16
+    const int* ent_meta;    // per G entry: tp | nid << 8 | key << 16
+    const int* ent_tp_off;  // per linear feature k: (n_tp + 1) entry offsets by type pair
+    const int* col_perm;    // pg_rows: for centres of this type, thread q of a chunk takes column col_perm[chunk0 + q]
 };
 
 struct DevModel {
@@ -45,8 +47,51 @@ struct DevModel {
     const int* type_pairs;
     const int* tp_nfn;
     const double *tp_beta, *tp_mu;
+    // Legendre/Y_lm constants (ylm_table_size doubles), see ylm_tables()
+    const double* ylm_tab;
     DevType types[kMaxTypes];
 };
+
+// Constants of the normalised associated Legendre recursion and of the Y_lm
+// gradients, which depend on (l, m) only:
+//   A[lm], B[lm]  recursion coefficients for m <= l - 2,
+//   D1[lm]        sqrt((l - m)(l + m + 1)) for m < l,
+//   C1[l] = -sqrt(1 + 0.5 / l), C2[m] = sqrt(2m + 3), D0[l] = sqrt(l (l + 1) / 2),
+//   DEC[idx]      (l, m') of the m <= 0 index idx = l(l+1)/2 + l - m'.
+// Layout: A | B | D1 | DEC (n_ylm each) | C1 | C2 | D0 (maxl + 1 each).
+__host__ __device__ inline int ylm_table_size(int n_ylm, int maxl) { return 4 * n_ylm + 3 * (maxl + 1); }
+
+template <typename T>
+struct YlmTab {
+    const T *A, *B, *D1, *C1, *C2, *D0;
+    const int* DEC;
+};
+
+template <typename T>
+__device__ inline YlmTab<T> ylm_tab_view(const T* base, int n_ylm, int maxl) {
+    YlmTab<T> t;
+    t.A = base;
+    t.B = base + n_ylm;
+    t.D1 = base + 2 * n_ylm;
+    t.DEC = reinterpret_cast<const int*>(base + 3 * n_ylm);
+    t.C1 = base + 4 * n_ylm;
+    t.C2 = t.C1 + maxl + 1;
+    t.D0 = t.C2 + maxl + 1;
+    return t;
+}
+
+// Copy the constants into shared memory as T (the DEC entries keep their bits).
+template <typename T>
+__device__ inline void load_ylm_tab(const double* src, T* dst, int n_ylm, int maxl) {
+    const int n = ylm_table_size(n_ylm, maxl);
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        if (q >= 3 * n_ylm && q < 4 * n_ylm) {
+            reinterpret_cast<int*>(dst + 3 * n_ylm)[q - 3 * n_ylm] = (int)src[q];
+        } else {
+            dst[q] = (T)src[q];
+        }
+    }
+}
 
 // Basis of one pair image, in shared memory, computed by one warp.
 template <typename T>
@@ -86,7 +131,7 @@ __device__ __forceinline__ int lmi(int l, int m) { return l * (l + 1) / 2 + m; }
 // Radial functions of one type pair at distance dis
 // (polymlp_basis_function.h:16-43, polymlp_functions_interface.cpp:41-62).
 template <typename T, bool DERIV>
-__device__ inline void warp_radial(const DevModel& M, int tp, double dis, BasisView<T>& B, int lane) {
+__device__ __noinline__ void warp_radial(const DevModel& M, int tp, double dis, BasisView<T> B, int lane) {
     const int nfn = M.tp_nfn[tp];
     const T r = (T)dis;
     const T rc = (T)M.cutoff;
@@ -112,11 +157,11 @@ __device__ inline void warp_radial(const DevModel& M, int tp, double dis, BasisV
 // Y_lm (m <= 0, index l(l+1)/2 + l + m) and gradients of the unit vector
 // (x, y, z)/r, following the normalised associated Legendre recursion of
 // polymlp_spherical_harmonics.cpp:27-209 (Limpanuparb & Milthorpe,
-// arXiv:1410.1748).  Lane m computes the Legendre column m; lanes then fill
-// the (l, m) table.  Caller must __syncwarp() before reading B.
+// arXiv:1410.1748), with the (l, m) constants read from a table.  Lane m
+// computes the Legendre column m; lanes then fill the (l, m) table.
 template <typename T, bool DERIV>
-__device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, double zd, double rd, BasisView<T>& B,
-                                int lane) {
+__device__ __noinline__ void warp_ylm(int maxl, int n_ylm, const YlmTab<T>& tab, double xd, double yd, double zd,
+                                double rd, BasisView<T> B, int lane) {
     const T x = (T)xd, y = (T)yd, z = (T)zd, r = (T)rd;
     const T ct = z / r;
     const T rho = hypot(x, y);
@@ -136,7 +181,7 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
             pmm = -st * sq32 * s2pi;
             qmm = -sq32 * s2pi;
             for (int l = 2; l <= m; ++l) {
-                const T c1 = -sqrt((T)1.0 + (T)0.5 / (T)l) * st;
+                const T c1 = tab.C1[l] * st;
                 pmm = c1 * pmm;
                 qmm = c1 * qmm;
             }
@@ -149,7 +194,7 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
                 p1 = ct * sq3 * s2pi;
                 q1 = 0;
             } else {
-                const T c2 = sqrt((T)2.0 * (T)m + (T)3.0) * ct;
+                const T c2 = tab.C2[m] * ct;
                 p1 = c2 * pmm;
                 q1 = c2 * qmm;
             }
@@ -157,9 +202,7 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
             B.Q[lmi(m + 1, m)] = q1;
             T p2 = pmm, q2 = qmm;
             for (int l = m + 2; l <= L; ++l) {
-                const T ls = (T)(l * l), lm1s = (T)((l - 1) * (l - 1)), ms = (T)(m * m);
-                const T alm = sqrt(((T)4.0 * ls - (T)1.0) / (ls - ms));
-                const T blm = -sqrt((lm1s - ms) / ((T)4.0 * lm1s - (T)1.0));
+                const T alm = tab.A[lmi(l, m)], blm = tab.B[lmi(l, m)];
                 const T p = alm * (ct * p1 + blm * p2);
                 const T q = alm * (ct * q1 + blm * q2);
                 B.P[lmi(l, m)] = p;
@@ -184,7 +227,6 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
         B.sn[m] = s1;
     }
     if (lane == 0) {
-        // Q_{l}^{1} for l = 0 reads index 1 (= Q_1^0 = 0); keep the slot past the end zero
         B.P[n_ylm] = 0;
         B.Q[n_ylm] = 0;
         B.P[n_ylm + 1] = 0;
@@ -194,14 +236,13 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
     const T h = (T)0.5 * (T)1.41421356237309504880;
     const T invr = (T)1 / r;
     for (int idx = lane; idx < n_ylm; idx += 32) {
-        int l = 0;
-        while ((l + 1) * (l + 2) / 2 <= idx) ++l;
-        const int mp = lmi(l, 0) + l - idx;  // m = -mp
+        const int dec = tab.DEC[idx];
+        const int l = dec & 0xff, mp = dec >> 8;  // m = -mp
         if (mp == 0) {
             B.Y[idx] = {B.P[lmi(l, 0)] * h, (T)0};
             if (DERIV) {
                 const T qv = (l == 0) ? B.Q[1] : B.Q[lmi(l, 1)];
-                const T common = qv * st * invr * sqrt((T)0.5 * (T)l * (T)(l + 1));
+                const T common = qv * st * invr * tab.D0[l];
                 B.dY[idx] = {common * ct * cp, (T)0};
                 B.dY[n_ylm + idx] = {common * ct * sp, (T)0};
                 B.dY[2 * n_ylm + idx] = {-common * st, (T)0};
@@ -215,9 +256,8 @@ __device__ inline void warp_ylm(int maxl, int n_ylm, double xd, double yd, doubl
                 const cplx<T> common = {c * h * invr, s * h * invr};
                 const T qlm = B.Q[lmi(l, mp)];
                 T dth = (T)mp * ct * qlm;
-                if (mp != l) dth += sqrt((T)((l - mp) * (l + mp + 1))) * B.Q[lmi(l, mp + 1)] * st;
+                if (mp != l) dth += tab.D1[lmi(l, mp)] * B.Q[lmi(l, mp + 1)] * st;
                 const T dph = (T)mp * qlm;  // imaginary
-                // common * (dth*ct*cp - i*dph*sp)
                 cplx<T> ax = cmul(common, cplx<T>{dth * ct * cp, -dph * sp});
                 cplx<T> ay = cmul(common, cplx<T>{dth * ct * sp, dph * cp});
                 cplx<T> az = {-common.re * dth * st, -common.im * dth * st};

@@ -2,6 +2,7 @@
 #include "flat_tables.h"
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <stdexcept>
 
@@ -87,20 +88,22 @@ FlatModel flatten_model(const ModelTables& mt) {
             ft.ent_off.push_back(0);
             ft.term_off.push_back(0);
             for (int k = 0; k < ft.n_lin; ++k) {
-                std::map<int, std::vector<FlatTerm>> by_head;
+                // key: (type pair of the head, head)
+                std::map<std::pair<int, int>, std::vector<FlatTerm>> by_head;
                 for (const auto& d : tt.deriv_terms[k]) {
                     const auto& fe = tt.full[d.head];
-                    if (fe.conj) {
-                        by_head[full_to_head.at(fe.ilocal_conj_id)].push_back(make_term(d.coeff, d.rest, 1));
-                    } else {
-                        by_head[full_to_head.at(d.head)].push_back(make_term(d.coeff, d.rest, 0));
-                    }
+                    const int h = fe.conj ? full_to_head.at(fe.ilocal_conj_id) : full_to_head.at(d.head);
+                    by_head[{tt.noconj[h].tp, h}].push_back(make_term(d.coeff, d.rest, fe.conj ? 1 : 0));
                 }
+                std::vector<int> tpo(mt.n_type_pairs + 1, 0);
                 for (auto& kv : by_head) {
-                    ft.ent_head.push_back(kv.first);
+                    ft.ent_head.push_back(kv.first.second);
                     for (auto& term : kv.second) ft.g_terms.push_back(term);
                     ft.term_off.push_back((int)ft.g_terms.size());
+                    tpo[kv.first.first + 1]++;
                 }
+                for (int t = 0; t < mt.n_type_pairs; ++t) tpo[t + 1] += tpo[t];
+                for (int t = 0; t <= mt.n_type_pairs; ++t) ft.ent_tp_off.push_back(ft.ent_off.back() + tpo[t]);
                 ft.ent_off.push_back((int)ft.ent_head.size());
             }
         } else {
@@ -126,9 +129,11 @@ FlatModel flatten_model(const ModelTables& mt) {
                 const int h = tt.value_terms[k][0].ids[0];
                 ft.val_terms.push_back(make_term(1.0, {h}, 0));
                 ft.val_off.push_back((int)ft.val_terms.size());
+                const int e0 = (int)ft.ent_head.size();
                 ft.ent_head.push_back(h);
                 ft.g_terms.push_back(make_term(1.0, {}, 0));
                 ft.term_off.push_back((int)ft.g_terms.size());
+                for (int t = 0; t <= mt.n_type_pairs; ++t) ft.ent_tp_off.push_back(t <= tt.ntp[h].tp ? e0 : e0 + 1);
                 ft.ent_off.push_back((int)ft.ent_head.size());
             }
         }
@@ -150,6 +155,30 @@ FlatModel flatten_model(const ModelTables& mt) {
             }
         }
         for (int c = 0; c < F; ++c) fm.max_nent_col = std::max(fm.max_nent_col, ft.col_nent[c]);
+    }
+    // Legendre / Y_lm constants, computed in IEEE double with the reference's
+    // expressions (polymlp_spherical_harmonics.cpp:95-196).
+    {
+        const int L = fm.maxl, n = fm.n_ylm;
+        auto lmi = [](int l, int m) { return l * (l + 1) / 2 + m; };
+        std::vector<double> t(4 * n + 3 * (L + 1), 0.0);
+        for (int l = 0; l <= L; ++l) {
+            const double ls = l * l, lm1s = (l - 1) * (l - 1);
+            for (int m = 0; m <= l; ++m) {
+                const double ms = m * m;
+                if (m <= l - 2) {
+                    t[lmi(l, m)] = std::sqrt((4.0 * ls - 1.0) / (ls - ms));
+                    t[n + lmi(l, m)] = -std::sqrt((lm1s - ms) / (4.0 * lm1s - 1.0));
+                }
+                if (m < l) t[2 * n + lmi(l, m)] = std::sqrt((double)((l - m) * (l + m + 1)));
+                // DEC: index l(l+1)/2 + l - m' for m' = m
+                t[3 * n + lmi(l, 0) + l - m] = (double)(l | (m << 8));
+            }
+            t[4 * n + l] = l >= 2 ? -std::sqrt(1.0 + 0.5 / l) : 0.0;
+            t[4 * n + (L + 1) + l] = std::sqrt(2.0 * l + 3.0);
+            t[4 * n + 2 * (L + 1) + l] = std::sqrt(0.5 * l * (l + 1));
+        }
+        fm.ylm_tab = t;
     }
     return fm;
 }

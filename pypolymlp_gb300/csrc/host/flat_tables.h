@@ -37,6 +37,9 @@ struct FlatType {
     std::vector<FlatTerm> val_terms;
     // G entries per linear feature (CSR over features), head per entry, terms per entry (CSR)
     std::vector<int> ent_off, ent_head, term_off;
+    // per linear feature k: (n_tp + 1) offsets of its entries by type pair
+    // (entries of a feature are sorted by type pair, then head)
+    std::vector<int> ent_tp_off;
     std::vector<FlatTerm> g_terms;
     // per column (all F columns): recipe components.  comp_k[col*3+c] is the
     // local linear feature (-1 = unused); comp_w[(col*3+c)*2+q] are the
@@ -56,6 +59,7 @@ struct FlatModel {
     std::vector<double> tp_beta, tp_mu; // [tp*n_fn_max + n_id]
     std::vector<FlatType> types;
     int max_nent_col = 0;               // max G entries of a single column (any type)
+    std::vector<double> ylm_tab;        // Legendre / Y_lm constants (device_model.cuh layout)
 };
 
 FlatModel flatten_model(const ModelTables& mt);

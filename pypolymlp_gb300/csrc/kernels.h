@@ -27,7 +27,7 @@ struct RowItem {
     int a0;
 };
 
-constexpr int kRowsTR = 32;  // target atoms per pg_rows block
+constexpr int kRowsTR = 16;  // target atoms per pg_rows block
 
 void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st);
 void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, cudaStream_t st);

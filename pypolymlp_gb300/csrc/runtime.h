@@ -99,7 +99,7 @@ struct DeviceModel {
     int n_chunks = 0;
     int chunk_cap_ent = 0;    // max G entries of a chunk (shared-memory sizing)
     std::vector<DevBuf> bufs;
-    void build(const FlatModel& fm, int chunk_width);
+    void build(const FlatModel& fm, int max_chunk, bool fp64);
 };
 
 // Batch of structures staged on the device with neighbour lists and per-atom data.

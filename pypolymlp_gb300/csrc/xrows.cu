@@ -110,14 +110,21 @@ __global__ void pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const i
         (reinterpret_cast<uintptr_t>(sb + slot * nw) + 15) & ~uintptr_t(15));
     int* s_tp = reinterpret_cast<int*>(acc + ty.K0);
     int* s_ok = s_tp + nw;
+    T* s_tab = reinterpret_cast<T*>(s_ok + nw + 4);
+    s_tab = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_tab) + 15) & ~uintptr_t(15));
+    load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
+    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) acc[h] = make_double2(0.0, 0.0);
+    __syncthreads();
     const long long b = nb_off[i], e = nb_off[i + 1];
     for (long long base = b; base < e; base += nw) {
         const long long k = base + warp;
         BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
         if (k < e) {
             const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
-            const double dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            double dis = 0.0;
+            if (lane == 0) dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            dis = __shfl_sync(0xffffffffu, dis, 0);
             const bool ok = dis < M.cutoff;
             const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
             if (lane == 0) {
@@ -127,7 +134,7 @@ __global__ void pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const i
             if (ok) {
                 warp_radial<T, false>(M, tp, dis, bv, lane);
                 if (M.gtinv) {
-                    warp_ylm<T, false>(M.maxl, M.n_ylm, dx, dy, dz, dis, bv, lane);
+                    warp_ylm<T, false>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
                 } else if (lane == 0) {
                     bv.Y[0] = {(T)1, (T)0};
                 }
@@ -138,16 +145,20 @@ __global__ void pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const i
         __syncthreads();
         for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) {
             const int htp = ty.head_tp[h], nid = ty.head_nid[h], key = ty.head_key[h];
-            double2 a = acc[h];
+            // partial sum over this batch of pairs in T, added to the FP64 total
+            T px = 0, py = 0;
             for (int w = 0; w < nw; ++w) {
                 if (!s_ok[w] || s_tp[w] != htp) continue;
                 BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
                 const T f = v.fn[nid];
                 if (!(f >= (T)1e-20)) continue;
                 const cplx<T> y = v.Y[key];
-                a.x += (double)(f * y.re);
-                a.y += (double)(f * y.im);
+                px += f * y.re;
+                py += f * y.im;
             }
+            double2 a = acc[h];
+            a.x += (double)px;
+            a.y += (double)py;
             acc[h] = a;
         }
         __syncthreads();
@@ -230,41 +241,50 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
 
 // --------------------------------------------------------------- K5 rows
 template <typename T, int TR>
-__global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256, 1) pg_rows(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
                         const long long* d_off, const T* D, const long long* g_off, const cplx<T>* G,
                         const RowItem* items, const long long* f_row, int chunk_cap_ent, T* X, long long ld,
                         double* partial /* [item][7][F] */) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const RowItem it = items[blockIdx.x];
+    // grid: x = column chunk (fastest, so the chunks of one structure run together), y = work item
+    const RowItem it = items[blockIdx.y];
     const int CH = blockDim.x;
-    const int col = blockIdx.y * CH + threadIdx.x;
-    const bool col_ok = col < M.F;
+    const int c0 = blockIdx.x * CH;            // first column of this chunk
+    const int cq = c0 + threadIdx.x;
+    const bool col_ok = cq < M.F;              // position threadIdx.x of the chunk exists
     const int nw = CH >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = it.st;
     const int sa0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - sa0;
-    const int blk0 = it.a0;                 // local index of the first target atom
+    const int blk0 = it.a0;  // local index of the first target atom
     const bool force = f_row[s] >= 0;
+    const int ntp = M.n_tp;
 
-    // shared layout: out[TR*3][CH] | gval[cap] | gmeta[cap] | basis slots | slot info
+    // shared layout: out[TR*3][CH] | gval[cap] | gmeta[cap] | tpo[CH][ntp+1] | table | basis slots | slot info
     T* out = reinterpret_cast<T*>(smem_raw);
     cplx<T>* gval = reinterpret_cast<cplx<T>*>(out + (size_t)TR * 3 * CH);
     int* gmeta = reinterpret_cast<int*>(gval + chunk_cap_ent);
+    int* tpo = gmeta + chunk_cap_ent;
+    T* s_tab = reinterpret_cast<T*>(
+        (reinterpret_cast<uintptr_t>(tpo + (size_t)CH * (ntp + 1)) + 15) & ~uintptr_t(15));
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    T* sb = reinterpret_cast<T*>(gmeta + chunk_cap_ent + ((chunk_cap_ent & 1) ? 1 : 0));
-    // align sb to 8 bytes
-    sb = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sb) + 15) & ~uintptr_t(15));
-    double* sdx = reinterpret_cast<double*>(sb + slot * nw);
-    sdx = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(sdx) + 15) & ~uintptr_t(15));
-    double* sdy = sdx + nw;
-    double* sdz = sdy + nw;
-    double* sdis = sdz + nw;
+    T* sb = reinterpret_cast<T*>(
+        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));
+    T* sdx = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sb + slot * nw) + 15) & ~uintptr_t(15));
+    T* sdy = sdx + nw;
+    T* sdz = sdy + nw;
+    T* sdis = sdz + nw;
     int* stp = reinterpret_cast<int*>(sdis + nw);
     int* sj = stp + nw;
     int* sok = sj + nw;
+    // per-column energy and stress sums (FP64), indexed by column position in the chunk
+    double* cacc = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(sok + nw) + 15) & ~uintptr_t(15));
+    for (int q = threadIdx.x; q < 7 * CH; q += CH) cacc[q] = 0.0;
 
+    load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
+    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     for (int q = threadIdx.x; q < TR * 3 * CH; q += CH) out[q] = (T)0;
-    double energy = 0.0;
-    double st6[6] = {0, 0, 0, 0, 0, 0};
+    int* my_tpo = tpo + (size_t)threadIdx.x * (ntp + 1);
+    __syncthreads();
 
     for (int i = 0; i < n; ++i) {
         const int gi = sa0 + i;
@@ -272,39 +292,48 @@ __global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const i
         const DevType& ty = M.types[t1];
         const bool centre_in = (i >= blk0 && i < blk0 + TR);
         const T* Di = D + d_off[gi];
-        // --- polynomial-weighted adjoint of my column for centre i
-        int my_off = 0, my_cnt = 0;
-        if (col_ok) {
-            const int nc = ty.col_ncomp[col];
-            my_off = ty.col_ent_off[col];
-            if (nc > 0) {
-                if (centre_in) {
-                    T pe = (T)1;
-                    for (int c = 0; c < nc; ++c) pe *= Di[ty.comp_k[col * 3 + c]];
-                    energy += (double)pe;
+        // --- the column this thread takes for centres of type t1, and its adjoint, grouped by type pair
+        const int col = col_ok ? ty.col_perm[cq] : 0;
+        const int cpos = col - c0;
+        const int nc = col_ok ? ty.col_ncomp[col] : 0;
+        const int my_off = col_ok ? ty.col_ent_off[col] : 0;
+        if (nc > 0 && centre_in) {
+            T pe = (T)1;
+            for (int c = 0; c < nc; ++c) pe *= Di[ty.comp_k[col * 3 + c]];
+            cacc[cpos] += (double)pe;
+        }
+        if (!force) {
+            __syncthreads();  // the next centre may map this column to another thread
+            continue;
+        }
+        {
+            const cplx<T>* Gi = G + g_off[gi];
+            T wt[3];
+            int kk[3];
+            for (int c = 0; c < nc; ++c) {
+                kk[c] = ty.comp_k[col * 3 + c];
+                T w = (T)1;
+                for (int q = 0; q < 2; ++q) {
+                    const int o = ty.comp_w[(col * 3 + c) * 2 + q];
+                    if (o >= 0) w *= Di[o];
                 }
-                if (force) {
-                    const cplx<T>* Gi = G + g_off[gi];
-                    int w = my_off;
-                    for (int c = 0; c < nc; ++c) {
-                        const int k = ty.comp_k[col * 3 + c];
-                        T wt = (T)1;
-                        for (int q = 0; q < 2; ++q) {
-                            const int o = ty.comp_w[(col * 3 + c) * 2 + q];
-                            if (o >= 0) wt *= Di[o];
-                        }
-                        for (int e = ty.ent_off[k]; e < ty.ent_off[k + 1]; ++e) {
-                            const cplx<T> g = Gi[e];
-                            gval[w] = {wt * g.re, wt * g.im};
-                            gmeta[w] = ty.ent_meta[e];
-                            ++w;
-                        }
+                wt[c] = w;
+            }
+            int w = my_off;
+            for (int t = 0; t < ntp; ++t) {
+                my_tpo[t] = w;
+                for (int c = 0; c < nc; ++c) {
+                    const int* eo = ty.ent_tp_off + (size_t)kk[c] * (ntp + 1);
+                    for (int e = eo[t]; e < eo[t + 1]; ++e) {
+                        const cplx<T> g = Gi[e];
+                        gval[w] = {wt[c] * g.re, wt[c] * g.im};
+                        gmeta[w] = ty.ent_meta[e] >> 8;  // nid | key << 8
+                        ++w;
                     }
-                    my_cnt = w - my_off;
                 }
             }
+            my_tpo[ntp] = w;
         }
-        if (!force) continue;
         // --- pair images of centre i that touch this block
         long long pb = nb_off[gi], pe_ = nb_off[gi + 1];
         if (!centre_in) {
@@ -324,23 +353,27 @@ __global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const i
             pb = lo;
             pe_ = lo2;
         }
-        double self[3] = {0, 0, 0};
-        __syncthreads();  // gval/gmeta of centre i are complete
+        // sums over the pairs of this centre in T; added to the FP64 totals per centre
+        T self[3] = {0, 0, 0};
+        T cst[6] = {0, 0, 0, 0, 0, 0};
+        __syncthreads();  // gval/gmeta/tpo of centre i are complete
         for (long long base = pb; base < pe_; base += nw) {
             const long long k = base + warp;
             BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
             if (k < pe_) {
                 const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
-                const double dis =
-                    sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+                double dis = 0.0;
+                if (lane == 0)
+                    dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+                dis = __shfl_sync(0xffffffffu, dis, 0);
                 const bool ok = dis < M.cutoff;
                 const int j = nb_j[k];
                 const int tp = M.type_pairs[t1 * M.n_type + B.types[j]];
                 if (lane == 0) {
-                    sdx[warp] = dx;
-                    sdy[warp] = dy;
-                    sdz[warp] = dz;
-                    sdis[warp] = dis;
+                    sdx[warp] = (T)dx;
+                    sdy[warp] = (T)dy;
+                    sdz[warp] = (T)dz;
+                    sdis[warp] = (T)dis;
                     stp[warp] = tp;
                     sj[warp] = j - sa0;
                     sok[warp] = ok;
@@ -348,7 +381,7 @@ __global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const i
                 if (ok) {
                     warp_radial<T, true>(M, tp, dis, bv, lane);
                     if (M.gtinv) {
-                        warp_ylm<T, true>(M.maxl, M.n_ylm, dx, dy, dz, dis, bv, lane);
+                        warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
                     } else if (lane == 0) {
                         bv.Y[0] = {(T)1, (T)0};
                         bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
@@ -358,43 +391,44 @@ __global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const i
                 sok[warp] = 0;
             }
             __syncthreads();
-            if (col_ok && my_cnt > 0) {
-                for (int w = 0; w < nw; ++w) {
+            if (col_ok && nc > 0) {
+                const int nb = (int)min((long long)nw, pe_ - base);
+                for (int w = 0; w < nb; ++w) {
                     if (!sok[w]) continue;
                     const int tp = stp[w];
+                    const int e0 = my_tpo[tp], e1 = my_tpo[tp + 1];
+                    if (e0 == e1) continue;
                     BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
                     T s0 = 0, sx = 0, sy = 0, sz = 0;
-                    for (int q = 0; q < my_cnt; ++q) {
-                        const int meta = gmeta[my_off + q];
-                        if ((meta & 0xff) != tp) continue;
-                        const int nid = (meta >> 8) & 0xff, key = meta >> 16;
+                    for (int q = e0; q < e1; ++q) {
+                        const int meta = gmeta[q];
+                        const int nid = meta & 0xff, key = meta >> 8;
                         const T f = v.fn[nid];
-                        if (!(f >= (T)1e-20)) continue;
-                        const cplx<T> g = gval[my_off + q];
+                        const cplx<T> g = gval[q];
                         s0 += v.fnd[nid] * creal_mul(g, v.Y[key]);
                         sx += f * creal_mul(g, v.dY[key]);
                         sy += f * creal_mul(g, v.dY[M.n_ylm + key]);
                         sz += f * creal_mul(g, v.dY[2 * M.n_ylm + key]);
                     }
-                    const double dx = sdx[w], dy = sdy[w], dz = sdz[w];
-                    const T sc = s0 / (T)sdis[w];
-                    const T vx = sc * (T)dx + sx, vy = sc * (T)dy + sy, vz = sc * (T)dz + sz;
+                    const T dx = sdx[w], dy = sdy[w], dz = sdz[w];
+                    const T sc = s0 / sdis[w];
+                    const T vx = sc * dx + sx, vy = sc * dy + sy, vz = sc * dz + sz;
                     const int jl = sj[w];
                     if (centre_in) {
                         if (jl != i) {
-                            self[0] += (double)vx;
-                            self[1] += (double)vy;
-                            self[2] += (double)vz;
+                            self[0] += vx;
+                            self[1] += vy;
+                            self[2] += vz;
                         }
-                        st6[0] -= (double)vx * dx;
-                        st6[1] -= (double)vy * dy;
-                        st6[2] -= (double)vz * dz;
-                        st6[3] -= (double)vx * dy;
-                        st6[4] -= (double)vy * dz;
-                        st6[5] -= (double)vz * dx;
+                        cst[0] -= vx * dx;
+                        cst[1] -= vy * dy;
+                        cst[2] -= vz * dz;
+                        cst[3] -= vx * dy;
+                        cst[4] -= vy * dz;
+                        cst[5] -= vz * dx;
                     }
                     if (jl != i && jl >= blk0 && jl < blk0 + TR) {
-                        T* o = out + (size_t)(jl - blk0) * 3 * CH + threadIdx.x;
+                        T* o = out + (size_t)(jl - blk0) * 3 * CH + cpos;
                         o[0] -= vx;
                         o[CH] -= vy;
                         o[2 * CH] -= vz;
@@ -404,24 +438,25 @@ __global__ void pg_rows(DevModel M, DevBatch B, const long long* nb_off, const i
             __syncthreads();
         }
         if (centre_in && col_ok) {
-            T* o = out + (size_t)(i - blk0) * 3 * CH + threadIdx.x;
-            o[0] += (T)self[0];
-            o[CH] += (T)self[1];
-            o[2 * CH] += (T)self[2];
+            T* o = out + (size_t)(i - blk0) * 3 * CH + cpos;
+            o[0] += self[0];
+            o[CH] += self[1];
+            o[2 * CH] += self[2];
+            for (int q = 0; q < 6; ++q) cacc[(size_t)(q + 1) * CH + cpos] += (double)cst[q];
         }
         __syncthreads();  // before gval is rebuilt for the next centre
     }
     if (!col_ok) return;
+    // column positions are in natural order: thread q writes column c0 + q
     if (force) {
         const long long r0 = f_row[s];
         const int na = min(TR, n - blk0);
         for (int a = 0; a < na; ++a)
             for (int c = 0; c < 3; ++c)
-                X[(size_t)col * ld + r0 + 3 * (blk0 + a) + c] = out[(size_t)a * 3 * CH + c * CH + threadIdx.x];
+                X[(size_t)cq * ld + r0 + 3 * (blk0 + a) + c] = out[(size_t)a * 3 * CH + c * CH + threadIdx.x];
     }
-    double* p = partial + (size_t)blockIdx.x * 7 * M.F;
-    p[col] = energy;
-    for (int q = 0; q < 6; ++q) p[(size_t)(q + 1) * M.F + col] = st6[q];
+    double* p = partial + (size_t)blockIdx.y * 7 * M.F;
+    for (int q = 0; q < 7; ++q) p[(size_t)q * M.F + cq] = cacc[(size_t)q * CH + threadIdx.x];
 }
 
 // Sum the per-block energy/stress partials of each structure into X.
@@ -485,7 +520,8 @@ void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, 
                  const long long* a_off, double2* A, int max_k0, cudaStream_t st) {
     const int threads = 128, nw = threads / 32;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) + 2 * nw * sizeof(int);
+    const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) + (2 * nw + 4) * sizeof(int) +
+                        16 + ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
     PG_CUDA(cudaFuncSetAttribute(pg_anlm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pg_anlm<T><<<B.n_atoms, threads, smem, st>>>(M, B, nb_off, nb_j, nb_d, a_off, A);
 }
@@ -505,8 +541,9 @@ size_t rows_smem_bytes(const DevModel& M, int chunk, int cap_ent, bool fp64) {
     const int nw = chunk / 32;
     const size_t slot = fp64 ? basis_slot_elems<double>(M.n_fn_max, M.n_ylm, M.maxl)
                              : basis_slot_elems<float>(M.n_fn_max, M.n_ylm, M.maxl);
-    return (size_t)kRowsTR * 3 * chunk * ts + (size_t)cap_ent * (2 * ts + 4) + 32 + slot * nw * ts + 32 +
-           (size_t)nw * (4 * 8 + 3 * 4);
+    return (size_t)kRowsTR * 3 * chunk * ts + (size_t)cap_ent * (2 * ts + 4) + (size_t)chunk * (M.n_tp + 1) * 4 +
+           16 + (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts + 16 + slot * nw * ts + 16 +
+           (size_t)nw * (4 * 8 + 3 * 4) + 16 + (size_t)7 * chunk * 8;
 }
 
 template <typename T>
@@ -516,7 +553,7 @@ void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, 
                  double* partial, cudaStream_t st) {
     const size_t smem = rows_smem_bytes(M, chunk, cap_ent, sizeof(T) == 8);
     PG_CUDA(cudaFuncSetAttribute(pg_rows<T, kRowsTR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(n_items, n_chunks);
+    dim3 grid(n_chunks, n_items);
     pg_rows<T, kRowsTR><<<grid, chunk, smem, st>>>(M, B, nb_off, nb_j, nb_d, d_off, D, g_off,
                                                    reinterpret_cast<const cplx<T>*>(G), items, f_row, cap_ent, X,
                                                    ld, partial);

@@ -361,16 +361,27 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
     xtx /= scales[None, :]
     xty /= scales
     coefs, info = solver_ridge(xtx, xty, alphas)
+    # ridge objective of every alpha from residuals (FP64 sums): |r|^2 + alpha |c|^2
+    xtr, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
+    obj = sq.sum(axis=0) + alphas * np.square(coefs).sum(axis=0)
     for _ in range(refine):
-        xtr, _, _ = batch_residual(gram, tb, coefs / scales[:, None])
+        # refinement step, kept only where it lowers the objective: with a mixed
+        # Gram, (A + alpha I)^-1 dA can exceed 1 for small alpha and the plain
+        # iteration would diverge
         g = xtr / scales[:, None] - coefs * alphas[None, :]
         g[zero_ids] = 0.0
+        trial = coefs.copy()
         for k, a in enumerate(alphas):
-            if info[k] != 0:
-                continue
-            d, _ = solver_ridge(xtx, g[:, k], [a])
-            coefs[:, k] += d[:, 0]
-    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
+            if info[k] == 0:
+                d, _ = solver_ridge(xtx, g[:, k], [a])
+                trial[:, k] += d[:, 0]
+        xtr2, sq2, _ = batch_residual(gram, tb, trial / scales[:, None])
+        obj2 = sq2.sum(axis=0) + alphas * np.square(trial).sum(axis=0)
+        better = obj2 < obj
+        coefs[:, better] = trial[:, better]
+        xtr[:, better] = xtr2[:, better]
+        sq[:, better] = sq2[:, better]
+        obj[better] = obj2[better]
     rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
     if np.all(rmse_train > 1e6):
         raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
