@@ -192,3 +192,31 @@ def profile_read():
         out[raw[pos:end].decode()] = (float(ms[k]), int(launches[k]))
         pos = end + 1
     return out
+
+
+class Evaluator:
+    """Handle of pg_eval: energies, forces and stresses of structures on the GPU."""
+
+    def __init__(self, params_dict: dict, coeffs, precision: int = PG_FP64):
+        require_device()
+        self.fp = FeatureParams(params_dict)
+        self.coeffs = np.ascontiguousarray(coeffs, dtype=np.float64).reshape(-1)
+        h = _vp()
+        check(lib().pg_eval_create(C.cast(self.fp.ref(), _vp), _p(self.coeffs, C.c_double), len(self.coeffs),
+                                   int(precision), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.pg_eval_destroy(h)
+            self._h = None
+
+    def run(self, st: Structures):
+        """(energy (n_st,), forces (sum N, 3) atom-major, stress (n_st, 6))."""
+        e = np.zeros(st.n_st)
+        f = np.zeros((int(st.n_atoms.sum()), 3))
+        s = np.zeros((st.n_st, 6))
+        check(lib().pg_eval_run(self._h, C.cast(st.ref(), _vp), _p(e, C.c_double), _p(f, C.c_double),
+                                _p(s, C.c_double)))
+        return e, f, s

@@ -1,1 +1,429 @@
-// placeholder
+// Energy / force / stress evaluation on the GPU (PotentialPropertiesFast,
+// src/pypolymlp/cxx/src/compute/py_properties_fast.cpp:19-77, PolymlpEval,
+// src/pypolymlp/cxx/src/compute/polymlp_eval.cpp:24-403).
+//
+// The reference already evaluates by an adjoint: per atom it forms
+// prod_sum = dE_i/da_nlm (polymlp_potential.cpp:235-295) and contracts it with
+// da/dr per half-list pair.  Here, per atom i (full neighbour list):
+//   pg_anlm            a_nlm (m <= 0), FP64 neighbour sums           (xrows.cu)
+//   pg_eval_adjoint    features d, beta_k = dE_i/dd_k from the polynomial with
+//                      the coefficients, E_i, and the folded adjoint
+//                      A_i[h] = sum_e beta_k(e) G_e (no G stored)
+//   pg_eval_pairs      per pair image p = (i -> j, d): g_p = Re(A_i . dphi(d)/dd),
+//                      one warp per pair with the shared pair basis
+//   pg_eval_mirror     index of the mirror image (j -> i, -d) of every pair
+//                      (exact: -d is bit-identical)
+//   pg_eval_gather     F_b = sum_{q in list(b)} (g_q - g_mirror(q))   (no atomics)
+//   pg_eval_reduce     E = sum_i E_i and stress = -sum_p d_p (x) g_p per structure
+// Energies match the reference's Euler-split pair sums, and forces/stress its
+// half-list collection, up to summation order.
+#include <cuda_runtime.h>
+
+#include <memory>
+
+#include "kernels.h"
+#include "model.h"
+
+namespace pg {
+
+// Extra per-type device tables of the evaluator.
+struct EvalType {
+    const int *ent_k, *head_ent_off, *head_ent, *tp_head_off, *tp_heads;
+    const int *kcol_off, *kcol_col, *kcol_o1, *kcol_o2;
+};
+
+struct EvalTables {
+    EvalType types[kMaxTypes];
+};
+
+// One block per atom.
+template <typename T>
+__global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, const long long* a_off,
+                                const double2* Anoconj, const double* coef, cplx<T>* Aout, double* Eatom) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int i = blockIdx.x;
+    const int t1 = types[i];
+    const DevType& ty = M.types[t1];
+    const EvalType& et = ET.types[t1];
+    cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw);
+    T* d = reinterpret_cast<T*>(a + ty.K);
+    T* beta = d + ty.n_lin;
+    __shared__ double red[32];
+    const double2* Ai = Anoconj + a_off[i];
+    for (int f = threadIdx.x; f < ty.K; f += blockDim.x) {
+        const double2 s = Ai[ty.full_src[f]];
+        if (ty.full_is_conj[f]) {
+            const double cc = ty.full_cc[f];
+            a[f] = {(T)(cc * s.x), (T)(-cc * s.y)};
+        } else {
+            a[f] = {(T)s.x, (T)s.y};
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
+        T v = 0;
+        for (int q = ty.val_off[k]; q < ty.val_off[k + 1]; ++q) {
+            const FlatTerm& t = ty.val_terms[q];
+            v += (T)t.coeff * term_product_real<T>(t, a);
+        }
+        d[k] = v;
+    }
+    __syncthreads();
+    // beta_k = sum over polynomial columns containing k of coef * product of the others
+    for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
+        T b = 0;
+        for (int q = et.kcol_off[k]; q < et.kcol_off[k + 1]; ++q) {
+            T w = (T)coef[et.kcol_col[q]];
+            const int o1 = et.kcol_o1[q], o2 = et.kcol_o2[q];
+            if (o1 >= 0) w *= d[o1];
+            if (o2 >= 0) w *= d[o2];
+            b += w;
+        }
+        beta[k] = b;
+    }
+    // E_i = sum over columns of coef * polynomial value (FP64 block sum)
+    double e = 0.0;
+    for (int col = threadIdx.x; col < M.F; col += blockDim.x) {
+        const int nc = ty.col_ncomp[col];
+        if (nc == 0) continue;
+        T p = (T)1;
+        for (int c = 0; c < nc; ++c) p *= d[ty.comp_k[col * 3 + c]];
+        e += coef[col] * (double)p;
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        Eatom[i] = s;
+    }
+    // A[h] = sum over entries with head h of beta_k(e) G_e
+    cplx<T>* Ao = Aout + a_off[i];
+    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) {
+        const T cc = (ty.head_m[h] & 1) ? (T)-1 : (T)1;
+        T re = 0, im = 0;
+        for (int q = et.head_ent_off[h]; q < et.head_ent_off[h + 1]; ++q) {
+            const int ent = et.head_ent[q];
+            const T b = beta[et.ent_k[ent]];
+            for (int u = ty.term_off[ent]; u < ty.term_off[ent + 1]; ++u) {
+                const FlatTerm& t = ty.g_terms[u];
+                const cplx<T> p = term_product<T>(t, a);
+                const T c = b * (T)t.coeff;
+                if (t.conj) {
+                    re += cc * c * p.re;
+                    im -= cc * c * p.im;
+                } else {
+                    re += c * p.re;
+                    im += c * p.im;
+                }
+            }
+        }
+        Ao[h] = {re, im};
+    }
+}
+
+// One block per centre atom; warps take its pair images.
+template <typename T>
+__global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long long* nb_off, const int* nb_j,
+                              const double* nb_d, const long long* a_off, const cplx<T>* Aadj, double* g_out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int i = blockIdx.x;
+    const int t1 = B.types[i];
+    const DevType& ty = M.types[t1];
+    const EvalType& et = ET.types[t1];
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    cplx<T>* A = reinterpret_cast<cplx<T>*>(smem_raw);
+    T* s_tab = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(A + ty.K0) + 15) & ~uintptr_t(15));
+    const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
+    T* sb = reinterpret_cast<T*>(
+        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));
+    const cplx<T>* Ai = Aadj + a_off[i];
+    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) A[h] = Ai[h];
+    load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
+    __syncthreads();
+    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
+    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
+    for (long long k = nb_off[i] + warp; k < nb_off[i + 1]; k += nw) {
+        const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
+        double dis = 0.0;
+        if (lane == 0) dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+        dis = __shfl_sync(0xffffffffu, dis, 0);
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        if (dis < M.cutoff) {
+            const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
+            warp_radial<T, true>(M, tp, dis, bv, lane);
+            if (M.gtinv) {
+                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
+            } else if (lane == 0) {
+                bv.Y[0] = {(T)1, (T)0};
+                bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
+            }
+            __syncwarp();
+            T s0 = 0, sx = 0, sy = 0, sz = 0;
+            for (int q = et.tp_head_off[tp] + lane; q < et.tp_head_off[tp + 1]; q += 32) {
+                const int h = et.tp_heads[q];
+                const int nid = ty.head_nid[h], key = ty.head_key[h];
+                const cplx<T> g = A[h];
+                const T f = bv.fn[nid];
+                s0 += bv.fnd[nid] * creal_mul(g, bv.Y[key]);
+                sx += f * creal_mul(g, bv.dY[key]);
+                sy += f * creal_mul(g, bv.dY[M.n_ylm + key]);
+                sz += f * creal_mul(g, bv.dY[2 * M.n_ylm + key]);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                s0 += __shfl_down_sync(0xffffffffu, s0, o);
+                sx += __shfl_down_sync(0xffffffffu, sx, o);
+                sy += __shfl_down_sync(0xffffffffu, sy, o);
+                sz += __shfl_down_sync(0xffffffffu, sz, o);
+            }
+            const T sc = s0 / (T)dis;
+            gx = (double)(sc * (T)dx + sx);
+            gy = (double)(sc * (T)dy + sy);
+            gz = (double)(sc * (T)dz + sz);
+        }
+        if (lane == 0) {
+            g_out[3 * k] = gx;
+            g_out[3 * k + 1] = gy;
+            g_out[3 * k + 2] = gz;
+        }
+        __syncwarp();
+    }
+}
+
+// Mirror of every pair: entry (b -> a, d) pairs with (a -> b, -d).  One warp per atom.
+__global__ void pg_eval_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d,
+                               long long* mirror, int* missing) {
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= n_atoms) return;
+    for (long long q = nb_off[b] + lane; q < nb_off[b + 1]; q += 32) {
+        const int a = nb_j[q];
+        const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
+        long long lo = nb_off[a], hi = nb_off[a + 1];
+        while (lo < hi) {
+            const long long mid = (lo + hi) >> 1;
+            if (nb_j[mid] < b) lo = mid + 1;
+            else hi = mid;
+        }
+        long long m = -1;
+        for (long long p = lo; p < nb_off[a + 1] && nb_j[p] == b; ++p)
+            if (nb_d[3 * p] == -dx && nb_d[3 * p + 1] == -dy && nb_d[3 * p + 2] == -dz) {
+                m = p;
+                break;
+            }
+        mirror[q] = m;
+        if (m < 0) atomicAdd(missing, 1);
+    }
+}
+
+// F_b = sum_{q in list(b)} (g_q - g_mirror(q)); one thread per atom, FP64.
+__global__ void pg_eval_gather(int n_atoms, const long long* nb_off, const long long* mirror, const double* g,
+                               double* forces) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_atoms) return;
+    double f[3] = {0, 0, 0};
+    for (long long q = nb_off[b]; q < nb_off[b + 1]; ++q) {
+        const long long m = mirror[q];
+        for (int c = 0; c < 3; ++c) f[c] += g[3 * q + c] - (m >= 0 ? g[3 * m + c] : 0.0);
+    }
+    for (int c = 0; c < 3; ++c) forces[3 * (size_t)b + c] = f[c];
+}
+
+// Per structure: E = sum_i E_i and stress = -sum_p d_p (x) g_p over the full list
+// (xx yy zz xy yz zx, with xy = -d_x g_y): the half-list sum of
+// polymlp_eval.cpp:293-336, whose pair force is -(g_ij - g_ji), written per
+// directed pair.
+__global__ void pg_eval_reduce(const int* st_atom_off, const long long* nb_off, const double* nb_d,
+                               const double* g, const double* Eatom, double* energy, double* stress) {
+    const int s = blockIdx.x;
+    const int a0 = st_atom_off[s], a1 = st_atom_off[s + 1];
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) acc[0] += Eatom[a];
+    for (long long p = nb_off[a0] + threadIdx.x; p < nb_off[a1]; p += blockDim.x) {
+        const double gx = g[3 * p], gy = g[3 * p + 1], gz = g[3 * p + 2];
+        const double dx = nb_d[3 * p], dy = nb_d[3 * p + 1], dz = nb_d[3 * p + 2];
+        acc[1] -= dx * gx;
+        acc[2] -= dy * gy;
+        acc[3] -= dz * gz;
+        acc[4] -= dx * gy;
+        acc[5] -= dy * gz;
+        acc[6] -= dz * gx;
+    }
+    __shared__ double red[7][256];
+    for (int q = 0; q < 7; ++q) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 7; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        energy[s] = red[0][0];
+        for (int q = 0; q < 6; ++q) stress[6 * s + q] = red[q + 1][0];
+    }
+}
+
+struct Evaluator {
+    std::unique_ptr<Model> m;
+    int precision;
+    DevBuf coef;
+    std::vector<DevBuf> bufs;
+    EvalTables et{};
+    DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_g, s_mirror, s_missing, d_E, d_S, d_F;
+    cudaStream_t stream = 0;
+
+    Evaluator(const pg_feature_params* fp, const double* coeffs, int n, int prec) : precision(prec) {
+        m = std::make_unique<Model>(fp);
+        if (n != m->flat.n_features) throw std::runtime_error("coefficient count does not match the model");
+        upload(coef, std::vector<double>(coeffs, coeffs + n));
+        bufs.reserve(16 * kMaxTypes);
+        auto up = [&](const std::vector<int>& v) -> const int* {
+            bufs.emplace_back();
+            upload(bufs.back(), v);
+            return bufs.back().as<int>();
+        };
+        for (int t = 0; t < m->flat.n_type; ++t) {
+            const FlatType& ft = m->flat.types[t];
+            EvalType& e = et.types[t];
+            e.ent_k = up(ft.ent_k);
+            e.head_ent_off = up(ft.head_ent_off);
+            e.head_ent = up(ft.head_ent);
+            e.tp_head_off = up(ft.tp_head_off);
+            e.tp_heads = up(ft.tp_heads);
+            e.kcol_off = up(ft.kcol_off);
+            e.kcol_col = up(ft.kcol_col);
+            e.kcol_o1 = up(ft.kcol_o1);
+            e.kcol_o2 = up(ft.kcol_o2);
+        }
+    }
+
+    template <typename T>
+    void run_batch(DeviceBatch& b, double* energy, double* forces, double* stress) {
+        const DeviceModel& dmod = sizeof(T) == 8 ? m->dev64 : m->dev32;
+        const DevModel& M = dmod.dm;
+        b.build_neighbors(m->flat.cutoff, stream);
+        const DevBatch B = b.view(m->flat.cutoff);
+        std::vector<long long> a_off, d_off, g_off;
+        long long a_tot, d_tot, g_tot;
+        m->atom_offsets(b, 0, a_off, d_off, g_off, a_tot, d_tot, g_tot);
+        upload(d_aoff, a_off);
+        s_Anc.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
+        s_Aadj.reserve(2 * sizeof(T) * std::max<long long>(1, a_tot));
+        s_E.reserve(sizeof(double) * std::max(1, b.n_atoms));
+        s_g.reserve(sizeof(double) * 3 * std::max<long long>(1, b.n_pairs));
+        s_mirror.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
+        s_missing.reserve(sizeof(int));
+        d_E.reserve(sizeof(double) * std::max(1, b.n_st));
+        d_S.reserve(sizeof(double) * 6 * std::max(1, b.n_st));
+        d_F.reserve(sizeof(double) * 3 * std::max(1, b.n_atoms));
+        PG_CUDA(cudaMemsetAsync(s_missing.as<void>(), 0, sizeof(int), stream));
+        if (b.n_atoms > 0) {
+            {
+                ProfScope ps("pg_anlm", stream);
+                launch_anlm<T>(M, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                               d_aoff.as<long long>(), s_Anc.as<double2>(), m->max_k0, stream);
+            }
+            int max_lin = 1;
+            for (const auto& ft : m->flat.types) max_lin = std::max(max_lin, ft.n_lin);
+            const size_t sm1 = (size_t)m->max_k * 2 * sizeof(T) + 2 * (size_t)max_lin * sizeof(T) + 16;
+            PG_CUDA(cudaFuncSetAttribute(pg_eval_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1));
+            {
+                ProfScope ps("pg_eval_adjoint", stream);
+                pg_eval_adjoint<T><<<b.n_atoms, 256, sm1, stream>>>(M, et, d_types(b), d_aoff.as<long long>(),
+                                                                   s_Anc.as<double2>(), coef.as<double>(),
+                                                                   reinterpret_cast<cplx<T>*>(s_Aadj.as<void>()),
+                                                                   s_E.as<double>());
+            }
+            const int threads = 256, nw = threads / 32;
+            const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
+            const size_t sm2 = (size_t)m->max_k0 * 2 * sizeof(T) + 16 +
+                               (size_t)ylm_table_size(M.n_ylm, M.maxl) * sizeof(T) + 16 + slot * nw * sizeof(T);
+            PG_CUDA(cudaFuncSetAttribute(pg_eval_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+            {
+                ProfScope ps("pg_eval_pairs", stream);
+                pg_eval_pairs<T><<<b.n_atoms, threads, sm2, stream>>>(
+                    M, et, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                    d_aoff.as<long long>(), reinterpret_cast<const cplx<T>*>(s_Aadj.as<void>()), s_g.as<double>());
+            }
+            {
+                ProfScope ps("pg_eval_mirror", stream);
+                pg_eval_mirror<<<(b.n_atoms * 32 + 255) / 256, 256, 0, stream>>>(
+                    b.n_atoms, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                    s_mirror.as<long long>(), s_missing.as<int>());
+            }
+            {
+                ProfScope ps("pg_eval_gather", stream);
+                pg_eval_gather<<<(b.n_atoms + 127) / 128, 128, 0, stream>>>(
+                    b.n_atoms, b.d_nb_off.as<long long>(), s_mirror.as<long long>(), s_g.as<double>(),
+                    d_F.as<double>());
+            }
+            ProfScope ps("pg_eval_reduce", stream);
+            pg_eval_reduce<<<b.n_st, 256, 0, stream>>>(b.d_st_atom_off.as<int>(), b.d_nb_off.as<long long>(),
+                                                       b.d_nb_d.as<double>(), s_g.as<double>(), s_E.as<double>(),
+                                                       d_E.as<double>(), d_S.as<double>());
+        } else {
+            PG_CUDA(cudaMemsetAsync(d_E.as<void>(), 0, sizeof(double) * b.n_st, stream));
+            PG_CUDA(cudaMemsetAsync(d_S.as<void>(), 0, sizeof(double) * 6 * b.n_st, stream));
+        }
+        PG_CUDA(cudaGetLastError());
+        int missing = 0;
+        PG_CUDA(cudaMemcpyAsync(&missing, s_missing.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, stream));
+        PG_CUDA(cudaMemcpyAsync(energy, d_E.as<double>(), sizeof(double) * b.n_st, cudaMemcpyDeviceToHost, stream));
+        PG_CUDA(cudaMemcpyAsync(stress, d_S.as<double>(), sizeof(double) * 6 * b.n_st, cudaMemcpyDeviceToHost, stream));
+        if (b.n_atoms > 0)
+            PG_CUDA(cudaMemcpyAsync(forces, d_F.as<double>(), sizeof(double) * 3 * b.n_atoms, cudaMemcpyDeviceToHost,
+                                    stream));
+        PG_CUDA(cudaStreamSynchronize(stream));
+        if (missing) throw std::runtime_error("internal: neighbour list is not symmetric");
+    }
+
+    static const int* d_types(const DeviceBatch& b) { return b.d_types.as<int>(); }
+};
+
+}  // namespace pg
+
+using namespace pg;
+
+struct pg_eval {
+    std::unique_ptr<Evaluator> e;
+};
+
+extern "C" {
+
+int pg_eval_create(const pg_feature_params* fp, const double* coeffs, int n_coeffs, int precision, pg_eval** out) {
+    return guarded([&] {
+        if (!fp || !coeffs || !out) throw std::runtime_error("null argument");
+        if (precision != PG_FP64 && precision != PG_MIXED) throw std::runtime_error("unknown precision");
+        auto h = new pg_eval;
+        try {
+            h->e = std::make_unique<Evaluator>(fp, coeffs, n_coeffs, precision);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int pg_eval_destroy(pg_eval* e) {
+    return guarded([&] { delete e; });
+}
+
+int pg_eval_run(pg_eval* eh, const pg_structures* st, double* energy, double* forces, double* stress) {
+    return guarded([&] {
+        if (!eh || !st || !energy || !forces || !stress) throw std::runtime_error("null argument");
+        Evaluator& ev = *eh->e;
+        const bool fp64 = ev.precision == PG_FP64;
+        DeviceBatch b;
+        long long a = 0;
+        for (const auto& bt : ev.m->plan_batches(st, fp64, device_budget_bytes())) {
+            b.upload_structures(st, bt.first, bt.second, ev.m->flat.cutoff);
+            if (fp64) ev.run_batch<double>(b, energy + bt.first, forces + 3 * a, stress + 6 * bt.first);
+            else ev.run_batch<float>(b, energy + bt.first, forces + 3 * a, stress + 6 * bt.first);
+            a += b.n_atoms;
+        }
+    });
+}
+
+}  // extern "C"

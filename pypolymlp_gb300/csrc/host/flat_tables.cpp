@@ -2,6 +2,7 @@
 #include "flat_tables.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <map>
 #include <stdexcept>
@@ -155,6 +156,43 @@ FlatModel flatten_model(const ModelTables& mt) {
             }
         }
         for (int c = 0; c < F; ++c) fm.max_nent_col = std::max(fm.max_nent_col, ft.col_nent[c]);
+        // evaluator tables: entry -> feature, head -> entries, type pair -> heads, feature -> columns
+        ft.ent_k.assign(ft.ent_head.size(), 0);
+        for (int k = 0; k < ft.n_lin; ++k)
+            for (int e = ft.ent_off[k]; e < ft.ent_off[k + 1]; ++e) ft.ent_k[e] = k;
+        std::vector<std::vector<int>> by_head(ft.K0);
+        for (size_t e = 0; e < ft.ent_head.size(); ++e) by_head[ft.ent_head[e]].push_back((int)e);
+        ft.head_ent_off.assign(1, 0);
+        for (const auto& v : by_head) {
+            ft.head_ent.insert(ft.head_ent.end(), v.begin(), v.end());
+            ft.head_ent_off.push_back((int)ft.head_ent.size());
+        }
+        ft.tp_head_off.assign(1, 0);
+        for (int tp = 0; tp < mt.n_type_pairs; ++tp) {
+            for (int h = 0; h < ft.K0; ++h)
+                if (ft.head_tp[h] == tp) ft.tp_heads.push_back(h);
+            ft.tp_head_off.push_back((int)ft.tp_heads.size());
+        }
+        std::vector<std::vector<std::array<int, 3>>> kc(ft.n_lin);
+        for (const auto& p : tt.poly) {
+            const int n = (int)p.local_ids.size();
+            for (int c = 0; c < n; ++c) {
+                std::array<int, 3> r{p.col, -1, -1};
+                int q = 1;
+                for (int o = 0; o < n; ++o)
+                    if (o != c) r[q++] = p.local_ids[o];
+                kc[p.local_ids[c]].push_back(r);
+            }
+        }
+        ft.kcol_off.assign(1, 0);
+        for (const auto& v : kc) {
+            for (const auto& r : v) {
+                ft.kcol_col.push_back(r[0]);
+                ft.kcol_o1.push_back(r[1]);
+                ft.kcol_o2.push_back(r[2]);
+            }
+            ft.kcol_off.push_back((int)ft.kcol_col.size());
+        }
     }
     // Legendre / Y_lm constants, computed in IEEE double with the reference's
     // expressions (polymlp_spherical_harmonics.cpp:95-196).

@@ -47,7 +47,13 @@ struct FlatType {
     std::vector<int> col_ncomp, comp_k, comp_w;
     // per column: number of G entries (sum over its components), for smem sizing
     std::vector<int> col_nent;
-    // evaluator: per head, the potential terms grouped (CSR) - built separately
+    // evaluator tables
+    std::vector<int> ent_k;                 // linear feature of each G entry
+    std::vector<int> head_ent_off, head_ent; // per head (K0): entries with that head (CSR)
+    std::vector<int> tp_head_off, tp_heads;  // per type pair: heads of that pair (CSR)
+    // per linear feature k: polynomial columns containing it (CSR): column and the
+    // (up to two) other features whose product weights d(col)/d(d_k); -1 = none
+    std::vector<int> kcol_off, kcol_col, kcol_o1, kcol_o2;
 };
 
 struct FlatModel {

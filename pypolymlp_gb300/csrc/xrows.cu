@@ -169,28 +169,6 @@ __global__ void pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const i
 
 // ----------------------------------------------- K4 features and adjoint G
 template <typename T>
-__device__ inline cplx<T> term_product(const FlatTerm& t, const cplx<T>* a) {
-    if (t.n == 0) return {(T)1, (T)0};
-    cplx<T> v = a[t.ids[0]];
-    for (int q = 1; q < t.n; ++q) v = cmul(v, a[t.ids[q]]);
-    return v;
-}
-
-// Re(prod a[ids]) in the reference's association (polymlp_products.cpp:21-37).
-template <typename T>
-__device__ inline T term_product_real(const FlatTerm& t, const cplx<T>* a) {
-    const int n = t.n;
-    if (n == 0) return (T)1;
-    if (n == 1) return a[t.ids[0]].re;
-    if (n == 2) return creal_mul(a[t.ids[0]], a[t.ids[1]]);
-    if (n == 3) return creal_mul(cmul(a[t.ids[0]], a[t.ids[1]]), a[t.ids[2]]);
-    if (n == 4) return creal_mul(cmul(cmul(a[t.ids[1]], a[t.ids[2]]), a[t.ids[3]]), a[t.ids[0]]);
-    cplx<T> v = a[t.ids[1]];
-    for (int q = 2; q < n; ++q) v = cmul(v, a[t.ids[q]]);
-    return creal_mul(v, a[t.ids[0]]);
-}
-
-template <typename T>
 __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_off, const double2* A,
                                     const long long* d_off, T* D, const long long* g_off, cplx<T>* G) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
