@@ -2,6 +2,7 @@
 // creation, X rows, neighbour lists.  The regression assembly, solver and
 // evaluator entry points live in gram.cu, solve.cu and eval.cu.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <map>
@@ -44,7 +45,7 @@ ProfScope::~ProfScope() {
 }
 
 // ------------------------------------------------------------ DeviceModel
-void DeviceModel::build(const FlatModel& fm, int max_chunk, bool fp64) {
+void DeviceModel::build(const FlatModel& fm, size_t smem_target, bool fp64) {
     if (fm.n_type > kMaxTypes) throw std::runtime_error("at most 8 atom types are supported on the device");
     bufs.clear();
     bufs.reserve(64 * kMaxTypes);
@@ -62,60 +63,38 @@ void DeviceModel::build(const FlatModel& fm, int max_chunk, bool fp64) {
     dm.n_ylm = fm.n_ylm;
     dm.gtinv = fm.gtinv ? 1 : 0;
     dm.cutoff = fm.cutoff;
-    // Column chunks: balanced widths (multiples of 32, at most max_chunk) whose
-    // shared-memory footprint, which grows with the G entries of a chunk, fits.
+    dm.max_k0 = dm.max_lin = dm.max_k0tp = 1;
+    for (const auto& ft : fm.types) {
+        dm.max_k0 = std::max(dm.max_k0, ft.K0);
+        dm.max_lin = std::max(dm.max_lin, ft.n_lin);
+        for (int tp = 0; tp < fm.n_tp; ++tp)
+            dm.max_k0tp = std::max(dm.max_k0tp, ft.tp_head_off[tp + 1] - ft.tp_head_off[tp]);
+    }
     const int F = fm.n_features;
-    auto cap_for = [&](int ch) {
-        int cap = 1;
-        for (const auto& ft : fm.types)
-            for (int c0 = 0; c0 < F; c0 += ch) {
-                int acc = 0;
-                for (int c = c0; c < std::min(F, c0 + ch); ++c) acc += ft.col_nent[c];
-                cap = std::max(cap, acc);
-            }
-        return cap;
-    };
+    // pg_rows block shape: all columns in one block when they fit, with as many
+    // target atoms (up to 4) as the shared-memory target allows; otherwise one
+    // target atom and balanced column chunks within the 227 KB limit.
     const size_t smem_limit = 227 * 1024;
-    int nch = (F + max_chunk - 1) / max_chunk;
-    for (;; ++nch) {
-        int ch = (F + nch - 1) / nch;
-        ch = (ch + 31) / 32 * 32;
-        const int cap = cap_for(ch);
-        if (rows_smem_bytes(dm, ch, cap, fp64) <= smem_limit || ch <= 32) {
-            chunk = ch;
-            chunk_cap_ent = cap;
+    rows_tr = 0;
+    for (int tr : {4, 2, 1})
+        if (rows_smem_bytes(dm, tr, F, fp64) <= smem_target) {
+            rows_tr = tr;
             break;
         }
-    }
-    if (rows_smem_bytes(dm, chunk, chunk_cap_ent, fp64) > smem_limit)
-        throw std::runtime_error("model too large for the pg_rows shared-memory layout");
-    n_chunks = (F + chunk - 1) / chunk;
-    // Per centre type, the threads of a chunk take its columns in order of their
-    // adjoint-entry signature (which type pairs have entries, then how many), so
-    // the lanes of a warp mostly share the same loop length for a given pair.
-    std::vector<std::vector<int>> perm(fm.n_type, std::vector<int>(F));
-    for (int t = 0; t < fm.n_type; ++t) {
-        const FlatType& ft = fm.types[t];
-        for (int c0 = 0; c0 < F; c0 += chunk) {
-            const int c1 = std::min(F, c0 + chunk);
-            std::vector<std::pair<std::vector<int>, int>> key;
-            for (int c = c0; c < c1; ++c) {
-                std::vector<int> cnt(fm.n_tp, 0);
-                for (int q = 0; q < ft.col_ncomp[c]; ++q) {
-                    const int k = ft.comp_k[(size_t)c * 3 + q];
-                    for (int tp = 0; tp < fm.n_tp; ++tp)
-                        cnt[tp] += ft.ent_tp_off[(size_t)k * (fm.n_tp + 1) + tp + 1] -
-                                   ft.ent_tp_off[(size_t)k * (fm.n_tp + 1) + tp];
-                }
-                std::vector<int> k2;
-                for (int tp = 0; tp < fm.n_tp; ++tp) k2.push_back(cnt[tp] > 0 ? 0 : 1);
-                for (int tp = 0; tp < fm.n_tp; ++tp) k2.push_back(-cnt[tp]);
-                key.push_back({k2, c});
-            }
-            std::stable_sort(key.begin(), key.end());
-            for (int q = 0; q < c1 - c0; ++q) perm[t][c0 + q] = key[q].second;
+    if (rows_tr > 0) {
+        chunk = F;
+    } else {
+        rows_tr = 1;
+        for (int nch = 1;; ++nch) {
+            chunk = (F + nch - 1) / nch;
+            if (rows_smem_bytes(dm, 1, chunk, fp64) <= smem_limit) break;
+            if (chunk <= 32) throw std::runtime_error("model too large for the pg_rows shared-memory layout");
         }
     }
+    n_chunks = (F + chunk - 1) / chunk;
+    if (rows_pairs_smem_bytes(dm, fp64) > smem_limit)
+        throw std::runtime_error("model too large for the pg_rows_pairs shared-memory layout");
+    if (fm.n_tp > kMaxTypePairs) throw std::runtime_error("at most 64 type pairs are supported");
     dm.type_pairs = (const int*)up(fm.type_pairs);
     dm.tp_nfn = (const int*)up(fm.tp_nfn);
     dm.tp_beta = (const double*)up(fm.tp_beta);
@@ -146,28 +125,37 @@ void DeviceModel::build(const FlatModel& fm, int max_chunk, bool fp64) {
         d.g_terms = (const FlatTerm*)up(ft.g_terms);
         d.col_ncomp = (const int*)up(ft.col_ncomp);
         d.comp_k = (const int*)up(ft.comp_k);
-        d.comp_w = (const int*)up(ft.comp_w);
-        d.col_nent = (const int*)up(ft.col_nent);
-        std::vector<int> coff(F, 0);
-        for (int c0 = 0; c0 < F; c0 += chunk) {
-            int acc = 0;
-            for (int q = c0; q < std::min(F, c0 + chunk); ++q) {
-                const int c = perm[t][q];
-                coff[c] = acc;
-                acc += ft.col_nent[c];
-            }
+        std::vector<int4> info(F);
+        for (int c = 0; c < F; ++c) {
+            const int nc = ft.col_ncomp[c];
+            if (nc > 3) throw std::runtime_error("polynomial order above 3 is not supported");
+            int k[3] = {0, 0, 0};
+            for (int q = 0; q < nc; ++q) k[q] = ft.comp_k[(size_t)c * 3 + q];
+            info[c] = make_int4(k[0], k[1], k[2], nc);
         }
-        d.col_perm = (const int*)up(perm[t]);
-        d.col_ent_off = (const int*)up(coff);
-        std::vector<int> meta(ft.ent_head.size());
+        d.col_info = (const int4*)up(info);
+        d.ent_tp_off = (const int*)up(ft.ent_tp_off);
+        std::vector<int> nk(ft.ent_head.size());
         for (size_t e = 0; e < ft.ent_head.size(); ++e) {
             const int h = ft.ent_head[e];
-            if (ft.head_tp[h] > 255 || ft.head_nid[h] > 255 || ft.head_key[h] > 32767)
-                throw std::runtime_error("model too large for the packed entry metadata");
-            meta[e] = ft.head_tp[h] | (ft.head_nid[h] << 8) | (ft.head_key[h] << 16);
+            if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
+                throw std::runtime_error("model too large for the packed entry indices");
+            nk[e] = ft.head_nid[h] | (ft.head_key[h] << 8);
         }
-        d.ent_meta = (const int*)up(meta);
-        d.ent_tp_off = (const int*)up(ft.ent_tp_off);
+        d.ent_nk = (const int*)up(nk);
+        std::vector<int> hpos(ft.K0, -1), tnk(ft.tp_heads.size());
+        for (int tp = 0; tp < fm.n_tp; ++tp)
+            for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q) {
+                const int h = ft.tp_heads[q];
+                hpos[h] = q - ft.tp_head_off[tp];
+                tnk[q] = ft.head_nid[h] | (ft.head_key[h] << 8);
+            }
+        std::vector<int> ehpos(ft.ent_head.size());
+        for (size_t e = 0; e < ft.ent_head.size(); ++e) ehpos[e] = hpos[ft.ent_head[e]];
+        d.tp_head_nk = (const int*)up(tnk);
+        d.ent_hpos = (const int*)up(ehpos);
+        d.tp_head_off = (const int*)up(ft.tp_head_off);
+        d.tp_heads = (const int*)up(ft.tp_heads);
     }
 }
 
@@ -267,8 +255,11 @@ Model::Model(const pg_feature_params* p)
     : tables(build_model_tables(feature_params_from_abi(p))), flat(flatten_model(tables)) {
     int dev = 0;
     PG_CUDA(cudaGetDevice(&dev));
-    dev64.build(flat, 256, true);
-    dev32.build(flat, 512, false);
+    // pg_rows blocks sized for four resident blocks per SM (FP32) or two (FP64)
+    dev64.build(flat, 110 * 1024, true);
+    dev32.build(flat, 56 * 1024, false);
+    s_missing.alloc(sizeof(int));
+    PG_CUDA(cudaMemset(s_missing.as<void>(), 0, sizeof(int)));
     max_k = max_k0 = 1;
     for (const auto& ft : flat.types) {
         max_k = std::max(max_k, ft.K);
@@ -297,17 +288,21 @@ void Model::atom_offsets(const DeviceBatch& b, size_t t_size, std::vector<long l
 }
 
 size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
+    const size_t ts = fp64 ? 8 : 4;
     size_t mx = 0;
     for (const auto& ft : flat.types) {
-        const size_t ts = fp64 ? 8 : 4;
-        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts + ft.ent_head.size() * 2 * ts;
+        // a_nlm, features, self/virial vectors (9 per feature) and G
+        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts * 10 + ft.ent_head.size() * 2 * ts;
         mx = std::max(mx, b);
     }
-    return mx + (size_t)(mean_pairs * 28.0) + (size_t)flat.n_features * 3 * (fp64 ? 8 : 4);
+    size_t max_lin = 1;
+    for (const auto& ft : flat.types) max_lin = std::max<size_t>(max_lin, ft.n_lin);
+    // per pair: index, displacement, mirror and the pair derivatives (3 per feature); X rows
+    return mx + (size_t)(mean_pairs * (28.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;
 }
 
 // Per-batch plan: per-atom storage offsets and pg_rows work items.
-void Model::plan_rows(const DeviceBatch& b, RowPlan& plan) const {
+void Model::plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const {
     std::vector<long long> a_off, d_off, g_off;
     atom_offsets(b, 0, a_off, d_off, g_off, plan.a_tot, plan.d_tot, plan.g_tot);
     upload(plan.d_a_off, a_off);
@@ -318,8 +313,8 @@ void Model::plan_rows(const DeviceBatch& b, RowPlan& plan) const {
     for (int s = 0; s < b.n_st; ++s) {
         const int n = b.st_atom_off[s + 1] - b.st_atom_off[s];
         // every centre belongs to exactly one block (energy rows need all of them)
-        const int nblk = std::max(1, (n + kRowsTR - 1) / kRowsTR);
-        for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * kRowsTR});
+        const int nblk = std::max(1, (n + tr - 1) / tr);
+        for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * tr});
         item_off.push_back((int)items.size());
     }
     plan.n_items = (int)items.size();
@@ -353,18 +348,34 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
                                        s_G.as<void>(), max_k, stream);
         }
     }
-    s_partial.reserve(sizeof(double) * 7 * (size_t)flat.n_features * std::max(1, plan.n_items));
-    if (plan.n_items > 0) {
+    s_DS.reserve(9 * sizeof(T) * std::max<long long>(1, plan.d_tot));
+    s_mirror.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
+    s_gslot.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
+    s_order.reserve(sizeof(int) * std::max<long long>(1, b.n_pairs));
+    s_Dp.reserve(3 * sizeof(T) * (size_t)dmod.dm.max_lin * std::max<long long>(1, b.n_pairs));
+    if (b.n_atoms > 0) {
+        {
+            ProfScope ps("pg_nb_mirror", stream);
+            launch_nb_mirror(b.n_atoms, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                             s_mirror.as<long long>(), s_gslot.as<long long>(), s_missing.as<int>(), stream);
+        }
+        {
+            ProfScope ps("pg_rows_pairs", stream);
+            launch_rows_pairs<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                                 s_gslot.as<long long>(), plan.d_d_off.as<long long>(), plan.d_g_off.as<long long>(),
+                                 s_G.as<void>(), d_f_row, s_order.as<int>(), s_Dp.as<T>(), s_DS.as<T>(), stream);
+        }
         {
             ProfScope ps("pg_rows", stream);
-            launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                           plan.d_d_off.as<long long>(), s_D.as<T>(), plan.d_g_off.as<long long>(), s_G.as<void>(),
-                           plan.d_items.as<RowItem>(), plan.n_items, d_f_row, dmod.chunk, dmod.n_chunks,
-                           dmod.chunk_cap_ent, Xd, ld, s_partial.as<double>(), stream);
+            launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), plan.d_d_off.as<long long>(),
+                           s_D.as<T>(), s_Dp.as<T>(), s_DS.as<T>(), plan.d_items.as<RowItem>(), plan.n_items, d_f_row,
+                           dmod.rows_tr, dmod.chunk, dmod.n_chunks, Xd, ld, stream);
         }
-        ProfScope ps("pg_rows_reduce", stream);
-        launch_rows_reduce<T>(flat.n_features, b.n_st, plan.d_item_off.as<int>(), s_partial.as<double>(), d_e_row,
-                              d_s_row, Xd, ld, stream);
+    }
+    if (b.n_st > 0) {
+        ProfScope ps("pg_rows_es", stream);
+        launch_rows_es<T>(dmod.dm, B, plan.d_d_off.as<long long>(), s_D.as<T>(), s_DS.as<T>(), d_e_row, d_f_row,
+                          d_s_row, Xd, ld, stream);
     }
     PG_CUDA(cudaGetLastError());
 }
@@ -373,9 +384,22 @@ template <typename T>
 void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row,
                        const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream) {
     RowPlan plan;
-    plan_rows(b, plan);
+    plan_rows(b, plan, (sizeof(T) == 8 ? dev64 : dev32).rows_tr);
     run_rows<T>(b, plan, d_e_row, d_f_row, d_s_row, Xd, ld, stream);
     PG_CUDA(cudaStreamSynchronize(stream));
+    check_mirrors();
+}
+
+// A pair without its exact mirror would mean an asymmetric neighbour list
+// (its force contribution is then dropped).  The counter accumulates over
+// batches until read here, after the work that fed it has completed.
+void Model::check_mirrors() {
+    int missing = 0;
+    PG_CUDA(cudaMemcpy(&missing, s_missing.as<int>(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (missing) {
+        PG_CUDA(cudaMemset(s_missing.as<void>(), 0, sizeof(int)));
+        throw std::runtime_error("internal: neighbour list is not symmetric");
+    }
 }
 
 template void Model::run_rows<double>(DeviceBatch&, const RowPlan&, const long long*, const long long*,
@@ -388,19 +412,28 @@ template void Model::batch_rows<float>(DeviceBatch&, const long long*, const lon
                                        long long, cudaStream_t);
 
 // Split [0, n_st) into batches whose staged data fits the device budget.
+// Split [0, n_st) into batches whose staged data fits the device budget.  Pairs
+// per atom are estimated from each cell's density: N / V * 4/3 pi rc^3, with a
+// margin for clustering.
 std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bool fp64, size_t budget) const {
     std::vector<std::pair<int, int>> out;
-    const size_t per_atom = bytes_per_atom(fp64, 300.0);
-    const long long max_atoms = std::max<long long>(1, (long long)(budget / std::max<size_t>(1, per_atom)));
+    const double rc = flat.cutoff;
+    const double sphere = 4.0 / 3.0 * 3.14159265358979323846 * rc * rc * rc;
     int s0 = 0;
-    long long acc = 0;
+    double acc = 0.0;
     for (int s = 0; s < st->n_st; ++s) {
-        if (s > s0 && acc + st->n_atoms[s] > max_atoms) {
+        const double* a = st->axis + 9 * (size_t)s;  // row-major, columns are lattice vectors
+        const double vol = std::fabs(a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                                     a[2] * (a[3] * a[7] - a[4] * a[6]));
+        const int n = st->n_atoms[s];
+        const double pairs = vol > 0.0 ? 1.5 * n / vol * sphere + 8.0 : 300.0;
+        const double bytes = (double)n * (double)bytes_per_atom(fp64, pairs);
+        if (s > s0 && acc + bytes > (double)budget) {
             out.push_back({s0, s});
             s0 = s;
-            acc = 0;
+            acc = 0.0;
         }
-        acc += st->n_atoms[s];
+        acc += bytes;
     }
     if (s0 < st->n_st) out.push_back({s0, st->n_st});
     return out;

@@ -58,14 +58,19 @@ struct DevType {
     const FlatTerm* val_terms;
     const int *ent_off, *ent_head, *term_off;
     const FlatTerm* g_terms;
-    const int *col_ncomp, *comp_k, *comp_w, *col_nent, *col_ent_off;
-    const int* ent_meta;    // per G entry: tp | nid << 8 | key << 16
-    const int* ent_tp_off;  // per linear feature k: (n_tp + 1) entry offsets by type pair
-    const int* col_perm;    // pg_rows: for centres of this type, thread q of a chunk takes column col_perm[chunk0 + q]
+    const int *col_ncomp, *comp_k;
+    const int4* col_info;      // per column: its (up to three) linear features and their count (w)
+    const int* ent_tp_off;     // per linear feature k: (n_tp + 1) entry offsets by type pair
+    const int* ent_nk;         // per G entry: radial index | Y_lm index << 8 of its head
+    const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
+    const int* tp_head_nk;     // per tp_heads entry: radial index | Y_lm index << 8
+    const int* ent_hpos;       // per G entry: position of its head in its type pair's head list
 };
 
 struct DevModel {
     int n_type, n_tp, F, n_fn_max, maxl, n_ylm, gtinv;
+    int max_k0, max_lin;  // largest K0 and n_lin over the centre types (shared-memory layouts)
+    int max_k0tp;         // largest number of heads of one type pair
     double cutoff;
     const int* type_pairs;
     const int* tp_nfn;

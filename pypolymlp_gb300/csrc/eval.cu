@@ -11,8 +11,8 @@
 //                      A_i[h] = sum_e beta_k(e) G_e (no G stored)
 //   pg_eval_pairs      per pair image p = (i -> j, d): g_p = Re(A_i . dphi(d)/dd),
 //                      one warp per pair with the shared pair basis
-//   pg_eval_mirror     index of the mirror image (j -> i, -d) of every pair
-//                      (exact: -d is bit-identical)
+//   pg_nb_mirror       index of the mirror image (j -> i, -d) of every pair
+//                      (exact: -d is bit-identical; xrows.cu)
 //   pg_eval_gather     F_b = sum_{q in list(b)} (g_q - g_mirror(q))   (no atomics)
 //   pg_eval_reduce     E = sum_i E_i and stress = -sum_p d_p (x) g_p per structure
 // Energies match the reference's Euler-split pair sums, and forces/stress its
@@ -191,32 +191,6 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
     }
 }
 
-// Mirror of every pair: entry (b -> a, d) pairs with (a -> b, -d).  One warp per atom.
-__global__ void pg_eval_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d,
-                               long long* mirror, int* missing) {
-    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (b >= n_atoms) return;
-    for (long long q = nb_off[b] + lane; q < nb_off[b + 1]; q += 32) {
-        const int a = nb_j[q];
-        const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
-        long long lo = nb_off[a], hi = nb_off[a + 1];
-        while (lo < hi) {
-            const long long mid = (lo + hi) >> 1;
-            if (nb_j[mid] < b) lo = mid + 1;
-            else hi = mid;
-        }
-        long long m = -1;
-        for (long long p = lo; p < nb_off[a + 1] && nb_j[p] == b; ++p)
-            if (nb_d[3 * p] == -dx && nb_d[3 * p + 1] == -dy && nb_d[3 * p + 2] == -dz) {
-                m = p;
-                break;
-            }
-        mirror[q] = m;
-        if (m < 0) atomicAdd(missing, 1);
-    }
-}
-
 // F_b = sum_{q in list(b)} (g_q - g_mirror(q)); one thread per atom, FP64.
 __global__ void pg_eval_gather(int n_atoms, const long long* nb_off, const long long* mirror, const double* g,
                                double* forces) {
@@ -347,10 +321,9 @@ struct Evaluator {
                     d_aoff.as<long long>(), reinterpret_cast<const cplx<T>*>(s_Aadj.as<void>()), s_g.as<double>());
             }
             {
-                ProfScope ps("pg_eval_mirror", stream);
-                pg_eval_mirror<<<(b.n_atoms * 32 + 255) / 256, 256, 0, stream>>>(
-                    b.n_atoms, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                    s_mirror.as<long long>(), s_missing.as<int>());
+                ProfScope ps("pg_nb_mirror", stream);
+                launch_nb_mirror(b.n_atoms, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
+                                 s_mirror.as<long long>(), nullptr, s_missing.as<int>(), stream);
             }
             {
                 ProfScope ps("pg_eval_gather", stream);

@@ -369,7 +369,7 @@ std::vector<std::unique_ptr<Prepared>> prepare_batches(Model& m, const pg_struct
             if (f_row[s0 + q] >= 0) P->s_end += 6;
         for (double v : yl) P->yty += v * v;
         P->b.upload_structures(st, s0, s1, m.flat.cutoff);
-        m.plan_rows(P->b, P->plan);
+        m.plan_rows(P->b, P->plan, (fp64 ? m.dev64 : m.dev32).rows_tr);
         upload(P->d_e, le);
         upload(P->d_f, lf);
         upload(P->d_s, ls);
@@ -528,6 +528,7 @@ int pg_gram_accumulate(pg_gram* gh, const pg_structures* st, const int64_t* e_ro
         auto parts = prepare_batches(*g.m, st, e_row, f_row, s_row, n_rows, w, y, g.precision == PG_FP64);
         for (auto& P : parts) g.accumulate(*P);
         PG_CUDA(cudaStreamSynchronize(g.stream));
+        g.m->check_mirrors();
     });
 }
 
@@ -577,6 +578,7 @@ int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef,
             rows += P->rows;
         }
         PG_CUDA(cudaStreamSynchronize(g.stream));
+        g.m->check_mirrors();
         if (xtr) PG_CUDA(cudaMemcpy(xtr, XtR.as<double>(), (size_t)F * n_coef * 8, cudaMemcpyDeviceToHost));
         if (sq) PG_CUDA(cudaMemcpy(sq, SQ.as<double>(), (size_t)3 * n_coef * 8, cudaMemcpyDeviceToHost));
         if (n_rows) *n_rows = rows;
@@ -593,6 +595,7 @@ int pg_gram_result(pg_gram* gh, double* xtx, double* xty, double* yty, double* x
         pg_symmetrize<<<grid, 256, 0, g.stream>>>(g.G.as<double>(), F);
         PG_CUDA(cudaGetLastError());
         PG_CUDA(cudaStreamSynchronize(g.stream));
+        g.m->check_mirrors();
         if (xtx) PG_CUDA(cudaMemcpy(xtx, g.G.as<double>(), (size_t)F * F * sizeof(double), cudaMemcpyDeviceToHost));
         if (xty) PG_CUDA(cudaMemcpy(xty, g.xty.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
         if (xe_sum) PG_CUDA(cudaMemcpy(xe_sum, g.xe_sum.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));

@@ -27,7 +27,8 @@ struct RowItem {
     int a0;
 };
 
-constexpr int kRowsTR = 16;  // target atoms per pg_rows block
+constexpr int kRowsThreads = 256;  // threads of pg_rows / pg_rows_pairs blocks
+constexpr int kMaxTypePairs = 64;
 
 void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st);
 void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, cudaStream_t st);
@@ -39,14 +40,21 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
-size_t rows_smem_bytes(const DevModel& M, int chunk, int cap_ent, bool fp64);
+size_t rows_smem_bytes(const DevModel& M, int TR, int CH, bool fp64);
+size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64);
+void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,
+                      long long* gslot, int* missing, cudaStream_t st);
 template <typename T>
-void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                 const long long* d_off, const T* D, const long long* g_off, const void* G, const RowItem* items,
-                 int n_items, const long long* f_row, int chunk, int n_chunks, int cap_ent, T* X, long long ld,
-                 double* partial, cudaStream_t st);
+void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
+                       const double* nb_d, const long long* gslot, const long long* d_off, const long long* g_off,
+                       const void* G, const long long* f_row, int* order, T* Dp, T* DS, cudaStream_t st);
 template <typename T>
-void launch_rows_reduce(int F, int n_st, const int* item_off, const double* partial, const long long* e_row,
-                        const long long* s_row, T* X, long long ld, cudaStream_t st);
+void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
+                 const long long* d_off, const T* D, const T* Dp, const T* DS, const RowItem* items, int n_items,
+                 const long long* f_row, int TR, int CH, int n_chunks, T* X, long long ld, cudaStream_t st);
+template <typename T>
+void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const T* DS,
+                    const long long* e_row, const long long* f_row, const long long* s_row, T* X, long long ld,
+                    cudaStream_t st);
 
 }  // namespace pg

@@ -20,10 +20,10 @@ struct RowPlan {
 struct Model {
     ModelTables tables;
     FlatModel flat;
-    DeviceModel dev64, dev32;   // pg_rows column chunk of 128 (FP64) and 256 (FP32)
+    DeviceModel dev64, dev32;   // device tables and pg_rows block shapes for FP64 and FP32
     int max_k = 1, max_k0 = 1;
     // per-batch scratch (grow-only)
-    DevBuf s_A, s_D, s_G, s_partial;
+    DevBuf s_A, s_D, s_G, s_DS, s_Dp, s_mirror, s_gslot, s_order, s_missing;
 
     explicit Model(const pg_feature_params* p);
 
@@ -33,10 +33,11 @@ struct Model {
     size_t bytes_per_atom(bool fp64, double mean_pairs) const;
     std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
 
-    void plan_rows(const DeviceBatch& b, RowPlan& plan) const;
+    void plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const;
     template <typename T>
     void run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_row, const long long* d_f_row,
                   const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream);
+    void check_mirrors();
     template <typename T>
     void batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row, const long long* d_s_row,
                     T* Xd, long long ld, cudaStream_t stream);

@@ -9,14 +9,16 @@
 //   pg_features_adjoint        invariant features d_k of every atom and the
 //                              sparse adjoint G_k[h] = d d_k / d a_h with the
 //                              conjugate half folded in (features.cpp:155-248).
-//   pg_rows                    energy, force and stress rows of X for a block
-//                              of target atoms and a chunk of columns:
-//                              X_force[3j+c, col] = sum over pairs of
-//                              +-Re(G_col(i) . d a(i)/d r_j,c), with G_col the
-//                              polynomial-weighted adjoint (model.cpp:159-267).
-//                              Each thread owns one column, so the sums are
-//                              race free and deterministic.
-//   pg_rows_reduce             per-structure sum of the energy/stress partials.
+//   pg_nb_mirror               mirror index of every pair.
+//   pg_rows_pairs              per centre: the derivatives dd_k/dd_p of its
+//                              linear features for every pair (the pair bases
+//                              contracted with the adjoint G), and their self
+//                              and virial sums.
+//   pg_rows                    force rows of X for a block of target atoms and
+//                              a chunk of columns: the pair derivatives landing
+//                              on each target expanded into the polynomial
+//                              columns (model.cpp:159-267).
+//   pg_rows_es                 energy and stress rows per structure.
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -218,145 +220,159 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
 }
 
 // --------------------------------------------------------------- K5 rows
-template <typename T, int TR>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256, 1) pg_rows(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                        const long long* d_off, const T* D, const long long* g_off, const cplx<T>* G,
-                        const RowItem* items, const long long* f_row, int chunk_cap_ent, T* X, long long ld,
-                        double* partial /* [item][7][F] */) {
+// The force rows of X factor through the linear features d_k of each centre:
+//   X_force[(j,c), col] = -sum_{p: i_p -> j, i_p != j} sum_{k in col} w_k,col(i_p) dd_k(i_p)/dd_p,c
+//                         + [j = i] sum_{k in col} w_k,col(i) sum_{p in list(i), j_p != i} dd_k(i)/dd_p,c,
+// where w_k,col(i) is the product of the other features of the column and
+// dd_k(i)/dd_p = sum_e Re(G_e(i) . dphi_(h_e)(d_p)/dd_p) over the adjoint
+// entries of k (model.cpp:159-267 builds the same rows column by column).
+//   pg_nb_mirror    index of the mirror (j -> i, -d) of every pair (i -> j, d)
+//   pg_rows_pairs   stage A, per centre: dd_k/dd_p for every pair p, stored at
+//                   the slot of its mirror (so the pairs landing on a target are
+//                   contiguous), plus the self and virial sums DS
+//   pg_rows         stage B, per target block: expansion into the columns
+//   pg_rows_es      energy and stress rows, per structure
+
+// Mirror of every pair: entry (b -> a, d) pairs with (a -> b, -d).  The
+// translation set is symmetric and displacements are formed without
+// contraction, so -d is bit-identical.  Optionally also the group slot of the
+// pair: the first entry of b in a's list.  One warp per atom.
+__global__ void pg_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d,
+                             long long* mirror, long long* gslot, int* missing) {
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= n_atoms) return;
+    for (long long q = nb_off[b] + lane; q < nb_off[b + 1]; q += 32) {
+        const int a = nb_j[q];
+        const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
+        long long lo = nb_off[a], hi = nb_off[a + 1];
+        while (lo < hi) {
+            const long long mid = (lo + hi) >> 1;
+            if (nb_j[mid] < b) lo = mid + 1;
+            else hi = mid;
+        }
+        if (gslot) gslot[q] = lo;  // first entry of b in a's list: the slot of the group (b, a)
+        long long m = -1;
+        for (long long p = lo; p < nb_off[a + 1] && nb_j[p] == b; ++p)
+            if (nb_d[3 * p] == -dx && nb_d[3 * p + 1] == -dy && nb_d[3 * p + 2] == -dz) {
+                m = p;
+                break;
+            }
+        mirror[q] = m;
+        if (m < 0) atomicAdd(missing, 1);
+    }
+}
+
+// Stage A.  Block per centre atom i of a force structure; its pairs are taken
+// in chunks of up to NW pairs of one type pair (pairs ordered by type pair,
+// stably, so the images of a neighbour stay consecutive).  Per chunk, warp w
+// builds the basis of pair w and its head-space gradient
+//   H[c][u][w] = d phi_h(d_w) / dd_w,c    (h the u-th head of the type pair),
+// then thread k contracts the adjoint entries of feature k with all pairs of
+// the chunk at once:  dd_k/dd_w,c = sum_e Re(G_e(i) . H[c][u_e][w]).
+// The images of one neighbour j are summed and stored once, at the group slot
+// (the first entry of i in j's list), so stage B reads one vector per
+// (centre, target).  Thread k also accumulates the centre's DS vectors
+//   DS[i][c][k]   = sum_{p, j_p != i} dd_k/dd_p,c                   (self rows)
+//   DS[i][3+q][k] = sum_p d_p,b(q) dd_k/dd_p,a(q)                   (virial)
+// with (a, b)(q) = (x,x) (y,y) (z,z) (x,y) (y,z) (z,x).
+template <typename T>
+__device__ __forceinline__ void load_h8(const cplx<T>* h, cplx<T> (&v)[8]) {
+#pragma unroll
+    for (int w = 0; w < 8; ++w) v[w] = h[w];
+}
+template <>
+__device__ __forceinline__ void load_h8<float>(const cplx<float>* h, cplx<float> (&v)[8]) {
+    const float4* p = reinterpret_cast<const float4*>(h);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 x = p[q];
+        v[2 * q] = {x.x, x.y};
+        v[2 * q + 1] = {x.z, x.w};
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off,
+                                                              const int* nb_j, const double* nb_d,
+                                                              const long long* gslot, const long long* d_off,
+                                                              const long long* g_off, const cplx<T>* G,
+                                                              const long long* f_row, int* order, T* Dp, T* DS) {
+    constexpr int NW = kRowsThreads / 32;
+    static_assert(NW == 8, "the chunk width is 8 pairs");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    // grid: x = column chunk (fastest, so the chunks of one structure run together), y = work item
-    const RowItem it = items[blockIdx.y];
-    const int CH = blockDim.x;
-    const int c0 = blockIdx.x * CH;            // first column of this chunk
-    const int cq = c0 + threadIdx.x;
-    const bool col_ok = cq < M.F;              // position threadIdx.x of the chunk exists
-    const int nw = CH >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int s = it.st;
-    const int sa0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - sa0;
-    const int blk0 = it.a0;  // local index of the first target atom
-    const bool force = f_row[s] >= 0;
-    const int ntp = M.n_tp;
-
-    // shared layout: out[TR*3][CH] | gval[cap] | gmeta[cap] | tpo[CH][ntp+1] | table | basis slots | slot info
-    T* out = reinterpret_cast<T*>(smem_raw);
-    cplx<T>* gval = reinterpret_cast<cplx<T>*>(out + (size_t)TR * 3 * CH);
-    int* gmeta = reinterpret_cast<int*>(gval + chunk_cap_ent);
-    int* tpo = gmeta + chunk_cap_ent;
-    T* s_tab = reinterpret_cast<T*>(
-        (reinterpret_cast<uintptr_t>(tpo + (size_t)CH * (ntp + 1)) + 15) & ~uintptr_t(15));
+    __shared__ int s_wcnt[NW], s_tpoff[kMaxTypePairs + 1];
+    __shared__ int s_q[NW], s_flag[NW];  // pair index; ok | self << 1 | flush << 2 | fresh << 3
+    __shared__ long long s_slot[NW];
+    const int i = blockIdx.x;
+    if (f_row[B.atom_st[i]] < 0) return;
+    const int t1 = B.types[i];
+    const DevType& ty = M.types[t1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nl = ty.n_lin, NL = M.max_lin, HT = M.max_k0tp;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    T* sb = reinterpret_cast<T*>(
-        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));
-    T* sdx = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sb + slot * nw) + 15) & ~uintptr_t(15));
-    T* sdy = sdx + nw;
-    T* sdz = sdy + nw;
-    T* sdis = sdz + nw;
-    int* stp = reinterpret_cast<int*>(sdis + nw);
-    int* sj = stp + nw;
-    int* sok = sj + nw;
-    // per-column energy and stress sums (FP64), indexed by column position in the chunk
-    double* cacc = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(sok + nw) + 15) & ~uintptr_t(15));
-    for (int q = threadIdx.x; q < 7 * CH; q += CH) cacc[q] = 0.0;
-
+    cplx<T>* H = reinterpret_cast<cplx<T>*>(smem_raw);  // [3][HT][NW]
+    T* sb = reinterpret_cast<T*>(H + (size_t)3 * HT * NW);
+    T* s_tab = sb + slot * NW;
+    T* sd = reinterpret_cast<T*>(
+        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));  // [NW][3]
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
-    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
-    for (int q = threadIdx.x; q < TR * 3 * CH; q += CH) out[q] = (T)0;
-    int* my_tpo = tpo + (size_t)threadIdx.x * (ntp + 1);
+    const long long p0 = nb_off[i], p1 = nb_off[i + 1];
+    const int np = (int)(p1 - p0);
+    int* ord = order + p0;
+    // stable order of the pairs by type pair
+    int cursor = 0;
+    for (int tp = 0; tp < M.n_tp; ++tp) {
+        if (threadIdx.x == 0) s_tpoff[tp] = cursor;
+        for (int r0 = 0; r0 < np; r0 += blockDim.x) {
+            const int r = r0 + threadIdx.x;
+            const bool f = r < np && M.type_pairs[t1 * M.n_type + B.types[nb_j[p0 + r]]] == tp;
+            const unsigned m = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) s_wcnt[warp] = __popc(m);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int w = 0; w < NW; ++w) {
+                before += w < warp ? s_wcnt[w] : 0;
+                total += s_wcnt[w];
+            }
+            if (f) ord[cursor + before + __popc(m & ((1u << lane) - 1u))] = r;
+            cursor += total;
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) s_tpoff[M.n_tp] = cursor;
     __syncthreads();
-
-    for (int i = 0; i < n; ++i) {
-        const int gi = sa0 + i;
-        const int t1 = B.types[gi];
-        const DevType& ty = M.types[t1];
-        const bool centre_in = (i >= blk0 && i < blk0 + TR);
-        const T* Di = D + d_off[gi];
-        // --- the column this thread takes for centres of type t1, and its adjoint, grouped by type pair
-        const int col = col_ok ? ty.col_perm[cq] : 0;
-        const int cpos = col - c0;
-        const int nc = col_ok ? ty.col_ncomp[col] : 0;
-        const int my_off = col_ok ? ty.col_ent_off[col] : 0;
-        if (nc > 0 && centre_in) {
-            T pe = (T)1;
-            for (int c = 0; c < nc; ++c) pe *= Di[ty.comp_k[col * 3 + c]];
-            cacc[cpos] += (double)pe;
-        }
-        if (!force) {
-            __syncthreads();  // the next centre may map this column to another thread
-            continue;
-        }
-        {
-            const cplx<T>* Gi = G + g_off[gi];
-            T wt[3];
-            int kk[3];
-            for (int c = 0; c < nc; ++c) {
-                kk[c] = ty.comp_k[col * 3 + c];
-                T w = (T)1;
-                for (int q = 0; q < 2; ++q) {
-                    const int o = ty.comp_w[(col * 3 + c) * 2 + q];
-                    if (o >= 0) w *= Di[o];
-                }
-                wt[c] = w;
-            }
-            int w = my_off;
-            for (int t = 0; t < ntp; ++t) {
-                my_tpo[t] = w;
-                for (int c = 0; c < nc; ++c) {
-                    const int* eo = ty.ent_tp_off + (size_t)kk[c] * (ntp + 1);
-                    for (int e = eo[t]; e < eo[t + 1]; ++e) {
-                        const cplx<T> g = Gi[e];
-                        gval[w] = {wt[c] * g.re, wt[c] * g.im};
-                        gmeta[w] = ty.ent_meta[e] >> 8;  // nid | key << 8
-                        ++w;
-                    }
-                }
-            }
-            my_tpo[ntp] = w;
-        }
-        // --- pair images of centre i that touch this block
-        long long pb = nb_off[gi], pe_ = nb_off[gi + 1];
-        if (!centre_in) {
-            // entries are sorted by neighbour index: find [lo, hi) with j in block
-            long long lo = pb, hi = pe_;
-            while (lo < hi) {
-                const long long mid = (lo + hi) >> 1;
-                if (nb_j[mid] - sa0 < blk0) lo = mid + 1;
-                else hi = mid;
-            }
-            long long lo2 = lo, hi2 = pe_;
-            while (lo2 < hi2) {
-                const long long mid = (lo2 + hi2) >> 1;
-                if (nb_j[mid] - sa0 < blk0 + TR) lo2 = mid + 1;
-                else hi2 = mid;
-            }
-            pb = lo;
-            pe_ = lo2;
-        }
-        // sums over the pairs of this centre in T; added to the FP64 totals per centre
-        T self[3] = {0, 0, 0};
-        T cst[6] = {0, 0, 0, 0, 0, 0};
-        __syncthreads();  // gval/gmeta/tpo of centre i are complete
-        for (long long base = pb; base < pe_; base += nw) {
-            const long long k = base + warp;
-            BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
-            if (k < pe_) {
-                const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
+    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
+    const cplx<T>* Gi = G + g_off[i];
+    T* ds = DS + 9 * d_off[i];
+    for (int q = threadIdx.x; q < 9 * nl; q += blockDim.x) ds[q] = (T)0;
+    for (int tp = 0; tp < M.n_tp; ++tp) {
+        const int r_end = s_tpoff[tp + 1];
+        const int q0 = ty.tp_head_off[tp], nh = ty.tp_head_off[tp + 1] - q0;
+        for (int r0 = s_tpoff[tp]; r0 < r_end; r0 += NW) {
+            const int n = min(NW, r_end - r0);
+            // ---- bases and head-space gradients of the chunk
+            if (warp < n) {
+                const long long q = p0 + ord[r0 + warp];
+                const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
                 double dis = 0.0;
                 if (lane == 0)
                     dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
                 dis = __shfl_sync(0xffffffffu, dis, 0);
                 const bool ok = dis < M.cutoff;
-                const int j = nb_j[k];
-                const int tp = M.type_pairs[t1 * M.n_type + B.types[j]];
+                const int j = nb_j[q];
                 if (lane == 0) {
-                    sdx[warp] = (T)dx;
-                    sdy[warp] = (T)dy;
-                    sdz[warp] = (T)dz;
-                    sdis[warp] = (T)dis;
-                    stp[warp] = tp;
-                    sj[warp] = j - sa0;
-                    sok[warp] = ok;
+                    sd[3 * warp] = (T)dx;
+                    sd[3 * warp + 1] = (T)dy;
+                    sd[3 * warp + 2] = (T)dz;
+                    s_q[warp] = (int)(q - p0);
+                    const bool first = q == p0 || nb_j[q - 1] != j;
+                    const bool last = q + 1 == p1 || nb_j[q + 1] != j;
+                    s_flag[warp] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (last ? 4 : 0) | (first ? 16 : 0);
+                    s_slot[warp] = gslot[q];
                 }
                 if (ok) {
+                    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
                     warp_radial<T, true>(M, tp, dis, bv, lane);
                     if (M.gtinv) {
                         warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
@@ -364,92 +380,270 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256, 1) pg_rows(DevMode
                         bv.Y[0] = {(T)1, (T)0};
                         bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
                     }
+                    __syncwarp();
+                    const T invr = (T)1 / (T)dis;
+                    const T ux = (T)dx * invr, uy = (T)dy * invr, uz = (T)dz * invr;
+                    for (int u = lane; u < nh; u += 32) {
+                        const int nk = ty.tp_head_nk[q0 + u];
+                        const int nid = nk & 0xff, key = nk >> 8;
+                        const T f = bv.fn[nid], fd = bv.fnd[nid];
+                        const cplx<T> y = bv.Y[key];
+                        const cplx<T> yx = bv.dY[key], yy = bv.dY[M.n_ylm + key], yz = bv.dY[2 * M.n_ylm + key];
+                        H[((size_t)0 * HT + u) * NW + warp] = {f * yx.re + fd * ux * y.re, f * yx.im + fd * ux * y.im};
+                        H[((size_t)1 * HT + u) * NW + warp] = {f * yy.re + fd * uy * y.re, f * yy.im + fd * uy * y.im};
+                        H[((size_t)2 * HT + u) * NW + warp] = {f * yz.re + fd * uz * y.re, f * yz.im + fd * uz * y.im};
+                    }
+                } else {
+                    for (int u = lane; u < nh; u += 32)
+                        for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + warp] = {(T)0, (T)0};
                 }
-            } else if (lane == 0) {
-                sok[warp] = 0;
+            } else {
+                for (int u = lane; u < nh; u += 32)
+                    for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + warp] = {(T)0, (T)0};
             }
             __syncthreads();
-            if (col_ok && nc > 0) {
-                const int nb = (int)min((long long)nw, pe_ - base);
-                for (int w = 0; w < nb; ++w) {
-                    if (!sok[w]) continue;
-                    const int tp = stp[w];
-                    const int e0 = my_tpo[tp], e1 = my_tpo[tp + 1];
-                    if (e0 == e1) continue;
-                    BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
-                    T s0 = 0, sx = 0, sy = 0, sz = 0;
-                    for (int q = e0; q < e1; ++q) {
-                        const int meta = gmeta[q];
-                        const int nid = meta & 0xff, key = meta >> 8;
-                        const T f = v.fn[nid];
-                        const cplx<T> g = gval[q];
-                        s0 += v.fnd[nid] * creal_mul(g, v.Y[key]);
-                        sx += f * creal_mul(g, v.dY[key]);
-                        sy += f * creal_mul(g, v.dY[M.n_ylm + key]);
-                        sz += f * creal_mul(g, v.dY[2 * M.n_ylm + key]);
+            if (threadIdx.x == 0) {
+                // where to store the running image sums: at a group's last image or
+                // the chunk's end; "fresh" when the group's first image is in this chunk
+                int seg = 0;
+                for (int w = 0; w < n; ++w) {
+                    int fl = s_flag[w];
+                    const bool flush = (fl & 4) || w == n - 1;
+                    if (s_flag[seg] & 16) fl |= 8;
+                    s_flag[w] = (fl & ~4) | (flush ? 4 : 0);
+                    if (flush) seg = w + 1;
+                }
+            }
+            __syncthreads();
+            // ---- contraction of the chunk
+            for (int kf = threadIdx.x; kf < nl; kf += blockDim.x) {
+                const int* eo = ty.ent_tp_off + (size_t)kf * (M.n_tp + 1);
+                T acc[NW][3];
+#pragma unroll
+                for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
+                for (int e = eo[tp]; e < eo[tp + 1]; ++e) {
+                    const cplx<T> g = Gi[e];
+                    const int u = ty.ent_hpos[e];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        cplx<T> h[8];
+                        load_h8<T>(H + ((size_t)c * HT + u) * NW, h);
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
                     }
-                    const T dx = sdx[w], dy = sdy[w], dz = sdz[w];
-                    const T sc = s0 / sdis[w];
-                    const T vx = sc * dx + sx, vy = sc * dy + sy, vz = sc * dz + sz;
-                    const int jl = sj[w];
-                    if (centre_in) {
-                        if (jl != i) {
-                            self[0] += vx;
-                            self[1] += vy;
-                            self[2] += vz;
+                }
+                T sv[9];
+#pragma unroll
+                for (int v = 0; v < 9; ++v) sv[v] = (T)0;
+                T run0 = 0, run1 = 0, run2 = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    if (w >= n) break;
+                    const int fl = s_flag[w];
+                    const T a0 = acc[w][0], a1 = acc[w][1], a2 = acc[w][2];
+                    if (fl & 1) {
+                        const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
+                        if (!(fl & 2)) {
+                            sv[0] += a0;
+                            sv[1] += a1;
+                            sv[2] += a2;
                         }
-                        cst[0] -= vx * dx;
-                        cst[1] -= vy * dy;
-                        cst[2] -= vz * dz;
-                        cst[3] -= vx * dy;
-                        cst[4] -= vy * dz;
-                        cst[5] -= vz * dx;
+                        sv[3] += dx * a0;
+                        sv[4] += dy * a1;
+                        sv[5] += dz * a2;
+                        sv[6] += dy * a0;
+                        sv[7] += dz * a1;
+                        sv[8] += dx * a2;
                     }
-                    if (jl != i && jl >= blk0 && jl < blk0 + TR) {
-                        T* o = out + (size_t)(jl - blk0) * 3 * CH + cpos;
-                        o[0] -= vx;
-                        o[CH] -= vy;
-                        o[2 * CH] -= vz;
+                    run0 += a0;
+                    run1 += a1;
+                    run2 += a2;
+                    if (fl & 4) {
+                        T* o = Dp + (size_t)s_slot[w] * 3 * NL + kf;
+                        if (fl & 8) {
+                            o[0] = run0;
+                            o[NL] = run1;
+                            o[2 * NL] = run2;
+                        } else {
+                            o[0] += run0;
+                            o[NL] += run1;
+                            o[2 * NL] += run2;
+                        }
+                        run0 = run1 = run2 = 0;
                     }
                 }
+#pragma unroll
+                for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + kf] += sv[v];
             }
             __syncthreads();
         }
-        if (centre_in && col_ok) {
-            T* o = out + (size_t)(i - blk0) * 3 * CH + cpos;
-            o[0] += self[0];
-            o[CH] += self[1];
-            o[2 * CH] += self[2];
-            for (int q = 0; q < 6; ++q) cacc[(size_t)(q + 1) * CH + cpos] += (double)cst[q];
-        }
-        __syncthreads();  // before gval is rebuilt for the next centre
     }
-    if (!col_ok) return;
-    // column positions are in natural order: thread q writes column c0 + q
-    if (force) {
-        const long long r0 = f_row[s];
-        const int na = min(TR, n - blk0);
-        for (int a = 0; a < na; ++a)
-            for (int c = 0; c < 3; ++c)
-                X[(size_t)cq * ld + r0 + 3 * (blk0 + a) + c] = out[(size_t)a * 3 * CH + c * CH + threadIdx.x];
-    }
-    double* p = partial + (size_t)blockIdx.y * 7 * M.F;
-    for (int q = 0; q < 7; ++q) p[(size_t)q * M.F + cq] = cacc[(size_t)q * CH + threadIdx.x];
 }
 
-// Sum the per-block energy/stress partials of each structure into X.
+// Stage B.  Columns [c0, c0 + CH) of the force rows of a block of TR target
+// atoms.  For target j, the centres i with images on it are the runs of j's
+// own list; the group vector of (i, j) sits at the run's first slot and is
+// expanded into the columns with the weights of centre i.  The
+// self rows of the block's centres come from DS.  Each thread owns columns,
+// so all sums are race free and deterministic.
 template <typename T>
-__global__ void pg_rows_reduce(int F, const int* item_off /* n_st+1 */, const double* partial,
-                               const long long* e_row, const long long* s_row, T* X, long long ld) {
-    const int s = blockIdx.x;
-    for (int col = threadIdx.x + blockIdx.y * blockDim.x; col < F; col += blockDim.x * gridDim.y) {
-        double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-        for (int b = item_off[s]; b < item_off[s + 1]; ++b)
-            for (int q = 0; q < 7; ++q) acc[q] += partial[((size_t)b * 7 + q) * F + col];
-        X[(size_t)col * ld + e_row[s]] = (T)acc[0];
-        if (s_row[s] >= 0)
-            for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[q + 1];
+__global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
+                                                        const int* nb_j, const long long* d_off, const T* D,
+                                                        const T* Dp, const T* DS, const RowItem* items,
+                                                        const long long* f_row, int TR, int CH, T* X, long long ld) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const RowItem it = items[blockIdx.x];
+    const int s = it.st;
+    if (f_row[s] < 0) return;
+    const int F = M.F;
+    const int c0 = blockIdx.y * CH, c1 = min(F, c0 + CH), nc_blk = c1 - c0;
+    const int sa0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - sa0;
+    const int blk0 = it.a0, nblk = min(TR, n - blk0);
+    const int NL = M.max_lin;
+    T* out = reinterpret_cast<T*>(smem_raw);  // [TR][3][CH]
+    T* Dk = out + (size_t)TR * 3 * CH;        // [3][NL]
+    T* dcur = Dk + 3 * (size_t)NL;            // [NL]
+    for (int q = threadIdx.x; q < TR * 3 * CH; q += blockDim.x) out[q] = (T)0;
+    for (int a = 0; a < nblk; ++a) {
+        const int gj = sa0 + blk0 + a;
+        T* o = out + (size_t)a * 3 * CH;
+        long long q = nb_off[gj];
+        const long long qe = nb_off[gj + 1];
+        while (q < qe) {
+            const int gi = nb_j[q];
+            long long qb = q + 1;
+            while (qb < qe && nb_j[qb] == gi) ++qb;
+            if (gi == gj) {  // images of the target itself: no force on it
+                q = qb;
+                continue;
+            }
+            const DevType& ty = M.types[B.types[gi]];
+            const int nl = ty.n_lin;
+            __syncthreads();  // the previous expansion has read Dk and dcur
+            for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+                dcur[k] = D[d_off[gi] + k];
+                const T* src = Dp + (size_t)q * 3 * NL + k;  // the group (gi, gj), images summed
+                Dk[k] = src[0];
+                Dk[NL + k] = src[NL];
+                Dk[2 * NL + k] = src[2 * NL];
+            }
+            __syncthreads();
+            for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
+                const int4 ci = ty.col_info[c0 + u];
+                if (ci.w == 0) continue;
+                T vx, vy, vz;
+                if (ci.w == 1) {
+                    vx = Dk[ci.x];
+                    vy = Dk[NL + ci.x];
+                    vz = Dk[2 * NL + ci.x];
+                } else {
+                    const T d0 = dcur[ci.x], d1 = dcur[ci.y];
+                    if (ci.w == 2) {
+                        vx = d1 * Dk[ci.x] + d0 * Dk[ci.y];
+                        vy = d1 * Dk[NL + ci.x] + d0 * Dk[NL + ci.y];
+                        vz = d1 * Dk[2 * NL + ci.x] + d0 * Dk[2 * NL + ci.y];
+                    } else {
+                        const T d2 = dcur[ci.z];
+                        const T w0 = d1 * d2, w1 = d0 * d2, w2 = d0 * d1;
+                        vx = w0 * Dk[ci.x] + w1 * Dk[ci.y] + w2 * Dk[ci.z];
+                        vy = w0 * Dk[NL + ci.x] + w1 * Dk[NL + ci.y] + w2 * Dk[NL + ci.z];
+                        vz = w0 * Dk[2 * NL + ci.x] + w1 * Dk[2 * NL + ci.y] + w2 * Dk[2 * NL + ci.z];
+                    }
+                }
+                o[u] -= vx;
+                o[CH + u] -= vy;
+                o[2 * CH + u] -= vz;
+            }
+            q = qb;
+        }
     }
+    // self rows of the block's centres
+    for (int a = 0; a < nblk; ++a) {
+        const int gi = sa0 + blk0 + a;
+        const DevType& ty = M.types[B.types[gi]];
+        const int nl = ty.n_lin;
+        const T* Di = D + d_off[gi];
+        const T* ds = DS + 9 * d_off[gi];
+        T* o = out + (size_t)a * 3 * CH;
+        for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
+            const int4 ci = ty.col_info[c0 + u];
+            if (ci.w == 0) continue;
+            T w0 = 1, w1 = 0, w2 = 0;
+            if (ci.w == 2) {
+                w0 = Di[ci.y];
+                w1 = Di[ci.x];
+            } else if (ci.w == 3) {
+                w0 = Di[ci.y] * Di[ci.z];
+                w1 = Di[ci.x] * Di[ci.z];
+                w2 = Di[ci.x] * Di[ci.y];
+            }
+            T v[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                v[c] = w0 * ds[(size_t)c * nl + ci.x];
+                if (ci.w > 1) v[c] += w1 * ds[(size_t)c * nl + ci.y];
+                if (ci.w > 2) v[c] += w2 * ds[(size_t)c * nl + ci.z];
+            }
+            o[u] += v[0];
+            o[CH + u] += v[1];
+            o[2 * CH + u] += v[2];
+        }
+    }
+    __syncthreads();
+    const long long r0 = f_row[s] + 3LL * blk0;
+    for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
+        T* xc = X + (size_t)(c0 + u) * ld + r0;
+        for (int a = 0; a < nblk; ++a)
+            for (int c = 0; c < 3; ++c) xc[3 * a + c] = out[(size_t)a * 3 * CH + c * CH + u];
+    }
+}
+
+// Energy and stress rows: block per (structure, 256 columns), thread per
+// column, FP64 sums over the structure's centres in atom order:
+//   X[e_row, col] = sum_i poly_col(d(i)),
+//   X[s_row + q, col] = -sum_i sum_{k in col} w_k,col(i) DS[i][3+q][k].
+template <typename T>
+__global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D, const T* DS,
+                           const long long* e_row, const long long* f_row, const long long* s_row, T* X,
+                           long long ld) {
+    const int s = blockIdx.x;
+    const int col = blockIdx.y * blockDim.x + threadIdx.x;
+    if (col >= M.F) return;
+    const bool force = f_row[s] >= 0;
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int gi = B.st_atom_off[s]; gi < B.st_atom_off[s + 1]; ++gi) {
+        const DevType& ty = M.types[B.types[gi]];
+        const int4 ci = ty.col_info[col];
+        if (ci.w == 0) continue;
+        const T* Di = D + d_off[gi];
+        T w0 = 1, w1 = 0, w2 = 0, e;
+        if (ci.w == 1) {
+            e = Di[ci.x];
+        } else if (ci.w == 2) {
+            w0 = Di[ci.y];
+            w1 = Di[ci.x];
+            e = Di[ci.x] * Di[ci.y];
+        } else {
+            w0 = Di[ci.y] * Di[ci.z];
+            w1 = Di[ci.x] * Di[ci.z];
+            w2 = Di[ci.x] * Di[ci.y];
+            e = Di[ci.x] * Di[ci.y] * Di[ci.z];
+        }
+        acc[0] += (double)e;
+        if (!force) continue;
+        const int nl = ty.n_lin;
+        const T* ds = DS + 9 * d_off[gi] + 3 * (size_t)nl;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            T v = w0 * ds[(size_t)q * nl + ci.x];
+            if (ci.w > 1) v += w1 * ds[(size_t)q * nl + ci.y];
+            if (ci.w > 2) v += w2 * ds[(size_t)q * nl + ci.z];
+            acc[1 + q] -= (double)v;
+        }
+    }
+    X[(size_t)col * ld + e_row[s]] = (T)acc[0];
+    if (force && s_row[s] >= 0)
+        for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[1 + q];
 }
 
 // ------------------------------------------------------------ prefix sums
@@ -514,34 +708,53 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                                                          reinterpret_cast<cplx<T>*>(G));
 }
 
-size_t rows_smem_bytes(const DevModel& M, int chunk, int cap_ent, bool fp64) {
+size_t rows_smem_bytes(const DevModel& M, int TR, int CH, bool fp64) {
     const size_t ts = fp64 ? 8 : 4;
-    const int nw = chunk / 32;
+    return ((size_t)TR * 3 * CH + (size_t)4 * M.max_lin) * ts;
+}
+
+size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64) {
+    const size_t ts = fp64 ? 8 : 4;
+    const int nw = kRowsThreads / 32;
     const size_t slot = fp64 ? basis_slot_elems<double>(M.n_fn_max, M.n_ylm, M.maxl)
                              : basis_slot_elems<float>(M.n_fn_max, M.n_ylm, M.maxl);
-    return (size_t)kRowsTR * 3 * chunk * ts + (size_t)cap_ent * (2 * ts + 4) + (size_t)chunk * (M.n_tp + 1) * 4 +
-           16 + (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts + 16 + slot * nw * ts + 16 +
-           (size_t)nw * (4 * 8 + 3 * 4) + 16 + (size_t)7 * chunk * 8;
+    return (size_t)3 * M.max_k0tp * nw * 2 * ts + slot * nw * ts + (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts +
+           16 + (size_t)3 * nw * ts + 16;
+}
+
+void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,
+                      long long* gslot, int* missing, cudaStream_t st) {
+    const int threads = 256;
+    pg_nb_mirror<<<(int)(((long long)n_atoms * 32 + threads - 1) / threads), threads, 0, st>>>(
+        n_atoms, nb_off, nb_j, nb_d, mirror, gslot, missing);
 }
 
 template <typename T>
-void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                 const long long* d_off, const T* D, const long long* g_off, const void* G, const RowItem* items,
-                 int n_items, const long long* f_row, int chunk, int n_chunks, int cap_ent, T* X, long long ld,
-                 double* partial, cudaStream_t st) {
-    const size_t smem = rows_smem_bytes(M, chunk, cap_ent, sizeof(T) == 8);
-    PG_CUDA(cudaFuncSetAttribute(pg_rows<T, kRowsTR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(n_chunks, n_items);
-    pg_rows<T, kRowsTR><<<grid, chunk, smem, st>>>(M, B, nb_off, nb_j, nb_d, d_off, D, g_off,
-                                                   reinterpret_cast<const cplx<T>*>(G), items, f_row, cap_ent, X,
-                                                   ld, partial);
+void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
+                       const double* nb_d, const long long* gslot, const long long* d_off, const long long* g_off,
+                       const void* G, const long long* f_row, int* order, T* Dp, T* DS, cudaStream_t st) {
+    const size_t smem = rows_pairs_smem_bytes(M, sizeof(T) == 8);
+    PG_CUDA(cudaFuncSetAttribute(pg_rows_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pg_rows_pairs<T><<<B.n_atoms, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, nb_d, gslot, d_off, g_off,
+                                                           reinterpret_cast<const cplx<T>*>(G), f_row, order, Dp, DS);
 }
 
 template <typename T>
-void launch_rows_reduce(int F, int n_st, const int* item_off, const double* partial, const long long* e_row,
-                        const long long* s_row, T* X, long long ld, cudaStream_t st) {
-    dim3 grid(n_st, (F + 255) / 256);
-    pg_rows_reduce<T><<<grid, 256, 0, st>>>(F, item_off, partial, e_row, s_row, X, ld);
+void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
+                 const long long* d_off, const T* D, const T* Dp, const T* DS, const RowItem* items, int n_items,
+                 const long long* f_row, int TR, int CH, int n_chunks, T* X, long long ld, cudaStream_t st) {
+    const size_t smem = rows_smem_bytes(M, TR, CH, sizeof(T) == 8);
+    PG_CUDA(cudaFuncSetAttribute(pg_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(n_items, n_chunks);
+    pg_rows<T><<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, DS, items, f_row, TR, CH, X, ld);
+}
+
+template <typename T>
+void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const T* DS,
+                    const long long* e_row, const long long* f_row, const long long* s_row, T* X, long long ld,
+                    cudaStream_t st) {
+    dim3 grid(B.n_st, (M.F + 255) / 256);
+    pg_rows_es<T><<<grid, 256, 0, st>>>(M, B, d_off, D, DS, e_row, f_row, s_row, X, ld);
 }
 
 template void launch_anlm<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
@@ -553,15 +766,23 @@ template void launch_features_adjoint<double>(const DevModel&, const DevBatch&, 
                                               cudaStream_t);
 template void launch_features_adjoint<float>(const DevModel&, const DevBatch&, const long long*, const double2*,
                                              const long long*, float*, const long long*, void*, int, cudaStream_t);
-template void launch_rows<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
-                                  const long long*, const double*, const long long*, const void*, const RowItem*,
-                                  int, const long long*, int, int, int, double*, long long, double*, cudaStream_t);
-template void launch_rows<float>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
-                                 const long long*, const float*, const long long*, const void*, const RowItem*, int,
-                                 const long long*, int, int, int, float*, long long, double*, cudaStream_t);
-template void launch_rows_reduce<double>(int, int, const int*, const double*, const long long*, const long long*,
-                                         double*, long long, cudaStream_t);
-template void launch_rows_reduce<float>(int, int, const int*, const double*, const long long*, const long long*,
-                                        float*, long long, cudaStream_t);
+template void launch_rows_pairs<double>(const DevModel&, const DevBatch&, const long long*, const int*,
+                                        const double*, const long long*, const long long*, const long long*,
+                                        const void*, const long long*, int*, double*, double*, cudaStream_t);
+template void launch_rows_pairs<float>(const DevModel&, const DevBatch&, const long long*, const int*,
+                                       const double*, const long long*, const long long*, const long long*,
+                                       const void*, const long long*, int*, float*, float*, cudaStream_t);
+template void launch_rows<double>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
+                                  const double*, const double*, const double*, const RowItem*, int,
+                                  const long long*, int, int, int, double*, long long, cudaStream_t);
+template void launch_rows<float>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
+                                 const float*, const float*, const float*, const RowItem*, int, const long long*, int,
+                                 int, int, float*, long long, cudaStream_t);
+template void launch_rows_es<double>(const DevModel&, const DevBatch&, const long long*, const double*,
+                                     const double*, const long long*, const long long*, const long long*, double*,
+                                     long long, cudaStream_t);
+template void launch_rows_es<float>(const DevModel&, const DevBatch&, const long long*, const float*, const float*,
+                                    const long long*, const long long*, const long long*, float*, long long,
+                                    cudaStream_t);
 
 }  // namespace pg
