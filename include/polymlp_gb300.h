@@ -148,6 +148,15 @@ int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
  */
 int pg_batch_residual(pg_gram* g, pg_batch* b, const double* coefs, int n_coef, double* xtr, double* sq,
                       int64_t* n_rows);
+/*
+ * X^T X V (F x n_v, n_v <= 16, column-major, X's own column scaling) of a
+ * staged batch with the rows regenerated at the pg_gram's precision and the
+ * products accumulated in FP64: the exact normal-matrix product that the
+ * preconditioned conjugate-gradient ridge solve of a mixed-precision fit
+ * iterates with.  No reference counterpart (the reference forms X^T X in FP64
+ * and solves directly).
+ */
+int pg_batch_normal_matvec(pg_gram* g, pg_batch* b, const double* v, int n_v, double* out);
 
 /*
  * Ridge solve over alphas in ascending order on the device, as solver_ridge
@@ -158,6 +167,18 @@ int pg_batch_residual(pg_gram* g, pg_batch* b, const double* coefs, int n_coef, 
  */
 int pg_solve_ridge(int n_features, const double* xtx, const double* xty, const double* alphas,
                    int n_alpha, double* coefs, int* info);
+
+/*
+ * The Cholesky factor of xtx + alpha*I kept on the device (factor once, solve
+ * many), the preconditioner of the mixed-precision conjugate-gradient solve.
+ * info != 0 marks a failed factorisation (solves then return 1e30).  The
+ * factorisation is posv's (solvers.py:48-84); keeping it has no reference
+ * counterpart.
+ */
+typedef struct pg_ridge_factor pg_ridge_factor;
+int pg_ridge_factor_create(int n_features, const double* xtx, double alpha, pg_ridge_factor** out, int* info);
+int pg_ridge_factor_solve(pg_ridge_factor* f, const double* rhs, int n_rhs, double* x);
+int pg_ridge_factor_destroy(pg_ridge_factor* f);
 
 /*
  * Ridge solve that allocates no memory.  No counterpart in the reference: it

@@ -258,7 +258,8 @@ __global__ void pg_residual(const T* X, long long ld, long long rows, int F, con
         const double x = (double)X[(size_t)c * ld + r];
         for (int k = 0; k < nc; ++k) acc[k] += x * C[(size_t)k * F + c];
     }
-    for (int k = 0; k < nc; ++k) R[(size_t)k * rows + r] = y[r] - acc[k];
+    const double yr = y ? y[r] : 0.0;  // no targets: R = -X C
+    for (int k = 0; k < nc; ++k) R[(size_t)k * rows + r] = yr - acc[k];
 }
 
 // XtR[c, k] += sum_r X[r, c] R[r, k]  (one block per column)
@@ -452,7 +453,8 @@ struct Gram {
 
     // Weighted residuals of coefficient columns C (F x nc, device) on one batch:
     // XtR += X^T R and sq += per-kind sums of R^2 (rows regenerated on the device).
-    void residual(Prepared& P, const double* C, int nc, double* XtR, double* sq, DevBuf& R) {
+    // Without targets (use_y false) R = -X C, so XtR accumulates -X^T X C.
+    void residual(Prepared& P, const double* C, int nc, double* XtR, double* sq, DevBuf& R, bool use_y = true) {
         const bool fp64 = precision == PG_FP64;
         const long long rows = P.rows;
         Xd.reserve((size_t)rows * F * (fp64 ? 8 : 4));
@@ -464,18 +466,22 @@ struct Gram {
             m->run_rows<double>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
                                 rows, stream);
             pg_scale_rows<double><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
-            pg_residual<double><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc, P.d_y.as<double>(), R.as<double>());
+            pg_residual<double><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc,
+                                                          use_y ? P.d_y.as<double>() : nullptr, R.as<double>());
             pg_xtr<double><<<F, 256, 0, stream>>>(X, rows, rows, F, R.as<double>(), nc, XtR);
         } else {
             float* X = Xd.as<float>();
             m->run_rows<float>(P.b, P.plan, P.d_e.as<long long>(), P.d_f.as<long long>(), P.d_s.as<long long>(), X,
                                rows, stream);
             pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
-            pg_residual<float><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc, P.d_y.as<double>(), R.as<double>());
+            pg_residual<float><<<nblk, 256, 0, stream>>>(X, rows, rows, F, C, nc,
+                                                         use_y ? P.d_y.as<double>() : nullptr, R.as<double>());
             pg_xtr<float><<<F, 256, 0, stream>>>(X, rows, rows, F, R.as<double>(), nc, XtR);
         }
-        dim3 g2(std::min(1024u, nblk), nc);
-        pg_residual_sq<<<g2, 256, 0, stream>>>(R.as<double>(), rows, nc, P.n_e, P.s_end, sq);
+        if (sq) {
+            dim3 g2(std::min(1024u, nblk), nc);
+            pg_residual_sq<<<g2, 256, 0, stream>>>(R.as<double>(), rows, nc, P.n_e, P.s_end, sq);
+        }
         PG_CUDA(cudaGetLastError());
     }
 };
@@ -582,6 +588,24 @@ int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef,
         if (xtr) PG_CUDA(cudaMemcpy(xtr, XtR.as<double>(), (size_t)F * n_coef * 8, cudaMemcpyDeviceToHost));
         if (sq) PG_CUDA(cudaMemcpy(sq, SQ.as<double>(), (size_t)3 * n_coef * 8, cudaMemcpyDeviceToHost));
         if (n_rows) *n_rows = rows;
+    });
+}
+
+int pg_batch_normal_matvec(pg_gram* gh, pg_batch* b, const double* v, int n_v, double* out) {
+    return guarded([&] {
+        if (!gh || !b || !v || !out || n_v < 1) throw std::runtime_error("bad arguments");
+        if (n_v > kMaxCoef) throw std::runtime_error("at most 16 vectors per pass");
+        Gram& g = *gh->g;
+        const int F = g.F;
+        DevBuf V((size_t)F * n_v * 8), XtR((size_t)F * n_v * 8), R;
+        PG_CUDA(cudaMemcpy(V.as<void>(), v, (size_t)F * n_v * 8, cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMemset(XtR.as<void>(), 0, XtR.bytes()));
+        for (auto& P : b->parts) g.residual(*P, V.as<double>(), n_v, XtR.as<double>(), nullptr, R, false);
+        PG_CUDA(cudaStreamSynchronize(g.stream));
+        g.m->check_mirrors();
+        std::vector<double> h((size_t)F * n_v);
+        PG_CUDA(cudaMemcpy(h.data(), XtR.as<double>(), h.size() * 8, cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < h.size(); ++q) out[q] = -h[q];
     });
 }
 

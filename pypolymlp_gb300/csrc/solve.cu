@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -213,6 +214,53 @@ extern "C" int pg_solve_ridge(int F, const double* xtx, const double* xty, const
             PG_CUDA(cudaMemcpy(coefs + (size_t)a * F, x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
         }
     });
+}
+
+// ---------------------------------------------------------------------------
+// Factor once, solve many: the Cholesky factor of xtx + alpha I kept on the
+// device, for preconditioned iterations that apply its inverse repeatedly.
+struct pg_ridge_factor {
+    int F = 0;
+    DevBuf L, b, x, info;
+};
+
+extern "C" int pg_ridge_factor_create(int F, const double* xtx, double alpha, pg_ridge_factor** out, int* info) {
+    return guarded([&] {
+        if (F <= 0 || !xtx || !out || !info) throw std::runtime_error("bad arguments");
+        if ((size_t)F * sizeof(double) > 200 * 1024) throw std::runtime_error("n_features too large for the solver");
+        auto f = std::make_unique<pg_ridge_factor>();
+        f->F = F;
+        DevBuf A0((size_t)F * F * 8);
+        f->L.alloc((size_t)F * F * 8);
+        f->b.alloc((size_t)F * 8);
+        f->x.alloc((size_t)F * 8);
+        f->info.alloc(sizeof(int));
+        PG_CUDA(cudaMemcpy(A0.as<void>(), xtx, (size_t)F * F * 8, cudaMemcpyHostToDevice));
+        pg_add_diag<<<1024, 256, 0, 0>>>(f->L.as<double>(), A0.as<double>(), F, alpha);
+        PG_CUDA(cudaMemset(f->info.as<void>(), 0, sizeof(int)));
+        *info = cholesky_device(f->L.as<double>(), F, f->info.as<int>(), 0);
+        *out = f.release();
+    });
+}
+
+extern "C" int pg_ridge_factor_solve(pg_ridge_factor* f, const double* rhs, int n_rhs, double* x) {
+    return guarded([&] {
+        if (!f || !rhs || !x || n_rhs < 0) throw std::runtime_error("bad arguments");
+        const int F = f->F;
+        const size_t smem = (size_t)F * sizeof(double);
+        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        for (int q = 0; q < n_rhs; ++q) {
+            PG_CUDA(cudaMemcpy(f->b.as<void>(), rhs + (size_t)q * F, (size_t)F * 8, cudaMemcpyHostToDevice));
+            pg_chol_solve<<<1, 1024, smem, 0>>>(f->L.as<double>(), F, f->b.as<double>(), f->x.as<double>(),
+                                               f->info.as<int>());
+            PG_CUDA(cudaGetLastError());
+            PG_CUDA(cudaMemcpy(x + (size_t)q * F, f->x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+extern "C" int pg_ridge_factor_destroy(pg_ridge_factor* f) {
+    return guarded([&] { delete f; });
 }
 
 // ---------------------------------------------------------------------------

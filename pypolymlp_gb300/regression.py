@@ -280,6 +280,101 @@ def solver_ridge(xtx: np.ndarray, xty: np.ndarray, alphas: Sequence[float]) -> n
     return np.asarray(coefs), info
 
 
+class RidgeFactor:
+    """Device Cholesky factor of xtx + alpha I, applied repeatedly (pg_ridge_factor_*)."""
+
+    def __init__(self, xtx: np.ndarray, alpha: float):
+        self.F = xtx.shape[0]
+        A = np.asfortranarray(xtx, dtype=np.float64)
+        h = _ffi._vp()
+        info = C.c_int()
+        _ffi.check(_ffi.lib().pg_ridge_factor_create(self.F, _ffi._p(A, C.c_double), float(alpha), C.byref(h),
+                                                     C.byref(info)))
+        self._h = h
+        self.info = info.value
+
+    def solve(self, rhs: np.ndarray) -> np.ndarray:
+        b = np.asfortranarray(np.atleast_2d(np.asarray(rhs, dtype=np.float64).T).T)
+        x = np.zeros_like(b, order="F")
+        _ffi.check(_ffi.lib().pg_ridge_factor_solve(self._h, _ffi._p(b, C.c_double), b.shape[1],
+                                                    _ffi._p(x, C.c_double)))
+        return x.reshape(np.shape(rhs))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _ffi._lib is not None:
+            _ffi._lib.pg_ridge_factor_destroy(h)
+            self._h = None
+
+
+def normal_matvec(gram: "GramAccumulator", batches: Sequence["DeviceBatch"], v: np.ndarray) -> np.ndarray:
+    """X^T X v (FP64 sums over rows regenerated on the device), v F x k, k <= 16."""
+    v = np.asfortranarray(np.atleast_2d(np.asarray(v, dtype=np.float64).T).T)
+    out = np.zeros_like(v, order="F")
+    for b in batches:
+        o = np.zeros_like(v, order="F")
+        _ffi.check(_ffi.lib().pg_batch_normal_matvec(gram._h, b.handle, _ffi._p(v, C.c_double), v.shape[1],
+                                                     _ffi._p(o, C.c_double)))
+        out += o
+    return out
+
+
+def ridge_pcg(xtx_mixed: np.ndarray, xty: np.ndarray, alphas: np.ndarray, matvec, zero_ids,
+              max_iter: int = 60, rtol: float = 1e-10):
+    """Solve (A + alpha I) c = b for every alpha by conjugate gradients whose
+    products A p come from `matvec` (exact FP64 sums over the rows) and whose
+    preconditioner is the device Cholesky factor of the mixed-precision
+    matrix, shifted by the smallest tau (0, then 1e-9 ... 1e-2 of its mean
+    diagonal) that makes it positive definite.  The mixed Gram's rounding is
+    larger than small alphas, so it cannot be solved directly; this keeps it
+    only as the preconditioner.  Returns (coefs F x n_alpha, iterations,
+    shift per alpha)."""
+    F = xtx_mixed.shape[0]
+    na = len(alphas)
+    dmean = float(np.mean(np.diag(xtx_mixed)))
+    facs, taus = [], []
+    for a in alphas:
+        for t in [0.0] + [dmean * 10.0 ** e for e in range(-9, -1)]:
+            f = RidgeFactor(xtx_mixed, a + t)
+            if f.info == 0:
+                break
+        facs.append(f)
+        taus.append(t)
+    mask = np.ones(F)
+    mask[zero_ids] = 0.0
+    b = (xty * mask)[:, None] * np.ones((1, na))
+
+    def apply_a(p):
+        return (matvec(p * mask[:, None]) + p * alphas[None, :]) * mask[:, None]
+
+    def precond(r):
+        return np.stack([facs[k].solve(r[:, k]) for k in range(na)], axis=1) * mask[:, None]
+
+    x = precond(b)
+    r = b - apply_a(x)
+    z = precond(r)
+    p = z.copy()
+    rz = np.einsum("ij,ij->j", r, z)
+    bn = np.linalg.norm(b, axis=0)
+    it = 0
+    active = np.ones(na, dtype=bool)
+    for it in range(1, max_iter + 1):
+        q = apply_a(p)
+        pq = np.einsum("ij,ij->j", p, q)
+        step = np.where(active & (pq > 0), rz / np.where(pq > 0, pq, 1.0), 0.0)
+        x += p * step[None, :]
+        r -= q * step[None, :]
+        active &= np.linalg.norm(r, axis=0) > rtol * bn
+        if not active.any():
+            break
+        z = precond(r)
+        rz_new = np.einsum("ij,ij->j", r, z)
+        beta = np.where(active, rz_new / np.where(rz != 0, rz, 1.0), 0.0)
+        p = z + p * beta[None, :]
+        rz = rz_new
+    return x, it, np.array(taus)
+
+
 def compute_rmse_seq(coefs_array, data_xy: DataXY, check_singular=False, error_threshold=1e6):
     out = []
     for c in coefs_array.T:
@@ -325,6 +420,8 @@ class FitResult:
     rmse_train_array: np.ndarray = field(repr=False, default=None)
     rmse_test_array: np.ndarray = field(repr=False, default=None)
     info: np.ndarray = field(repr=False, default=None)
+    cg_iterations: int = 0                 # conjugate-gradient iterations (mixed path)
+    shifts: np.ndarray = field(repr=False, default=None)  # preconditioner shift per alpha
 
     @property
     def scaled_coeffs(self):
@@ -337,14 +434,16 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
         weight_stress: float = 0.1) -> FitResult:
     """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60).
 
-    The Gram is assembled once (mixed or FP64); the ridge systems are solved
-    in FP64; with the mixed Gram, `refine` FP64 iterative-refinement steps
-    c <- c + (A + alpha I)^-1 (S^-1 X^T (y - X S^-1 c) - alpha c) use residuals
-    of freshly generated rows.  RMSEs are computed from residuals (weighted
-    rows, as the reference's Gram-based formula defines them)."""
+    The Gram is assembled once (mixed or FP64).  FP64: the ridge systems are
+    solved directly (device Cholesky, as posv).  Mixed: the mixed Gram only
+    preconditions a conjugate-gradient solve whose matrix products are FP64
+    sums over freshly generated rows (`refine` caps the iterations; default
+    60, stopping at a relative residual of 1e-10).  RMSEs are computed from
+    residuals (weighted rows, as the reference's Gram-based formula defines
+    them)."""
     model = model or _ffi.Model(params_dict)
     if refine is None:
-        refine = 1 if precision == _ffi.PG_MIXED else 0
+        refine = 60 if precision == _ffi.PG_MIXED else 0
     alphas = np.asarray(alphas, dtype=np.float64)
     min_e = get_min_energy(train)
     tb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in train]
@@ -360,28 +459,18 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
     xtx /= scales[:, None]
     xtx /= scales[None, :]
     xty /= scales
-    coefs, info = solver_ridge(xtx, xty, alphas)
-    # ridge objective of every alpha from residuals (FP64 sums): |r|^2 + alpha |c|^2
-    xtr, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
-    obj = sq.sum(axis=0) + alphas * np.square(coefs).sum(axis=0)
-    for _ in range(refine):
-        # refinement step, kept only where it lowers the objective: with a mixed
-        # Gram, (A + alpha I)^-1 dA can exceed 1 for small alpha and the plain
-        # iteration would diverge
-        g = xtr / scales[:, None] - coefs * alphas[None, :]
-        g[zero_ids] = 0.0
-        trial = coefs.copy()
-        for k, a in enumerate(alphas):
-            if info[k] == 0:
-                d, _ = solver_ridge(xtx, g[:, k], [a])
-                trial[:, k] += d[:, 0]
-        xtr2, sq2, _ = batch_residual(gram, tb, trial / scales[:, None])
-        obj2 = sq2.sum(axis=0) + alphas * np.square(trial).sum(axis=0)
-        better = obj2 < obj
-        coefs[:, better] = trial[:, better]
-        xtr[:, better] = xtr2[:, better]
-        sq[:, better] = sq2[:, better]
-        obj[better] = obj2[better]
+    n_iter, shifts = 0, np.zeros(len(alphas))
+    if precision == _ffi.PG_FP64 and not refine:
+        coefs, info = solver_ridge(xtx, xty, alphas)
+    else:
+        # The mixed Gram preconditions a conjugate-gradient solve whose
+        # products X^T X p are exact FP64 sums over freshly generated rows.
+        def matvec(v):
+            return normal_matvec(gram, tb, v / scales[:, None]) / scales[:, None]
+
+        coefs, n_iter, shifts = ridge_pcg(xtx, xty, alphas, matvec, zero_ids, max_iter=max(1, refine))
+        info = np.zeros(len(alphas), dtype=np.int32)
+    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
     rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
     if np.all(rmse_train > 1e6):
         raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
@@ -392,4 +481,4 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
     rmse_test = np.sqrt(sq.sum(axis=0) / n_te)
     idx = int(np.argmin(rmse_test))
     return FitResult(coefs[:, idx], scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
-                     coefs, rmse_train, rmse_test, info)
+                     coefs, rmse_train, rmse_test, info, n_iter, shifts)

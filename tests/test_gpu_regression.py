@@ -100,9 +100,10 @@ def _energy_force_rmse(params, coefs_unscaled, datasets):
 
 def test_fit_mixed_vs_fp64_rmse():
     """End-to-end fit.  FP64 GPU path: test RMSEs of every alpha equal the CPU
-    pipeline's (Gram formula, LAPACK posv) to 1e-6.  Mixed path (BF16x3 Gram,
-    FP64 Cholesky + one refinement step): the selected model's energy RMSE
-    within 0.05 meV/atom and force RMSE within 1 meV/A of the FP64 fit."""
+    pipeline's (Gram formula, LAPACK posv) to 1e-6.  Mixed path (BF16x3 Gram as
+    the preconditioner of a conjugate-gradient solve with FP64 normal-matrix
+    products): the selected model's energy RMSE within 0.05 meV/atom and force
+    RMSE within 1 meV/A of the FP64 fit."""
     from pypolymlp_gb300 import _ffi
     from pypolymlp_gb300.regression import compute_rmse_seq, fit
 
@@ -119,6 +120,7 @@ def test_fit_mixed_vs_fp64_rmse():
     e64, f64 = _energy_force_rmse(p, r64.scaled_coeffs, test)
     e32, f32 = _energy_force_rmse(p, r32.scaled_coeffs, test)
     print(f"fp64: alpha {r64.alpha} rmse_test {r64.rmse_test_array}; E {e64 * 1e3:.4f} meV/atom F {f64 * 1e3:.3f} meV/A")
-    print(f"mixed: alpha {r32.alpha} rmse_test {r32.rmse_test_array}; E {e32 * 1e3:.4f} meV/atom F {f32 * 1e3:.3f} meV/A")
+    print(f"mixed: alpha {r32.alpha} rmse_test {r32.rmse_test_array}; E {e32 * 1e3:.4f} meV/atom F {f32 * 1e3:.3f} meV/A"
+          f"; cg iterations {r32.cg_iterations}, shifts {r32.shifts}")
     assert abs(e32 - e64) < 0.05e-3, (e32, e64)
     assert abs(f32 - f64) < 1e-3, (f32, f64)
