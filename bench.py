@@ -142,6 +142,43 @@ def cpu_baseline(params, data, sample, n_threads):
     return xy.total_n_data / dt, dt, xy.total_n_data
 
 
+def eval_bench(params, args):
+    """E/F/S atoms/s of the evaluator (pg_eval_run through the C ABI, host
+    buffers, neighbour lists included) on a bcc cell of n^3 x 2 atoms
+    (a = 3.2 A, sigma 0.1 A, 50/50 random species) with the X^T X model,
+    mixed precision; kernel times from the device profiler."""
+    import torch
+
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300 import synthetic as syn
+    from pypolymlp_gb300.abi import Structures
+
+    n = args.eval_cell
+    sset = syn.bcc_supercell(n, a=3.2, sigma=0.1, seed=4)
+    st = Structures(sset.axis, sset.positions, sset.types)
+    n_atoms = int(st.n_atoms.sum())
+    coefs = np.random.default_rng(4).normal(size=_ffi.Model(params).n_features) * 1e-3
+    ev = _ffi.Evaluator(params, coefs, _ffi.PG_MIXED)
+    ev.run(st)  # warm-up
+    torch.cuda.synchronize()
+    reps = 3
+    _ffi.profile_enable(True)
+    _ffi.profile_read()
+    t0 = time.time()
+    for _ in range(reps):
+        ev.run(st)
+    dt = (time.time() - t0) / reps
+    prof = _ffi.profile_read()
+    _ffi.profile_enable(False)
+    dev_ms = sum(v[0] for v in prof.values()) / reps
+    return {"metric": "E/F/S atoms/s (mixed)", "value": n_atoms / dt, "unit": "atoms/s",
+            "device_atoms_per_s": n_atoms / (dev_ms / 1e3) if dev_ms > 0 else None,
+            "workload": f"bcc {n}x{n}x{n}x2 = {n_atoms} atoms, a 3.2 A, the X^T X model (F = {len(coefs)})",
+            "h2d_bytes": int(st.positions.nbytes + st.axis.nbytes + st.types.nbytes),
+            "d2h_bytes": int(n_atoms * 24 + 56),
+            "kernels": {k: {"ms": v[0] / reps, "launches": v[1] // reps} for k, v in prof.items()}}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -184,6 +221,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64", action="store_true", help="time the FP64 judge path instead")
+    ap.add_argument("--no-eval", action="store_true", help="skip the E/F/S evaluation figure")
+    ap.add_argument("--eval-cell", type=int, default=20, help="bcc repeats n (n^3 x 2 atoms) of the E/F/S cell")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -252,12 +291,19 @@ def main():
     step()
     prof = _ffi.profile_read()
     _ffi.profile_enable(False)
-    launches_per_step = sum(v[1] for v in prof.values()) + 4  # + energy stats, row scaling, X^T y, symmetrize
-    # dominant kernel and its roofline
+    # + per batch: prefix scan, energy-row statistics, row weighting, X^T y (not individually timed)
+    launches_per_step = sum(v[1] for v in prof.values()) + 4 * prof.get("pg_nb_count", (0, 1))[1]
+    # dominant kernel and its roofline.  X-row kernels (neighbours to rows) are
+    # accounted per X row as F x 4 B written + F x 4 B read by the Gram (FP64: x 2),
+    # HBM-bound; the Gram per X row as F (F + 1) flops on the tensor cores.
     hbm_gbs, bf16_tf, peak_kind = measured_peaks()
     dom = max(prof.items(), key=lambda kv: kv[1][0])
     dname, (dms, dn) = dom
     per_launch_s = dms / dn / 1e3
+    row_kernels = ("pg_nb_count", "pg_nb_fill", "pg_nb_mirror", "pg_anlm", "pg_features_adjoint", "pg_rows_pairs",
+                   "pg_rows", "pg_rows_es")
+    xrow_ms = sum(prof[k][0] for k in row_kernels if k in prof)
+    tb = 4 if precision == _ffi.PG_MIXED else 8
     if dname.startswith("pg_gram"):
         flops = F * (F + 1) * rows_per_step / dn
         achieved = flops / per_launch_s / 1e12
@@ -266,12 +312,15 @@ def main():
                 "frac": achieved / peak if peak else None, "traffic": None,
                 "note": f"peak = {peak_kind} bf16 dense / 3 (three split products)"}
     else:
-        bytes_ = F * (4 if precision == _ffi.PG_MIXED else 8) * rows_per_step / dn
+        bytes_ = 2 * F * tb * rows_per_step / dn
         achieved = bytes_ / per_launch_s / 1e9
+        sub = 2 * F * tb * rows_per_step / (xrow_ms / 1e3) / 1e9
         roof = {"kernel": dname, "bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
                 "frac": achieved / hbm_gbs, "traffic": None,
-                "note": f"algorithmic bytes = F x {4 if precision == _ffi.PG_MIXED else 8} B per X row written; "
-                        f"peak {peak_kind}"}
+                "xrow_subpath": {"kernels": [k for k in row_kernels if k in prof], "ms_per_step": xrow_ms,
+                                 "achieved": sub, "frac": sub / hbm_gbs},
+                "note": f"algorithmic bytes = F x {tb} B written + F x {tb} B read per X row (the X tile); "
+                        f"peak {peak_kind} copy bandwidth; DRAM traffic of the kernel from ncu is in profiles/"}
     kernels = {k: {"ms_per_step": v[0], "launches": v[1]} for k, v in prof.items()}
 
     # e2e through the C ABI with host buffers (one pass; host prep + H2D + D2H inside)
@@ -292,6 +341,8 @@ def main():
     e2e = {"value": n_rows * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h)}
     del res
+
+    ev = eval_bench(params, args) if not args.no_eval else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -316,6 +367,7 @@ def main():
             "kernels": kernels,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "eval": ev,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
