@@ -138,6 +138,16 @@ int pg_batch_create(pg_model* m, const pg_structures* st, const int64_t* e_row, 
 int pg_batch_destroy(pg_batch* b);
 int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
 /*
+ * X^T X of one host block X (n_rows x n_features, column-major, leading
+ * dimension ld), on the device: the `xtx += x.T @ x` of calc_xtx_xty
+ * (mlp_dev/core/data_sequential.py:145-152) for a block that is already
+ * materialised.  PG_FP64: FP64 products and sums; PG_MIXED: X rounded to FP32,
+ * BF16x3 products on the tensor cores, FP32 partial sums flushed to FP64 every
+ * 4,096 rows.  xtx is F x F (full, symmetric).
+ */
+int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int precision, double* xtx);
+
+/*
  * Weighted residuals R = y - X C of a staged batch for n_coef (<= 16)
  * coefficient vectors C (F x n_coef, column-major, in X's own column scaling),
  * with the rows regenerated at the pg_gram's precision and accumulated in

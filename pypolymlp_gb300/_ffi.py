@@ -62,6 +62,7 @@ def lib():
                 ("pg_gram_accumulate_batch", [_vp, _vp]),
                 ("pg_batch_residual", [_vp, _vp, _dp, C.c_int, _dp, _dp, _i64p]),
                 ("pg_batch_normal_matvec", [_vp, _vp, _dp, C.c_int, _dp]),
+                ("pg_gram_xtx", [_dp, C.c_int64, C.c_int, C.c_int64, C.c_int, _dp]),
                 ("pg_ridge_factor_create", [C.c_int, _dp, C.c_double, C.POINTER(_vp), _ip]),
                 ("pg_ridge_factor_solve", [_vp, _dp, C.c_int, _dp]),
                 ("pg_ridge_factor_destroy", [_vp]),
@@ -175,6 +176,16 @@ def neighbor_list(st: Structures, s: int, cutoff: float):
     check(L.pg_neighbor_list(C.cast(st.ref(), _vp), s, cutoff, 0, C.byref(n), _p(offs, C.c_int), _p(nb, C.c_int),
                              _p(d, C.c_double)))
     return offs, nb[:n.value], d[:n.value]
+
+
+def gram_xtx(x: np.ndarray, precision: int = PG_MIXED) -> np.ndarray:
+    """X^T X of a host block on the device (pg_gram_xtx)."""
+    require_device()
+    x = np.asfortranarray(x, dtype=np.float64)
+    n, F = x.shape
+    out = np.zeros((F, F), order="F")
+    check(lib().pg_gram_xtx(_p(x, C.c_double), n, F, max(n, 1), int(precision), _p(out, C.c_double)))
+    return out
 
 
 def profile_enable(on: bool = True):

@@ -22,7 +22,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libpolymlp_gb300.so")
 
-CU_SOURCES = ["xrows.cu", "capi.cu", "gram.cu", "solve.cu", "eval.cu"]
+CU_SOURCES = ["xrows.cu", "capi.cu", "gram.cu", "gram_tc.cu", "solve.cu", "eval.cu"]
 CPP_SOURCES = ["host/model_tables.cpp", "host/params.cpp", "host/cell.cpp", "host/flat_tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

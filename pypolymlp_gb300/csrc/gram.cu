@@ -21,6 +21,7 @@
 
 namespace pg {
 
+
 // ------------------------------------------------------------ statistics
 // xe_sum[c] += sum_r X[e_rows[r], c], xe_sq_sum[c] += sum X^2 (unweighted energy rows).
 template <typename T>
@@ -387,6 +388,7 @@ struct Gram {
     int precision;
     int F;
     DevBuf G, xty, xe_sum, xe_sq, tiles64, tiles128, Xd;
+    GramTcScratch tc;
     int n_tiles64 = 0, n_tiles128 = 0;
     double yty = 0;
     long long n_rows_total = 0;
@@ -443,8 +445,8 @@ struct Gram {
                                                                        xe_sum.as<double>(), xe_sq.as<double>());
             pg_scale_rows<float><<<sg, 256, 0, stream>>>(X, rows, rows, F, P.d_w.as<double>());
             pg_xty<float><<<F, 256, 0, stream>>>(X, rows, rows, P.d_y.as<double>(), xty.as<double>());
-            ProfScope ps("pg_gram_bf16x3", stream);
-            launch_gram_bf16x3(X, rows, rows, F, tiles128.as<int2>(), n_tiles128, G.as<double>(), stream);
+            ProfScope ps("pg_gram_tc", stream);
+            gram_tc_accumulate(X, rows, rows, F, G.as<double>(), tc, stream);
         }
         PG_CUDA(cudaGetLastError());
         yty += P.yty;
@@ -500,6 +502,45 @@ struct pg_batch {
 
 extern "C" {
 
+__global__ void pg_f64_to_f32(const double* src, float* dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int precision, double* xtx) {
+    return guarded([&] {
+        if (!x || !xtx || n_rows < 0 || n_features <= 0 || ld < n_rows) throw std::runtime_error("bad arguments");
+        if (precision != PG_FP64 && precision != PG_MIXED) throw std::runtime_error("unknown precision");
+        const int F = n_features;
+        cudaStream_t st = 0;
+        DevBuf X64((size_t)std::max<int64_t>(1, n_rows) * F * 8), G((size_t)F * F * 8);
+        PG_CUDA(cudaMemset(G.as<void>(), 0, G.bytes()));
+        if (n_rows > 0)
+            PG_CUDA(cudaMemcpy2D(X64.as<void>(), (size_t)n_rows * 8, x, (size_t)ld * 8, (size_t)n_rows * 8, F,
+                                 cudaMemcpyHostToDevice));
+        if (n_rows > 0 && precision == PG_FP64) {
+            const int nt = (F + kS64 - 1) / kS64;
+            std::vector<int2> t;
+            for (int j = 0; j < nt; ++j)
+                for (int i = 0; i <= j; ++i) t.push_back(make_int2(i, j));
+            DevBuf tiles;
+            upload(tiles, t);
+            launch_syrk_f64(X64.as<double>(), n_rows, n_rows, F, tiles.as<int2>(), (int)t.size(), G.as<double>(), st);
+        } else if (n_rows > 0) {
+            DevBuf X32((size_t)n_rows * F * 4);
+            pg_f64_to_f32<<<1024, 256, 0, st>>>(X64.as<double>(), X32.as<float>(), (size_t)n_rows * F);
+            GramTcScratch tc;
+            gram_tc_accumulate(X32.as<float>(), n_rows, n_rows, F, G.as<double>(), tc, st);
+            PG_CUDA(cudaStreamSynchronize(st));
+            gram_tc_check(tc);
+        }
+        dim3 grid((F + 255) / 256, F);
+        pg_symmetrize<<<grid, 256, 0, st>>>(G.as<double>(), F);
+        PG_CUDA(cudaGetLastError());
+        PG_CUDA(cudaMemcpy(xtx, G.as<double>(), (size_t)F * F * 8, cudaMemcpyDeviceToHost));
+    });
+}
+
 int pg_gram_create(pg_model* m, int precision, pg_gram** out) {
     return guarded([&] {
         if (!m || !out) throw std::runtime_error("null argument");
@@ -535,6 +576,7 @@ int pg_gram_accumulate(pg_gram* gh, const pg_structures* st, const int64_t* e_ro
         for (auto& P : parts) g.accumulate(*P);
         PG_CUDA(cudaStreamSynchronize(g.stream));
         g.m->check_mirrors();
+        gram_tc_check(g.tc);
     });
 }
 
@@ -620,6 +662,7 @@ int pg_gram_result(pg_gram* gh, double* xtx, double* xty, double* yty, double* x
         PG_CUDA(cudaGetLastError());
         PG_CUDA(cudaStreamSynchronize(g.stream));
         g.m->check_mirrors();
+        gram_tc_check(g.tc);
         if (xtx) PG_CUDA(cudaMemcpy(xtx, g.G.as<double>(), (size_t)F * F * sizeof(double), cudaMemcpyDeviceToHost));
         if (xty) PG_CUDA(cudaMemcpy(xty, g.xty.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
         if (xe_sum) PG_CUDA(cudaMemcpy(xe_sum, g.xe_sum.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));

@@ -57,4 +57,15 @@ void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off
                     const long long* e_row, const long long* f_row, const long long* s_row, T* X, long long ld,
                     cudaStream_t st);
 
+// Tensor-core Gram (gram_tc.cu): scratch (BF16 halves of X, work units,
+// partial tiles of the row splits, error flag) and entry points.
+struct GramTcScratch {
+    DevBuf H, L, units, P, err;
+    int n_units = 0, n_splits = 0, F = 0;
+    long long rows = -1;
+};
+void gram_tc_accumulate(const float* X, long long ld, long long rows, int F, double* G, GramTcScratch& S,
+                        cudaStream_t st);
+void gram_tc_check(GramTcScratch& S);
+
 }  // namespace pg
