@@ -9,7 +9,8 @@ model_type 3, max_p 2 (F = 2,618 columns, ~1.3 M rows).
 One step = one pass of the hot path over the whole dataset: neighbour lists,
 a_nlm, invariant features and their force/stress derivatives (X rows, FP32
 features with FP64 neighbour sums), row weighting, X^T y, and X^T X on the
-tensor cores (BF16x3 split products, FP32 accumulation flushed into FP64).
+tcgen05 tensor cores (BF16x3 split products, FP32 accumulation in TMEM flushed into
+FP64).
 
   value : rows/s with the structures, weights and targets resident in HBM.
   e2e   : rows/s through the C ABI with host buffers (pg_gram_accumulate: host
@@ -307,7 +308,7 @@ def main():
     if dname.startswith("pg_gram"):
         flops = F * (F + 1) * rows_per_step / dn
         achieved = flops / per_launch_s / 1e12
-        peak = bf16_tf / 3.0 if dname == "pg_gram_bf16x3" else None
+        peak = bf16_tf / 3.0 if dname == "pg_gram_tc" else None
         roof = {"kernel": dname, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": None,
                 "note": f"peak = {peak_kind} bf16 dense / 3 (three split products)"}
@@ -321,6 +322,12 @@ def main():
                                  "achieved": sub, "frac": sub / hbm_gbs},
                 "note": f"algorithmic bytes = F x {tb} B written + F x {tb} B read per X row (the X tile); "
                         f"peak {peak_kind} copy bandwidth; DRAM traffic of the kernel from ncu is in profiles/"}
+    if "pg_gram_tc" in prof and not dname.startswith("pg_gram"):
+        gms, gn = prof["pg_gram_tc"]
+        g_ach = F * (F + 1) * rows_per_step / (gms / 1e3) / 1e12
+        roof["gram"] = {"kernel": "pg_gram_tc", "bound": "tensor", "achieved": g_ach, "peak": bf16_tf / 3.0,
+                        "unit": "TFLOP/s", "frac": g_ach / (bf16_tf / 3.0),
+                        "note": f"F(F+1) flops per X row; peak = {peak_kind} bf16 dense / 3 (three split products)"}
     kernels = {k: {"ms_per_step": v[0], "launches": v[1]} for k, v in prof.items()}
 
     # e2e through the C ABI with host buffers (one pass; host prep + H2D + D2H inside)

@@ -5,10 +5,9 @@
 //
 //   pg_syrk_f64        FP64 judge path: upper-triangle tiles of X^T X on the
 //                      CUDA cores (64x64 tile per block, 4x4 per thread).
-//   pg_gram_bf16x3     mixed path: X (FP32) split into bf16 hi + lo, and
-//                      X^T X ~= hi^T hi + hi^T lo + lo^T hi accumulated in FP32
-//                      on the tensor cores, flushed into the FP64 Gram every
-//                      kFlushRows rows.
+//   gram_tc (file gram_tc.cu) mixed path: X (FP32) split into bf16 hi + lo,
+//                      X^T X ~= hi^T hi + hi^T lo + lo^T hi on the tcgen05
+//                      tensor cores, FP32 segments flushed into the FP64 Gram.
 //   helpers            energy-row sums, row weighting, X^T y.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -110,119 +109,6 @@ __global__ void __launch_bounds__(256) pg_syrk_f64(const double* X, long long ld
         }
 }
 
-// ------------------------------------------------------------ BF16x3 (mma.sync)
-constexpr int kT = 128;        // output tile (features x features)
-constexpr int kKc = 32;        // rows per k-chunk
-constexpr int kPad = 8;        // bf16 padding per smem row (bank spread)
-constexpr long long kFlushRows = 8192;
-
-__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-
-__device__ __forceinline__ void ldsm_x2(unsigned (&r)[2], const void* p) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
-}
-
-// 256 threads, 8 warps as 2 (M) x 4 (N); each warp 64 x 32 of the 128 x 128 tile.
-__global__ void __launch_bounds__(256) pg_gram_bf16x3(const float* X, long long ld, long long n_rows, int F,
-                                                      const int2* tiles, double* G) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int RS = kKc + kPad;  // row stride (bf16 elements)
-    __nv_bfloat16* Ah = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    __nv_bfloat16* Al = Ah + kT * RS;
-    __nv_bfloat16* Bh = Al + kT * RS;
-    __nv_bfloat16* Bl = Bh + kT * RS;
-    const int2 tl = tiles[blockIdx.x];
-    const int i0 = tl.x * kT, j0 = tl.y * kT;
-    const bool diag = tl.x == tl.y;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = warp >> 2, wn = warp & 3;  // warp tile origin: (wm*64, wn*32)
-    float acc[4][4][4];                       // [m16 block][n8 block][frag]
-    for (int a = 0; a < 4; ++a)
-        for (int b = 0; b < 4; ++b)
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-    long long since_flush = 0;
-    for (long long k0 = 0; k0 < n_rows; k0 += kKc) {
-        // load 128 columns x 32 rows for A (columns i0..) and B (j0..), split into hi/lo
-        for (int q = threadIdx.x; q < kT * kKc; q += 256) {
-            const int kk = q % kKc, cc = q / kKc;
-            const long long r = k0 + kk;
-            const int ci = i0 + cc;
-            const float va = (r < n_rows && ci < F) ? X[(size_t)ci * ld + r] : 0.f;
-            const __nv_bfloat16 ha = __float2bfloat16_rn(va);
-            Ah[cc * RS + kk] = ha;
-            Al[cc * RS + kk] = __float2bfloat16_rn(va - __bfloat162float(ha));
-            if (!diag) {
-                const int cj = j0 + cc;
-                const float vb = (r < n_rows && cj < F) ? X[(size_t)cj * ld + r] : 0.f;
-                const __nv_bfloat16 hb = __float2bfloat16_rn(vb);
-                Bh[cc * RS + kk] = hb;
-                Bl[cc * RS + kk] = __float2bfloat16_rn(vb - __bfloat162float(hb));
-            }
-        }
-        __syncthreads();
-        const __nv_bfloat16* BH = diag ? Ah : Bh;
-        const __nv_bfloat16* BL = diag ? Al : Bl;
-#pragma unroll
-        for (int ks = 0; ks < kKc; ks += 16) {
-            unsigned ah[4][4], al[4][4], bh[4][2], bl[4][2];
-#pragma unroll
-            for (int mi = 0; mi < 4; ++mi) {
-                const int row = wm * 64 + mi * 16 + (lane & 15);
-                const int col = ks + ((lane >> 4) << 3);
-                ldsm_x4(ah[mi], Ah + row * RS + col);
-                ldsm_x4(al[mi], Al + row * RS + col);
-            }
-#pragma unroll
-            for (int ni = 0; ni < 4; ++ni) {
-                const int row = wn * 32 + ni * 8 + (lane & 7);
-                const int col = ks + (((lane >> 3) & 1) << 3);
-                ldsm_x2(bh[ni], BH + row * RS + col);
-                ldsm_x2(bl[ni], BL + row * RS + col);
-            }
-#pragma unroll
-            for (int mi = 0; mi < 4; ++mi)
-#pragma unroll
-                for (int ni = 0; ni < 4; ++ni) {
-                    mma_bf16_16816(acc[mi][ni], al[mi], bh[ni]);
-                    mma_bf16_16816(acc[mi][ni], ah[mi], bl[ni]);
-                    mma_bf16_16816(acc[mi][ni], ah[mi], bh[ni]);
-                }
-        }
-        __syncthreads();
-        since_flush += kKc;
-        const bool last = k0 + kKc >= n_rows;
-        if (since_flush >= kFlushRows || last) {
-            // flush the FP32 partial sums into the FP64 Gram (this block owns the tile)
-#pragma unroll
-            for (int mi = 0; mi < 4; ++mi)
-#pragma unroll
-                for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const int i = i0 + wm * 64 + mi * 16 + (lane >> 2) + ((c >> 1) << 3);
-                        const int j = j0 + wn * 32 + ni * 8 + ((lane & 3) << 1) + (c & 1);
-                        if (i < F && j < F && i <= j) G[(size_t)j * F + i] += (double)acc[mi][ni][c];
-                        acc[mi][ni][c] = 0.f;
-                    }
-            since_flush = 0;
-        }
-    }
-}
-
 // Mirror the upper triangle into the lower one.
 __global__ void pg_symmetrize(double* G, int F) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,14 +121,7 @@ void launch_syrk_f64(const double* X, long long ld, long long n_rows, int F, con
     pg_syrk_f64<<<n_tiles, 256, 0, st>>>(X, ld, n_rows, F, tiles, G);
 }
 
-size_t gram_bf16_smem() { return (size_t)4 * kT * (kKc + kPad) * sizeof(__nv_bfloat16); }
 
-void launch_gram_bf16x3(const float* X, long long ld, long long n_rows, int F, const int2* tiles, int n_tiles,
-                        double* G, cudaStream_t st) {
-    const size_t smem = gram_bf16_smem();
-    PG_CUDA(cudaFuncSetAttribute(pg_gram_bf16x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pg_gram_bf16x3<<<n_tiles, 256, smem, st>>>(X, ld, n_rows, F, tiles, G);
-}
 
 // ------------------------------------------------------------ residuals
 constexpr int kMaxCoef = 16;
@@ -387,9 +266,9 @@ struct Gram {
     Model* m;
     int precision;
     int F;
-    DevBuf G, xty, xe_sum, xe_sq, tiles64, tiles128, Xd;
+    DevBuf G, xty, xe_sum, xe_sq, tiles64, Xd;
     GramTcScratch tc;
-    int n_tiles64 = 0, n_tiles128 = 0;
+    int n_tiles64 = 0;
     double yty = 0;
     long long n_rows_total = 0;
     cudaStream_t stream = 0;
@@ -409,7 +288,6 @@ struct Gram {
             n = (int)t.size();
         };
         tile_list(kS64, tiles64, n_tiles64);
-        tile_list(kT, tiles128, n_tiles128);
     }
 
     void reset() {
