@@ -135,25 +135,26 @@ void DeviceModel::build(const FlatModel& fm, size_t smem_target, bool fp64) {
         }
         d.col_info = (const int4*)up(info);
         d.ent_tp_off = (const int*)up(ft.ent_tp_off);
-        std::vector<int> nk(ft.ent_head.size());
-        for (size_t e = 0; e < ft.ent_head.size(); ++e) {
-            const int h = ft.ent_head[e];
-            if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
-                throw std::runtime_error("model too large for the packed entry indices");
-            nk[e] = ft.head_nid[h] | (ft.head_key[h] << 8);
-        }
-        d.ent_nk = (const int*)up(nk);
-        std::vector<int> hpos(ft.K0, -1), tnk(ft.tp_heads.size());
+        std::vector<int> tnk(ft.tp_heads.size());
         for (int tp = 0; tp < fm.n_tp; ++tp)
             for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q) {
                 const int h = ft.tp_heads[q];
-                hpos[h] = q - ft.tp_head_off[tp];
+                if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
+                    throw std::runtime_error("model too large for the packed head indices");
                 tnk[q] = ft.head_nid[h] | (ft.head_key[h] << 8);
             }
-        std::vector<int> ehpos(ft.ent_head.size());
-        for (size_t e = 0; e < ft.ent_head.size(); ++e) ehpos[e] = hpos[ft.ent_head[e]];
         d.tp_head_nk = (const int*)up(tnk);
-        d.ent_hpos = (const int*)up(ehpos);
+        d.n_groups = ft.n_groups;
+        d.lay_size = ft.lay_size;
+        d.n_tpl = (int)ft.tpl_tp.size();
+        d.lay_ent = (const int*)up(ft.lay_ent);
+        d.lay_hpos = (const int*)up(ft.lay_hpos);
+        d.lay_grp_base = (const int*)up(ft.lay_grp_base);
+        d.lay_grp_cnt = (const int*)up(ft.lay_grp_cnt);
+        d.tp_perm = (const int*)up(ft.tp_perm);
+        d.tp_ipos = (const int*)up(ft.tp_ipos);
+        d.tpl = (const int*)up(ft.tpl);
+        d.tpl_tp = (const int*)up(ft.tpl_tp);
         d.tp_head_off = (const int*)up(ft.tp_head_off);
         d.tp_heads = (const int*)up(ft.tp_heads);
     }
@@ -268,23 +269,26 @@ Model::Model(const pg_feature_params* p)
 }
 
 // Per-atom storage offsets (a_nlm, features, adjoint entries) of a staged batch.
-void Model::atom_offsets(const DeviceBatch& b, size_t t_size, std::vector<long long>& a_off,
-                         std::vector<long long>& d_off, std::vector<long long>& g_off, long long& a_tot,
-                         long long& d_tot, long long& g_tot) const {
-    a_off.resize(b.n_atoms);
-    d_off.resize(b.n_atoms);
-    g_off.resize(b.n_atoms);
-    a_tot = d_tot = g_tot = 0;
+// Per-atom storage offsets of a staged batch: a_nlm (K0), features (n_lin),
+// adjoint entries in the X-row layout (lay_size), self/virial vectors
+// (9 x n_lin per type pair of the centre type).
+void Model::atom_offsets(const DeviceBatch& b, AtomOffsets& o) const {
+    o.a_off.resize(b.n_atoms);
+    o.d_off.resize(b.n_atoms);
+    o.g_off.resize(b.n_atoms);
+    o.s_off.resize(b.n_atoms);
+    o.a_tot = o.d_tot = o.g_tot = o.s_tot = 0;
     for (int i = 0; i < b.n_atoms; ++i) {
         const auto& ft = flat.types[b.types[i]];
-        a_off[i] = a_tot;
-        d_off[i] = d_tot;
-        g_off[i] = g_tot;
-        a_tot += ft.K0;
-        d_tot += ft.n_lin;
-        g_tot += (long long)ft.ent_head.size();
+        o.a_off[i] = o.a_tot;
+        o.d_off[i] = o.d_tot;
+        o.g_off[i] = o.g_tot;
+        o.s_off[i] = o.s_tot;
+        o.a_tot += ft.K0;
+        o.d_tot += ft.n_lin;
+        o.g_tot += ft.lay_size;
+        o.s_tot += 9LL * ft.n_lin * (long long)ft.tpl_tp.size();
     }
-    (void)t_size;
 }
 
 size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
@@ -292,7 +296,8 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
     size_t mx = 0;
     for (const auto& ft : flat.types) {
         // a_nlm, features, self/virial vectors (9 per feature) and G
-        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts * 10 + ft.ent_head.size() * 2 * ts;
+        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts * (1 + 9 * ft.tpl_tp.size()) +
+                         (size_t)ft.lay_size * 2 * ts;
         mx = std::max(mx, b);
     }
     size_t max_lin = 1;
@@ -303,11 +308,16 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
 
 // Per-batch plan: per-atom storage offsets and pg_rows work items.
 void Model::plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const {
-    std::vector<long long> a_off, d_off, g_off;
-    atom_offsets(b, 0, a_off, d_off, g_off, plan.a_tot, plan.d_tot, plan.g_tot);
-    upload(plan.d_a_off, a_off);
-    upload(plan.d_d_off, d_off);
-    upload(plan.d_g_off, g_off);
+    AtomOffsets o;
+    atom_offsets(b, o);
+    plan.a_tot = o.a_tot;
+    plan.d_tot = o.d_tot;
+    plan.g_tot = o.g_tot;
+    plan.s_tot = o.s_tot;
+    upload(plan.d_a_off, o.a_off);
+    upload(plan.d_d_off, o.d_off);
+    upload(plan.d_g_off, o.g_off);
+    upload(plan.d_s_off, o.s_off);
     std::vector<RowItem> items;
     std::vector<int> item_off(1, 0);
     for (int s = 0; s < b.n_st; ++s) {
@@ -348,7 +358,7 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
                                        s_G.as<void>(), max_k, stream);
         }
     }
-    s_DS.reserve(9 * sizeof(T) * std::max<long long>(1, plan.d_tot));
+    s_DS.reserve(sizeof(T) * std::max<long long>(1, plan.s_tot));
     s_mirror.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
     s_gslot.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
     s_order.reserve(sizeof(int) * std::max<long long>(1, b.n_pairs));
@@ -362,20 +372,21 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
         {
             ProfScope ps("pg_rows_pairs", stream);
             launch_rows_pairs<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                                 s_gslot.as<long long>(), plan.d_d_off.as<long long>(), plan.d_g_off.as<long long>(),
+                                 s_gslot.as<long long>(), plan.d_s_off.as<long long>(), plan.d_g_off.as<long long>(),
                                  s_G.as<void>(), d_f_row, s_order.as<int>(), s_Dp.as<T>(), s_DS.as<T>(), stream);
         }
         {
             ProfScope ps("pg_rows", stream);
             launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), plan.d_d_off.as<long long>(),
-                           s_D.as<T>(), s_Dp.as<T>(), s_DS.as<T>(), plan.d_items.as<RowItem>(), plan.n_items, d_f_row,
-                           dmod.rows_tr, dmod.chunk, dmod.n_chunks, Xd, ld, stream);
+                           s_D.as<T>(), s_Dp.as<T>(), plan.d_s_off.as<long long>(), s_DS.as<T>(),
+                           plan.d_items.as<RowItem>(), plan.n_items, d_f_row, dmod.rows_tr, dmod.chunk, dmod.n_chunks,
+                           Xd, ld, stream);
         }
     }
     if (b.n_st > 0) {
         ProfScope ps("pg_rows_es", stream);
-        launch_rows_es<T>(dmod.dm, B, plan.d_d_off.as<long long>(), s_D.as<T>(), s_DS.as<T>(), d_e_row, d_f_row,
-                          d_s_row, Xd, ld, stream);
+        launch_rows_es<T>(dmod.dm, B, plan.d_d_off.as<long long>(), s_D.as<T>(), plan.d_s_off.as<long long>(),
+                          s_DS.as<T>(), d_e_row, d_f_row, d_s_row, Xd, ld, stream);
     }
     PG_CUDA(cudaGetLastError());
 }

@@ -61,10 +61,11 @@ struct DevType {
     const int *col_ncomp, *comp_k;
     const int4* col_info;      // per column: its (up to three) linear features and their count (w)
     const int* ent_tp_off;     // per linear feature k: (n_tp + 1) entry offsets by type pair
-    const int* ent_nk;         // per G entry: radial index | Y_lm index << 8 of its head
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
     const int* tp_head_nk;     // per tp_heads entry: radial index | Y_lm index << 8
-    const int* ent_hpos;       // per G entry: position of its head in its type pair's head list
+    // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
+    int n_groups, lay_size, n_tpl;
+    const int *lay_ent, *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
 };
 
 struct DevModel {

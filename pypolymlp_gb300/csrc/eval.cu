@@ -278,10 +278,10 @@ struct Evaluator {
         const DevModel& M = dmod.dm;
         b.build_neighbors(m->flat.cutoff, stream);
         const DevBatch B = b.view(m->flat.cutoff);
-        std::vector<long long> a_off, d_off, g_off;
-        long long a_tot, d_tot, g_tot;
-        m->atom_offsets(b, 0, a_off, d_off, g_off, a_tot, d_tot, g_tot);
-        upload(d_aoff, a_off);
+        AtomOffsets off;
+        m->atom_offsets(b, off);
+        const long long a_tot = off.a_tot;
+        upload(d_aoff, off.a_off);
         s_Anc.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
         s_Aadj.reserve(2 * sizeof(T) * std::max<long long>(1, a_tot));
         s_E.reserve(sizeof(double) * std::max(1, b.n_atoms));

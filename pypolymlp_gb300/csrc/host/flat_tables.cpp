@@ -193,6 +193,50 @@ FlatModel flatten_model(const ModelTables& mt) {
             }
             ft.kcol_off.push_back((int)ft.kcol_col.size());
         }
+        // X-row entry layout by type pair (see flat_tables.h)
+        {
+            const int ntp = mt.n_type_pairs, nl = ft.n_lin;
+            ft.n_groups = (nl + 31) / 32;
+            std::vector<int> hpos_of(ft.K0, 0);
+            for (int tp = 0; tp < ntp; ++tp)
+                for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q)
+                    hpos_of[ft.tp_heads[q]] = q - ft.tp_head_off[tp];
+            ft.tp_perm.assign((size_t)ntp * nl, 0);
+            ft.tp_ipos.assign((size_t)ntp * nl, 0);
+            ft.lay_grp_base.assign((size_t)ntp * ft.n_groups, 0);
+            ft.lay_grp_cnt.assign((size_t)ntp * ft.n_groups, 0);
+            ft.tpl.assign(ntp, -1);
+            for (int tp = 0; tp < ntp; ++tp) {
+                if (ft.tp_head_off[tp + 1] > ft.tp_head_off[tp]) {
+                    ft.tpl[tp] = (int)ft.tpl_tp.size();
+                    ft.tpl_tp.push_back(tp);
+                }
+                auto cnt = [&](int k) {
+                    return ft.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1] - ft.ent_tp_off[(size_t)k * (ntp + 1) + tp];
+                };
+                std::vector<int> order(nl);
+                for (int k = 0; k < nl; ++k) order[k] = k;
+                std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt(a) > cnt(b); });
+                for (int x = 0; x < nl; ++x) {
+                    ft.tp_perm[(size_t)tp * nl + x] = order[x];
+                    ft.tp_ipos[(size_t)tp * nl + order[x]] = x;
+                }
+                for (int g = 0; g < ft.n_groups; ++g) {
+                    const int c = cnt(order[32 * g]);
+                    ft.lay_grp_base[(size_t)tp * ft.n_groups + g] = (int)ft.lay_ent.size();
+                    ft.lay_grp_cnt[(size_t)tp * ft.n_groups + g] = c;
+                    for (int r = 0; r < c; ++r)
+                        for (int l = 0; l < 32; ++l) {
+                            const int x = 32 * g + l;
+                            int e = -1;
+                            if (x < nl && r < cnt(order[x])) e = ft.ent_tp_off[(size_t)order[x] * (ntp + 1) + tp] + r;
+                            ft.lay_ent.push_back(e);
+                            ft.lay_hpos.push_back(e >= 0 ? hpos_of[ft.ent_head[e]] : 0);
+                        }
+                }
+            }
+            ft.lay_size = (int)ft.lay_ent.size();
+        }
     }
     // Legendre / Y_lm constants, computed in IEEE double with the reference's
     // expressions (polymlp_spherical_harmonics.cpp:95-196).

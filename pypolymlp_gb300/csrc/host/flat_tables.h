@@ -54,6 +54,19 @@ struct FlatType {
     // per linear feature k: polynomial columns containing it (CSR): column and the
     // (up to two) other features whose product weights d(col)/d(d_k); -1 = none
     std::vector<int> kcol_off, kcol_col, kcol_o1, kcol_o2;
+    // X-row layout of the adjoint entries, per type pair tp of this centre
+    // type: the features are ordered by their number of entries of tp
+    // (descending; tp_perm[tp][x] is the feature at position x, tp_ipos the
+    // inverse) and taken 32 at a time (group g = positions 32g .. 32g+31);
+    // group g stores its entries rank-major: slot lay_grp_base[tp][g] + 32 r +
+    // lane holds the r-th entry of the feature at position 32g + lane
+    // (lay_ent = -1 where that feature has fewer entries: a zero entry).
+    // n_groups = ceil(n_lin / 32); lay_grp_cnt[tp][g] = entries of the group's
+    // first (largest) feature.
+    int n_groups = 0, lay_size = 0;
+    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos;
+    // type pairs with heads for this centre type: local index or -1, and back
+    std::vector<int> tpl, tpl_tp;
 };
 
 struct FlatModel {

@@ -46,16 +46,17 @@ void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, con
                       long long* gslot, int* missing, cudaStream_t st);
 template <typename T>
 void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
-                       const double* nb_d, const long long* gslot, const long long* d_off, const long long* g_off,
+                       const double* nb_d, const long long* gslot, const long long* s_off, const long long* g_off,
                        const void* G, const long long* f_row, int* order, T* Dp, T* DS, cudaStream_t st);
 template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
-                 const long long* d_off, const T* D, const T* Dp, const T* DS, const RowItem* items, int n_items,
-                 const long long* f_row, int TR, int CH, int n_chunks, T* X, long long ld, cudaStream_t st);
+                 const long long* d_off, const T* D, const T* Dp, const long long* s_off, const T* DS,
+                 const RowItem* items, int n_items, const long long* f_row, int TR, int CH, int n_chunks, T* X,
+                 long long ld, cudaStream_t st);
 template <typename T>
-void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const T* DS,
-                    const long long* e_row, const long long* f_row, const long long* s_row, T* X, long long ld,
-                    cudaStream_t st);
+void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const long long* s_off,
+                    const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,
+                    long long ld, cudaStream_t st);
 
 // Tensor-core Gram (gram_tc.cu): scratch (BF16 halves of X, work units,
 // partial tiles of the row splits, error flag) and entry points.

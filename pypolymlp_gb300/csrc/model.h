@@ -12,9 +12,14 @@ namespace pg {
 
 // Per-batch offsets of per-atom data and the pg_rows work items.
 struct RowPlan {
-    long long a_tot = 0, d_tot = 0, g_tot = 0;
+    long long a_tot = 0, d_tot = 0, g_tot = 0, s_tot = 0;
     int n_items = 0;
-    DevBuf d_a_off, d_d_off, d_g_off, d_items, d_item_off;
+    DevBuf d_a_off, d_d_off, d_g_off, d_s_off, d_items, d_item_off;
+};
+
+struct AtomOffsets {
+    std::vector<long long> a_off, d_off, g_off, s_off;
+    long long a_tot = 0, d_tot = 0, g_tot = 0, s_tot = 0;
 };
 
 struct Model {
@@ -27,9 +32,7 @@ struct Model {
 
     explicit Model(const pg_feature_params* p);
 
-    void atom_offsets(const DeviceBatch& b, size_t t_size, std::vector<long long>& a_off,
-                      std::vector<long long>& d_off, std::vector<long long>& g_off, long long& a_tot,
-                      long long& d_tot, long long& g_tot) const;
+    void atom_offsets(const DeviceBatch& b, AtomOffsets& o) const;
     size_t bytes_per_atom(bool fp64, double mean_pairs) const;
     std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
 

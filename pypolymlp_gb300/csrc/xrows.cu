@@ -8,7 +8,8 @@
 //                              sums over neighbours accumulated in FP64.
 //   pg_features_adjoint        invariant features d_k of every atom and the
 //                              sparse adjoint G_k[h] = d d_k / d a_h with the
-//                              conjugate half folded in (features.cpp:155-248).
+//                              conjugate half folded in (features.cpp:155-248),
+//                              stored in the X-row layout by type pair.
 //   pg_nb_mirror               mirror index of every pair.
 //   pg_rows_pairs              per centre: the derivatives dd_k/dd_p of its
 //                              linear features for every pair (the pair bases
@@ -199,10 +200,17 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
         Di[k] = v;
     }
     cplx<T>* Gi = G + g_off[i];
-    for (int e = threadIdx.x; e < ty.n_ent; e += blockDim.x) {
+    // entries in the X-row layout (rank-major groups of 32 features per type
+    // pair); padding slots hold zero
+    for (int slot = threadIdx.x; slot < ty.lay_size; slot += blockDim.x) {
+        const int e = ty.lay_ent[slot];
+        cplx<T> g = {(T)0, (T)0};
+        if (e < 0) {
+            Gi[slot] = g;
+            continue;
+        }
         const int h = ty.ent_head[e];
         const T cc = (ty.head_m[h] & 1) ? (T)-1 : (T)1;
-        cplx<T> g = {(T)0, (T)0};
         for (int q = ty.term_off[e]; q < ty.term_off[e + 1]; ++q) {
             const FlatTerm& t = ty.g_terms[q];
             const cplx<T> p = term_product<T>(t, a);
@@ -215,7 +223,7 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
                 g.im += c * p.im;
             }
         }
-        Gi[e] = g;
+        Gi[slot] = g;
     }
 }
 
@@ -270,23 +278,38 @@ __global__ void pg_nb_mirror(int n_atoms, const long long* nb_off, const int* nb
 //   H[c][u][w] = d phi_h(d_w) / dd_w,c    (h the u-th head of the type pair),
 // then thread k contracts the adjoint entries of feature k with all pairs of
 // the chunk at once:  dd_k/dd_w,c = sum_e Re(G_e(i) . H[c][u_e][w]).
+// The entries of the centre are stored by type pair, features ordered by
+// their number of entries and interleaved 32 at a time (pg_features_adjoint),
+// so warp = 32 feature positions reads them coalesced with equal loop lengths.
 // The images of one neighbour j are summed and stored once, at the group slot
-// (the first entry of i in j's list), so stage B reads one vector per
-// (centre, target).  Thread k also accumulates the centre's DS vectors
-//   DS[i][c][k]   = sum_{p, j_p != i} dd_k/dd_p,c                   (self rows)
-//   DS[i][3+q][k] = sum_p d_p,b(q) dd_k/dd_p,a(q)                   (virial)
-// with (a, b)(q) = (x,x) (y,y) (z,z) (x,y) (y,z) (z,x).
+// (the first entry of i in j's list), indexed by feature position, so stage B
+// reads one vector per (centre, target).  The centre's DS vectors are
+// accumulated per type pair, also by feature position:
+//   DS[i][tp][c][x]   = sum_{p of tp, j_p != i} dd_k/dd_p,c         (self rows)
+//   DS[i][tp][3+q][x] = sum_{p of tp} d_p,b(q) dd_k/dd_p,a(q)       (virial)
+// with k = perm_tp[x] and (a, b)(q) = (x,x) (y,y) (z,z) (x,y) (y,z) (z,x).
+// H rows (8 complex values: the pairs of a chunk) are read by lanes at random
+// head positions u, so the 16-byte pieces of a row are XOR-swizzled by u to
+// spread them over the shared-memory banks.
 template <typename T>
-__device__ __forceinline__ void load_h8(const cplx<T>* h, cplx<T> (&v)[8]) {
-#pragma unroll
-    for (int w = 0; w < 8; ++w) v[w] = h[w];
+__device__ __forceinline__ int h_pos(int u, int w) {
+    return w ^ (u & 7);  // one complex<double> per 16 bytes
 }
 template <>
-__device__ __forceinline__ void load_h8<float>(const cplx<float>* h, cplx<float> (&v)[8]) {
+__device__ __forceinline__ int h_pos<float>(int u, int w) {
+    return (((w >> 1) ^ (u & 3)) << 1) | (w & 1);  // two complex<float> per 16 bytes
+}
+template <typename T>
+__device__ __forceinline__ void load_h8(const cplx<T>* h, int u, cplx<T> (&v)[8]) {
+#pragma unroll
+    for (int w = 0; w < 8; ++w) v[w] = h[h_pos<T>(u, w)];
+}
+template <>
+__device__ __forceinline__ void load_h8<float>(const cplx<float>* h, int u, cplx<float> (&v)[8]) {
     const float4* p = reinterpret_cast<const float4*>(h);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float4 x = p[q];
+        const float4 x = p[q ^ (u & 3)];
         v[2 * q] = {x.x, x.y};
         v[2 * q + 1] = {x.z, x.w};
     }
@@ -295,7 +318,7 @@ __device__ __forceinline__ void load_h8<float>(const cplx<float>* h, cplx<float>
 template <typename T>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off,
                                                               const int* nb_j, const double* nb_d,
-                                                              const long long* gslot, const long long* d_off,
+                                                              const long long* gslot, const long long* s_off,
                                                               const long long* g_off, const cplx<T>* G,
                                                               const long long* f_row, int* order, T* Dp, T* DS) {
     constexpr int NW = kRowsThreads / 32;
@@ -344,8 +367,8 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
     __syncthreads();
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     const cplx<T>* Gi = G + g_off[i];
-    T* ds = DS + 9 * d_off[i];
-    for (int q = threadIdx.x; q < 9 * nl; q += blockDim.x) ds[q] = (T)0;
+    T* dsa = DS + s_off[i];  // [type pair of the centre type][9][n_lin], feature positions of that pair
+    for (int q = threadIdx.x; q < 9 * nl * ty.n_tpl; q += blockDim.x) dsa[q] = (T)0;
     for (int tp = 0; tp < M.n_tp; ++tp) {
         const int r_end = s_tpoff[tp + 1];
         const int q0 = ty.tp_head_off[tp], nh = ty.tp_head_off[tp + 1] - q0;
@@ -389,17 +412,18 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                         const T f = bv.fn[nid], fd = bv.fnd[nid];
                         const cplx<T> y = bv.Y[key];
                         const cplx<T> yx = bv.dY[key], yy = bv.dY[M.n_ylm + key], yz = bv.dY[2 * M.n_ylm + key];
-                        H[((size_t)0 * HT + u) * NW + warp] = {f * yx.re + fd * ux * y.re, f * yx.im + fd * ux * y.im};
-                        H[((size_t)1 * HT + u) * NW + warp] = {f * yy.re + fd * uy * y.re, f * yy.im + fd * uy * y.im};
-                        H[((size_t)2 * HT + u) * NW + warp] = {f * yz.re + fd * uz * y.re, f * yz.im + fd * uz * y.im};
+                        const int hw = h_pos<T>(u, warp);
+                        H[((size_t)0 * HT + u) * NW + hw] = {f * yx.re + fd * ux * y.re, f * yx.im + fd * ux * y.im};
+                        H[((size_t)1 * HT + u) * NW + hw] = {f * yy.re + fd * uy * y.re, f * yy.im + fd * uy * y.im};
+                        H[((size_t)2 * HT + u) * NW + hw] = {f * yz.re + fd * uz * y.re, f * yz.im + fd * uz * y.im};
                     }
                 } else {
                     for (int u = lane; u < nh; u += 32)
-                        for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + warp] = {(T)0, (T)0};
+                        for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + h_pos<T>(u, warp)] = {(T)0, (T)0};
                 }
             } else {
                 for (int u = lane; u < nh; u += 32)
-                    for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + warp] = {(T)0, (T)0};
+                    for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + h_pos<T>(u, warp)] = {(T)0, (T)0};
             }
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -415,65 +439,86 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                 }
             }
             __syncthreads();
-            // ---- contraction of the chunk
-            for (int kf = threadIdx.x; kf < nl; kf += blockDim.x) {
-                const int* eo = ty.ent_tp_off + (size_t)kf * (M.n_tp + 1);
-                T acc[NW][3];
+            // ---- contraction of the chunk: warp = group of 32 feature positions,
+            // lane = position; the group's entries are read rank-major (coalesced)
+            {
+                // (a type pair without heads for this centre type contributes zeros and keeps no DS)
+                T* ds = ty.tpl[tp] >= 0 ? dsa + (size_t)ty.tpl[tp] * 9 * nl : nullptr;
+                const int ng = ty.n_groups;
+                for (int grp = warp; grp < ng; grp += NW) {
+                    const int x = 32 * grp + lane;
+                    const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
+                    T acc[NW][3];
 #pragma unroll
-                for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
-                for (int e = eo[tp]; e < eo[tp + 1]; ++e) {
-                    const cplx<T> g = Gi[e];
-                    const int u = ty.ent_hpos[e];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        cplx<T> h[8];
-                        load_h8<T>(H + ((size_t)c * HT + u) * NW, h);
-#pragma unroll
-                        for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
+                    for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
+                    // the next rank's entry is loaded while this one is contracted
+                    cplx<T> gn = {(T)0, (T)0};
+                    int un = 0;
+                    if (cnt > 0) {
+                        gn = Gi[base + lane];
+                        un = ty.lay_hpos[base + lane];
                     }
-                }
-                T sv[9];
-#pragma unroll
-                for (int v = 0; v < 9; ++v) sv[v] = (T)0;
-                T run0 = 0, run1 = 0, run2 = 0;
-#pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    if (w >= n) break;
-                    const int fl = s_flag[w];
-                    const T a0 = acc[w][0], a1 = acc[w][1], a2 = acc[w][2];
-                    if (fl & 1) {
-                        const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
-                        if (!(fl & 2)) {
-                            sv[0] += a0;
-                            sv[1] += a1;
-                            sv[2] += a2;
+                    for (int r = 0; r < cnt; ++r) {
+                        const cplx<T> g = gn;
+                        const int u = un;
+                        if (r + 1 < cnt) {
+                            const int sl = base + 32 * (r + 1) + lane;
+                            gn = Gi[sl];
+                            un = ty.lay_hpos[sl];
                         }
-                        sv[3] += dx * a0;
-                        sv[4] += dy * a1;
-                        sv[5] += dz * a2;
-                        sv[6] += dy * a0;
-                        sv[7] += dz * a1;
-                        sv[8] += dx * a2;
-                    }
-                    run0 += a0;
-                    run1 += a1;
-                    run2 += a2;
-                    if (fl & 4) {
-                        T* o = Dp + (size_t)s_slot[w] * 3 * NL + kf;
-                        if (fl & 8) {
-                            o[0] = run0;
-                            o[NL] = run1;
-                            o[2 * NL] = run2;
-                        } else {
-                            o[0] += run0;
-                            o[NL] += run1;
-                            o[2 * NL] += run2;
-                        }
-                        run0 = run1 = run2 = 0;
-                    }
-                }
 #pragma unroll
-                for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + kf] += sv[v];
+                        for (int c = 0; c < 3; ++c) {
+                            cplx<T> h[8];
+                            load_h8<T>(H + ((size_t)c * HT + u) * NW, u, h);
+#pragma unroll
+                            for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
+                        }
+                    }
+                    if (x >= nl) continue;
+                    T sv[9];
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) sv[v] = (T)0;
+                    T run0 = 0, run1 = 0, run2 = 0;
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        if (w >= n) break;
+                        const int fl = s_flag[w];
+                        const T a0 = acc[w][0], a1 = acc[w][1], a2 = acc[w][2];
+                        if (fl & 1) {
+                            const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
+                            if (!(fl & 2)) {
+                                sv[0] += a0;
+                                sv[1] += a1;
+                                sv[2] += a2;
+                            }
+                            sv[3] += dx * a0;
+                            sv[4] += dy * a1;
+                            sv[5] += dz * a2;
+                            sv[6] += dy * a0;
+                            sv[7] += dz * a1;
+                            sv[8] += dx * a2;
+                        }
+                        run0 += a0;
+                        run1 += a1;
+                        run2 += a2;
+                        if (fl & 4) {
+                            T* o = Dp + (size_t)s_slot[w] * 3 * NL + x;
+                            if (fl & 8) {
+                                o[0] = run0;
+                                o[NL] = run1;
+                                o[2 * NL] = run2;
+                            } else {
+                                o[0] += run0;
+                                o[NL] += run1;
+                                o[2 * NL] += run2;
+                            }
+                            run0 = run1 = run2 = 0;
+                        }
+                    }
+                    if (ds)
+#pragma unroll
+                        for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + x] += sv[v];
+                }
             }
             __syncthreads();
         }
@@ -489,7 +534,8 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
 template <typename T>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
-                                                        const T* Dp, const T* DS, const RowItem* items,
+                                                        const T* Dp, const long long* s_off, const T* DS,
+                                                        const RowItem* items,
                                                         const long long* f_row, int TR, int CH, T* X, long long ld) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const RowItem it = items[blockIdx.x];
@@ -517,12 +563,15 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 q = qb;
                 continue;
             }
-            const DevType& ty = M.types[B.types[gi]];
+            const int t1 = B.types[gi];
+            const DevType& ty = M.types[t1];
             const int nl = ty.n_lin;
+            const int* perm = ty.tp_perm + (size_t)M.type_pairs[t1 * M.n_type + B.types[gj]] * nl;
             __syncthreads();  // the previous expansion has read Dk and dcur
-            for (int k = threadIdx.x; k < nl; k += blockDim.x) {
-                dcur[k] = D[d_off[gi] + k];
-                const T* src = Dp + (size_t)q * 3 * NL + k;  // the group (gi, gj), images summed
+            for (int x = threadIdx.x; x < nl; x += blockDim.x) {
+                dcur[x] = D[d_off[gi] + x];
+                const T* src = Dp + (size_t)q * 3 * NL + x;  // the group (gi, gj), images summed, by position
+                const int k = perm[x];
                 Dk[k] = src[0];
                 Dk[NL + k] = src[NL];
                 Dk[2 * NL + k] = src[2 * NL];
@@ -563,7 +612,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
         const DevType& ty = M.types[B.types[gi]];
         const int nl = ty.n_lin;
         const T* Di = D + d_off[gi];
-        const T* ds = DS + 9 * d_off[gi];
+        const T* dsa = DS + s_off[gi];
         T* o = out + (size_t)a * 3 * CH;
         for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
             const int4 ci = ty.col_info[c0 + u];
@@ -577,12 +626,17 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 w1 = Di[ci.x] * Di[ci.z];
                 w2 = Di[ci.x] * Di[ci.y];
             }
-            T v[3];
+            T v[3] = {0, 0, 0};
+            for (int l = 0; l < ty.n_tpl; ++l) {  // self vectors are stored per type pair, by position
+                const T* ds = dsa + (size_t)l * 9 * nl;
+                const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
+                const int x0 = ip[ci.x], x1 = ci.w > 1 ? ip[ci.y] : 0, x2 = ci.w > 2 ? ip[ci.z] : 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                v[c] = w0 * ds[(size_t)c * nl + ci.x];
-                if (ci.w > 1) v[c] += w1 * ds[(size_t)c * nl + ci.y];
-                if (ci.w > 2) v[c] += w2 * ds[(size_t)c * nl + ci.z];
+                for (int c = 0; c < 3; ++c) {
+                    v[c] += w0 * ds[(size_t)c * nl + x0];
+                    if (ci.w > 1) v[c] += w1 * ds[(size_t)c * nl + x1];
+                    if (ci.w > 2) v[c] += w2 * ds[(size_t)c * nl + x2];
+                }
             }
             o[u] += v[0];
             o[CH + u] += v[1];
@@ -603,7 +657,8 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
 //   X[e_row, col] = sum_i poly_col(d(i)),
 //   X[s_row + q, col] = -sum_i sum_{k in col} w_k,col(i) DS[i][3+q][k].
 template <typename T>
-__global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D, const T* DS,
+__global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D, const long long* s_off,
+                           const T* DS,
                            const long long* e_row, const long long* f_row, const long long* s_row, T* X,
                            long long ld) {
     const int s = blockIdx.x;
@@ -632,13 +687,17 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
         acc[0] += (double)e;
         if (!force) continue;
         const int nl = ty.n_lin;
-        const T* ds = DS + 9 * d_off[gi] + 3 * (size_t)nl;
+        for (int l = 0; l < ty.n_tpl; ++l) {  // virial vectors per type pair, by position
+            const T* ds = DS + s_off[gi] + (size_t)l * 9 * nl + 3 * (size_t)nl;
+            const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
+            const int x0 = ip[ci.x], x1 = ci.w > 1 ? ip[ci.y] : 0, x2 = ci.w > 2 ? ip[ci.z] : 0;
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            T v = w0 * ds[(size_t)q * nl + ci.x];
-            if (ci.w > 1) v += w1 * ds[(size_t)q * nl + ci.y];
-            if (ci.w > 2) v += w2 * ds[(size_t)q * nl + ci.z];
-            acc[1 + q] -= (double)v;
+            for (int q = 0; q < 6; ++q) {
+                T v = w0 * ds[(size_t)q * nl + x0];
+                if (ci.w > 1) v += w1 * ds[(size_t)q * nl + x1];
+                if (ci.w > 2) v += w2 * ds[(size_t)q * nl + x2];
+                acc[1 + q] -= (double)v;
+            }
         }
     }
     X[(size_t)col * ld + e_row[s]] = (T)acc[0];
@@ -731,30 +790,32 @@ void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, con
 
 template <typename T>
 void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
-                       const double* nb_d, const long long* gslot, const long long* d_off, const long long* g_off,
+                       const double* nb_d, const long long* gslot, const long long* s_off, const long long* g_off,
                        const void* G, const long long* f_row, int* order, T* Dp, T* DS, cudaStream_t st) {
     const size_t smem = rows_pairs_smem_bytes(M, sizeof(T) == 8);
     PG_CUDA(cudaFuncSetAttribute(pg_rows_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pg_rows_pairs<T><<<B.n_atoms, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, nb_d, gslot, d_off, g_off,
+    pg_rows_pairs<T><<<B.n_atoms, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, nb_d, gslot, s_off, g_off,
                                                            reinterpret_cast<const cplx<T>*>(G), f_row, order, Dp, DS);
 }
 
 template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
-                 const long long* d_off, const T* D, const T* Dp, const T* DS, const RowItem* items, int n_items,
-                 const long long* f_row, int TR, int CH, int n_chunks, T* X, long long ld, cudaStream_t st) {
+                 const long long* d_off, const T* D, const T* Dp, const long long* s_off, const T* DS,
+                 const RowItem* items, int n_items, const long long* f_row, int TR, int CH, int n_chunks, T* X,
+                 long long ld, cudaStream_t st) {
     const size_t smem = rows_smem_bytes(M, TR, CH, sizeof(T) == 8);
     PG_CUDA(cudaFuncSetAttribute(pg_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(n_items, n_chunks);
-    pg_rows<T><<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, DS, items, f_row, TR, CH, X, ld);
+    pg_rows<T><<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, items, f_row, TR, CH, X,
+                                                 ld);
 }
 
 template <typename T>
-void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const T* DS,
-                    const long long* e_row, const long long* f_row, const long long* s_row, T* X, long long ld,
-                    cudaStream_t st) {
+void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const long long* s_off,
+                    const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,
+                    long long ld, cudaStream_t st) {
     dim3 grid(B.n_st, (M.F + 255) / 256);
-    pg_rows_es<T><<<grid, 256, 0, st>>>(M, B, d_off, D, DS, e_row, f_row, s_row, X, ld);
+    pg_rows_es<T><<<grid, 256, 0, st>>>(M, B, d_off, D, s_off, DS, e_row, f_row, s_row, X, ld);
 }
 
 template void launch_anlm<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
@@ -773,16 +834,16 @@ template void launch_rows_pairs<float>(const DevModel&, const DevBatch&, const l
                                        const double*, const long long*, const long long*, const long long*,
                                        const void*, const long long*, int*, float*, float*, cudaStream_t);
 template void launch_rows<double>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
-                                  const double*, const double*, const double*, const RowItem*, int,
+                                  const double*, const double*, const long long*, const double*, const RowItem*, int,
                                   const long long*, int, int, int, double*, long long, cudaStream_t);
 template void launch_rows<float>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
-                                 const float*, const float*, const float*, const RowItem*, int, const long long*, int,
-                                 int, int, float*, long long, cudaStream_t);
+                                 const float*, const float*, const long long*, const float*, const RowItem*, int,
+                                 const long long*, int, int, int, float*, long long, cudaStream_t);
 template void launch_rows_es<double>(const DevModel&, const DevBatch&, const long long*, const double*,
-                                     const double*, const long long*, const long long*, const long long*, double*,
-                                     long long, cudaStream_t);
-template void launch_rows_es<float>(const DevModel&, const DevBatch&, const long long*, const float*, const float*,
-                                    const long long*, const long long*, const long long*, float*, long long,
-                                    cudaStream_t);
+                                     const long long*, const double*, const long long*, const long long*,
+                                     const long long*, double*, long long, cudaStream_t);
+template void launch_rows_es<float>(const DevModel&, const DevBatch&, const long long*, const float*,
+                                    const long long*, const float*, const long long*, const long long*,
+                                    const long long*, float*, long long, cudaStream_t);
 
 }  // namespace pg
