@@ -451,6 +451,10 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                     T acc[NW][3];
 #pragma unroll
                     for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
+                    // this position's DS sums so far, loaded before the contraction hides their latency
+                    T sv[9];
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) sv[v] = (ds && x < nl) ? ds[(size_t)v * nl + x] : (T)0;
                     // the next rank's entry is loaded while this one is contracted
                     cplx<T> gn = {(T)0, (T)0};
                     int un = 0;
@@ -475,9 +479,6 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                         }
                     }
                     if (x >= nl) continue;
-                    T sv[9];
-#pragma unroll
-                    for (int v = 0; v < 9; ++v) sv[v] = (T)0;
                     T run0 = 0, run1 = 0, run2 = 0;
 #pragma unroll
                     for (int w = 0; w < NW; ++w) {
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                     }
                     if (ds)
 #pragma unroll
-                        for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + x] += sv[v];
+                        for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + x] = sv[v];
                 }
             }
             __syncthreads();
