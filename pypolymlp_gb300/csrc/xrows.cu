@@ -528,11 +528,20 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
 
 // Stage B.  Columns [c0, c0 + CH) of the force rows of a block of TR target
 // atoms.  For target j, the centres i with images on it are the runs of j's
-// own list; the group vector of (i, j) sits at the run's first slot and is
-// expanded into the columns with the weights of centre i.  The
-// self rows of the block's centres come from DS.  Each thread owns columns,
-// so all sums are race free and deterministic.
-template <typename T>
+// own list; the group vector of (i, j) sits at the run's first slot (by
+// feature position) and is expanded into the columns with the weights of
+// centre i.  Each thread loads the next run's values for its PM feature
+// positions into registers while the current run is expanded (PM = 0: no
+// prefetch, for models with more than 8 x 256 linear features).  The self rows
+// of the block's centres come from DS.  Each thread owns columns, so all sums
+// are race free and deterministic.
+struct RowRun {
+    int a;            // target position in the block
+    long long q, qb;  // its entries [q, qb) of the target's list (one centre)
+    int gi;           // the centre
+};
+
+template <typename T, int PM>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
                                                         const T* Dp, const long long* s_off, const T* DS,
@@ -551,62 +560,117 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     T* Dk = out + (size_t)TR * 3 * CH;        // [3][NL]
     T* dcur = Dk + 3 * (size_t)NL;            // [NL]
     for (int q = threadIdx.x; q < TR * 3 * CH; q += blockDim.x) out[q] = (T)0;
-    for (int a = 0; a < nblk; ++a) {
-        const int gj = sa0 + blk0 + a;
-        T* o = out + (size_t)a * 3 * CH;
-        long long q = nb_off[gj];
-        const long long qe = nb_off[gj + 1];
-        while (q < qe) {
-            const int gi = nb_j[q];
-            long long qb = q + 1;
-            while (qb < qe && nb_j[qb] == gi) ++qb;
-            if (gi == gj) {  // images of the target itself: no force on it
-                q = qb;
-                continue;
-            }
-            const int t1 = B.types[gi];
-            const DevType& ty = M.types[t1];
-            const int nl = ty.n_lin;
-            const int* perm = ty.tp_perm + (size_t)M.type_pairs[t1 * M.n_type + B.types[gj]] * nl;
-            __syncthreads();  // the previous expansion has read Dk and dcur
-            for (int x = threadIdx.x; x < nl; x += blockDim.x) {
-                dcur[x] = D[d_off[gi] + x];
-                const T* src = Dp + (size_t)q * 3 * NL + x;  // the group (gi, gj), images summed, by position
-                const int k = perm[x];
-                Dk[k] = src[0];
-                Dk[NL + k] = src[NL];
-                Dk[2 * NL + k] = src[2 * NL];
-            }
-            __syncthreads();
-            for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
-                const int4 ci = ty.col_info[c0 + u];
-                if (ci.w == 0) continue;
-                T vx, vy, vz;
-                if (ci.w == 1) {
-                    vx = Dk[ci.x];
-                    vy = Dk[NL + ci.x];
-                    vz = Dk[2 * NL + ci.x];
-                } else {
-                    const T d0 = dcur[ci.x], d1 = dcur[ci.y];
-                    if (ci.w == 2) {
-                        vx = d1 * Dk[ci.x] + d0 * Dk[ci.y];
-                        vy = d1 * Dk[NL + ci.x] + d0 * Dk[NL + ci.y];
-                        vz = d1 * Dk[2 * NL + ci.x] + d0 * Dk[2 * NL + ci.y];
-                    } else {
-                        const T d2 = dcur[ci.z];
-                        const T w0 = d1 * d2, w1 = d0 * d2, w2 = d0 * d1;
-                        vx = w0 * Dk[ci.x] + w1 * Dk[ci.y] + w2 * Dk[ci.z];
-                        vy = w0 * Dk[NL + ci.x] + w1 * Dk[NL + ci.y] + w2 * Dk[NL + ci.z];
-                        vz = w0 * Dk[2 * NL + ci.x] + w1 * Dk[2 * NL + ci.y] + w2 * Dk[2 * NL + ci.z];
-                    }
+
+    // the next run at or after entry q of target a (q < 0: the target's first entry); uniform
+    auto find = [&](int a, long long q, RowRun& r) -> bool {
+        while (a < nblk) {
+            const int gj = sa0 + blk0 + a;
+            const long long qe = nb_off[gj + 1];
+            if (q < 0) q = nb_off[gj];
+            while (q < qe) {
+                const int gi = nb_j[q];
+                long long qb = q + 1;
+                while (qb < qe && nb_j[qb] == gi) ++qb;
+                if (gi != gj) {  // images of the target itself exert no force on it
+                    r = RowRun{a, q, qb, gi};
+                    return true;
                 }
-                o[u] -= vx;
-                o[CH + u] -= vy;
-                o[2 * CH + u] -= vz;
+                q = qb;
             }
-            q = qb;
+            ++a;
+            q = -1;
         }
+        return false;
+    };
+    auto perm_of = [&](const RowRun& r) {
+        const int t1 = B.types[r.gi];
+        return M.types[t1].tp_perm +
+               (size_t)M.type_pairs[t1 * M.n_type + B.types[sa0 + blk0 + r.a]] * M.types[t1].n_lin;
+    };
+    T pv[PM > 0 ? PM : 1][4];
+    int pk[PM > 0 ? PM : 1];
+    auto prefetch = [&](const RowRun& r) {
+        const int nl = M.types[B.types[r.gi]].n_lin;
+        const int* perm = perm_of(r);
+        const T* src = Dp + (size_t)r.q * 3 * NL;
+        const T* dsrc = D + d_off[r.gi];
+#pragma unroll
+        for (int m = 0; m < PM; ++m) {
+            const int x = threadIdx.x + m * blockDim.x;
+            if (x < nl) {
+                pk[m] = perm[x];
+                pv[m][0] = src[x];
+                pv[m][1] = src[NL + x];
+                pv[m][2] = src[2 * NL + x];
+                pv[m][3] = dsrc[x];
+            }
+        }
+    };
+
+    RowRun cur;
+    bool have = find(0, -1, cur);
+    if (PM > 0 && have) prefetch(cur);
+    while (have) {
+        const DevType& ty = M.types[B.types[cur.gi]];
+        const int nl = ty.n_lin;
+        __syncthreads();  // the previous expansion has read Dk and dcur
+        if (PM > 0) {
+#pragma unroll
+            for (int m = 0; m < (PM > 0 ? PM : 1); ++m) {
+                const int x = threadIdx.x + m * blockDim.x;
+                if (x < nl) {
+                    Dk[pk[m]] = pv[m][0];
+                    Dk[NL + pk[m]] = pv[m][1];
+                    Dk[2 * NL + pk[m]] = pv[m][2];
+                    dcur[x] = pv[m][3];
+                }
+            }
+        } else {
+            const int* perm = perm_of(cur);
+            const T* src = Dp + (size_t)cur.q * 3 * NL;
+            for (int x = threadIdx.x; x < nl; x += blockDim.x) {
+                const int k = perm[x];
+                Dk[k] = src[x];
+                Dk[NL + k] = src[NL + x];
+                Dk[2 * NL + k] = src[2 * NL + x];
+                dcur[x] = D[d_off[cur.gi] + x];
+            }
+        }
+        RowRun nxt;
+        const bool more = find(cur.a, cur.qb, nxt);
+        if (PM > 0 && more) prefetch(nxt);  // in flight during the expansion below
+        __syncthreads();
+        T* o = out + (size_t)cur.a * 3 * CH;
+        for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
+            const int4 ci = ty.col_info[c0 + u];
+            if (ci.w == 0) continue;
+            T vx, vy, vz;
+            if (ci.w == 1) {
+                vx = Dk[ci.x];
+                vy = Dk[NL + ci.x];
+                vz = Dk[2 * NL + ci.x];
+            } else {
+                const T d0 = dcur[ci.x], d1 = dcur[ci.y];
+                if (ci.w == 2) {
+                    vx = d1 * Dk[ci.x] + d0 * Dk[ci.y];
+                    vy = d1 * Dk[NL + ci.x] + d0 * Dk[NL + ci.y];
+                    vz = d1 * Dk[2 * NL + ci.x] + d0 * Dk[2 * NL + ci.y];
+                } else {
+                    const T d2 = dcur[ci.z];
+                    const T w0 = d1 * d2, w1 = d0 * d2, w2 = d0 * d1;
+                    vx = w0 * Dk[ci.x] + w1 * Dk[ci.y] + w2 * Dk[ci.z];
+                    vy = w0 * Dk[NL + ci.x] + w1 * Dk[NL + ci.y] + w2 * Dk[NL + ci.z];
+                    vz = w0 * Dk[2 * NL + ci.x] + w1 * Dk[2 * NL + ci.y] + w2 * Dk[2 * NL + ci.z];
+                }
+            }
+            o[u] -= vx;
+            o[CH + u] -= vy;
+            o[2 * CH + u] -= vz;
+        }
+        cur = nxt;
+        have = more;
     }
+    __syncthreads();
     // self rows of the block's centres
     for (int a = 0; a < nblk; ++a) {
         const int gi = sa0 + blk0 + a;
@@ -805,10 +869,12 @@ void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, 
                  const RowItem* items, int n_items, const long long* f_row, int TR, int CH, int n_chunks, T* X,
                  long long ld, cudaStream_t st) {
     const size_t smem = rows_smem_bytes(M, TR, CH, sizeof(T) == 8);
-    PG_CUDA(cudaFuncSetAttribute(pg_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int need = (M.max_lin + kRowsThreads - 1) / kRowsThreads;  // feature positions per thread
+    auto kern = need <= 2 ? pg_rows<T, 2> : need <= 4 ? pg_rows<T, 4> : need <= 6 ? pg_rows<T, 6>
+              : need <= 8 ? pg_rows<T, 8> : pg_rows<T, 0>;
+    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(n_items, n_chunks);
-    pg_rows<T><<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, items, f_row, TR, CH, X,
-                                                 ld);
+    kern<<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, items, f_row, TR, CH, X, ld);
 }
 
 template <typename T>
