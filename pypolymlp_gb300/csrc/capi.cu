@@ -188,9 +188,23 @@ void DeviceBatch::upload_structures(const pg_structures* st, int s_begin, int s_
         }
         st_atom_off.push_back(st_atom_off.back() + n);
         st_trans_off.push_back((int)(trans.size() / 3));
+        if ((long long)n * (st_trans_off.back() - st_trans_off[st_trans_off.size() - 2]) >= (1LL << 31))
+            throw std::runtime_error("structure too large: atoms x lattice translations must stay below 2^31");
         a += n;
     }
     n_atoms = st_atom_off.back();
+    coord_max = 0.0;
+    std::vector<float4> posf(pos.size() / 3), transf(trans.size() / 3);
+    for (size_t q = 0; q < posf.size(); ++q) {
+        posf[q] = make_float4((float)pos[3 * q], (float)pos[3 * q + 1], (float)pos[3 * q + 2], 0.f);
+        for (int c = 0; c < 3; ++c) coord_max = std::max(coord_max, std::fabs(pos[3 * q + c]));
+    }
+    for (size_t q = 0; q < transf.size(); ++q) {
+        transf[q] = make_float4((float)trans[3 * q], (float)trans[3 * q + 1], (float)trans[3 * q + 2], 0.f);
+        for (int c = 0; c < 3; ++c) coord_max = std::max(coord_max, std::fabs(trans[3 * q + c]));
+    }
+    upload(d_posf, posf);
+    upload(d_transf, transf);
     upload(d_st_atom_off, st_atom_off);
     upload(d_st_trans_off, st_trans_off);
     upload(d_trans, trans);
@@ -247,7 +261,14 @@ DevBatch DeviceBatch::view(double cutoff) const {
     B.pos = d_pos.as<double>();
     B.types = d_types.as<int>();
     B.atom_st = d_atom_st.as<int>();
+    B.posf = d_posf.as<float4>();
+    B.transf = d_transf.as<float4>();
     B.cutoff = cutoff;
+    // FP32 differences of coordinates up to L carry an error below 4 L 2^-24 per
+    // component, so |r2_f32 - r2| < 2 rc (12 L 2^-24) + O(L^2 2^-48) + the FP32
+    // rounding of r2; the margin below covers that with a factor > 10
+    const double L = std::max(1.0, coord_max);
+    B.prefilter_r2 = (float)(cutoff * cutoff * (1.0 + 1e-4) + 1e-5 * L * (cutoff + L) + 1e-3);
     return B;
 }
 

@@ -18,7 +18,10 @@ struct DevBatch {
     const double* pos;         // 3 per atom (wrapped as NeighborCell does)
     const int* types;          // per atom
     const int* atom_st;        // per atom: structure index
+    const float4* posf;        // FP32 copies of pos (w unused), for the candidate pre-filter
+    const float4* transf;      // FP32 copies of trans
     double cutoff;
+    float prefilter_r2;        // FP32 squared distance above which a candidate is surely beyond the cutoff
 };
 
 // Work item: (structure, first target atom of a block of TR atoms).

@@ -108,7 +108,8 @@ struct DeviceBatch {
     long long n_pairs = 0;
     std::vector<int> st_atom_off, st_trans_off, types, atom_st;
     std::vector<double> trans, pos;
-    DevBuf d_st_atom_off, d_st_trans_off, d_trans, d_pos, d_types, d_atom_st;
+    double coord_max = 0.0;  // largest |coordinate| or |translation component| of the batch
+    DevBuf d_st_atom_off, d_st_trans_off, d_trans, d_pos, d_types, d_atom_st, d_posf, d_transf;
     DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d, d_total;
     std::vector<long long> nb_off;  // host copy, only after host_offsets()
     // Host: translations and wrapped positions (NeighborCell), uploaded to the device.

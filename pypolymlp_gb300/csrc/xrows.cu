@@ -31,6 +31,13 @@ namespace pg {
 // __dadd_rn/__dmul_rn are used so nothing is contracted into an FMA.
 __device__ __forceinline__ bool pair_keep(const DevBatch& B, int i, int j, int t, double rc2, double tol2,
                                           double& dx, double& dy, double& dz) {
+    // FP32 pre-filter: a candidate whose FP32 distance exceeds the cutoff by more
+    // than the rounding margin is beyond it in FP64 too; the rest are decided in FP64
+    {
+        const float4 a = B.posf[i], b = B.posf[j], tt = B.transf[t];
+        const float fx = b.x - a.x + tt.x, fy = b.y - a.y + tt.y, fz = b.z - a.z + tt.z;
+        if (fx * fx + fy * fy + fz * fz > B.prefilter_r2) return false;
+    }
     const double* pi = B.pos + 3 * (size_t)i;
     const double* pj = B.pos + 3 * (size_t)j;
     const double* tr = B.trans + 3 * (size_t)t;
@@ -50,12 +57,20 @@ __global__ void pg_nb_count(DevBatch B, int* counts) {
     const int a0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - a0;
     const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
     const double rc2 = __dmul_rn(B.cutoff, B.cutoff), tol2 = __dmul_rn(1e-10, 1e-10);
-    const long long total = (long long)n * nt;
+    const int total = n * nt;  // candidates (j, t), j-major; n * nt < 2^31 (checked on the host)
     int cnt = 0;
-    for (long long q = lane; q < total; q += 32) {
-        const int j = (int)(q / nt), t = (int)(q % nt);
+    // lane q = j * nt + t walks the candidates with a carried (j, t) instead of dividing
+    int j = lane / nt, t = lane % nt;
+    const int dj = 32 / nt, dt = 32 % nt;
+    for (int q = lane; q < total; q += 32) {
         double dx, dy, dz;
         cnt += pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz) ? 1 : 0;
+        j += dj;
+        t += dt;
+        if (t >= nt) {
+            t -= nt;
+            ++j;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     if (lane == 0) counts[i] = cnt;
@@ -70,23 +85,28 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
     const int a0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - a0;
     const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
     const double rc2 = __dmul_rn(B.cutoff, B.cutoff), tol2 = __dmul_rn(1e-10, 1e-10);
-    const long long total = (long long)n * nt;
+    const int total = n * nt;
     long long w = offsets[i];
     const long long wend = offsets[i + 1];
-    for (long long base = 0; base < total; base += 32) {
-        const long long q = base + lane;
+    int j = lane / nt, t = lane % nt;
+    const int dj = 32 / nt, dt = 32 % nt;
+    for (int base = 0; base < total; base += 32) {
+        const int q = base + lane;
         double dx = 0, dy = 0, dz = 0;
-        int j = 0;
+        const int jq = j;
         bool keep = false;
-        if (q < total) {
-            j = (int)(q / nt);
-            keep = pair_keep(B, i, a0 + j, t0 + (int)(q % nt), rc2, tol2, dx, dy, dz);
+        if (q < total) keep = pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz);
+        j += dj;
+        t += dt;
+        if (t >= nt) {
+            t -= nt;
+            ++j;
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) {
             const long long k = w + __popc(m & ((1u << lane) - 1u));
             if (k < wend) {
-                nb_j[k] = a0 + j;
+                nb_j[k] = a0 + jq;
                 nb_d[3 * k] = dx;
                 nb_d[3 * k + 1] = dy;
                 nb_d[3 * k + 2] = dz;
