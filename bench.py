@@ -44,6 +44,25 @@ UNIT = "rows/s"
 
 CFG2 = dict(n_type=2, cutoff=7.0, model_type=3, max_p=2, gaussian_params2=(0.0, 5.0, 10), gtinv_order=3,
             gtinv_maxl=(8, 4))
+# The other configurations of the benchmark family, for `--model`: the unary
+# fcc model (F = 1,539), the ternary model (F = 8,262) and the order-4 ternary
+# model (F = 21,945); each with its structure generator and default size.
+MODELS = {
+    "cfg1": (dict(n_type=1, cutoff=6.0, model_type=2, max_p=2, gaussian_params2=(0.0, 5.0, 8), gtinv_order=2,
+                  gtinv_maxl=(4,)), "fcc", 200,
+             "unary fcc, 200 structures of 32 atoms, gtinv order 2, l_max 4, 8+1 Gaussians, rc 6 A, model_type 2"),
+    "cfg2": (CFG2, "binary", 5000,
+             "binary alloy, 5000 structures of 64-128 atoms, gtinv order 3, l_max (8,4), 10+1 Gaussians, rc 7 A, "
+             "model_type 3, max_p 2"),
+    "cfg3": (dict(n_type=3, cutoff=6.0, model_type=3, max_p=2, gaussian_params2=(0.0, 5.0, 8), gtinv_order=3,
+                  gtinv_maxl=(6, 4)), "ternary", 20000,
+             "ternary, random triclinic cells of 8-256 atoms, gtinv order 3, l_max (6,4), 8+1 Gaussians, rc 6 A, "
+             "model_type 3, max_p 2"),
+    "cfg5": (dict(n_type=3, cutoff=8.0, model_type=3, max_p=2, gaussian_params2=(0.0, 5.0, 4), gtinv_order=4,
+                  gtinv_maxl=(8, 8, 2)), "ternary32", 50000,
+             "ternary, random triclinic cells of 32-192 atoms, gtinv order 4, l_max (8,8,2), 4+1 Gaussians, rc 8 A, "
+             "model_type 3, max_p 2"),
+}
 
 
 def log(*a):
@@ -55,13 +74,20 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_dataset(n_struct, seed, device):
+def make_dataset(n_struct, seed, device, kind="binary", rc=7.0):
     from pypolymlp_gb300 import synthetic as syn
     from pypolymlp_gb300.regression import Dataset
 
-    ss = syn.binary_set(n_struct, seed=seed)
+    if kind == "fcc":
+        ss, nt = syn.fcc_set(n_struct, seed=seed), 1
+    elif kind == "ternary":
+        ss, nt = syn.ternary_set(n_struct, seed=seed), 3
+    elif kind == "ternary32":
+        ss, nt = syn.ternary_set(n_struct, seed=seed, n_range=(32, 192)), 3
+    else:
+        ss, nt = syn.binary_set(n_struct, seed=seed), 2
     t = time.time()
-    syn.morse_labels(ss, syn.morse_D(2), device=device)
+    syn.morse_labels(ss, syn.morse_D(nt), rc=rc, device=device)
     log(f"labels for {n_struct} structures in {time.time() - t:.1f}s")
     return Dataset.from_structure_set(ss, name="binary")
 
@@ -186,8 +212,9 @@ def run_reference(args):
         return 0
     from pypolymlp_gb300.params import make_params_dict
 
-    params = make_params_dict(**CFG2)
-    data = make_dataset(max(args.ref_sample, 8), seed=2, device=None)
+    kw, kind, n_default, workload = MODELS[args.model]
+    params = make_params_dict(**kw)
+    data = make_dataset(max(args.ref_sample, 8), seed=2, device=None, kind=kind, rc=kw["cutoff"])
     n_threads = os.cpu_count() or 1
     for _ in range(args.warmup if args.warmup < 1 else 1):
         cpu_baseline(params, data, min(4, len(data)), n_threads)
@@ -201,10 +228,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "binary alloy, gtinv order 3, l_max (8,4), 10+1 Gaussians, rc 7, model_type 3, "
-                               "max_p 2 (F=2618)", "sample_structures": args.ref_sample},
+        "config": {"workload": workload, "model": args.model, "sample_structures": args.ref_sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port",
-                         "sample": f"first {args.ref_sample} structures of the 5,000-structure workload per step"},
+                         "sample": f"first {args.ref_sample} structures of the {n_default}-structure workload per step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -217,7 +243,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n-struct", type=int, default=5000)
+    ap.add_argument("--n-struct", type=int, default=0, help="structures (default: the model's workload size)")
+    ap.add_argument("--model", default="cfg2", choices=sorted(MODELS), help="model and workload (default cfg2)")
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -242,8 +269,10 @@ def main():
     from pypolymlp_gb300.regression import DeviceBatch, GramAccumulator, get_min_energy, weights_and_targets
 
     precision = _ffi.PG_FP64 if args.fp64 else _ffi.PG_MIXED
-    params = make_params_dict(**CFG2)
-    data = make_dataset(args.n_struct, seed=2 + rank, device="cuda")
+    kw, kind, n_default, workload = MODELS[args.model]
+    params = make_params_dict(**kw)
+    n_struct = args.n_struct or n_default
+    data = make_dataset(n_struct, seed=2 + rank, device="cuda", kind=kind, rc=kw["cutoff"])
     min_e = get_min_energy([data])
     model = _ffi.Model(params)
     F = model.n_features
@@ -349,7 +378,7 @@ def main():
            "d2h_bytes_per_step": int(d2h)}
     del res
 
-    ev = eval_bench(params, args) if not args.no_eval else None
+    ev = eval_bench(params, args) if not args.no_eval and args.model == "cfg2" else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -364,8 +393,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.fp64 else "f32+bf16x3", "data": "synthetic",
-            "config": {"workload": "binary alloy, 5000 structures of 64-128 atoms, gtinv order 3, l_max (8,4), "
-                                   "10+1 Gaussians, rc 7 A, model_type 3, max_p 2",
+            "config": {"workload": workload.replace(f"{n_default} structures", f"{len(data)} structures")
+                       if n_struct != n_default else workload, "model": args.model,
                        "n_features": F, "rows_per_step": int(rows_per_step), "n_structures": len(data),
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs larger than L2 (X is rows x F x 4 B)"},

@@ -45,7 +45,7 @@ ProfScope::~ProfScope() {
 }
 
 // ------------------------------------------------------------ DeviceModel
-void DeviceModel::build(const FlatModel& fm, size_t smem_target, bool fp64) {
+void DeviceModel::build(const FlatModel& fm, bool fp64) {
     if (fm.n_type > kMaxTypes) throw std::runtime_error("at most 8 atom types are supported on the device");
     bufs.clear();
     bufs.reserve(64 * kMaxTypes);
@@ -71,27 +71,7 @@ void DeviceModel::build(const FlatModel& fm, size_t smem_target, bool fp64) {
             dm.max_k0tp = std::max(dm.max_k0tp, ft.tp_head_off[tp + 1] - ft.tp_head_off[tp]);
     }
     const int F = fm.n_features;
-    // pg_rows block shape: all columns in one block when they fit, with as many
-    // target atoms (up to 4) as the shared-memory target allows; otherwise one
-    // target atom and balanced column chunks within the 227 KB limit.
     const size_t smem_limit = 227 * 1024;
-    rows_tr = 0;
-    for (int tr : {4, 2, 1})
-        if (rows_smem_bytes(dm, tr, F, fp64) <= smem_target) {
-            rows_tr = tr;
-            break;
-        }
-    if (rows_tr > 0) {
-        chunk = F;
-    } else {
-        rows_tr = 1;
-        for (int nch = 1;; ++nch) {
-            chunk = (F + nch - 1) / nch;
-            if (rows_smem_bytes(dm, 1, chunk, fp64) <= smem_limit) break;
-            if (chunk <= 32) throw std::runtime_error("model too large for the pg_rows shared-memory layout");
-        }
-    }
-    n_chunks = (F + chunk - 1) / chunk;
     if (rows_pairs_smem_bytes(dm, fp64) > smem_limit)
         throw std::runtime_error("model too large for the pg_rows_pairs shared-memory layout");
     if (fm.n_tp > kMaxTypePairs) throw std::runtime_error("at most 64 type pairs are supported");
@@ -125,15 +105,29 @@ void DeviceModel::build(const FlatModel& fm, size_t smem_target, bool fp64) {
         d.g_terms = (const FlatTerm*)up(ft.g_terms);
         d.col_ncomp = (const int*)up(ft.col_ncomp);
         d.comp_k = (const int*)up(ft.comp_k);
-        std::vector<int4> info(F);
+        std::vector<int2> pack(F);
+        if (ft.n_lin >= 65536) throw std::runtime_error("too many linear features for the packed column recipes");
         for (int c = 0; c < F; ++c) {
             const int nc = ft.col_ncomp[c];
             if (nc > 3) throw std::runtime_error("polynomial order above 3 is not supported");
             int k[3] = {0, 0, 0};
             for (int q = 0; q < nc; ++q) k[q] = ft.comp_k[(size_t)c * 3 + q];
-            info[c] = make_int4(k[0], k[1], k[2], nc);
+            pack[c] = make_int2(k[0] | (k[1] << 16), k[2] | (nc << 16));
         }
-        d.col_info = (const int4*)up(info);
+        d.col_pack = (const int2*)up(pack);
+        std::vector<int> lin(ft.n_lin, -1), prod;
+        for (int c = 0; c < F; ++c) {
+            if (ft.col_ncomp[c] == 1) {
+                const int k = ft.comp_k[(size_t)c * 3];
+                if (lin[k] >= 0) throw std::runtime_error("internal: two linear columns for one feature");
+                lin[k] = c;
+            } else if (ft.col_ncomp[c] >= 2) {
+                prod.push_back(c);
+            }
+        }
+        d.n_prod = (int)prod.size();
+        d.lin_col = (const int*)up(lin);
+        d.prod_col = (const int*)up(prod);
         d.ent_tp_off = (const int*)up(ft.ent_tp_off);
         std::vector<int> tnk(ft.tp_heads.size());
         for (int tp = 0; tp < fm.n_tp; ++tp)
@@ -277,9 +271,8 @@ Model::Model(const pg_feature_params* p)
     : tables(build_model_tables(feature_params_from_abi(p))), flat(flatten_model(tables)) {
     int dev = 0;
     PG_CUDA(cudaGetDevice(&dev));
-    // pg_rows blocks sized for four resident blocks per SM (FP32) or two (FP64)
-    dev64.build(flat, 110 * 1024, true);
-    dev32.build(flat, 56 * 1024, false);
+    dev64.build(flat, true);
+    dev32.build(flat, false);
     s_missing.alloc(sizeof(int));
     PG_CUDA(cudaMemset(s_missing.as<void>(), 0, sizeof(int)));
     max_k = max_k0 = 1;
@@ -328,7 +321,7 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
 }
 
 // Per-batch plan: per-atom storage offsets and pg_rows work items.
-void Model::plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const {
+void Model::plan_rows(const DeviceBatch& b, RowPlan& plan) const {
     AtomOffsets o;
     atom_offsets(b, o);
     plan.a_tot = o.a_tot;
@@ -339,18 +332,6 @@ void Model::plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const {
     upload(plan.d_d_off, o.d_off);
     upload(plan.d_g_off, o.g_off);
     upload(plan.d_s_off, o.s_off);
-    std::vector<RowItem> items;
-    std::vector<int> item_off(1, 0);
-    for (int s = 0; s < b.n_st; ++s) {
-        const int n = b.st_atom_off[s + 1] - b.st_atom_off[s];
-        // every centre belongs to exactly one block (energy rows need all of them)
-        const int nblk = std::max(1, (n + tr - 1) / tr);
-        for (int q = 0; q < nblk; ++q) items.push_back(RowItem{s, q * tr});
-        item_off.push_back((int)items.size());
-    }
-    plan.n_items = (int)items.size();
-    upload(plan.d_items, items);
-    upload(plan.d_item_off, item_off);
 }
 
 // Rows of one uploaded batch into Xd (device, column-major, leading dim ld), in
@@ -398,10 +379,10 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
         }
         {
             ProfScope ps("pg_rows", stream);
+            PG_CUDA(cudaMemsetAsync(Xd, 0, sizeof(T) * (size_t)ld * flat.n_features, stream));
             launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), plan.d_d_off.as<long long>(),
-                           s_D.as<T>(), s_Dp.as<T>(), plan.d_s_off.as<long long>(), s_DS.as<T>(),
-                           plan.d_items.as<RowItem>(), plan.n_items, d_f_row, dmod.rows_tr, dmod.chunk, dmod.n_chunks,
-                           Xd, ld, stream);
+                           s_D.as<T>(), s_Dp.as<T>(), plan.d_s_off.as<long long>(), s_DS.as<T>(), d_f_row, Xd, ld,
+                           stream);
         }
     }
     if (b.n_st > 0) {
@@ -416,7 +397,7 @@ template <typename T>
 void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long* d_f_row,
                        const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream) {
     RowPlan plan;
-    plan_rows(b, plan, (sizeof(T) == 8 ? dev64 : dev32).rows_tr);
+    plan_rows(b, plan);
     run_rows<T>(b, plan, d_e_row, d_f_row, d_s_row, Xd, ld, stream);
     PG_CUDA(cudaStreamSynchronize(stream));
     check_mirrors();

@@ -59,7 +59,9 @@ struct DevType {
     const int *ent_off, *ent_head, *term_off;
     const FlatTerm* g_terms;
     const int *col_ncomp, *comp_k;
-    const int4* col_info;      // per column: its (up to three) linear features and their count (w)
+    const int2* col_pack;      // per column: k0 | k1 << 16, k2 | count << 16 (its up to three linear features)
+    int n_prod;                // columns that are products of two or three features of this type
+    const int *lin_col, *prod_col;  // per feature: its linear column (-1: none); the product columns
     const int* ent_tp_off;     // per linear feature k: (n_tp + 1) entry offsets by type pair
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
     const int* tp_head_nk;     // per tp_heads entry: radial index | Y_lm index << 8

@@ -250,7 +250,7 @@ std::vector<std::unique_ptr<Prepared>> prepare_batches(Model& m, const pg_struct
             if (f_row[s0 + q] >= 0) P->s_end += 6;
         for (double v : yl) P->yty += v * v;
         P->b.upload_structures(st, s0, s1, m.flat.cutoff);
-        m.plan_rows(P->b, P->plan, (fp64 ? m.dev64 : m.dev32).rows_tr);
+        m.plan_rows(P->b, P->plan);
         upload(P->d_e, le);
         upload(P->d_f, lf);
         upload(P->d_s, ls);

@@ -24,12 +24,6 @@ struct DevBatch {
     float prefilter_r2;        // FP32 squared distance above which a candidate is surely beyond the cutoff
 };
 
-// Work item: (structure, first target atom of a block of TR atoms).
-struct RowItem {
-    int st;
-    int a0;
-};
-
 constexpr int kRowsThreads = 256;  // threads of pg_rows / pg_rows_pairs blocks
 constexpr int kMaxTypePairs = 64;
 
@@ -43,7 +37,6 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
-size_t rows_smem_bytes(const DevModel& M, int TR, int CH, bool fp64);
 size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64);
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,
                       long long* gslot, int* missing, cudaStream_t st);
@@ -54,8 +47,7 @@ void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb
 template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
                  const long long* d_off, const T* D, const T* Dp, const long long* s_off, const T* DS,
-                 const RowItem* items, int n_items, const long long* f_row, int TR, int CH, int n_chunks, T* X,
-                 long long ld, cudaStream_t st);
+                 const long long* f_row, T* X, long long ld, cudaStream_t st);
 template <typename T>
 void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const long long* s_off,
                     const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,

@@ -10,11 +10,10 @@
 
 namespace pg {
 
-// Per-batch offsets of per-atom data and the pg_rows work items.
+// Per-batch offsets of per-atom data.
 struct RowPlan {
     long long a_tot = 0, d_tot = 0, g_tot = 0, s_tot = 0;
-    int n_items = 0;
-    DevBuf d_a_off, d_d_off, d_g_off, d_s_off, d_items, d_item_off;
+    DevBuf d_a_off, d_d_off, d_g_off, d_s_off;
 };
 
 struct AtomOffsets {
@@ -36,7 +35,7 @@ struct Model {
     size_t bytes_per_atom(bool fp64, double mean_pairs) const;
     std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
 
-    void plan_rows(const DeviceBatch& b, RowPlan& plan, int tr) const;
+    void plan_rows(const DeviceBatch& b, RowPlan& plan) const;
     template <typename T>
     void run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_row, const long long* d_f_row,
                   const long long* d_s_row, T* Xd, long long ld, cudaStream_t stream);

@@ -92,14 +92,11 @@ void upload(DevBuf& b, const std::vector<V>& v) {
     if (!v.empty()) PG_CUDA(cudaMemcpy(b.as<void>(), v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
 }
 
-// Model uploaded to the device, with the pg_rows block shape for one precision.
+// Model uploaded to the device for one precision.
 struct DeviceModel {
     DevModel dm{};
-    int rows_tr = 1;          // target atoms per pg_rows block
-    int chunk = 0;            // columns per pg_rows block
-    int n_chunks = 0;
     std::vector<DevBuf> bufs;
-    void build(const FlatModel& fm, size_t smem_target, bool fp64);
+    void build(const FlatModel& fm, bool fp64);
 };
 
 // Batch of structures staged on the device with neighbour lists and per-atom data.

@@ -15,9 +15,9 @@
 //                              linear features for every pair (the pair bases
 //                              contracted with the adjoint G), and their self
 //                              and virial sums.
-//   pg_rows                    force rows of X for a block of target atoms and
-//                              a chunk of columns: the pair derivatives landing
-//                              on each target expanded into the polynomial
+//   pg_rows                    force rows of X per target atom: the pair
+//                              derivatives landing on it summed into its
+//                              linear columns and weighted into its product
 //                              columns (model.cpp:159-267).
 //   pg_rows_es                 energy and stress rows per structure.
 #include <cuda_runtime.h>
@@ -546,194 +546,170 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
     }
 }
 
-// Stage B.  Columns [c0, c0 + CH) of the force rows of a block of TR target
-// atoms.  For target j, the centres i with images on it are the runs of j's
-// own list; the group vector of (i, j) sits at the run's first slot (by
-// feature position) and is expanded into the columns with the weights of
-// centre i.  Each thread loads the next run's values for its PM feature
-// positions into registers while the current run is expanded (PM = 0: no
-// prefetch, for models with more than 8 x 256 linear features).  The self rows
-// of the block's centres come from DS.  Each thread owns columns, so all sums
-// are race free and deterministic.
-struct RowRun {
-    int a;            // target position in the block
-    long long q, qb;  // its entries [q, qb) of the target's list (one centre)
-    int gi;           // the centre
-};
+// Stage B.  Force rows of one target atom j (block per target, X zeroed
+// beforehand).  A centre type contributes to its own columns only: a linear
+// column of feature k receives -sum_i dd_k(i)/dd_(i->j) over the centres i of
+// that type with images on j (the runs of j's list; their group vectors sit
+// at the runs' first slots, by feature position), and a product column
+// d_a d_b (d_c) receives -sum_i (d_b dd_a + d_a dd_b ...) with centre i's
+// features as weights.  The linear part is a coalesced column sum of the
+// group vectors (each thread owns S positions per slab); the product columns
+// (a few hundred) are gathered per column.  The self rows add the centre's DS
+// vectors to its own type's columns.  Every X element has one owner thread
+// per type, and types are taken in order, so the sums are deterministic.
+__device__ __forceinline__ void unpack_col(int2 c, int& k0, int& k1, int& k2, int& w) {
+    k0 = c.x & 0xffff;
+    k1 = (c.x >> 16) & 0xffff;
+    k2 = c.y & 0xffff;
+    w = (c.y >> 16) & 0xffff;
+}
 
-template <typename T, int PM>
+template <typename T>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
                                                         const T* Dp, const long long* s_off, const T* DS,
-                                                        const RowItem* items,
-                                                        const long long* f_row, int TR, int CH, T* X, long long ld) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const RowItem it = items[blockIdx.x];
-    const int s = it.st;
+                                                        const long long* f_row, T* X, long long ld) {
+    constexpr int S = 4;  // positions per thread per slab
+    const int gj = blockIdx.x;
+    const int s = B.atom_st[gj];
     if (f_row[s] < 0) return;
-    const int F = M.F;
-    const int c0 = blockIdx.y * CH, c1 = min(F, c0 + CH), nc_blk = c1 - c0;
-    const int sa0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - sa0;
-    const int blk0 = it.a0, nblk = min(TR, n - blk0);
+    const int sa0 = B.st_atom_off[s];
+    const int tj = B.types[gj];
+    const long long r0 = f_row[s] + 3LL * (gj - sa0);
+    const long long q0 = nb_off[gj], qe = nb_off[gj + 1];
     const int NL = M.max_lin;
-    T* out = reinterpret_cast<T*>(smem_raw);  // [TR][3][CH]
-    T* Dk = out + (size_t)TR * 3 * CH;        // [3][NL]
-    T* dcur = Dk + 3 * (size_t)NL;            // [NL]
-    for (int q = threadIdx.x; q < TR * 3 * CH; q += blockDim.x) out[q] = (T)0;
-
-    // the next run at or after entry q of target a (q < 0: the target's first entry); uniform
-    auto find = [&](int a, long long q, RowRun& r) -> bool {
-        while (a < nblk) {
-            const int gj = sa0 + blk0 + a;
-            const long long qe = nb_off[gj + 1];
-            if (q < 0) q = nb_off[gj];
-            while (q < qe) {
+    for (int tc = 0; tc < M.n_type; ++tc) {
+        const DevType& ty = M.types[tc];
+        const int nl = ty.n_lin;
+        const int tp = M.type_pairs[tc * M.n_type + tj];
+        const int* perm = ty.tp_perm + (size_t)tp * nl;
+        const int* ipos = ty.tp_ipos + (size_t)tp * nl;
+        // linear columns: sum of the group vectors of this centre type
+        for (int slab = 0; slab < nl; slab += S * blockDim.x) {
+            T acc[S][3];
+#pragma unroll
+            for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
+            for (long long q = q0; q < qe;) {
                 const int gi = nb_j[q];
                 long long qb = q + 1;
                 while (qb < qe && nb_j[qb] == gi) ++qb;
-                if (gi != gj) {  // images of the target itself exert no force on it
-                    r = RowRun{a, q, qb, gi};
-                    return true;
+                if (gi != gj && B.types[gi] == tc) {
+                    const T* src = Dp + (size_t)q * 3 * NL;
+#pragma unroll
+                    for (int m = 0; m < S; ++m) {
+                        const int x = slab + threadIdx.x + m * blockDim.x;
+                        if (x < nl) {
+                            acc[m][0] += src[x];
+                            acc[m][1] += src[NL + x];
+                            acc[m][2] += src[2 * NL + x];
+                        }
+                    }
                 }
                 q = qb;
             }
-            ++a;
-            q = -1;
-        }
-        return false;
-    };
-    auto perm_of = [&](const RowRun& r) {
-        const int t1 = B.types[r.gi];
-        return M.types[t1].tp_perm +
-               (size_t)M.type_pairs[t1 * M.n_type + B.types[sa0 + blk0 + r.a]] * M.types[t1].n_lin;
-    };
-    T pv[PM > 0 ? PM : 1][4];
-    int pk[PM > 0 ? PM : 1];
-    auto prefetch = [&](const RowRun& r) {
-        const int nl = M.types[B.types[r.gi]].n_lin;
-        const int* perm = perm_of(r);
-        const T* src = Dp + (size_t)r.q * 3 * NL;
-        const T* dsrc = D + d_off[r.gi];
 #pragma unroll
-        for (int m = 0; m < PM; ++m) {
-            const int x = threadIdx.x + m * blockDim.x;
-            if (x < nl) {
-                pk[m] = perm[x];
-                pv[m][0] = src[x];
-                pv[m][1] = src[NL + x];
-                pv[m][2] = src[2 * NL + x];
-                pv[m][3] = dsrc[x];
+            for (int m = 0; m < S; ++m) {
+                const int x = slab + threadIdx.x + m * blockDim.x;
+                if (x >= nl) continue;
+                const int col = ty.lin_col[perm[x]];
+                if (col < 0) continue;
+                T* o = X + (size_t)col * ld + r0;
+                o[0] -= acc[m][0];
+                o[1] -= acc[m][1];
+                o[2] -= acc[m][2];
             }
         }
-    };
-
-    RowRun cur;
-    bool have = find(0, -1, cur);
-    if (PM > 0 && have) prefetch(cur);
-    while (have) {
-        const DevType& ty = M.types[B.types[cur.gi]];
-        const int nl = ty.n_lin;
-        __syncthreads();  // the previous expansion has read Dk and dcur
-        if (PM > 0) {
-#pragma unroll
-            for (int m = 0; m < (PM > 0 ? PM : 1); ++m) {
-                const int x = threadIdx.x + m * blockDim.x;
-                if (x < nl) {
-                    Dk[pk[m]] = pv[m][0];
-                    Dk[NL + pk[m]] = pv[m][1];
-                    Dk[2 * NL + pk[m]] = pv[m][2];
-                    dcur[x] = pv[m][3];
+        // product columns
+        for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
+            const int col = ty.prod_col[p];
+            int k0, k1, k2, w;
+            unpack_col(ty.col_pack[col], k0, k1, k2, w);
+            const int x0 = ipos[k0], x1 = ipos[k1], x2 = w > 2 ? ipos[k2] : 0;
+            T v0 = 0, v1 = 0, v2 = 0;
+            for (long long q = q0; q < qe;) {
+                const int gi = nb_j[q];
+                long long qb = q + 1;
+                while (qb < qe && nb_j[qb] == gi) ++qb;
+                if (gi != gj && B.types[gi] == tc) {
+                    const T* src = Dp + (size_t)q * 3 * NL;
+                    const T* Di = D + d_off[gi];
+                    T w0, w1, w2 = 0;
+                    if (w == 2) {
+                        w0 = Di[k1];
+                        w1 = Di[k0];
+                    } else {
+                        w0 = Di[k1] * Di[k2];
+                        w1 = Di[k0] * Di[k2];
+                        w2 = Di[k0] * Di[k1];
+                    }
+                    v0 += w0 * src[x0] + w1 * src[x1];
+                    v1 += w0 * src[NL + x0] + w1 * src[NL + x1];
+                    v2 += w0 * src[2 * NL + x0] + w1 * src[2 * NL + x1];
+                    if (w > 2) {
+                        v0 += w2 * src[x2];
+                        v1 += w2 * src[NL + x2];
+                        v2 += w2 * src[2 * NL + x2];
+                    }
                 }
+                q = qb;
             }
+            T* o = X + (size_t)col * ld + r0;
+            o[0] -= v0;
+            o[1] -= v1;
+            o[2] -= v2;
+        }
+        __syncthreads();  // a column shared by several types is updated type by type
+    }
+    // self rows: the target as a centre (type tj), its DS self vectors (per type pair, by position)
+    const DevType& ty = M.types[tj];
+    const int nl = ty.n_lin;
+    const T* Di = D + d_off[gj];
+    const T* dsa = DS + s_off[gj];
+    for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+        const int col = ty.lin_col[k];
+        if (col < 0) continue;
+        T v0 = 0, v1 = 0, v2 = 0;
+        for (int l = 0; l < ty.n_tpl; ++l) {
+            const T* ds = dsa + (size_t)l * 9 * nl;
+            const int x = ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + k];
+            v0 += ds[x];
+            v1 += ds[nl + x];
+            v2 += ds[2 * nl + x];
+        }
+        T* o = X + (size_t)col * ld + r0;
+        o[0] += v0;
+        o[1] += v1;
+        o[2] += v2;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
+        const int col = ty.prod_col[p];
+        int k0, k1, k2, w;
+        unpack_col(ty.col_pack[col], k0, k1, k2, w);
+        T w0, w1, w2 = 0;
+        if (w == 2) {
+            w0 = Di[k1];
+            w1 = Di[k0];
         } else {
-            const int* perm = perm_of(cur);
-            const T* src = Dp + (size_t)cur.q * 3 * NL;
-            for (int x = threadIdx.x; x < nl; x += blockDim.x) {
-                const int k = perm[x];
-                Dk[k] = src[x];
-                Dk[NL + k] = src[NL + x];
-                Dk[2 * NL + k] = src[2 * NL + x];
-                dcur[x] = D[d_off[cur.gi] + x];
-            }
+            w0 = Di[k1] * Di[k2];
+            w1 = Di[k0] * Di[k2];
+            w2 = Di[k0] * Di[k1];
         }
-        RowRun nxt;
-        const bool more = find(cur.a, cur.qb, nxt);
-        if (PM > 0 && more) prefetch(nxt);  // in flight during the expansion below
-        __syncthreads();
-        T* o = out + (size_t)cur.a * 3 * CH;
-        for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
-            const int4 ci = ty.col_info[c0 + u];
-            if (ci.w == 0) continue;
-            T vx, vy, vz;
-            if (ci.w == 1) {
-                vx = Dk[ci.x];
-                vy = Dk[NL + ci.x];
-                vz = Dk[2 * NL + ci.x];
-            } else {
-                const T d0 = dcur[ci.x], d1 = dcur[ci.y];
-                if (ci.w == 2) {
-                    vx = d1 * Dk[ci.x] + d0 * Dk[ci.y];
-                    vy = d1 * Dk[NL + ci.x] + d0 * Dk[NL + ci.y];
-                    vz = d1 * Dk[2 * NL + ci.x] + d0 * Dk[2 * NL + ci.y];
-                } else {
-                    const T d2 = dcur[ci.z];
-                    const T w0 = d1 * d2, w1 = d0 * d2, w2 = d0 * d1;
-                    vx = w0 * Dk[ci.x] + w1 * Dk[ci.y] + w2 * Dk[ci.z];
-                    vy = w0 * Dk[NL + ci.x] + w1 * Dk[NL + ci.y] + w2 * Dk[NL + ci.z];
-                    vz = w0 * Dk[2 * NL + ci.x] + w1 * Dk[2 * NL + ci.y] + w2 * Dk[2 * NL + ci.z];
-                }
-            }
-            o[u] -= vx;
-            o[CH + u] -= vy;
-            o[2 * CH + u] -= vz;
-        }
-        cur = nxt;
-        have = more;
-    }
-    __syncthreads();
-    // self rows of the block's centres
-    for (int a = 0; a < nblk; ++a) {
-        const int gi = sa0 + blk0 + a;
-        const DevType& ty = M.types[B.types[gi]];
-        const int nl = ty.n_lin;
-        const T* Di = D + d_off[gi];
-        const T* dsa = DS + s_off[gi];
-        T* o = out + (size_t)a * 3 * CH;
-        for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
-            const int4 ci = ty.col_info[c0 + u];
-            if (ci.w == 0) continue;
-            T w0 = 1, w1 = 0, w2 = 0;
-            if (ci.w == 2) {
-                w0 = Di[ci.y];
-                w1 = Di[ci.x];
-            } else if (ci.w == 3) {
-                w0 = Di[ci.y] * Di[ci.z];
-                w1 = Di[ci.x] * Di[ci.z];
-                w2 = Di[ci.x] * Di[ci.y];
-            }
-            T v[3] = {0, 0, 0};
-            for (int l = 0; l < ty.n_tpl; ++l) {  // self vectors are stored per type pair, by position
-                const T* ds = dsa + (size_t)l * 9 * nl;
-                const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
-                const int x0 = ip[ci.x], x1 = ci.w > 1 ? ip[ci.y] : 0, x2 = ci.w > 2 ? ip[ci.z] : 0;
+        T v[3] = {0, 0, 0};
+        for (int l = 0; l < ty.n_tpl; ++l) {
+            const T* ds = dsa + (size_t)l * 9 * nl;
+            const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
+            const int x0 = ip[k0], x1 = ip[k1], x2 = w > 2 ? ip[k2] : 0;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    v[c] += w0 * ds[(size_t)c * nl + x0];
-                    if (ci.w > 1) v[c] += w1 * ds[(size_t)c * nl + x1];
-                    if (ci.w > 2) v[c] += w2 * ds[(size_t)c * nl + x2];
-                }
+            for (int c = 0; c < 3; ++c) {
+                v[c] += w0 * ds[(size_t)c * nl + x0] + w1 * ds[(size_t)c * nl + x1];
+                if (w > 2) v[c] += w2 * ds[(size_t)c * nl + x2];
             }
-            o[u] += v[0];
-            o[CH + u] += v[1];
-            o[2 * CH + u] += v[2];
         }
-    }
-    __syncthreads();
-    const long long r0 = f_row[s] + 3LL * blk0;
-    for (int u = threadIdx.x; u < nc_blk; u += blockDim.x) {
-        T* xc = X + (size_t)(c0 + u) * ld + r0;
-        for (int a = 0; a < nblk; ++a)
-            for (int c = 0; c < 3; ++c) xc[3 * a + c] = out[(size_t)a * 3 * CH + c * CH + u];
+        T* o = X + (size_t)col * ld + r0;
+        o[0] += v[0];
+        o[1] += v[1];
+        o[2] += v[2];
     }
 }
 
@@ -753,7 +729,8 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     for (int gi = B.st_atom_off[s]; gi < B.st_atom_off[s + 1]; ++gi) {
         const DevType& ty = M.types[B.types[gi]];
-        const int4 ci = ty.col_info[col];
+        int4 ci;
+        unpack_col(ty.col_pack[col], ci.x, ci.y, ci.z, ci.w);
         if (ci.w == 0) continue;
         const T* Di = D + d_off[gi];
         T w0 = 1, w1 = 0, w2 = 0, e;
@@ -852,11 +829,6 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                                                          reinterpret_cast<cplx<T>*>(G));
 }
 
-size_t rows_smem_bytes(const DevModel& M, int TR, int CH, bool fp64) {
-    const size_t ts = fp64 ? 8 : 4;
-    return ((size_t)TR * 3 * CH + (size_t)4 * M.max_lin) * ts;
-}
-
 size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64) {
     const size_t ts = fp64 ? 8 : 4;
     const int nw = kRowsThreads / 32;
@@ -886,15 +858,8 @@ void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb
 template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
                  const long long* d_off, const T* D, const T* Dp, const long long* s_off, const T* DS,
-                 const RowItem* items, int n_items, const long long* f_row, int TR, int CH, int n_chunks, T* X,
-                 long long ld, cudaStream_t st) {
-    const size_t smem = rows_smem_bytes(M, TR, CH, sizeof(T) == 8);
-    const int need = (M.max_lin + kRowsThreads - 1) / kRowsThreads;  // feature positions per thread
-    auto kern = need <= 2 ? pg_rows<T, 2> : need <= 4 ? pg_rows<T, 4> : need <= 6 ? pg_rows<T, 6>
-              : need <= 8 ? pg_rows<T, 8> : pg_rows<T, 0>;
-    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(n_items, n_chunks);
-    kern<<<grid, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, items, f_row, TR, CH, X, ld);
+                 const long long* f_row, T* X, long long ld, cudaStream_t st) {
+    pg_rows<T><<<B.n_atoms, kRowsThreads, 0, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X, ld);
 }
 
 template <typename T>
@@ -921,11 +886,11 @@ template void launch_rows_pairs<float>(const DevModel&, const DevBatch&, const l
                                        const double*, const long long*, const long long*, const long long*,
                                        const void*, const long long*, int*, float*, float*, cudaStream_t);
 template void launch_rows<double>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
-                                  const double*, const double*, const long long*, const double*, const RowItem*, int,
-                                  const long long*, int, int, int, double*, long long, cudaStream_t);
+                                  const double*, const double*, const long long*, const double*, const long long*,
+                                  double*, long long, cudaStream_t);
 template void launch_rows<float>(const DevModel&, const DevBatch&, const long long*, const int*, const long long*,
-                                 const float*, const float*, const long long*, const float*, const RowItem*, int,
-                                 const long long*, int, int, int, float*, long long, cudaStream_t);
+                                 const float*, const float*, const long long*, const float*, const long long*,
+                                 float*, long long, cudaStream_t);
 template void launch_rows_es<double>(const DevModel&, const DevBatch&, const long long*, const double*,
                                      const long long*, const double*, const long long*, const long long*,
                                      const long long*, double*, long long, cudaStream_t);
