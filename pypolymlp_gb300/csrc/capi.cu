@@ -365,6 +365,7 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
     s_gslot.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
     s_order.reserve(sizeof(int) * std::max<long long>(1, b.n_pairs));
     s_Dp.reserve(3 * sizeof(T) * (size_t)dmod.dm.max_lin * std::max<long long>(1, b.n_pairs));
+    PG_CUDA(cudaMemsetAsync(Xd, 0, sizeof(T) * (size_t)ld * flat.n_features, stream));
     if (b.n_atoms > 0) {
         {
             ProfScope ps("pg_nb_mirror", stream);
@@ -379,7 +380,6 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
         }
         {
             ProfScope ps("pg_rows", stream);
-            PG_CUDA(cudaMemsetAsync(Xd, 0, sizeof(T) * (size_t)ld * flat.n_features, stream));
             launch_rows<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), plan.d_d_off.as<long long>(),
                            s_D.as<T>(), s_Dp.as<T>(), plan.d_s_off.as<long long>(), s_DS.as<T>(), d_f_row, Xd, ld,
                            stream);
