@@ -165,6 +165,10 @@ void DeviceBatch::upload_structures(const pg_structures* st, int s_begin, int s_
     atom_st.clear();
     trans.clear();
     pos.clear();
+    std::vector<int> st_cl, cl_bin_start(1, 0), cl_atoms;
+    std::vector<int4> cl_grid, tn;
+    std::vector<double> cl_geom, frac;
+    n_cl = 0;
     long long a = off0;
     for (int s = s_begin; s < s_end; ++s) {
         const int n = st->n_atoms[s];
@@ -175,6 +179,75 @@ void DeviceBatch::upload_structures(const pg_structures* st, int s_begin, int s_
         }
         const CellTranslations ct = cell_translations(st->axis + 9 * (size_t)s, st->positions + 3 * a, n, cutoff);
         for (const auto& t : ct.trans) trans.insert(trans.end(), t.begin(), t.end());
+        for (const auto& t : ct.tn) tn.push_back(make_int4(t[0], t[1], t[2], 0));
+        // fractional coordinates (all atoms; used by cell-list structures)
+        double inv[3][3];
+        {
+            const double(&m)[3][3] = ct.axis;
+            const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                               m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                               m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+            inv[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) / det;
+            inv[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) / det;
+            inv[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) / det;
+            inv[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) / det;
+            inv[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) / det;
+            inv[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) / det;
+            inv[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) / det;
+            inv[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) / det;
+            inv[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / det;
+        }
+        const size_t f0 = frac.size();
+        for (int i = 0; i < n; ++i)
+            for (int r = 0; r < 3; ++r)
+                frac.push_back(inv[r][0] * ct.pos[i][0] + inv[r][1] * ct.pos[i][1] + inv[r][2] * ct.pos[i][2]);
+        if (n >= kCellListMinAtoms) {
+            // bins of at least rc in each direction over the atoms' fractional range; a
+            // sphere of radius rc spans at most rc / h_d in fractional coordinate d
+            // (h_d the cell height across the other two lattice vectors)
+            double fmin[3], fmax[3], h[3], scale[3], rq[3];
+            int g[3];
+            const double(&m)[3][3] = ct.axis;
+            const double vol = std::fabs(m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                                         m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                                         m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]));
+            for (int d = 0; d < 3; ++d) {
+                const int e = (d + 1) % 3, f = (d + 2) % 3;
+                const double cx = m[1][e] * m[2][f] - m[2][e] * m[1][f];
+                const double cy = m[2][e] * m[0][f] - m[0][e] * m[2][f];
+                const double cz = m[0][e] * m[1][f] - m[1][e] * m[0][f];
+                h[d] = vol / std::sqrt(cx * cx + cy * cy + cz * cz);
+                fmin[d] = 1e300;
+                fmax[d] = -1e300;
+                for (int i = 0; i < n; ++i) {
+                    fmin[d] = std::min(fmin[d], frac[f0 + 3 * i + d]);
+                    fmax[d] = std::max(fmax[d], frac[f0 + 3 * i + d]);
+                }
+                const double span = fmax[d] - fmin[d] + 1e-9;
+                g[d] = std::max(1, std::min(256, (int)std::floor(h[d] * span / cutoff)));
+                scale[d] = g[d] / span;
+                rq[d] = cutoff / h[d] * (1.0 + 1e-9) + 1e-12;
+            }
+            const int nb = g[0] * g[1] * g[2];
+            std::vector<std::vector<int>> bins(nb);
+            for (int i = 0; i < n; ++i) {
+                int bi[3];
+                for (int d = 0; d < 3; ++d)
+                    bi[d] = std::min(g[d] - 1, std::max(0, (int)std::floor((frac[f0 + 3 * i + d] - fmin[d]) * scale[d])));
+                bins[(bi[2] * g[1] + bi[1]) * g[0] + bi[0]].push_back((int)(pos.size() / 3) + i);
+            }
+            st_cl.push_back(n_cl++);
+            cl_grid.push_back(make_int4(g[0], g[1], g[2], (int)cl_bin_start.size() - 1));
+            for (int d = 0; d < 3; ++d) cl_geom.push_back(fmin[d]);
+            for (int d = 0; d < 3; ++d) cl_geom.push_back(scale[d]);
+            for (int d = 0; d < 3; ++d) cl_geom.push_back(rq[d]);
+            for (const auto& b : bins) {
+                cl_atoms.insert(cl_atoms.end(), b.begin(), b.end());
+                cl_bin_start.push_back((int)cl_atoms.size());
+            }
+        } else {
+            st_cl.push_back(-1);
+        }
         for (int i = 0; i < n; ++i) {
             pos.insert(pos.end(), ct.pos[i].begin(), ct.pos[i].end());
             types.push_back(st->types[a + i]);
@@ -199,6 +272,14 @@ void DeviceBatch::upload_structures(const pg_structures* st, int s_begin, int s_
     }
     upload(d_posf, posf);
     upload(d_transf, transf);
+    upload(d_st_cl, st_cl);
+    upload(d_cl_grid, cl_grid);
+    upload(d_cl_geom, cl_geom);
+    upload(d_cl_bin_start, cl_bin_start);
+    upload(d_cl_atoms, cl_atoms);
+    upload(d_frac, frac);
+    upload(d_tn, tn);
+    if (d_maxcnt.bytes() == 0) d_maxcnt.alloc(sizeof(int));
     upload(d_st_atom_off, st_atom_off);
     upload(d_st_trans_off, st_trans_off);
     upload(d_trans, trans);
@@ -219,19 +300,26 @@ void DeviceBatch::build_neighbors(double cutoff, cudaStream_t stream) {
         PG_CUDA(cudaMemsetAsync(d_nb_off.as<void>(), 0, sizeof(long long), stream));
         return;
     }
+    PG_CUDA(cudaMemsetAsync(d_maxcnt.as<void>(), 0, sizeof(int), stream));
     {
         ProfScope ps("pg_nb_count", stream);
-        launch_nb_count(B, d_counts.as<int>(), stream);
+        launch_nb_count(B, d_counts.as<int>(), d_maxcnt.as<int>(), stream);
     }
     launch_exclusive_scan(d_counts.as<int>(), n_atoms, d_nb_off.as<long long>(), d_total.as<long long>(), stream);
     long long total = 0;
+    int maxcnt = 0;
     PG_CUDA(cudaMemcpyAsync(&total, d_total.as<long long>(), sizeof(long long), cudaMemcpyDeviceToHost, stream));
+    PG_CUDA(cudaMemcpyAsync(&maxcnt, d_maxcnt.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, stream));
     PG_CUDA(cudaStreamSynchronize(stream));
+    if (maxcnt > kCellListMaxPairs)
+        throw std::runtime_error("more than 4096 neighbours of one atom in a large structure");
     n_pairs = total;
     d_nb_j.reserve(sizeof(int) * std::max<long long>(1, n_pairs));
     d_nb_d.reserve(sizeof(double) * 3 * std::max<long long>(1, n_pairs));
+    if (n_cl > 0) d_keys.reserve(sizeof(long long) * std::max<long long>(1, n_pairs));
     ProfScope ps("pg_nb_fill", stream);
-    launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), stream);
+    launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), d_keys.as<long long>(),
+                   n_cl > 0, stream);
 }
 
 void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
@@ -257,6 +345,13 @@ DevBatch DeviceBatch::view(double cutoff) const {
     B.atom_st = d_atom_st.as<int>();
     B.posf = d_posf.as<float4>();
     B.transf = d_transf.as<float4>();
+    B.st_cl = d_st_cl.as<int>();
+    B.cl_grid = d_cl_grid.as<int4>();
+    B.cl_geom = d_cl_geom.as<double>();
+    B.cl_bin_start = d_cl_bin_start.as<int>();
+    B.cl_atoms = d_cl_atoms.as<int>();
+    B.frac = d_frac.as<double>();
+    B.tn = d_tn.as<int4>();
     B.cutoff = cutoff;
     // FP32 differences of coordinates up to L carry an error below 4 L 2^-24 per
     // component, so |r2_f32 - r2| < 2 rc (12 L 2^-24) + O(L^2 2^-48) + the FP32

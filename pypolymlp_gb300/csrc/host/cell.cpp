@@ -160,8 +160,13 @@ CellTranslations cell_translations(const double* axis, const double* pos, int n,
                 double v[3];
                 c.cart(i, j, k, v);
                 const double d = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-                if (d < max_len + cutoff) out.trans.push_back({v[0], v[1], v[2]});
+                if (d < max_len + cutoff) {
+                    out.trans.push_back({v[0], v[1], v[2]});
+                    out.tn.push_back({i, j, k});
+                }
             }
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) out.axis[r][q] = c.ax[r][q];
     return out;
 }
 

@@ -13,7 +13,9 @@ namespace pg {
 
 struct CellTranslations {
     std::vector<std::array<double, 3>> trans;   // lattice translations (Cartesian)
+    std::vector<std::array<int, 3>> tn;         // their integer coefficients on the (reduced) axis
     std::vector<std::array<double, 3>> pos;     // positions after optional wrapping
+    double axis[3][3];                          // the (reduced) axis, [row][col], columns are lattice vectors
 };
 
 // axis: row-major 3x3 with lattice vectors as columns; pos: n x 3 Cartesian.

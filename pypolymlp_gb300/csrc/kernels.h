@@ -22,13 +22,26 @@ struct DevBatch {
     const float4* transf;      // FP32 copies of trans
     double cutoff;
     float prefilter_r2;        // FP32 squared distance above which a candidate is surely beyond the cutoff
+    // cell lists of the large structures (st_cl[s] >= 0): per such structure a
+    // grid of bins over its atoms' fractional coordinates
+    const int* st_cl;          // per structure: cell-list index or -1
+    const int4* cl_grid;       // per cell list: bins along the three axes, first bin
+    const double* cl_geom;     // per cell list: fmin[3], bins per fractional unit[3], query radius[3]
+    const int* cl_bin_start;   // per bin (all cell lists) + 1: start in cl_atoms
+    const int* cl_atoms;       // batch atom indices, by bin then index
+    const double* frac;        // per atom: fractional coordinates on the reduced axis (cell-list structures)
+    const int4* tn;            // per translation: its integer coefficients
 };
+
+constexpr int kCellListMinAtoms = 1024;  // structures this large use a cell list
+constexpr int kCellListMaxPairs = 4096;  // per atom, for the in-block ordering
 
 constexpr int kRowsThreads = 256;  // threads of pg_rows / pg_rows_pairs blocks
 constexpr int kMaxTypePairs = 64;
 
-void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st);
-void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, cudaStream_t st);
+void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st);
+void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, long long* keys, bool any_cl,
+                    cudaStream_t st);
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
                  const long long* a_off, double2* A, int max_k0, cudaStream_t st);

@@ -1,9 +1,11 @@
 // Training rows of X on the GPU.
 //
 //   pg_nb_count / pg_nb_fill   full neighbour list of every atom of a batch
-//                              (NeighborFull, compute/neighbor_full.cpp:10-76):
+//   (+ pg_nb_order)            (NeighborFull, compute/neighbor_full.cpp:10-76):
 //                              same (j, translation) order and bit-identical
-//                              displacements (IEEE double, no contraction).
+//                              displacements (IEEE double, no contraction);
+//                              structures of 1,024+ atoms search a cell list and
+//                              order their candidates afterwards.
 //   pg_anlm                    a_nlm for m <= 0 of every atom (local.cpp:62-114),
 //                              sums over neighbours accumulated in FP64.
 //   pg_features_adjoint        invariant features d_k of every atom and the
@@ -21,6 +23,8 @@
 //                              columns (model.cpp:159-267).
 //   pg_rows_es                 energy and stress rows per structure.
 #include <cuda_runtime.h>
+
+#include <climits>
 
 #include "kernels.h"
 
@@ -48,7 +52,30 @@ __device__ __forceinline__ bool pair_keep(const DevBatch& B, int i, int j, int t
     return r2 < rc2 && r2 > tol2;
 }
 
-__global__ void pg_nb_count(DevBatch B, int* counts) {
+// Cell-list candidates of atom i (structure with cell list c): for every
+// translation u whose shifted sphere meets the atoms' fractional range, the
+// atoms of the bins it covers.  Calls visit(k_in_cl_atoms_range...) through the
+// bin ranges; the warp iterates bins uniformly and lanes take the atoms.
+struct ClQuery {
+    int lo[3], hi[3];
+};
+__device__ __forceinline__ bool cl_range(const DevBatch& B, int c, const double* fi, int4 n, ClQuery& q) {
+    const int4 g = B.cl_grid[c];
+    const double* geo = B.cl_geom + 9 * c;
+    const int gd[3] = {g.x, g.y, g.z};
+    const int nd[3] = {n.x, n.y, n.z};
+    for (int d = 0; d < 3; ++d) {
+        const double cq = fi[d] - nd[d];
+        const double l = floor((cq - geo[6 + d] - geo[d]) * geo[3 + d]);
+        const double h = floor((cq + geo[6 + d] - geo[d]) * geo[3 + d]);
+        if (h < 0.0 || l > gd[d] - 1) return false;
+        q.lo[d] = l < 0.0 ? 0 : (int)l;
+        q.hi[d] = h > gd[d] - 1 ? gd[d] - 1 : (int)h;
+    }
+    return true;
+}
+
+__global__ void pg_nb_count(DevBatch B, int* counts, int* max_cl) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= B.n_atoms) return;
@@ -57,26 +84,50 @@ __global__ void pg_nb_count(DevBatch B, int* counts) {
     const int a0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - a0;
     const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
     const double rc2 = __dmul_rn(B.cutoff, B.cutoff), tol2 = __dmul_rn(1e-10, 1e-10);
-    const int total = n * nt;  // candidates (j, t), j-major; n * nt < 2^31 (checked on the host)
     int cnt = 0;
-    // lane q = j * nt + t walks the candidates with a carried (j, t) instead of dividing
-    int j = lane / nt, t = lane % nt;
-    const int dj = 32 / nt, dt = 32 % nt;
-    for (int q = lane; q < total; q += 32) {
-        double dx, dy, dz;
-        cnt += pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz) ? 1 : 0;
-        j += dj;
-        t += dt;
-        if (t >= nt) {
-            t -= nt;
-            ++j;
+    const int c = B.st_cl[s];
+    if (c >= 0) {
+        const double fi[3] = {B.frac[3 * (size_t)i], B.frac[3 * (size_t)i + 1], B.frac[3 * (size_t)i + 2]};
+        const int4 g = B.cl_grid[c];
+        for (int u = 0; u < nt; ++u) {
+            ClQuery q;
+            if (!cl_range(B, c, fi, B.tn[t0 + u], q)) continue;
+            for (int bz = q.lo[2]; bz <= q.hi[2]; ++bz)
+                for (int by = q.lo[1]; by <= q.hi[1]; ++by)
+                    for (int bx = q.lo[0]; bx <= q.hi[0]; ++bx) {
+                        const int bin = g.w + (bz * g.y + by) * g.x + bx;
+                        for (int k = B.cl_bin_start[bin] + lane; k < B.cl_bin_start[bin + 1]; k += 32) {
+                            double dx, dy, dz;
+                            cnt += pair_keep(B, i, B.cl_atoms[k], t0 + u, rc2, tol2, dx, dy, dz) ? 1 : 0;
+                        }
+                    }
+        }
+    } else {
+        const int total = n * nt;  // candidates (j, t), j-major; n * nt < 2^31 (checked on the host)
+        // lane q = j * nt + t walks the candidates with a carried (j, t) instead of dividing
+        int j = lane / nt, t = lane % nt;
+        const int dj = 32 / nt, dt = 32 % nt;
+        for (int q = lane; q < total; q += 32) {
+            double dx, dy, dz;
+            cnt += pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz) ? 1 : 0;
+            j += dj;
+            t += dt;
+            if (t >= nt) {
+                t -= nt;
+                ++j;
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if (lane == 0) counts[i] = cnt;
+    if (lane == 0) {
+        counts[i] = cnt;
+        if (c >= 0) atomicMax(max_cl, cnt);
+    }
 }
 
-__global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, double* nb_d) {
+// Brute-force atoms write their list in (j, t) order directly; cell-list atoms
+// write their candidates' keys j_local * nt + t unordered, ordered by pg_nb_order.
+__global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, double* nb_d, long long* keys) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= B.n_atoms) return;
@@ -85,9 +136,41 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
     const int a0 = B.st_atom_off[s], n = B.st_atom_off[s + 1] - a0;
     const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
     const double rc2 = __dmul_rn(B.cutoff, B.cutoff), tol2 = __dmul_rn(1e-10, 1e-10);
-    const int total = n * nt;
     long long w = offsets[i];
     const long long wend = offsets[i + 1];
+    const int c = B.st_cl[s];
+    if (c >= 0) {
+        const double fi[3] = {B.frac[3 * (size_t)i], B.frac[3 * (size_t)i + 1], B.frac[3 * (size_t)i + 2]};
+        const int4 g = B.cl_grid[c];
+        for (int u = 0; u < nt; ++u) {
+            ClQuery q;
+            if (!cl_range(B, c, fi, B.tn[t0 + u], q)) continue;
+            for (int bz = q.lo[2]; bz <= q.hi[2]; ++bz)
+                for (int by = q.lo[1]; by <= q.hi[1]; ++by)
+                    for (int bx = q.lo[0]; bx <= q.hi[0]; ++bx) {
+                        const int bin = g.w + (bz * g.y + by) * g.x + bx;
+                        const int kb = B.cl_bin_start[bin], ke = B.cl_bin_start[bin + 1];
+                        for (int k0 = kb; k0 < ke; k0 += 32) {
+                            const int k = k0 + lane;
+                            int j = 0;
+                            bool keep = false;
+                            if (k < ke) {
+                                double dx, dy, dz;
+                                j = B.cl_atoms[k];
+                                keep = pair_keep(B, i, j, t0 + u, rc2, tol2, dx, dy, dz);
+                            }
+                            const unsigned m = __ballot_sync(0xffffffffu, keep);
+                            if (keep) {
+                                const long long p = w + __popc(m & ((1u << lane) - 1u));
+                                if (p < wend) keys[p] = (long long)(j - a0) * nt + u;
+                            }
+                            w += __popc(m);
+                        }
+                    }
+        }
+        return;
+    }
+    const int total = n * nt;
     int j = lane / nt, t = lane % nt;
     const int dj = 32 / nt, dt = 32 % nt;
     for (int base = 0; base < total; base += 32) {
@@ -113,6 +196,51 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
             }
         }
         w += __popc(m);
+    }
+}
+
+// Cell-list atoms: sort the candidate keys (block per atom, bitonic in shared
+// memory) into the reference's (j, t) order and write the list entries, with
+// the displacement recomputed exactly as pair_keep forms it.
+__global__ void pg_nb_order(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d) {
+    __shared__ long long sk[kCellListMaxPairs];
+    const int i = blockIdx.x;
+    const int s = B.atom_st[i];
+    if (B.st_cl[s] < 0) return;
+    const int a0 = B.st_atom_off[s];
+    const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
+    const long long o0 = offsets[i];
+    const int m = (int)(offsets[i + 1] - o0);
+    if (m > kCellListMaxPairs) return;  // rejected on the host before this launch
+    int p2 = 1;
+    while (p2 < m) p2 <<= 1;
+    for (int q = threadIdx.x; q < p2; q += blockDim.x) sk[q] = q < m ? keys[o0 + q] : LLONG_MAX;
+    __syncthreads();
+    for (int k = 2; k <= p2; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int q = threadIdx.x; q < p2; q += blockDim.x) {
+                const int r = q ^ jj;
+                if (r > q) {
+                    const long long x = sk[q], y = sk[r];
+                    const bool up = (q & k) == 0;
+                    if ((x > y) == up) {
+                        sk[q] = y;
+                        sk[r] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        const long long key = sk[q];
+        const int j = a0 + (int)(key / nt), t = t0 + (int)(key % nt);
+        const double* pi = B.pos + 3 * (size_t)i;
+        const double* pj = B.pos + 3 * (size_t)j;
+        const double* tr = B.trans + 3 * (size_t)t;
+        nb_j[o0 + q] = j;
+        nb_d[3 * (o0 + q)] = __dadd_rn(__dadd_rn(pj[0], -pi[0]), tr[0]);
+        nb_d[3 * (o0 + q) + 1] = __dadd_rn(__dadd_rn(pj[1], -pi[1]), tr[1]);
+        nb_d[3 * (o0 + q) + 2] = __dadd_rn(__dadd_rn(pj[2], -pi[2]), tr[2]);
     }
 }
 
@@ -798,14 +926,16 @@ void launch_exclusive_scan(const int* counts, int n, long long* offsets, long lo
     pg_exclusive_scan<<<1, 1024, 0, st>>>(counts, n, offsets, total);
 }
 
-void launch_nb_count(const DevBatch& B, int* counts, cudaStream_t st) {
+void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st) {
     const int threads = 256, warps = threads / 32;
-    pg_nb_count<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, counts);
+    pg_nb_count<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, counts, max_cl);
 }
 
-void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, cudaStream_t st) {
+void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, long long* keys, bool any_cl,
+                    cudaStream_t st) {
     const int threads = 256, warps = threads / 32;
-    pg_nb_fill<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, nb_j, nb_d);
+    pg_nb_fill<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, nb_j, nb_d, keys);
+    if (any_cl) pg_nb_order<<<B.n_atoms, 256, 0, st>>>(B, off, keys, nb_j, nb_d);
 }
 
 template <typename T>

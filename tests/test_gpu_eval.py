@@ -146,3 +146,18 @@ def test_properties_api_matches_oracle():
     assert forces[0].shape == (3, n0)
     # fractional round trip changes positions at the 1e-15 level
     assert _rel(energies, e_ref) < 1e-8
+
+
+def test_eval_large_cell_matches_oracle():
+    """A 1,024-atom bcc cell (cell-list neighbour search) against the oracle."""
+    from pypolymlp_gb300 import _ffi
+
+    kw, _ = EVAL_CASES["binary_mt3"]
+    p = make_params_dict(**kw)
+    ss = syn.bcc_supercell(8, a=3.2, sigma=0.1, seed=7)
+    st = Structures(ss.axis, ss.positions, ss.types)
+    c = _coeffs(p, 11)
+    ref = oracle.evaluate(p, c, st)
+    got = _ffi.Evaluator(p, c, _ffi.PG_FP64).run(st)
+    for g, r in zip(got, ref):
+        assert _rel(g, r) < FP64_RTOL

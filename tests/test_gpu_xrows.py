@@ -118,3 +118,26 @@ def test_empty_and_single_atom_structures():
     ref = oracle.features_x(p, st, e, f, s, n)
     x = _model(p).features_x(st, e, f, s, n, precision=_ffi.PG_FP64)
     assert _colrel(x, ref) < FP64_RTOL
+
+
+def test_neighbor_list_bit_exact_cell_list():
+    """Structures of 1,024+ atoms search a cell list and re-order their
+    candidates; the list must still equal the reference's (j, translation)
+    order bit for bit: a bcc 8x8x8 cell (1,024 atoms) and a sheared triclinic
+    cell of 1,200 atoms."""
+    from pypolymlp_gb300 import _ffi
+
+    ss = syn.bcc_supercell(8, a=3.2, sigma=0.1, seed=6)
+    rng = np.random.default_rng(8)
+    ax = np.array([[21.0, 3.0, -2.0], [0.0, 19.0, 4.0], [0.0, 0.0, 18.0]])
+    frac = rng.random((1200, 3))
+    axis = [ss.axis[0], ax]
+    pos = [ss.positions[0], frac @ ax.T]
+    types = [ss.types[0], rng.integers(0, 2, 1200).astype(np.int32)]
+    st = Structures(axis, pos, types)
+    for s in range(st.n_st):
+        go, gj, gd = _ffi.neighbor_list(st, s, 7.0)
+        oo, oj, od = oracle.neighbor_list(st, s, 7.0, half=False)
+        np.testing.assert_array_equal(go, oo)
+        np.testing.assert_array_equal(gj, oj)
+        np.testing.assert_array_equal(gd, od)
