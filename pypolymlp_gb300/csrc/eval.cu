@@ -14,7 +14,8 @@
 //   pg_nb_mirror       index of the mirror image (j -> i, -d) of every pair
 //                      (exact: -d is bit-identical; xrows.cu)
 //   pg_eval_gather     F_b = sum_{q in list(b)} (g_q - g_mirror(q))   (no atomics)
-//   pg_eval_reduce     E = sum_i E_i and stress = -sum_p d_p (x) g_p per structure
+//   pg_eval_gather     also the per-centre virial -sum_{p in list(i)} d_p (x) g_p
+//   pg_eval_reduce     E = sum_i E_i and stress = sum_i virial_i per structure
 // Energies match the reference's Euler-split pair sums, and forces/stress its
 // half-list collection, up to summation order.
 #include <cuda_runtime.h>
@@ -193,36 +194,40 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
 
 // F_b = sum_{q in list(b)} (g_q - g_mirror(q)); one thread per atom, FP64.
 __global__ void pg_eval_gather(int n_atoms, const long long* nb_off, const long long* mirror, const double* g,
-                               double* forces) {
+                               const double* nb_d, double* forces, double* vir) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_atoms) return;
-    double f[3] = {0, 0, 0};
+    double f[3] = {0, 0, 0}, v[6] = {0, 0, 0, 0, 0, 0};
     for (long long q = nb_off[b]; q < nb_off[b + 1]; ++q) {
         const long long m = mirror[q];
-        for (int c = 0; c < 3; ++c) f[c] += g[3 * q + c] - (m >= 0 ? g[3 * m + c] : 0.0);
+        const double gx = g[3 * q], gy = g[3 * q + 1], gz = g[3 * q + 2];
+        f[0] += gx - (m >= 0 ? g[3 * m] : 0.0);
+        f[1] += gy - (m >= 0 ? g[3 * m + 1] : 0.0);
+        f[2] += gz - (m >= 0 ? g[3 * m + 2] : 0.0);
+        const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
+        v[0] -= dx * gx;
+        v[1] -= dy * gy;
+        v[2] -= dz * gz;
+        v[3] -= dx * gy;
+        v[4] -= dy * gz;
+        v[5] -= dz * gx;
     }
     for (int c = 0; c < 3; ++c) forces[3 * (size_t)b + c] = f[c];
+    for (int c = 0; c < 6; ++c) vir[6 * (size_t)b + c] = v[c];
 }
 
-// Per structure: E = sum_i E_i and stress = -sum_p d_p (x) g_p over the full list
-// (xx yy zz xy yz zx, with xy = -d_x g_y): the half-list sum of
-// polymlp_eval.cpp:293-336, whose pair force is -(g_ij - g_ji), written per
-// directed pair.
-__global__ void pg_eval_reduce(const int* st_atom_off, const long long* nb_off, const double* nb_d,
-                               const double* g, const double* Eatom, double* energy, double* stress) {
+// Per structure: E = sum_i E_i and stress = sum_i vir_i, with vir_i =
+// -sum_{p in list(i)} d_p (x) g_p (xx yy zz xy yz zx, xy = -d_x g_y): the
+// half-list sum of polymlp_eval.cpp:293-336, whose pair force is
+// -(g_ij - g_ji), written per directed pair and summed per centre first.
+__global__ void pg_eval_reduce(const int* st_atom_off, const double* Eatom, const double* vir, double* energy,
+                               double* stress) {
     const int s = blockIdx.x;
     const int a0 = st_atom_off[s], a1 = st_atom_off[s + 1];
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) acc[0] += Eatom[a];
-    for (long long p = nb_off[a0] + threadIdx.x; p < nb_off[a1]; p += blockDim.x) {
-        const double gx = g[3 * p], gy = g[3 * p + 1], gz = g[3 * p + 2];
-        const double dx = nb_d[3 * p], dy = nb_d[3 * p + 1], dz = nb_d[3 * p + 2];
-        acc[1] -= dx * gx;
-        acc[2] -= dy * gy;
-        acc[3] -= dz * gz;
-        acc[4] -= dx * gy;
-        acc[5] -= dy * gz;
-        acc[6] -= dz * gx;
+    for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+        acc[0] += Eatom[a];
+        for (int q = 0; q < 6; ++q) acc[1 + q] += vir[6 * (size_t)a + q];
     }
     __shared__ double red[7][256];
     for (int q = 0; q < 7; ++q) red[q][threadIdx.x] = acc[q];
@@ -244,7 +249,7 @@ struct Evaluator {
     DevBuf coef;
     std::vector<DevBuf> bufs;
     EvalTables et{};
-    DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_g, s_mirror, s_missing, d_E, d_S, d_F;
+    DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_vir, s_g, s_mirror, s_missing, d_E, d_S, d_F;
     cudaStream_t stream = 0;
 
     Evaluator(const pg_feature_params* fp, const double* coeffs, int n, int prec) : precision(prec) {
@@ -285,6 +290,7 @@ struct Evaluator {
         s_Anc.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
         s_Aadj.reserve(2 * sizeof(T) * std::max<long long>(1, a_tot));
         s_E.reserve(sizeof(double) * std::max(1, b.n_atoms));
+        s_vir.reserve(sizeof(double) * 6 * std::max(1, b.n_atoms));
         s_g.reserve(sizeof(double) * 3 * std::max<long long>(1, b.n_pairs));
         s_mirror.reserve(sizeof(long long) * std::max<long long>(1, b.n_pairs));
         s_missing.reserve(sizeof(int));
@@ -329,12 +335,11 @@ struct Evaluator {
                 ProfScope ps("pg_eval_gather", stream);
                 pg_eval_gather<<<(b.n_atoms + 127) / 128, 128, 0, stream>>>(
                     b.n_atoms, b.d_nb_off.as<long long>(), s_mirror.as<long long>(), s_g.as<double>(),
-                    d_F.as<double>());
+                    b.d_nb_d.as<double>(), d_F.as<double>(), s_vir.as<double>());
             }
             ProfScope ps("pg_eval_reduce", stream);
-            pg_eval_reduce<<<b.n_st, 256, 0, stream>>>(b.d_st_atom_off.as<int>(), b.d_nb_off.as<long long>(),
-                                                       b.d_nb_d.as<double>(), s_g.as<double>(), s_E.as<double>(),
-                                                       d_E.as<double>(), d_S.as<double>());
+            pg_eval_reduce<<<b.n_st, 256, 0, stream>>>(b.d_st_atom_off.as<int>(), s_E.as<double>(),
+                                                       s_vir.as<double>(), d_E.as<double>(), d_S.as<double>());
         } else {
             PG_CUDA(cudaMemsetAsync(d_E.as<void>(), 0, sizeof(double) * b.n_st, stream));
             PG_CUDA(cudaMemsetAsync(d_S.as<void>(), 0, sizeof(double) * 6 * b.n_st, stream));
