@@ -171,39 +171,51 @@ def cpu_baseline(params, data, sample, n_threads):
 
 def eval_bench(params, args):
     """E/F/S atoms/s of the evaluator (pg_eval_run through the C ABI, host
-    buffers, neighbour lists included) on a bcc cell of n^3 x 2 atoms
-    (a = 3.2 A, sigma 0.1 A, 50/50 random species) with the X^T X model,
-    mixed precision; kernel times from the device profiler."""
+    buffers, neighbour lists included) on bcc cells of n^3 x 2 atoms (a = 3.2 A,
+    sigma 0.1 A, 50/50 random species) with the X^T X model, mixed precision;
+    kernel times from the device profiler.  The headline cell is --eval-cell
+    (default 20: 16,000 atoms); the 1,024- and 128,000-atom cells of the same
+    family are reported beside it."""
     import torch
 
     from pypolymlp_gb300 import _ffi
     from pypolymlp_gb300 import synthetic as syn
     from pypolymlp_gb300.abi import Structures
 
-    n = args.eval_cell
-    sset = syn.bcc_supercell(n, a=3.2, sigma=0.1, seed=4)
-    st = Structures(sset.axis, sset.positions, sset.types)
-    n_atoms = int(st.n_atoms.sum())
     coefs = np.random.default_rng(4).normal(size=_ffi.Model(params).n_features) * 1e-3
     ev = _ffi.Evaluator(params, coefs, _ffi.PG_MIXED)
-    ev.run(st)  # warm-up
-    torch.cuda.synchronize()
-    reps = 3
-    _ffi.profile_enable(True)
-    _ffi.profile_read()
-    t0 = time.time()
-    for _ in range(reps):
-        ev.run(st)
-    dt = (time.time() - t0) / reps
-    prof = _ffi.profile_read()
-    _ffi.profile_enable(False)
-    dev_ms = sum(v[0] for v in prof.values()) / reps
-    return {"metric": "E/F/S atoms/s (mixed)", "value": n_atoms / dt, "unit": "atoms/s",
-            "device_atoms_per_s": n_atoms / (dev_ms / 1e3) if dev_ms > 0 else None,
-            "workload": f"bcc {n}x{n}x{n}x2 = {n_atoms} atoms, a 3.2 A, the X^T X model (F = {len(coefs)})",
-            "h2d_bytes": int(st.positions.nbytes + st.axis.nbytes + st.types.nbytes),
-            "d2h_bytes": int(n_atoms * 24 + 56),
-            "kernels": {k: {"ms": v[0] / reps, "launches": v[1] // reps} for k, v in prof.items()}}
+
+    def one(n):
+        sset = syn.bcc_supercell(n, a=3.2, sigma=0.1, seed=4)
+        st = Structures(sset.axis, sset.positions, sset.types)
+        n_atoms = int(st.n_atoms.sum())
+        ev.run(st)  # warm-up
+        torch.cuda.synchronize()
+        reps = 3
+        _ffi.profile_enable(True)
+        _ffi.profile_read()
+        t0 = time.time()
+        for _ in range(reps):
+            ev.run(st)
+        dt = (time.time() - t0) / reps
+        prof = _ffi.profile_read()
+        _ffi.profile_enable(False)
+        dev_ms = sum(v[0] for v in prof.values()) / reps
+        return {"metric": "E/F/S atoms/s (mixed)", "value": n_atoms / dt, "unit": "atoms/s",
+                "device_atoms_per_s": n_atoms / (dev_ms / 1e3) if dev_ms > 0 else None,
+                "workload": f"bcc {n}x{n}x{n}x2 = {n_atoms} atoms, a 3.2 A, the X^T X model (F = {len(coefs)})",
+                "h2d_bytes": int(st.positions.nbytes + st.axis.nbytes + st.types.nbytes),
+                "d2h_bytes": int(n_atoms * 24 + 56),
+                "kernels": {k: {"ms": v[0] / reps, "launches": v[1] // reps} for k, v in prof.items()}}
+
+    out = one(args.eval_cell)
+    out["other_cells"] = {}
+    for n in (8, 40):
+        if n != args.eval_cell:
+            r = one(n)
+            out["other_cells"][r["workload"].split(" = ")[1].split(",")[0]] = {
+                "value": r["value"], "device_atoms_per_s": r["device_atoms_per_s"]}
+    return out
 
 
 def run_reference(args):
