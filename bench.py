@@ -209,6 +209,18 @@ def eval_bench(params, args):
                 "kernels": {k: {"ms": v[0] / reps, "launches": v[1] // reps} for k, v in prof.items()}}
 
     out = one(args.eval_cell)
+    if not args.no_cpu_baseline:
+        # the reference's evaluator restated (oracle, all host threads) on the 1,024-atom cell
+        from oracle import oracle
+
+        sset = syn.bcc_supercell(8, a=3.2, sigma=0.1, seed=4)
+        st = Structures(sset.axis, sset.positions, sset.types)
+        n_threads = os.cpu_count() or 1
+        t0 = time.time()
+        oracle.evaluate(params, coefs, st, n_threads=n_threads)
+        dt = time.time() - t0
+        out["cpu_baseline"] = {"value": 1024 / dt, "unit": "atoms/s", "cores": n_threads, "kind": "port",
+                               "sample": f"bcc 8x8x8x2 = 1024 atoms, CPU oracle E/F/S, {dt:.2f}s"}
     out["other_cells"] = {}
     for n in (8, 40):
         if n != args.eval_cell:
