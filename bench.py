@@ -272,7 +272,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--ref-sample", type=int, default=48)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fp64", action="store_true", help="time the FP64 judge path instead")
+    ap.add_argument("--fp64", action="store_true", help="time the FP64 reference-precision path instead")
     ap.add_argument("--no-eval", action="store_true", help="skip the E/F/S evaluation figure")
     ap.add_argument("--eval-cell", type=int, default=20, help="bcc repeats n (n^3 x 2 atoms) of the E/F/S cell")
     args = ap.parse_args()

@@ -519,11 +519,10 @@ template void Model::batch_rows<double>(DeviceBatch&, const long long*, const lo
 template void Model::batch_rows<float>(DeviceBatch&, const long long*, const long long*, const long long*, float*,
                                        long long, cudaStream_t);
 
-// Split [0, n_st) into batches whose staged data fits the device budget.
-// Split [0, n_st) into batches whose staged data fits the device budget.  Pairs
+// Split [0, n_st) into batches whose staged data fits the device memory limit.  Pairs
 // per atom are estimated from each cell's density: N / V * 4/3 pi rc^3, with a
 // margin for clustering.
-std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bool fp64, size_t budget) const {
+std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bool fp64, size_t limit) const {
     std::vector<std::pair<int, int>> out;
     const double rc = flat.cutoff;
     const double sphere = 4.0 / 3.0 * 3.14159265358979323846 * rc * rc * rc;
@@ -536,7 +535,7 @@ std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bo
         const int n = st->n_atoms[s];
         const double pairs = vol > 0.0 ? 1.5 * n / vol * sphere + 8.0 : 300.0;
         const double bytes = (double)n * (double)bytes_per_atom(fp64, pairs);
-        if (s > s0 && acc + bytes > (double)budget) {
+        if (s > s0 && acc + bytes > (double)limit) {
             out.push_back({s0, s});
             s0 = s;
             acc = 0.0;
@@ -547,7 +546,7 @@ std::vector<std::pair<int, int>> Model::plan_batches(const pg_structures* st, bo
     return out;
 }
 
-size_t device_budget_bytes() {
+size_t device_batch_bytes() {
     if (const char* e = std::getenv("PG_BATCH_BYTES")) return (size_t)std::atoll(e);
     size_t free_b = 0, total_b = 0;
     PG_CUDA(cudaMemGetInfo(&free_b, &total_b));
@@ -667,7 +666,7 @@ int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, c
         const bool fp64 = precision == PG_FP64;
         const int F = m.flat.n_features;
         cudaStream_t stream = 0;
-        const auto batches = m.plan_batches(st, fp64, device_budget_bytes());
+        const auto batches = m.plan_batches(st, fp64, device_batch_bytes());
         DeviceBatch b;
         DevBuf Xd, X64, d_e, d_f, d_s;
         for (const auto& bt : batches) {

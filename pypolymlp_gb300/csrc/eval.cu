@@ -395,7 +395,7 @@ int pg_eval_run(pg_eval* eh, const pg_structures* st, double* energy, double* fo
         const bool fp64 = ev.precision == PG_FP64;
         DeviceBatch b;
         long long a = 0;
-        for (const auto& bt : ev.m->plan_batches(st, fp64, device_budget_bytes())) {
+        for (const auto& bt : ev.m->plan_batches(st, fp64, device_batch_bytes())) {
             b.upload_structures(st, bt.first, bt.second, ev.m->flat.cutoff);
             if (fp64) ev.run_batch<double>(b, energy + bt.first, forces + 3 * a, stress + 6 * bt.first);
             else ev.run_batch<float>(b, energy + bt.first, forces + 3 * a, stress + 6 * bt.first);

@@ -3,7 +3,7 @@
 // (src/pypolymlp/mlp_dev/core/data_sequential.py:97-153) with X generated in
 // HBM by pg_rows.
 //
-//   pg_syrk_f64        FP64 judge path: upper-triangle tiles of X^T X on the
+//   pg_syrk_f64        FP64 path: upper-triangle tiles of X^T X on the
 //                      CUDA cores (64x64 tile per block, 4x4 per thread).
 //   gram_tc (file gram_tc.cu) mixed path: X (FP32) split into bf16 hi + lo,
 //                      X^T X ~= hi^T hi + hi^T lo + lo^T hi on the tcgen05
@@ -213,7 +213,7 @@ std::vector<std::unique_ptr<Prepared>> prepare_batches(Model& m, const pg_struct
             throw std::runtime_error("force/stress rows out of range");
     }
     std::vector<std::unique_ptr<Prepared>> out;
-    for (const auto& bt : m.plan_batches(st, fp64, device_budget_bytes())) {
+    for (const auto& bt : m.plan_batches(st, fp64, device_batch_bytes())) {
         const int s0 = bt.first, s1 = bt.second, nb = s1 - s0;
         auto P = std::make_unique<Prepared>();
         std::vector<long long> le(nb), lf(nb, -1), ls(nb, -1);

@@ -33,7 +33,7 @@ struct Model {
 
     void atom_offsets(const DeviceBatch& b, AtomOffsets& o) const;
     size_t bytes_per_atom(bool fp64, double mean_pairs) const;
-    std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t budget) const;
+    std::vector<std::pair<int, int>> plan_batches(const pg_structures* st, bool fp64, size_t limit) const;
 
     void plan_rows(const DeviceBatch& b, RowPlan& plan) const;
     template <typename T>
@@ -45,7 +45,7 @@ struct Model {
                     T* Xd, long long ld, cudaStream_t stream);
 };
 
-size_t device_budget_bytes();
+size_t device_batch_bytes();
 
 }  // namespace pg
 
