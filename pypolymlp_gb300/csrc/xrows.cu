@@ -445,7 +445,9 @@ __device__ __forceinline__ int h_pos(int u, int w) {
 }
 template <>
 __device__ __forceinline__ int h_pos<float>(int u, int w) {
-    return (((w >> 1) ^ (u & 3)) << 1) | (w & 1);  // two complex<float> per 16 bytes
+    // two complex<float> per 16 bytes; a 64-byte row is half a bank row, so
+    // bit 0 of u picks the half and bits 1-2 the piece: 8 positions in all
+    return (((w >> 1) ^ ((u >> 1) & 3)) << 1) | (w & 1);
 }
 template <typename T>
 __device__ __forceinline__ void load_h8(const cplx<T>* h, int u, cplx<T> (&v)[8]) {
@@ -457,7 +459,7 @@ __device__ __forceinline__ void load_h8<float>(const cplx<float>* h, int u, cplx
     const float4* p = reinterpret_cast<const float4*>(h);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float4 x = p[q ^ (u & 3)];
+        const float4 x = p[q ^ ((u >> 1) & 3)];
         v[2 * q] = {x.x, x.y};
         v[2 * q + 1] = {x.z, x.w};
     }
