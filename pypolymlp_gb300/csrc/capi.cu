@@ -135,7 +135,7 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
                 const int h = ft.tp_heads[q];
                 if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
                     throw std::runtime_error("model too large for the packed head indices");
-                tnk[q] = ft.head_nid[h] | (ft.head_key[h] << 8);
+                tnk[ft.tp_head_off[tp] + ft.tp_head_row[q]] = ft.head_nid[h] | (ft.head_key[h] << 8);
             }
         d.tp_head_nk = (const int*)up(tnk);
         d.n_groups = ft.n_groups;

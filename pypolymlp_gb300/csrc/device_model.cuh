@@ -64,7 +64,7 @@ struct DevType {
     const int *lin_col, *prod_col;  // per feature: its linear column (-1: none); the product columns
     const int* ent_tp_off;     // per linear feature k: (n_tp + 1) entry offsets by type pair
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
-    const int* tp_head_nk;     // per tp_heads entry: radial index | Y_lm index << 8
+    const int* tp_head_nk;     // per gradient-tile row of a type pair (tp_head_off order): radial index | Y_lm index << 8
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
     int n_groups, lay_size, n_tpl;
     const int *lay_ent, *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;

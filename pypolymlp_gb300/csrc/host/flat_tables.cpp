@@ -20,6 +20,83 @@ FlatTerm make_term(double coeff, const std::vector<int>& ids, int conj) {
     return t;
 }
 
+// Rows of the head-space gradient tile for the nh heads of one type pair.
+// The force-row contraction reads, per rank of a 32-feature group, the rows of
+// the heads that the group's entries of that rank name; row r sits in
+// shared-memory bank set r mod 8, so heads read together should have distinct
+// rows mod 8 (same head: broadcast, no conflict).  `ranks` lists the distinct
+// heads (0..nh-1) read together.  Greedy colouring (most-read heads first,
+// each to the class that least raises the ranks' largest class), then one
+// pass of pairwise swaps that lower the sum over ranks of the largest class;
+// class c gets rows c, c + 8, ...  Returns the row of each head.
+std::vector<int> colour_head_rows(int nh, const std::vector<std::vector<int>>& ranks) {
+    constexpr int kC = 8;
+    std::vector<std::vector<int>> ranks_of(nh);
+    for (size_t r = 0; r < ranks.size(); ++r)
+        for (int u : ranks[r]) ranks_of[u].push_back((int)r);
+    std::vector<std::array<int, kC>> cls(ranks.size());
+    for (auto& a : cls) a.fill(0);
+    auto largest = [&](int r) { return *std::max_element(cls[r].begin(), cls[r].end()); };
+    std::vector<int> cap(kC, 0), col(nh, 0), order(nh);
+    for (int u = 0; u < nh; ++u) {
+        cap[u % kC]++;
+        order[u] = u;
+    }
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return ranks_of[a].size() > ranks_of[b].size(); });
+    for (int u : order) {
+        long best = -1;
+        int bc = 0;
+        for (int c = 0; c < kC; ++c) {
+            if (cap[c] == 0) continue;
+            long cost = 0;
+            for (int r : ranks_of[u]) cost += (cls[r][c] + 1 > largest(r) ? 16 : 0) + cls[r][c];
+            if (best < 0 || cost < best) {
+                best = cost;
+                bc = c;
+            }
+        }
+        col[u] = bc;
+        cap[bc]--;
+        for (int r : ranks_of[u]) cls[r][bc]++;
+    }
+    auto move = [&](int u, int from, int to) {
+        for (int r : ranks_of[u]) {
+            cls[r][from]--;
+            cls[r][to]++;
+        }
+    };
+    std::vector<int> touched;
+    for (int a = 0; a < nh; ++a)
+        for (int b = a + 1; b < nh; ++b) {
+            const int ca = col[a], cb = col[b];
+            if (ca == cb || ranks_of[a].empty()) continue;
+            touched.assign(ranks_of[a].begin(), ranks_of[a].end());
+            touched.insert(touched.end(), ranks_of[b].begin(), ranks_of[b].end());
+            std::sort(touched.begin(), touched.end());
+            touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+            long before = 0, after = 0;
+            for (int r : touched) before += largest(r);
+            move(a, ca, cb);
+            move(b, cb, ca);
+            for (int r : touched) after += largest(r);
+            if (after < before) {
+                col[a] = cb;
+                col[b] = ca;
+            } else {
+                move(a, cb, ca);
+                move(b, ca, cb);
+            }
+        }
+    std::vector<int> next(kC), row(nh);
+    for (int c = 0; c < kC; ++c) next[c] = c;
+    for (int u = 0; u < nh; ++u) {
+        row[u] = next[col[u]];
+        next[col[u]] += kC;
+    }
+    return row;
+}
+
 }  // namespace
 
 FlatModel flatten_model(const ModelTables& mt) {
@@ -206,6 +283,7 @@ FlatModel flatten_model(const ModelTables& mt) {
             ft.lay_grp_base.assign((size_t)ntp * ft.n_groups, 0);
             ft.lay_grp_cnt.assign((size_t)ntp * ft.n_groups, 0);
             ft.tpl.assign(ntp, -1);
+            ft.tp_head_row.assign(ft.tp_heads.size(), 0);
             for (int tp = 0; tp < ntp; ++tp) {
                 if (ft.tp_head_off[tp + 1] > ft.tp_head_off[tp]) {
                     ft.tpl[tp] = (int)ft.tpl_tp.size();
@@ -221,18 +299,36 @@ FlatModel flatten_model(const ModelTables& mt) {
                     ft.tp_perm[(size_t)tp * nl + x] = order[x];
                     ft.tp_ipos[(size_t)tp * nl + order[x]] = x;
                 }
+                const size_t tp_base = ft.lay_ent.size();
+                std::vector<std::vector<int>> ranks;
                 for (int g = 0; g < ft.n_groups; ++g) {
                     const int c = cnt(order[32 * g]);
                     ft.lay_grp_base[(size_t)tp * ft.n_groups + g] = (int)ft.lay_ent.size();
                     ft.lay_grp_cnt[(size_t)tp * ft.n_groups + g] = c;
-                    for (int r = 0; r < c; ++r)
+                    for (int r = 0; r < c; ++r) {
+                        std::vector<int> heads;
                         for (int l = 0; l < 32; ++l) {
                             const int x = 32 * g + l;
                             int e = -1;
                             if (x < nl && r < cnt(order[x])) e = ft.ent_tp_off[(size_t)order[x] * (ntp + 1) + tp] + r;
                             ft.lay_ent.push_back(e);
                             ft.lay_hpos.push_back(e >= 0 ? hpos_of[ft.ent_head[e]] : 0);
+                            if (e >= 0) heads.push_back(hpos_of[ft.ent_head[e]]);
                         }
+                        std::sort(heads.begin(), heads.end());
+                        heads.erase(std::unique(heads.begin(), heads.end()), heads.end());
+                        ranks.push_back(std::move(heads));
+                    }
+                }
+                // head -> row of the gradient tile; a zero entry reads the row of
+                // its rank's first entry (lane 0 holds the group's largest feature)
+                const int q0 = ft.tp_head_off[tp], nh = ft.tp_head_off[tp + 1] - q0;
+                const std::vector<int> row = colour_head_rows(nh, ranks);
+                for (int q = 0; q < nh; ++q) ft.tp_head_row[q0 + q] = row[q];
+                for (size_t s = tp_base; s < ft.lay_ent.size(); s += 32) {
+                    const int first = row[ft.lay_hpos[s]];
+                    for (int l = 0; l < 32; ++l)
+                        ft.lay_hpos[s + l] = ft.lay_ent[s + l] >= 0 ? row[ft.lay_hpos[s + l]] : first;
                 }
             }
             ft.lay_size = (int)ft.lay_ent.size();

@@ -62,9 +62,12 @@ struct FlatType {
     // lane holds the r-th entry of the feature at position 32g + lane
     // (lay_ent = -1 where that feature has fewer entries: a zero entry).
     // n_groups = ceil(n_lin / 32); lay_grp_cnt[tp][g] = entries of the group's
-    // first (largest) feature.
+    // first (largest) feature.  lay_hpos is the row of the entry's head in the
+    // per-type-pair gradient tile: tp_head_row[q] for the tp_heads entry q, rows
+    // coloured so that the heads one rank reads fall in distinct bank sets; a
+    // zero entry repeats the row of its rank's lane 0.
     int n_groups = 0, lay_size = 0;
-    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos;
+    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_head_row;
     // type pairs with heads for this centre type: local index or -1, and back
     std::vector<int> tpl, tpl_tp;
 };
