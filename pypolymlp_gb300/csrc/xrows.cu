@@ -605,27 +605,38 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                     T sv[9];
 #pragma unroll
                     for (int v = 0; v < 9; ++v) sv[v] = (ds && x < nl) ? ds[(size_t)v * nl + x] : (T)0;
-                    // the next rank's entry is loaded while this one is contracted
-                    cplx<T> gn = {(T)0, (T)0};
-                    int un = 0;
-                    if (cnt > 0) {
-                        gn = Gi[base + lane];
-                        un = ty.lay_hpos[base + lane];
-                    }
-                    for (int r = 0; r < cnt; ++r) {
-                        const cplx<T> g = gn;
-                        const int u = un;
-                        if (r + 1 < cnt) {
-                            const int sl = base + 32 * (r + 1) + lane;
-                            gn = Gi[sl];
-                            un = ty.lay_hpos[sl];
+                    // entries are loaded kPrefetch ranks ahead of the one contracted
+                    constexpr int kPrefetch = 4;
+                    cplx<T> gq[kPrefetch];
+                    int uq[kPrefetch];
+#pragma unroll
+                    for (int s = 0; s < kPrefetch; ++s) {
+                        gq[s] = {(T)0, (T)0};
+                        uq[s] = 0;
+                        if (s < cnt) {
+                            gq[s] = Gi[base + 32 * s + lane];
+                            uq[s] = ty.lay_hpos[base + 32 * s + lane];
                         }
+                    }
+                    for (int r0 = 0; r0 < cnt; r0 += kPrefetch) {
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            cplx<T> h[8];
-                            load_h8<T>(H + ((size_t)c * HT + u) * NW, u, h);
+                        for (int s = 0; s < kPrefetch; ++s) {
+                            const int r = r0 + s;
+                            if (r >= cnt) break;
+                            const cplx<T> g = gq[s];
+                            const int u = uq[s];
+                            if (r + kPrefetch < cnt) {
+                                const int sl = base + 32 * (r + kPrefetch) + lane;
+                                gq[s] = Gi[sl];
+                                uq[s] = ty.lay_hpos[sl];
+                            }
 #pragma unroll
-                            for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
+                            for (int c = 0; c < 3; ++c) {
+                                cplx<T> h[8];
+                                load_h8<T>(H + ((size_t)c * HT + u) * NW, u, h);
+#pragma unroll
+                                for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
+                            }
                         }
                     }
                     if (x >= nl) continue;
