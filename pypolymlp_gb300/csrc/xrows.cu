@@ -245,74 +245,91 @@ __global__ void pg_nb_order(DevBatch B, const long long* offsets, const long lon
 }
 
 // ---------------------------------------------------------------- K2 a_nlm
-// Block per centre atom.  Warps compute the basis of one neighbour each;
-// every thread then adds fn * Y into the heads it owns (FP64 sums).
+// Block per centre atom, pairs taken one type pair at a time: the pairs of
+// that type pair are compacted into a list (256 at a time), warps compute the
+// basis of one pair each (8 pairs per chunk), then every thread adds the
+// chunk's fn * Y into the heads of that type pair it owns: a partial sum over
+// the chunk in T, added to the FP64 total once per chunk.
 template <typename T>
-__global__ void pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                        const long long* a_off, double2* A) {
+__global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j,
+                                               const double* nb_d, const long long* a_off, double2* A) {
+    constexpr int NW = 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_list[256], s_wcnt[NW], s_ok[NW];
     const int i = blockIdx.x;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
-    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
     T* sb = reinterpret_cast<T*>(smem_raw);
     double2* acc = reinterpret_cast<double2*>(
-        (reinterpret_cast<uintptr_t>(sb + slot * nw) + 15) & ~uintptr_t(15));
-    int* s_tp = reinterpret_cast<int*>(acc + ty.K0);
-    int* s_ok = s_tp + nw;
-    T* s_tab = reinterpret_cast<T*>(s_ok + nw + 4);
-    s_tab = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_tab) + 15) & ~uintptr_t(15));
+        (reinterpret_cast<uintptr_t>(sb + slot * NW) + 15) & ~uintptr_t(15));
+    T* s_tab = reinterpret_cast<T*>(acc + ty.K0);
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) acc[h] = make_double2(0.0, 0.0);
-    __syncthreads();
-    const long long b = nb_off[i], e = nb_off[i + 1];
-    for (long long base = b; base < e; base += nw) {
-        const long long k = base + warp;
-        BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
-        if (k < e) {
-            const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
-            double dis = 0.0;
-            if (lane == 0) dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-            dis = __shfl_sync(0xffffffffu, dis, 0);
-            const bool ok = dis < M.cutoff;
-            const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
-            if (lane == 0) {
-                s_tp[warp] = tp;
-                s_ok[warp] = ok;
+    const long long p0 = nb_off[i];
+    const int np = (int)(nb_off[i + 1] - p0);
+    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
+    for (int tp = 0; tp < M.n_tp; ++tp) {
+        const int q0 = ty.tp_head_off[tp], nh = ty.tp_head_off[tp + 1] - q0;
+        if (nh == 0) continue;  // the type pair is not one of this centre type's
+        for (int r0 = 0; r0 < np; r0 += 256) {
+            // compact the pairs of tp among r0 .. r0 + 255, in list order
+            const int r = r0 + threadIdx.x;
+            const bool f = r < np && M.type_pairs[t1 * M.n_type + B.types[nb_j[p0 + r]]] == tp;
+            const unsigned m = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) s_wcnt[warp] = __popc(m);
+            __syncthreads();
+            int before = 0, c = 0;
+            for (int w = 0; w < NW; ++w) {
+                before += w < warp ? s_wcnt[w] : 0;
+                c += s_wcnt[w];
             }
-            if (ok) {
-                warp_radial<T, false>(M, tp, dis, bv, lane);
-                if (M.gtinv) {
-                    warp_ylm<T, false>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
-                } else if (lane == 0) {
-                    bv.Y[0] = {(T)1, (T)0};
+            if (f) s_list[before + __popc(m & ((1u << lane) - 1u))] = r;
+            __syncthreads();
+            for (int k0 = 0; k0 < c; k0 += NW) {
+                const int n = min(NW, c - k0);
+                if (warp < n) {
+                    const long long k = p0 + s_list[k0 + warp];
+                    const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
+                    double dis = 0.0;
+                    if (lane == 0)
+                        dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+                    dis = __shfl_sync(0xffffffffu, dis, 0);
+                    const bool ok = dis < M.cutoff;
+                    if (lane == 0) s_ok[warp] = ok;
+                    if (ok) {
+                        warp_radial<T, false>(M, tp, dis, bv, lane);
+                        if (M.gtinv) {
+                            warp_ylm<T, false>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
+                        } else if (lane == 0) {
+                            bv.Y[0] = {(T)1, (T)0};
+                        }
+                    }
                 }
+                __syncthreads();
+                for (int q = threadIdx.x; q < nh; q += blockDim.x) {
+                    const int h = ty.tp_heads[q0 + q];
+                    const int nid = ty.head_nid[h], key = ty.head_key[h];
+                    T px = 0, py = 0;
+                    for (int w = 0; w < n; ++w) {
+                        if (!s_ok[w]) continue;
+                        BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
+                        const T fw = v.fn[nid];
+                        if (!(fw >= (T)1e-20)) continue;
+                        const cplx<T> y = v.Y[key];
+                        px += fw * y.re;
+                        py += fw * y.im;
+                    }
+                    double2 a = acc[h];
+                    a.x += (double)px;
+                    a.y += (double)py;
+                    acc[h] = a;
+                }
+                __syncthreads();
             }
-        } else if (lane == 0) {
-            s_ok[warp] = 0;
         }
-        __syncthreads();
-        for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) {
-            const int htp = ty.head_tp[h], nid = ty.head_nid[h], key = ty.head_key[h];
-            // partial sum over this batch of pairs in T, added to the FP64 total
-            T px = 0, py = 0;
-            for (int w = 0; w < nw; ++w) {
-                if (!s_ok[w] || s_tp[w] != htp) continue;
-                BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
-                const T f = v.fn[nid];
-                if (!(f >= (T)1e-20)) continue;
-                const cplx<T> y = v.Y[key];
-                px += f * y.re;
-                py += f * y.im;
-            }
-            double2 a = acc[h];
-            a.x += (double)px;
-            a.y += (double)py;
-            acc[h] = a;
-        }
-        __syncthreads();
     }
     double2* out = A + a_off[i];
     for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) out[h] = acc[h];
@@ -954,10 +971,10 @@ void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* 
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
                  const long long* a_off, double2* A, int max_k0, cudaStream_t st) {
-    const int threads = 128, nw = threads / 32;
+    const int threads = 256, nw = threads / 32;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) + (2 * nw + 4) * sizeof(int) +
-                        16 + ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
+    const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) +
+                        ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
     PG_CUDA(cudaFuncSetAttribute(pg_anlm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pg_anlm<T><<<B.n_atoms, threads, smem, st>>>(M, B, nb_off, nb_j, nb_d, a_off, A);
 }
