@@ -151,6 +151,33 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.tpl_tp = (const int*)up(ft.tpl_tp);
         d.tp_head_off = (const int*)up(ft.tp_head_off);
         d.tp_heads = (const int*)up(ft.tp_heads);
+        // adjoint terms in slot order, for pg_features_adjoint
+        if (ft.K >= 65536) throw std::runtime_error("too many a_nlm entries for the packed term ids");
+        std::vector<int> slot_toff(ft.lay_size + 1, 0);
+        std::vector<int4> tcode;
+        std::vector<double> tcoef;
+        for (int sl = 0; sl < ft.lay_size; ++sl) {
+            const int e = ft.lay_ent[sl];
+            if (e >= 0) {
+                const double cc = (ft.head_m[ft.ent_head[e]] & 1) ? -1.0 : 1.0;
+                for (int q = ft.term_off[e]; q < ft.term_off[e + 1]; ++q) {
+                    const FlatTerm& t = ft.g_terms[q];
+                    int id[6] = {0, 0, 0, 0, 0, 0};
+                    for (int r = 0; r < t.n; ++r) id[r] = t.ids[r];
+                    tcode.push_back(make_int4(id[0] | (id[1] << 16), id[2] | (id[3] << 16), id[4] | (id[5] << 16),
+                                              t.n | (t.conj << 8)));
+                    tcoef.push_back(t.conj ? cc * t.coeff : t.coeff);
+                }
+            }
+            slot_toff[sl + 1] = (int)tcode.size();
+        }
+        d.slot_toff = (const int*)up(slot_toff);
+        d.tcode = (const int4*)up(tcode);
+        if (fp64) {
+            d.tcoef = up(tcoef);
+        } else {
+            d.tcoef = up(std::vector<float>(tcoef.begin(), tcoef.end()));
+        }
     }
 }
 

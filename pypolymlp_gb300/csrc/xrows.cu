@@ -366,27 +366,47 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
     }
     cplx<T>* Gi = G + g_off[i];
     // entries in the X-row layout (rank-major groups of 32 features per type
-    // pair); padding slots hold zero
-    for (int slot = threadIdx.x; slot < ty.lay_size; slot += blockDim.x) {
-        const int e = ty.lay_ent[slot];
+    // pair; padding slots hold zero).  Warp per rank of 32 slots: the rank's
+    // terms (slot order) are evaluated 32 at a time by all lanes, whatever
+    // slot they belong to, into a window of s_v; then each lane adds its own
+    // slot's terms from the window, in order.
+    constexpr int NW = 8, kWin = 128;
+    __shared__ cplx<T> s_v[NW][kWin];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T* coef = reinterpret_cast<const T*>(ty.tcoef);
+    for (int rk = warp; rk < ty.lay_size / 32; rk += NW) {
+        const int slot = 32 * rk + lane;
+        const int tb = ty.slot_toff[32 * rk], te = ty.slot_toff[32 * rk + 32];
+        const int ms = ty.slot_toff[slot], me = ty.slot_toff[slot + 1];
         cplx<T> g = {(T)0, (T)0};
-        if (e < 0) {
-            Gi[slot] = g;
-            continue;
-        }
-        const int h = ty.ent_head[e];
-        const T cc = (ty.head_m[h] & 1) ? (T)-1 : (T)1;
-        for (int q = ty.term_off[e]; q < ty.term_off[e + 1]; ++q) {
-            const FlatTerm& t = ty.g_terms[q];
-            const cplx<T> p = term_product<T>(t, a);
-            const T c = (T)t.coeff;
-            if (t.conj) {
-                g.re += cc * c * p.re;
-                g.im -= cc * c * p.im;
-            } else {
-                g.re += c * p.re;
-                g.im += c * p.im;
+        for (int w0 = tb; w0 < te; w0 += kWin) {
+#pragma unroll
+            for (int u = 0; u < kWin / 32; ++u) {
+                const int t = w0 + 32 * u + lane;
+                if (t < te) {
+                    const int4 c4 = ty.tcode[t];
+                    const T cf = coef[t];
+                    const int n = c4.w & 0xff;
+                    const int id[6] = {c4.x & 0xffff, (c4.x >> 16) & 0xffff, c4.y & 0xffff,
+                                       (c4.y >> 16) & 0xffff, c4.z & 0xffff, (c4.z >> 16) & 0xffff};
+                    cplx<T> p = {(T)1, (T)0};
+                    if (n > 0) p = a[id[0]];
+#pragma unroll
+                    for (int q = 1; q < 6; ++q)
+                        if (q < n) p = cmul(p, a[id[q]]);
+                    cplx<T> v = {cf * p.re, cf * p.im};
+                    if (c4.w >> 8) v.im = -v.im;
+                    s_v[warp][32 * u + lane] = v;
+                }
             }
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kWin);
+            for (int t = lo; t < hi; ++t) {
+                const cplx<T> v = s_v[warp][t - w0];
+                g.re += v.re;
+                g.im += v.im;
+            }
+            __syncwarp();
         }
         Gi[slot] = g;
     }
