@@ -355,24 +355,39 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
         }
     }
     __syncthreads();
-    T* Di = D + d_off[i];
-    for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
-        T v = 0;
-        for (int q = ty.val_off[k]; q < ty.val_off[k + 1]; ++q) {
-            const FlatTerm& t = ty.val_terms[q];
-            v += (T)t.coeff * term_product_real<T>(t, a);
-        }
-        Di[k] = v;
-    }
-    cplx<T>* Gi = G + g_off[i];
-    // entries in the X-row layout (rank-major groups of 32 features per type
-    // pair; padding slots hold zero).  Warp per rank of 32 slots: the rank's
-    // terms (slot order) are evaluated 32 at a time by all lanes, whatever
-    // slot they belong to, into a window of s_v; then each lane adds its own
-    // slot's terms from the window, in order.
+    // Both loops below give a warp 32 outputs whose terms are contiguous: the
+    // terms are evaluated 32 at a time by all lanes, whatever output they
+    // belong to, into a window of s_v; then each lane adds its own output's
+    // terms from the window, in order.
     constexpr int NW = 8, kWin = 128;
     __shared__ cplx<T> s_v[NW][kWin];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // feature values, 32 features per warp
+    T* Di = D + d_off[i];
+    for (int k0 = 32 * warp; k0 < ty.n_lin; k0 += 32 * NW) {
+        const int k = k0 + lane;
+        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, ty.n_lin)];
+        const int ms = k < ty.n_lin ? ty.val_off[k] : te, me = k < ty.n_lin ? ty.val_off[k + 1] : te;
+        T v = 0;
+        for (int w0 = tb; w0 < te; w0 += kWin) {
+#pragma unroll
+            for (int u = 0; u < kWin / 32; ++u) {
+                const int t = w0 + 32 * u + lane;
+                if (t < te) {
+                    const FlatTerm& f = ty.val_terms[t];
+                    s_v[warp][32 * u + lane].re = (T)f.coeff * term_product_real<T>(f, a);
+                }
+            }
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kWin);
+            for (int t = lo; t < hi; ++t) v += s_v[warp][t - w0].re;
+            __syncwarp();
+        }
+        if (k < ty.n_lin) Di[k] = v;
+    }
+    // adjoint entries in the X-row layout (rank-major groups of 32 features
+    // per type pair; padding slots hold zero), warp per rank of 32 slots
+    cplx<T>* Gi = G + g_off[i];
     const T* coef = reinterpret_cast<const T*>(ty.tcoef);
     for (int rk = warp; rk < ty.lay_size / 32; rk += NW) {
         const int slot = 32 * rk + lane;
