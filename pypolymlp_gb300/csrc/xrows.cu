@@ -771,23 +771,49 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     const long long r0 = f_row[s] + 3LL * (gj - sa0);
     const long long q0 = nb_off[gj], qe = nb_off[gj + 1];
     const int NL = M.max_lin;
+    // the groups of j's list (runs of one neighbour i != j) of one centre type,
+    // listed kSeg pairs of the list at a time: a group's vector sits at its
+    // first pair, so a group that crosses a segment is taken in the first one
+    constexpr int kSeg = 2048;
+    __shared__ int s_list[kSeg];
+    __shared__ int s_wcnt[kRowsThreads / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int tc = 0; tc < M.n_type; ++tc) {
         const DevType& ty = M.types[tc];
         const int nl = ty.n_lin;
         const int tp = M.type_pairs[tc * M.n_type + tj];
         const int* perm = ty.tp_perm + (size_t)tp * nl;
         const int* ipos = ty.tp_ipos + (size_t)tp * nl;
-        // linear columns: sum of the group vectors of this centre type
-        for (int slab = 0; slab < nl; slab += S * blockDim.x) {
-            T acc[S][3];
+        for (long long sb = q0; sb < qe; sb += kSeg) {
+            const long long se = min(sb + kSeg, qe);
+            int n = 0;
+            for (long long w0 = sb; w0 < se; w0 += blockDim.x) {
+                const long long q = w0 + threadIdx.x;
+                bool head = false;
+                if (q < se) {
+                    const int gi = nb_j[q];
+                    head = gi != gj && (q == q0 || nb_j[q - 1] != gi) && B.types[gi] == tc;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, head);
+                if (lane == 0) s_wcnt[warp] = __popc(m);
+                __syncthreads();
+                int before = 0, total = 0;
+                for (int w = 0; w < kRowsThreads / 32; ++w) {
+                    before += w < warp ? s_wcnt[w] : 0;
+                    total += s_wcnt[w];
+                }
+                if (head) s_list[n + before + __popc(m & ((1u << lane) - 1u))] = (int)(q - sb);
+                n += total;
+                __syncthreads();
+            }
+            // linear columns: sum of the group vectors
+            for (int slab = 0; slab < nl; slab += S * blockDim.x) {
+                T acc[S][3];
 #pragma unroll
-            for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
-            for (long long q = q0; q < qe;) {
-                const int gi = nb_j[q];
-                long long qb = q + 1;
-                while (qb < qe && nb_j[qb] == gi) ++qb;
-                if (gi != gj && B.types[gi] == tc) {
-                    const T* src = Dp + (size_t)q * 3 * NL;
+                for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
+#pragma unroll 2
+                for (int k = 0; k < n; ++k) {
+                    const T* src = Dp + (size_t)(sb + s_list[k]) * 3 * NL;
 #pragma unroll
                     for (int m = 0; m < S; ++m) {
                         const int x = slab + threadIdx.x + m * blockDim.x;
@@ -798,34 +824,29 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                         }
                     }
                 }
-                q = qb;
-            }
 #pragma unroll
-            for (int m = 0; m < S; ++m) {
-                const int x = slab + threadIdx.x + m * blockDim.x;
-                if (x >= nl) continue;
-                const int col = ty.lin_col[perm[x]];
-                if (col < 0) continue;
-                T* o = X + (size_t)col * ld + r0;
-                o[0] -= acc[m][0];
-                o[1] -= acc[m][1];
-                o[2] -= acc[m][2];
+                for (int m = 0; m < S; ++m) {
+                    const int x = slab + threadIdx.x + m * blockDim.x;
+                    if (x >= nl) continue;
+                    const int col = ty.lin_col[perm[x]];
+                    if (col < 0) continue;
+                    T* o = X + (size_t)col * ld + r0;
+                    o[0] -= acc[m][0];
+                    o[1] -= acc[m][1];
+                    o[2] -= acc[m][2];
+                }
             }
-        }
-        // product columns
-        for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
-            const int col = ty.prod_col[p];
-            int k0, k1, k2, w;
-            unpack_col(ty.col_pack[col], k0, k1, k2, w);
-            const int x0 = ipos[k0], x1 = ipos[k1], x2 = w > 2 ? ipos[k2] : 0;
-            T v0 = 0, v1 = 0, v2 = 0;
-            for (long long q = q0; q < qe;) {
-                const int gi = nb_j[q];
-                long long qb = q + 1;
-                while (qb < qe && nb_j[qb] == gi) ++qb;
-                if (gi != gj && B.types[gi] == tc) {
+            // product columns
+            for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
+                const int col = ty.prod_col[p];
+                int k0, k1, k2, w;
+                unpack_col(ty.col_pack[col], k0, k1, k2, w);
+                const int x0 = ipos[k0], x1 = ipos[k1], x2 = w > 2 ? ipos[k2] : 0;
+                T v0 = 0, v1 = 0, v2 = 0;
+                for (int k = 0; k < n; ++k) {
+                    const long long q = sb + s_list[k];
                     const T* src = Dp + (size_t)q * 3 * NL;
-                    const T* Di = D + d_off[gi];
+                    const T* Di = D + d_off[nb_j[q]];
                     T w0, w1, w2 = 0;
                     if (w == 2) {
                         w0 = Di[k1];
@@ -844,14 +865,15 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                         v2 += w2 * src[2 * NL + x2];
                     }
                 }
-                q = qb;
+                T* o = X + (size_t)col * ld + r0;
+                o[0] -= v0;
+                o[1] -= v1;
+                o[2] -= v2;
             }
-            T* o = X + (size_t)col * ld + r0;
-            o[0] -= v0;
-            o[1] -= v1;
-            o[2] -= v2;
+            // before the list is rebuilt; a column shared by several types is
+            // also updated type by type
+            __syncthreads();
         }
-        __syncthreads();  // a column shared by several types is updated type by type
     }
     // self rows: the target as a centre (type tj), its DS self vectors (per type pair, by position)
     const DevType& ty = M.types[tj];
