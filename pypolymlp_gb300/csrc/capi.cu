@@ -147,6 +147,7 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.lay_grp_cnt = (const int*)up(ft.lay_grp_cnt);
         d.tp_perm = (const int*)up(ft.tp_perm);
         d.tp_ipos = (const int*)up(ft.tp_ipos);
+        d.tp_nnz = (const int*)up(ft.tp_nnz);
         d.tpl = (const int*)up(ft.tpl);
         d.tpl_tp = (const int*)up(ft.tpl_tp);
         d.tp_head_off = (const int*)up(ft.tp_head_off);

@@ -68,6 +68,7 @@ struct DevType {
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
     int n_groups, lay_size, n_tpl;
     const int *lay_ent, *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
+    const int* tp_nnz;  // per type pair: feature positions with entries (the first ones)
     // adjoint terms in X-row slot order: slot s owns terms slot_toff[s] ..
     // slot_toff[s + 1]; per term the full a ids (16 bits each, two per word in
     // x, y, z), n | conj << 8 in w, and its coefficient (T of the model; the

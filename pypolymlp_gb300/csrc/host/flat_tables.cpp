@@ -282,6 +282,7 @@ FlatModel flatten_model(const ModelTables& mt) {
             ft.tp_ipos.assign((size_t)ntp * nl, 0);
             ft.lay_grp_base.assign((size_t)ntp * ft.n_groups, 0);
             ft.lay_grp_cnt.assign((size_t)ntp * ft.n_groups, 0);
+            ft.tp_nnz.assign(ntp, 0);
             ft.tpl.assign(ntp, -1);
             ft.tp_head_row.assign(ft.tp_heads.size(), 0);
             for (int tp = 0; tp < ntp; ++tp) {
@@ -298,6 +299,7 @@ FlatModel flatten_model(const ModelTables& mt) {
                 for (int x = 0; x < nl; ++x) {
                     ft.tp_perm[(size_t)tp * nl + x] = order[x];
                     ft.tp_ipos[(size_t)tp * nl + order[x]] = x;
+                    if (cnt(order[x]) > 0) ft.tp_nnz[tp] = x + 1;
                 }
                 const size_t tp_base = ft.lay_ent.size();
                 std::vector<std::vector<int>> ranks;

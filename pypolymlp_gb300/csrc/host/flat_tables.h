@@ -66,8 +66,10 @@ struct FlatType {
     // per-type-pair gradient tile: tp_head_row[q] for the tp_heads entry q, rows
     // coloured so that the heads one rank reads fall in distinct bank sets; a
     // zero entry repeats the row of its rank's lane 0.
+    // tp_nnz[tp]: positions with entries of tp (they come first); the
+    // derivatives of the other features by a pair of tp vanish.
     int n_groups = 0, lay_size = 0;
-    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_head_row;
+    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_head_row, tp_nnz;
     // type pairs with heads for this centre type: local index or -1, and back
     std::vector<int> tpl, tpl_tp;
 };

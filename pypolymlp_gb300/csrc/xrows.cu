@@ -650,6 +650,9 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                 for (int grp = warp; grp < ng; grp += NW) {
                     const int x = 32 * grp + lane;
                     const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
+                    // positions without entries of tp: zero derivatives, nothing
+                    // stored (stage B reads positions below tp_nnz only)
+                    if (cnt == 0) continue;
                     T acc[NW][3];
 #pragma unroll
                     for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
@@ -784,6 +787,8 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
         const int tp = M.type_pairs[tc * M.n_type + tj];
         const int* perm = ty.tp_perm + (size_t)tp * nl;
         const int* ipos = ty.tp_ipos + (size_t)tp * nl;
+        const int nnz = ty.tp_nnz[tp];  // the group vectors hold positions below nnz; the rest vanish
+        if (nnz == 0) continue;
         for (long long sb = q0; sb < qe; sb += kSeg) {
             const long long se = min(sb + kSeg, qe);
             int n = 0;
@@ -807,7 +812,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 __syncthreads();
             }
             // linear columns: sum of the group vectors
-            for (int slab = 0; slab < nl; slab += S * blockDim.x) {
+            for (int slab = 0; slab < nnz; slab += S * blockDim.x) {
                 T acc[S][3];
 #pragma unroll
                 for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
@@ -817,7 +822,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
 #pragma unroll
                     for (int m = 0; m < S; ++m) {
                         const int x = slab + threadIdx.x + m * blockDim.x;
-                        if (x < nl) {
+                        if (x < nnz) {
                             acc[m][0] += src[x];
                             acc[m][1] += src[NL + x];
                             acc[m][2] += src[2 * NL + x];
@@ -827,7 +832,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
                     const int x = slab + threadIdx.x + m * blockDim.x;
-                    if (x >= nl) continue;
+                    if (x >= nnz) continue;
                     const int col = ty.lin_col[perm[x]];
                     if (col < 0) continue;
                     T* o = X + (size_t)col * ld + r0;
@@ -842,6 +847,9 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 int k0, k1, k2, w;
                 unpack_col(ty.col_pack[col], k0, k1, k2, w);
                 const int x0 = ipos[k0], x1 = ipos[k1], x2 = w > 2 ? ipos[k2] : 0;
+                // components at positions from nnz on vanish
+                const bool b0 = x0 < nnz, b1 = x1 < nnz, b2 = w > 2 && x2 < nnz;
+                if (!(b0 || b1 || b2)) continue;
                 T v0 = 0, v1 = 0, v2 = 0;
                 for (int k = 0; k < n; ++k) {
                     const long long q = sb + s_list[k];
@@ -856,10 +864,13 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                         w1 = Di[k0] * Di[k2];
                         w2 = Di[k0] * Di[k1];
                     }
-                    v0 += w0 * src[x0] + w1 * src[x1];
-                    v1 += w0 * src[NL + x0] + w1 * src[NL + x1];
-                    v2 += w0 * src[2 * NL + x0] + w1 * src[2 * NL + x1];
-                    if (w > 2) {
+                    const T s0 = b0 ? src[x0] : (T)0, s1 = b1 ? src[x1] : (T)0;
+                    const T t0 = b0 ? src[NL + x0] : (T)0, t1 = b1 ? src[NL + x1] : (T)0;
+                    const T u0 = b0 ? src[2 * NL + x0] : (T)0, u1 = b1 ? src[2 * NL + x1] : (T)0;
+                    v0 += w0 * s0 + w1 * s1;
+                    v1 += w0 * t0 + w1 * t1;
+                    v2 += w0 * u0 + w1 * u1;
+                    if (b2) {
                         v0 += w2 * src[x2];
                         v1 += w2 * src[NL + x2];
                         v2 += w2 * src[2 * NL + x2];
