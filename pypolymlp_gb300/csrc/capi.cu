@@ -79,6 +79,11 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
     dm.tp_nfn = (const int*)up(fm.tp_nfn);
     dm.tp_beta = (const double*)up(fm.tp_beta);
     dm.tp_mu = (const double*)up(fm.tp_mu);
+    dm.tp_beta_f = (const float*)up(std::vector<float>(fm.tp_beta.begin(), fm.tp_beta.end()));
+    dm.tp_mu_f = (const float*)up(std::vector<float>(fm.tp_mu.begin(), fm.tp_mu.end()));
+    dm.cutoff_f = (float)fm.cutoff;
+    // FP32 squared distances carry a relative error below 1e-6
+    dm.rc2_safe_f = (float)(fm.cutoff * fm.cutoff * (1.0 - 1e-5));
     dm.ylm_tab = (const double*)up(fm.ylm_tab);
     for (int t = 0; t < fm.n_type; ++t) {
         const FlatType& ft = fm.types[t];
@@ -345,9 +350,11 @@ void DeviceBatch::build_neighbors(double cutoff, cudaStream_t stream) {
     d_nb_j.reserve(sizeof(int) * std::max<long long>(1, n_pairs));
     d_nb_d.reserve(sizeof(double) * 3 * std::max<long long>(1, n_pairs));
     if (n_cl > 0) d_keys.reserve(sizeof(long long) * std::max<long long>(1, n_pairs));
+    d_nb_df.reserve(sizeof(float4) * std::max<long long>(1, n_pairs));
     ProfScope ps("pg_nb_fill", stream);
     launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), d_keys.as<long long>(),
                    n_cl > 0, stream);
+    launch_nb_f32(n_pairs, d_nb_d.as<double>(), d_nb_df.as<float4>(), stream);
 }
 
 void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
@@ -380,6 +387,7 @@ DevBatch DeviceBatch::view(double cutoff) const {
     B.cl_atoms = d_cl_atoms.as<int>();
     B.frac = d_frac.as<double>();
     B.tn = d_tn.as<int4>();
+    B.nb_df = d_nb_df.as<float4>();
     B.cutoff = cutoff;
     // FP32 differences of coordinates up to L carry an error below 4 L 2^-24 per
     // component, so |r2_f32 - r2| < 2 rc (12 L 2^-24) + O(L^2 2^-48) + the FP32
@@ -439,8 +447,9 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
     }
     size_t max_lin = 1;
     for (const auto& ft : flat.types) max_lin = std::max<size_t>(max_lin, ft.n_lin);
-    // per pair: index, displacement, mirror and the pair derivatives (3 per feature); X rows
-    return mx + (size_t)(mean_pairs * (28.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;
+    // per pair: index, FP64 and FP32 displacements, mirror, group slot, order and
+    // the pair derivatives (3 per feature); X rows
+    return mx + (size_t)(mean_pairs * (64.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;
 }
 
 // Per-batch plan: per-atom storage offsets and pg_rows work items.

@@ -86,6 +86,10 @@ struct DevModel {
     const int* type_pairs;
     const int* tp_nfn;
     const double *tp_beta, *tp_mu;
+    // FP32 copies for the FP32 kernels; rc2_safe_f: a squared distance
+    // whose FP32 value lies below it is surely inside the cutoff in FP64
+    float cutoff_f, rc2_safe_f;
+    const float *tp_beta_f, *tp_mu_f;
     // Legendre/Y_lm constants (ylm_table_size doubles), see ylm_tables()
     const double* ylm_tab;
     DevType types[kMaxTypes];
@@ -167,13 +171,57 @@ __device__ inline BasisView<T> basis_view(T* base, int n_fn_max, int n_ylm, int 
 
 __device__ __forceinline__ int lmi(int l, int m) { return l * (l + 1) / 2 + m; }
 
+// Model constants in the precision T of a kernel (no FP64 work in FP32 kernels).
+template <typename T>
+__device__ __forceinline__ T model_cutoff(const DevModel& M);
+template <>
+__device__ __forceinline__ double model_cutoff<double>(const DevModel& M) { return M.cutoff; }
+template <>
+__device__ __forceinline__ float model_cutoff<float>(const DevModel& M) { return M.cutoff_f; }
+template <typename T>
+__device__ __forceinline__ T model_beta(const DevModel& M, int q);
+template <>
+__device__ __forceinline__ double model_beta<double>(const DevModel& M, int q) { return M.tp_beta[q]; }
+template <>
+__device__ __forceinline__ float model_beta<float>(const DevModel& M, int q) { return M.tp_beta_f[q]; }
+template <typename T>
+__device__ __forceinline__ T model_mu(const DevModel& M, int q);
+template <>
+__device__ __forceinline__ double model_mu<double>(const DevModel& M, int q) { return M.tp_mu[q]; }
+template <>
+__device__ __forceinline__ float model_mu<float>(const DevModel& M, int q) { return M.tp_mu_f[q]; }
+
+// Sum in T with a long result: FP64 for T = double; for T = float a
+// float-float pair (Knuth's TwoSum keeps the rounding error of every addition
+// in lo), about 48 significant bits without FP64 instructions.
+template <typename T>
+struct LongSum {
+    double v = 0.0;
+    __device__ __forceinline__ void add(double x) { v += x; }
+    __device__ __forceinline__ double value() const { return v; }
+    __device__ __forceinline__ double value64() const { return v; }
+};
+template <>
+struct LongSum<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ float value() const { return __fadd_rn(hi, lo); }
+    __device__ __forceinline__ double value64() const { return (double)hi + (double)lo; }
+};
+
 // Radial functions of one type pair at distance dis
 // (polymlp_basis_function.h:16-43, polymlp_functions_interface.cpp:41-62).
 template <typename T, bool DERIV>
-__device__ __noinline__ void warp_radial(const DevModel& M, int tp, double dis, BasisView<T> B, int lane) {
+__device__ __noinline__ void warp_radial(const DevModel& M, int tp, T dis, BasisView<T> B, int lane) {
     const int nfn = M.tp_nfn[tp];
-    const T r = (T)dis;
-    const T rc = (T)M.cutoff;
+    const T r = dis;
+    const T rc = model_cutoff<T>(M);
     const T v1 = (T)kPiD / rc;
     const T v2 = v1 * r;
     T fc, fcd = 0;
@@ -184,8 +232,8 @@ __device__ __noinline__ void warp_radial(const DevModel& M, int tp, double dis, 
         fc = (T)0.5 * (cos((T)kPiD * r / rc) + (T)1.0);
     }
     for (int q = lane; q < nfn; q += 32) {
-        const T beta = (T)M.tp_beta[tp * M.n_fn_max + q];
-        const T mu = (T)M.tp_mu[tp * M.n_fn_max + q];
+        const T beta = model_beta<T>(M, tp * M.n_fn_max + q);
+        const T mu = model_mu<T>(M, tp * M.n_fn_max + q);
         const T x = r - mu;
         const T bf = exp(-beta * x * x);
         B.fn[q] = bf * fc;
@@ -199,9 +247,8 @@ __device__ __noinline__ void warp_radial(const DevModel& M, int tp, double dis, 
 // arXiv:1410.1748), with the (l, m) constants read from a table.  Lane m
 // computes the Legendre column m; lanes then fill the (l, m) table.
 template <typename T, bool DERIV>
-__device__ __noinline__ void warp_ylm(int maxl, int n_ylm, const YlmTab<T>& tab, double xd, double yd, double zd,
-                                double rd, BasisView<T> B, int lane) {
-    const T x = (T)xd, y = (T)yd, z = (T)zd, r = (T)rd;
+__device__ __noinline__ void warp_ylm(int maxl, int n_ylm, const YlmTab<T>& tab, T x, T y, T z, T r, BasisView<T> B,
+                                int lane) {
     const T ct = z / r;
     const T rho = hypot(x, y);
     const T cp = rho > (T)0 ? x / rho : (T)1;

@@ -153,9 +153,9 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
         double gx = 0.0, gy = 0.0, gz = 0.0;
         if (dis < M.cutoff) {
             const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
-            warp_radial<T, true>(M, tp, dis, bv, lane);
+            warp_radial<T, true>(M, tp, (T)dis, bv, lane);
             if (M.gtinv) {
-                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
+                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, (T)dx, (T)dy, (T)dz, (T)dis, bv, lane);
             } else if (lane == 0) {
                 bv.Y[0] = {(T)1, (T)0};
                 bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};

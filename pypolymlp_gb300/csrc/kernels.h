@@ -31,6 +31,9 @@ struct DevBatch {
     const int* cl_atoms;       // batch atom indices, by bin then index
     const double* frac;        // per atom: fractional coordinates on the reduced axis (cell-list structures)
     const int4* tn;            // per translation: its integer coefficients
+    // per neighbour-list entry: FP32 displacement and squared distance (after
+    // the lists are built), for the FP32 kernels
+    const float4* nb_df;
 };
 
 constexpr int kCellListMinAtoms = 1024;  // structures this large use a cell list
@@ -49,6 +52,7 @@ template <typename T>
 void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
+void launch_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df, cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
 size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64);
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,

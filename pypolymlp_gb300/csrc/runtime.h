@@ -109,7 +109,7 @@ struct DeviceBatch {
     DevBuf d_st_atom_off, d_st_trans_off, d_trans, d_pos, d_types, d_atom_st, d_posf, d_transf;
     int n_cl = 0;             // structures searched with a cell list
     DevBuf d_st_cl, d_cl_grid, d_cl_geom, d_cl_bin_start, d_cl_atoms, d_frac, d_tn, d_keys, d_maxcnt;
-    DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d, d_total;
+    DevBuf d_counts, d_nb_off, d_nb_j, d_nb_d, d_nb_df, d_total;
     std::vector<long long> nb_off;  // host copy, only after host_offsets()
     // Host: translations and wrapped positions (NeighborCell), uploaded to the device.
     void upload_structures(const pg_structures* st, int s_begin, int s_end, double cutoff);

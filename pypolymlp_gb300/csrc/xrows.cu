@@ -244,6 +244,43 @@ __global__ void pg_nb_order(DevBatch B, const long long* offsets, const long lon
     }
 }
 
+// FP32 copy of the neighbour-list displacements: (dx, dy, dz, dx^2 + dy^2 + dz^2).
+__global__ void pg_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pairs) return;
+    const float x = (float)nb_d[3 * k], y = (float)nb_d[3 * k + 1], z = (float)nb_d[3 * k + 2];
+    nb_df[k] = make_float4(x, y, z, x * x + y * y + z * z);
+}
+
+// Displacement and distance of neighbour-list entry k in T, and whether the
+// pair counts: sqrt(dx^2 + dy^2 + dz^2) < cutoff in FP64 (local.cpp's test).
+// The FP32 form decides from the FP32 squared distance when it is clearly
+// inside and falls back to the FP64 test near the cutoff.  Warp-uniform.
+template <typename T>
+__device__ __forceinline__ bool pair_geometry(const DevModel& M, const DevBatch& B, const double* nb_d, long long k,
+                                              T& dx, T& dy, T& dz, T& dis);
+template <>
+__device__ __forceinline__ bool pair_geometry<double>(const DevModel& M, const DevBatch& B, const double* nb_d,
+                                                      long long k, double& dx, double& dy, double& dz, double& dis) {
+    dx = nb_d[3 * k];
+    dy = nb_d[3 * k + 1];
+    dz = nb_d[3 * k + 2];
+    dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    return dis < M.cutoff;
+}
+template <>
+__device__ __forceinline__ bool pair_geometry<float>(const DevModel& M, const DevBatch& B, const double* nb_d,
+                                                     long long k, float& dx, float& dy, float& dz, float& dis) {
+    const float4 g = B.nb_df[k];
+    dx = g.x;
+    dy = g.y;
+    dz = g.z;
+    dis = sqrtf(g.w);
+    if (g.w < M.rc2_safe_f) return true;
+    const double ex = nb_d[3 * k], ey = nb_d[3 * k + 1], ez = nb_d[3 * k + 2];
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez))) < M.cutoff;
+}
+
 // ---------------------------------------------------------------- K2 a_nlm
 // Block per centre atom, pairs taken one type pair at a time: the pairs of
 // that type pair are compacted into a list (256 at a time), warps compute the
@@ -262,12 +299,13 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
     T* sb = reinterpret_cast<T*>(smem_raw);
-    double2* acc = reinterpret_cast<double2*>(
+    // per head: running sums of the real and imaginary parts (16 bytes)
+    LongSum<T>* acc = reinterpret_cast<LongSum<T>*>(
         (reinterpret_cast<uintptr_t>(sb + slot * NW) + 15) & ~uintptr_t(15));
-    T* s_tab = reinterpret_cast<T*>(acc + ty.K0);
+    T* s_tab = reinterpret_cast<T*>(acc + 2 * (size_t)ty.K0);
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
-    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) acc[h] = make_double2(0.0, 0.0);
+    for (int h = threadIdx.x; h < 2 * ty.K0; h += blockDim.x) acc[h] = LongSum<T>();
     const long long p0 = nb_off[i];
     const int np = (int)(nb_off[i + 1] - p0);
     BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
@@ -292,12 +330,8 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
                 const int n = min(NW, c - k0);
                 if (warp < n) {
                     const long long k = p0 + s_list[k0 + warp];
-                    const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
-                    double dis = 0.0;
-                    if (lane == 0)
-                        dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-                    dis = __shfl_sync(0xffffffffu, dis, 0);
-                    const bool ok = dis < M.cutoff;
+                    T dx, dy, dz, dis;
+                    const bool ok = pair_geometry<T>(M, B, nb_d, k, dx, dy, dz, dis);
                     if (lane == 0) s_ok[warp] = ok;
                     if (ok) {
                         warp_radial<T, false>(M, tp, dis, bv, lane);
@@ -322,17 +356,16 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
                         px += fw * y.re;
                         py += fw * y.im;
                     }
-                    double2 a = acc[h];
-                    a.x += (double)px;
-                    a.y += (double)py;
-                    acc[h] = a;
+                    acc[2 * h].add(px);
+                    acc[2 * h + 1].add(py);
                 }
                 __syncthreads();
             }
         }
     }
     double2* out = A + a_off[i];
-    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) out[h] = acc[h];
+    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x)
+        out[h] = make_double2(acc[2 * h].value64(), acc[2 * h + 1].value64());
 }
 
 // ----------------------------------------------- K4 features and adjoint G
@@ -579,17 +612,13 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
             // ---- bases and head-space gradients of the chunk
             if (warp < n) {
                 const long long q = p0 + ord[r0 + warp];
-                const double dx = nb_d[3 * q], dy = nb_d[3 * q + 1], dz = nb_d[3 * q + 2];
-                double dis = 0.0;
-                if (lane == 0)
-                    dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-                dis = __shfl_sync(0xffffffffu, dis, 0);
-                const bool ok = dis < M.cutoff;
+                T dx, dy, dz, dis;
+                const bool ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
                 const int j = nb_j[q];
                 if (lane == 0) {
-                    sd[3 * warp] = (T)dx;
-                    sd[3 * warp + 1] = (T)dy;
-                    sd[3 * warp + 2] = (T)dz;
+                    sd[3 * warp] = dx;
+                    sd[3 * warp + 1] = dy;
+                    sd[3 * warp + 2] = dz;
                     s_q[warp] = (int)(q - p0);
                     const bool first = q == p0 || nb_j[q - 1] != j;
                     const bool last = q + 1 == p1 || nb_j[q + 1] != j;
@@ -606,8 +635,8 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                         bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
                     }
                     __syncwarp();
-                    const T invr = (T)1 / (T)dis;
-                    const T ux = (T)dx * invr, uy = (T)dy * invr, uz = (T)dz * invr;
+                    const T invr = (T)1 / dis;
+                    const T ux = dx * invr, uy = dy * invr, uz = dz * invr;
                     for (int u = lane; u < nh; u += 32) {
                         const int nk = ty.tp_head_nk[q0 + u];
                         const int nid = nk & 0xff, key = nk >> 8;
@@ -952,7 +981,7 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
     const int col = blockIdx.y * blockDim.x + threadIdx.x;
     if (col >= M.F) return;
     const bool force = f_row[s] >= 0;
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    LongSum<T> acc[7];
     for (int gi = B.st_atom_off[s]; gi < B.st_atom_off[s + 1]; ++gi) {
         const DevType& ty = M.types[B.types[gi]];
         int4 ci;
@@ -972,7 +1001,7 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
             w2 = Di[ci.x] * Di[ci.y];
             e = Di[ci.x] * Di[ci.y] * Di[ci.z];
         }
-        acc[0] += (double)e;
+        acc[0].add(e);
         if (!force) continue;
         const int nl = ty.n_lin;
         for (int l = 0; l < ty.n_tpl; ++l) {  // virial vectors per type pair, by position
@@ -984,13 +1013,13 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
                 T v = w0 * ds[(size_t)q * nl + x0];
                 if (ci.w > 1) v += w1 * ds[(size_t)q * nl + x1];
                 if (ci.w > 2) v += w2 * ds[(size_t)q * nl + x2];
-                acc[1 + q] -= (double)v;
+                acc[1 + q].add(-v);
             }
         }
     }
-    X[(size_t)col * ld + e_row[s]] = (T)acc[0];
+    X[(size_t)col * ld + e_row[s]] = (T)acc[0].value();
     if (force && s_row[s] >= 0)
-        for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[1 + q];
+        for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[1 + q].value();
 }
 
 // ------------------------------------------------------------ prefix sums
@@ -1022,6 +1051,10 @@ __global__ void pg_exclusive_scan(const int* counts, int n, long long* offsets, 
 // ------------------------------------------------------------- launchers
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st) {
     pg_exclusive_scan<<<1, 1024, 0, st>>>(counts, n, offsets, total);
+}
+
+void launch_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df, cudaStream_t st) {
+    if (n_pairs > 0) pg_nb_f32<<<(unsigned)((n_pairs + 255) / 256), 256, 0, st>>>(n_pairs, nb_d, nb_df);
 }
 
 void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st) {
