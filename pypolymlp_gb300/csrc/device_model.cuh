@@ -200,6 +200,7 @@ struct LongSum {
     __device__ __forceinline__ void add(double x) { v += x; }
     __device__ __forceinline__ double value() const { return v; }
     __device__ __forceinline__ double value64() const { return v; }
+    __device__ __forceinline__ void merge(const LongSum& o) { v += o.v; }
 };
 template <>
 struct LongSum<float> {
@@ -213,6 +214,10 @@ struct LongSum<float> {
     }
     __device__ __forceinline__ float value() const { return __fadd_rn(hi, lo); }
     __device__ __forceinline__ double value64() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ void merge(const LongSum& o) {
+        add(o.hi);
+        lo = __fadd_rn(lo, o.lo);
+    }
 };
 
 // Radial functions of one type pair at distance dis

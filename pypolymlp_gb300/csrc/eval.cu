@@ -146,16 +146,14 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
     for (long long k = nb_off[i] + warp; k < nb_off[i + 1]; k += nw) {
-        const double dx = nb_d[3 * k], dy = nb_d[3 * k + 1], dz = nb_d[3 * k + 2];
-        double dis = 0.0;
-        if (lane == 0) dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-        dis = __shfl_sync(0xffffffffu, dis, 0);
+        T dx, dy, dz, dis;
+        const bool ok = pair_geometry<T>(M, B, nb_d, k, dx, dy, dz, dis);
         double gx = 0.0, gy = 0.0, gz = 0.0;
-        if (dis < M.cutoff) {
+        if (ok) {
             const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
-            warp_radial<T, true>(M, tp, (T)dis, bv, lane);
+            warp_radial<T, true>(M, tp, dis, bv, lane);
             if (M.gtinv) {
-                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, (T)dx, (T)dy, (T)dz, (T)dis, bv, lane);
+                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
             } else if (lane == 0) {
                 bv.Y[0] = {(T)1, (T)0};
                 bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
@@ -178,10 +176,10 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
                 sy += __shfl_down_sync(0xffffffffu, sy, o);
                 sz += __shfl_down_sync(0xffffffffu, sz, o);
             }
-            const T sc = s0 / (T)dis;
-            gx = (double)(sc * (T)dx + sx);
-            gy = (double)(sc * (T)dy + sy);
-            gz = (double)(sc * (T)dz + sz);
+            const T sc = s0 / dis;
+            gx = (double)(sc * dx + sx);
+            gy = (double)(sc * dy + sy);
+            gz = (double)(sc * dz + sz);
         }
         if (lane == 0) {
             g_out[3 * k] = gx;

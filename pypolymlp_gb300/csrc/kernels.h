@@ -36,6 +36,35 @@ struct DevBatch {
     const float4* nb_df;
 };
 
+// Displacement and distance of neighbour-list entry k in T, and whether the
+// pair counts: sqrt(dx^2 + dy^2 + dz^2) < cutoff in FP64 (local.cpp's test).
+// The FP32 form decides from the FP32 squared distance when it is clearly
+// inside and falls back to the FP64 test near the cutoff.  Warp-uniform.
+template <typename T>
+__device__ __forceinline__ bool pair_geometry(const DevModel& M, const DevBatch& B, const double* nb_d, long long k,
+                                              T& dx, T& dy, T& dz, T& dis);
+template <>
+__device__ __forceinline__ bool pair_geometry<double>(const DevModel& M, const DevBatch& B, const double* nb_d,
+                                                      long long k, double& dx, double& dy, double& dz, double& dis) {
+    dx = nb_d[3 * k];
+    dy = nb_d[3 * k + 1];
+    dz = nb_d[3 * k + 2];
+    dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+    return dis < M.cutoff;
+}
+template <>
+__device__ __forceinline__ bool pair_geometry<float>(const DevModel& M, const DevBatch& B, const double* nb_d,
+                                                     long long k, float& dx, float& dy, float& dz, float& dis) {
+    const float4 g = B.nb_df[k];
+    dx = g.x;
+    dy = g.y;
+    dz = g.z;
+    dis = sqrtf(g.w);
+    if (g.w < M.rc2_safe_f) return true;
+    const double ex = nb_d[3 * k], ey = nb_d[3 * k + 1], ez = nb_d[3 * k + 2];
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez))) < M.cutoff;
+}
+
 constexpr int kCellListMinAtoms = 1024;  // structures this large use a cell list
 constexpr int kCellListMaxPairs = 4096;  // per atom, for the in-block ordering
 

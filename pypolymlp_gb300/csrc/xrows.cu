@@ -252,35 +252,6 @@ __global__ void pg_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df) 
     nb_df[k] = make_float4(x, y, z, x * x + y * y + z * z);
 }
 
-// Displacement and distance of neighbour-list entry k in T, and whether the
-// pair counts: sqrt(dx^2 + dy^2 + dz^2) < cutoff in FP64 (local.cpp's test).
-// The FP32 form decides from the FP32 squared distance when it is clearly
-// inside and falls back to the FP64 test near the cutoff.  Warp-uniform.
-template <typename T>
-__device__ __forceinline__ bool pair_geometry(const DevModel& M, const DevBatch& B, const double* nb_d, long long k,
-                                              T& dx, T& dy, T& dz, T& dis);
-template <>
-__device__ __forceinline__ bool pair_geometry<double>(const DevModel& M, const DevBatch& B, const double* nb_d,
-                                                      long long k, double& dx, double& dy, double& dz, double& dis) {
-    dx = nb_d[3 * k];
-    dy = nb_d[3 * k + 1];
-    dz = nb_d[3 * k + 2];
-    dis = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-    return dis < M.cutoff;
-}
-template <>
-__device__ __forceinline__ bool pair_geometry<float>(const DevModel& M, const DevBatch& B, const double* nb_d,
-                                                     long long k, float& dx, float& dy, float& dz, float& dis) {
-    const float4 g = B.nb_df[k];
-    dx = g.x;
-    dy = g.y;
-    dz = g.z;
-    dis = sqrtf(g.w);
-    if (g.w < M.rc2_safe_f) return true;
-    const double ex = nb_d[3 * k], ey = nb_d[3 * k + 1], ez = nb_d[3 * k + 2];
-    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez))) < M.cutoff;
-}
-
 // ---------------------------------------------------------------- K2 a_nlm
 // Block per centre atom, pairs taken one type pair at a time: the pairs of
 // that type pair are compacted into a list (256 at a time), warps compute the
@@ -968,21 +939,25 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     }
 }
 
-// Energy and stress rows: block per (structure, 256 columns), thread per
-// column, FP64 sums over the structure's centres in atom order:
+// Energy and stress rows: block per (structure, kEsCols columns), kEsSlices
+// threads per column, each summing every kEsSlices-th centre of the structure
+// (long sums: FP64, or float-float in the FP32 kernel); the slices' sums are
+// then added in slice order:
 //   X[e_row, col] = sum_i poly_col(d(i)),
 //   X[s_row + q, col] = -sum_i sum_{k in col} w_k,col(i) DS[i][3+q][k].
+constexpr int kEsCols = 64, kEsSlices = 4;
 template <typename T>
-__global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D, const long long* s_off,
-                           const T* DS,
-                           const long long* e_row, const long long* f_row, const long long* s_row, T* X,
-                           long long ld) {
+__global__ void __launch_bounds__(kEsCols * kEsSlices) pg_rows_es(DevModel M, DevBatch B, const long long* d_off,
+                                                                  const T* D, const long long* s_off, const T* DS,
+                                                                  const long long* e_row, const long long* f_row,
+                                                                  const long long* s_row, T* X, long long ld) {
+    __shared__ LongSum<T> s_part[kEsSlices - 1][7][kEsCols];
     const int s = blockIdx.x;
-    const int col = blockIdx.y * blockDim.x + threadIdx.x;
-    if (col >= M.F) return;
+    const int cl = threadIdx.x % kEsCols, slice = threadIdx.x / kEsCols;
+    const int col = blockIdx.y * kEsCols + cl;
     const bool force = f_row[s] >= 0;
     LongSum<T> acc[7];
-    for (int gi = B.st_atom_off[s]; gi < B.st_atom_off[s + 1]; ++gi) {
+    for (int gi = B.st_atom_off[s] + slice; col < M.F && gi < B.st_atom_off[s + 1]; gi += kEsSlices) {
         const DevType& ty = M.types[B.types[gi]];
         int4 ci;
         unpack_col(ty.col_pack[col], ci.x, ci.y, ci.z, ci.w);
@@ -1017,6 +992,12 @@ __global__ void pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const
             }
         }
     }
+    if (slice > 0)
+        for (int q = 0; q < 7; ++q) s_part[slice - 1][q][cl] = acc[q];
+    __syncthreads();
+    if (slice > 0 || col >= M.F) return;
+    for (int r = 0; r < kEsSlices - 1; ++r)
+        for (int q = 0; q < 7; ++q) acc[q].merge(s_part[r][q][cl]);
     X[(size_t)col * ld + e_row[s]] = (T)acc[0].value();
     if (force && s_row[s] >= 0)
         for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[1 + q].value();
@@ -1127,8 +1108,8 @@ template <typename T>
 void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const long long* s_off,
                     const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,
                     long long ld, cudaStream_t st) {
-    dim3 grid(B.n_st, (M.F + 255) / 256);
-    pg_rows_es<T><<<grid, 256, 0, st>>>(M, B, d_off, D, s_off, DS, e_row, f_row, s_row, X, ld);
+    dim3 grid(B.n_st, (M.F + kEsCols - 1) / kEsCols);
+    pg_rows_es<T><<<grid, kEsCols * kEsSlices, 0, st>>>(M, B, d_off, D, s_off, DS, e_row, f_row, s_row, X, ld);
 }
 
 template void launch_anlm<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
