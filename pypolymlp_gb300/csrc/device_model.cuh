@@ -48,6 +48,13 @@ __device__ inline T term_product_real(const FlatTerm& t, const cplx<T>* a) {
     return creal_mul(v, a[t.ids[0]]);
 }
 
+// Windowed warp sums.  A warp owns 32 outputs whose terms are contiguous in
+// a term list (output l's terms are [off_l, off_l+1)): the terms are evaluated
+// 32 at a time by all lanes, whatever output they belong to, into a window
+// s_v of kTermWin values; then each lane adds its own output's terms from the
+// window, in list order.  This balances outputs with unequal term counts.
+constexpr int kTermWin = 128;
+
 struct DevType {
     int K, K0, n_lin, n_ent;
     const int *head_tp, *head_nid, *head_key, *head_m, *head_full, *head_jloc;
@@ -77,6 +84,49 @@ struct DevType {
     const int4* tcode;
     const void* tcoef;
 };
+
+// Feature values d_k = sum_q coeff_q Re(prod a[ids_q]) of one centre, one
+// warp per 32 consecutive features (windowed warp sums over val_terms).
+template <typename T>
+__device__ __forceinline__ void warp_feature_values(const DevType& ty, const cplx<T>* a, T* out, cplx<T>* s_v,
+                                                    int warp, int n_warps, int lane) {
+    for (int k0 = 32 * warp; k0 < ty.n_lin; k0 += 32 * n_warps) {
+        const int k = k0 + lane;
+        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, ty.n_lin)];
+        const int ms = k < ty.n_lin ? ty.val_off[k] : te, me = k < ty.n_lin ? ty.val_off[k + 1] : te;
+        T v = 0;
+        for (int w0 = tb; w0 < te; w0 += kTermWin) {
+#pragma unroll
+            for (int u = 0; u < kTermWin / 32; ++u) {
+                const int t = w0 + 32 * u + lane;
+                if (t < te) {
+                    const FlatTerm& f = ty.val_terms[t];
+                    s_v[32 * u + lane].re = (T)f.coeff * term_product_real<T>(f, a);
+                }
+            }
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kTermWin);
+            for (int t = lo; t < hi; ++t) v += s_v[t - w0].re;
+            __syncwarp();
+        }
+        if (k < ty.n_lin) out[k] = v;
+    }
+}
+
+// Product of the a ids of a packed term (ids 16 bits each, two per word in x,
+// y, z; n in the low byte of w), in the order of term_product.
+template <typename T>
+__device__ __forceinline__ cplx<T> packed_term_product(const int4 c4, const cplx<T>* a) {
+    const int n = c4.w & 0xff;
+    const int id[6] = {c4.x & 0xffff, (c4.x >> 16) & 0xffff, c4.y & 0xffff,
+                       (c4.y >> 16) & 0xffff, c4.z & 0xffff, (c4.z >> 16) & 0xffff};
+    cplx<T> p = {(T)1, (T)0};
+    if (n > 0) p = a[id[0]];
+#pragma unroll
+    for (int q = 1; q < 6; ++q)
+        if (q < n) p = cmul(p, a[id[q]]);
+    return p;
+}
 
 struct DevModel {
     int n_type, n_tp, F, n_fn_max, maxl, n_ylm, gtinv;

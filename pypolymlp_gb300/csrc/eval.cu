@@ -31,7 +31,23 @@ namespace pg {
 struct EvalType {
     const int *ent_k, *head_ent_off, *head_ent, *tp_head_off, *tp_heads;
     const int *kcol_off, *kcol_col, *kcol_o1, *kcol_o2;
+    // adjoint terms by head: head h owns terms head_toff[h] .. head_toff[h + 1]
+    // (its entries in head_ent order, their terms in order); per term the
+    // packed a ids (as tcode), the feature of its entry and its coefficient
+    // (the sign of a conjugate head folded into conjugate terms)
+    const int* head_toff;
+    const int4* htcode;
+    const int* htk;
+    const double* htcoef64;
+    const float* htcoef32;
 };
+
+template <typename T>
+__device__ __forceinline__ const T* head_term_coef(const EvalType& e);
+template <>
+__device__ __forceinline__ const double* head_term_coef<double>(const EvalType& e) { return e.htcoef64; }
+template <>
+__device__ __forceinline__ const float* head_term_coef<float>(const EvalType& e) { return e.htcoef32; }
 
 struct EvalTables {
     EvalType types[kMaxTypes];
@@ -61,14 +77,10 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
-        T v = 0;
-        for (int q = ty.val_off[k]; q < ty.val_off[k + 1]; ++q) {
-            const FlatTerm& t = ty.val_terms[q];
-            v += (T)t.coeff * term_product_real<T>(t, a);
-        }
-        d[k] = v;
-    }
+    constexpr int NW = 8;  // 256 threads
+    __shared__ cplx<T> s_v[NW][kTermWin];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    warp_feature_values<T>(ty, a, d, s_v[warp], warp, NW, lane);
     __syncthreads();
     // beta_k = sum over polynomial columns containing k of coef * product of the others
     for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
@@ -99,28 +111,38 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
         Eatom[i] = s;
     }
-    // A[h] = sum over entries with head h of beta_k(e) G_e
+    // A[h] = sum over entries with head h of beta_k(e) G_e: windowed warp sums
+    // over the head-ordered terms, 32 heads per warp (beta is complete: the
+    // block synchronised after it)
     cplx<T>* Ao = Aout + a_off[i];
-    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) {
-        const T cc = (ty.head_m[h] & 1) ? (T)-1 : (T)1;
+    const T* hcoef = head_term_coef<T>(et);
+    for (int h0 = 32 * warp; h0 < ty.K0; h0 += 32 * NW) {
+        const int h = h0 + lane;
+        const int tb = et.head_toff[h0], te = et.head_toff[min(h0 + 32, ty.K0)];
+        const int ms = h < ty.K0 ? et.head_toff[h] : te, me = h < ty.K0 ? et.head_toff[h + 1] : te;
         T re = 0, im = 0;
-        for (int q = et.head_ent_off[h]; q < et.head_ent_off[h + 1]; ++q) {
-            const int ent = et.head_ent[q];
-            const T b = beta[et.ent_k[ent]];
-            for (int u = ty.term_off[ent]; u < ty.term_off[ent + 1]; ++u) {
-                const FlatTerm& t = ty.g_terms[u];
-                const cplx<T> p = term_product<T>(t, a);
-                const T c = b * (T)t.coeff;
-                if (t.conj) {
-                    re += cc * c * p.re;
-                    im -= cc * c * p.im;
-                } else {
-                    re += c * p.re;
-                    im += c * p.im;
+        for (int w0 = tb; w0 < te; w0 += kTermWin) {
+#pragma unroll
+            for (int u = 0; u < kTermWin / 32; ++u) {
+                const int t = w0 + 32 * u + lane;
+                if (t < te) {
+                    const int4 c4 = et.htcode[t];
+                    const T c = beta[et.htk[t]] * hcoef[t];
+                    const cplx<T> p = packed_term_product<T>(c4, a);
+                    cplx<T> v = {c * p.re, c * p.im};
+                    if (c4.w >> 8) v.im = -v.im;
+                    s_v[warp][32 * u + lane] = v;
                 }
             }
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kTermWin);
+            for (int t = lo; t < hi; ++t) {
+                re += s_v[warp][t - w0].re;
+                im += s_v[warp][t - w0].im;
+            }
+            __syncwarp();
         }
-        Ao[h] = {re, im};
+        if (h < ty.K0) Ao[h] = {re, im};
     }
 }
 
@@ -254,7 +276,7 @@ struct Evaluator {
         m = std::make_unique<Model>(fp);
         if (n != m->flat.n_features) throw std::runtime_error("coefficient count does not match the model");
         upload(coef, std::vector<double>(coeffs, coeffs + n));
-        bufs.reserve(16 * kMaxTypes);
+        bufs.reserve(32 * kMaxTypes);
         auto up = [&](const std::vector<int>& v) -> const int* {
             bufs.emplace_back();
             upload(bufs.back(), v);
@@ -272,6 +294,37 @@ struct Evaluator {
             e.kcol_col = up(ft.kcol_col);
             e.kcol_o1 = up(ft.kcol_o1);
             e.kcol_o2 = up(ft.kcol_o2);
+            if (ft.K >= 65536) throw std::runtime_error("too many a_nlm entries for the packed term ids");
+            std::vector<int> toff(1, 0), tk;
+            std::vector<int4> tcode;
+            std::vector<double> tcoef;
+            for (int h = 0; h < ft.K0; ++h) {
+                const double cc = (ft.head_m[h] & 1) ? -1.0 : 1.0;
+                for (int q = ft.head_ent_off[h]; q < ft.head_ent_off[h + 1]; ++q) {
+                    const int ent = ft.head_ent[q];
+                    for (int u = ft.term_off[ent]; u < ft.term_off[ent + 1]; ++u) {
+                        const FlatTerm& t = ft.g_terms[u];
+                        int id[6] = {0, 0, 0, 0, 0, 0};
+                        for (int r = 0; r < t.n; ++r) id[r] = t.ids[r];
+                        tcode.push_back(make_int4(id[0] | (id[1] << 16), id[2] | (id[3] << 16),
+                                                  id[4] | (id[5] << 16), t.n | (t.conj << 8)));
+                        tcoef.push_back(t.conj ? cc * t.coeff : t.coeff);
+                        tk.push_back(ft.ent_k[ent]);
+                    }
+                }
+                toff.push_back((int)tcode.size());
+            }
+            e.head_toff = up(toff);
+            e.htk = up(tk);
+            bufs.emplace_back();
+            upload(bufs.back(), tcode);
+            e.htcode = bufs.back().as<int4>();
+            bufs.emplace_back();
+            upload(bufs.back(), tcoef);
+            e.htcoef64 = bufs.back().as<double>();
+            bufs.emplace_back();
+            upload(bufs.back(), std::vector<float>(tcoef.begin(), tcoef.end()));
+            e.htcoef32 = bufs.back().as<float>();
         }
     }
 

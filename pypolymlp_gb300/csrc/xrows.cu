@@ -359,36 +359,11 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
         }
     }
     __syncthreads();
-    // Both loops below give a warp 32 outputs whose terms are contiguous: the
-    // terms are evaluated 32 at a time by all lanes, whatever output they
-    // belong to, into a window of s_v; then each lane adds its own output's
-    // terms from the window, in order.
-    constexpr int NW = 8, kWin = 128;
+    // windowed warp sums (see kTermWin): feature values, then adjoint entries
+    constexpr int NW = 8, kWin = kTermWin;
     __shared__ cplx<T> s_v[NW][kWin];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // feature values, 32 features per warp
-    T* Di = D + d_off[i];
-    for (int k0 = 32 * warp; k0 < ty.n_lin; k0 += 32 * NW) {
-        const int k = k0 + lane;
-        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, ty.n_lin)];
-        const int ms = k < ty.n_lin ? ty.val_off[k] : te, me = k < ty.n_lin ? ty.val_off[k + 1] : te;
-        T v = 0;
-        for (int w0 = tb; w0 < te; w0 += kWin) {
-#pragma unroll
-            for (int u = 0; u < kWin / 32; ++u) {
-                const int t = w0 + 32 * u + lane;
-                if (t < te) {
-                    const FlatTerm& f = ty.val_terms[t];
-                    s_v[warp][32 * u + lane].re = (T)f.coeff * term_product_real<T>(f, a);
-                }
-            }
-            __syncwarp();
-            const int lo = max(ms, w0), hi = min(me, w0 + kWin);
-            for (int t = lo; t < hi; ++t) v += s_v[warp][t - w0].re;
-            __syncwarp();
-        }
-        if (k < ty.n_lin) Di[k] = v;
-    }
+    warp_feature_values<T>(ty, a, D + d_off[i], s_v[warp], warp, NW, lane);
     // adjoint entries in the X-row layout (rank-major groups of 32 features
     // per type pair; padding slots hold zero), warp per rank of 32 slots
     cplx<T>* Gi = G + g_off[i];
@@ -405,14 +380,7 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
                 if (t < te) {
                     const int4 c4 = ty.tcode[t];
                     const T cf = coef[t];
-                    const int n = c4.w & 0xff;
-                    const int id[6] = {c4.x & 0xffff, (c4.x >> 16) & 0xffff, c4.y & 0xffff,
-                                       (c4.y >> 16) & 0xffff, c4.z & 0xffff, (c4.z >> 16) & 0xffff};
-                    cplx<T> p = {(T)1, (T)0};
-                    if (n > 0) p = a[id[0]];
-#pragma unroll
-                    for (int q = 1; q < 6; ++q)
-                        if (q < n) p = cmul(p, a[id[q]]);
+                    const cplx<T> p = packed_term_product<T>(c4, a);
                     cplx<T> v = {cf * p.re, cf * p.im};
                     if (c4.w >> 8) v.im = -v.im;
                     s_v[warp][32 * u + lane] = v;
