@@ -349,12 +349,11 @@ void DeviceBatch::build_neighbors(double cutoff, cudaStream_t stream) {
     n_pairs = total;
     d_nb_j.reserve(sizeof(int) * std::max<long long>(1, n_pairs));
     d_nb_d.reserve(sizeof(double) * 3 * std::max<long long>(1, n_pairs));
-    if (n_cl > 0) d_keys.reserve(sizeof(long long) * std::max<long long>(1, n_pairs));
+    d_keys.reserve(sizeof(long long) * std::max<long long>(1, n_pairs));
     d_nb_df.reserve(sizeof(float4) * std::max<long long>(1, n_pairs));
     ProfScope ps("pg_nb_fill", stream);
-    launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), d_keys.as<long long>(),
-                   n_cl > 0, stream);
-    launch_nb_f32(n_pairs, d_nb_d.as<double>(), d_nb_df.as<float4>(), stream);
+    launch_nb_fill(B, d_nb_off.as<long long>(), d_nb_j.as<int>(), d_nb_d.as<double>(), d_nb_df.as<float4>(),
+                   d_keys.as<long long>(), n_cl > 0, stream);
 }
 
 void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double cutoff, cudaStream_t stream) {
@@ -394,6 +393,7 @@ DevBatch DeviceBatch::view(double cutoff) const {
     // rounding of r2; the margin below covers that with a factor > 10
     const double L = std::max(1.0, coord_max);
     B.prefilter_r2 = (float)(cutoff * cutoff * (1.0 + 1e-4) + 1e-5 * L * (cutoff + L) + 1e-3);
+    B.inner_r2 = (float)std::max(0.0, cutoff * cutoff * (1.0 - 1e-4) - 1e-5 * L * (cutoff + L) - 1e-3);
     return B;
 }
 
@@ -447,9 +447,9 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
     }
     size_t max_lin = 1;
     for (const auto& ft : flat.types) max_lin = std::max<size_t>(max_lin, ft.n_lin);
-    // per pair: index, FP64 and FP32 displacements, mirror, group slot, order and
+    // per pair: index, key, FP64 and FP32 displacements, mirror, group slot, order and
     // the pair derivatives (3 per feature); X rows
-    return mx + (size_t)(mean_pairs * (64.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;
+    return mx + (size_t)(mean_pairs * (72.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;
 }
 
 // Per-batch plan: per-atom storage offsets and pg_rows work items.

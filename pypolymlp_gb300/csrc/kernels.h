@@ -22,6 +22,7 @@ struct DevBatch {
     const float4* transf;      // FP32 copies of trans
     double cutoff;
     float prefilter_r2;        // FP32 squared distance above which a candidate is surely beyond the cutoff
+    float inner_r2;            // FP32 squared distance below which a candidate is surely inside it
     // cell lists of the large structures (st_cl[s] >= 0): per such structure a
     // grid of bins over its atoms' fractional coordinates
     const int* st_cl;          // per structure: cell-list index or -1
@@ -72,8 +73,8 @@ constexpr int kRowsThreads = 256;  // threads of pg_rows / pg_rows_pairs blocks
 constexpr int kMaxTypePairs = 64;
 
 void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st);
-void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, long long* keys, bool any_cl,
-                    cudaStream_t st);
+void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, float4* nb_df, long long* keys,
+                    bool any_cl, cudaStream_t st);
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
                  const long long* a_off, double2* A, int max_k0, cudaStream_t st);
@@ -81,7 +82,6 @@ template <typename T>
 void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
-void launch_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df, cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
 size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64);
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,

@@ -1,13 +1,14 @@
 // Training rows of X on the GPU.
 //
 //   pg_nb_count / pg_nb_fill   full neighbour list of every atom of a batch
-//   (+ pg_nb_order)            (NeighborFull, compute/neighbor_full.cpp:10-76):
+//   (+ pg_nb_order/pg_nb_disp) (NeighborFull, compute/neighbor_full.cpp:10-76):
 //                              same (j, translation) order and bit-identical
 //                              displacements (IEEE double, no contraction);
 //                              structures of 1,024+ atoms search a cell list and
 //                              order their candidates afterwards.
 //   pg_anlm                    a_nlm for m <= 0 of every atom (local.cpp:62-114),
-//                              sums over neighbours accumulated in FP64.
+//                              sums over neighbours accumulated in FP64 (FP32
+//                              kernel: float-float).
 //   pg_features_adjoint        invariant features d_k of every atom and the
 //                              sparse adjoint G_k[h] = d d_k / d a_h with the
 //                              conjugate half folded in (features.cpp:155-248),
@@ -33,23 +34,46 @@ namespace pg {
 // ------------------------------------------------------------ K1 neighbours
 // One warp per centre atom; candidates (j, t) in j-major order.  Only
 // __dadd_rn/__dmul_rn are used so nothing is contracted into an FMA.
-__device__ __forceinline__ bool pair_keep(const DevBatch& B, int i, int j, int t, double rc2, double tol2,
-                                          double& dx, double& dy, double& dz) {
-    // FP32 pre-filter: a candidate whose FP32 distance exceeds the cutoff by more
-    // than the rounding margin is beyond it in FP64 too; the rest are decided in FP64
-    {
-        const float4 a = B.posf[i], b = B.posf[j], tt = B.transf[t];
-        const float fx = b.x - a.x + tt.x, fy = b.y - a.y + tt.y, fz = b.z - a.z + tt.z;
-        if (fx * fx + fy * fy + fz * fz > B.prefilter_r2) return false;
-    }
+// Whether candidate (j, translation t) is a neighbour of i: the FP64
+// squared distance r2 = dx^2 + dy^2 + dz^2 (dx = (pj - pi) + t, no
+// contraction) satisfies tol2 < r2 < rc2.  FP32 decides every candidate
+// whose FP32 squared distance is beyond the rounding margin on either side
+// (prefilter_r2 above, inner_r2 below, and well above zero); the rest (a
+// thin shell at the cutoff, near-coincident atoms) are decided in FP64.
+__device__ __forceinline__ bool pair_in(const DevBatch& B, int i, int j, int t, double rc2, double tol2) {
+    const float4 a = B.posf[i], b = B.posf[j], tt = B.transf[t];
+    const float fx = b.x - a.x + tt.x, fy = b.y - a.y + tt.y, fz = b.z - a.z + tt.z;
+    const float r2f = fx * fx + fy * fy + fz * fz;
+    if (r2f > B.prefilter_r2) return false;
+    if (r2f < B.inner_r2 && r2f > 1e-6f) return true;
     const double* pi = B.pos + 3 * (size_t)i;
     const double* pj = B.pos + 3 * (size_t)j;
     const double* tr = B.trans + 3 * (size_t)t;
-    dx = __dadd_rn(__dadd_rn(pj[0], -pi[0]), tr[0]);
-    dy = __dadd_rn(__dadd_rn(pj[1], -pi[1]), tr[1]);
-    dz = __dadd_rn(__dadd_rn(pj[2], -pi[2]), tr[2]);
+    const double dx = __dadd_rn(__dadd_rn(pj[0], -pi[0]), tr[0]);
+    const double dy = __dadd_rn(__dadd_rn(pj[1], -pi[1]), tr[1]);
+    const double dz = __dadd_rn(__dadd_rn(pj[2], -pi[2]), tr[2]);
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     return r2 < rc2 && r2 > tol2;
+}
+
+// List entry q of atom i from its key j_local * nt + t: the neighbour, the
+// FP64 displacement (pj - pi) + t (the form the neighbour test uses) and its
+// FP32 copy with the FP32 squared distance.
+__device__ __forceinline__ void write_entry(const DevBatch& B, int i, int a0, int t0, int nt, long long key,
+                                            long long q, int* nb_j, double* nb_d, float4* nb_df) {
+    const int j = a0 + (int)(key / nt), t = t0 + (int)(key % nt);
+    const double* pi = B.pos + 3 * (size_t)i;
+    const double* pj = B.pos + 3 * (size_t)j;
+    const double* tr = B.trans + 3 * (size_t)t;
+    const double dx = __dadd_rn(__dadd_rn(pj[0], -pi[0]), tr[0]);
+    const double dy = __dadd_rn(__dadd_rn(pj[1], -pi[1]), tr[1]);
+    const double dz = __dadd_rn(__dadd_rn(pj[2], -pi[2]), tr[2]);
+    nb_j[q] = j;
+    nb_d[3 * q] = dx;
+    nb_d[3 * q + 1] = dy;
+    nb_d[3 * q + 2] = dz;
+    const float x = (float)dx, y = (float)dy, z = (float)dz;
+    nb_df[q] = make_float4(x, y, z, x * x + y * y + z * z);
 }
 
 // Cell-list candidates of atom i (structure with cell list c): for every
@@ -96,10 +120,8 @@ __global__ void pg_nb_count(DevBatch B, int* counts, int* max_cl) {
                 for (int by = q.lo[1]; by <= q.hi[1]; ++by)
                     for (int bx = q.lo[0]; bx <= q.hi[0]; ++bx) {
                         const int bin = g.w + (bz * g.y + by) * g.x + bx;
-                        for (int k = B.cl_bin_start[bin] + lane; k < B.cl_bin_start[bin + 1]; k += 32) {
-                            double dx, dy, dz;
-                            cnt += pair_keep(B, i, B.cl_atoms[k], t0 + u, rc2, tol2, dx, dy, dz) ? 1 : 0;
-                        }
+                        for (int k = B.cl_bin_start[bin] + lane; k < B.cl_bin_start[bin + 1]; k += 32)
+                            cnt += pair_in(B, i, B.cl_atoms[k], t0 + u, rc2, tol2) ? 1 : 0;
                     }
         }
     } else {
@@ -108,8 +130,7 @@ __global__ void pg_nb_count(DevBatch B, int* counts, int* max_cl) {
         int j = lane / nt, t = lane % nt;
         const int dj = 32 / nt, dt = 32 % nt;
         for (int q = lane; q < total; q += 32) {
-            double dx, dy, dz;
-            cnt += pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz) ? 1 : 0;
+            cnt += pair_in(B, i, a0 + j, t0 + t, rc2, tol2) ? 1 : 0;
             j += dj;
             t += dt;
             if (t >= nt) {
@@ -125,9 +146,10 @@ __global__ void pg_nb_count(DevBatch B, int* counts, int* max_cl) {
     }
 }
 
-// Brute-force atoms write their list in (j, t) order directly; cell-list atoms
-// write their candidates' keys j_local * nt + t unordered, ordered by pg_nb_order.
-__global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, double* nb_d, long long* keys) {
+// The kept candidates' keys j_local * nt + t: in (j, t) order for brute-force
+// atoms (entries written by pg_nb_disp), unordered for cell-list atoms
+// (ordered and written by pg_nb_order).
+__global__ void pg_nb_fill(DevBatch B, const long long* offsets, long long* keys) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= B.n_atoms) return;
@@ -155,9 +177,8 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
                             int j = 0;
                             bool keep = false;
                             if (k < ke) {
-                                double dx, dy, dz;
                                 j = B.cl_atoms[k];
-                                keep = pair_keep(B, i, j, t0 + u, rc2, tol2, dx, dy, dz);
+                                keep = pair_in(B, i, j, t0 + u, rc2, tol2);
                             }
                             const unsigned m = __ballot_sync(0xffffffffu, keep);
                             if (keep) {
@@ -175,10 +196,9 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
     const int dj = 32 / nt, dt = 32 % nt;
     for (int base = 0; base < total; base += 32) {
         const int q = base + lane;
-        double dx = 0, dy = 0, dz = 0;
-        const int jq = j;
+        const int jq = j, tq = t;
         bool keep = false;
-        if (q < total) keep = pair_keep(B, i, a0 + j, t0 + t, rc2, tol2, dx, dy, dz);
+        if (q < total) keep = pair_in(B, i, a0 + j, t0 + t, rc2, tol2);
         j += dj;
         t += dt;
         if (t >= nt) {
@@ -188,21 +208,31 @@ __global__ void pg_nb_fill(DevBatch B, const long long* offsets, int* nb_j, doub
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) {
             const long long k = w + __popc(m & ((1u << lane) - 1u));
-            if (k < wend) {
-                nb_j[k] = a0 + jq;
-                nb_d[3 * k] = dx;
-                nb_d[3 * k + 1] = dy;
-                nb_d[3 * k + 2] = dz;
-            }
+            if (k < wend) keys[k] = (long long)jq * nt + tq;
         }
         w += __popc(m);
     }
 }
 
+// Entries of the brute-force atoms from their keys (one warp per atom).
+__global__ void pg_nb_disp(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d,
+                           float4* nb_df) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= B.n_atoms) return;
+    const int s = B.atom_st[i];
+    if (B.st_cl[s] >= 0) return;
+    const int a0 = B.st_atom_off[s];
+    const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
+    for (long long q = offsets[i] + lane; q < offsets[i + 1]; q += 32)
+        write_entry(B, i, a0, t0, nt, keys[q], q, nb_j, nb_d, nb_df);
+}
+
 // Cell-list atoms: sort the candidate keys (block per atom, bitonic in shared
 // memory) into the reference's (j, t) order and write the list entries, with
-// the displacement recomputed exactly as pair_keep forms it.
-__global__ void pg_nb_order(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d) {
+// the displacement recomputed exactly as the neighbour test forms it.
+__global__ void pg_nb_order(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d,
+                            float4* nb_df) {
     __shared__ long long sk[kCellListMaxPairs];
     const int i = blockIdx.x;
     const int s = B.atom_st[i];
@@ -231,25 +261,7 @@ __global__ void pg_nb_order(DevBatch B, const long long* offsets, const long lon
             }
             __syncthreads();
         }
-    for (int q = threadIdx.x; q < m; q += blockDim.x) {
-        const long long key = sk[q];
-        const int j = a0 + (int)(key / nt), t = t0 + (int)(key % nt);
-        const double* pi = B.pos + 3 * (size_t)i;
-        const double* pj = B.pos + 3 * (size_t)j;
-        const double* tr = B.trans + 3 * (size_t)t;
-        nb_j[o0 + q] = j;
-        nb_d[3 * (o0 + q)] = __dadd_rn(__dadd_rn(pj[0], -pi[0]), tr[0]);
-        nb_d[3 * (o0 + q) + 1] = __dadd_rn(__dadd_rn(pj[1], -pi[1]), tr[1]);
-        nb_d[3 * (o0 + q) + 2] = __dadd_rn(__dadd_rn(pj[2], -pi[2]), tr[2]);
-    }
-}
-
-// FP32 copy of the neighbour-list displacements: (dx, dy, dz, dx^2 + dy^2 + dz^2).
-__global__ void pg_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df) {
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_pairs) return;
-    const float x = (float)nb_d[3 * k], y = (float)nb_d[3 * k + 1], z = (float)nb_d[3 * k + 2];
-    nb_df[k] = make_float4(x, y, z, x * x + y * y + z * z);
+    for (int q = threadIdx.x; q < m; q += blockDim.x) write_entry(B, i, a0, t0, nt, sk[q], o0 + q, nb_j, nb_d, nb_df);
 }
 
 // ---------------------------------------------------------------- K2 a_nlm
@@ -1002,20 +1014,17 @@ void launch_exclusive_scan(const int* counts, int n, long long* offsets, long lo
     pg_exclusive_scan<<<1, 1024, 0, st>>>(counts, n, offsets, total);
 }
 
-void launch_nb_f32(long long n_pairs, const double* nb_d, float4* nb_df, cudaStream_t st) {
-    if (n_pairs > 0) pg_nb_f32<<<(unsigned)((n_pairs + 255) / 256), 256, 0, st>>>(n_pairs, nb_d, nb_df);
-}
-
 void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st) {
     const int threads = 256, warps = threads / 32;
     pg_nb_count<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, counts, max_cl);
 }
 
-void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, long long* keys, bool any_cl,
-                    cudaStream_t st) {
+void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, float4* nb_df, long long* keys,
+                    bool any_cl, cudaStream_t st) {
     const int threads = 256, warps = threads / 32;
-    pg_nb_fill<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, nb_j, nb_d, keys);
-    if (any_cl) pg_nb_order<<<B.n_atoms, 256, 0, st>>>(B, off, keys, nb_j, nb_d);
+    pg_nb_fill<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, keys);
+    if (any_cl) pg_nb_order<<<B.n_atoms, 256, 0, st>>>(B, off, keys, nb_j, nb_d, nb_df);
+    pg_nb_disp<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, keys, nb_j, nb_d, nb_df);
 }
 
 template <typename T>
