@@ -740,6 +740,46 @@ __device__ __forceinline__ void unpack_col(int2 c, int& k0, int& k1, int& k2, in
     w = (c.y >> 16) & 0xffff;
 }
 
+// Recipe of product column p of a centre type for stage B: the column, its
+// features k0, k1 (, k2) with their positions x in the group vectors of the
+// type pair, and which positions lie below nnz (the others hold no data: their
+// derivatives vanish).  False when the column has no such position.
+struct ProdCol {
+    int col, k0, k1, k2, w, x0, x1, x2;
+    bool b0, b1, b2;
+};
+__device__ __forceinline__ bool prod_col(const DevType& ty, const int* ipos, int nnz, int p, ProdCol& pc) {
+    pc.col = ty.prod_col[p];
+    unpack_col(ty.col_pack[pc.col], pc.k0, pc.k1, pc.k2, pc.w);
+    pc.x0 = ipos[pc.k0];
+    pc.x1 = ipos[pc.k1];
+    pc.x2 = pc.w > 2 ? ipos[pc.k2] : 0;
+    pc.b0 = pc.x0 < nnz;
+    pc.b1 = pc.x1 < nnz;
+    pc.b2 = pc.w > 2 && pc.x2 < nnz;
+    return pc.b0 || pc.b1 || pc.b2;
+}
+// v += the column's derivative from one group vector src (3 x NL), with the
+// centre's features Di as weights.
+template <typename T>
+__device__ __forceinline__ void prod_col_add(const ProdCol& pc, const T* src, const T* Di, int NL, T (&v)[3]) {
+    T w0, w1, w2 = 0;
+    if (pc.w == 2) {
+        w0 = Di[pc.k1];
+        w1 = Di[pc.k0];
+    } else {
+        w0 = Di[pc.k1] * Di[pc.k2];
+        w1 = Di[pc.k0] * Di[pc.k2];
+        w2 = Di[pc.k0] * Di[pc.k1];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T s0 = pc.b0 ? src[c * NL + pc.x0] : (T)0, s1 = pc.b1 ? src[c * NL + pc.x1] : (T)0;
+        v[c] += w0 * s0 + w1 * s1;
+        if (pc.b2) v[c] += w2 * src[c * NL + pc.x2];
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
@@ -791,14 +831,22 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 n += total;
                 __syncthreads();
             }
-            // linear columns: sum of the group vectors
+            // linear columns: sum of the group vectors.  When one slab covers
+            // the positions and a thread per product column suffices, the
+            // product columns are gathered in the same pass over the groups,
+            // while the group vector is in L1; else in a pass of their own.
+            const bool fuse = nnz <= S * (int)blockDim.x && ty.n_prod <= (int)blockDim.x;
+            ProdCol pc;
+            const bool has_pc = fuse && (int)threadIdx.x < ty.n_prod && prod_col(ty, ipos, nnz, threadIdx.x, pc);
+            T pv[3] = {0, 0, 0};
             for (int slab = 0; slab < nnz; slab += S * blockDim.x) {
                 T acc[S][3];
 #pragma unroll
                 for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
 #pragma unroll 2
                 for (int k = 0; k < n; ++k) {
-                    const T* src = Dp + (size_t)(sb + s_list[k]) * 3 * NL;
+                    const long long q = sb + s_list[k];
+                    const T* src = Dp + (size_t)q * 3 * NL;
 #pragma unroll
                     for (int m = 0; m < S; ++m) {
                         const int x = slab + threadIdx.x + m * blockDim.x;
@@ -808,6 +856,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                             acc[m][2] += src[2 * NL + x];
                         }
                     }
+                    if (has_pc) prod_col_add(pc, src, D + d_off[nb_j[q]], NL, pv);
                 }
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
@@ -821,45 +870,24 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                     o[2] -= acc[m][2];
                 }
             }
-            // product columns
-            for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
-                const int col = ty.prod_col[p];
-                int k0, k1, k2, w;
-                unpack_col(ty.col_pack[col], k0, k1, k2, w);
-                const int x0 = ipos[k0], x1 = ipos[k1], x2 = w > 2 ? ipos[k2] : 0;
-                // components at positions from nnz on vanish
-                const bool b0 = x0 < nnz, b1 = x1 < nnz, b2 = w > 2 && x2 < nnz;
-                if (!(b0 || b1 || b2)) continue;
-                T v0 = 0, v1 = 0, v2 = 0;
+            if (has_pc) {
+                T* o = X + (size_t)pc.col * ld + r0;
+                o[0] -= pv[0];
+                o[1] -= pv[1];
+                o[2] -= pv[2];
+            }
+            // product columns, own pass
+            for (int p = threadIdx.x; !fuse && p < ty.n_prod; p += blockDim.x) {
+                if (!prod_col(ty, ipos, nnz, p, pc)) continue;
+                T v[3] = {0, 0, 0};
                 for (int k = 0; k < n; ++k) {
                     const long long q = sb + s_list[k];
-                    const T* src = Dp + (size_t)q * 3 * NL;
-                    const T* Di = D + d_off[nb_j[q]];
-                    T w0, w1, w2 = 0;
-                    if (w == 2) {
-                        w0 = Di[k1];
-                        w1 = Di[k0];
-                    } else {
-                        w0 = Di[k1] * Di[k2];
-                        w1 = Di[k0] * Di[k2];
-                        w2 = Di[k0] * Di[k1];
-                    }
-                    const T s0 = b0 ? src[x0] : (T)0, s1 = b1 ? src[x1] : (T)0;
-                    const T t0 = b0 ? src[NL + x0] : (T)0, t1 = b1 ? src[NL + x1] : (T)0;
-                    const T u0 = b0 ? src[2 * NL + x0] : (T)0, u1 = b1 ? src[2 * NL + x1] : (T)0;
-                    v0 += w0 * s0 + w1 * s1;
-                    v1 += w0 * t0 + w1 * t1;
-                    v2 += w0 * u0 + w1 * u1;
-                    if (b2) {
-                        v0 += w2 * src[x2];
-                        v1 += w2 * src[NL + x2];
-                        v2 += w2 * src[2 * NL + x2];
-                    }
+                    prod_col_add(pc, Dp + (size_t)q * 3 * NL, D + d_off[nb_j[q]], NL, v);
                 }
-                T* o = X + (size_t)col * ld + r0;
-                o[0] -= v0;
-                o[1] -= v1;
-                o[2] -= v2;
+                T* o = X + (size_t)pc.col * ld + r0;
+                o[0] -= v[0];
+                o[1] -= v[1];
+                o[2] -= v[2];
             }
             // before the list is rebuilt; a column shared by several types is
             // also updated type by type
