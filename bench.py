@@ -222,7 +222,7 @@ def eval_bench(params, args):
         out["cpu_baseline"] = {"value": 1024 / dt, "unit": "atoms/s", "cores": n_threads, "kind": "port",
                                "sample": f"bcc 8x8x8x2 = 1024 atoms, CPU oracle E/F/S, {dt:.2f}s"}
     out["other_cells"] = {}
-    for n in (8, 40):
+    for n in () if args.no_other_cells else (8, 40):
         if n != args.eval_cell:
             r = one(n)
             out["other_cells"][r["workload"].split(" = ")[1].split(",")[0]] = {
@@ -275,6 +275,8 @@ def main():
     ap.add_argument("--fp64", action="store_true", help="time the FP64 reference-precision path instead")
     ap.add_argument("--no-eval", action="store_true", help="skip the E/F/S evaluation figure")
     ap.add_argument("--eval-cell", type=int, default=20, help="bcc repeats n (n^3 x 2 atoms) of the E/F/S cell")
+    ap.add_argument("--no-other-cells", action="store_true",
+                    help="E/F/S on the headline cell only (not the 1,024- and 128,000-atom cells)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
