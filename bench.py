@@ -65,6 +65,14 @@ MODELS = {
 }
 
 
+# DRAM traffic of pg_rows_pairs per X row, from one ncu capture (binary model,
+# mixed precision, 20 structures, 5,552 rows: dram__bytes_read.sum 0.188 GB +
+# dram__bytes_write.sum 1.275 GB).  The kernel's traffic is the group vectors it
+# writes, which grow with the pair images, in proportion to the rows; the bench
+# line scales it to a launch by the rows the launch processes.
+NCU_ROWS_PAIRS_BYTES_PER_ROW = {"cfg2": 1.463456e9 / 5552}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -371,12 +379,16 @@ def main():
         bytes_ = 2 * F * tb * rows_per_step / dn
         achieved = bytes_ / per_launch_s / 1e9
         sub = 2 * F * tb * rows_per_step / (xrow_ms / 1e3) / 1e9
+        traffic = None
+        if dname == "pg_rows_pairs" and precision == _ffi.PG_MIXED and args.model in NCU_ROWS_PAIRS_BYTES_PER_ROW:
+            traffic = NCU_ROWS_PAIRS_BYTES_PER_ROW[args.model] * rows_per_step / dn / 1e9
         roof = {"kernel": dname, "bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
-                "frac": achieved / hbm_gbs, "traffic": None,
+                "frac": achieved / hbm_gbs, "traffic": traffic, "traffic_unit": "GB per launch",
                 "xrow_subpath": {"kernels": [k for k in row_kernels if k in prof], "ms_per_step": xrow_ms,
                                  "achieved": sub, "frac": sub / hbm_gbs},
                 "note": f"algorithmic bytes = F x {tb} B written + F x {tb} B read per X row (the X tile); "
-                        f"peak {peak_kind} copy bandwidth; DRAM traffic of the kernel from ncu is in profiles/"}
+                        f"peak {peak_kind} copy bandwidth; traffic = ncu DRAM bytes per X row of the kernel "
+                        f"(one ncu capture of 20 structures) x rows per launch"}
     if "pg_gram_tc" in prof and not dname.startswith("pg_gram"):
         gms, gn = prof["pg_gram_tc"]
         g_ach = F * (F + 1) * rows_per_step / (gms / 1e3) / 1e12
