@@ -91,23 +91,14 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.K = ft.K;
         d.K0 = ft.K0;
         d.n_lin = ft.n_lin;
-        d.n_ent = (int)ft.ent_head.size();
-        d.head_tp = (const int*)up(ft.head_tp);
         d.head_nid = (const int*)up(ft.head_nid);
         d.head_key = (const int*)up(ft.head_key);
         d.head_m = (const int*)up(ft.head_m);
-        d.head_full = (const int*)up(ft.head_full);
-        d.head_jloc = (const int*)up(ft.head_jloc);
-        d.head_signj = (const double*)up(ft.head_signj);
         d.full_src = (const int*)up(ft.full_src);
         d.full_is_conj = (const int*)up(ft.full_is_conj);
         d.full_cc = (const double*)up(ft.full_cc);
         d.val_off = (const int*)up(ft.val_off);
         d.val_terms = (const FlatTerm*)up(ft.val_terms);
-        d.ent_off = (const int*)up(ft.ent_off);
-        d.ent_head = (const int*)up(ft.ent_head);
-        d.term_off = (const int*)up(ft.term_off);
-        d.g_terms = (const FlatTerm*)up(ft.g_terms);
         d.col_ncomp = (const int*)up(ft.col_ncomp);
         d.comp_k = (const int*)up(ft.comp_k);
         std::vector<int2> pack(F);
@@ -133,7 +124,6 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.n_prod = (int)prod.size();
         d.lin_col = (const int*)up(lin);
         d.prod_col = (const int*)up(prod);
-        d.ent_tp_off = (const int*)up(ft.ent_tp_off);
         std::vector<int> tnk(ft.tp_heads.size());
         for (int tp = 0; tp < fm.n_tp; ++tp)
             for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q) {
@@ -146,7 +136,6 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.n_groups = ft.n_groups;
         d.lay_size = ft.lay_size;
         d.n_tpl = (int)ft.tpl_tp.size();
-        d.lay_ent = (const int*)up(ft.lay_ent);
         d.lay_hpos = (const int*)up(ft.lay_hpos);
         d.lay_grp_base = (const int*)up(ft.lay_grp_base);
         d.lay_grp_cnt = (const int*)up(ft.lay_grp_cnt);

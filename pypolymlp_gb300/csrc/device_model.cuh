@@ -56,25 +56,21 @@ __device__ inline T term_product_real(const FlatTerm& t, const cplx<T>* a) {
 constexpr int kTermWin = 128;
 
 struct DevType {
-    int K, K0, n_lin, n_ent;
-    const int *head_tp, *head_nid, *head_key, *head_m, *head_full, *head_jloc;
-    const double* head_signj;
+    int K, K0, n_lin;
+    const int *head_nid, *head_key, *head_m;
     const int *full_src, *full_is_conj;
     const double* full_cc;
     const int* val_off;
     const FlatTerm* val_terms;
-    const int *ent_off, *ent_head, *term_off;
-    const FlatTerm* g_terms;
     const int *col_ncomp, *comp_k;
     const int2* col_pack;      // per column: k0 | k1 << 16, k2 | count << 16 (its up to three linear features)
     int n_prod;                // columns that are products of two or three features of this type
     const int *lin_col, *prod_col;  // per feature: its linear column (-1: none); the product columns
-    const int* ent_tp_off;     // per linear feature k: (n_tp + 1) entry offsets by type pair
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
     const int* tp_head_nk;     // per gradient-tile row of a type pair (tp_head_off order): radial index | Y_lm index << 8
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
     int n_groups, lay_size, n_tpl;
-    const int *lay_ent, *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
+    const int *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
     const int* tp_nnz;  // per type pair: feature positions with entries (the first ones)
     // adjoint terms in X-row slot order: slot s owns terms slot_toff[s] ..
     // slot_toff[s + 1]; per term the full a ids (16 bits each, two per word in

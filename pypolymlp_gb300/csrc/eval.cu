@@ -29,7 +29,7 @@ namespace pg {
 
 // Extra per-type device tables of the evaluator.
 struct EvalType {
-    const int *ent_k, *head_ent_off, *head_ent, *tp_head_off, *tp_heads;
+    const int *tp_head_off, *tp_heads;
     const int *kcol_off, *kcol_col, *kcol_o1, *kcol_o2;
     // adjoint terms by head: head h owns terms head_toff[h] .. head_toff[h + 1]
     // (its entries in head_ent order, their terms in order); per term the
@@ -285,9 +285,6 @@ struct Evaluator {
         for (int t = 0; t < m->flat.n_type; ++t) {
             const FlatType& ft = m->flat.types[t];
             EvalType& e = et.types[t];
-            e.ent_k = up(ft.ent_k);
-            e.head_ent_off = up(ft.head_ent_off);
-            e.head_ent = up(ft.head_ent);
             e.tp_head_off = up(ft.tp_head_off);
             e.tp_heads = up(ft.tp_heads);
             e.kcol_off = up(ft.kcol_off);
