@@ -97,6 +97,7 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.full_src = (const int*)up(ft.full_src);
         d.full_is_conj = (const int*)up(ft.full_is_conj);
         d.full_cc = (const double*)up(ft.full_cc);
+        d.full_cc_f = (const float*)up(std::vector<float>(ft.full_cc.begin(), ft.full_cc.end()));
         d.val_off = (const int*)up(ft.val_off);
         d.val_terms = (const FlatTerm*)up(ft.val_terms);
         d.col_ncomp = (const int*)up(ft.col_ncomp);
@@ -465,18 +466,18 @@ void Model::run_rows(DeviceBatch& b, const RowPlan& plan, const long long* d_e_r
     const DeviceModel& dmod = fp64 ? dev64 : dev32;
     b.build_neighbors(flat.cutoff, stream);
     const DevBatch B = b.view(flat.cutoff);
-    s_A.reserve(sizeof(double2) * std::max<long long>(1, plan.a_tot));
+    s_A.reserve(2 * sizeof(T) * std::max<long long>(1, plan.a_tot));
     s_D.reserve(sizeof(T) * std::max<long long>(1, plan.d_tot));
     s_G.reserve(2 * sizeof(T) * std::max<long long>(1, plan.g_tot));
     if (b.n_atoms > 0) {
         {
             ProfScope ps("pg_anlm", stream);
             launch_anlm<T>(dmod.dm, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                           plan.d_a_off.as<long long>(), s_A.as<double2>(), max_k0, stream);
+                           plan.d_a_off.as<long long>(), s_A.as<void>(), max_k0, stream);
         }
         {
             ProfScope ps("pg_features_adjoint", stream);
-            launch_features_adjoint<T>(dmod.dm, B, plan.d_a_off.as<long long>(), s_A.as<double2>(),
+            launch_features_adjoint<T>(dmod.dm, B, plan.d_a_off.as<long long>(), s_A.as<void>(),
                                        plan.d_d_off.as<long long>(), s_D.as<T>(), plan.d_g_off.as<long long>(),
                                        s_G.as<void>(), max_k, stream);
         }

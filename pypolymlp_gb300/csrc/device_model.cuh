@@ -60,6 +60,7 @@ struct DevType {
     const int *head_nid, *head_key, *head_m;
     const int *full_src, *full_is_conj;
     const double* full_cc;
+    const float* full_cc_f;    // FP32 copy of full_cc
     const int* val_off;
     const FlatTerm* val_terms;
     const int *col_ncomp, *comp_k;
@@ -122,6 +123,28 @@ __device__ __forceinline__ cplx<T> packed_term_product(const int4 c4, const cplx
     for (int q = 1; q < 6; ++q)
         if (q < n) p = cmul(p, a[id[q]]);
     return p;
+}
+
+template <typename T>
+__device__ __forceinline__ T full_cc_of(const DevType& ty, int f);
+template <>
+__device__ __forceinline__ double full_cc_of<double>(const DevType& ty, int f) { return ty.full_cc[f]; }
+template <>
+__device__ __forceinline__ float full_cc_of<float>(const DevType& ty, int f) { return ty.full_cc_f[f]; }
+
+// All K a_nlm of a centre (smem a) from its K0 no-conjugate ones (A, in T):
+// a conjugate entry is cc * conj(its source).
+template <typename T>
+__device__ __forceinline__ void load_full_a(const DevType& ty, const cplx<T>* A, cplx<T>* a) {
+    for (int f = threadIdx.x; f < ty.K; f += blockDim.x) {
+        const cplx<T> s = A[ty.full_src[f]];
+        if (ty.full_is_conj[f]) {
+            const T cc = full_cc_of<T>(ty, f);
+            a[f] = {cc * s.re, -cc * s.im};
+        } else {
+            a[f] = s;
+        }
+    }
 }
 
 struct DevModel {
@@ -245,7 +268,6 @@ struct LongSum {
     double v = 0.0;
     __device__ __forceinline__ void add(double x) { v += x; }
     __device__ __forceinline__ double value() const { return v; }
-    __device__ __forceinline__ double value64() const { return v; }
     __device__ __forceinline__ void merge(const LongSum& o) { v += o.v; }
 };
 template <>
@@ -259,7 +281,6 @@ struct LongSum<float> {
         lo = __fadd_rn(lo, e);
     }
     __device__ __forceinline__ float value() const { return __fadd_rn(hi, lo); }
-    __device__ __forceinline__ double value64() const { return (double)hi + (double)lo; }
     __device__ __forceinline__ void merge(const LongSum& o) {
         add(o.hi);
         lo = __fadd_rn(lo, o.lo);

@@ -56,7 +56,7 @@ struct EvalTables {
 // One block per atom.
 template <typename T>
 __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, const long long* a_off,
-                                const double2* Anoconj, const double* coef, cplx<T>* Aout, double* Eatom) {
+                                const cplx<T>* Anoconj, const double* coef, cplx<T>* Aout, double* Eatom) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int i = blockIdx.x;
     const int t1 = types[i];
@@ -66,16 +66,7 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
     T* d = reinterpret_cast<T*>(a + ty.K);
     T* beta = d + ty.n_lin;
     __shared__ double red[32];
-    const double2* Ai = Anoconj + a_off[i];
-    for (int f = threadIdx.x; f < ty.K; f += blockDim.x) {
-        const double2 s = Ai[ty.full_src[f]];
-        if (ty.full_is_conj[f]) {
-            const double cc = ty.full_cc[f];
-            a[f] = {(T)(cc * s.x), (T)(-cc * s.y)};
-        } else {
-            a[f] = {(T)s.x, (T)s.y};
-        }
-    }
+    load_full_a<T>(ty, Anoconj + a_off[i], a);
     __syncthreads();
     constexpr int NW = 8;  // 256 threads
     __shared__ cplx<T> s_v[NW][kTermWin];
@@ -335,7 +326,7 @@ struct Evaluator {
         m->atom_offsets(b, off);
         const long long a_tot = off.a_tot;
         upload(d_aoff, off.a_off);
-        s_Anc.reserve(sizeof(double2) * std::max<long long>(1, a_tot));
+        s_Anc.reserve(2 * sizeof(T) * std::max<long long>(1, a_tot));
         s_Aadj.reserve(2 * sizeof(T) * std::max<long long>(1, a_tot));
         s_E.reserve(sizeof(double) * std::max(1, b.n_atoms));
         s_vir.reserve(sizeof(double) * 6 * std::max(1, b.n_atoms));
@@ -350,7 +341,7 @@ struct Evaluator {
             {
                 ProfScope ps("pg_anlm", stream);
                 launch_anlm<T>(M, B, b.d_nb_off.as<long long>(), b.d_nb_j.as<int>(), b.d_nb_d.as<double>(),
-                               d_aoff.as<long long>(), s_Anc.as<double2>(), m->max_k0, stream);
+                               d_aoff.as<long long>(), s_Anc.as<void>(), m->max_k0, stream);
             }
             int max_lin = 1;
             for (const auto& ft : m->flat.types) max_lin = std::max(max_lin, ft.n_lin);
@@ -359,7 +350,7 @@ struct Evaluator {
             {
                 ProfScope ps("pg_eval_adjoint", stream);
                 pg_eval_adjoint<T><<<b.n_atoms, 256, sm1, stream>>>(M, et, d_types(b), d_aoff.as<long long>(),
-                                                                   s_Anc.as<double2>(), coef.as<double>(),
+                                                                   s_Anc.as<cplx<T>>(), coef.as<double>(),
                                                                    reinterpret_cast<cplx<T>*>(s_Aadj.as<void>()),
                                                                    s_E.as<double>());
             }

@@ -77,9 +77,9 @@ void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* 
                     bool any_cl, cudaStream_t st);
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                 const long long* a_off, double2* A, int max_k0, cudaStream_t st);
+                 const long long* a_off, void* A, int max_k0, cudaStream_t st);
 template <typename T>
-void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
+void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const void* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);

@@ -272,7 +272,7 @@ __global__ void pg_nb_order(DevBatch B, const long long* offsets, const long lon
 // the chunk in T, added to the FP64 total once per chunk.
 template <typename T>
 __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j,
-                                               const double* nb_d, const long long* a_off, double2* A) {
+                                               const double* nb_d, const long long* a_off, cplx<T>* A) {
     constexpr int NW = 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_list[256], s_wcnt[NW], s_ok[NW];
@@ -346,30 +346,20 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
             }
         }
     }
-    double2* out = A + a_off[i];
-    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x)
-        out[h] = make_double2(acc[2 * h].value64(), acc[2 * h + 1].value64());
+    cplx<T>* out = A + a_off[i];
+    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) out[h] = {acc[2 * h].value(), acc[2 * h + 1].value()};
 }
 
 // ----------------------------------------------- K4 features and adjoint G
 template <typename T>
-__global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_off, const double2* A,
+__global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_off, const cplx<T>* A,
                                     const long long* d_off, T* D, const long long* g_off, cplx<T>* G) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int i = blockIdx.x;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
     cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw);
-    const double2* Ai = A + a_off[i];
-    for (int f = threadIdx.x; f < ty.K; f += blockDim.x) {
-        const double2 s = Ai[ty.full_src[f]];
-        if (ty.full_is_conj[f]) {
-            const double cc = ty.full_cc[f];
-            a[f] = {(T)(cc * s.x), (T)(-cc * s.y)};
-        } else {
-            a[f] = {(T)s.x, (T)s.y};
-        }
-    }
+    load_full_a<T>(ty, A + a_off[i], a);
     __syncthreads();
     // windowed warp sums (see kTermWin): feature values, then adjoint entries
     constexpr int NW = 8, kWin = kTermWin;
@@ -1057,22 +1047,22 @@ void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* 
 
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
-                 const long long* a_off, double2* A, int max_k0, cudaStream_t st) {
+                 const long long* a_off, void* A, int max_k0, cudaStream_t st) {
     const int threads = 256, nw = threads / 32;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
     const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) +
                         ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
     PG_CUDA(cudaFuncSetAttribute(pg_anlm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pg_anlm<T><<<B.n_atoms, threads, smem, st>>>(M, B, nb_off, nb_j, nb_d, a_off, A);
+    pg_anlm<T><<<B.n_atoms, threads, smem, st>>>(M, B, nb_off, nb_j, nb_d, a_off, reinterpret_cast<cplx<T>*>(A));
 }
 
 template <typename T>
-void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const double2* A,
+void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const void* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st) {
     const size_t smem = (size_t)max_k * sizeof(cplx<T>);
     PG_CUDA(cudaFuncSetAttribute(pg_features_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pg_features_adjoint<T><<<B.n_atoms, 256, smem, st>>>(M, B, a_off, A, d_off, D, g_off,
+    pg_features_adjoint<T><<<B.n_atoms, 256, smem, st>>>(M, B, a_off, reinterpret_cast<const cplx<T>*>(A), d_off, D, g_off,
                                                          reinterpret_cast<cplx<T>*>(G));
 }
 
@@ -1118,13 +1108,13 @@ void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off
 }
 
 template void launch_anlm<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
-                                  const long long*, double2*, int, cudaStream_t);
+                                  const long long*, void*, int, cudaStream_t);
 template void launch_anlm<float>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
-                                 const long long*, double2*, int, cudaStream_t);
-template void launch_features_adjoint<double>(const DevModel&, const DevBatch&, const long long*, const double2*,
+                                 const long long*, void*, int, cudaStream_t);
+template void launch_features_adjoint<double>(const DevModel&, const DevBatch&, const long long*, const void*,
                                               const long long*, double*, const long long*, void*, int,
                                               cudaStream_t);
-template void launch_features_adjoint<float>(const DevModel&, const DevBatch&, const long long*, const double2*,
+template void launch_features_adjoint<float>(const DevModel&, const DevBatch&, const long long*, const void*,
                                              const long long*, float*, const long long*, void*, int, cudaStream_t);
 template void launch_rows_pairs<double>(const DevModel&, const DevBatch&, const long long*, const int*,
                                         const double*, const long long*, const long long*, const long long*,
