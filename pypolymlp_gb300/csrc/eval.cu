@@ -30,6 +30,7 @@ namespace pg {
 // Extra per-type device tables of the evaluator.
 struct EvalType {
     const int *tp_head_off, *tp_heads;
+    const int* tp_head_nk;  // per tp_heads entry: radial index | Y_lm index << 8
     const int *kcol_off, *kcol_col, *kcol_o1, *kcol_o2;
     // adjoint terms by head: head h owns terms head_toff[h] .. head_toff[h + 1]
     // (its entries in head_ent order, their terms in order); per term the
@@ -153,7 +154,8 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
     T* sb = reinterpret_cast<T*>(
         (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));
     const cplx<T>* Ai = Aadj + a_off[i];
-    for (int h = threadIdx.x; h < ty.K0; h += blockDim.x) A[h] = Ai[h];
+    // the adjoint in type-pair head order (tp_heads), read by consecutive lanes below
+    for (int q = threadIdx.x; q < ty.K0; q += blockDim.x) A[q] = Ai[et.tp_heads[q]];
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     __syncthreads();
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
@@ -174,9 +176,9 @@ __global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long 
             __syncwarp();
             T s0 = 0, sx = 0, sy = 0, sz = 0;
             for (int q = et.tp_head_off[tp] + lane; q < et.tp_head_off[tp + 1]; q += 32) {
-                const int h = et.tp_heads[q];
-                const int nid = ty.head_nid[h], key = ty.head_key[h];
-                const cplx<T> g = A[h];
+                const int nk = et.tp_head_nk[q];
+                const int nid = nk & 0xff, key = nk >> 8;
+                const cplx<T> g = A[q];
                 const T f = bv.fn[nid];
                 s0 += bv.fnd[nid] * creal_mul(g, bv.Y[key]);
                 sx += f * creal_mul(g, bv.dY[key]);
@@ -278,6 +280,15 @@ struct Evaluator {
             EvalType& e = et.types[t];
             e.tp_head_off = up(ft.tp_head_off);
             e.tp_heads = up(ft.tp_heads);
+            if ((int)ft.tp_heads.size() != ft.K0) throw std::runtime_error("internal: heads without a type pair");
+            std::vector<int> nk(ft.tp_heads.size());
+            for (size_t q = 0; q < nk.size(); ++q) {
+                const int h = ft.tp_heads[q];
+                if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
+                    throw std::runtime_error("model too large for the packed head indices");
+                nk[q] = ft.head_nid[h] | (ft.head_key[h] << 8);
+            }
+            e.tp_head_nk = up(nk);
             e.kcol_off = up(ft.kcol_off);
             e.kcol_col = up(ft.kcol_col);
             e.kcol_o1 = up(ft.kcol_o1);
