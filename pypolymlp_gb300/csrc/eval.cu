@@ -57,7 +57,7 @@ struct EvalTables {
 // One block per atom.
 template <typename T>
 __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, const long long* a_off,
-                                const cplx<T>* Anoconj, const double* coef, cplx<T>* Aout, double* Eatom) {
+                                const cplx<T>* Anoconj, const T* coef, cplx<T>* Aout, double* Eatom) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int i = blockIdx.x;
     const int t1 = types[i];
@@ -78,7 +78,7 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
     for (int k = threadIdx.x; k < ty.n_lin; k += blockDim.x) {
         T b = 0;
         for (int q = et.kcol_off[k]; q < et.kcol_off[k + 1]; ++q) {
-            T w = (T)coef[et.kcol_col[q]];
+            T w = coef[et.kcol_col[q]];
             const int o1 = et.kcol_o1[q], o2 = et.kcol_o2[q];
             if (o1 >= 0) w *= d[o1];
             if (o2 >= 0) w *= d[o2];
@@ -86,15 +86,16 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
         }
         beta[k] = b;
     }
-    // E_i = sum over columns of coef * polynomial value (FP64 block sum)
-    double e = 0.0;
+    // E_i = sum over columns of coef * polynomial value (long sums per thread, FP64 block sum)
+    LongSum<T> ls;
     for (int col = threadIdx.x; col < M.F; col += blockDim.x) {
         const int nc = ty.col_ncomp[col];
         if (nc == 0) continue;
         T p = (T)1;
         for (int c = 0; c < nc; ++c) p *= d[ty.comp_k[col * 3 + c]];
-        e += coef[col] * (double)p;
+        ls.add(coef[col] * p);
     }
+    double e = (double)ls.value();
     for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
     __syncthreads();
@@ -259,7 +260,7 @@ __global__ void pg_eval_reduce(const int* st_atom_off, const double* Eatom, cons
 struct Evaluator {
     std::unique_ptr<Model> m;
     int precision;
-    DevBuf coef;
+    DevBuf coef, coef32;  // the coefficients in FP64 and FP32
     std::vector<DevBuf> bufs;
     EvalTables et{};
     DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_vir, s_g, s_mirror, s_missing, d_E, d_S, d_F;
@@ -269,6 +270,7 @@ struct Evaluator {
         m = std::make_unique<Model>(fp);
         if (n != m->flat.n_features) throw std::runtime_error("coefficient count does not match the model");
         upload(coef, std::vector<double>(coeffs, coeffs + n));
+        upload(coef32, std::vector<float>(coeffs, coeffs + n));
         bufs.reserve(32 * kMaxTypes);
         auto up = [&](const std::vector<int>& v) -> const int* {
             bufs.emplace_back();
@@ -361,7 +363,8 @@ struct Evaluator {
             {
                 ProfScope ps("pg_eval_adjoint", stream);
                 pg_eval_adjoint<T><<<b.n_atoms, 256, sm1, stream>>>(M, et, d_types(b), d_aoff.as<long long>(),
-                                                                   s_Anc.as<cplx<T>>(), coef.as<double>(),
+                                                                   s_Anc.as<cplx<T>>(),
+                                                                   (sizeof(T) == 8 ? coef : coef32).template as<T>(),
                                                                    reinterpret_cast<cplx<T>*>(s_Aadj.as<void>()),
                                                                    s_E.as<double>());
             }
