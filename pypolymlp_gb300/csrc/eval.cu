@@ -5,7 +5,8 @@
 // The reference already evaluates by an adjoint: per atom it forms
 // prod_sum = dE_i/da_nlm (polymlp_potential.cpp:235-295) and contracts it with
 // da/dr per half-list pair.  Here, per atom i (full neighbour list):
-//   pg_anlm            a_nlm (m <= 0), FP64 neighbour sums           (xrows.cu)
+//   pg_anlm            a_nlm (m <= 0), long neighbour sums (FP64, or float-float
+//                      in the FP32 kernel)                             (xrows.cu)
 //   pg_eval_adjoint    features d, beta_k = dE_i/dd_k from the polynomial with
 //                      the coefficients, E_i, and the folded adjoint
 //                      A_i[h] = sum_e beta_k(e) G_e (no G stored)

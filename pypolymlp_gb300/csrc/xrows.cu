@@ -718,11 +718,14 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
 // that type with images on j (the runs of j's list; their group vectors sit
 // at the runs' first slots, by feature position), and a product column
 // d_a d_b (d_c) receives -sum_i (d_b dd_a + d_a dd_b ...) with centre i's
-// features as weights.  The linear part is a coalesced column sum of the
-// group vectors (each thread owns S positions per slab); the product columns
-// (a few hundred) are gathered per column.  The self rows add the centre's DS
-// vectors to its own type's columns.  Every X element has one owner thread
-// per type, and types are taken in order, so the sums are deterministic.
+// features as weights.  The groups of one centre type are listed in shared
+// memory first; the linear part is a coalesced column sum of their vectors
+// over the positions with entries (each thread owns S positions per slab);
+// the product columns (a few hundred, thread per column) are gathered in the
+// same pass over the groups when one slab covers the positions, else in a
+// pass of their own.  The self rows add the centre's DS vectors to its own
+// type's columns.  Every X element has one owner thread per type, and types
+// are taken in order, so the sums are deterministic.
 __device__ __forceinline__ void unpack_col(int2 c, int& k0, int& k1, int& k2, int& w) {
     k0 = c.x & 0xffff;
     k1 = (c.x >> 16) & 0xffff;
