@@ -155,3 +155,30 @@ def feature_attrs(params_dict):
     tcomb = [list(tcv[tco[i]:tco[i + 1]]) for i in range(nl.value)]
     poly = [list(pv[po[i]:po[i + 1]]) for i in range(npoly.value)]
     return rad[:nl.value].tolist(), gt[:nl.value].tolist(), tcomb, poly
+
+
+def parse_potential(path: str, legacy: bool = False) -> dict:
+    """A model file read by the reference's own C++ parsers (ref_parse_potential):
+    {elements, cutoff, pair_type, feature_type, model_type, max_p, max_l,
+    n_l_comb, params (n x 2), cond {(i, j): ids}, coeffs (2 x the file's), mass}."""
+    lib = _load()
+    buf = C.create_string_buffer(1 << 24)
+    _check(lib.ref_parse_potential(path.encode(), 1 if legacy else 0, buf, C.c_size_t(1 << 24)))
+    out = {"cond": {}}
+    for line in buf.value.decode().splitlines():
+        key, *vals = line.split()
+        if key == "cond":
+            out["cond"][(int(vals[0]), int(vals[1]))] = [int(v) for v in vals[2:]]
+        elif key == "elements":
+            out[key] = vals
+        elif key in ("pair_type", "feature_type"):
+            out[key] = vals[0]
+        elif key in ("model_type", "max_p", "max_l", "n_l_comb"):
+            out[key] = int(vals[0])
+        elif key == "cutoff":
+            out[key] = float(vals[0])
+        elif key == "params":
+            out[key] = np.array([float(v) for v in vals]).reshape(-1, 2)
+        else:
+            out[key] = np.array([float(v) for v in vals])
+    return out

@@ -14,7 +14,11 @@
 #include "compute/neighbor_full.h"
 #include "compute/neighbor_half.h"
 #include "compute/polymlp_eval.h"
+#include <sstream>
+
 #include "polymlp/polymlp_api.h"
+#include "polymlp/polymlp_parse_potential.h"
+#include "polymlp/polymlp_parse_potential_legacy.h"
 #include "polymlp/polymlp_read_gtinv.h"
 #include "polymlp_gb300.h"
 
@@ -301,6 +305,48 @@ int ref_feature_attrs(const pg_feature_params* p, int* n_linear, int* radial_ids
             for (int v : poly[i]) poly_values[k++] = v;
             poly_offsets[i + 1] = k;
         }
+    });
+}
+
+// A polymlp.yaml (legacy = 0) or polymlp.lammps (legacy = 1) file read by the
+// reference's own parsers (polymlp/polymlp_parse_potential.cpp:214-257,
+// polymlp/polymlp_parse_potential_legacy.cpp), summarised as text lines
+// "key v1 v2 ..." in buf: elements, cutoff, pair_type, feature_type,
+// model_type, max_p, max_l, n_l_comb (the invariant tables it derived),
+// params (pairs of Gaussian parameters), cond i j ids... per type pair,
+// coeffs (as the parser returns them: 2 x the file's values), mass.
+int ref_parse_potential(const char* file, int legacy, char* buf, size_t len) {
+    return guarded([&] {
+        feature_params fp;
+        vector1d coeffs, mass;
+        std::vector<std::string> ele;
+        if (legacy)
+            parse_polymlp_legacy(file, fp, coeffs, ele, mass);
+        else
+            parse_polymlp(file, fp, coeffs, ele, mass);
+        std::ostringstream o;
+        o.precision(17);
+        o << "elements";
+        for (const auto& e : ele) o << " " << e;
+        o << "\ncutoff " << fp.cutoff << "\npair_type " << fp.pair_type << "\nfeature_type " << fp.feature_type
+          << "\nmodel_type " << fp.model_type << "\nmax_p " << fp.maxp << "\nmax_l " << fp.maxl
+          << "\nn_l_comb " << fp.l_comb.size() << "\nparams";
+        for (const auto& p : fp.params) o << " " << p[0] << " " << p[1];
+        o << "\n";
+        for (size_t i = 0; i < fp.params_conditional.size(); ++i)
+            for (size_t j = i; j < fp.params_conditional[i].size(); ++j) {
+                o << "cond " << i << " " << j;
+                for (int v : fp.params_conditional[i][j]) o << " " << v;
+                o << "\n";
+            }
+        o << "coeffs";
+        for (double c : coeffs) o << " " << c;
+        o << "\nmass";
+        for (double m : mass) o << " " << m;
+        o << "\n";
+        const std::string t = o.str();
+        if (t.size() + 1 > len) throw std::runtime_error("summary buffer too small");
+        std::memcpy(buf, t.c_str(), t.size() + 1);
     });
 }
 
