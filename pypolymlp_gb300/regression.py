@@ -429,6 +429,122 @@ class FitResult:
         return self.coeffs / self.scales
 
 
+def _assemble(model: _ffi.Model, train: Sequence[Dataset], precision: int, weight_stress: float,
+              scales=None, min_energy=None, zero_ids=None):
+    """Training batches on the device, their Gram (one pass) and the scaled
+    normal equations: (batches, gram, xtx, xty, scales, zero_ids, min_energy)."""
+    min_e = get_min_energy(train) if min_energy is None else min_energy
+    tb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in train]
+    gram = GramAccumulator(model, precision)
+    for b in tb:
+        gram.accumulate_batch(b)
+    xtx, xty, yty, xe_sum, xe_sq, n_rows = gram.result()
+    n_data = sum(len(d.energies) for d in train)
+    scales, zids = compute_scales(scales, xe_sum, xe_sq, n_data, any(d.include_force for d in train))
+    zero_ids = zids if zero_ids is None else zero_ids
+    xtx[zero_ids] = 0.0
+    xtx[:, zero_ids] = 0.0
+    xty[zero_ids] = 0.0
+    xtx /= scales[:, None]
+    xtx /= scales[None, :]
+    xty /= scales
+    return tb, gram, xtx, xty, scales, zero_ids, min_e
+
+
+def _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info, n_iter, shifts):
+    """Residual RMSEs on the training and test batches and the best alpha (FitResult)."""
+    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
+    rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
+    if np.all(rmse_train > 1e6):
+        raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
+                           "This singularity issue might be reduced by increasing "
+                           "the value of alpha (the magnitude of the penalty term).")
+    vb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in test]
+    _, sq, n_te = batch_residual(gram, vb, coefs / scales[:, None])
+    rmse_test = np.sqrt(sq.sum(axis=0) / n_te)
+    idx = int(np.argmin(rmse_test))
+    return FitResult(coefs[:, idx], scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
+                     coefs, rmse_train, rmse_test, info, n_iter, shifts)
+
+
+def solver_cg(xtx: np.ndarray, xty: np.ndarray, alpha: float = 1e-3, coef0: Optional[np.ndarray] = None,
+              gtol: float = 1e-2, max_iter: int = 10000):
+    """Conjugate gradients on (X^T X + alpha I) c = X^T y as solvers_cg.py:33-100
+    runs them: start at coef0 (or 0), stop after more than 100 iterations once
+    |r| / sqrt(F) < gtol, or after max_iter.  Returns (c, iterations); c is the
+    last iterate, which is what the reference returns (its kept "best" array is
+    the running iterate itself, updated in place)."""
+    F = xtx.shape[1]
+    c = np.zeros(F) if coef0 is None else np.array(coef0, dtype=np.float64)
+    r = xty - (xtx @ c + alpha * c)
+    d = r.copy()
+    rn = float(np.linalg.norm(r))
+    it = 0
+    for it in range(max_iter):
+        if it > 100 and rn / np.sqrt(F) < gtol:
+            break
+        t = xtx @ d + alpha * d
+        lr = rn * rn / float(t @ d)
+        c += lr * d
+        r -= lr * t
+        rn_new = float(np.linalg.norm(r))
+        d = r + (rn_new * rn_new) / (rn * rn) * d
+        rn = rn_new
+    return c, it
+
+
+def fit_cg(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
+           gtol: float = 1e-2, max_iter: Optional[int] = None, precision: int = _ffi.PG_FP64,
+           model: Optional[_ffi.Model] = None, weight_stress: float = 0.1) -> FitResult:
+    """GPU counterpart of fit_cg (src/pypolymlp/mlp_dev/gradient/fit_cg.py:23-80):
+    the Gram from the GPU, then conjugate gradients (`solver_cg`) for the alphas
+    from the largest down, each started at the previous solution; model
+    selection as `fit`."""
+    model = model or _ffi.Model(params_dict)
+    alphas = np.asarray(alphas, dtype=np.float64)
+    tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
+    if max_iter is None:
+        max_iter = max(model.n_features * 3, 50000)
+    coefs, c0, n_iter = np.zeros((len(xty), len(alphas))), None, 0
+    for k in reversed(range(len(alphas))):
+        c0, it = solver_cg(xtx, xty, float(alphas[k]), c0, gtol, max_iter)
+        coefs[:, k] = c0
+        n_iter += it
+    return _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress,
+                   np.zeros(len(alphas), dtype=np.int32), n_iter, np.zeros(len(alphas)))
+
+
+def fit_learning_curve(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset],
+                       alphas: Sequence[float], precision: int = _ffi.PG_FP64, weight_stress: float = 0.1):
+    """GPU counterpart of fit_learning_curve (src/pypolymlp/mlp_dev/standard/fit.py:115-179):
+    ridge fits on the first n structures of the single training dataset, n =
+    n_train // 10, 2 n_train // 10, ..., with the scales and the reference
+    energy of the whole training set; after each, the best model's errors on
+    every test dataset (`accuracy.PolymlpEvalAccuracy`).  Returns
+    [[n, error dict], ...] in that order."""
+    from pypolymlp_gb300.accuracy import PolymlpEvalAccuracy
+
+    if len(train) != 1:
+        raise RuntimeError("Number of training datasets must be one for learning curve.")
+    model = _ffi.Model(params_dict)
+    full = train[0]
+    _, _, _, _, scales, zero_ids, min_e = _assemble(model, [full], precision, weight_stress)
+    n_train = len(full)
+    step = max(n_train // 10, 1)
+    log = []
+    for n in range(step, n_train + 1, step):
+        sub = full.slice(0, n)
+        tb, gram, xtx, xty, sc, _, _ = _assemble(model, [sub], precision, weight_stress, scales=scales,
+                                                 min_energy=min_e, zero_ids=zero_ids)
+        coefs, info = solver_ridge(xtx, xty, alphas)
+        best = _select(model, gram, tb, test, coefs, sc, np.asarray(alphas, dtype=np.float64), min_e, precision,
+                       weight_stress, info, 0, np.zeros(len(alphas)))
+        acc = PolymlpEvalAccuracy(params_dict, best.scaled_coeffs, precision=precision)
+        for d in test:
+            log.append([n, acc.compute_error_single(d, log_energy=False)])
+    return log
+
+
 def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
         precision: int = _ffi.PG_MIXED, model: Optional[_ffi.Model] = None, refine: Optional[int] = None,
         weight_stress: float = 0.1) -> FitResult:
@@ -445,20 +561,7 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
     if refine is None:
         refine = 60 if precision == _ffi.PG_MIXED else 0
     alphas = np.asarray(alphas, dtype=np.float64)
-    min_e = get_min_energy(train)
-    tb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in train]
-    gram = GramAccumulator(model, precision)
-    for b in tb:
-        gram.accumulate_batch(b)
-    xtx, xty, yty, xe_sum, xe_sq, n_rows = gram.result()
-    n_data = sum(len(d.energies) for d in train)
-    scales, zero_ids = compute_scales(None, xe_sum, xe_sq, n_data, any(d.include_force for d in train))
-    xtx[zero_ids] = 0.0
-    xtx[:, zero_ids] = 0.0
-    xty[zero_ids] = 0.0
-    xtx /= scales[:, None]
-    xtx /= scales[None, :]
-    xty /= scales
+    tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
     n_iter, shifts = 0, np.zeros(len(alphas))
     if precision == _ffi.PG_FP64 and not refine:
         coefs, info = solver_ridge(xtx, xty, alphas)
@@ -470,15 +573,5 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
 
         coefs, n_iter, shifts = ridge_pcg(xtx, xty, alphas, matvec, zero_ids, max_iter=max(1, refine))
         info = np.zeros(len(alphas), dtype=np.int32)
-    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
-    rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
-    if np.all(rmse_train > 1e6):
-        raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
-                           "This singularity issue might be reduced by increasing "
-                           "the value of alpha (the magnitude of the penalty term).")
-    vb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in test]
-    _, sq, n_te = batch_residual(gram, vb, coefs / scales[:, None])
-    rmse_test = np.sqrt(sq.sum(axis=0) / n_te)
-    idx = int(np.argmin(rmse_test))
-    return FitResult(coefs[:, idx], scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
-                     coefs, rmse_train, rmse_test, info, n_iter, shifts)
+    return _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info, n_iter,
+                   shifts)

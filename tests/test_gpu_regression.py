@@ -124,3 +124,33 @@ def test_fit_mixed_vs_fp64_rmse():
           f"; cg iterations {r32.cg_iterations}, shifts {r32.shifts}")
     assert abs(e32 - e64) < 0.05e-3, (e32, e64)
     assert abs(f32 - f64) < 1e-3, (f32, f64)
+
+
+def test_fit_cg_matches_direct_solve():
+    """fit_cg (GPU Gram, conjugate gradients from the largest alpha down, warm
+    started) reaches the direct FP64 ridge solution: test RMSEs to 1e-4 (the
+    solver stops on an absolute residual, so the smallest alpha, the worst
+    conditioned, is the least exact: 5e-6 relative at gtol 1e-9)."""
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.regression import fit, fit_cg
+
+    p = _params()
+    train, test = _datasets(30, seed=9)
+    alphas = [1e-3, 1e-2, 1e-1]
+    direct = fit(p, train, test, alphas, precision=_ffi.PG_FP64)
+    cg = fit_cg(p, train, test, alphas, gtol=1e-9, max_iter=20000, precision=_ffi.PG_FP64)
+    np.testing.assert_allclose(cg.rmse_test_array, direct.rmse_test_array, rtol=1e-4)
+    assert cg.alpha == direct.alpha and cg.cg_iterations > 0
+
+
+def test_learning_curve():
+    """fit_learning_curve: ten fits on growing prefixes of the training set, the
+    test errors of each from the GPU evaluator."""
+    from pypolymlp_gb300.regression import fit_learning_curve
+
+    p = _params()
+    train, test = _datasets(25, seed=10)
+    log = fit_learning_curve(p, train, test, [1e-3, 1e-2])
+    assert [n for n, _ in log] == list(range(2, 21, 2))
+    for _, err in log:
+        assert np.isfinite(err["energy"]) and np.isfinite(err["force"]) and err["energy"] < 1.0
