@@ -106,7 +106,9 @@ def save_mlp_yaml(params_dict: dict, coeffs, scales, filename: str = "polymlp.ya
     lines += ["", f"n_type_pairs: {len(pairs)}", "type_pairs:"]
     for (i, j), ids in pairs:
         lines += [f"- atom_type_pair:      {_fmt_list([i, j])}", f"  pair_params_indices: {_fmt_list(ids)}"]
-    lines += ["", "type_full:    1", f"type_indices: {_fmt_list(list(range(n_type)))}", "",
+    tfull = 1 if params_dict.get("type_full", True) in (True, 1, None) else 0
+    tidx = [int(v) for v in params_dict.get("type_indices", list(range(n_type)))]
+    lines += ["", f"type_full:    {tfull}", f"type_indices: {_fmt_list(tidx)}", "",
               f"n_coeffs: {len(c)}", "coeffs: [" + ", ".join(f"{v:.15e}" for v in c) + "]"]
     with open(filename, "w") as f:
         f.write("\n".join(lines) + "\n")
@@ -137,7 +139,9 @@ def save_mlp_lammps(params_dict: dict, coeffs, scales, filename: str = "polymlp.
     lines += [f"{len(pairs)} # n_type_pairs"]
     for (i, j), ids in pairs:
         lines += [f"{i} {j} {len(ids)} # atom type pair", " ".join(map(str, ids)) + " # pair params indices"]
-    lines += ["1 # type_full", " ".join(str(i) for i in range(n_type)) + " # type_indices"]
+    tfull = 1 if params_dict.get("type_full", True) in (True, 1, None) else 0
+    tidx = [int(v) for v in params_dict.get("type_indices", list(range(n_type)))]
+    lines += [f"{tfull} # type_full", " ".join(map(str, tidx)) + " # type_indices"]
     with open(filename, "w") as f:
         f.write("\n".join(lines) + "\n")
 
@@ -233,6 +237,8 @@ def load_mlp_yaml(filename: str = "polymlp.yaml"):
                           gtinv_maxl=y.get("gtinv_maxl", []) if gt else [],
                           gtinv_version=y.get("gtinv_version", 1) if gt else 1, pair_type=y.get("pair_type", "gaussian"))
     p["mass"] = [float(v) for v in y.get("mass", [])]
+    p["type_full"] = bool(y.get("type_full", 1))
+    p["type_indices"] = [int(v) for v in y.get("type_indices", list(range(len(elements))))]
     return p, np.asarray(y["coeffs"], dtype=np.float64)
 
 
@@ -283,10 +289,16 @@ def load_mlp_lammps(filename: str = "polymlp.lammps"):
         for i in range(n_type):
             for j in range(i, n_type):
                 cond[(i, j)] = list(range(n_params))
+    type_full, type_indices = True, list(range(n_type))
+    if tagged("type_full"):
+        type_full = values(lambda t: t.lower() in ("1", "true", "t", "yes", "y", "on"))[0]
+        type_indices = values(int)
     p = params_from_model(n_type, elements, cutoff, model_type, max_p, max_l, feature_type, pair_params, cond,
                           gtinv_order=gtinv_order, gtinv_maxl=gtinv_maxl, gtinv_version=version,
                           pair_type=pair_type)
     p["mass"] = [float(v) for v in mass]
+    p["type_full"] = type_full
+    p["type_indices"] = type_indices
     return p, coeffs / scales
 
 

@@ -1,19 +1,19 @@
-"""Known-answer fixtures from the reference's own tests.
+"""Known-answer fixtures from the reference's own property tests.
 
 Run where the reference tree is available (it reads /root/reference):
 
     python tests/golden/make_known_answers.py
 
-The reference's test_calc/test_properties_MgO.py evaluates two shipped
-potentials (tests/test_calc/files/mlps/polymlp.yaml.pair.MgO and
-polymlp.yaml.gtinv.MgO) on the displaced rocksalt cell
-tests/test_calc/files/poscars/POSCAR.RS.MgO and asserts energy, forces and
-stresses (GPa) at fixed values (test_eval1, test_eval2).  This script copies
-those three data files into tests/golden/known_answers/, takes the asserted
-values from the test source (the literal assignments energy_true, forces_true,
-stresses_true of each test function, read with `ast`, not executed) into
-known_answers.json, and writes the invariant tables the gtinv potential needs
-(order 3, l_max (4, 4)) with the reference's Readgtinv (oracle/_ref).
+The reference's tests/test_calc/test_properties_*.py evaluate potentials
+shipped with its tests on small cells and assert energies, forces and
+stresses at fixed values.  For the cases listed in CASES this script copies
+the potential files and POSCARs into tests/golden/known_answers/ and takes the
+asserted values from the test source (literal assignments such as
+`energy_true = ...`, or the literal of the energy's `pytest.approx(...)`, read
+with `ast`, never executed) into known_answers.json, together with the
+comparison each test makes (forces (N, 3) or only forces[0][0]; stresses in
+GPa or eV per cell; tolerances).  It also writes the invariant tables the
+gtinv potentials need with the reference's Readgtinv (oracle/_ref).
 """
 
 import ast
@@ -26,56 +26,119 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-REF_TESTS = "/root/reference/tests/test_calc"
+REF = "/root/reference/tests/test_calc"
 OUT = os.path.join(HERE, "known_answers")
-FILES = {
-    "polymlp.yaml.pair.MgO": "files/mlps/polymlp.yaml.pair.MgO",
-    "polymlp.yaml.gtinv.MgO": "files/mlps/polymlp.yaml.gtinv.MgO",
-    "POSCAR.RS.MgO": "files/poscars/POSCAR.RS.MgO",
+
+# id: (test file, function, potentials, POSCAR, forces layout, stress unit)
+#   forces: "NxT" forces_true is (N, 3) (the test compares forces.T), "3xN" it is
+#   (3, N), "f00" only forces[0][0] == 0 is asserted
+CASES = {
+    "MgO_pair_yaml": ("test_properties_MgO.py", "test_eval1", ["polymlp.yaml.pair.MgO"], "POSCAR.RS.MgO", "NxT", "GPa"),
+    "MgO_gtinv_yaml": ("test_properties_MgO.py", "test_eval2", ["polymlp.yaml.gtinv.MgO"], "POSCAR.RS.MgO", "NxT",
+                       "GPa"),
+    "MgO_pair_legacy": ("test_properties_legacy_MgO.py", "test_eval1", ["polymlp.lammps.pair.MgO"], "POSCAR.RS.MgO",
+                        "NxT", "GPa"),
+    "Ag_pair_legacy": ("test_properties_legacy_Ag.py", "test_eval1", ["polymlp.lammps.pair.Ag"], "POSCAR.fcc.Ag",
+                       "3xN", "eV"),
+    "SrTiO3_pair_legacy": ("test_properties_legacy_SrTiO3.py", "test_eval1", ["polymlp.lammps.pair.SrTiO3"],
+                           "POSCAR.perovskite.SrTiO3", "f00", "GPa"),
+    "SrTiO3_pair_cond_legacy": ("test_properties_legacy_SrTiO3.py", "test_eval2_cond",
+                                ["polymlp.lammps.pair.cond.SrTiO3"], "POSCAR.perovskite.SrTiO3", "f00", "GPa"),
+    "SrTiO3_gtinv_cond_yaml": ("test_properties_SrTiO3.py", "test_eval_cond", ["polymlp.yaml.gtinv.cond.SrTiO3"],
+                               "POSCAR.perovskite.SrTiO3", "f00", "GPa"),
+    "SrTiO3_hybrid_yaml": ("test_properties_SrTiO3.py", "test_eval_flexible",
+                           ["polymlp.yaml.flexible.1.SrTiO3", "polymlp.yaml.flexible.2.SrTiO3"],
+                           "POSCAR.perovskite.SrTiO3", "f00", None),
 }
-# reference test function -> (potential, structure)
-CASES = {"test_eval1": ("polymlp.yaml.pair.MgO", "POSCAR.RS.MgO"),
-         "test_eval2": ("polymlp.yaml.gtinv.MgO", "POSCAR.RS.MgO")}
 
 
-def asserted_values(path):
+def _function(path, name):
     tree = ast.parse(open(path).read())
-    out = {}
     for fn in tree.body:
-        if not isinstance(fn, ast.FunctionDef) or fn.name not in CASES:
-            continue
-        vals = {}
-        for node in ast.walk(fn):
-            if isinstance(node, ast.Assign) and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name):
-                name = node.targets[0].id
-                if name in ("energy_true", "forces_true", "stresses_true"):
-                    vals[name] = ast.literal_eval(node.value)
-        pot, poscar = CASES[fn.name]
-        out[fn.name] = {"potential": pot, "structure": poscar, "energy": vals["energy_true"],
-                        "forces": vals["forces_true"], "stresses_gpa": vals["stresses_true"],
-                        "tolerances": {"energy_rel": 1e-8, "forces_abs": 1e-6, "stresses_gpa_abs": 1e-5}}
-    return out
+        if isinstance(fn, ast.FunctionDef) and fn.name == name:
+            return fn
+    raise KeyError(name)
+
+
+def _assigned(fn, name):
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Assign) and len(node.targets) == 1 and isinstance(node.targets[0], ast.Name) \
+                and node.targets[0].id == name:
+            return ast.literal_eval(node.value)
+    return None
+
+
+def _energy_approx(fn):
+    """(value or None, tolerance kwargs) of `energy == pytest.approx(x, rel=.. | abs=..)`."""
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Compare) and isinstance(node.left, ast.Name) and node.left.id == "energy":
+            call = node.comparators[0]
+            if isinstance(call, ast.Call) and getattr(call.func, "attr", "") == "approx":
+                kw = {k.arg: ast.literal_eval(k.value) for k in call.keywords}
+                try:
+                    val = ast.literal_eval(call.args[0])
+                except ValueError:
+                    val = None
+                return val, kw
+    raise KeyError("energy approx")
+
+
+def gtinv_spec(path):
+    """(order, maxl) of a gtinv potential file, None for a pair potential."""
+    lines = open(path).read().splitlines()
+    if "# ele" in lines[0]:
+        vals = [ln.split("#")[0].split() for ln in lines]
+        if vals[3][0] != "gtinv":
+            return None
+        order = int(vals[7][0])
+        return order, tuple(int(v) for v in vals[8][: order - 1])
+    kv = {ln.split(":", 1)[0].strip(): ln.split(":", 1)[1].strip() for ln in lines if ":" in ln and
+          not ln.startswith(("-", " "))}
+    if kv.get("feature_type") != "gtinv":
+        return None
+    order = int(kv["gtinv_order"])
+    maxl = tuple(int(v) for v in kv["gtinv_maxl"].strip("[]").split(","))
+    return order, maxl[: order - 1]
 
 
 def main():
-    os.makedirs(OUT, exist_ok=True)
-    for name, rel in FILES.items():
-        shutil.copyfile(os.path.join(REF_TESTS, rel), os.path.join(OUT, name))
-        print("copied", name)
-    answers = asserted_values(os.path.join(REF_TESTS, "test_properties_MgO.py"))
-    with open(os.path.join(OUT, "known_answers.json"), "w") as f:
-        json.dump({"source": "tests/test_calc/test_properties_MgO.py", "cases": answers}, f, indent=1)
-    print("wrote known_answers.json:", sorted(answers))
-
     from oracle import ref
     from pypolymlp_gb300.params import gtinv_file
 
-    order, maxl = 3, (4, 4)
-    l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
-    with open(gtinv_file(order, maxl), "w") as f:
-        json.dump({"order": order, "maxl": list(maxl), "version": 1, "l_comb": l_comb, "lm_seq": lm_seq,
-                   "lm_coeffs": lm_coeffs}, f, separators=(",", ":"))
-    print("wrote", gtinv_file(order, maxl))
+    os.makedirs(OUT, exist_ok=True)
+    cases, tables = {}, set()
+    for cid, (test, fname, pots, poscar, forces_kind, s_unit) in CASES.items():
+        fn = _function(os.path.join(REF, test), fname)
+        e_val, e_tol = _energy_approx(fn)
+        if e_val is None:
+            e_val = _assigned(fn, "energy_true")
+        case = {"test": f"tests/test_calc/{test}::{fname}", "potentials": pots, "structure": poscar,
+                "energy": e_val, "energy_tol": e_tol, "forces_kind": forces_kind, "forces_atol": 1e-6}
+        if forces_kind in ("NxT", "3xN"):
+            f = _assigned(fn, "forces_true")
+            case["forces"] = [list(r) for r in zip(*f)] if forces_kind == "3xN" else f
+        else:
+            case["forces_atol"] = 1e-12
+        s = _assigned(fn, "stresses_true")
+        if s_unit is not None and s is not None:
+            case.update({"stresses": s, "stresses_unit": s_unit, "stresses_atol": 1e-5})
+        cases[cid] = case
+        for name in pots + [poscar]:
+            src = os.path.join(REF, "files", "mlps" if name.startswith("polymlp") else "poscars", name)
+            shutil.copyfile(src, os.path.join(OUT, name))
+        for p in pots:
+            spec = gtinv_spec(os.path.join(OUT, p))
+            if spec:
+                tables.add(spec)
+        print(cid, case["energy"], case["energy_tol"])
+    with open(os.path.join(OUT, "known_answers.json"), "w") as f:
+        json.dump({"source": "tests/test_calc/test_properties_*.py", "cases": cases}, f, indent=1)
+    for order, maxl in sorted(tables):
+        l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
+        with open(gtinv_file(order, maxl), "w") as f:
+            json.dump({"order": order, "maxl": list(maxl), "version": 1, "l_comb": l_comb, "lm_seq": lm_seq,
+                       "lm_coeffs": lm_coeffs}, f, separators=(",", ":"))
+        print("wrote", gtinv_file(order, maxl))
 
 
 if __name__ == "__main__":

@@ -1,9 +1,12 @@
-"""Known answers of the reference's own tests (test_calc/test_properties_MgO.py:
-two shipped MgO potentials on a displaced rocksalt cell; fixtures and the
-asserted values copied by tests/golden/make_known_answers.py).  The shipped
-polymlp.yaml files are read by pypolymlp_gb300.io_polymlp; the oracle (CPU)
-and the GPU evaluator must reproduce the asserted energy (1e-8 relative),
-forces (1e-6 eV/A) and stresses (1e-5 GPa), the reference test's tolerances."""
+"""Known answers of the reference's own property tests
+(tests/test_calc/test_properties_*.py: potentials shipped with its tests, in
+polymlp.yaml and legacy polymlp.lammps form, pair and gtinv, with conditional
+pair parameters and one hybrid model, on small cells; fixtures and asserted
+values copied by tests/golden/make_known_answers.py).  The files are read by
+pypolymlp_gb300.io_polymlp; the oracle (CPU) must reproduce every asserted value
+at the reference test's tolerance, the GPU evaluator (FP64) too, with the
+energy compared to 1e-10 relative where the reference asserts 1e-12 absolute
+(its own summation order)."""
 
 import json
 import os
@@ -13,6 +16,7 @@ import pytest
 
 from pypolymlp_gb300 import io_polymlp
 from pypolymlp_gb300.abi import Structures
+from pypolymlp_gb300.hybrid import active_atoms
 
 KA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers")
 EV_TO_GPA = 160.21766208
@@ -37,18 +41,26 @@ def _cases():
         return json.load(f)["cases"]
 
 
-def _check(case, e, f, s, axis, force_atol=None, energy_rel=None, stress_atol=None):
-    tol = case["tolerances"]
-    assert e == pytest.approx(case["energy"], rel=energy_rel or tol["energy_rel"])
-    np.testing.assert_allclose(f, case["forces"], atol=force_atol or tol["forces_abs"], rtol=0)
-    s_gpa = np.asarray(s) / abs(np.linalg.det(axis)) * EV_TO_GPA
-    np.testing.assert_allclose(s_gpa, case["stresses_gpa"], atol=stress_atol or tol["stresses_gpa_abs"], rtol=0)
-
-
 def _load(case):
-    p, c = io_polymlp.load_mlp(os.path.join(KA, case["potential"]))
-    axis, pos, types = read_poscar(os.path.join(KA, case["structure"]), p["elements"])
-    return p, c, Structures([axis], [pos], [types]), axis
+    models = [io_polymlp.load_mlp(os.path.join(KA, p)) for p in case["potentials"]]
+    axis, pos, types = read_poscar(os.path.join(KA, case["structure"]), models[0][0]["elements"])
+    return models, axis, pos, types
+
+
+def _check(case, e, f, s, axis, gpu=False):
+    tol = dict(case["energy_tol"])
+    if gpu and "abs" in tol:
+        tol = {"rel": 1e-10}
+    assert e == pytest.approx(case["energy"], **tol)
+    if case["forces_kind"] == "f00":
+        assert abs(f[0][0]) <= case["forces_atol"]
+    else:
+        np.testing.assert_allclose(f, case["forces"], atol=case["forces_atol"], rtol=0)
+    if "stresses" in case:
+        s = np.asarray(s, dtype=np.float64)
+        if case["stresses_unit"] == "GPa":
+            s = s / abs(np.linalg.det(axis)) * EV_TO_GPA
+        np.testing.assert_allclose(s, case["stresses"], atol=case["stresses_atol"], rtol=0)
 
 
 @pytest.mark.parametrize("name", sorted(_cases()))
@@ -56,20 +68,27 @@ def test_oracle_reproduces_reference_known_answers(name):
     from oracle import oracle
 
     case = _cases()[name]
-    p, c, st, axis = _load(case)
-    e, f, s = oracle.evaluate(p, c, st)
-    _check(case, float(e[0]), f, s[0], axis)
+    models, axis, pos, types = _load(case)
+    e, f, s = 0.0, np.zeros((len(types), 3)), np.zeros(6)
+    for p, c in models:
+        idx, t = active_atoms(types, p)
+        if len(idx) == 0:
+            continue
+        em, fm, sm = oracle.evaluate(p, c, Structures([axis], [pos[idx]], [t]))
+        e += float(em[0])
+        f[idx] += fm
+        s += sm[0]
+    _check(case, e, f, s, axis)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(_cases()))
 def test_gpu_evaluator_reproduces_reference_known_answers(name):
     from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.hybrid import PropertiesHybrid
 
     case = _cases()[name]
-    p, c, st, axis = _load(case)
-    e, f, s = _ffi.Evaluator(p, c, _ffi.PG_FP64).run(st)
-    _check(case, float(e[0]), f, s[0], axis)
-    # mixed precision: FP32 features and adjoint (1e-6 relative energy, 1e-4 eV/A, 1e-3 GPa)
-    e, f, s = _ffi.Evaluator(p, c, _ffi.PG_MIXED).run(st)
-    _check(case, float(e[0]), f, s[0], axis, force_atol=1e-4, energy_rel=1e-6, stress_atol=1e-3)
+    models, axis, pos, types = _load(case)
+    hy = PropertiesHybrid([p for p, _ in models], [c for _, c in models], _ffi.PG_FP64)
+    e, f, s = hy.eval(axis, pos.T, types)
+    _check(case, e, f, s, axis, gpu=True)
