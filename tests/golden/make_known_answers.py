@@ -12,8 +12,10 @@ asserted values from the test source (literal assignments such as
 `energy_true = ...`, or the literal of the energy's `pytest.approx(...)`, read
 with `ast`, never executed) into known_answers.json, together with the
 comparison each test makes (forces (N, 3) or only forces[0][0]; stresses in
-GPa or eV per cell; tolerances).  It also writes the invariant tables the
-gtinv potentials need with the reference's Readgtinv (oracle/_ref).
+GPa or eV per cell; tolerances); from test_compute_features.py it takes the
+shape, sum and first-minus-second-row sum of the energy rows of X for two MgO
+cells (known_x.json).  It also writes the invariant tables the gtinv
+potentials need with the reference's Readgtinv (oracle/_ref).
 """
 
 import ast
@@ -83,6 +85,25 @@ def _energy_approx(fn):
     raise KeyError("energy approx")
 
 
+# X known answers (test_compute_features.py): potential, the assert helper, POSCARs
+X_CASES = {
+    "X_MgO_pair": ("polymlp.yaml.pair.MgO", "_assert_pair_MgO"),
+    "X_MgO_gtinv": ("polymlp.yaml.gtinv.MgO", "_assert_gtinv_MgO"),
+}
+X_POSCARS = ["POSCAR-00001.MgO", "POSCAR-00002.MgO"]
+
+
+def _x_asserts(fn):
+    """shape and the two pytest.approx literals (sum(x), sum(x[0] - x[1])) with their kwargs."""
+    shape, approx = None, []
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Compare) and isinstance(node.left, ast.Attribute) and node.left.attr == "shape":
+            shape = list(ast.literal_eval(node.comparators[0]))
+        if isinstance(node, ast.Call) and getattr(node.func, "attr", "") == "approx":
+            approx.append((ast.literal_eval(node.args[0]), {k.arg: ast.literal_eval(k.value) for k in node.keywords}))
+    return shape, approx
+
+
 def gtinv_spec(path):
     """(order, maxl) of a gtinv potential file, None for a pair potential."""
     lines = open(path).read().splitlines()
@@ -133,6 +154,17 @@ def main():
         print(cid, case["energy"], case["energy_tol"])
     with open(os.path.join(OUT, "known_answers.json"), "w") as f:
         json.dump({"source": "tests/test_calc/test_properties_*.py", "cases": cases}, f, indent=1)
+    xcases = {}
+    for cid, (pot, helper) in X_CASES.items():
+        shape, approx = _x_asserts(_function(os.path.join(REF, "test_compute_features.py"), helper))
+        xcases[cid] = {"test": f"tests/test_calc/test_compute_features.py::{helper}", "potential": pot,
+                       "structures": X_POSCARS, "rows": "energy", "shape": shape,
+                       "sum": approx[0][0], "sum_tol": approx[0][1], "diff01": approx[1][0], "diff01_tol": approx[1][1]}
+        print(cid, shape, approx)
+    for name in X_POSCARS:
+        shutil.copyfile(os.path.join(REF, "files", "poscars", name), os.path.join(OUT, name))
+    with open(os.path.join(OUT, "known_x.json"), "w") as f:
+        json.dump({"source": "tests/test_calc/test_compute_features.py", "cases": xcases}, f, indent=1)
     for order, maxl in sorted(tables):
         l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
         with open(gtinv_file(order, maxl), "w") as f:

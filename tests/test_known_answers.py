@@ -92,3 +92,48 @@ def test_gpu_evaluator_reproduces_reference_known_answers(name):
     hy = PropertiesHybrid([p for p, _ in models], [c for _, c in models], _ffi.PG_FP64)
     e, f, s = hy.eval(axis, pos.T, types)
     _check(case, e, f, s, axis, gpu=True)
+
+
+def _x_cases():
+    with open(os.path.join(KA, "known_x.json")) as f:
+        return json.load(f)["cases"]
+
+
+def _x_inputs(case):
+    from pypolymlp_gb300.abi import row_layout
+
+    p, _ = io_polymlp.load_mlp(os.path.join(KA, case["potential"]))
+    cells = [read_poscar(os.path.join(KA, n), p["elements"]) for n in case["structures"]]
+    st = Structures([c[0] for c in cells], [c[1] for c in cells], [c[2] for c in cells])
+    return p, st, row_layout(st.n_atoms, [False] * st.n_st)
+
+
+def _check_x(case, x):
+    assert list(x.shape) == case["shape"]
+    assert float(np.sum(x)) == pytest.approx(case["sum"], **case["sum_tol"])
+    assert float(np.sum(x[0] - x[1])) == pytest.approx(case["diff01"], **case["diff01_tol"])
+
+
+@pytest.mark.parametrize("name", sorted(_x_cases()))
+def test_oracle_x_reproduces_reference_known_answers(name):
+    """Energy rows of X (test_compute_features.py: shape, sum, row difference)."""
+    from oracle import oracle
+
+    case = _x_cases()[name]
+    p, st, (e, f, s, n) = _x_inputs(case)
+    _check_x(case, oracle.features_x(p, st, e, f, s, n))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(_x_cases()))
+def test_gpu_x_reproduces_reference_known_answers(name):
+    from pypolymlp_gb300 import _ffi
+
+    case = _x_cases()[name]
+    p, st, (e, f, s, n) = _x_inputs(case)
+    m = _ffi.Model(p)
+    _check_x(case, m.features_x(st, e, f, s, n, precision=_ffi.PG_FP64))
+    # mixed (FP32 rows): the total to 1e-5; the row difference is a small
+    # difference of large sums and below FP32 resolution at 1e-6
+    x32 = m.features_x(st, e, f, s, n, precision=_ffi.PG_MIXED)
+    assert float(np.sum(x32)) == pytest.approx(case["sum"], rel=1e-5)
