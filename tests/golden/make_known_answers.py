@@ -15,7 +15,9 @@ comparison each test makes (forces (N, 3) or only forces[0][0]; stresses in
 GPa or eV per cell; tolerances); from test_compute_features.py it takes the
 shape, sum and first-minus-second-row sum of the energy rows of X for two MgO
 cells (known_x.json).  It also writes the invariant tables the gtinv
-potentials need with the reference's Readgtinv (oracle/_ref).
+potentials need with the reference's Readgtinv (oracle/_ref), and the radial
+function and Y_lm values of tests/test_cxx/test_functions.py
+(known_functions.json).
 """
 
 import ast
@@ -104,6 +106,36 @@ def _x_asserts(fn):
     return shape, approx
 
 
+def function_answers():
+    """Radial functions and Y_lm of tests/test_cxx/test_functions.py: the inputs and
+    the asserted values (test_get_fn, test_get_ylm sums, test_get_ylm_2 tables)."""
+    path = "/root/reference/tests/test_cxx/test_functions.py"
+    out = {}
+    fn = _function(path, "test_get_fn")
+    call = next(n for n in ast.walk(fn) if isinstance(n, ast.Call) and getattr(n.func, "id", "") == "get_fn")
+    kw = {k.arg: k.value for k in call.keywords}
+    expected = [ast.literal_eval(n.args[1]) for n in ast.walk(fn)
+                if isinstance(n, ast.Call) and getattr(n.func, "attr", "") == "assert_allclose"]
+    out["fn"] = {"r": ast.literal_eval(kw["r"]), "cutoff": ast.literal_eval(kw["cutoff"]),
+                 "params": _assigned(fn, "params"), "fn": expected[0], "fn_d": expected[1], "rtol": 1e-7}
+    for name in ("test_get_ylm", "test_get_ylm_2"):
+        f = _function(path, name)
+        call = next(n for n in ast.walk(f) if isinstance(n, ast.Call) and getattr(n.func, "id", "") == "get_ylm")
+        lmax = ast.literal_eval({k.arg: k.value for k in call.keywords}["lmax"])
+        case = {"x": _assigned(f, "x"), "y": _assigned(f, "y"), "z": _assigned(f, "z"), "lmax": lmax}
+        sums = [ast.literal_eval(n.args[0]) for n in ast.walk(f)
+                if isinstance(n, ast.Call) and getattr(n.func, "attr", "") == "approx"]
+        if sums:
+            case["sums"] = [[v.real, v.imag] for v in sums]
+            case["sums_rel"] = 1e-6
+        tables = {k: _assigned(f, k) for k in ("ylm_true", "ylm_dx_true", "ylm_dy_true", "ylm_dz_true")}
+        if all(v is not None for v in tables.values()):
+            case["tables"] = {k: [[complex(v).real, complex(v).imag] for v in t] for k, t in tables.items()}
+            case["tables_atol"] = 1e-7
+        out[name] = case
+    return out
+
+
 def gtinv_spec(path):
     """(order, maxl) of a gtinv potential file, None for a pair potential."""
     lines = open(path).read().splitlines()
@@ -165,6 +197,9 @@ def main():
         shutil.copyfile(os.path.join(REF, "files", "poscars", name), os.path.join(OUT, name))
     with open(os.path.join(OUT, "known_x.json"), "w") as f:
         json.dump({"source": "tests/test_calc/test_compute_features.py", "cases": xcases}, f, indent=1)
+    with open(os.path.join(OUT, "known_functions.json"), "w") as f:
+        json.dump({"source": "tests/test_cxx/test_functions.py", "cases": function_answers()}, f, indent=1)
+    print("wrote known_functions.json")
     for order, maxl in sorted(tables):
         l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
         with open(gtinv_file(order, maxl), "w") as f:

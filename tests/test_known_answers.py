@@ -137,3 +137,35 @@ def test_gpu_x_reproduces_reference_known_answers(name):
     # difference of large sums and below FP32 resolution at 1e-6
     x32 = m.features_x(st, e, f, s, n, precision=_ffi.PG_MIXED)
     assert float(np.sum(x32)) == pytest.approx(case["sum"], rel=1e-5)
+
+
+def _fn_cases():
+    with open(os.path.join(KA, "known_functions.json")) as f:
+        return json.load(f)["cases"]
+
+
+def test_oracle_radial_functions_reproduce_reference_known_answers():
+    """f_n and df_n/dr of tests/test_cxx/test_functions.py::test_get_fn."""
+    from oracle import oracle
+
+    c = _fn_cases()["fn"]
+    f, fd = oracle.fn(c["r"], c["cutoff"], c["params"])
+    np.testing.assert_allclose(f, c["fn"], rtol=c["rtol"])
+    np.testing.assert_allclose(fd, c["fn_d"], rtol=c["rtol"])
+
+
+@pytest.mark.parametrize("name", ["test_get_ylm", "test_get_ylm_2"])
+def test_oracle_ylm_reproduce_reference_known_answers(name):
+    """Y_lm and its gradients (sums for l_max 10, tables for l_max 3)."""
+    from oracle import oracle
+
+    c = _fn_cases()[name]
+    x, y, z = c["x"], c["y"], c["z"]
+    got = oracle.ylm(float(np.sqrt(x * x + y * y + z * z)), x, y, z, c["lmax"])
+    if "sums" in c:
+        for g, (re, im) in zip(got, c["sums"]):
+            assert complex(np.sum(g)) == pytest.approx(complex(re, im), rel=c["sums_rel"])
+    if "tables" in c:
+        for g, key in zip(got, ("ylm_true", "ylm_dx_true", "ylm_dy_true", "ylm_dz_true")):
+            want = np.array([complex(a, b) for a, b in c["tables"][key]])
+            np.testing.assert_allclose(g, want, atol=c["tables_atol"], rtol=0)
