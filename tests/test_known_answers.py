@@ -169,3 +169,38 @@ def test_oracle_ylm_reproduce_reference_known_answers(name):
         for g, key in zip(got, ("ylm_true", "ylm_dx_true", "ylm_dy_true", "ylm_dz_true")):
             want = np.array([complex(a, b) for a, b in c["tables"][key]])
             np.testing.assert_allclose(g, want, atol=c["tables_atol"], rtol=0)
+
+
+@pytest.mark.parametrize("name", ["MgO_pair_legacy", "SrTiO3_pair_cond_legacy"])
+def test_legacy_file_converted_to_yaml_keeps_the_known_answers(tmp_path, name):
+    """A shipped legacy file rewritten by convert_to_yaml evaluates to the same known answers."""
+    from oracle import oracle
+
+    case = _cases()[name]
+    out = str(tmp_path / "polymlp.yaml")
+    assert io_polymlp.convert_to_yaml(os.path.join(KA, case["potentials"][0]), out)
+    p, c = io_polymlp.load_mlp(out)
+    axis, pos, types = read_poscar(os.path.join(KA, case["structure"]), p["elements"])
+    e, f, s = oracle.evaluate(p, c, Structures([axis], [pos], [types]))
+    _check(case, float(e[0]), f, s[0], axis)
+
+
+@pytest.mark.parametrize("name", ["polymlp.yaml.gtinv.MgO", "polymlp.lammps.pair.Ag"])
+def test_rewritten_shipped_file_parses_like_the_original(tmp_path, name):
+    """Load a shipped file, write it again as polymlp.yaml: the reference's C++ parser
+    reads the same model and coefficients (to the 16 significant digits written)."""
+    from oracle import ref as refb
+
+    if not refb.available():
+        pytest.skip("the reference build (oracle/_ref) is not present")
+    src = os.path.join(KA, name)
+    p, c = io_polymlp.load_mlp(src)
+    out = str(tmp_path / "polymlp.yaml")
+    io_polymlp.save_mlp_yaml(p, c, np.ones(len(c)), out, mass=p["mass"])
+    a = refb.parse_potential(src, legacy=io_polymlp.is_legacy(src))
+    b = refb.parse_potential(out, legacy=False)
+    for k in ("elements", "cutoff", "pair_type", "feature_type", "model_type", "max_p", "cond"):
+        assert a[k] == b[k], k
+    np.testing.assert_array_equal(a["params"], b["params"])
+    np.testing.assert_allclose(b["coeffs"], a["coeffs"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(b["mass"], a["mass"], rtol=0, atol=0)
