@@ -15,9 +15,11 @@ comparison each test makes (forces (N, 3) or only forces[0][0]; stresses in
 GPa or eV per cell; tolerances); from test_compute_features.py it takes the
 shape, sum and first-minus-second-row sum of the energy rows of X for two MgO
 cells (known_x.json).  It also writes the invariant tables the gtinv
-potentials need with the reference's Readgtinv (oracle/_ref), and the radial
+potentials need with the reference's Readgtinv (oracle/_ref), the radial
 function and Y_lm values of tests/test_cxx/test_functions.py
-(known_functions.json).
+(known_functions.json), and the MgO pair fit of
+tests/test_mlp_dev_api/test_mlp_devel_vasp.py (its vasprun data as arrays,
+fit_pair_MgO.npz, and the asserted train/test errors, known_fit.json).
 """
 
 import ast
@@ -136,6 +138,99 @@ def function_answers():
     return out
 
 
+FIT_DIR = "/root/reference/tests/test_mlp_dev_api"
+EV_TO_KBAR = 1602.1766208
+
+
+def _read_input(path):
+    """key -> list of tokens of a polymlp.in file."""
+    out = {}
+    for line in open(path).read().splitlines():
+        tok = line.split("#")[0].split()
+        if tok:
+            out[tok[0]] = tok[1:]
+    return out
+
+
+def _vasprun(path, elements):
+    """One single-point vasprun (.xml.polymlp): the reference's Vasprun reading
+    (core/interface_vasp.py:108-220) of energy (e_wo_entrp), forces, stress (kbar
+    -> eV per cell, interface_vasp.py:72) and the final structure, atoms in the
+    parameter file's element order (dataset_utils.py:225-245)."""
+    import xml.etree.ElementTree as ET
+
+    import numpy as np
+
+    root = ET.parse(path).getroot()
+    arr = lambda v: np.array([[float(x) for x in e.text.split()] for e in v])  # noqa: E731
+    energy = float(root.find("calculation").find("energy")[1].text)
+    forces = arr(root.find(".//*[@name='forces']"))
+    stress = arr(root.find(".//*[@name='stress']"))
+    st = root.find(".//*[@name='finalpos']")
+    basis = arr(st.find(".//*[@name='basis']"))
+    frac = arr(st.find(".//*[@name='positions']"))
+    volume = float(st.find(".//*[@name='volume']").text)
+    names = [rc.findall("c")[0].text.strip() for rc in root.findall(".//*[@name='atoms']/set/rc")]
+    types = np.array([elements.index(n) for n in names])
+    order = np.argsort(types, kind="stable")
+    axis = basis.T
+    pos = (frac @ basis)[order]
+    sigma = stress * volume / EV_TO_KBAR
+    s6 = [sigma[0][0], sigma[1][1], sigma[2][2], sigma[0][1], sigma[1][2], sigma[2][0]]
+    return axis, pos, types[order], energy, forces[order], s6
+
+
+def fit_known_answers():
+    """The MgO pair fit of tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair:
+    the settings of polymlp.in.vasp.pair.single.MgO, the training and test
+    vasprun data (atomic energies subtracted, dataset.py:295-310) as arrays, and
+    the errors _check_errors_pair_single_dataset_MgO asserts."""
+    import glob
+
+    import numpy as np
+
+    inp = _read_input(os.path.join(FIT_DIR, "polymlp.in.vasp.pair.single.MgO"))
+    elements = inp["elements"]
+    atom_e = np.array([float(v) for v in inp["atomic_energy"]])
+    arrays = {}
+    for tag in ("train", "test"):
+        files = sorted(glob.glob(os.path.join(FIT_DIR, inp[f"{tag}_data"][0])))
+        rows = [_vasprun(f, elements) for f in files]
+        n_atoms = np.array([len(r[2]) for r in rows])
+        e = np.array([r[3] - np.bincount(r[2], minlength=len(elements)) @ atom_e for r in rows])
+        arrays.update({f"{tag}_n_atoms": n_atoms, f"{tag}_axis": np.array([r[0] for r in rows]),
+                       f"{tag}_positions": np.concatenate([r[1] for r in rows]),
+                       f"{tag}_types": np.concatenate([r[2] for r in rows]), f"{tag}_energies": e,
+                       f"{tag}_forces": np.concatenate([r[4] for r in rows]),
+                       f"{tag}_stresses": np.array([r[5] for r in rows])})
+        print(tag, len(files), "structures")
+    np.savez_compressed(os.path.join(OUT, "fit_pair_MgO.npz"), **arrays)
+    fn = _function(os.path.join(FIT_DIR, "test_mlp_devel_vasp.py"), "_check_errors_pair_single_dataset_MgO")
+    expected = {}
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Compare) and isinstance(node.left, ast.Subscript):
+            ds = node.left.value.id  # error_test1 / error_train1
+            key = ast.literal_eval(node.left.slice)
+            call = node.comparators[0]
+            expected.setdefault(ds.replace("error_", "").rstrip("1"), {})[key] = {
+                "value": ast.literal_eval(call.args[0]),
+                **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
+    fit = _function(os.path.join(FIT_DIR, "test_mlp_devel_vasp.py"), "test_mlp_devel_pair")
+    n_features = next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
+                      if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
+    a0, a1, na = (float(v) for v in inp["reg_alpha_params"])
+    settings = {"n_type": int(inp["n_type"][0]), "elements": elements, "feature_type": inp["feature_type"][0],
+                "cutoff": float(inp["cutoff"][0]), "model_type": int(inp["model_type"][0]),
+                "max_p": int(inp["max_p"][0]),
+                "gaussian_params1": [float(v) for v in inp["gaussian_params1"]],
+                "gaussian_params2": [float(v) for v in inp["gaussian_params2"]],
+                "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features}
+    with open(os.path.join(OUT, "known_fit.json"), "w") as f:
+        json.dump({"source": "tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair",
+                   "settings": settings, "errors": expected}, f, indent=1)
+    print("wrote known_fit.json", expected)
+
+
 def gtinv_spec(path):
     """(order, maxl) of a gtinv potential file, None for a pair potential."""
     lines = open(path).read().splitlines()
@@ -200,6 +295,7 @@ def main():
     with open(os.path.join(OUT, "known_functions.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_functions.py", "cases": function_answers()}, f, indent=1)
     print("wrote known_functions.json")
+    fit_known_answers()
     for order, maxl in sorted(tables):
         l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
         with open(gtinv_file(order, maxl), "w") as f:

@@ -1,0 +1,88 @@
+"""Known answers of the reference's end-to-end fit test
+(tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair: a pair model
+of MgO fitted to 270 vasprun structures and tested on 30; data and asserted
+errors copied by tests/golden/make_known_answers.py).  The regression pipeline
+restated on the CPU (oracle X rows, numpy Gram, LAPACK posv, the reference's
+weights, scales and alpha selection) and the GPU fit (FP64) must both give the
+asserted train/test errors: energy 1e-8 eV/atom, force 1e-6 eV/A, stress
+1e-5 eV/atom absolute, the reference test's tolerances."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from pypolymlp_gb300.accuracy import prediction_errors
+from pypolymlp_gb300.params import make_params_dict
+from pypolymlp_gb300.regression import Dataset
+
+KA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers")
+
+
+def _known():
+    with open(os.path.join(KA, "known_fit.json")) as f:
+        return json.load(f)
+
+
+def _datasets():
+    z = np.load(os.path.join(KA, "fit_pair_MgO.npz"))
+    out = []
+    for tag in ("train", "test"):
+        n = z[f"{tag}_n_atoms"]
+        offs = np.concatenate([[0], np.cumsum(n)])
+        sl = [slice(offs[i], offs[i + 1]) for i in range(len(n))]
+        out.append(Dataset([a for a in z[f"{tag}_axis"]], [z[f"{tag}_positions"][s] for s in sl],
+                           [z[f"{tag}_types"][s] for s in sl], z[f"{tag}_energies"],
+                           [z[f"{tag}_forces"][s] for s in sl], z[f"{tag}_stresses"], name=tag))
+    return out
+
+
+def _params(st):
+    return make_params_dict(n_type=st["n_type"], cutoff=st["cutoff"], model_type=st["model_type"],
+                            max_p=st["max_p"], feature_type=st["feature_type"],
+                            gaussian_params1=tuple(st["gaussian_params1"]),
+                            gaussian_params2=tuple(st["gaussian_params2"]), elements=st["elements"])
+
+
+def _check(errors, known):
+    for tag, got in errors.items():
+        for key, want in known[tag].items():
+            assert got[key] == pytest.approx(want["value"], abs=want["abs"]), (tag, key, got[key], want["value"])
+
+
+def test_cpu_pipeline_reproduces_reference_fit_errors():
+    from oracle import oracle
+    from oracle.pipeline import calc_xtx_xty_cpu, solver_ridge_cpu
+    from pypolymlp_gb300.abi import Structures
+    from pypolymlp_gb300.regression import compute_rmse_seq
+
+    k = _known()
+    p = _params(k["settings"])
+    assert oracle.n_features(p) == k["settings"]["n_features"]
+    train, test = _datasets()
+    xy = calc_xtx_xty_cpu(p, [train])
+    coefs = solver_ridge_cpu(xy.xtx, xy.xty, k["settings"]["alphas"])
+    txy = calc_xtx_xty_cpu(p, [test], scales=xy.scales, min_energy=xy.min_energy)
+    best = coefs[:, int(np.argmin(compute_rmse_seq(coefs, txy)))] / xy.scales
+    errors = {}
+    for tag, d in (("train", train), ("test", test)):
+        e, f, s = oracle.evaluate(p, best, Structures(d.axis, d.positions, d.types))
+        offs = np.concatenate([[0], np.cumsum(d.total_n_atoms)])
+        errors[tag], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
+    _check(errors, k["errors"])
+
+
+@pytest.mark.gpu
+def test_gpu_fit_reproduces_reference_fit_errors():
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.accuracy import PolymlpEvalAccuracy
+    from pypolymlp_gb300.regression import fit
+
+    k = _known()
+    p = _params(k["settings"])
+    train, test = _datasets()
+    res = fit(p, [train], [test], k["settings"]["alphas"], precision=_ffi.PG_FP64)
+    acc = PolymlpEvalAccuracy(p, res.scaled_coeffs)
+    errors = {tag: acc.compute_error_single(d, log_energy=False) for tag, d in (("train", train), ("test", test))}
+    _check(errors, k["errors"])
