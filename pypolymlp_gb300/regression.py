@@ -320,22 +320,25 @@ def normal_matvec(gram: "GramAccumulator", batches: Sequence["DeviceBatch"], v: 
 
 
 def ridge_pcg(xtx_mixed: np.ndarray, xty: np.ndarray, alphas: np.ndarray, matvec, zero_ids,
-              max_iter: int = 60, rtol: float = 1e-10):
+              max_iter: int = 60, rtol: float = 1e-10, factor=None, return_residuals: bool = False):
     """Solve (A + alpha I) c = b for every alpha by conjugate gradients whose
     products A p come from `matvec` (exact FP64 sums over the rows) and whose
     preconditioner is the device Cholesky factor of the mixed-precision
     matrix, shifted by the smallest tau (0, then 1e-9 ... 1e-2 of its mean
     diagonal) that makes it positive definite.  The mixed Gram's rounding is
     larger than small alphas, so it cannot be solved directly; this keeps it
-    only as the preconditioner.  Returns (coefs F x n_alpha, iterations,
-    shift per alpha)."""
+    only as the preconditioner.  `factor(matrix, shift)` builds the
+    preconditioner (default: `RidgeFactor`, on the device).  Returns (coefs
+    F x n_alpha, iterations, shift per alpha), and the final relative residual
+    norm per alpha with return_residuals."""
+    factor = RidgeFactor if factor is None else factor
     F = xtx_mixed.shape[0]
     na = len(alphas)
     dmean = float(np.mean(np.diag(xtx_mixed)))
     facs, taus = [], []
     for a in alphas:
         for t in [0.0] + [dmean * 10.0 ** e for e in range(-9, -1)]:
-            f = RidgeFactor(xtx_mixed, a + t)
+            f = factor(xtx_mixed, a + t)
             if f.info == 0:
                 break
         facs.append(f)
@@ -372,6 +375,8 @@ def ridge_pcg(xtx_mixed: np.ndarray, xty: np.ndarray, alphas: np.ndarray, matvec
         beta = np.where(active, rz_new / np.where(rz != 0, rz, 1.0), 0.0)
         p = z + p * beta[None, :]
         rz = rz_new
+    if return_residuals:
+        return x, it, np.array(taus), np.linalg.norm(r, axis=0) / np.where(bn > 0, bn, 1.0)
     return x, it, np.array(taus)
 
 
@@ -422,6 +427,7 @@ class FitResult:
     info: np.ndarray = field(repr=False, default=None)
     cg_iterations: int = 0                 # conjugate-gradient iterations (mixed path)
     shifts: np.ndarray = field(repr=False, default=None)  # preconditioner shift per alpha
+    fp64_fallback: bool = False            # mixed path: CG did not converge, FP64 Gram solved directly
 
     @property
     def scaled_coeffs(self):
@@ -547,14 +553,19 @@ def fit_learning_curve(params_dict: dict, train: Sequence[Dataset], test: Sequen
 
 def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
         precision: int = _ffi.PG_MIXED, model: Optional[_ffi.Model] = None, refine: Optional[int] = None,
-        weight_stress: float = 0.1) -> FitResult:
+        weight_stress: float = 0.1, fp64_fallback: bool = False) -> FitResult:
     """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60).
 
     The Gram is assembled once (mixed or FP64).  FP64: the ridge systems are
     solved directly (device Cholesky, as posv).  Mixed: the mixed Gram only
     preconditions a conjugate-gradient solve whose matrix products are FP64
     sums over freshly generated rows (`refine` caps the iterations; default
-    60, stopping at a relative residual of 1e-10).  RMSEs are computed from
+    60, stopping at a relative residual of 1e-10).  With fp64_fallback, when an
+    alpha's residual is still above 1e-8 after the cap (an ill-conditioned
+    normal matrix, where the mixed Gram needs a large shift to factor and
+    preconditions small alphas weakly), the FP64 Gram is assembled in one more
+    pass and solved directly (FitResult.fp64_fallback); each CG iteration costs
+    a pass over the rows, so this bounds the cost.  RMSEs are computed from
     residuals (weighted rows, as the reference's Gram-based formula defines
     them)."""
     model = model or _ffi.Model(params_dict)
@@ -571,7 +582,17 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
         def matvec(v):
             return normal_matvec(gram, tb, v / scales[:, None]) / scales[:, None]
 
-        coefs, n_iter, shifts = ridge_pcg(xtx, xty, alphas, matvec, zero_ids, max_iter=max(1, refine))
+        coefs, n_iter, shifts, resid = ridge_pcg(xtx, xty, alphas, matvec, zero_ids, max_iter=max(1, refine),
+                                                 return_residuals=True)
         info = np.zeros(len(alphas), dtype=np.int32)
+        if fp64_fallback and precision == _ffi.PG_MIXED and np.any(resid > 1e-8):
+            del tb, gram
+            precision = _ffi.PG_FP64
+            tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
+            coefs, info = solver_ridge(xtx, xty, alphas)
+            res = _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info,
+                          n_iter, shifts)
+            res.fp64_fallback = True
+            return res
     return _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info, n_iter,
                    shifts)
