@@ -17,9 +17,9 @@ shape, sum and first-minus-second-row sum of the energy rows of X for two MgO
 cells (known_x.json).  It also writes the invariant tables the gtinv
 potentials need with the reference's Readgtinv (oracle/_ref), the radial
 function and Y_lm values of tests/test_cxx/test_functions.py
-(known_functions.json), and the MgO pair fit of
-tests/test_mlp_dev_api/test_mlp_devel_vasp.py (its vasprun data as arrays,
-fit_pair_MgO.npz, and the asserted train/test errors, known_fit.json).
+(known_functions.json), and the MgO pair and gtinv fits of
+tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
+fit_MgO.npz, and the asserted train/test errors, known_fit.json).
 """
 
 import ast
@@ -180,55 +180,85 @@ def _vasprun(path, elements):
     return axis, pos, types[order], energy, forces[order], s6
 
 
+# end-to-end fits of tests/test_mlp_dev_api/test_mlp_devel_vasp.py on the MgO
+# train1/test1 data: case -> (input file, test function, error-check helper)
+FIT_CASES = {
+    "pair_single": ("polymlp.in.vasp.pair.single.MgO", "test_mlp_devel_pair", "_check_errors_pair_single_dataset_MgO"),
+    "gtinv_single": ("polymlp.in.vasp.single.MgO", "test_mlp_devel_single_dataset", "_check_errors_single_dataset_MgO"),
+}
+
+
+def _fit_errors(fn):
+    """{"train"|"test": {quantity: {value, abs}}} of an error-check helper; checks
+    under `if use_stress:` are left out (the tests call them without stress)."""
+    expected = {}
+
+    def visit(stmts):
+        for node in stmts:
+            if isinstance(node, ast.If):
+                continue
+            if isinstance(node, ast.Assert) and isinstance(node.test, ast.Compare):
+                cmp = node.test
+                if isinstance(cmp.left, ast.Subscript):
+                    ds = cmp.left.value.id
+                    key = ast.literal_eval(cmp.left.slice)
+                    call = cmp.comparators[0]
+                    expected.setdefault(ds.replace("error_", "").rstrip("1"), {})[key] = {
+                        "value": ast.literal_eval(call.args[0]),
+                        **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
+
+    visit(fn.body)
+    return expected
+
+
 def fit_known_answers():
-    """The MgO pair fit of tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair:
-    the settings of polymlp.in.vasp.pair.single.MgO, the training and test
-    vasprun data (atomic energies subtracted, dataset.py:295-310) as arrays, and
-    the errors _check_errors_pair_single_dataset_MgO asserts."""
+    """The MgO fits of tests/test_mlp_dev_api/test_mlp_devel_vasp.py (FIT_CASES): the
+    settings of each input file, the training and test vasprun data (atomic
+    energies subtracted, dataset.py:295-310) as arrays, and the errors each
+    test asserts."""
     import glob
 
     import numpy as np
 
-    inp = _read_input(os.path.join(FIT_DIR, "polymlp.in.vasp.pair.single.MgO"))
-    elements = inp["elements"]
-    atom_e = np.array([float(v) for v in inp["atomic_energy"]])
-    arrays = {}
-    for tag in ("train", "test"):
-        files = sorted(glob.glob(os.path.join(FIT_DIR, inp[f"{tag}_data"][0])))
-        rows = [_vasprun(f, elements) for f in files]
-        n_atoms = np.array([len(r[2]) for r in rows])
-        e = np.array([r[3] - np.bincount(r[2], minlength=len(elements)) @ atom_e for r in rows])
-        arrays.update({f"{tag}_n_atoms": n_atoms, f"{tag}_axis": np.array([r[0] for r in rows]),
-                       f"{tag}_positions": np.concatenate([r[1] for r in rows]),
-                       f"{tag}_types": np.concatenate([r[2] for r in rows]), f"{tag}_energies": e,
-                       f"{tag}_forces": np.concatenate([r[4] for r in rows]),
-                       f"{tag}_stresses": np.array([r[5] for r in rows])})
-        print(tag, len(files), "structures")
-    np.savez_compressed(os.path.join(OUT, "fit_pair_MgO.npz"), **arrays)
-    fn = _function(os.path.join(FIT_DIR, "test_mlp_devel_vasp.py"), "_check_errors_pair_single_dataset_MgO")
-    expected = {}
-    for node in ast.walk(fn):
-        if isinstance(node, ast.Compare) and isinstance(node.left, ast.Subscript):
-            ds = node.left.value.id  # error_test1 / error_train1
-            key = ast.literal_eval(node.left.slice)
-            call = node.comparators[0]
-            expected.setdefault(ds.replace("error_", "").rstrip("1"), {})[key] = {
-                "value": ast.literal_eval(call.args[0]),
-                **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
-    fit = _function(os.path.join(FIT_DIR, "test_mlp_devel_vasp.py"), "test_mlp_devel_pair")
-    n_features = next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
-                      if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
-    a0, a1, na = (float(v) for v in inp["reg_alpha_params"])
-    settings = {"n_type": int(inp["n_type"][0]), "elements": elements, "feature_type": inp["feature_type"][0],
-                "cutoff": float(inp["cutoff"][0]), "model_type": int(inp["model_type"][0]),
-                "max_p": int(inp["max_p"][0]),
-                "gaussian_params1": [float(v) for v in inp["gaussian_params1"]],
-                "gaussian_params2": [float(v) for v in inp["gaussian_params2"]],
-                "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features}
+    cases, data_done = {}, False
+    test_src = os.path.join(FIT_DIR, "test_mlp_devel_vasp.py")
+    for cid, (infile, test_fn, helper) in FIT_CASES.items():
+        inp = _read_input(os.path.join(FIT_DIR, infile))
+        elements = inp["elements"]
+        if not data_done:
+            atom_e = np.array([float(v) for v in inp["atomic_energy"]])
+            arrays = {}
+            for tag in ("train", "test"):
+                files = sorted(glob.glob(os.path.join(FIT_DIR, inp[f"{tag}_data"][0])))
+                rows = [_vasprun(f, elements) for f in files]
+                e = np.array([r[3] - np.bincount(r[2], minlength=len(elements)) @ atom_e for r in rows])
+                arrays.update({f"{tag}_n_atoms": np.array([len(r[2]) for r in rows]),
+                               f"{tag}_axis": np.array([r[0] for r in rows]),
+                               f"{tag}_positions": np.concatenate([r[1] for r in rows]),
+                               f"{tag}_types": np.concatenate([r[2] for r in rows]), f"{tag}_energies": e,
+                               f"{tag}_forces": np.concatenate([r[4] for r in rows]),
+                               f"{tag}_stresses": np.array([r[5] for r in rows])})
+                print(tag, len(files), "structures")
+            np.savez_compressed(os.path.join(OUT, "fit_MgO.npz"), **arrays)
+            data_done = True
+        fit = _function(test_src, test_fn)
+        n_features = next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
+                          if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
+        a0, a1, na = (float(v) for v in inp["reg_alpha_params"])
+        st = {"n_type": int(inp["n_type"][0]), "elements": elements, "feature_type": inp["feature_type"][0],
+              "cutoff": float(inp["cutoff"][0]), "model_type": int(inp["model_type"][0]),
+              "max_p": int(inp["max_p"][0]), "gaussian_params1": [float(v) for v in inp["gaussian_params1"]],
+              "gaussian_params2": [float(v) for v in inp["gaussian_params2"]],
+              "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features,
+              "include_stress": inp.get("include_stress", ["True"])[0].lower() in ("true", "1")}
+        if st["feature_type"] == "gtinv":
+            st["gtinv_order"] = int(inp["gtinv_order"][0])
+            st["gtinv_maxl"] = [int(v) for v in inp["gtinv_maxl"]]
+        cases[cid] = {"test": f"tests/test_mlp_dev_api/test_mlp_devel_vasp.py::{test_fn}", "settings": st,
+                      "errors": _fit_errors(_function(test_src, helper)), "data": "fit_MgO.npz"}
+        print(cid, cases[cid]["errors"])
     with open(os.path.join(OUT, "known_fit.json"), "w") as f:
-        json.dump({"source": "tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair",
-                   "settings": settings, "errors": expected}, f, indent=1)
-    print("wrote known_fit.json", expected)
+        json.dump({"cases": cases}, f, indent=1)
 
 
 def gtinv_spec(path):

@@ -1,11 +1,11 @@
-"""Known answers of the reference's end-to-end fit test
-(tests/test_mlp_dev_api/test_mlp_devel_vasp.py::test_mlp_devel_pair: a pair model
-of MgO fitted to 270 vasprun structures and tested on 30; data and asserted
-errors copied by tests/golden/make_known_answers.py).  The regression pipeline
-restated on the CPU (oracle X rows, numpy Gram, LAPACK posv, the reference's
-weights, scales and alpha selection) and the GPU fit (FP64) must both give the
-asserted train/test errors: energy 1e-8 eV/atom, force 1e-6 eV/A, stress
-1e-5 eV/atom absolute, the reference test's tolerances."""
+"""Known answers of the reference's end-to-end fit tests
+(tests/test_mlp_dev_api/test_mlp_devel_vasp.py: a pair and a gtinv model of MgO
+fitted to 270 vasprun structures and tested on 30; data and asserted errors
+copied by tests/golden/make_known_answers.py).  The regression pipeline restated
+on the CPU (oracle X rows, numpy Gram, LAPACK posv, the reference's weights,
+scales and alpha selection) and the GPU fit (FP64) must give the asserted
+train/test errors: energy 1e-8 eV/atom, force 1e-6 eV/A, stress 1e-5 eV/atom
+absolute, the reference test's tolerances."""
 
 import json
 import os
@@ -20,13 +20,14 @@ from pypolymlp_gb300.regression import Dataset
 KA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers")
 
 
-def _known():
+def _cases():
     with open(os.path.join(KA, "known_fit.json")) as f:
-        return json.load(f)
+        return json.load(f)["cases"]
 
 
-def _datasets():
-    z = np.load(os.path.join(KA, "fit_pair_MgO.npz"))
+def _datasets(case):
+    z = np.load(os.path.join(KA, case["data"]))
+    stress = case["settings"]["include_stress"]
     out = []
     for tag in ("train", "test"):
         n = z[f"{tag}_n_atoms"]
@@ -34,15 +35,18 @@ def _datasets():
         sl = [slice(offs[i], offs[i + 1]) for i in range(len(n))]
         out.append(Dataset([a for a in z[f"{tag}_axis"]], [z[f"{tag}_positions"][s] for s in sl],
                            [z[f"{tag}_types"][s] for s in sl], z[f"{tag}_energies"],
-                           [z[f"{tag}_forces"][s] for s in sl], z[f"{tag}_stresses"], name=tag))
+                           [z[f"{tag}_forces"][s] for s in sl], z[f"{tag}_stresses"], include_stress=stress,
+                           name=tag))
     return out
 
 
 def _params(st):
-    return make_params_dict(n_type=st["n_type"], cutoff=st["cutoff"], model_type=st["model_type"],
-                            max_p=st["max_p"], feature_type=st["feature_type"],
-                            gaussian_params1=tuple(st["gaussian_params1"]),
-                            gaussian_params2=tuple(st["gaussian_params2"]), elements=st["elements"])
+    kw = dict(n_type=st["n_type"], cutoff=st["cutoff"], model_type=st["model_type"], max_p=st["max_p"],
+              feature_type=st["feature_type"], gaussian_params1=tuple(st["gaussian_params1"]),
+              gaussian_params2=tuple(st["gaussian_params2"]), elements=st["elements"])
+    if st["feature_type"] == "gtinv":
+        kw.update(gtinv_order=st["gtinv_order"], gtinv_maxl=tuple(st["gtinv_maxl"]))
+    return make_params_dict(**kw)
 
 
 def _check(errors, known):
@@ -51,18 +55,19 @@ def _check(errors, known):
             assert got[key] == pytest.approx(want["value"], abs=want["abs"]), (tag, key, got[key], want["value"])
 
 
-def test_cpu_pipeline_reproduces_reference_fit_errors():
+@pytest.mark.parametrize("name", sorted(_cases()))
+def test_cpu_pipeline_reproduces_reference_fit_errors(name):
     from oracle import oracle
     from oracle.pipeline import calc_xtx_xty_cpu, solver_ridge_cpu
     from pypolymlp_gb300.abi import Structures
     from pypolymlp_gb300.regression import compute_rmse_seq
 
-    k = _known()
-    p = _params(k["settings"])
-    assert oracle.n_features(p) == k["settings"]["n_features"]
-    train, test = _datasets()
+    case = _cases()[name]
+    p = _params(case["settings"])
+    assert oracle.n_features(p) == case["settings"]["n_features"]
+    train, test = _datasets(case)
     xy = calc_xtx_xty_cpu(p, [train])
-    coefs = solver_ridge_cpu(xy.xtx, xy.xty, k["settings"]["alphas"])
+    coefs = solver_ridge_cpu(xy.xtx, xy.xty, case["settings"]["alphas"])
     txy = calc_xtx_xty_cpu(p, [test], scales=xy.scales, min_energy=xy.min_energy)
     best = coefs[:, int(np.argmin(compute_rmse_seq(coefs, txy)))] / xy.scales
     errors = {}
@@ -70,19 +75,20 @@ def test_cpu_pipeline_reproduces_reference_fit_errors():
         e, f, s = oracle.evaluate(p, best, Structures(d.axis, d.positions, d.types))
         offs = np.concatenate([[0], np.cumsum(d.total_n_atoms)])
         errors[tag], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
-    _check(errors, k["errors"])
+    _check(errors, case["errors"])
 
 
 @pytest.mark.gpu
-def test_gpu_fit_reproduces_reference_fit_errors():
+@pytest.mark.parametrize("name", ["pair_single"])
+def test_gpu_fit_reproduces_reference_fit_errors(name):
     from pypolymlp_gb300 import _ffi
     from pypolymlp_gb300.accuracy import PolymlpEvalAccuracy
     from pypolymlp_gb300.regression import fit
 
-    k = _known()
-    p = _params(k["settings"])
-    train, test = _datasets()
-    res = fit(p, [train], [test], k["settings"]["alphas"], precision=_ffi.PG_FP64)
+    case = _cases()[name]
+    p = _params(case["settings"])
+    train, test = _datasets(case)
+    res = fit(p, [train], [test], case["settings"]["alphas"], precision=_ffi.PG_FP64)
     acc = PolymlpEvalAccuracy(p, res.scaled_coeffs)
     errors = {tag: acc.compute_error_single(d, log_energy=False) for tag, d in (("train", train), ("test", test))}
-    _check(errors, k["errors"])
+    _check(errors, case["errors"])
