@@ -49,7 +49,8 @@ def prediction_errors(dataset, energies, forces, stresses, stress_unit: Literal[
     err = {"energy": _rmse(true_e, pred_e), "energy_mae": _mae(true_e, pred_e), "force": None, "force_mae": None,
            "stress": None, "stress_mae": None, "percent_force_norm": None, "force_direction": None}
     arrays = {"energy": (true_e, pred_e)}
-    if dataset.forces is not None and dataset.include_force:
+    # errors wherever the data exist, fitted or not (eval_accuracy.py:82, 115: exist_force / exist_stress)
+    if dataset.forces is not None:
         true_f = np.concatenate([np.asarray(f, dtype=np.float64).reshape(-1) for f in dataset.forces])
         pred_f = np.concatenate([np.asarray(f, dtype=np.float64).reshape(-1) for f in forces])
         err["force"], err["force_mae"] = _rmse(true_f, pred_f), _mae(true_f, pred_f)
@@ -60,7 +61,7 @@ def prediction_errors(dataset, energies, forces, stresses, stress_unit: Literal[
             cosine = np.einsum("ij,ij->i", t3 / nt[:, None], p3 / npred[:, None])
             err["percent_force_norm"] = float(np.average(np.abs((npred - nt) / nt)))
             err["force_direction"] = degrees(acos(min(1.0, float(np.average(np.abs(cosine))))))
-    if dataset.stresses is not None and dataset.include_stress:
+    if dataset.stresses is not None:
         if stress_unit == "eV":
             norm = np.repeat(n_atoms, 6)
         elif stress_unit == "GPa":
