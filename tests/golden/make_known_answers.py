@@ -181,66 +181,64 @@ def _vasprun(path, elements):
 
 
 # end-to-end fits of tests/test_mlp_dev_api/test_mlp_devel_vasp.py on the MgO
-# train1/test1 data: case -> (input file, test function, error-check helper)
+# vasprun data: case -> (input file, test function, error-check helper, the
+# helper's arguments in order (dataset names))
 FIT_CASES = {
-    "pair_single": ("polymlp.in.vasp.pair.single.MgO", "test_mlp_devel_pair", "_check_errors_pair_single_dataset_MgO"),
-    "gtinv_single": ("polymlp.in.vasp.single.MgO", "test_mlp_devel_single_dataset", "_check_errors_single_dataset_MgO"),
+    "pair_single": ("polymlp.in.vasp.pair.single.MgO", "test_mlp_devel_pair", "_check_errors_pair_single_dataset_MgO",
+                    ["train1", "test1"]),
+    "gtinv_single": ("polymlp.in.vasp.single.MgO", "test_mlp_devel_single_dataset",
+                     "_check_errors_single_dataset_MgO", ["train1", "test1"]),
+    "gtinv_multi": ("polymlp.in.vasp.multi.MgO", "test_mlp_devel_multiple_datasets",
+                    "_check_errors_multiple_datasets_MgO", ["train1", "train2", "test1", "test2"]),
 }
+FIT_DATA = "data-vasp-MgO/vaspruns/{}/vasprun-*.xml.polymlp"
 
 
-def _fit_errors(fn):
-    """{"train"|"test": {quantity: {value, abs}}} of an error-check helper; checks
-    under `if use_stress:` are left out (the tests call them without stress)."""
+def _fit_errors(fn, names):
+    """{dataset name: {quantity: {value, abs}}} of an error-check helper whose
+    arguments are the datasets' error dicts in `names` order; checks under
+    `if use_stress:` are left out (the tests call them without stress)."""
+    args = [a.arg for a in fn.args.args]
     expected = {}
-
-    def visit(stmts):
-        for node in stmts:
-            if isinstance(node, ast.If):
-                continue
-            if isinstance(node, ast.Assert) and isinstance(node.test, ast.Compare):
-                cmp = node.test
-                if isinstance(cmp.left, ast.Subscript):
-                    ds = cmp.left.value.id
-                    key = ast.literal_eval(cmp.left.slice)
-                    call = cmp.comparators[0]
-                    expected.setdefault(ds.replace("error_", "").rstrip("1"), {})[key] = {
-                        "value": ast.literal_eval(call.args[0]),
-                        **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
-
-    visit(fn.body)
+    for node in fn.body:
+        if isinstance(node, ast.Assert) and isinstance(node.test, ast.Compare) and \
+                isinstance(node.test.left, ast.Subscript):
+            cmp = node.test
+            ds = names[args.index(cmp.left.value.id)]
+            call = cmp.comparators[0]
+            expected.setdefault(ds, {})[ast.literal_eval(cmp.left.slice)] = {
+                "value": ast.literal_eval(call.args[0]), **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
     return expected
 
 
 def fit_known_answers():
     """The MgO fits of tests/test_mlp_dev_api/test_mlp_devel_vasp.py (FIT_CASES): the
-    settings of each input file, the training and test vasprun data (atomic
-    energies subtracted, dataset.py:295-310) as arrays, and the errors each
-    test asserts."""
+    settings of each input file, the vasprun data of every dataset they use
+    (atomic energies subtracted, dataset.py:295-310) as arrays, and the errors
+    each test asserts per dataset."""
     import glob
 
     import numpy as np
 
-    cases, data_done = {}, False
+    cases, arrays = {}, {}
     test_src = os.path.join(FIT_DIR, "test_mlp_devel_vasp.py")
-    for cid, (infile, test_fn, helper) in FIT_CASES.items():
+    for cid, (infile, test_fn, helper, names) in FIT_CASES.items():
         inp = _read_input(os.path.join(FIT_DIR, infile))
         elements = inp["elements"]
-        if not data_done:
-            atom_e = np.array([float(v) for v in inp["atomic_energy"]])
-            arrays = {}
-            for tag in ("train", "test"):
-                files = sorted(glob.glob(os.path.join(FIT_DIR, inp[f"{tag}_data"][0])))
-                rows = [_vasprun(f, elements) for f in files]
-                e = np.array([r[3] - np.bincount(r[2], minlength=len(elements)) @ atom_e for r in rows])
-                arrays.update({f"{tag}_n_atoms": np.array([len(r[2]) for r in rows]),
-                               f"{tag}_axis": np.array([r[0] for r in rows]),
-                               f"{tag}_positions": np.concatenate([r[1] for r in rows]),
-                               f"{tag}_types": np.concatenate([r[2] for r in rows]), f"{tag}_energies": e,
-                               f"{tag}_forces": np.concatenate([r[4] for r in rows]),
-                               f"{tag}_stresses": np.array([r[5] for r in rows])})
-                print(tag, len(files), "structures")
-            np.savez_compressed(os.path.join(OUT, "fit_MgO.npz"), **arrays)
-            data_done = True
+        atom_e = np.array([float(v) for v in inp["atomic_energy"]])
+        for tag in names:
+            if f"{tag}_n_atoms" in arrays:
+                continue
+            files = sorted(glob.glob(os.path.join(FIT_DIR, FIT_DATA.format(tag))))
+            rows = [_vasprun(f, elements) for f in files]
+            e = np.array([r[3] - np.bincount(r[2], minlength=len(elements)) @ atom_e for r in rows])
+            arrays.update({f"{tag}_n_atoms": np.array([len(r[2]) for r in rows]),
+                           f"{tag}_axis": np.array([r[0] for r in rows]),
+                           f"{tag}_positions": np.concatenate([r[1] for r in rows]),
+                           f"{tag}_types": np.concatenate([r[2] for r in rows]), f"{tag}_energies": e,
+                           f"{tag}_forces": np.concatenate([r[4] for r in rows]),
+                           f"{tag}_stresses": np.array([r[5] for r in rows])})
+            print(tag, len(files), "structures")
         fit = _function(test_src, test_fn)
         n_features = next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
                           if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
@@ -255,8 +253,11 @@ def fit_known_answers():
             st["gtinv_order"] = int(inp["gtinv_order"][0])
             st["gtinv_maxl"] = [int(v) for v in inp["gtinv_maxl"]]
         cases[cid] = {"test": f"tests/test_mlp_dev_api/test_mlp_devel_vasp.py::{test_fn}", "settings": st,
-                      "errors": _fit_errors(_function(test_src, helper)), "data": "fit_MgO.npz"}
+                      "train": [n for n in names if n.startswith("train")],
+                      "test_sets": [n for n in names if n.startswith("test")],
+                      "errors": _fit_errors(_function(test_src, helper), names), "data": "fit_MgO.npz"}
         print(cid, cases[cid]["errors"])
+    np.savez_compressed(os.path.join(OUT, "fit_MgO.npz"), **arrays)
     with open(os.path.join(OUT, "known_fit.json"), "w") as f:
         json.dump({"cases": cases}, f, indent=1)
 

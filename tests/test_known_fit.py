@@ -1,7 +1,8 @@
 """Known answers of the reference's end-to-end fit tests
 (tests/test_mlp_dev_api/test_mlp_devel_vasp.py: a pair and a gtinv model of MgO
-fitted to 270 vasprun structures and tested on 30; data and asserted errors
-copied by tests/golden/make_known_answers.py).  The regression pipeline restated
+fitted to 270 vasprun structures and tested on 30, and the gtinv model fitted
+to two datasets (270 + 630) and tested on two (30 + 70); data and asserted
+errors copied by tests/golden/make_known_answers.py).  The regression pipeline restated
 on the CPU (oracle X rows, numpy Gram, LAPACK posv, the reference's weights,
 scales and alpha selection) and the GPU fit (FP64) must give the asserted
 train/test errors: energy 1e-8 eV/atom, force 1e-6 eV/A, stress 1e-5 eV/atom
@@ -26,18 +27,19 @@ def _cases():
 
 
 def _datasets(case):
+    """(training datasets, test datasets) of a case, named as in its error table."""
     z = np.load(os.path.join(KA, case["data"]))
     stress = case["settings"]["include_stress"]
-    out = []
-    for tag in ("train", "test"):
+
+    def one(tag):
         n = z[f"{tag}_n_atoms"]
         offs = np.concatenate([[0], np.cumsum(n)])
         sl = [slice(offs[i], offs[i + 1]) for i in range(len(n))]
-        out.append(Dataset([a for a in z[f"{tag}_axis"]], [z[f"{tag}_positions"][s] for s in sl],
-                           [z[f"{tag}_types"][s] for s in sl], z[f"{tag}_energies"],
-                           [z[f"{tag}_forces"][s] for s in sl], z[f"{tag}_stresses"], include_stress=stress,
-                           name=tag))
-    return out
+        return Dataset([a for a in z[f"{tag}_axis"]], [z[f"{tag}_positions"][s] for s in sl],
+                       [z[f"{tag}_types"][s] for s in sl], z[f"{tag}_energies"],
+                       [z[f"{tag}_forces"][s] for s in sl], z[f"{tag}_stresses"], include_stress=stress, name=tag)
+
+    return [one(t) for t in case["train"]], [one(t) for t in case["test_sets"]]
 
 
 def _params(st):
@@ -66,15 +68,15 @@ def test_cpu_pipeline_reproduces_reference_fit_errors(name):
     p = _params(case["settings"])
     assert oracle.n_features(p) == case["settings"]["n_features"]
     train, test = _datasets(case)
-    xy = calc_xtx_xty_cpu(p, [train])
+    xy = calc_xtx_xty_cpu(p, train)
     coefs = solver_ridge_cpu(xy.xtx, xy.xty, case["settings"]["alphas"])
-    txy = calc_xtx_xty_cpu(p, [test], scales=xy.scales, min_energy=xy.min_energy)
+    txy = calc_xtx_xty_cpu(p, test, scales=xy.scales, min_energy=xy.min_energy)
     best = coefs[:, int(np.argmin(compute_rmse_seq(coefs, txy)))] / xy.scales
     errors = {}
-    for tag, d in (("train", train), ("test", test)):
+    for d in train + test:
         e, f, s = oracle.evaluate(p, best, Structures(d.axis, d.positions, d.types))
         offs = np.concatenate([[0], np.cumsum(d.total_n_atoms)])
-        errors[tag], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
+        errors[d.name], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
     _check(errors, case["errors"])
 
 
@@ -88,7 +90,7 @@ def test_gpu_fit_reproduces_reference_fit_errors(name):
     case = _cases()[name]
     p = _params(case["settings"])
     train, test = _datasets(case)
-    res = fit(p, [train], [test], case["settings"]["alphas"], precision=_ffi.PG_FP64)
+    res = fit(p, train, test, case["settings"]["alphas"], precision=_ffi.PG_FP64)
     acc = PolymlpEvalAccuracy(p, res.scaled_coeffs)
-    errors = {tag: acc.compute_error_single(d, log_energy=False) for tag, d in (("train", train), ("test", test))}
+    errors = {d.name: acc.compute_error_single(d, log_energy=False) for d in train + test}
     _check(errors, case["errors"])
