@@ -17,7 +17,9 @@ shape, sum and first-minus-second-row sum of the energy rows of X for two MgO
 cells (known_x.json).  It also writes the invariant tables the gtinv
 potentials need with the reference's Readgtinv (oracle/_ref), the radial
 function and Y_lm values of tests/test_cxx/test_functions.py
-(known_functions.json), and the MgO pair and gtinv fits of
+(known_functions.json), the neighbour-list and cell-translation values of
+tests/test_cxx/test_neighbor*.py (known_neighbors.json), and the MgO pair and
+gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
 """
@@ -262,6 +264,72 @@ def fit_known_answers():
         json.dump({"cases": cases}, f, indent=1)
 
 
+# neighbour-list known answers (tests/test_cxx/test_neighbor*.py)
+# (types in the POSCAR's element order, as the reference's Poscar reader gives them)
+NEIGHBOR_TESTS = {"test_neighbor.py": "POSCAR-rocksalt", "test_neighbor_variants.py": "POSCAR-BiGd2"}
+
+
+def _neighbor_expr(node):
+    """(variable, indices, op, arg) of the left side of a neighbour-test assert."""
+    def chain(n):
+        idx = []
+        while isinstance(n, ast.Subscript):
+            idx.insert(0, ast.literal_eval(n.slice))
+            n = n.value
+        return n.id, idx
+
+    if isinstance(node, ast.Call):
+        f = node.func
+        name = f.id if isinstance(f, ast.Name) else f.attr
+        arg = node.args[0]
+        if name == "len":
+            return (*chain(arg), "len", None)
+        if name == "sum":
+            if isinstance(arg, ast.Call) and getattr(arg.func, "attr", "") == "square":
+                return (*chain(arg.args[0]), "sumsq", None)
+            return (*chain(arg), "sum", None)
+        if name == "count_nonzero":
+            inner = arg
+            return (*chain(inner.args[0]), "count_close", ast.literal_eval(inner.args[1]))
+    if isinstance(node, ast.Attribute) and node.attr == "shape":
+        return (*chain(node.value.args[0]), "shape", None)
+    if isinstance(node, ast.Subscript):
+        return (*chain(node), "item", None)
+    return None
+
+
+def neighbor_answers():
+    out = {}
+    for fname, poscar in NEIGHBOR_TESTS.items():
+        tree = ast.parse(open(os.path.join("/root/reference/tests/test_cxx", fname)).read())
+        for fn in tree.body:
+            if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
+                continue
+            ctor, cutoff, attrs, checks = None, None, {}, []
+            for st in fn.body:
+                if isinstance(st, ast.Assign) and isinstance(st.value, ast.Call) and \
+                        getattr(st.value.func, "id", "").startswith("Neighbor"):
+                    ctor = st.value.func.id
+                    cutoff = ast.literal_eval({k.arg: k.value for k in st.value.keywords}["cutoff"])
+                elif isinstance(st, ast.Assign) and isinstance(st.value, ast.Attribute) and \
+                        getattr(st.value.value, "id", "") == "neigh":
+                    attrs[st.targets[0].id] = st.value.attr
+                elif isinstance(st, ast.Assert) and isinstance(st.test, ast.Compare):
+                    e = _neighbor_expr(st.test.left)
+                    if e is None or e[0] not in attrs:
+                        continue
+                    cmpv = st.test.comparators[0]
+                    approx = isinstance(cmpv, ast.Call)
+                    val = ast.literal_eval(cmpv.args[0] if approx else cmpv)
+                    checks.append({"ctor": ctor, "cutoff": cutoff, "attr": attrs[e[0]], "idx": e[1], "op": e[2],
+                                   "arg": e[3], "expect": list(val) if isinstance(val, tuple) else val,
+                                   "approx": approx})
+            if checks:
+                out[f"{fname}::{fn.name}"] = {"structure": poscar, "checks": checks}
+        shutil.copyfile(os.path.join("/root/reference/tests/files", poscar), os.path.join(OUT, poscar))
+    return out
+
+
 def gtinv_spec(path):
     """(order, maxl) of a gtinv potential file, None for a pair potential."""
     lines = open(path).read().splitlines()
@@ -326,6 +394,10 @@ def main():
     with open(os.path.join(OUT, "known_functions.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_functions.py", "cases": function_answers()}, f, indent=1)
     print("wrote known_functions.json")
+    nb = neighbor_answers()
+    with open(os.path.join(OUT, "known_neighbors.json"), "w") as f:
+        json.dump({"source": "tests/test_cxx/test_neighbor*.py", "cases": nb}, f, indent=1)
+    print("wrote known_neighbors.json:", {k: len(v["checks"]) for k, v in nb.items()})
     fit_known_answers()
     for order, maxl in sorted(tables):
         l_comb, lm_seq, lm_coeffs = ref.readgtinv(order, maxl)
