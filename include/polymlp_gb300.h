@@ -92,6 +92,17 @@ int pg_model_feature_attrs(const pg_model* m, int* n_linear, int* radial_ids, in
                            int* n_poly, int* n_poly_values, int* poly_offsets, int* poly_values);
 
 /*
+ * The same attributes from the feature parameters alone, host only (no
+ * device, no model handle), as the FeaturesAttr constructor
+ * (src/pypolymlp/cxx/src/compute/py_features_attr.cpp:11-41).  type_pairs, if
+ * non-NULL, receives the n_type x n_type type-pair ids, row-major
+ * (FeaturesAttr::get_type_pairs).  gtinv_ids are -1 for pair features.
+ */
+int pg_feature_attrs(const pg_feature_params* fp, int* n_linear, int* radial_ids, int* gtinv_ids,
+                     int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,
+                     int* n_poly_values, int* poly_offsets, int* poly_values, int* type_pairs);
+
+/*
  * X rows of a batch of structures, as PotentialModel
  * (src/pypolymlp/cxx/src/compute/py_model.cpp:10-56 with Model::run,
  *  src/pypolymlp/cxx/src/compute/model.cpp:39).  For structure s, the energy

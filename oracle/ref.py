@@ -157,6 +157,15 @@ def feature_attrs(params_dict):
     return rad[:nl.value].tolist(), gt[:nl.value].tolist(), tcomb, poly
 
 
+def type_pairs(params_dict):
+    """FeaturesAttr::get_type_pairs: [t1][t2] -> type-pair id."""
+    lib = _load()
+    n = int(params_dict["n_type"])
+    out = np.zeros(n * n, np.int32)
+    _check(lib.ref_type_pairs(FeatureParams(params_dict).ref(), _p(out, C.c_int)))
+    return out.reshape(n, n).tolist()
+
+
 def parse_potential(path: str, legacy: bool = False) -> dict:
     """A model file read by the reference's own C++ parsers (ref_parse_potential):
     {elements, cutoff, pair_type, feature_type, model_type, max_p, max_l,

@@ -255,6 +255,18 @@ int ref_readgtinv(int order, const int* maxl, int n_maxl, int version, int* size
     });
 }
 
+// FeaturesAttr::get_type_pairs (py_features_attr.cpp:19): n_type x n_type, row-major.
+int ref_type_pairs(const pg_feature_params* p, int* out) {
+    return guarded([&] {
+        const feature_params fp = to_fp(p);
+        PolymlpAPI api;
+        api.set_model_parameters(fp);
+        const auto& tps = api.get_maps().type_pairs;
+        for (size_t a = 0; a < tps.size(); ++a)
+            for (size_t b = 0; b < tps[a].size(); ++b) out[a * tps.size() + b] = tps[a][b];
+    });
+}
+
 // FeaturesAttr-equivalent sizes and ids (py_features_attr.cpp:11-45).
 int ref_feature_attrs(const pg_feature_params* p, int* n_linear, int* radial_ids, int* gtinv_ids,
                       int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,

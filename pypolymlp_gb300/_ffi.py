@@ -49,6 +49,7 @@ def lib():
             L.pg_model_destroy.argtypes = [_vp]
             L.pg_model_n_features.argtypes = [_vp, _ip]
             L.pg_model_feature_attrs.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip]
+            L.pg_feature_attrs.argtypes = [_vp, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip]
             L.pg_features_x.argtypes = [_vp, _vp, _i64p, _i64p, _i64p, _dp, C.c_int64, C.c_int]
             L.pg_neighbor_list.argtypes = [_vp, C.c_int, C.c_double, C.c_int, _i64p, _ip, _ip, _dp]
             for name, args in [

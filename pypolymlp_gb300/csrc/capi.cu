@@ -635,52 +635,63 @@ int pg_model_n_features(const pg_model* m, int* n) {
     });
 }
 
+namespace {
+
+// Flattened FeatureAttrs into the caller's arrays (sizes always written;
+// arrays filled when radial_ids is non-null).
+void write_feature_attrs(const pg::ModelTables& mt, int* n_linear, int* radial_ids, int* gtinv_ids,
+                         int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,
+                         int* n_poly_values, int* poly_offsets, int* poly_values) {
+    if (!n_linear || !n_tcomb_values || !n_poly || !n_poly_values) throw std::runtime_error("null size output");
+    const pg::FeatureAttrs a = pg::feature_attrs(mt);
+    int ntv = 0, npv = 0;
+    for (const auto& v : a.tcomb_ids) ntv += (int)v.size();
+    for (const auto& v : a.polynomial_ids) npv += (int)v.size();
+    *n_linear = (int)a.radial_ids.size();
+    *n_tcomb_values = ntv;
+    *n_poly = (int)a.polynomial_ids.size();
+    *n_poly_values = npv;
+    if (!radial_ids) return;
+    if (!tcomb_offsets || !tcomb_values || !poly_offsets || !poly_values) throw std::runtime_error("null array output");
+    int k = 0;
+    tcomb_offsets[0] = 0;
+    for (size_t i = 0; i < a.radial_ids.size(); ++i) {
+        radial_ids[i] = a.radial_ids[i];
+        if (gtinv_ids) gtinv_ids[i] = a.gtinv_ids.empty() ? -1 : a.gtinv_ids[i];
+        for (int v : a.tcomb_ids[i]) tcomb_values[k++] = v;
+        tcomb_offsets[i + 1] = k;
+    }
+    k = 0;
+    poly_offsets[0] = 0;
+    for (size_t i = 0; i < a.polynomial_ids.size(); ++i) {
+        for (int v : a.polynomial_ids[i]) poly_values[k++] = v;
+        poly_offsets[i + 1] = k;
+    }
+}
+
+}  // namespace
+
 int pg_model_feature_attrs(const pg_model* m, int* n_linear, int* radial_ids, int* gtinv_ids, int* n_tcomb_values,
                            int* tcomb_offsets, int* tcomb_values, int* n_poly, int* n_poly_values,
                            int* poly_offsets, int* poly_values) {
     return guarded([&] {
         if (!m) throw std::runtime_error("null model");
-        const ModelTables& mt = m->m->tables;
-        std::vector<int> rad, gt;
-        std::vector<std::vector<int>> tc, poly;
-        if (!mt.fp.gtinv) {
-            // ntp attributes in global order (py_features_attr.cpp:23-28)
-            for (int tp = 0; tp < mt.n_type_pairs; ++tp)
-                for (int n : mt.tp_to_n[tp]) {
-                    rad.push_back(n);
-                    tc.push_back({tp});
-                }
-        } else {
-            for (const auto& lt : mt.linear_terms) {
-                rad.push_back(lt.n);
-                gt.push_back(lt.lm_comb_id);
-                tc.push_back(mt.tp_combs[lt.order][lt.tp_comb_id]);
-            }
-        }
-        for (const auto& c : mt.comb2) poly.push_back(c);
-        for (const auto& c : mt.comb3) poly.push_back(c);
-        int ntv = 0, npv = 0;
-        for (const auto& v : tc) ntv += (int)v.size();
-        for (const auto& v : poly) npv += (int)v.size();
-        *n_linear = (int)rad.size();
-        *n_tcomb_values = ntv;
-        *n_poly = (int)poly.size();
-        *n_poly_values = npv;
-        if (!radial_ids) return;
-        int k = 0;
-        tcomb_offsets[0] = 0;
-        for (size_t i = 0; i < rad.size(); ++i) {
-            radial_ids[i] = rad[i];
-            if (gtinv_ids) gtinv_ids[i] = gt.empty() ? -1 : gt[i];
-            for (int v : tc[i]) tcomb_values[k++] = v;
-            tcomb_offsets[i + 1] = k;
-        }
-        k = 0;
-        poly_offsets[0] = 0;
-        for (size_t i = 0; i < poly.size(); ++i) {
-            for (int v : poly[i]) poly_values[k++] = v;
-            poly_offsets[i + 1] = k;
-        }
+        write_feature_attrs(m->m->tables, n_linear, radial_ids, gtinv_ids, n_tcomb_values, tcomb_offsets,
+                            tcomb_values, n_poly, n_poly_values, poly_offsets, poly_values);
+    });
+}
+
+int pg_feature_attrs(const pg_feature_params* fp, int* n_linear, int* radial_ids, int* gtinv_ids,
+                     int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,
+                     int* n_poly_values, int* poly_offsets, int* poly_values, int* type_pairs) {
+    return guarded([&] {
+        if (!fp) throw std::runtime_error("null feature params");
+        const pg::ModelTables mt = pg::build_model_tables(pg::feature_params_from_abi(fp));
+        write_feature_attrs(mt, n_linear, radial_ids, gtinv_ids, n_tcomb_values, tcomb_offsets, tcomb_values,
+                            n_poly, n_poly_values, poly_offsets, poly_values);
+        if (type_pairs)
+            for (int a = 0; a < mt.fp.n_type; ++a)
+                for (int b = 0; b < mt.fp.n_type; ++b) type_pairs[a * mt.fp.n_type + b] = mt.type_pairs[a][b];
     });
 }
 

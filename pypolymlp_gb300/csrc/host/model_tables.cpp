@@ -530,4 +530,25 @@ std::vector<std::vector<std::vector<PotTerm>>> build_potential_terms(const Model
     return out;
 }
 
+FeatureAttrs feature_attrs(const ModelTables& mt) {
+    FeatureAttrs a;
+    if (!mt.fp.gtinv) {
+        // ntp attributes in global (type pair, radial) order
+        for (int tp = 0; tp < mt.n_type_pairs; ++tp)
+            for (int n : mt.tp_to_n[tp]) {
+                a.radial_ids.push_back(n);
+                a.tcomb_ids.push_back({tp});
+            }
+    } else {
+        for (const auto& lt : mt.linear_terms) {
+            a.radial_ids.push_back(lt.n);
+            a.gtinv_ids.push_back(lt.lm_comb_id);
+            a.tcomb_ids.push_back(mt.tp_combs[lt.order][lt.tp_comb_id]);
+        }
+    }
+    for (const auto& c : mt.comb2) a.polynomial_ids.push_back(c);
+    for (const auto& c : mt.comb3) a.polynomial_ids.push_back(c);
+    return a;
+}
+
 }  // namespace pg

@@ -117,6 +117,17 @@ struct ModelTables {
 // the reference calls exit(8)).
 ModelTables build_model_tables(const FeatureParams& fp);
 
+// Feature attributes as FeaturesAttr returns them
+// (src/pypolymlp/cxx/src/compute/py_features_attr.cpp:11-60): per linear
+// feature its radial id, invariant id (-1 for pair features) and type
+// combination (type-pair ids); then the polynomial columns as lists of linear
+// ids (second order, then third order).
+struct FeatureAttrs {
+    std::vector<int> radial_ids, gtinv_ids;
+    std::vector<std::vector<int>> tcomb_ids, polynomial_ids;
+};
+FeatureAttrs feature_attrs(const ModelTables& mt);
+
 // Evaluator terms (reference Potential::set_terms_using_mapping).  For gtinv
 // the heads are no-conjugate local ids; for pair they are ntp local ids.
 // Coefficients are used as given (the reference's 2x factor is applied by

@@ -11,8 +11,8 @@ comments, elements line tagged "# element").  `load_mlp_yaml`,
 `load_mlp_lammps` and `load_mlp` (dispatch on the legacy tag,
 io_polymlp.py:59-76, 142-156) read both back as a params dict of the form
 `make_params_dict` builds and the coefficients divided by the scales.  The
-invariant tables of a gtinv model come from the committed tables
-(`params.load_gtinv`), so a file loads when its (gtinv order, l_max) has one.
+invariant tables of a gtinv model are screened from the reference's basis
+for the file's gtinv order, l_max and version (`gtinv.Readgtinv`).
 """
 
 from __future__ import annotations

@@ -7,38 +7,24 @@ parameters as ``set_gaussian_params`` makes them (product of two linspaces,
 plus the constant (0, 0) function appended at the end, params_utils.py:69-93),
 and every radial function active for every type pair.  The gtinv tables
 (l_comb, lm_seq, lm_coeffs) are the reference's invariant tables for the
-chosen order and l_max; they are loaded from JSON files written from the
-reference's Readgtinv (tests/golden/gtinv/).
+chosen order and l_max, screened from the reference's basis by
+`gtinv.Readgtinv` (src/pypolymlp/cxx/src/polymlp/polymlp_read_gtinv.cpp:12).
 """
 
 from __future__ import annotations
 
 import itertools
 import json
-import os
 from typing import Optional, Sequence
 
 import numpy as np
 
-_REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-GTINV_DIR = os.path.join(_REPO, "tests", "golden", "gtinv")
-
-
-def gtinv_file(order: int, maxl: Sequence[int], version: int = 1) -> str:
-    tag = "_".join(str(int(v)) for v in list(maxl)[: max(order - 1, 0)])
-    return os.path.join(GTINV_DIR, f"gtinv_v{version}_order{order}_maxl{tag}.json")
+from pypolymlp_gb300.gtinv import get_gtinv_attrs
 
 
 def load_gtinv(order: int, maxl: Sequence[int], version: int = 1):
-    path = gtinv_file(order, maxl, version)
-    if not os.path.exists(path):
-        raise FileNotFoundError(
-            f"gtinv tables for order={order} maxl={tuple(maxl)} not found at {path}; "
-            "generate them with tests/golden/make_golden.py where the reference is available"
-        )
-    with open(path) as f:
-        d = json.load(f)
-    return d["l_comb"], d["lm_seq"], d["lm_coeffs"]
+    """(l_comb, lm_seq, lm_coeffs) of the invariants up to `order` (gtinv.Readgtinv)."""
+    return get_gtinv_attrs(order, maxl, version)
 
 
 def gaussian_params(params1=(1.0, 1.0, 1), params2=(0.0, 5.0, 7)):
@@ -60,6 +46,7 @@ def make_params_dict(
     gtinv_order: int = 3,
     gtinv_maxl: Sequence[int] = (4, 4, 2, 1, 1),
     gtinv_tables: Optional[tuple] = None,
+    gtinv_version: int = 1,
     elements: Optional[Sequence[str]] = None,
     include_force: bool = True,
     include_stress: bool = True,
@@ -72,7 +59,7 @@ def make_params_dict(
             cond[(i, j)] = list(range(len(pair_params)))
     if feature_type == "gtinv":
         if gtinv_tables is None:
-            gtinv_tables = load_gtinv(gtinv_order, gtinv_maxl)
+            gtinv_tables = load_gtinv(gtinv_order, gtinv_maxl, gtinv_version)
         l_comb, lm_seq, lm_coeffs = gtinv_tables
         max_l = int(max(gtinv_maxl[: max(gtinv_order - 1, 1)])) if gtinv_order > 1 else 0
         gtinv = {
@@ -82,7 +69,7 @@ def make_params_dict(
             "lm_seq": lm_seq,
             "l_comb": l_comb,
             "lm_coeffs": lm_coeffs,
-            "version": 1,
+            "version": gtinv_version,
         }
     else:
         max_l = 0

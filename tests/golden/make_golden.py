@@ -30,7 +30,14 @@ sys.path.insert(0, REPO)
 from oracle import ref  # noqa: E402
 from pypolymlp_gb300 import synthetic as syn  # noqa: E402
 from pypolymlp_gb300.abi import Structures, row_layout  # noqa: E402
-from pypolymlp_gb300.params import gtinv_file, make_params_dict, to_json  # noqa: E402
+from pypolymlp_gb300.params import make_params_dict, to_json  # noqa: E402
+
+def gtinv_file(order, maxl, version=1):
+    """Fixture path of the reference's Readgtinv output for (order, l_max per order)."""
+    tag = "_".join(str(int(v)) for v in list(maxl)[: max(order - 1, 0)])
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "gtinv",
+                        f"gtinv_v{version}_order{order}_maxl{tag}.json")
+
 
 CONFIGS = {
     "cfg1": dict(n_type=1, cutoff=6.0, model_type=2, max_p=2, gaussian_params2=(0.0, 5.0, 8), gtinv_order=2,

@@ -330,6 +330,13 @@ def neighbor_answers():
     return out
 
 
+def gtinv_file(order, maxl, version=1):
+    """Fixture path of the reference's Readgtinv output for (order, l_max per order)."""
+    tag = "_".join(str(int(v)) for v in list(maxl)[: max(order - 1, 0)])
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "gtinv",
+                        f"gtinv_v{version}_order{order}_maxl{tag}.json")
+
+
 def gtinv_spec(path):
     """(order, maxl) of a gtinv potential file, None for a pair potential."""
     lines = open(path).read().splitlines()
@@ -350,7 +357,6 @@ def gtinv_spec(path):
 
 def main():
     from oracle import ref
-    from pypolymlp_gb300.params import gtinv_file
 
     os.makedirs(OUT, exist_ok=True)
     cases, tables = {}, set()
