@@ -6,8 +6,9 @@ host by `pg_feature_attrs` from the same model tables the GPU kernels use (no
 device needed).  Per linear feature: its radial function id, its invariant id
 (gtinv models; the index into gtinv.l_comb) and its type combination (type-pair
 ids); then the polynomial columns as lists of linear-feature ids.
-`get_features_attr` and `get_num_features` follow
-src/pypolymlp/mlp_dev/core/features_attr.py:12-48, on params dictionaries.
+`get_features_attr`, `get_num_features` and `write_polymlp_params_yaml`
+follow src/pypolymlp/mlp_dev/core/features_attr.py:12-133, on params
+dictionaries.
 """
 
 from __future__ import annotations
@@ -91,3 +92,58 @@ def get_num_features(params: Union[dict, Sequence[dict]]) -> int:
         features_attr, polynomial_attr, _ = get_features_attr(p)
         total += len(features_attr) + len(polynomial_attr)
     return total
+
+
+def _write_params_yaml(params_dict: dict, filename: str) -> int:
+    features_attr, polynomial_attr, atomtype_pair_dict = get_features_attr(params_dict)
+    model = params_dict["model"]
+    elements = list(params_dict["elements"])
+    with open(filename, "w") as f:
+        print("radial_params:", file=f)
+        for i, p in enumerate(model["pair_params"]):
+            print("- radial_id: ", i, file=f)
+            print("  params:    ", [float(v) for v in p], file=f)
+            print("", file=f)
+        print("", file=f)
+        print("atomtype_pairs:", file=f)
+        for k, v in atomtype_pair_dict.items():
+            print("- pair_id:       ", k, file=f)
+            print("  pair_elements: ", file=f)
+            for t1, t2 in v:
+                print("  - ", [elements[t1], elements[t2]], file=f)
+            print("", file=f)
+        print("", file=f)
+        print("features:", file=f)
+        seq_id = 0
+        for i, attr in enumerate(features_attr):
+            print("- id:               ", seq_id, file=f)
+            print("  feature_id:       ", i, file=f)
+            print("  radial_id:        ", attr[0], file=f)
+            if model["feature_type"] == "gtinv":
+                print("  gtinv_id:         ", attr[1], file=f)
+                print("  l_combination:    ", list(model["gtinv"]["l_comb"][attr[1]]), file=f)
+            print("  atomtype_pair_ids:", attr[-1], file=f)
+            print("", file=f)
+            seq_id += 1
+        print("", file=f)
+        if polynomial_attr:
+            print("polynomial_features:", file=f)
+            for attr in polynomial_attr:
+                print("- id:          ", seq_id, file=f)
+                print("  feature_ids: ", attr, file=f)
+                print("", file=f)
+                seq_id += 1
+    return seq_id
+
+
+def write_polymlp_params_yaml(params: Union[dict, Sequence[dict]], filename: str = "polymlp_params.yaml") -> int:
+    """Write the column attributes of X as polymlp_params.yaml, in the layout of
+    src/pypolymlp/mlp_dev/core/features_attr.py:51-133: radial parameters, the
+    element pairs of each type pair, one entry per linear feature (radial id,
+    invariant id and l combination for gtinv models, type-pair ids), then the
+    polynomial columns; ids run over all columns.  A hybrid (list of params
+    dicts) writes polymlp_params1.yaml, polymlp_params2.yaml, ...  Returns the
+    number of columns."""
+    if isinstance(params, dict):
+        return _write_params_yaml(params, filename)
+    return sum(_write_params_yaml(p, f"polymlp_params{i + 1}.yaml") for i, p in enumerate(params))

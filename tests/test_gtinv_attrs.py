@@ -139,3 +139,37 @@ def test_num_features_of_a_hybrid_sums_the_models():
 
     a, b = _attr_params("pair_binary_mt1_p3"), _attr_params("pair_ternary_mt2")
     assert get_num_features([a, b]) == get_num_features(a) + get_num_features(b)
+
+
+@pytest.mark.parametrize("name", ["pair_binary_mt1_p3", "pair_ternary_mt2", "gtinv_quaternary_o3_mt3"])
+def test_polymlp_params_yaml_lists_every_column(tmp_path, name, monkeypatch):
+    """polymlp_params.yaml (features_attr.py:51-117 layout): one entry per column,
+    ids consecutive, linear entries carrying FeaturesAttr's radial/gtinv/type-pair ids."""
+    import ast
+
+    from pypolymlp_gb300.features_attr import get_features_attr, write_polymlp_params_yaml
+
+    p = _attr_params(name)
+    out = str(tmp_path / "polymlp_params.yaml")
+    n = write_polymlp_params_yaml(p, out)
+    lin, poly, tp_dict = get_features_attr(p)
+    assert n == len(lin) + len(poly)
+    ids, radial, tps, feats = [], [], [], []
+    for line in open(out).read().splitlines():
+        key, _, val = line.strip().lstrip("- ").partition(":")
+        if key == "id":
+            ids.append(int(val))
+        elif key == "radial_id" and line.startswith("  "):
+            radial.append(int(val))
+        elif key == "atomtype_pair_ids":
+            tps.append(ast.literal_eval(val.strip()))
+        elif key == "feature_ids":
+            feats.append(ast.literal_eval(val.strip()))
+    assert ids == list(range(n))
+    assert radial == [a[0] for a in lin] and tps == [list(a[-1]) for a in lin] and feats == poly
+    text = open(out).read()
+    assert text.count("- pair_id:") == len(tp_dict) and text.count("- radial_id:") == len(p["model"]["pair_params"])
+    # a hybrid writes one numbered file per model into the working directory
+    monkeypatch.chdir(tmp_path)
+    assert write_polymlp_params_yaml([p, p]) == 2 * n
+    assert (tmp_path / "polymlp_params1.yaml").exists() and (tmp_path / "polymlp_params2.yaml").exists()
