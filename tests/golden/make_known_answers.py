@@ -18,8 +18,9 @@ cells (known_x.json).  It also writes the invariant tables the gtinv
 potentials need with the reference's Readgtinv (oracle/_ref), the radial
 function and Y_lm values of tests/test_cxx/test_functions.py
 (known_functions.json), the neighbour-list and cell-translation values of
-tests/test_cxx/test_neighbor*.py (known_neighbors.json), and the MgO pair and
-gtinv fits of
+tests/test_cxx/test_neighbor*.py (known_neighbors.json), the invariant-table
+values of tests/test_cxx/test_gtinv.py (known_gtinv.json), and the MgO pair
+and gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
 """
@@ -137,6 +138,38 @@ def function_answers():
             case["tables"] = {k: [[complex(v).real, complex(v).imag] for v in t] for k, t in tables.items()}
             case["tables_atol"] = 1e-7
         out[name] = case
+    return out
+
+
+def gtinv_answers():
+    """Invariant-table requests of tests/test_cxx/test_gtinv.py and their asserted
+    values: (kind, index path, expected, approx) per assert."""
+    tree = ast.parse(open("/root/reference/tests/test_cxx/test_gtinv.py").read())
+    out = {}
+    for fn in tree.body:
+        if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
+            continue
+        call = next(n for n in ast.walk(fn) if isinstance(n, ast.Call) and getattr(n.func, "id", "") == "get_gtinv_attrs")
+        kw = {k.arg: ast.literal_eval(k.value) for k in call.keywords}
+        checks = []
+        for st in fn.body:
+            if not (isinstance(st, ast.Assert) and isinstance(st.test, ast.Compare)):
+                continue
+            left, right = st.test.left, st.test.comparators[0]
+            approx = isinstance(right, ast.Call)
+            want = ast.literal_eval(right.args[0] if approx else right)
+            if isinstance(left, ast.Call):   # len(x) or tuple(x[i]...)
+                kind = left.func.id
+                node = left.args[0]
+            else:
+                kind, node = "item", left
+            idx = []
+            while isinstance(node, ast.Subscript):
+                idx.insert(0, ast.literal_eval(node.slice))
+                node = node.value
+            checks.append({"name": node.id, "kind": kind, "idx": idx,
+                           "expect": list(want) if isinstance(want, tuple) else want, "approx": approx})
+        out[fn.name] = {"order": kw["order"], "lmax": kw["lmax"], "version": kw["version"], "checks": checks}
     return out
 
 
@@ -400,6 +433,9 @@ def main():
     with open(os.path.join(OUT, "known_functions.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_functions.py", "cases": function_answers()}, f, indent=1)
     print("wrote known_functions.json")
+    with open(os.path.join(OUT, "known_gtinv.json"), "w") as f:
+        json.dump({"source": "tests/test_cxx/test_gtinv.py", "cases": gtinv_answers()}, f, indent=1)
+    print("wrote known_gtinv.json")
     nb = neighbor_answers()
     with open(os.path.join(OUT, "known_neighbors.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_neighbor*.py", "cases": nb}, f, indent=1)
