@@ -31,6 +31,9 @@ def active_atoms(types, params_dict: dict):
     types = np.asarray(types, dtype=np.int64)
     if params_dict.get("type_full", True) in (True, 1, None):
         return np.arange(len(types)), types
+    if params_dict.get("spin_elements"):
+        # the reference has no partial models with spins (properties_utils.py:14-16)
+        raise RuntimeError("Not available for system with spin configurations.")
     order = [int(t) for t in params_dict["type_indices"]]
     lookup = {t: k for k, t in enumerate(order)}
     idx = np.array([a for a, t in enumerate(types) if int(t) in lookup], dtype=np.int64)

@@ -23,7 +23,7 @@ from typing import Optional, Sequence
 
 import numpy as np
 
-from pypolymlp_gb300.params import load_gtinv
+from pypolymlp_gb300.params import expand_spins, load_gtinv
 
 # Standard atomic weights (IUPAC, abridged) for the mass entry of the files.
 ATOMIC_MASS = {
@@ -51,14 +51,25 @@ def _masses(elements: Sequence[str], mass: Optional[Sequence[float]]):
 
 
 def _model_parts(params_dict: dict):
+    """(model, n_type, elements, type pairs with radial ids), element-level: for a
+    model with spins (params.expand_spins) the elements before the split, each
+    element pair taking the radial ids of its first types."""
     m = params_dict["model"]
-    n_type = int(params_dict["n_type"])
-    elements = list(params_dict.get("elements") or [f"E{i}" for i in range(n_type)])
+    sp = params_dict.get("spin_elements")
+    if sp:
+        elements = list(sp["elements"])
+        n_type = len(elements)
+        first = [int(t[0]) for t in sp["types"]]
+    else:
+        n_type = int(params_dict["n_type"])
+        elements = list(params_dict.get("elements") or [f"E{i}" for i in range(n_type)])
+        first = list(range(n_type))
     cond = m.get("pair_params_conditional") or {}
     pairs = []
     for i in range(n_type):
         for j in range(i, n_type):
-            ids = cond.get((i, j), cond.get(f"{i},{j}"))
+            a, b = first[i], first[j]
+            ids = cond.get((a, b), cond.get(f"{a},{b}"))
             if ids is None:
                 ids = list(range(len(m["pair_params"])))
             pairs.append(((i, j), [int(v) for v in ids]))
@@ -75,9 +86,12 @@ def save_mlp_yaml(params_dict: dict, coeffs, scales, filename: str = "polymlp.ya
     m, n_type, elements, pairs = _model_parts(params_dict)
     c = np.asarray(coeffs, dtype=np.float64) / np.asarray(scales, dtype=np.float64)
     gt = m.get("gtinv") or {}
+    sp = params_dict.get("spin_elements")
+    spins = [int(bool(v)) for v in sp["enable_spins"]] if sp else [0] * n_type
+    type_elements = list(params_dict["elements"]) if sp else elements
     lines = [
         f"elements:      [{', '.join(str(e) for e in elements)}]",
-        f"enable_spins:  {_fmt_list([0] * n_type)}",
+        f"enable_spins:  {_fmt_list(spins)}",
         f"cutoff:        {float(m['cutoff'])!r}",
         f"pair_type:     {m.get('pair_type', 'gaussian')}",
         f"feature_type:  {m['feature_type']}",
@@ -97,7 +111,7 @@ def save_mlp_yaml(params_dict: dict, coeffs, scales, filename: str = "polymlp.ya
         ]
     lines += [
         "electrostatic: 0",
-        f"mass:          {_fmt_list(_masses(elements, mass))}",
+        f"mass:          {_fmt_list(_masses(type_elements, mass))}",
         "",
         f"n_pair_params: {len(m['pair_params'])}",
         "pair_params:",
@@ -117,6 +131,8 @@ def save_mlp_yaml(params_dict: dict, coeffs, scales, filename: str = "polymlp.ya
 def save_mlp_lammps(params_dict: dict, coeffs, scales, filename: str = "polymlp.lammps",
                     mass: Optional[Sequence[float]] = None) -> None:
     """Write the legacy polymlp.lammps format (coefficients and scales on separate lines)."""
+    if params_dict.get("spin_elements"):
+        raise ValueError("the legacy polymlp.lammps format has no spin entries: use save_mlp_yaml")
     m, n_type, elements, pairs = _model_parts(params_dict)
     c = np.asarray(coeffs, dtype=np.float64)
     s = np.asarray(scales, dtype=np.float64)
@@ -239,6 +255,8 @@ def load_mlp_yaml(filename: str = "polymlp.yaml"):
     p["mass"] = [float(v) for v in y.get("mass", [])]
     p["type_full"] = bool(y.get("type_full", 1))
     p["type_indices"] = [int(v) for v in y.get("type_indices", list(range(len(elements))))]
+    # spin-enabled elements become two atom types each (io_polymlp_yaml.py:111-116, 146-150)
+    expand_spins(p, y.get("enable_spins"))
     return p, np.asarray(y["coeffs"], dtype=np.float64)
 
 

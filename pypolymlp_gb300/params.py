@@ -51,6 +51,7 @@ def make_params_dict(
     include_force: bool = True,
     include_stress: bool = True,
     alphas: Optional[Sequence[float]] = None,
+    enable_spins: Optional[Sequence[bool]] = None,
 ) -> dict:
     pair_params = gaussian_params(gaussian_params1, gaussian_params2)
     cond = {}
@@ -77,7 +78,7 @@ def make_params_dict(
                  "lm_coeffs": [], "version": 1}
     if elements is None:
         elements = [f"E{i}" for i in range(n_type)]
-    return {
+    return expand_spins({
         "n_type": n_type,
         "elements": list(elements),
         "model": {
@@ -96,7 +97,46 @@ def make_params_dict(
         "include_stress": include_stress,
         "print_memory": False,
         "alphas": list(alphas) if alphas is not None else None,
-    }
+    }, enable_spins)
+
+
+def expand_spins(params_dict: dict, enable_spins: Optional[Sequence[bool]]) -> dict:
+    """Split every element with its spin enabled into two atom types (spin up and
+    down), as PolymlpParamsSingle._set_params_spins and
+    PolymlpModelParams.revise_params do (src/pypolymlp/core/data_format.py:291-320,
+    192-201): types are renumbered element by element, an enabled element taking two
+    consecutive types; elements are repeated; each element pair's radial ids go to
+    every pair of their types.  params_dict["n_type"] and ["elements"] are
+    element-level on entry.  The element-level settings are kept under
+    "spin_elements" (elements, enable_spins, per-element types) for the model
+    writers.  Without an enabled spin the dict is returned with
+    "enable_spins": None."""
+    if enable_spins is None or not any(bool(v) for v in enable_spins):
+        params_dict["enable_spins"] = None
+        return params_dict
+    elements = list(params_dict["elements"])
+    if len(enable_spins) != len(elements) or int(params_dict["n_type"]) != len(elements):
+        raise ValueError("enable_spins needs one flag per element")
+    map_types, new_elements, flags = [], [], []
+    for ele, spin in zip(elements, enable_spins):
+        types = [len(new_elements)] + ([len(new_elements) + 1] if spin else [])
+        map_types.append(types)
+        new_elements += [ele] * len(types)
+        flags += [bool(spin)] * len(types)
+    model = params_dict["model"]
+    cond = model.get("pair_params_conditional") or {}
+    revised = {}
+    for (a, b), ids in cond.items():
+        for t1 in map_types[a]:
+            for t2 in map_types[b]:
+                revised[tuple(sorted((t1, t2)))] = list(ids)
+    model["pair_params_conditional"] = revised
+    params_dict["spin_elements"] = {"elements": elements, "enable_spins": [bool(v) for v in enable_spins],
+                                    "types": map_types}
+    params_dict["n_type"] = len(new_elements)
+    params_dict["elements"] = new_elements
+    params_dict["enable_spins"] = flags
+    return params_dict
 
 
 def to_json(params_dict: dict) -> str:

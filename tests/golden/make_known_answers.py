@@ -31,6 +31,8 @@ import os
 import shutil
 import sys
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
@@ -58,7 +60,31 @@ CASES = {
     "SrTiO3_hybrid_yaml": ("test_properties_SrTiO3.py", "test_eval_flexible",
                            ["polymlp.yaml.flexible.1.SrTiO3", "polymlp.yaml.flexible.2.SrTiO3"],
                            "POSCAR.perovskite.SrTiO3", "f00", None),
+    # spin-polarised Fe (enable_spins: one element, two atom types), the cell is
+    # written in the test module; "zero": all forces are asserted to vanish
+    "Fe_spin_pair_yaml": ("test_properties_Fe.py", "test_eval1", ["polymlp.yaml.1.Fe"], None, "zero", "GPa"),
+    "Fe_spin_hybrid_yaml": ("test_properties_Fe.py", "test_eval2", ["polymlp.yaml.1.Fe", "polymlp.yaml.2.Fe"], None,
+                            "zero", "GPa"),
 }
+
+
+def _module_cell(path):
+    """axis (columns = lattice vectors), fractional positions (3, N) and types of
+    a test module's `axis = np.eye(3) * a`, `positions = np.array([...]).T`,
+    `types = [...]` assignments (read as syntax, not run)."""
+    found = {}
+    for node in ast.parse(open(path).read()).body:
+        if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name):
+            found[node.targets[0].id] = node.value
+    ax = found["axis"]
+    if not (isinstance(ax, ast.BinOp) and isinstance(ax.op, ast.Mult) and getattr(ax.left.func, "attr", "") == "eye"):
+        raise ValueError("unexpected axis expression")
+    axis = (np.eye(ast.literal_eval(ax.left.args[0])) * ast.literal_eval(ax.right)).tolist()
+    pos = found["positions"]
+    transpose = isinstance(pos, ast.Attribute) and pos.attr == "T"
+    arr = np.array(ast.literal_eval((pos.value if transpose else pos).args[0]), dtype=float)
+    frac = (arr.T if transpose else arr).tolist()
+    return {"axis": axis, "positions_frac": frac, "types": ast.literal_eval(found["types"])}
 
 
 def _function(path, name):
@@ -194,8 +220,6 @@ def _vasprun(path, elements):
     parameter file's element order (dataset_utils.py:225-245)."""
     import xml.etree.ElementTree as ET
 
-    import numpy as np
-
     root = ET.parse(path).getroot()
     arr = lambda v: np.array([[float(x) for x in e.text.split()] for e in v])  # noqa: E731
     energy = float(root.find("calculation").find("energy")[1].text)
@@ -252,8 +276,6 @@ def fit_known_answers():
     (atomic energies subtracted, dataset.py:295-310) as arrays, and the errors
     each test asserts per dataset."""
     import glob
-
-    import numpy as np
 
     cases, arrays = {}, {}
     test_src = os.path.join(FIT_DIR, "test_mlp_devel_vasp.py")
@@ -400,16 +422,18 @@ def main():
             e_val = _assigned(fn, "energy_true")
         case = {"test": f"tests/test_calc/{test}::{fname}", "potentials": pots, "structure": poscar,
                 "energy": e_val, "energy_tol": e_tol, "forces_kind": forces_kind, "forces_atol": 1e-6}
+        if poscar is None:
+            case["cell"] = _module_cell(os.path.join(REF, test))
         if forces_kind in ("NxT", "3xN"):
             f = _assigned(fn, "forces_true")
             case["forces"] = [list(r) for r in zip(*f)] if forces_kind == "3xN" else f
-        else:
+        elif forces_kind == "f00":
             case["forces_atol"] = 1e-12
         s = _assigned(fn, "stresses_true")
         if s_unit is not None and s is not None:
             case.update({"stresses": s, "stresses_unit": s_unit, "stresses_atol": 1e-5})
         cases[cid] = case
-        for name in pots + [poscar]:
+        for name in pots + ([poscar] if poscar else []):
             src = os.path.join(REF, "files", "mlps" if name.startswith("polymlp") else "poscars", name)
             shutil.copyfile(src, os.path.join(OUT, name))
         for p in pots:

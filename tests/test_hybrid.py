@@ -19,6 +19,11 @@ def test_active_atoms():
     assert idx.tolist() == [0, 1, 2, 3, 4] and tt.tolist() == t.tolist()
     idx, tt = active_atoms(t, {})
     assert idx.tolist() == [0, 1, 2, 3, 4]
+    # a spin model sees every atom, or none is chosen (properties_utils.py:14-16)
+    spin = {"type_full": False, "type_indices": [0], "spin_elements": {"elements": ["Fe"]}}
+    with pytest.raises(RuntimeError):
+        active_atoms(t, spin)
+    assert active_atoms(t, dict(spin, type_full=True))[0].tolist() == [0, 1, 2, 3, 4]
 
 
 def _hybrid():

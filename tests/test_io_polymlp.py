@@ -106,3 +106,45 @@ def test_convert_and_find(tmp_path):
     q, cq = io.load_mlp(out)
     _same_model(p, q)
     np.testing.assert_allclose(cq, c / s, rtol=1e-15)
+
+
+def test_spin_expansion_follows_revise_params():
+    """enable_spins splits an element into two consecutive types and gives every
+    pair of their types the element pair's radial ids (data_format.py:192-201, 291-320)."""
+    from pypolymlp_gb300.params import expand_spins
+
+    p = make_params_dict(n_type=2, cutoff=5.0, model_type=2, max_p=2, feature_type="pair",
+                         gaussian_params2=(0.0, 4.0, 4), elements=["Fe", "Co"])
+    p["model"]["pair_params_conditional"] = {(0, 0): [0, 1], (0, 1): [2], (1, 1): [3, 4]}
+    q = expand_spins(p, [True, False])
+    assert q["n_type"] == 3 and q["elements"] == ["Fe", "Fe", "Co"]
+    assert q["enable_spins"] == [True, True, False]
+    assert q["spin_elements"] == {"elements": ["Fe", "Co"], "enable_spins": [True, False], "types": [[0, 1], [2]]}
+    assert q["model"]["pair_params_conditional"] == {(0, 0): [0, 1], (0, 1): [0, 1], (1, 1): [0, 1],
+                                                     (0, 2): [2], (1, 2): [2], (2, 2): [3, 4]}
+    r = make_params_dict(n_type=2, cutoff=5.0, model_type=2, max_p=2, feature_type="pair",
+                         gaussian_params2=(0.0, 4.0, 4), elements=["Fe", "Co"], enable_spins=[False, False])
+    assert r["n_type"] == 2 and r["enable_spins"] is None and "spin_elements" not in r
+
+
+def test_spin_model_round_trip(tmp_path):
+    """A spin model is written element-level (elements, enable_spins, element-pair
+    radial ids, one mass per atom type) as io_polymlp_yaml.py:17-94 writes it, and
+    reads back as the same expanded model; the legacy format refuses it."""
+    p = make_params_dict(n_type=2, cutoff=5.0, model_type=2, max_p=2, feature_type="pair",
+                         gaussian_params2=(0.0, 4.0, 4), elements=["Fe", "Co"], enable_spins=[True, False])
+    n = oracle.n_features(p)
+    rng = np.random.default_rng(4)
+    c, s = rng.normal(size=n), rng.uniform(0.5, 2.0, size=n)
+    path = str(tmp_path / "polymlp.yaml")
+    io.save_mlp_yaml(p, c, s, path)
+    text = open(path).read()
+    assert "elements:      [Fe, Co]" in text and "enable_spins:  [1, 0]" in text
+    assert f"mass:          [{io.ATOMIC_MASS['Fe']!r}, {io.ATOMIC_MASS['Fe']!r}, {io.ATOMIC_MASS['Co']!r}]" in text
+    assert "n_type_pairs: 3" in text and "type_indices: [0, 1]" in text
+    q, cq = io.load_mlp(path)
+    _same_model(p, q)
+    assert q["spin_elements"] == p["spin_elements"] and q["enable_spins"] == [True, True, False]
+    np.testing.assert_allclose(cq, c / s, rtol=1e-15, atol=0)
+    with pytest.raises(ValueError):
+        io.save_mlp_lammps(p, c, s, str(tmp_path / "polymlp.lammps"))

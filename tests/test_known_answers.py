@@ -1,7 +1,8 @@
 """Known answers of the reference's own property tests
 (tests/test_calc/test_properties_*.py: potentials shipped with its tests, in
 polymlp.yaml and legacy polymlp.lammps form, pair and gtinv, with conditional
-pair parameters and one hybrid model, on small cells; fixtures and asserted
+pair parameters, a spin-polarised Fe model (enable_spins: one element, two atom
+types) and two hybrid models, on small cells; fixtures and asserted
 values copied by tests/golden/make_known_answers.py).  The files are read by
 pypolymlp_gb300.io_polymlp; the oracle (CPU) must reproduce every asserted value
 at the reference test's tolerance, the GPU evaluator (FP64) too, with the
@@ -43,6 +44,11 @@ def _cases():
 
 def _load(case):
     models = [io_polymlp.load_mlp(os.path.join(KA, p)) for p in case["potentials"]]
+    if "cell" in case:
+        # a cell written in the test module: axis columns are the lattice vectors
+        axis = np.array(case["cell"]["axis"], dtype=np.float64)
+        pos = (axis @ np.array(case["cell"]["positions_frac"], dtype=np.float64)).T
+        return models, axis, pos, np.array(case["cell"]["types"])
     axis, pos, types = read_poscar(os.path.join(KA, case["structure"]), models[0][0]["elements"])
     return models, axis, pos, types
 
@@ -54,6 +60,8 @@ def _check(case, e, f, s, axis, gpu=False):
     assert e == pytest.approx(case["energy"], **tol)
     if case["forces_kind"] == "f00":
         assert abs(f[0][0]) <= case["forces_atol"]
+    elif case["forces_kind"] == "zero":
+        np.testing.assert_allclose(f, 0.0, atol=case["forces_atol"])
     else:
         np.testing.assert_allclose(f, case["forces"], atol=case["forces_atol"], rtol=0)
     if "stresses" in case:
