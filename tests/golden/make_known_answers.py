@@ -19,7 +19,9 @@ potentials need with the reference's Readgtinv (oracle/_ref), the radial
 function and Y_lm values of tests/test_cxx/test_functions.py
 (known_functions.json), the neighbour-list and cell-translation values of
 tests/test_cxx/test_neighbor*.py (known_neighbors.json), the invariant-table
-values of tests/test_cxx/test_gtinv.py (known_gtinv.json), and the MgO pair
+values of tests/test_cxx/test_gtinv.py (known_gtinv.json), the energies of
+the Ti-Al legacy gtinv test and of the MgO cell-shape test
+(known_energies.json), and the MgO pair
 and gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
@@ -197,6 +199,50 @@ def gtinv_answers():
                            "expect": list(want) if isinstance(want, tuple) else want, "approx": approx})
         out[fn.name] = {"order": kw["order"], "lmax": kw["lmax"], "version": kw["version"], "checks": checks}
     return out
+
+
+def _load_poscars_sequence(fn):
+    """[(POSCAR name, energy, tolerance kwargs)] of a test that alternates
+    `polymlp.load_poscars(path_file + "poscars/X")` and
+    `assert energies[0] == pytest.approx(v, rel=..)`."""
+    out, current = [], None
+    for st in fn.body:
+        if isinstance(st, ast.Expr) and isinstance(st.value, ast.Call) and \
+                getattr(st.value.func, "attr", "") == "load_poscars":
+            current = ast.literal_eval(st.value.args[0].right).split("/")[-1]
+        elif isinstance(st, ast.Assert) and isinstance(st.test.comparators[0], ast.Call):
+            call = st.test.comparators[0]
+            out.append((current, ast.literal_eval(call.args[0]),
+                        {k.arg: ast.literal_eval(k.value) for k in call.keywords}))
+    return out
+
+
+def energy_answers():
+    """Energies the reference asserts for several cells of one potential:
+    tests/test_calc/test_api_properties_legacy_Ti-Al.py::test_eval1 (legacy gtinv
+    Ti-Al on five cells) and test_check_neighbors.py::test_eval_neighbors_MgO (pair
+    MgO on 25 unimodular re-shapings of one rocksalt cell, energies all equal)."""
+    cases = {}
+    fn = _function(os.path.join(REF, "test_api_properties_legacy_Ti-Al.py"), "test_eval1")
+    cells = [{"structure": n, "energy": e, "tol": tol} for n, e, tol in _load_poscars_sequence(fn)]
+    cases["TiAl_gtinv_legacy"] = {"test": "tests/test_calc/test_api_properties_legacy_Ti-Al.py::test_eval1",
+                                  "potential": "polymlp.lammps.gtinv.Ti-Al", "cells": cells}
+    fn = _function(os.path.join(REF, "test_check_neighbors.py"), "test_eval_neighbors_MgO")
+    expansions = _assigned(fn, "expansions")
+    poscar = next(ast.literal_eval(n.args[0].right).split("/")[-1] for n in ast.walk(fn)
+                  if isinstance(n, ast.Call) and getattr(n.func, "id", "") == "Poscar")
+    close = next(n for n in ast.walk(fn) if isinstance(n, ast.Call) and getattr(n.func, "attr", "") == "assert_allclose")
+    energy = ast.literal_eval(close.args[1])
+    tol = {k.arg: ast.literal_eval(k.value) for k in close.keywords}
+    cases["MgO_pair_cell_shapes"] = {
+        "test": "tests/test_calc/test_check_neighbors.py::test_eval_neighbors_MgO",
+        "potential": "polymlp.yaml.pair.MgO",
+        "cells": [{"structure": poscar, "expansion": h, "energy": energy, "tol": tol} for h in expansions]}
+    for case in cases.values():
+        shutil.copyfile(os.path.join(REF, "files", "mlps", case["potential"]), os.path.join(OUT, case["potential"]))
+        for c in case["cells"]:
+            shutil.copyfile(os.path.join(REF, "files", "poscars", c["structure"]), os.path.join(OUT, c["structure"]))
+    return cases
 
 
 FIT_DIR = "/root/reference/tests/test_mlp_dev_api"
@@ -457,6 +503,10 @@ def main():
     with open(os.path.join(OUT, "known_functions.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_functions.py", "cases": function_answers()}, f, indent=1)
     print("wrote known_functions.json")
+    with open(os.path.join(OUT, "known_energies.json"), "w") as f:
+        json.dump({"source": "tests/test_calc/test_api_properties_legacy_Ti-Al.py, test_check_neighbors.py",
+                   "cases": energy_answers()}, f, indent=1)
+    print("wrote known_energies.json")
     with open(os.path.join(OUT, "known_gtinv.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_gtinv.py", "cases": gtinv_answers()}, f, indent=1)
     print("wrote known_gtinv.json")

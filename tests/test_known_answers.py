@@ -212,3 +212,58 @@ def test_rewritten_shipped_file_parses_like_the_original(tmp_path, name):
     np.testing.assert_array_equal(a["params"], b["params"])
     np.testing.assert_allclose(b["coeffs"], a["coeffs"], rtol=1e-15, atol=0)
     np.testing.assert_allclose(b["mass"], a["mass"], rtol=0, atol=0)
+
+
+def _energy_cases():
+    with open(os.path.join(KA, "known_energies.json")) as f:
+        return json.load(f)["cases"]
+
+
+def _energy_cells(case):
+    """(params, coefficients, axes, Cartesian positions (N, 3) and types per cell,
+    asserted energies, tolerances).
+    An "expansion" H re-shapes the cell: lattice vectors become the rows of H times the
+    unit cell's (H unimodular: the same crystal), positions stay where they are."""
+    p, c = io_polymlp.load_mlp(os.path.join(KA, case["potential"]))
+    axes, pos, types = [], [], []
+    for cell in case["cells"]:
+        axis, x, t = read_poscar(os.path.join(KA, cell["structure"]), p["elements"])
+        if "expansion" in cell:
+            h = np.array(cell["expansion"], dtype=np.float64)
+            assert round(abs(np.linalg.det(h))) == 1
+            axis = axis @ h.T
+        axes.append(axis)
+        pos.append(x)
+        types.append(t)
+    return p, c, axes, pos, types, [cell["energy"] for cell in case["cells"]], [cell["tol"] for cell in case["cells"]]
+
+
+def _approx(want, tol):
+    return pytest.approx(want, rel=tol.get("rel"), abs=tol.get("atol", tol.get("abs")))
+
+
+@pytest.mark.parametrize("name", sorted(_energy_cases()))
+def test_oracle_energies_reproduce_reference_known_answers(name):
+    """Legacy gtinv Ti-Al on five cells (test_api_properties_legacy_Ti-Al.py) and pair
+    MgO on 25 differently shaped cells of one crystal, down to lattice vectors ten
+    times the cell edge (test_check_neighbors.py::test_eval_neighbors_MgO)."""
+    from oracle import oracle
+
+    p, c, axes, pos, types, want, tol = _energy_cells(_energy_cases()[name])
+    e, _, _ = oracle.evaluate(p, c, Structures(axes, pos, types))
+    for got, w, t in zip(e, want, tol):
+        assert float(got) == _approx(w, t)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(_energy_cases()))
+def test_gpu_energies_reproduce_reference_known_answers(name):
+    """The same cells through PotentialPropertiesFast.eval_multiple (FP64), energies
+    to 1e-10 relative (the reference asserts 1e-12: its own summation order)."""
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.properties import PotentialPropertiesFast
+
+    p, c, axes, pos, types, want, _ = _energy_cells(_energy_cases()[name])
+    prop = PotentialPropertiesFast(p, c, _ffi.PG_FP64)
+    prop.eval_multiple(axes, [x.T for x in pos], types)
+    np.testing.assert_allclose(prop.get_e_array(), want, rtol=1e-10, atol=0)
