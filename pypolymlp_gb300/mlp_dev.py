@@ -1,0 +1,284 @@
+"""Model-development front end: parameters, datasets, GPU fit, errors, files.
+
+`Pypolymlp` mirrors the reference's class of the same name
+(src/pypolymlp/mlp_dev/pypolymlp.py:34-850) for the structure-list entry point:
+`set_params` takes the settings of `set_all_params` (core/params_utils.py:141-245:
+elements, cutoff, model type, polynomial order, Gaussian radial functions as two
+linspaces or `n_gaussians`, `distance`-conditioned radial functions, ridge
+alphas 10^linspace(reg_alpha_params), invariant order and l_max, atomic
+energies in eV or Hartree, spins); `set_datasets_structures` takes training and
+test structures (`calculator.PolymlpStructure`, atom types set from element
+names) with energies in eV per cell, forces (3, n_atom) and stress tensors
+(3, 3) in eV per cell, turning force and stress fitting off where the data are
+absent (pypolymlp.py:264-271) and subtracting the atomic energies
+(dataset_utils.py:300-305); `fit`, `fit_cg`, `run`, `estimate_error` and
+`fit_learning_curve` call the GPU regression (`regression.fit`, `fit_cg`,
+`fit_learning_curve`) and `accuracy.PolymlpEvalAccuracy`; `save_mlp`,
+`load_mlp`, `save_params` and `save_errors` write the reference's files.
+
+`precision` selects the Gram: PG_FP64 (default; the reference's arithmetic) or
+PG_MIXED (BF16x3 tensor-core Gram preconditioning an FP64 conjugate-gradient
+solve, with the FP64 Gram as fallback where that solve does not converge).
+Electron, SSCHA, phono3py and VASP dataset readers of the reference are not
+part of this module.
+"""
+
+from __future__ import annotations
+
+from typing import Optional, Sequence
+
+import numpy as np
+
+from pypolymlp_gb300 import _ffi
+from pypolymlp_gb300.calculator import PolymlpStructure, replace_types
+from pypolymlp_gb300.params import make_params_dict
+
+HARTREE_TO_EV = 27.211386245981  # the reference's conversion (core/units.py:31)
+
+
+class Pypolymlp:
+    def __init__(self, verbose: bool = False, precision: int = _ffi.PG_FP64):
+        self._verbose = verbose
+        self._precision = precision
+        self._params: Optional[dict] = None
+        self._alphas = None
+        self._atomic_energy = None
+        self._train = self._test = None
+        self._result = None
+        self._coeffs = self._scales = None
+        self._error_train = self._error_test = None
+        self._learning_log = None
+
+    # -- parameters -----------------------------------------------------------------
+    def set_params(self, params: Optional[dict] = None, elements: Optional[Sequence[str]] = None,
+                   include_force: bool = True, include_stress: bool = True, cutoff: float = 6.0,
+                   model_type: int = 4, max_p: int = 2, feature_type: str = "gtinv",
+                   gaussian_params1=(1.0, 1.0, 1), gaussian_params2=(0.0, 5.0, 7),
+                   n_gaussians: Optional[int] = None, distance: Optional[dict] = None,
+                   reg_alpha_params=(-3.0, 1.0, 5), gtinv_order: int = 3, gtinv_maxl=(4, 4, 2, 1, 1),
+                   gtinv_version: int = 1, atomic_energy_unit: str = "eV",
+                   atomic_energy: Optional[Sequence[float]] = None, enable_spins: Optional[Sequence[bool]] = None):
+        alphas = [10.0 ** a for a in np.linspace(reg_alpha_params[0], reg_alpha_params[1],
+                                                 round(reg_alpha_params[2]))]
+        if params is not None:
+            self._params = params
+            self._alphas = params.get("alphas") or alphas
+            n = len(params.get("spin_elements", {}).get("elements", params["elements"]))
+            self._atomic_energy = self._expand_atomic_energy(params, [0.0] * n)
+            return self
+        if elements is None:
+            raise RuntimeError("elements are required")
+        n_type = len(elements)
+        if atomic_energy is None:
+            atomic_energy = [0.0] * n_type
+        elif len(atomic_energy) != n_type:
+            raise ValueError("one atomic energy per element")
+        if atomic_energy_unit == "Hartree":
+            atomic_energy = [e * HARTREE_TO_EV for e in atomic_energy]
+        self._params = make_params_dict(
+            n_type=n_type, cutoff=cutoff, model_type=model_type, max_p=max_p, feature_type=feature_type,
+            gaussian_params1=gaussian_params1, gaussian_params2=gaussian_params2, gtinv_order=gtinv_order,
+            gtinv_maxl=gtinv_maxl, gtinv_version=gtinv_version, elements=list(elements),
+            include_force=include_force, include_stress=include_stress, alphas=alphas, enable_spins=enable_spins,
+            n_gaussians=n_gaussians, distance=distance)
+        self._alphas = alphas
+        self._atomic_energy = self._expand_atomic_energy(self._params, list(atomic_energy))
+        return self
+
+    @staticmethod
+    def _expand_atomic_energy(params: dict, per_element: list) -> np.ndarray:
+        """Atomic energy per atom type (spin-split elements repeat theirs)."""
+        sp = params.get("spin_elements")
+        if not sp:
+            return np.asarray(per_element, dtype=np.float64)
+        out = np.zeros(int(params["n_type"]))
+        for e, types in zip(per_element, sp["types"]):
+            out[types] = e
+        return out
+
+    # -- datasets -------------------------------------------------------------------
+    def set_datasets_structures(self, train_structures: Sequence[PolymlpStructure],
+                                test_structures: Sequence[PolymlpStructure], train_energies, test_energies,
+                                train_forces: Optional[Sequence] = None, test_forces: Optional[Sequence] = None,
+                                train_stresses=None, test_stresses=None):
+        from pypolymlp_gb300.regression import Dataset
+
+        if self._params is None:
+            raise RuntimeError("Set parameters before datasets.")
+        for forces, stresses in ((train_forces, train_stresses), (test_forces, test_stresses)):
+            if forces is None:
+                self._params["include_force"] = self._params["include_stress"] = False
+            if stresses is None:
+                self._params["include_stress"] = False
+
+        def one(structures, energies, forces, stresses, name):
+            elements = list(self._params["elements"])
+            types = [replace_types(st, elements) for st in structures]
+            axis = [np.asarray(st.axis, dtype=np.float64) for st in structures]
+            pos = [(a @ np.asarray(st.positions, dtype=np.float64)).T for a, st in zip(axis, structures)]
+            e = np.asarray(energies, dtype=np.float64) - np.array([self._atomic_energy[t].sum() for t in types])
+            f = None if forces is None else [np.asarray(x, dtype=np.float64).T for x in forces]
+            s = None
+            if stresses is not None:
+                t = np.asarray(stresses, dtype=np.float64).reshape(-1, 3, 3)
+                s = np.stack([t[:, 0, 0], t[:, 1, 1], t[:, 2, 2], t[:, 0, 1], t[:, 1, 2], t[:, 2, 0]], axis=1)
+            return Dataset(axis, pos, types, e, f, s, include_force=self._params["include_force"],
+                           include_stress=self._params["include_stress"], name=name)
+
+        self._train = [one(train_structures, train_energies, train_forces, train_stresses, "data1")]
+        self._test = [one(test_structures, test_energies, test_forces, test_stresses, "data2")]
+        return self
+
+    def _ready(self):
+        if self._params is None or self._train is None or self._test is None:
+            raise RuntimeError("Set parameters and datasets before using fit.")
+
+    # -- fitting --------------------------------------------------------------------
+    def fit(self, batch_size: Optional[int] = None, verbose: Optional[bool] = None):
+        """Ridge regression over the alphas on the GPU Gram (batch_size: the
+        device batches are sized by memory; the argument is accepted and unused)."""
+        from pypolymlp_gb300 import regression
+
+        self._ready()
+        res = regression.fit(self._params, self._train, self._test, self._alphas, precision=self._precision,
+                             fp64_fallback=self._precision == _ffi.PG_MIXED)
+        return self._set_result(res)
+
+    def fit_standard(self, verbose: Optional[bool] = None):
+        return self.fit(verbose=verbose)
+
+    def fit_cg(self, gtol: float = 1e-2, max_iter: Optional[int] = None, verbose: Optional[bool] = None):
+        from pypolymlp_gb300 import regression
+
+        self._ready()
+        res = regression.fit_cg(self._params, self._train, self._test, self._alphas, gtol=gtol, max_iter=max_iter,
+                                precision=self._precision)
+        return self._set_result(res)
+
+    def fit_sgd(self, verbose: Optional[bool] = None):
+        raise NotImplementedError("SGD not available.")
+
+    def _set_result(self, res):
+        self._result = res
+        self._scales = np.asarray(res.scales, dtype=np.float64)
+        self._coeffs = np.asarray(res.coeffs, dtype=np.float64)
+        return self
+
+    def estimate_error(self, log_energy: bool = False, file_path: str = "./", verbose: Optional[bool] = None):
+        from pypolymlp_gb300.accuracy import PolymlpEvalAccuracy
+
+        if self._coeffs is None:
+            raise RuntimeError("Regression must be performed before estimating errors.")
+        acc = PolymlpEvalAccuracy(self._params, self._coeffs / self._scales, verbose=self._verbose)
+        self._error_train = acc.compute_error(self._train, log_energy=log_energy, path_output=file_path, tag="train")
+        self._error_test = acc.compute_error(self._test, log_energy=log_energy, path_output=file_path, tag="test")
+        return self
+
+    def run(self, batch_size: Optional[int] = None, use_cg: bool = False, gtol: float = 1e-2,
+            max_iter: Optional[int] = None, verbose: Optional[bool] = None):
+        if use_cg:
+            self.fit_cg(gtol=gtol, max_iter=max_iter)
+        else:
+            self.fit(batch_size=batch_size)
+        return self.estimate_error()
+
+    def fit_learning_curve(self, verbose: Optional[bool] = None):
+        from pypolymlp_gb300 import regression
+
+        self._ready()
+        self._learning_log = regression.fit_learning_curve(self._params, self._train, self._test, self._alphas,
+                                                           precision=self._precision)
+        return self
+
+    def save_learning_curve(self, filename: str = "polymlp_learning_curve.dat"):
+        """One line per (training size, test dataset): n, energy RMSE (meV/atom),
+        force RMSE (eV/angstrom), stress RMSE, as utils_learning_curve.py:4-15."""
+        with open(filename, "w") as f:
+            print("# n_str, RMSE(energy, meV/atom) RMSE(force, eV/ang), RMSE(stress)", file=f)
+            for n, err in self._learning_log:
+                print(n, err["energy"] * 1000, err["force"], err["stress"], file=f)
+        return self
+
+    # -- files ----------------------------------------------------------------------
+    def save_mlp(self, filename: str = "polymlp.yaml"):
+        from pypolymlp_gb300.io_polymlp import save_mlp_yaml
+
+        if self._coeffs is None:
+            raise RuntimeError("No polymlp has been developed.")
+        save_mlp_yaml(self._params, self._coeffs, self._scales, filename)
+        return self
+
+    def load_mlp(self, filename: str = "polymlp.yaml"):
+        from pypolymlp_gb300.io_polymlp import load_mlp
+
+        self._params, coeffs = load_mlp(filename)
+        self._coeffs, self._scales = np.asarray(coeffs, dtype=np.float64), np.ones(len(coeffs))
+        return self
+
+    def save_params(self, filename: str = "polymlp_params.yaml"):
+        from pypolymlp_gb300.features_attr import write_polymlp_params_yaml
+
+        if self._params is None:
+            raise RuntimeError("Set parameters first.")
+        write_polymlp_params_yaml(self._params, filename)
+        return self
+
+    def save_errors(self, filename: str = "polymlp_error.yaml"):
+        """Errors in the layout of eval_accuracy.py:271-301 (meV/atom, eV/angstrom)."""
+        if self._error_train is None:
+            raise RuntimeError("estimate_error must be performed before save_errors.")
+        with open(filename, "w") as f:
+            print("units:\n  energy: meV/atom\n  force:  eV/angstrom\n  stress: meV/atom\n", file=f)
+            print("prediction_errors:", file=f)
+            for errors in (self._error_train, self._error_test):
+                for key, e in errors.items():
+                    print("- dataset:", key, file=f)
+                    print("  rmse_energy: ", e["energy"] * 1000, file=f)
+                    if e["force"] is not None:
+                        print("  rmse_force:  ", e["force"], file=f)
+                    if e["stress"] is not None:
+                        print("  rmse_stress: ", e["stress"] * 1000, file=f)
+                    print("", file=f)
+                    print("  mae_energy:  ", e["energy_mae"] * 1000, file=f)
+                    if e["force_mae"] is not None:
+                        print("  mae_force:   ", e["force_mae"], file=f)
+                    if e["stress_mae"] is not None:
+                        print("  mae_stress:  ", e["stress_mae"] * 1000, file=f)
+                    print("", file=f)
+        return self
+
+    # -- results --------------------------------------------------------------------
+    @property
+    def parameters(self) -> dict:
+        return self._params
+
+    @property
+    def coeffs(self):
+        """Coefficients of the unscaled features (c / s)."""
+        return None if self._coeffs is None else self._coeffs / self._scales
+
+    @property
+    def n_features(self) -> int:
+        from pypolymlp_gb300.features_attr import get_num_features
+
+        return get_num_features(self._params)
+
+    @property
+    def errors(self):
+        return self._error_train, self._error_test
+
+    @property
+    def learning_curve(self):
+        return self._learning_log
+
+    @property
+    def train(self):
+        return self._train
+
+    @property
+    def test(self):
+        return self._test
+
+    @property
+    def fit_result(self):
+        return self._result

@@ -27,12 +27,53 @@ def load_gtinv(order: int, maxl: Sequence[int], version: int = 1):
     return get_gtinv_attrs(order, maxl, version)
 
 
-def gaussian_params(params1=(1.0, 1.0, 1), params2=(0.0, 5.0, 7)):
-    g1 = np.linspace(float(params1[0]), float(params1[1]), int(params1[2]))
-    g2 = np.linspace(float(params2[0]), float(params2[1]), int(params2[2]))
-    pp = [[float(a), float(b)] for a, b in itertools.product(g1, g2)]
+def gaussian_params(params1=(1.0, 1.0, 1), params2=(0.0, 5.0, 7), n_gaussians: Optional[int] = None,
+                    cutoff: Optional[float] = None):
+    """(beta, mu) of the Gaussian radial functions, the constant (0, 0) last
+    (params_utils.py:69-93): the product of two linspaces, or with n_gaussians
+    n-1 centres spread over [0, cutoff - 1] with width max(1, spacing)."""
+    if n_gaussians is None:
+        g1 = np.linspace(float(params1[0]), float(params1[1]), int(params1[2]))
+        g2 = np.linspace(float(params2[0]), float(params2[1]), int(params2[2]))
+        pp = [[float(a), float(b)] for a, b in itertools.product(g1, g2)]
+    else:
+        if cutoff is None:
+            raise RuntimeError("Cutoff required for automatic setting of Gaussians.")
+        if int(n_gaussians) < 3:
+            raise ValueError("n_gaussians must be at least 3 (two Gaussians set the width)")
+        mu = np.linspace(0.0, 1.0, int(n_gaussians) - 1) * (float(cutoff) - 1.0)
+        width = max(1.0, float(mu[1] - mu[0]))
+        pp = [[width, float(m)] for m in mu]
     pp.append([0.0, 0.0])
     return pp
+
+
+def active_gaussian_params(pair_params, elements: Sequence[str], distance: Optional[dict] = None):
+    """Radial ids per type pair (i <= j) and whether they are conditional
+    (params_utils.py:96-140): without `distance` every function for every pair;
+    for an element pair given typical distances, the constant function and each
+    Gaussian whose centre lies within 1/beta of one of them."""
+    elements = list(elements)
+    given = {}
+    for pair, dis in (distance or {}).items():
+        if len(pair) != 2:
+            raise RuntimeError("Keys of distance must be element pair.")
+        if not isinstance(dis, (list, tuple, np.ndarray)):
+            raise RuntimeError("Values of distance must be array-type.")
+        given[tuple(sorted(pair, key=elements.index))] = list(dis)
+    cond = {}
+    for i, j in itertools.combinations_with_replacement(range(len(elements)), 2):
+        key = (elements[i], elements[j])
+        if key not in given:
+            cond[(i, j)] = list(range(len(pair_params)))
+            continue
+        match = {len(pair_params) - 1}
+        for d in given[key]:
+            for k, (beta, mu) in enumerate(pair_params[:-1]):
+                if mu - 1.0 / beta < d < mu + 1.0 / beta:
+                    match.add(k)
+        cond[(i, j)] = sorted(match)
+    return cond, distance is not None
 
 
 def make_params_dict(
@@ -52,12 +93,13 @@ def make_params_dict(
     include_stress: bool = True,
     alphas: Optional[Sequence[float]] = None,
     enable_spins: Optional[Sequence[bool]] = None,
+    n_gaussians: Optional[int] = None,
+    distance: Optional[dict] = None,
 ) -> dict:
-    pair_params = gaussian_params(gaussian_params1, gaussian_params2)
-    cond = {}
-    for i in range(n_type):
-        for j in range(i, n_type):
-            cond[(i, j)] = list(range(len(pair_params)))
+    pair_params = gaussian_params(gaussian_params1, gaussian_params2, n_gaussians, cutoff)
+    if elements is None:
+        elements = [f"E{i}" for i in range(n_type)]
+    cond, pair_conditional = active_gaussian_params(pair_params, elements, distance)
     if feature_type == "gtinv":
         if gtinv_tables is None:
             gtinv_tables = load_gtinv(gtinv_order, gtinv_maxl, gtinv_version)
@@ -76,8 +118,6 @@ def make_params_dict(
         max_l = 0
         gtinv = {"order": 0, "max_l": [], "n_type": n_type, "lm_seq": [], "l_comb": [],
                  "lm_coeffs": [], "version": 1}
-    if elements is None:
-        elements = [f"E{i}" for i in range(n_type)]
     return expand_spins({
         "n_type": n_type,
         "elements": list(elements),
@@ -89,7 +129,7 @@ def make_params_dict(
             "feature_type": feature_type,
             "gtinv": gtinv,
             "pair_type": "gaussian",
-            "pair_conditional": False,
+            "pair_conditional": pair_conditional,
             "pair_params": pair_params,
             "pair_params_conditional": cond,
         },

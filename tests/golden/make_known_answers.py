@@ -21,7 +21,8 @@ function and Y_lm values of tests/test_cxx/test_functions.py
 tests/test_cxx/test_neighbor*.py (known_neighbors.json), the invariant-table
 values of tests/test_cxx/test_gtinv.py (known_gtinv.json), the energies of
 the Ti-Al legacy gtinv test and of the MgO cell-shape test
-(known_energies.json), and the MgO pair
+(known_energies.json), radial-function settings computed by the reference's
+params_utils.py (known_params.json), and the MgO pair
 and gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
@@ -243,6 +244,40 @@ def energy_answers():
         for c in case["cells"]:
             shutil.copyfile(os.path.join(REF, "files", "poscars", c["structure"]), os.path.join(OUT, c["structure"]))
     return cases
+
+
+def param_answers():
+    """Radial-function settings computed by the reference's own Python
+    (core/params_utils.py set_gaussian_params with n_gaussians, and
+    set_active_gaussian_params with element-pair distances), imported from the
+    reference sources with its compiled module stubbed out (not used by them)."""
+    import types
+
+    sys.path.insert(0, "/root/reference/src")
+    stub = types.ModuleType("pypolymlp.cxx.lib")
+    stub.libmlpcpp = None
+    sys.modules.setdefault("pypolymlp.cxx.lib", stub)
+    from pypolymlp.core.params_utils import set_active_gaussian_params, set_gaussian_params
+
+    out = {"n_gaussians": [], "distance": []}
+    for n, rc in ((3, 5.0), (5, 6.0), (10, 8.0), (14, 7.5)):
+        out["n_gaussians"].append({"n_gaussians": n, "cutoff": rc,
+                                   "pair_params": [list(map(float, p)) for p in set_gaussian_params(
+                                       n_gaussians=n, cutoff=rc)]})
+    settings = [
+        (["Sr", "Ti", "O"], {("Sr", "Sr"): [3.5, 4.8], ("Ti", "O"): [1.9, 3.4], ("O", "Sr"): [2.7]},
+         dict(params1=(1.0, 1.0, 1), params2=(0.0, 6.0, 13))),
+        (["Mg", "O"], {("O", "Mg"): [2.1, 4.4]}, dict(n_gaussians=8, cutoff=7.0)),
+        (["Al", "Cu", "Zn"], {("Cu", "Cu"): [2.55], ("Zn", "Al"): [2.7, 3.9]},
+         dict(params1=(0.5, 1.5, 3), params2=(0.0, 5.0, 6))),
+    ]
+    for elements, dist, g in settings:
+        pp = set_gaussian_params(**g)
+        cond, flag = set_active_gaussian_params(pp, elements, dist)
+        out["distance"].append({"elements": elements, "distance": [[list(k), v] for k, v in dist.items()],
+                                "pair_params": [list(map(float, p)) for p in pp], "conditional": flag,
+                                "cond": [[list(k), v] for k, v in cond.items()]})
+    return out
 
 
 FIT_DIR = "/root/reference/tests/test_mlp_dev_api"
@@ -507,6 +542,10 @@ def main():
         json.dump({"source": "tests/test_calc/test_api_properties_legacy_Ti-Al.py, test_check_neighbors.py",
                    "cases": energy_answers()}, f, indent=1)
     print("wrote known_energies.json")
+    with open(os.path.join(OUT, "known_params.json"), "w") as f:
+        json.dump({"source": "src/pypolymlp/core/params_utils.py (run here)", "cases": param_answers()}, f,
+                  indent=1)
+    print("wrote known_params.json")
     with open(os.path.join(OUT, "known_gtinv.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_gtinv.py", "cases": gtinv_answers()}, f, indent=1)
     print("wrote known_gtinv.json")

@@ -57,27 +57,41 @@ def _check(errors, known):
             assert got[key] == pytest.approx(want["value"], abs=want["abs"]), (tag, key, got[key], want["value"])
 
 
+def cpu_fit(p, train, test, alphas):
+    """(coefficients of the best alpha in the scaled basis, scales): oracle X rows,
+    numpy Gram, LAPACK posv, the reference's selection by test RMSE."""
+    from oracle.pipeline import calc_xtx_xty_cpu, solver_ridge_cpu
+    from pypolymlp_gb300.regression import compute_rmse_seq
+
+    xy = calc_xtx_xty_cpu(p, train)
+    coefs = solver_ridge_cpu(xy.xtx, xy.xty, alphas)
+    txy = calc_xtx_xty_cpu(p, test, scales=xy.scales, min_energy=xy.min_energy)
+    return coefs[:, int(np.argmin(compute_rmse_seq(coefs, txy)))], xy.scales
+
+
+def cpu_errors(p, coeffs, datasets):
+    """Prediction errors per dataset with the oracle's E/F/S."""
+    from oracle import oracle
+    from pypolymlp_gb300.abi import Structures
+
+    errors = {}
+    for d in datasets:
+        e, f, s = oracle.evaluate(p, coeffs, Structures(d.axis, d.positions, d.types))
+        offs = np.concatenate([[0], np.cumsum(d.total_n_atoms)])
+        errors[d.name], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
+    return errors
+
+
 @pytest.mark.parametrize("name", sorted(_cases()))
 def test_cpu_pipeline_reproduces_reference_fit_errors(name):
     from oracle import oracle
-    from oracle.pipeline import calc_xtx_xty_cpu, solver_ridge_cpu
-    from pypolymlp_gb300.abi import Structures
-    from pypolymlp_gb300.regression import compute_rmse_seq
 
     case = _cases()[name]
     p = _params(case["settings"])
     assert oracle.n_features(p) == case["settings"]["n_features"]
     train, test = _datasets(case)
-    xy = calc_xtx_xty_cpu(p, train)
-    coefs = solver_ridge_cpu(xy.xtx, xy.xty, case["settings"]["alphas"])
-    txy = calc_xtx_xty_cpu(p, test, scales=xy.scales, min_energy=xy.min_energy)
-    best = coefs[:, int(np.argmin(compute_rmse_seq(coefs, txy)))] / xy.scales
-    errors = {}
-    for d in train + test:
-        e, f, s = oracle.evaluate(p, best, Structures(d.axis, d.positions, d.types))
-        offs = np.concatenate([[0], np.cumsum(d.total_n_atoms)])
-        errors[d.name], _ = prediction_errors(d, e, [f[offs[i]:offs[i + 1]] for i in range(len(d))], s)
-    _check(errors, case["errors"])
+    c, scales = cpu_fit(p, train, test, case["settings"]["alphas"])
+    _check(cpu_errors(p, c / scales, train + test), case["errors"])
 
 
 @pytest.mark.gpu

@@ -1,0 +1,173 @@
+"""The model-development front end (pypolymlp_gb300.mlp_dev.Pypolymlp).
+
+The reference's pair MgO fit (test_mlp_devel_vasp.py::test_mlp_devel_pair; its
+vasprun data in tests/golden/known_answers/fit_MgO.npz) is passed in as the
+reference's users pass structures: PolymlpStructure objects with element names
+(atoms shuffled against the element order), fractional positions, energies
+with atomic energies added back, forces (3, n_atom) and 3x3 stress tensors.
+On the CPU the GPU regression and evaluator are replaced by the oracle
+pipeline (test infrastructure), so the front end's parameter and dataset
+handling is checked against the reference's asserted train/test errors; the
+`gpu` test runs the same through the GPU."""
+
+import numpy as np
+import pytest
+
+from pypolymlp_gb300 import _ffi
+from pypolymlp_gb300.calculator import PolymlpStructure
+from pypolymlp_gb300.mlp_dev import Pypolymlp
+
+ATOMIC_E = (-0.6, -1.7)
+
+
+def _structures(z, tag, rng):
+    n = z[f"{tag}_n_atoms"]
+    offs = np.concatenate([[0], np.cumsum(n)])
+    names = np.array(["Mg", "O"])
+    sts, energies, forces, stresses = [], [], [], []
+    for i in range(len(n)):
+        sl = slice(offs[i], offs[i + 1])
+        axis = z[f"{tag}_axis"][i]
+        perm = rng.permutation(n[i])
+        pos = z[f"{tag}_positions"][sl][perm]
+        types = z[f"{tag}_types"][sl][perm]
+        frac = np.linalg.solve(axis, pos.T)
+        sts.append(PolymlpStructure(axis, frac, [int(np.sum(types == t)) for t in (0, 1)], list(names[types]),
+                                    [5] * len(types)))
+        energies.append(z[f"{tag}_energies"][i] + sum(ATOMIC_E[t] for t in types))
+        forces.append(z[f"{tag}_forces"][sl][perm].T)
+        xx, yy, zz, xy, yz, zx = z[f"{tag}_stresses"][i]
+        stresses.append([[xx, xy, zx], [xy, yy, yz], [zx, yz, zz]])
+    return sts, np.array(energies), forces, np.array(stresses)
+
+
+def _front_end(precision=_ffi.PG_FP64):
+    from test_known_fit import KA, _cases
+
+    case = _cases()["pair_single"]
+    st = case["settings"]
+    z = np.load(f"{KA}/{case['data']}")
+    rng = np.random.default_rng(3)
+    tr = _structures(z, "train1", rng)
+    te = _structures(z, "test1", rng)
+    pm = Pypolymlp(precision=precision)
+    pm.set_params(elements=st["elements"], cutoff=st["cutoff"], model_type=st["model_type"], max_p=st["max_p"],
+                  feature_type=st["feature_type"], gaussian_params1=tuple(st["gaussian_params1"]),
+                  gaussian_params2=tuple(st["gaussian_params2"]), reg_alpha_params=(-3, 1, 5),
+                  atomic_energy=ATOMIC_E)
+    pm.set_datasets_structures(tr[0], te[0], tr[1], te[1], tr[2], te[2], tr[3], te[3])
+    return pm, case
+
+
+@pytest.fixture
+def on_oracle(monkeypatch):
+    """The GPU fit and evaluator replaced by the oracle pipeline."""
+    from test_calculator import _OracleEvaluator
+    from test_known_fit import cpu_fit
+
+    from pypolymlp_gb300 import properties, regression
+
+    class _Result:
+        def __init__(self, c, s):
+            self.coeffs, self.scales = c, s
+
+    def fake_fit(params, train, test, alphas, **kw):
+        return _Result(*cpu_fit(params, train, test, alphas))
+
+    monkeypatch.setattr(properties, "PotentialPropertiesFast", _OracleEvaluator)
+    monkeypatch.setattr(regression, "fit", fake_fit)
+
+
+def _check(pm, case):
+    from test_known_fit import _check as check_errors
+
+    train, test = pm.errors
+    got = {"train1": train["data1"], "test1": test["data2"]}
+    check_errors(got, case["errors"])
+
+
+def test_front_end_datasets_match_the_reference_dataset(tmp_path):
+    from test_known_fit import _datasets
+
+    pm, case = _front_end()
+    assert pm.n_features == case["settings"]["n_features"]
+    ref_train, _ = _datasets(case)
+    d, r = pm.train[0], ref_train[0]
+    assert len(d) == len(r) and d.include_force and d.include_stress
+    np.testing.assert_allclose(d.energies, r.energies, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(d.stresses, r.stresses, rtol=0, atol=0)
+    for a, b in zip(d.types, r.types):
+        assert sorted(a.tolist()) == sorted(b.tolist())
+    # the reference's row order does not matter: per structure, the same atoms
+    for a, b, fa, fb in zip(d.positions, r.positions, d.forces, r.forces):
+        ka, kb = np.lexsort(np.round(a, 9).T), np.lexsort(np.round(b, 9).T)
+        np.testing.assert_allclose(a[ka], b[kb], atol=1e-12)
+        np.testing.assert_array_equal(fa[ka], fb[kb])
+
+
+def test_front_end_reproduces_reference_fit_errors(on_oracle, tmp_path):
+    pm, case = _front_end()
+    pm.run()
+    _check(pm, case)
+    pm.save_mlp(str(tmp_path / "polymlp.yaml"))
+    pm.save_errors(str(tmp_path / "polymlp_error.yaml"))
+    pm.save_params(str(tmp_path / "polymlp_params.yaml"))
+    text = open(tmp_path / "polymlp_error.yaml").read()
+    assert text.count("- dataset:") == 2 and "rmse_stress:" in text
+    back = Pypolymlp().load_mlp(str(tmp_path / "polymlp.yaml"))
+    np.testing.assert_allclose(back.coeffs, pm.coeffs, rtol=1e-15)
+    assert back.n_features == case["settings"]["n_features"]
+
+
+def test_missing_forces_turn_off_force_and_stress_fitting():
+    pm = Pypolymlp().set_params(elements=["Mg", "O"], feature_type="pair", model_type=2, max_p=2)
+    st = PolymlpStructure(np.eye(3) * 4.0, np.array([[0.0, 0.5], [0.0, 0.5], [0.0, 0.5]]), [1, 1], ["Mg", "O"],
+                          [0, 1])
+    pm.set_datasets_structures([st], [st], [-1.0], [-1.0])
+    assert not pm.train[0].include_force and not pm.train[0].include_stress and pm.train[0].forces is None
+    pm = Pypolymlp().set_params(elements=["Mg", "O"], feature_type="pair", model_type=2, max_p=2,
+                                atomic_energy=(-1.0, -0.5), atomic_energy_unit="Hartree")
+    pm.set_datasets_structures([st], [st], [-1.0], [-1.0], [np.zeros((3, 2))], [np.zeros((3, 2))])
+    assert pm.train[0].include_force and not pm.train[0].include_stress
+    assert pm.train[0].energies[0] == pytest.approx(-1.0 + 1.5 * 27.211386245981)
+
+
+@pytest.mark.gpu
+def test_gpu_front_end_reproduces_reference_fit_errors():
+    pm, case = _front_end()
+    pm.run()
+    _check(pm, case)
+
+
+def _param_cases():
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers", "known_params.json")
+    with open(path) as f:
+        return json.load(f)["cases"]
+
+
+def test_gaussians_from_n_gaussians_match_reference():
+    from pypolymlp_gb300.params import gaussian_params
+
+    for c in _param_cases()["n_gaussians"]:
+        got = gaussian_params(n_gaussians=c["n_gaussians"], cutoff=c["cutoff"])
+        np.testing.assert_array_equal(np.array(got), np.array(c["pair_params"]))
+    with pytest.raises(ValueError):
+        gaussian_params(n_gaussians=2, cutoff=6.0)
+
+
+def test_distance_conditioned_radial_functions_match_reference():
+    from pypolymlp_gb300.params import active_gaussian_params, make_params_dict
+
+    for c in _param_cases()["distance"]:
+        dist = {tuple(k): v for k, v in c["distance"]}
+        cond, flag = active_gaussian_params(c["pair_params"], c["elements"], dist)
+        assert flag == c["conditional"]
+        assert cond == {tuple(k): v for k, v in c["cond"]}
+    c = _param_cases()["distance"][1]
+    p = make_params_dict(n_type=2, cutoff=7.0, model_type=2, max_p=2, feature_type="pair", n_gaussians=8,
+                         elements=c["elements"], distance={tuple(k): v for k, v in c["distance"]})
+    assert p["model"]["pair_conditional"] and p["model"]["pair_params"] == c["pair_params"]
+    assert p["model"]["pair_params_conditional"] == {tuple(k): v for k, v in c["cond"]}
