@@ -19,8 +19,9 @@ absent (pypolymlp.py:264-271) and subtracting the atomic energies
 `precision` selects the Gram: PG_FP64 (default; the reference's arithmetic) or
 PG_MIXED (BF16x3 tensor-core Gram preconditioning an FP64 conjugate-gradient
 solve, with the FP64 Gram as fallback where that solve does not converge).
-Electron, SSCHA, phono3py and VASP dataset readers of the reference are not
-part of this module.
+`set_datasets_vasp` and `set_multiple_datasets_vasp` read vasprun.xml files
+(`io_vasp`); the reference's electron, SSCHA, phono3py and property-yaml
+dataset readers are not part of this module.
 """
 
 from __future__ import annotations
@@ -101,8 +102,6 @@ class Pypolymlp:
                                 test_structures: Sequence[PolymlpStructure], train_energies, test_energies,
                                 train_forces: Optional[Sequence] = None, test_forces: Optional[Sequence] = None,
                                 train_stresses=None, test_stresses=None):
-        from pypolymlp_gb300.regression import Dataset
-
         if self._params is None:
             raise RuntimeError("Set parameters before datasets.")
         for forces, stresses in ((train_forces, train_stresses), (test_forces, test_stresses)):
@@ -111,22 +110,64 @@ class Pypolymlp:
             if stresses is None:
                 self._params["include_stress"] = False
 
-        def one(structures, energies, forces, stresses, name):
-            elements = list(self._params["elements"])
-            types = [replace_types(st, elements) for st in structures]
-            axis = [np.asarray(st.axis, dtype=np.float64) for st in structures]
-            pos = [(a @ np.asarray(st.positions, dtype=np.float64)).T for a, st in zip(axis, structures)]
-            e = np.asarray(energies, dtype=np.float64) - np.array([self._atomic_energy[t].sum() for t in types])
-            f = None if forces is None else [np.asarray(x, dtype=np.float64).T for x in forces]
-            s = None
-            if stresses is not None:
-                t = np.asarray(stresses, dtype=np.float64).reshape(-1, 3, 3)
-                s = np.stack([t[:, 0, 0], t[:, 1, 1], t[:, 2, 2], t[:, 0, 1], t[:, 1, 2], t[:, 2, 0]], axis=1)
-            return Dataset(axis, pos, types, e, f, s, include_force=self._params["include_force"],
-                           include_stress=self._params["include_stress"], name=name)
+        self._train = [self._dataset(train_structures, train_energies, train_forces, train_stresses, "data1")]
+        self._test = [self._dataset(test_structures, test_energies, test_forces, test_stresses, "data2")]
+        return self
 
-        self._train = [one(train_structures, train_energies, train_forces, train_stresses, "data1")]
-        self._test = [one(test_structures, test_energies, test_forces, test_stresses, "data2")]
+    def _dataset(self, structures, energies, forces, stresses, name):
+        """regression.Dataset of structures typed by the model's element order,
+        atomic energies subtracted, stresses as (xx, yy, zz, xy, yz, zx)."""
+        from pypolymlp_gb300.regression import Dataset
+
+        elements = list(self._params["elements"])
+        types = [replace_types(st, elements) for st in structures]
+        axis = [np.asarray(st.axis, dtype=np.float64) for st in structures]
+        pos = [(a @ np.asarray(st.positions, dtype=np.float64)).T for a, st in zip(axis, structures)]
+        e = np.asarray(energies, dtype=np.float64) - np.array([self._atomic_energy[t].sum() for t in types])
+        f = None if forces is None else [np.asarray(x, dtype=np.float64).T for x in forces]
+        s = None
+        if stresses is not None:
+            t = np.asarray(stresses, dtype=np.float64).reshape(-1, 3, 3)
+            s = np.stack([t[:, 0, 0], t[:, 1, 1], t[:, 2, 2], t[:, 0, 1], t[:, 1, 2], t[:, 2, 0]], axis=1)
+        return Dataset(axis, pos, types, e, f, s, include_force=self._params["include_force"],
+                       include_stress=self._params["include_stress"], name=name)
+
+    def _vasp_dataset(self, files, name):
+        from pypolymlp_gb300.io_vasp import parse_properties_from_vaspruns
+
+        sts, (e, f, s) = parse_properties_from_vaspruns(sorted(files), verbose=self._verbose)
+        return self._dataset(sts, e, f, s, name)
+
+    def set_datasets_vasp(self, train_vaspruns: Optional[Sequence[str]] = None,
+                          test_vaspruns: Optional[Sequence[str]] = None, vaspruns=None, train_ratio: float = 0.9):
+        """One training and one test dataset from vasprun.xml files (dataset.py:567-637):
+        given lists, or one list split by the reference's rule (files sorted
+        first), or one MD vasprun whose steps are split."""
+        from pypolymlp_gb300.io_vasp import parse_properties_from_vaspruns, split_ids_train_test, split_train_test
+
+        if self._params is None:
+            raise RuntimeError("Set parameters before datasets.")
+        if train_vaspruns is not None and test_vaspruns is not None:
+            self._train = [self._vasp_dataset(train_vaspruns, "data1")]
+            self._test = [self._vasp_dataset(test_vaspruns, "data2")]
+        elif isinstance(vaspruns, str):
+            sts, (e, f, s) = parse_properties_from_vaspruns([vaspruns], verbose=self._verbose)
+            tr, te = split_ids_train_test(len(sts), train_ratio)
+            self._train = [self._dataset([sts[i] for i in tr], e[tr], [f[i] for i in tr], s[tr], "data1")]
+            self._test = [self._dataset([sts[i] for i in te], e[te], [f[i] for i in te], s[te], "data2")]
+        else:
+            tr_files, te_files = split_train_test(sorted(vaspruns), train_ratio)
+            self._train = [self._vasp_dataset(tr_files, "data1")]
+            self._test = [self._vasp_dataset(te_files, "data2")]
+        return self
+
+    def set_multiple_datasets_vasp(self, train_vaspruns: Sequence[Sequence[str]],
+                                   test_vaspruns: Sequence[Sequence[str]]):
+        """Several training and test datasets, named data1, data2, ... in each list."""
+        if self._params is None:
+            raise RuntimeError("Set parameters before datasets.")
+        self._train = [self._vasp_dataset(f, f"data{i + 1}") for i, f in enumerate(train_vaspruns)]
+        self._test = [self._vasp_dataset(f, f"data{i + 1}") for i, f in enumerate(test_vaspruns)]
         return self
 
     def _ready(self):

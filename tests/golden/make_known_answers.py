@@ -22,7 +22,8 @@ tests/test_cxx/test_neighbor*.py (known_neighbors.json), the invariant-table
 values of tests/test_cxx/test_gtinv.py (known_gtinv.json), the energies of
 the Ti-Al legacy gtinv test and of the MgO cell-shape test
 (known_energies.json), radial-function settings computed by the reference's
-params_utils.py (known_params.json), and the MgO pair
+params_utils.py (known_params.json), the reference's reading of a few vasprun
+files (known_vasp.json), and the MgO pair
 and gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
@@ -277,6 +278,41 @@ def param_answers():
         out["distance"].append({"elements": elements, "distance": [[list(k), v] for k, v in dist.items()],
                                 "pair_params": [list(map(float, p)) for p in pp], "conditional": flag,
                                 "cond": [[list(k), v] for k, v in cond.items()]})
+    return out
+
+
+VASP_FILES = {
+    "vasprun-00001-MgO.xml": "/root/reference/tests/files/vasprun-00001-MgO.xml",
+    "vasprun-00002-MgO.xml": "/root/reference/tests/files/vasprun-00002-MgO.xml",
+    "vasprun-train1-00001.xml.polymlp": "data-vasp-MgO/vaspruns/train1/vasprun-00001.xml.polymlp",
+    "vasprun-test1-00010.xml.polymlp": "data-vasp-MgO/vaspruns/test1/vasprun-00010.xml.polymlp",
+}
+
+
+def vasp_answers():
+    """The reference's own vasprun reading (core/interface_vasp.py Vasprun and
+    parse_properties_from_vaspruns, imported from its sources with the compiled
+    module stubbed out) of a few files, copied alongside."""
+    import types
+
+    sys.path.insert(0, "/root/reference/src")
+    stub = types.ModuleType("pypolymlp.cxx.lib")
+    stub.libmlpcpp = None
+    sys.modules.setdefault("pypolymlp.cxx.lib", stub)
+    from pypolymlp.core.interface_vasp import Vasprun, parse_properties_from_vaspruns
+
+    out = {}
+    for name, src in VASP_FILES.items():
+        src = src if src.startswith("/") else os.path.join(FIT_DIR, src)
+        shutil.copyfile(src, os.path.join(OUT, name))
+        v = Vasprun(src)
+        st = v.structure
+        out[name] = {"energy": v.energy, "forces": v.forces.tolist(), "stress_kbar": v.stress.tolist(),
+                     "axis": st.axis.tolist(), "positions": st.positions.tolist(), "n_atoms": list(st.n_atoms),
+                     "elements": list(st.elements), "types": list(st.types), "volume": st.volume}
+    files = [os.path.join(OUT, n) for n in VASP_FILES]
+    sts, (e, f, s) = parse_properties_from_vaspruns(files)
+    out["_parsed"] = {"files": list(VASP_FILES), "energies": e.tolist(), "stresses_ev": s.tolist()}
     return out
 
 
@@ -546,6 +582,10 @@ def main():
         json.dump({"source": "src/pypolymlp/core/params_utils.py (run here)", "cases": param_answers()}, f,
                   indent=1)
     print("wrote known_params.json")
+    with open(os.path.join(OUT, "known_vasp.json"), "w") as f:
+        json.dump({"source": "src/pypolymlp/core/interface_vasp.py (run here)", "cases": vasp_answers()}, f,
+                  indent=1)
+    print("wrote known_vasp.json")
     with open(os.path.join(OUT, "known_gtinv.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_gtinv.py", "cases": gtinv_answers()}, f, indent=1)
     print("wrote known_gtinv.json")
