@@ -569,6 +569,8 @@ def main():
         print(cid, shape, approx)
     for name in X_POSCARS:
         shutil.copyfile(os.path.join(REF, "files", "poscars", name), os.path.join(OUT, name))
+    # the input file of test_api_features.py::test_features_from_infile1 (same model as X_MgO_gtinv)
+    shutil.copyfile(os.path.join(REF, "files", "mlps", "polymlp.in.gtinv.MgO"), os.path.join(OUT, "polymlp.in.gtinv.MgO"))
     with open(os.path.join(OUT, "known_x.json"), "w") as f:
         json.dump({"source": "tests/test_calc/test_compute_features.py", "cases": xcases}, f, indent=1)
     with open(os.path.join(OUT, "known_functions.json"), "w") as f:
