@@ -34,6 +34,15 @@ from pypolymlp_gb300 import _ffi
 from pypolymlp_gb300.calculator import PolymlpStructure, replace_types
 from pypolymlp_gb300.params import make_params_dict
 
+def _strtobool(v) -> bool:
+    t = str(v).strip().lower()
+    if t in ("y", "yes", "t", "true", "on", "1"):
+        return True
+    if t in ("n", "no", "f", "false", "off", "0"):
+        return False
+    raise ValueError(f"invalid truth value {v!r}")
+
+
 HARTREE_TO_EV = 27.211386245981  # the reference's conversion (core/units.py:31)
 
 
@@ -114,7 +123,76 @@ class Pypolymlp:
         self._test = [self._dataset(test_structures, test_energies, test_forces, test_stresses, "data2")]
         return self
 
-    def _dataset(self, structures, energies, forces, stresses, name):
+    def load_parameter_file(self, file_params: str, train_ratio: float = 0.9, prefix: Optional[str] = None):
+        """Settings and vasprun datasets of a polymlp.in file
+        (core/parser_polymlp_params.py, parser_infile.py:15-30, dataset.py:119-140):
+        model keys as `set_params` takes them, `distance A B d1 d2 ...` lines,
+        `atomic_energy`, `reg_alpha_params`, `include_force` / `include_stress`,
+        and `train_data` / `test_data` / `data` lines "glob [include_force [weight]]"
+        (files sorted; `data` split by the reference's rule; the dataset is named by
+        its glob, `prefix` is prepended to it)."""
+        import glob
+
+        from pypolymlp_gb300.io_vasp import split_train_test
+
+        kv, distance, data_lines = {}, {}, []
+        with open(file_params) as f:
+            for line in f:
+                d = line.split("#", 1)[0].split()
+                if len(d) < 2:
+                    continue
+                if d[0] == "distance":
+                    distance[(d[1], d[2])] = [float(v) for v in d[3:]]
+                elif "data" in d[0] and "dataset_type" not in d[0]:
+                    data_lines.append(d)
+                else:
+                    kv[d[0]] = d[1:]
+        if kv.get("dataset_type", ["vasp"])[0] != "vasp":
+            raise NotImplementedError("only vasp datasets are read from parameter files")
+
+        def one(key, conv, default=None):
+            return conv(kv[key][0]) if key in kv else default
+
+        def triple(key, default):
+            if key not in kv:
+                return default
+            a, b, n = kv[key][:3]
+            return float(a), float(b), int(float(n))
+
+        kw = dict(elements=kv["elements"], include_force=one("include_force", _strtobool, True),
+                  include_stress=one("include_stress", _strtobool, True), cutoff=one("cutoff", float, 6.0),
+                  model_type=one("model_type", int, 4), max_p=one("max_p", int, 2),
+                  feature_type=one("feature_type", str, "gtinv"),
+                  gaussian_params1=triple("gaussian_params1", (1.0, 1.0, 1)),
+                  gaussian_params2=triple("gaussian_params2", (0.0, 5.0, 7)),
+                  n_gaussians=one("n_gaussians", int), distance=distance or None,
+                  reg_alpha_params=triple("reg_alpha_params", (-3.0, 1.0, 5)),
+                  gtinv_order=one("gtinv_order", int, 3),
+                  gtinv_maxl=tuple(int(v) for v in kv.get("gtinv_maxl", [4, 4, 2, 1, 1])),
+                  gtinv_version=one("gtinv_version", int, 1),
+                  atomic_energy=[float(v) for v in kv["atomic_energy"]] if "atomic_energy" in kv else None,
+                  enable_spins=[_strtobool(v) for v in kv["enable_spins"]] if "enable_spins" in kv else None)
+        self.set_params(**kw)
+        self._train, self._test = [], []
+        for d in data_lines:
+            tag, name = d[0], d[1]
+            files = sorted(glob.glob(name if prefix is None else prefix + "/" + name))
+            force = _strtobool(d[2]) if len(d) > 2 else self._params["include_force"]
+            force = force and self._params["include_force"]
+            stress = force and self._params["include_stress"]
+            weight = float(d[3]) if len(d) > 3 else 1.0
+            if tag == "train_data":
+                self._train.append(self._vasp_dataset(files, name, force, stress, weight))
+            elif tag == "test_data":
+                self._test.append(self._vasp_dataset(files, name, force, stress, weight))
+            elif tag == "data":
+                tr, te = split_train_test(files, train_ratio)
+                self._train.append(self._vasp_dataset(tr, name, force, stress, weight))
+                self._test.append(self._vasp_dataset(te, name, force, stress, weight))
+        return self
+
+    def _dataset(self, structures, energies, forces, stresses, name, include_force=None, include_stress=None,
+                 weight=1.0):
         """regression.Dataset of structures typed by the model's element order,
         atomic energies subtracted, stresses as (xx, yy, zz, xy, yz, zx)."""
         from pypolymlp_gb300.regression import Dataset
@@ -129,14 +207,15 @@ class Pypolymlp:
         if stresses is not None:
             t = np.asarray(stresses, dtype=np.float64).reshape(-1, 3, 3)
             s = np.stack([t[:, 0, 0], t[:, 1, 1], t[:, 2, 2], t[:, 0, 1], t[:, 1, 2], t[:, 2, 0]], axis=1)
-        return Dataset(axis, pos, types, e, f, s, include_force=self._params["include_force"],
-                       include_stress=self._params["include_stress"], name=name)
+        force = self._params["include_force"] if include_force is None else include_force
+        stress = self._params["include_stress"] if include_stress is None else include_stress
+        return Dataset(axis, pos, types, e, f, s, include_force=force, include_stress=stress, weight=weight, name=name)
 
-    def _vasp_dataset(self, files, name):
+    def _vasp_dataset(self, files, name, include_force=None, include_stress=None, weight=1.0):
         from pypolymlp_gb300.io_vasp import parse_properties_from_vaspruns
 
         sts, (e, f, s) = parse_properties_from_vaspruns(sorted(files), verbose=self._verbose)
-        return self._dataset(sts, e, f, s, name)
+        return self._dataset(sts, e, f, s, name, include_force, include_stress, weight)
 
     def set_datasets_vasp(self, train_vaspruns: Optional[Sequence[str]] = None,
                           test_vaspruns: Optional[Sequence[str]] = None, vaspruns=None, train_ratio: float = 0.9):

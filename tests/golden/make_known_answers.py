@@ -398,6 +398,7 @@ def fit_known_answers():
     test_src = os.path.join(FIT_DIR, "test_mlp_devel_vasp.py")
     for cid, (infile, test_fn, helper, names) in FIT_CASES.items():
         inp = _read_input(os.path.join(FIT_DIR, infile))
+        shutil.copyfile(os.path.join(FIT_DIR, infile), os.path.join(OUT, infile))
         elements = inp["elements"]
         atom_e = np.array([float(v) for v in inp["atomic_energy"]])
         for tag in names:

@@ -171,3 +171,43 @@ def test_distance_conditioned_radial_functions_match_reference():
                          elements=c["elements"], distance={tuple(k): v for k, v in c["distance"]})
     assert p["model"]["pair_conditional"] and p["model"]["pair_params"] == c["pair_params"]
     assert p["model"]["pair_params_conditional"] == {tuple(k): v for k, v in c["cond"]}
+
+
+@pytest.mark.parametrize("name", ["pair_single", "gtinv_single", "gtinv_multi"])
+def test_load_parameter_file_reads_the_reference_input(name, tmp_path):
+    """The reference's input files of the known fits (data locations absent here):
+    the model (feature count), alphas, stress flag, and one dataset per data line
+    named by its glob."""
+    from test_known_fit import KA, _cases
+
+    from pypolymlp_gb300.features_attr import get_num_features
+
+    files = {"pair_single": "polymlp.in.vasp.pair.single.MgO", "gtinv_single": "polymlp.in.vasp.single.MgO",
+             "gtinv_multi": "polymlp.in.vasp.multi.MgO"}
+    st = _cases()[name]["settings"]
+    pm = Pypolymlp().load_parameter_file(f"{KA}/{files[name]}", prefix=str(tmp_path))
+    assert get_num_features(pm.parameters) == st["n_features"]
+    np.testing.assert_allclose(pm._alphas, st["alphas"], rtol=1e-15)
+    assert pm.parameters["include_stress"] == st["include_stress"]
+    n_sets = 2 if name == "gtinv_multi" else 1
+    assert len(pm.train) == len(pm.test) == n_sets
+    assert all(d.name.startswith("data-vasp-MgO/vaspruns/") and len(d) == 0 for d in pm.train + pm.test)
+
+
+def test_load_parameter_file_dataset_lines(tmp_path):
+    """train_data / test_data / data lines: glob, include_force flag, weight."""
+    from test_known_fit import KA
+
+    text = "\n".join(["n_type 2", "elements Mg O", "feature_type pair", "cutoff 6.0", "model_type 2", "max_p 2",
+                      "atomic_energy -0.5 -1.5", "distance Mg O 2.1", "",
+                      "train_data vasprun-0000*-MgO.xml True 2.0",
+                      "test_data vasprun-t*.xml.polymlp False",
+                      "data vasprun-*.xml* True 0.5"])
+    path = tmp_path / "polymlp.in"
+    path.write_text(text + "\n")
+    pm = Pypolymlp().load_parameter_file(str(path), train_ratio=0.75, prefix=KA)
+    assert [len(d) for d in pm.train] == [2, 3] and [len(d) for d in pm.test] == [2, 1]
+    a, b = pm.train[0], pm.test[0]
+    assert a.include_force and a.include_stress and a.weight == 2.0 and a.name == "vasprun-0000*-MgO.xml"
+    assert not b.include_force and not b.include_stress and b.weight == 1.0
+    assert pm.train[1].weight == 0.5 and pm.parameters["model"]["pair_conditional"]
