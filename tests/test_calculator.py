@@ -166,3 +166,43 @@ def test_load_poscar_matches_the_test_reader():
 def test_properties_needs_a_model():
     with pytest.raises(RuntimeError):
         calc.Properties()
+
+
+class _FakeAtoms:
+    """The ASE Atoms accessors the calculator uses (ASE is not installed here)."""
+
+    def __init__(self, st):
+        self.cell = st.axis.T
+        self._frac, self._symbols = st.positions.T, list(st.elements)
+
+    def get_scaled_positions(self):
+        return self._frac
+
+    def get_chemical_symbols(self):
+        return self._symbols
+
+    def get_volume(self):
+        return abs(np.linalg.det(self.cell))
+
+
+def test_ase_calculator_reproduces_reference_known_answers(on_oracle):
+    """calculator/utils/ase_calculator.py: energy, forces (n_atom, 3), stress in
+    eV per cell (the reference's order), for atoms with interleaved elements."""
+    from pypolymlp_gb300.ase_calculator import PolymlpASECalculator, ase_atoms_to_structure
+
+    case = _cases()["MgO_pair_yaml"]
+    st = calc.load_poscar(os.path.join(KA, case["structure"]))
+    perm = np.array([0, 4, 1, 5, 2, 6, 3, 7])
+    shuffled = calc.PolymlpStructure(st.axis, st.positions[:, perm], st.n_atoms, [st.elements[i] for i in perm],
+                                     [st.types[i] for i in perm])
+    atoms = _FakeAtoms(shuffled)
+    assert ase_atoms_to_structure(atoms).elements == ["Mg", "O"] * 4
+    ase_calc = PolymlpASECalculator(pot=_pots(case)[0])
+    e = ase_calc.get_potential_energy(atoms)
+    assert e == pytest.approx(case["energy"], **case["energy_tol"])
+    f = ase_calc.get_forces(atoms)
+    np.testing.assert_allclose(f, np.array(case["forces"])[perm], atol=case["forces_atol"], rtol=0)
+    s = ase_calc.get_stress(atoms) * 160.21766208 / abs(np.linalg.det(st.axis))
+    np.testing.assert_allclose(s, case["stresses"], atol=case["stresses_atol"], rtol=0)
+    with pytest.raises(RuntimeError):
+        PolymlpASECalculator()
