@@ -26,7 +26,7 @@ path.  `load_poscar` reads a POSCAR as the reference's Poscar class does
 from __future__ import annotations
 
 import re
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Optional, Sequence, Union
 
 import numpy as np
@@ -51,7 +51,6 @@ class PolymlpStructure:
     volume: Optional[float] = None
     comment: Optional[str] = None
     name: Optional[str] = None
-    extra: dict = field(default_factory=dict)
 
     def __post_init__(self):
         self.axis = np.asarray(self.axis, dtype=np.float64)
