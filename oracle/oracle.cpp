@@ -817,3 +817,154 @@ int or_ylm(double r, double x, double y, double z, int lmax, double* ylm, double
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- PolymlpAPI surface
+// The per-type steps of PolymlpAPI on given order parameters, for the
+// reference's own unit tests (tests/test_cxx/test_polymlp_api*.py).
+namespace {
+
+std::vector<cd> complex_in(const double* a, size_t n) {
+    std::vector<cd> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = cd(a[2 * i], a[2 * i + 1]);
+    return v;
+}
+
+const pg::TypeTables& type_tables(const pg::ModelTables& mt, int type) {
+    if (type < 0 || type >= (int)mt.types.size()) throw std::runtime_error("type out of range");
+    return mt.types[type];
+}
+
+}  // namespace
+
+int or_api_sizes(const pg_feature_params* p, int type, int* sizes) {
+    return guarded([&] {
+        const Model m(p);
+        const auto& tt = type_tables(m.mt, type);
+        sizes[0] = (int)tt.full.size();
+        sizes[1] = (int)tt.noconj.size();
+        sizes[2] = (int)tt.ntp.size();
+        sizes[3] = (int)tt.lin_index.size();
+        sizes[4] = (int)(m.mt.fp.gtinv ? tt.noconj.size() : tt.ntp.size());
+    });
+}
+
+// m of each no-conjugate a_nlm entry, in the input order of or_api_conjugate
+int or_api_noconj_m(const pg_feature_params* p, int type, int* m) {
+    return guarded([&] {
+        const Model mo(p);
+        const auto& tt = type_tables(mo.mt, type);
+        for (size_t q = 0; q < tt.noconj.size(); ++q) m[q] = tt.noconj[q].m;
+    });
+}
+
+// compute_anlmtp_conjugate (polymlp_api.cpp:62-80)
+int or_api_conjugate(const pg_feature_params* p, int type, const double* re, const double* im, double* a) {
+    return guarded([&] {
+        const Model m(p);
+        const auto& tt = type_tables(m.mt, type);
+        std::vector<cd> out(tt.full.size(), cd());
+        for (size_t q = 0; q < tt.noconj.size(); ++q) {
+            const auto& e = tt.noconj[q];
+            out[e.ilocal_id] = cd(re[q], im[q]);
+            out[e.ilocal_conj_id] = cd(e.cc * re[q], -e.cc * im[q]);
+        }
+        for (size_t i = 0; i < out.size(); ++i) {
+            a[2 * i] = out[i].real();
+            a[2 * i + 1] = out[i].imag();
+        }
+    });
+}
+
+// Features::compute_features (polymlp_features.cpp:155-206)
+int or_api_features(const pg_feature_params* p, int type, const double* a, double* out) {
+    return guarded([&] {
+        const Model m(p);
+        const auto& tt = type_tables(m.mt, type);
+        if (m.mt.fp.gtinv) {
+            const auto av = complex_in(a, tt.full.size());
+            for (size_t f = 0; f < tt.lin_index.size(); ++f) {
+                double v = 0.0;
+                for (const auto& s : tt.value_terms[f]) v += s.coeff * product_real(s.ids, av);
+                out[f] = v;
+            }
+        } else {
+            for (size_t f = 0; f < tt.lin_index.size(); ++f) out[f] = a[tt.value_terms[f][0].ids[0]];
+        }
+    });
+}
+
+// Features::compute_features_deriv (polymlp_features.cpp:208-248), gtinv
+int or_api_features_deriv(const pg_feature_params* p, int type, const double* a, const double* dax,
+                          const double* day, const double* daz, const double* das, int n_col, double* ox,
+                          double* oy, double* oz, double* os) {
+    return guarded([&] {
+        const Model m(p);
+        if (!m.mt.fp.gtinv) throw std::runtime_error("feature derivatives from a_nlm need a gtinv model");
+        const auto& tt = type_tables(m.mt, type);
+        const size_t K = tt.full.size(), nl = tt.lin_index.size();
+        const auto av = complex_in(a, K);
+        const auto vx = complex_in(dax, K * n_col), vy = complex_in(day, K * n_col), vz = complex_in(daz, K * n_col);
+        const auto vs = complex_in(das, K * 6);
+        std::fill(ox, ox + nl * n_col, 0.0);
+        std::fill(oy, oy + nl * n_col, 0.0);
+        std::fill(oz, oz + nl * n_col, 0.0);
+        std::fill(os, os + nl * 6, 0.0);
+        for (size_t f = 0; f < nl; ++f)
+            for (const auto& s : tt.deriv_terms[f]) {
+                const cd val = s.coeff * product<cd>(s.rest, av);
+                const size_t h = (size_t)s.head;
+                for (int q = 0; q < n_col; ++q) {
+                    ox[f * n_col + q] += prod_real(val, vx[h * n_col + q]);
+                    oy[f * n_col + q] += prod_real(val, vy[h * n_col + q]);
+                    oz[f * n_col + q] += prod_real(val, vz[h * n_col + q]);
+                }
+                for (int q = 0; q < 6; ++q) os[f * 6 + q] += prod_real(val, vs[h * 6 + q]);
+            }
+    });
+}
+
+// Potential::compute_sum_of_prod_anlmtp / _antp (polymlp_potential.cpp:203-295);
+// coefficients as the reference's parser returns them (twice the stored ones)
+int or_api_sum_of_prod(const pg_feature_params* p, const double* coeffs, int n_coeffs, int type, const double* a,
+                       double* pe, double* pf) {
+    return guarded([&] {
+        const Model m(p);
+        const auto& tt = type_tables(m.mt, type);
+        const auto terms = pg::build_potential_terms(m.mt, std::vector<double>(coeffs, coeffs + n_coeffs));
+        const auto& heads = terms[type];
+        std::vector<double> feat(tt.lin_index.size());
+        if (or_api_features(p, type, a, feat.data()) != 0) throw std::runtime_error("feature values failed");
+        std::vector<double> pfv(tt.prod_features.size());
+        for (size_t q = 0; q < pfv.size(); ++q) pfv[q] = product<double>(tt.prod_features[q], feat);
+        if (m.mt.fp.gtinv) {
+            const auto av = complex_in(a, tt.full.size());
+            std::vector<cd> pd(tt.prod_deriv.size());
+            for (size_t q = 0; q < pd.size(); ++q) pd[q] = product<cd>(tt.prod_deriv[q], av);
+            for (size_t h = 0; h < heads.size(); ++h) {
+                cd se, sf;
+                for (const auto& pt : heads[h]) {
+                    se += pd[pt.prod_id] * (pfv[pt.prod_features_id] * pt.coeff_e);
+                    sf += pd[pt.prod_id] * (pfv[pt.prod_features_id] * pt.coeff_f);
+                }
+                pe[2 * h] = se.real();
+                pe[2 * h + 1] = se.imag();
+                pf[2 * h] = sf.real();
+                pf[2 * h + 1] = sf.imag();
+            }
+        } else {
+            std::vector<double> av(a, a + tt.ntp.size());
+            std::vector<double> pd(tt.prod_deriv.size());
+            for (size_t q = 0; q < pd.size(); ++q) pd[q] = product<double>(tt.prod_deriv[q], av);
+            for (size_t h = 0; h < heads.size(); ++h) {
+                double se = 0.0, sf = 0.0;
+                for (const auto& pt : heads[h]) {
+                    const double v = pfv[pt.prod_features_id] * pd[pt.prod_id];
+                    se += pt.coeff_e * v;
+                    sf += pt.coeff_f * v;
+                }
+                pe[h] = 0.5 * se;
+                pf[h] = 0.5 * sf;
+            }
+        }
+    });
+}

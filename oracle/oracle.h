@@ -38,6 +38,20 @@ int or_fn(double dis, double cutoff, int n_fn, const double* params, double* fn,
 int or_ylm(double r, double x, double y, double z, int lmax, double* ylm, double* ylm_dx, double* ylm_dy,
            double* ylm_dz);
 
+/* PolymlpAPI test surface (src/pypolymlp/cxx/src/polymlp/polymlp_api.cpp:62-190,
+ * polymlp_features.cpp:155-248, polymlp_potential.cpp:203-295) for one atom
+ * type; complex arrays interleave re/im.  sizes: [full a_nlm K, no-conjugate
+ * K0, a_ntp, linear features, potential heads]. */
+int or_api_sizes(const pg_feature_params* fp, int type, int* sizes);
+int or_api_noconj_m(const pg_feature_params* fp, int type, int* m);
+int or_api_conjugate(const pg_feature_params* fp, int type, const double* re, const double* im, double* a);
+int or_api_features(const pg_feature_params* fp, int type, const double* a, double* out);
+int or_api_features_deriv(const pg_feature_params* fp, int type, const double* a, const double* dax,
+                          const double* day, const double* daz, const double* das, int n_col, double* ox,
+                          double* oy, double* oz, double* os);
+int or_api_sum_of_prod(const pg_feature_params* fp, const double* coeffs, int n_coeffs, int type, const double* a,
+                       double* pe, double* pf);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,3 +119,60 @@ def ylm(r: float, x: float, y: float, z: float, lmax: int):
     _check(_load().or_ylm(C.c_double(r), C.c_double(x), C.c_double(y), C.c_double(z), lmax,
                           *[_p(a, C.c_double) for a in arrs]))
     return [a[0::2] + 1j * a[1::2] for a in arrs]
+
+
+class PolymlpAPI:
+    """The per-type PolymlpAPI steps of the reference (polymlp_api.cpp:62-190) on
+    given order parameters: conjugate completion, features, feature derivatives
+    and the adjoint sums (coefficients as the reference's parser returns them)."""
+
+    def __init__(self, params_dict, coeffs=None):
+        self._fp = FeatureParams(params_dict)
+        self._gtinv = params_dict["model"]["feature_type"] == "gtinv"
+        self._c = None if coeffs is None else np.ascontiguousarray(coeffs, dtype=np.float64)
+
+    def sizes(self, t):
+        s = np.zeros(5, np.int32)
+        _check(_load().or_api_sizes(self._fp.ref(), t, _p(s, C.c_int)))
+        return [int(v) for v in s]
+
+    @staticmethod
+    def _cplx(a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.complex128))
+        return a.view(np.float64)
+
+    def compute_anlmtp_conjugate(self, re, im, t):
+        k, k0 = self.sizes(t)[:2]
+        re = np.ascontiguousarray(np.asarray(re, dtype=np.float64)[:k0])
+        im = np.ascontiguousarray(np.asarray(im, dtype=np.float64)[:k0])
+        out = np.zeros(k, np.complex128)
+        _check(_load().or_api_conjugate(self._fp.ref(), t, _p(re, C.c_double), _p(im, C.c_double),
+                                        _p(out.view(np.float64), C.c_double)))
+        return out
+
+    def compute_features(self, a, t):
+        out = np.zeros(self.sizes(t)[3])
+        src = self._cplx(a) if self._gtinv else np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+        _check(_load().or_api_features(self._fp.ref(), t, _p(src, C.c_double), _p(out, C.c_double)))
+        return out
+
+    def compute_features_deriv(self, a, dfx, dfy, dfz, ds, t):
+        nl = self.sizes(t)[3]
+        n_col = np.asarray(dfx).shape[1]
+        outs = [np.zeros((nl, n_col)), np.zeros((nl, n_col)), np.zeros((nl, n_col)), np.zeros((nl, 6))]
+        ins = [self._cplx(v) for v in (a, dfx, dfy, dfz, ds)]
+        _check(_load().or_api_features_deriv(self._fp.ref(), t, *[_p(v, C.c_double) for v in ins], n_col,
+                                             *[_p(o, C.c_double) for o in outs]))
+        return outs
+
+    def compute_sum_of_prod(self, a, t):
+        n = self.sizes(t)[4]
+        if self._gtinv:
+            src, pe, pf = self._cplx(a), np.zeros(n, np.complex128), np.zeros(n, np.complex128)
+            pe_p, pf_p = pe.view(np.float64), pf.view(np.float64)
+        else:
+            src, pe, pf = np.ascontiguousarray(np.asarray(a, dtype=np.float64)), np.zeros(n), np.zeros(n)
+            pe_p, pf_p = pe, pf
+        _check(_load().or_api_sum_of_prod(self._fp.ref(), _p(self._c, C.c_double), len(self._c), t,
+                                          _p(src, C.c_double), _p(pe_p, C.c_double), _p(pf_p, C.c_double)))
+        return pe, pf

@@ -363,3 +363,27 @@ int ref_parse_potential(const char* file, int legacy, char* buf, size_t len) {
 }
 
 }  // extern "C"
+
+// PolymlpAPI::parse_polymlp_file + compute_sum_of_prod_anlmtp
+// (polymlp_api.cpp:20-32, polymlp_potential.cpp:235-289): a (interleaved re/im,
+// the type's full a_nlm order) -> prod_sum_e / prod_sum_f (interleaved, *n heads).
+extern "C" int ref_api_sum_of_prod(const char* file, const char* ele0, const char* ele1, int type, const double* a, int K,
+                        double* pe, double* pf, int* n) {
+    return guarded([&] {
+        PolymlpAPI api;
+        std::vector<std::string> ele{ele0, ele1};
+        vector1d mass{1.0, 1.0};
+        api.parse_polymlp_file(file, ele, mass);
+        vector1dc av(K);
+        for (int i = 0; i < K; ++i) av[i] = dc(a[2 * i], a[2 * i + 1]);
+        vector1dc e, f;
+        api.compute_sum_of_prod_anlmtp(av, type, e, f);
+        *n = (int)e.size();
+        for (size_t i = 0; i < e.size(); ++i) {
+            pe[2 * i] = e[i].real();
+            pe[2 * i + 1] = e[i].imag();
+            pf[2 * i] = f[i].real();
+            pf[2 * i + 1] = f[i].imag();
+        }
+    });
+}

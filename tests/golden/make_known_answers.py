@@ -23,7 +23,8 @@ values of tests/test_cxx/test_gtinv.py (known_gtinv.json), the energies of
 the Ti-Al legacy gtinv test and of the MgO cell-shape test
 (known_energies.json), radial-function settings computed by the reference's
 params_utils.py (known_params.json), the reference's reading of a few vasprun
-files (known_vasp.json), and the MgO pair
+files (known_vasp.json), the PolymlpAPI sums of tests/test_cxx/test_polymlp_api*.py
+(known_api.json), and the MgO pair
 and gtinv fits of
 tests/test_mlp_dev_api/test_mlp_devel_vasp.py (their vasprun data as arrays,
 fit_MgO.npz, and the asserted train/test errors, known_fit.json).
@@ -316,6 +317,36 @@ def vasp_answers():
     return out
 
 
+API_TESTS = {"test_polymlp_api.py": "polymlp.yaml.MgO", "test_polymlp_api_pair.py": "polymlp.yaml.pair.MgO"}
+
+
+def api_answers():
+    """Shapes and sums asserted by tests/test_cxx/test_polymlp_api*.py (the
+    PolymlpAPI steps on arange / constant order parameters), per test function:
+    [variable, "shape" | "sum", expected]; the potential files they load are
+    copied (as api.<name>)."""
+    out = {}
+    for fname, pot in API_TESTS.items():
+        tree = ast.parse(open(os.path.join("/root/reference/tests/test_cxx", fname)).read())
+        shutil.copyfile(os.path.join("/root/reference/tests/files", pot), os.path.join(OUT, "api." + pot))
+        for fn in tree.body:
+            if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_compute"):
+                continue
+            checks = []
+            for st in ast.walk(fn):
+                if not (isinstance(st, ast.Assert) and isinstance(st.test, ast.Compare)):
+                    continue
+                left, right = st.test.left, st.test.comparators[0]
+                if isinstance(left, ast.Attribute) and left.attr == "shape":
+                    checks.append([left.value.id, "shape", list(ast.literal_eval(right))])
+                elif isinstance(left, ast.Call) and getattr(left.func, "attr", "") == "sum":
+                    want = ast.literal_eval(right.args[0] if isinstance(right, ast.Call) else right)
+                    want = [want.real, want.imag] if isinstance(want, complex) else [float(want), 0.0]
+                    checks.append([left.args[0].id, "sum", want])
+            out[f"{fname}::{fn.name}"] = {"potential": "api." + pot, "checks": checks}
+    return out
+
+
 FIT_DIR = "/root/reference/tests/test_mlp_dev_api"
 EV_TO_KBAR = 1602.1766208
 
@@ -589,6 +620,9 @@ def main():
         json.dump({"source": "src/pypolymlp/core/interface_vasp.py (run here)", "cases": vasp_answers()}, f,
                   indent=1)
     print("wrote known_vasp.json")
+    with open(os.path.join(OUT, "known_api.json"), "w") as f:
+        json.dump({"source": "tests/test_cxx/test_polymlp_api*.py", "cases": api_answers()}, f, indent=1)
+    print("wrote known_api.json")
     with open(os.path.join(OUT, "known_gtinv.json"), "w") as f:
         json.dump({"source": "tests/test_cxx/test_gtinv.py", "cases": gtinv_answers()}, f, indent=1)
     print("wrote known_gtinv.json")
