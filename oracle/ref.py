@@ -191,3 +191,16 @@ def parse_potential(path: str, legacy: bool = False) -> dict:
         else:
             out[key] = np.array([float(v) for v in vals])
     return out
+
+
+def api_sum_of_prod(path: str, elements, type1: int, anlmtp):
+    """PolymlpAPI::parse_polymlp_file + compute_sum_of_prod_anlmtp of the reference
+    build: (prod_sum_e, prod_sum_f), complex."""
+    a = np.ascontiguousarray(np.asarray(anlmtp, dtype=np.complex128))
+    k = len(a)
+    pe, pf = np.zeros(2 * k), np.zeros(2 * k)
+    n = C.c_int()
+    _check(_load().ref_api_sum_of_prod(path.encode(), elements[0].encode(), elements[1].encode(), type1,
+                                       _p(a.view(np.float64), C.c_double), k, _p(pe, C.c_double),
+                                       _p(pf, C.c_double), C.byref(n)))
+    return pe.view(np.complex128)[:n.value], pf.view(np.complex128)[:n.value]

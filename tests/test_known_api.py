@@ -64,3 +64,29 @@ def test_oracle_reproduces_polymlp_api_known_answers(name):
         else:
             got = complex(np.sum(v[var]))
             assert got == pytest.approx(complex(*want)), (var, got, want)
+
+
+@pytest.mark.parametrize("type1", [0, 1])
+def test_oracle_adjoint_sums_match_reference_build(type1):
+    """On a_nlm with real m = 0 entries (as physical ones are), per head."""
+    import ctypes as C
+
+    from oracle import ref
+    from oracle.oracle import PolymlpAPI, _check, _load, _p
+
+    if not ref.available():
+        pytest.skip("the reference build (oracle/_ref) is not present")
+    path = os.path.join(KA, "api.polymlp.yaml.MgO")
+    p, c = io_polymlp.load_mlp(path)
+    api = PolymlpAPI(p, 2.0 * c)
+    k0 = api.sizes(type1)[1]
+    m = np.zeros(k0, np.int32)
+    _check(_load().or_api_noconj_m(api._fp.ref(), type1, _p(m, C.c_int)))
+    rng = np.random.default_rng(5 + type1)
+    re, im = rng.normal(size=k0), rng.normal(size=k0)
+    im[m == 0] = 0.0
+    a = api.compute_anlmtp_conjugate(re, im, type1)
+    pe, pf = api.compute_sum_of_prod(a, type1)
+    re_e, re_f = ref.api_sum_of_prod(path, ["Mg", "O"], type1, a)
+    np.testing.assert_allclose(pe, re_e, rtol=1e-12, atol=1e-12 * np.abs(re_e).max())
+    np.testing.assert_allclose(pf, re_f, rtol=1e-12, atol=1e-12 * np.abs(re_f).max())
