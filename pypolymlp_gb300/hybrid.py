@@ -18,7 +18,7 @@ rows 3 a + c of its active atoms a.
 
 from __future__ import annotations
 
-from typing import Sequence
+from typing import Optional, Sequence
 
 import numpy as np
 
@@ -132,3 +132,69 @@ class PotentialHybridModel:
 
     def get_n_data(self):
         return self._n_data
+
+
+def hybrid_normal_equations(params_list: Sequence[dict], datasets, precision: int = _ffi.PG_FP64,
+                            weight_stress: float = 0.1, min_energy: Optional[float] = None, scales=None,
+                            batch_size: int = 500):
+    """Scaled normal equations of a hybrid model (regression.DataXY), as the
+    reference's calc_xtx_xty forms them for PotentialHybridModel's X
+    (mlp_dev/core/data_sequential.py:95-160): per batch of structures the rows of X
+    on the GPU (`hybrid_features_x`), the column sums of the unweighted energy
+    rows, the reference's weights and targets, and the Gram of the weighted rows
+    on the device (`_ffi.gram_xtx`); then the feature scales and zero columns of
+    `regression.compute_scales`."""
+    from pypolymlp_gb300 import regression as rg
+
+    min_energy = rg.get_min_energy(datasets) if min_energy is None else min_energy
+    xtx = xty = xe_sum = xe_sq = None
+    yty, n_total = 0.0, 0
+    for d in datasets:
+        for b in range(0, len(d), batch_size):
+            sub = d.slice(b, min(len(d), b + batch_size))
+            e_row, f_row, s_row, n_rows, w, y = rg.weights_and_targets(sub, min_energy, weight_stress)
+            st = Structures(sub.axis, sub.positions, sub.types)
+            x, cum = hybrid_features_x(params_list, st, e_row, f_row, s_row, n_rows, precision)
+            xe = x[np.asarray(e_row)]
+            xw = np.asfortranarray(x * np.asarray(w)[:, None])
+            g, r = _ffi.gram_xtx(xw, precision), xw.T @ np.asarray(y)
+            if xtx is None:
+                xtx, xty, xe_sum, xe_sq = g, r, xe.sum(axis=0), np.square(xe).sum(axis=0)
+            else:
+                xtx, xty = xtx + g, xty + r
+                xe_sum, xe_sq = xe_sum + xe.sum(axis=0), xe_sq + np.square(xe).sum(axis=0)
+            yty += float(np.asarray(y) @ np.asarray(y))
+            n_total += int(n_rows)
+    n_data = sum(len(d.energies) for d in datasets)
+    scales, zero_ids = rg.compute_scales(scales, xe_sum, xe_sq, n_data, any(d.include_force for d in datasets))
+    xtx = np.array(xtx, dtype=np.float64)
+    xtx[zero_ids] = 0.0
+    xtx[:, zero_ids] = 0.0
+    xty = np.array(xty, dtype=np.float64)
+    xty[zero_ids] = 0.0
+    xtx /= scales[:, None]
+    xtx /= scales[None, :]
+    xty /= scales
+    return rg.DataXY(xtx, xty, yty, n_total, scales, zero_ids, min_energy, xe_sum, xe_sq), cum
+
+
+def fit_hybrid(params_list: Sequence[dict], train, test, alphas: Sequence[float], precision: int = _ffi.PG_FP64,
+               weight_stress: float = 0.1):
+    """Ridge fit of a hybrid model (the reference's fit over PotentialHybridModel,
+    mlp_dev/standard/fit.py:12-60): the training normal equations, posv per
+    alpha on the device, the test normal equations with the training scales and
+    reference energy, the alpha of the smallest test RMSE (compute_rmse_seq).
+    Returns (regression.FitResult, cumulative feature counts of the models)."""
+    from pypolymlp_gb300 import regression as rg
+
+    alphas = np.asarray(alphas, dtype=np.float64)
+    xy, cum = hybrid_normal_equations(params_list, train, precision, weight_stress)
+    coefs, info = rg.solver_ridge(xy.xtx, xy.xty, alphas)
+    txy, _ = hybrid_normal_equations(params_list, test, precision, weight_stress, min_energy=xy.min_energy,
+                                     scales=xy.scales)
+    rmse_train = np.asarray(rg.compute_rmse_seq(coefs, xy))
+    rmse_test = np.asarray(rg.compute_rmse_seq(coefs, txy))
+    idx = int(np.argmin(rmse_test))
+    res = rg.FitResult(coefs[:, idx], xy.scales, float(alphas[idx]), float(rmse_train[idx]),
+                       float(rmse_test[idx]), coefs, rmse_train, rmse_test, info)
+    return res, cum

@@ -95,6 +95,24 @@ class Pypolymlp:
         self._atomic_energy = self._expand_atomic_energy(self._params, list(atomic_energy))
         return self
 
+    def append_hybrid_params(self, **kwargs):
+        """Add one more model over the same elements (a hybrid; mlp_dev/pypolymlp.py:152-237):
+        the settings of `set_params`; the datasets and alphas stay those of the first model."""
+        if self._params is None:
+            raise RuntimeError("Set the first model's parameters before appending hybrid ones.")
+        first = (self._params, self._alphas, self._atomic_energy)
+        self.set_params(**kwargs)
+        extra = self._params
+        self._params, self._alphas, self._atomic_energy = first
+        if list(extra["elements"]) != list(self._params["elements"]):
+            raise ValueError("hybrid models here share the first model's elements")
+        self._hybrid = getattr(self, "_hybrid", []) + [extra]
+        return self
+
+    @property
+    def _models(self) -> list:
+        return [self._params] + list(getattr(self, "_hybrid", []))
+
     @staticmethod
     def _expand_atomic_energy(params: dict, per_element: list) -> np.ndarray:
         """Atomic energy per atom type (spin-split elements repeat theirs)."""
@@ -260,6 +278,12 @@ class Pypolymlp:
         from pypolymlp_gb300 import regression
 
         self._ready()
+        if len(self._models) > 1:
+            from pypolymlp_gb300.hybrid import fit_hybrid
+
+            res, self._cumulative = fit_hybrid(self._models, self._train, self._test, self._alphas,
+                                               precision=_ffi.PG_FP64)
+            return self._set_result(res)
         res = regression.fit(self._params, self._train, self._test, self._alphas, precision=self._precision,
                              fp64_fallback=self._precision == _ffi.PG_MIXED)
         return self._set_result(res)
@@ -289,9 +313,31 @@ class Pypolymlp:
 
         if self._coeffs is None:
             raise RuntimeError("Regression must be performed before estimating errors.")
+        if len(self._models) > 1:
+            return self._estimate_error_hybrid()
         acc = PolymlpEvalAccuracy(self._params, self._coeffs / self._scales, verbose=self._verbose)
         self._error_train = acc.compute_error(self._train, log_energy=log_energy, path_output=file_path, tag="train")
         self._error_test = acc.compute_error(self._test, log_energy=log_energy, path_output=file_path, tag="test")
+        return self
+
+    def _estimate_error_hybrid(self):
+        """Errors of the summed models (hybrid.PropertiesHybrid on the GPU)."""
+        from pypolymlp_gb300.accuracy import prediction_errors
+        from pypolymlp_gb300.hybrid import PropertiesHybrid
+
+        bounds = [0] + list(self._cumulative)
+        c = self._coeffs / self._scales
+        ph = PropertiesHybrid(self._models, [c[bounds[k]:bounds[k + 1]] for k in range(len(self._models))],
+                              _ffi.PG_FP64)
+
+        def errors(datasets):
+            out = {}
+            for d in datasets:
+                e, f, s = ph.eval_multiple(d.axis, [np.asarray(x).T for x in d.positions], d.types)
+                out[d.name], _ = prediction_errors(d, e, f, s)
+            return out
+
+        self._error_train, self._error_test = errors(self._train), errors(self._test)
         return self
 
     def run(self, batch_size: Optional[int] = None, use_cg: bool = False, gtol: float = 1e-2,
@@ -325,7 +371,14 @@ class Pypolymlp:
 
         if self._coeffs is None:
             raise RuntimeError("No polymlp has been developed.")
-        save_mlp_yaml(self._params, self._coeffs, self._scales, filename)
+        if len(self._models) == 1:
+            save_mlp_yaml(self._params, self._coeffs, self._scales, filename)
+            return self
+        # a hybrid: filename.1, filename.2, ... with each model's columns (pypolymlp.py:710-719)
+        bounds = [0] + list(self._cumulative)
+        for k, p in enumerate(self._models):
+            sl = slice(bounds[k], bounds[k + 1])
+            save_mlp_yaml(p, self._coeffs[sl], self._scales[sl], f"{filename}.{k + 1}")
         return self
 
     def load_mlp(self, filename: str = "polymlp.yaml"):
@@ -381,7 +434,7 @@ class Pypolymlp:
     def n_features(self) -> int:
         from pypolymlp_gb300.features_attr import get_num_features
 
-        return get_num_features(self._params)
+        return get_num_features(self._models)
 
     @property
     def errors(self):

@@ -102,3 +102,49 @@ def test_hybrid_x_matches_oracle_per_model():
     scale = np.maximum(np.abs(ref).max(axis=0), 1e-300)
     assert (np.abs(x - ref) / scale).max() < 1e-10
     assert cum == [x0.shape[1], x0.shape[1] + x1.shape[1]]
+
+
+def _oracle_hybrid_x(params_list, st, e_row, f_row, s_row, n_rows, precision=None):
+    """hybrid_features_x with the oracle's X per model (checker only)."""
+    from oracle import oracle
+
+    offs = st.atom_offsets
+    cum, blocks = [], []
+    for p in params_list:
+        pos = [st.positions[offs[s]:offs[s + 1]] for s in range(st.n_st)]
+        types = [st.types[offs[s]:offs[s + 1]] for s in range(st.n_st)]
+        sel = [active_atoms(t, p) for t in types]
+        sub = Structures(list(st.axis), [pos[s][sel[s][0]] for s in range(st.n_st)], [sel[s][1] for s in range(st.n_st)])
+        e, f, s6, n = row_layout(sub.n_atoms, [f_row[s] >= 0 for s in range(st.n_st)])
+        xs = oracle.features_x(p, sub, e, f, s6, n)
+        x = np.zeros((n_rows, xs.shape[1]))
+        for s in range(st.n_st):
+            x[e_row[s]] = xs[e[s]]
+            if f_row[s] >= 0:
+                x[s_row[s]:s_row[s] + 6] = xs[s6[s]:s6[s] + 6]
+                rows = f_row[s] + (3 * sel[s][0][:, None] + np.arange(3)[None, :]).reshape(-1)
+                x[rows] = xs[f[s]:f[s] + 3 * len(sel[s][0])]
+        blocks.append(x)
+        cum.append(sum(b.shape[1] for b in blocks))
+    return np.asfortranarray(np.hstack(blocks)), cum
+
+
+def test_hybrid_fit_of_one_model_reproduces_reference_fit_errors(monkeypatch):
+    """fit_hybrid with the pair MgO model alone, on the reference's MgO fit data, must
+    give the reference's asserted errors (test_mlp_devel_vasp.py::test_mlp_devel_pair);
+    the GPU X rows, device Gram and device posv are replaced by the oracle, numpy and
+    LAPACK (checker only)."""
+    from test_known_fit import _cases, _check, _datasets, _params, cpu_errors
+
+    from oracle.pipeline import solver_ridge_cpu
+    from pypolymlp_gb300 import _ffi, hybrid, regression
+
+    monkeypatch.setattr(hybrid, "hybrid_features_x", _oracle_hybrid_x)
+    monkeypatch.setattr(_ffi, "gram_xtx", lambda x, precision=None: x.T @ x)
+    monkeypatch.setattr(regression, "solver_ridge", lambda a, b, al: (solver_ridge_cpu(a, b, al), None))
+    case = _cases()["pair_single"]
+    p = _params(case["settings"])
+    train, test = _datasets(case)
+    res, cum = hybrid.fit_hybrid([p], train, test, case["settings"]["alphas"])
+    assert cum == [case["settings"]["n_features"]]
+    _check(cpu_errors(p, res.coeffs / res.scales, train + test), case["errors"])

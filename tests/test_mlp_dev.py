@@ -211,3 +211,50 @@ def test_load_parameter_file_dataset_lines(tmp_path):
     assert a.include_force and a.include_stress and a.weight == 2.0 and a.name == "vasprun-0000*-MgO.xml"
     assert not b.include_force and not b.include_stress and b.weight == 1.0
     assert pm.train[1].weight == 0.5 and pm.parameters["model"]["pair_conditional"]
+
+
+def test_hybrid_front_end_fits_saves_and_reloads(monkeypatch, tmp_path):
+    """Two pair models over Mg and O fitted together (append_hybrid_params): the GPU
+    X rows, Gram, posv and evaluator replaced by the oracle, numpy and LAPACK
+    (checker only).  The saved polymlp.yaml.1 / .2, evaluated together, give the
+    errors the fit reported."""
+    from test_hybrid import _oracle_hybrid_x
+
+    from oracle import oracle
+    from oracle.pipeline import solver_ridge_cpu
+    from pypolymlp_gb300 import hybrid, regression
+    from pypolymlp_gb300.abi import Structures  # noqa: F401
+
+    class _OracleRun:
+        def __init__(self, p, c, precision=None):
+            self._p, self._c = p, np.asarray(c, dtype=np.float64)
+
+        def run(self, st):
+            return oracle.evaluate(self._p, self._c, st)
+
+    monkeypatch.setattr(hybrid, "hybrid_features_x", _oracle_hybrid_x)
+    monkeypatch.setattr(_ffi, "gram_xtx", lambda x, precision=None: x.T @ x)
+    monkeypatch.setattr(_ffi, "Evaluator", _OracleRun)
+    monkeypatch.setattr(regression, "solver_ridge", lambda a, b, al: (solver_ridge_cpu(a, b, al), None))
+    pm, case = _front_end()
+    pm._train = [d.slice(0, 40) for d in pm._train]
+    pm._test = [d.slice(0, 10) for d in pm._test]
+    pm.append_hybrid_params(elements=["Mg", "O"], cutoff=5.0, model_type=2, max_p=2, feature_type="pair",
+                            gaussian_params2=(0.0, 4.0, 4))
+    pm.run()
+    train_err, _ = pm.errors
+    pm.save_mlp(str(tmp_path / "polymlp.yaml"))
+    from pypolymlp_gb300.accuracy import prediction_errors
+    from pypolymlp_gb300.io_polymlp import load_mlp
+
+    models = [load_mlp(str(tmp_path / f"polymlp.yaml.{k}")) for k in (1, 2)]
+    from pypolymlp_gb300.features_attr import get_num_features
+
+    assert [len(c) for _, c in models] == [case["settings"]["n_features"], get_num_features(models[1][0])]
+    assert pm.n_features == sum(len(c) for _, c in models)
+    ph = hybrid.PropertiesHybrid([p for p, _ in models], [c for _, c in models])
+    d = pm.train[0]
+    e, f, s = ph.eval_multiple(d.axis, [np.asarray(x).T for x in d.positions], d.types)
+    err, _ = prediction_errors(d, e, f, s)
+    for k in ("energy", "force", "stress"):
+        assert err[k] == pytest.approx(train_err["data1"][k], rel=1e-9)
