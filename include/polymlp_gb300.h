@@ -153,8 +153,10 @@ int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
  * dimension ld), on the device: the `xtx += x.T @ x` of calc_xtx_xty
  * (mlp_dev/core/data_sequential.py:145-152) for a block that is already
  * materialised.  PG_FP64: FP64 products and sums; PG_MIXED: X rounded to FP32,
- * BF16x3 products on the tensor cores, FP32 partial sums flushed to FP64 every
- * 4,096 rows.  xtx is F x F (full, symmetric).
+ * then per 1,024-row segment and column split into four BF16 fixed-point
+ * slices (28 bits of the segment's column maximum); 13 slice products on the
+ * tensor cores with exact FP32 partial sums and float-float segment sums give
+ * the Gram of those rows to ~1e-12.  xtx is F x F (full, symmetric).
  */
 int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int precision, double* xtx);
 
@@ -163,59 +165,48 @@ int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int
  * coefficient vectors C (F x n_coef, column-major, in X's own column scaling),
  * with the rows regenerated at the pg_gram's precision and accumulated in
  * FP64.  Writes X^T R (F x n_coef) and the sums of R^2 over energy, force and
- * stress rows (3 x n_coef, kind-major).  Used for FP64 iterative refinement
- * of a mixed-precision fit and for RMSEs from residuals rather than from
- * c^T A c - 2 c^T b + y^T y.
+ * stress rows (3 x n_coef, kind-major).  Used for the iterative refinement of
+ * a fit (r = X^T (y - X c)) and for test-set RMSEs from residuals.
  */
 int pg_batch_residual(pg_gram* g, pg_batch* b, const double* coefs, int n_coef, double* xtr, double* sq,
                       int64_t* n_rows);
-/*
- * X^T X V (F x n_v, n_v <= 16, column-major, X's own column scaling) of a
- * staged batch with the rows regenerated at the pg_gram's precision and the
- * products accumulated in FP64: the exact normal-matrix product that the
- * preconditioned conjugate-gradient ridge solve of a mixed-precision fit
- * iterates with.  No reference counterpart (the reference forms X^T X in FP64
- * and solves directly).
- */
-int pg_batch_normal_matvec(pg_gram* g, pg_batch* b, const double* v, int n_v, double* out);
 
 /*
- * Ridge solve over alphas in ascending order on the device, as solver_ridge
+ * Ridge solve for every alpha on the device, as solver_ridge
  * (src/pypolymlp/mlp_dev/standard/solvers.py:48-84) with LAPACK posv: for each
- * alpha, Cholesky of xtx + alpha*I and two triangular solves.  xtx (F x F) and
- * xty (F) are host arrays; coefs is F x n_alpha column-major.  info[i] != 0
- * marks a failed factorisation, for which the column is filled with 1e30.
+ * alpha, Cholesky of xtx + alpha*I and two triangular solves.  All alphas are
+ * factored together (one set of launches, no host round trip per alpha).
+ * xtx (F x F) and xty (F) are host arrays; coefs is F x n_alpha column-major.
+ * info[i] != 0 marks a failed factorisation, for which the column is filled
+ * with 1e30.
  */
 int pg_solve_ridge(int n_features, const double* xtx, const double* xty, const double* alphas,
                    int n_alpha, double* coefs, int* info);
-
 /*
- * The Cholesky factor of xtx + alpha*I kept on the device (factor once, solve
- * many), the preconditioner of the mixed-precision conjugate-gradient solve.
- * info != 0 marks a failed factorisation (solves then return 1e30).  The
- * factorisation is posv's (solvers.py:48-84); keeping it has no reference
- * counterpart.
+ * The same with one right-hand side per alpha: rhs is F x n_alpha
+ * (column-major), column i solved with xtx + alphas[i]*I.  Iterative
+ * refinement of a fit solves for per-alpha residuals; no reference
+ * counterpart (posv's right-hand side, solvers.py:21-46, is the same X^T y for
+ * every alpha).
  */
-typedef struct pg_ridge_factor pg_ridge_factor;
-int pg_ridge_factor_create(int n_features, const double* xtx, double alpha, pg_ridge_factor** out, int* info);
-int pg_ridge_factor_solve(pg_ridge_factor* f, const double* rhs, int n_rhs, double* x);
-int pg_ridge_factor_destroy(pg_ridge_factor* f);
+int pg_solve_ridge_rhs(int n_features, const double* xtx, const double* rhs, const double* alphas,
+                       int n_alpha, double* coefs, int* info);
 
 /*
  * Ridge solve that allocates no memory.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory at the point where
- * they solve - a host framework or inference server that owns the GPU's
- * allocator, code running while a CUDA stream is being captured, or a loop
- * that must never enter the allocator.  The caller passes device buffers:
+ * they solve - a host framework or inference server whose own allocator owns
+ * the GPU's memory, or a loop that must never enter the allocator.  The
+ * caller passes device buffers:
  * d_xtx (F x F, column-major, symmetric), d_xty (F) and d_coefs (F, written);
  * *info (host) is 0, or column + 1 of a failed factorisation (then d_coefs is
  * filled with 1e30), as for pg_solve_ridge with one alpha.  The factor is
  * built in a fixed device array inside the library: n_features must be at
  * most 1024 (larger sizes are rejected with an error), and each GPU that loads
  * the library keeps that array (about 8 MiB) until the process exits.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls on a device share
- * the array, so calls whose GPU work overlaps (other threads or streams) race.
+ * first call on a device looks up the array's address (cudaGetSymbolAddress).
+ * All calls on a device share the array and it keeps the last call's
+ * contents, so calls whose GPU work overlaps (other threads or streams) race.
  * Work is issued on the default stream and the call returns when it is done.
  */
 int pg_solve_ridge_noalloc(int n_features, const double* d_xtx, const double* d_xty, double alpha,

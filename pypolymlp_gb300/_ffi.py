@@ -62,14 +62,11 @@ def lib():
                 ("pg_batch_destroy", [_vp]),
                 ("pg_gram_accumulate_batch", [_vp, _vp]),
                 ("pg_batch_residual", [_vp, _vp, _dp, C.c_int, _dp, _dp, _i64p]),
-                ("pg_batch_normal_matvec", [_vp, _vp, _dp, C.c_int, _dp]),
                 ("pg_gram_xtx", [_dp, C.c_int64, C.c_int, C.c_int64, C.c_int, _dp]),
-                ("pg_ridge_factor_create", [C.c_int, _dp, C.c_double, C.POINTER(_vp), _ip]),
-                ("pg_ridge_factor_solve", [_vp, _dp, C.c_int, _dp]),
-                ("pg_ridge_factor_destroy", [_vp]),
                 ("pg_profile_enable", [C.c_int]),
                 ("pg_profile_read", [C.c_char_p, C.c_size_t, _dp, _ip, C.c_int, _ip]),
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
+                ("pg_solve_ridge_rhs", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
                 ("pg_solve_ridge_noalloc", [C.c_int, _vp, _vp, C.c_double, _vp, _ip]),
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),

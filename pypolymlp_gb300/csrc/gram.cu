@@ -5,9 +5,11 @@
 //
 //   pg_syrk_f64        FP64 path: upper-triangle tiles of X^T X on the
 //                      CUDA cores (64x64 tile per block, 4x4 per thread).
-//   gram_tc (file gram_tc.cu) mixed path: X (FP32) split into bf16 hi + lo,
-//                      X^T X ~= hi^T hi + hi^T lo + lo^T hi on the tcgen05
-//                      tensor cores, FP32 segments flushed into the FP64 Gram.
+//   gram_tc (file gram_tc.cu) mixed path: X (FP32) split into four BF16
+//                      fixed-point slices per 1,024-row segment, 13 slice
+//                      products on the tcgen05 tensor cores with exact FP32
+//                      partial sums, float-float segment sums: the Gram of
+//                      the FP32 rows to ~1e-12.
 //   helpers            energy-row sums, row weighting, X^T y.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -508,24 +510,6 @@ int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef,
         if (xtr) PG_CUDA(cudaMemcpy(xtr, XtR.as<double>(), (size_t)F * n_coef * 8, cudaMemcpyDeviceToHost));
         if (sq) PG_CUDA(cudaMemcpy(sq, SQ.as<double>(), (size_t)3 * n_coef * 8, cudaMemcpyDeviceToHost));
         if (n_rows) *n_rows = rows;
-    });
-}
-
-int pg_batch_normal_matvec(pg_gram* gh, pg_batch* b, const double* v, int n_v, double* out) {
-    return guarded([&] {
-        if (!gh || !b || !v || !out || n_v < 1) throw std::runtime_error("bad arguments");
-        if (n_v > kMaxCoef) throw std::runtime_error("at most 16 vectors per pass");
-        Gram& g = *gh->g;
-        const int F = g.F;
-        DevBuf V((size_t)F * n_v * 8), XtR((size_t)F * n_v * 8), R;
-        PG_CUDA(cudaMemcpy(V.as<void>(), v, (size_t)F * n_v * 8, cudaMemcpyHostToDevice));
-        PG_CUDA(cudaMemset(XtR.as<void>(), 0, XtR.bytes()));
-        for (auto& P : b->parts) g.residual(*P, V.as<double>(), n_v, XtR.as<double>(), nullptr, R, false);
-        PG_CUDA(cudaStreamSynchronize(g.stream));
-        g.m->check_mirrors();
-        std::vector<double> h((size_t)F * n_v);
-        PG_CUDA(cudaMemcpy(h.data(), XtR.as<double>(), h.size() * 8, cudaMemcpyDeviceToHost));
-        for (size_t q = 0; q < h.size(); ++q) out[q] = -h[q];
     });
 }
 

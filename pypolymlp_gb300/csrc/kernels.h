@@ -99,10 +99,11 @@ void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off
                     const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,
                     long long ld, cudaStream_t st);
 
-// Tensor-core Gram (gram_tc.cu): scratch (BF16 halves of X, work units,
+// Tensor-core Gram (gram_tc.cu): scratch (the four BF16 fixed-point slices
+// of X and their exponents per segment and column, work units, float-float
 // partial tiles of the row splits, error flag) and entry points.
 struct GramTcScratch {
-    DevBuf H, L, units, P, err;
+    DevBuf H, E, units, P, err;
     int n_units = 0, n_splits = 0, F = 0;
     long long rows = -1;
 };

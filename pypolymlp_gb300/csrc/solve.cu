@@ -3,14 +3,21 @@
 // (Cholesky of X^T X + alpha I, two triangular solves) for each alpha and
 // fills the coefficients with 1e30 when the factorisation fails (:40-44).
 //
-// Blocked right-looking Cholesky A = L L^T (lower, column-major, block 64):
-//   pg_chol_diag    factor the diagonal block in shared memory (one block),
+// All alphas are factored together: the shifted matrices A + alpha_a I sit
+// side by side in HBM and every launch covers all of them (blockIdx.y = the
+// alpha), so the sweep costs the launches of one factorisation and no host
+// round trip per alpha or per step.  Blocked right-looking Cholesky
+// A = L L^T (lower, column-major, block 64):
+//   pg_chol_diag    factor the diagonal block in shared memory,
 //   pg_chol_panel   panel rows below it: L21 = A21 L11^-T (one thread per row),
-//   pg_chol_update  trailing update A22 -= L21 L21^T (64x64 tiles, lower only).
-// Triangular solves L z = b and L^T x = z run in one block each.
-// A non-positive or non-finite pivot sets info = column + 1 and stops.
+//   pg_chol_update  trailing update A22 -= L21 L21^T (64 x 64 lower tiles,
+//                   the tile of a block decoded from its index).
+// The triangular solves L z = b and L^T x = z run in one block per alpha.
+// A non-positive or non-finite pivot sets info = column + 1 and stops that
+// alpha's factorisation; its solution is filled with 1e30.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -23,21 +30,27 @@ namespace pg {
 
 constexpr int kCB = 64;
 
-__global__ void pg_add_diag(double* A, const double* A0, int F, double alpha) {
-    const size_t n = (size_t)F * F;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = q % F, j = q / F;
-        A[q] = A0[q] + (i == j ? alpha : 0.0);
+// A[m] = A0 + alphas[m] I for the n matrices (F x F each, column-major).
+__global__ void pg_add_diag(double* A, const double* A0, int F, const double* alphas, int n) {
+    const size_t ff = (size_t)F * F;
+    const size_t tot = ff * n;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t m = q / ff, r = q % ff;
+        const size_t i = r % F, j = r / F;
+        A[q] = A0[r] + (i == j ? alphas[m] : 0.0);
     }
 }
 
-// Factor A[k:k+b, k:k+b] in place (lower).  info[0] != 0 stops all later work.
+// Factor A_m[k:k+b, k:k+b] in place (lower), m = blockIdx.x.  info[m] != 0
+// stops all later work on that matrix.
 __global__ void pg_chol_diag(double* A, int F, int k, int* info) {
     __shared__ double S[kCB][kCB + 1];
     __shared__ int bad;
+    const int mi = blockIdx.x;
+    A += (size_t)mi * F * F;
     const int b = min(kCB, F - k);
     if (threadIdx.x == 0) bad = 0;
-    if (*info != 0) return;
+    if (info[mi] != 0) return;
     for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
         const int i = q % b, j = q / b;
         S[i][j] = A[(size_t)(k + j) * F + k + i];
@@ -64,7 +77,7 @@ __global__ void pg_chol_diag(double* A, int F, int k, int* info) {
         __syncthreads();
     }
     if (bad) {
-        if (threadIdx.x == 0) *info = bad;
+        if (threadIdx.x == 0) info[mi] = bad;
         return;
     }
     for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
@@ -73,10 +86,12 @@ __global__ void pg_chol_diag(double* A, int F, int k, int* info) {
     }
 }
 
-// Rows i >= k+b: solve x L11^T = a (forward substitution along the row).
+// Rows i >= k+b of matrix blockIdx.y: solve x L11^T = a (forward substitution along the row).
 __global__ void pg_chol_panel(double* A, int F, int k, const int* info) {
     __shared__ double L[kCB][kCB + 1];
-    if (*info != 0) return;
+    const int mi = blockIdx.y;
+    if (info[mi] != 0) return;
+    A += (size_t)mi * F * F;
     const int b = min(kCB, F - k);
     for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
         const int i = q % b, j = q / b;
@@ -94,15 +109,27 @@ __global__ void pg_chol_panel(double* A, int F, int k, const int* info) {
     for (int j = 0; j < b; ++j) A[(size_t)(k + j) * F + row] = x[j];
 }
 
-// A22 -= L21 L21^T over the lower triangle; tiles listed by (ti, tj), ti >= tj.
-__global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, const int2* tiles, const int* info) {
+// Lower tile (ti, tj), ti >= tj, of lower-triangle index t (row-major order).
+__device__ __forceinline__ void lower_tile(int t, int& ti, int& tj) {
+    int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    ti = i;
+    tj = t - i * (i + 1) / 2;
+}
+
+// A22 -= L21 L21^T over the lower triangle of matrix blockIdx.y; block x = tile index.
+__global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, const int* info) {
     __shared__ double Pi[kCB][kCB + 1];
     __shared__ double Pj[kCB][kCB + 1];
-    if (*info != 0) return;
+    const int mi = blockIdx.y;
+    if (info[mi] != 0) return;
+    A += (size_t)mi * F * F;
     const int b = min(kCB, F - k);
     const int s0 = k + b;
-    const int2 t = tiles[blockIdx.x];
-    const int i0 = s0 + t.x * kCB, j0 = s0 + t.y * kCB;
+    int ti, tj;
+    lower_tile(blockIdx.x, ti, tj);
+    const int i0 = s0 + ti * kCB, j0 = s0 + tj * kCB;
     for (int q = threadIdx.x; q < kCB * kCB; q += 256) {
         const int r = q % kCB, p = q / kCB;
         Pi[r][p] = (i0 + r < F && p < b) ? A[(size_t)(k + p) * F + i0 + r] : 0.0;
@@ -132,11 +159,17 @@ __global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, c
         }
 }
 
-// L z = b, then L^T x = z; one block of 1024 threads.
-__global__ void pg_chol_solve(const double* L, int F, const double* b, double* x, const int* info) {
+// L z = b, then L^T x = z for matrix m = blockIdx.x with right-hand side
+// b + m b_stride (b_stride 0: one right-hand side for every matrix); 1024 threads.
+__global__ void pg_chol_solve(const double* L, int F, const double* b, long long b_stride, double* x,
+                              const int* info) {
     extern __shared__ double v[];  // F entries
     __shared__ double red[32];
-    if (*info != 0) {
+    const int mi = blockIdx.x;
+    L += (size_t)mi * F * F;
+    b += (size_t)mi * b_stride;
+    x += (size_t)mi * F;
+    if (info[mi] != 0) {
         for (int i = threadIdx.x; i < F; i += blockDim.x) x[i] = 1e30;
         return;
     }
@@ -166,28 +199,62 @@ __global__ void pg_chol_solve(const double* L, int F, const double* b, double* x
     for (int i = threadIdx.x; i < F; i += blockDim.x) x[i] = v[i];
 }
 
-// Factor A (F x F, column-major, lower used) in place; returns info.
-int cholesky_device(double* A, int F, int* d_info, cudaStream_t st) {
-    std::vector<int2> tiles;
-    DevBuf d_tiles;
+// Factor the n matrices A (F x F each, column-major, lower used) in place;
+// d_info (n ints, zeroed by the caller) receives each status.  No host
+// synchronisation: the launches are queued on st.
+void cholesky_device(double* A, int F, int n, int* d_info, cudaStream_t st) {
     for (int k = 0; k < F; k += kCB) {
-        pg_chol_diag<<<1, 256, 0, st>>>(A, F, k, d_info);
+        pg_chol_diag<<<n, 256, 0, st>>>(A, F, k, d_info);
         const int b = std::min(kCB, F - k);
         const int rest = F - k - b;
         if (rest <= 0) break;
-        pg_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, F, k, d_info);
+        pg_chol_panel<<<dim3((unsigned)((rest + 127) / 128), (unsigned)n), 128, 0, st>>>(A, F, k, d_info);
         const int nt = (rest + kCB - 1) / kCB;
-        tiles.clear();
-        for (int i = 0; i < nt; ++i)
-            for (int j = 0; j <= i; ++j) tiles.push_back(make_int2(i, j));
-        upload(d_tiles, tiles);
-        pg_chol_update<<<(int)tiles.size(), 256, 0, st>>>(A, F, k, d_tiles.as<int2>(), d_info);
+        pg_chol_update<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)n), 256, 0, st>>>(A, F, k, d_info);
     }
     PG_CUDA(cudaGetLastError());
-    int info = 0;
-    PG_CUDA(cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    return info;
+}
+
+void chol_solve_device(const double* L, int F, int n, const double* b, long long b_stride, double* x,
+                       const int* d_info, cudaStream_t st) {
+    const size_t smem = (size_t)F * sizeof(double);
+    PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pg_chol_solve<<<n, 1024, smem, st>>>(L, F, b, b_stride, x, d_info);
+    PG_CUDA(cudaGetLastError());
+}
+
+constexpr size_t kSolveMaxSmem = 200 * 1024;  // the triangular solves keep one F-vector in shared memory
+
+// (A + alpha_a I) x_a = rhs_a for every alpha: rhs is F x n_alpha with
+// rhs_stride F (one right-hand side per alpha) or 0 (the same for all).
+void ridge_batched(int F, const double* xtx, const double* rhs, long long rhs_stride, const double* alphas,
+                   int n_alpha, double* coefs, int* info) {
+    if (F <= 0 || !xtx || !rhs || !alphas || !coefs || !info || n_alpha < 0) throw std::runtime_error("bad arguments");
+    if ((size_t)F * sizeof(double) > kSolveMaxSmem) throw std::runtime_error("n_features too large for the solver");
+    if (n_alpha == 0) return;
+    cudaStream_t st = 0;
+    const size_t ff = (size_t)F * F * sizeof(double);
+    // as many alphas per group as half the free memory holds
+    size_t free_b = 0, total_b = 0;
+    PG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const int group = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_alpha, free_b / 2 / ff));
+    DevBuf A0(ff), A(ff * group), b((size_t)F * n_alpha * 8), x((size_t)F * group * 8), al(n_alpha * 8),
+        d_info(sizeof(int) * group);
+    PG_CUDA(cudaMemcpyAsync(A0.as<void>(), xtx, ff, cudaMemcpyHostToDevice, st));
+    const size_t nb = rhs_stride ? (size_t)F * n_alpha : (size_t)F;
+    PG_CUDA(cudaMemcpyAsync(b.as<void>(), rhs, nb * 8, cudaMemcpyHostToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(al.as<void>(), alphas, (size_t)n_alpha * 8, cudaMemcpyHostToDevice, st));
+    for (int a0 = 0; a0 < n_alpha; a0 += group) {
+        const int n = std::min(group, n_alpha - a0);
+        pg_add_diag<<<2048, 256, 0, st>>>(A.as<double>(), A0.as<double>(), F, al.as<double>() + a0, n);
+        PG_CUDA(cudaMemsetAsync(d_info.as<void>(), 0, sizeof(int) * n, st));
+        cholesky_device(A.as<double>(), F, n, d_info.as<int>(), st);
+        chol_solve_device(A.as<double>(), F, n, b.as<double>() + (rhs_stride ? (size_t)a0 * F : 0),
+                          rhs_stride ? F : 0, x.as<double>(), d_info.as<int>(), st);
+        PG_CUDA(cudaMemcpyAsync(coefs + (size_t)a0 * F, x.as<double>(), (size_t)F * n * 8, cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaMemcpyAsync(info + a0, d_info.as<int>(), sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+        PG_CUDA(cudaStreamSynchronize(st));
+    }
 }
 
 }  // namespace pg
@@ -196,71 +263,12 @@ using namespace pg;
 
 extern "C" int pg_solve_ridge(int F, const double* xtx, const double* xty, const double* alphas, int n_alpha,
                               double* coefs, int* info) {
-    return guarded([&] {
-        if (F <= 0 || !xtx || !xty || !alphas || !coefs || !info) throw std::runtime_error("bad arguments");
-        if ((size_t)F * sizeof(double) > 200 * 1024) throw std::runtime_error("n_features too large for the solver");
-        cudaStream_t st = 0;
-        DevBuf A0((size_t)F * F * 8), A((size_t)F * F * 8), b(F * 8), x(F * 8), d_info(sizeof(int));
-        PG_CUDA(cudaMemcpy(A0.as<void>(), xtx, (size_t)F * F * 8, cudaMemcpyHostToDevice));
-        PG_CUDA(cudaMemcpy(b.as<void>(), xty, (size_t)F * 8, cudaMemcpyHostToDevice));
-        const size_t smem = (size_t)F * sizeof(double);
-        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        for (int a = 0; a < n_alpha; ++a) {
-            pg_add_diag<<<1024, 256, 0, st>>>(A.as<double>(), A0.as<double>(), F, alphas[a]);
-            PG_CUDA(cudaMemsetAsync(d_info.as<void>(), 0, sizeof(int), st));
-            info[a] = cholesky_device(A.as<double>(), F, d_info.as<int>(), st);
-            pg_chol_solve<<<1, 1024, smem, st>>>(A.as<double>(), F, b.as<double>(), x.as<double>(), d_info.as<int>());
-            PG_CUDA(cudaGetLastError());
-            PG_CUDA(cudaMemcpy(coefs + (size_t)a * F, x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
-        }
-    });
+    return guarded([&] { ridge_batched(F, xtx, xty, 0, alphas, n_alpha, coefs, info); });
 }
 
-// ---------------------------------------------------------------------------
-// Factor once, solve many: the Cholesky factor of xtx + alpha I kept on the
-// device, for preconditioned iterations that apply its inverse repeatedly.
-struct pg_ridge_factor {
-    int F = 0;
-    DevBuf L, b, x, info;
-};
-
-extern "C" int pg_ridge_factor_create(int F, const double* xtx, double alpha, pg_ridge_factor** out, int* info) {
-    return guarded([&] {
-        if (F <= 0 || !xtx || !out || !info) throw std::runtime_error("bad arguments");
-        if ((size_t)F * sizeof(double) > 200 * 1024) throw std::runtime_error("n_features too large for the solver");
-        auto f = std::make_unique<pg_ridge_factor>();
-        f->F = F;
-        DevBuf A0((size_t)F * F * 8);
-        f->L.alloc((size_t)F * F * 8);
-        f->b.alloc((size_t)F * 8);
-        f->x.alloc((size_t)F * 8);
-        f->info.alloc(sizeof(int));
-        PG_CUDA(cudaMemcpy(A0.as<void>(), xtx, (size_t)F * F * 8, cudaMemcpyHostToDevice));
-        pg_add_diag<<<1024, 256, 0, 0>>>(f->L.as<double>(), A0.as<double>(), F, alpha);
-        PG_CUDA(cudaMemset(f->info.as<void>(), 0, sizeof(int)));
-        *info = cholesky_device(f->L.as<double>(), F, f->info.as<int>(), 0);
-        *out = f.release();
-    });
-}
-
-extern "C" int pg_ridge_factor_solve(pg_ridge_factor* f, const double* rhs, int n_rhs, double* x) {
-    return guarded([&] {
-        if (!f || !rhs || !x || n_rhs < 0) throw std::runtime_error("bad arguments");
-        const int F = f->F;
-        const size_t smem = (size_t)F * sizeof(double);
-        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        for (int q = 0; q < n_rhs; ++q) {
-            PG_CUDA(cudaMemcpy(f->b.as<void>(), rhs + (size_t)q * F, (size_t)F * 8, cudaMemcpyHostToDevice));
-            pg_chol_solve<<<1, 1024, smem, 0>>>(f->L.as<double>(), F, f->b.as<double>(), f->x.as<double>(),
-                                               f->info.as<int>());
-            PG_CUDA(cudaGetLastError());
-            PG_CUDA(cudaMemcpy(x + (size_t)q * F, f->x.as<double>(), (size_t)F * 8, cudaMemcpyDeviceToHost));
-        }
-    });
-}
-
-extern "C" int pg_ridge_factor_destroy(pg_ridge_factor* f) {
-    return guarded([&] { delete f; });
+extern "C" int pg_solve_ridge_rhs(int F, const double* xtx, const double* rhs, const double* alphas, int n_alpha,
+                                  double* coefs, int* info) {
+    return guarded([&] { ridge_batched(F, xtx, rhs, F, alphas, n_alpha, coefs, info); });
 }
 
 // ---------------------------------------------------------------------------
@@ -268,22 +276,20 @@ extern "C" int pg_ridge_factor_destroy(pg_ridge_factor* f) {
 //
 // Some callers cannot allocate device memory when they solve: code that runs
 // inside an inference server or a host framework whose allocator owns every
-// byte of the GPU, code that runs while a CUDA stream is being captured (where
-// cudaMalloc is not allowed), or a real-time loop that must not touch the
-// allocator.  They hand over device buffers they already own.  This variant of
-// the blocked Cholesky solve keeps its workspace (the factor of
-// xtx + alpha I, the list of update tiles and the status word) in one
-// file-scope device array instead of cudaMalloc'ed buffers.
+// byte of the GPU (a cudaMalloc of ours would fail or would fragment its
+// pool), or a real-time loop that must never enter the allocator.  They hand
+// over device buffers they already own.  This variant of the blocked
+// Cholesky solve keeps its workspace (the factor of xtx + alpha I and the
+// status word) in one file-scope device array instead of cudaMalloc'ed
+// buffers.
 //
 // Limits and sharing: n_features <= kNoAllocMaxF (1024); every GPU that loads
-// this library holds the array (8 MiB + a few KiB) until the process exits.
+// this library holds the array (8 MiB + 256 bytes) until the process exits.
 // All calls on a device share the one array and it keeps the last call's
 // contents (the status word is cleared at the start of each call), so calls
 // whose GPU work overlaps - from several host threads or streams - race on it.
 constexpr int kNoAllocMaxF = 1024;
-constexpr int kNoAllocMaxTiles = (kNoAllocMaxF / kCB) * (kNoAllocMaxF / kCB + 1) / 2;
-constexpr size_t kNoAllocBytes = (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double) +
-                                 (size_t)kNoAllocMaxTiles * sizeof(int2) + 256;
+constexpr size_t kNoAllocBytes = (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double) + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -309,6 +315,15 @@ static unsigned char* noalloc_scratch() {
     return static_cast<unsigned char*>(g_noalloc_ptr[dev]);
 }
 
+// A = A0 + alpha I (one matrix, alpha by value).
+__global__ void pg_add_diag1(double* A, const double* A0, int F, double alpha) {
+    const size_t n = (size_t)F * F;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = q % F, j = q / F;
+        A[q] = A0[q] + (i == j ? alpha : 0.0);
+    }
+}
+
 extern "C" int pg_solve_ridge_noalloc(int F, const double* d_xtx, const double* d_xty, double alpha,
                                       double* d_coefs, int* info) {
     return guarded([&] {
@@ -321,31 +336,11 @@ extern "C" int pg_solve_ridge_noalloc(int F, const double* d_xtx, const double* 
         cudaStream_t st = 0;
         unsigned char* base = noalloc_scratch();
         double* A = reinterpret_cast<double*>(base);
-        int2* tiles = reinterpret_cast<int2*>(base + (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double));
-        int* d_info = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(tiles) +
-                                             (size_t)kNoAllocMaxTiles * sizeof(int2));
+        int* d_info = reinterpret_cast<int*>(base + (size_t)kNoAllocMaxF * kNoAllocMaxF * sizeof(double));
         PG_CUDA(cudaMemsetAsync(d_info, 0, sizeof(int), st));
-        pg_add_diag<<<1024, 256, 0, st>>>(A, d_xtx, F, alpha);
-        std::vector<int2> tl;
-        for (int k = 0; k < F; k += kCB) {
-            pg_chol_diag<<<1, 256, 0, st>>>(A, F, k, d_info);
-            const int b = std::min(kCB, F - k);
-            const int rest = F - k - b;
-            if (rest <= 0) break;
-            pg_chol_panel<<<(rest + 127) / 128, 128, 0, st>>>(A, F, k, d_info);
-            const int nt = (rest + kCB - 1) / kCB;
-            tl.clear();
-            for (int i = 0; i < nt; ++i)
-                for (int j = 0; j <= i; ++j) tl.push_back(make_int2(i, j));
-            // the tile list of this step is consumed by the next kernel on the same stream
-            PG_CUDA(cudaMemcpyAsync(tiles, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-            pg_chol_update<<<(int)tl.size(), 256, 0, st>>>(A, F, k, tiles, d_info);
-            PG_CUDA(cudaStreamSynchronize(st));  // the host tile list is reused next step
-        }
-        const size_t smem = (size_t)F * sizeof(double);
-        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        pg_chol_solve<<<1, 1024, smem, st>>>(A, F, d_xty, d_coefs, d_info);
-        PG_CUDA(cudaGetLastError());
+        pg_add_diag1<<<1024, 256, 0, st>>>(A, d_xtx, F, alpha);
+        cholesky_device(A, F, 1, d_info, st);
+        chol_solve_device(A, F, 1, d_xty, 0, d_coefs, d_info, st);
         PG_CUDA(cudaMemcpyAsync(info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st));
         PG_CUDA(cudaStreamSynchronize(st));
     });

@@ -16,9 +16,9 @@ absent (pypolymlp.py:264-271) and subtracting the atomic energies
 `fit_learning_curve`) and `accuracy.PolymlpEvalAccuracy`; `save_mlp`,
 `load_mlp`, `save_params` and `save_errors` write the reference's files.
 
-`precision` selects the Gram: PG_FP64 (default; the reference's arithmetic) or
-PG_MIXED (BF16x3 tensor-core Gram preconditioning an FP64 conjugate-gradient
-solve, with the FP64 Gram as fallback where that solve does not converge).
+`precision` selects the rows and the Gram: PG_FP64 (default; the reference's
+arithmetic) or PG_MIXED (FP32 rows, and their Gram on the tensor cores from
+fixed-point BF16 slices, accurate to ~1e-12, solved directly in FP64).
 `set_datasets_vasp` and `set_multiple_datasets_vasp` read vasprun.xml files
 (`io_vasp`); the reference's electron, SSCHA, phono3py and property-yaml
 dataset readers are not part of this module.
@@ -58,6 +58,8 @@ class Pypolymlp:
         self._coeffs = self._scales = None
         self._error_train = self._error_test = None
         self._learning_log = None
+        self._hybrid: list = []
+        self._cumulative = None
 
     # -- parameters -----------------------------------------------------------------
     def set_params(self, params: Optional[dict] = None, elements: Optional[Sequence[str]] = None,
@@ -70,6 +72,8 @@ class Pypolymlp:
                    atomic_energy: Optional[Sequence[float]] = None, enable_spins: Optional[Sequence[bool]] = None):
         alphas = [10.0 ** a for a in np.linspace(reg_alpha_params[0], reg_alpha_params[1],
                                                  round(reg_alpha_params[2]))]
+        # a new first model drops the models appended to the previous one
+        self._hybrid, self._cumulative = [], None
         if params is not None:
             self._params = params
             self._alphas = params.get("alphas") or alphas
@@ -100,18 +104,23 @@ class Pypolymlp:
         the settings of `set_params`; the datasets and alphas stay those of the first model."""
         if self._params is None:
             raise RuntimeError("Set the first model's parameters before appending hybrid ones.")
-        first = (self._params, self._alphas, self._atomic_energy)
+        first = (self._params, self._alphas, self._atomic_energy, self._hybrid)
         self.set_params(**kwargs)
         extra = self._params
-        self._params, self._alphas, self._atomic_energy = first
+        self._params, self._alphas, self._atomic_energy, self._hybrid = first
         if list(extra["elements"]) != list(self._params["elements"]):
             raise ValueError("hybrid models here share the first model's elements")
-        self._hybrid = getattr(self, "_hybrid", []) + [extra]
+        self._hybrid = list(self._hybrid) + [extra]
         return self
 
     @property
     def _models(self) -> list:
-        return [self._params] + list(getattr(self, "_hybrid", []))
+        return [self._params] + list(self._hybrid)
+
+    def _single_model_only(self, what: str):
+        if self._hybrid:
+            raise RuntimeError(f"{what} fits one model; this Pypolymlp holds a hybrid of {len(self._models)} "
+                               "models (use fit or run without use_cg)")
 
     @staticmethod
     def _expand_atomic_energy(params: dict, per_element: list) -> np.ndarray:
@@ -282,10 +291,9 @@ class Pypolymlp:
             from pypolymlp_gb300.hybrid import fit_hybrid
 
             res, self._cumulative = fit_hybrid(self._models, self._train, self._test, self._alphas,
-                                               precision=_ffi.PG_FP64)
+                                               precision=self._precision)
             return self._set_result(res)
-        res = regression.fit(self._params, self._train, self._test, self._alphas, precision=self._precision,
-                             fp64_fallback=self._precision == _ffi.PG_MIXED)
+        res = regression.fit(self._params, self._train, self._test, self._alphas, precision=self._precision)
         return self._set_result(res)
 
     def fit_standard(self, verbose: Optional[bool] = None):
@@ -295,6 +303,7 @@ class Pypolymlp:
         from pypolymlp_gb300 import regression
 
         self._ready()
+        self._single_model_only("fit_cg")
         res = regression.fit_cg(self._params, self._train, self._test, self._alphas, gtol=gtol, max_iter=max_iter,
                                 precision=self._precision)
         return self._set_result(res)
@@ -352,6 +361,7 @@ class Pypolymlp:
         from pypolymlp_gb300 import regression
 
         self._ready()
+        self._single_model_only("fit_learning_curve")
         self._learning_log = regression.fit_learning_curve(self._params, self._train, self._test, self._alphas,
                                                            precision=self._precision)
         return self
@@ -385,6 +395,7 @@ class Pypolymlp:
         from pypolymlp_gb300.io_polymlp import load_mlp
 
         self._params, coeffs = load_mlp(filename)
+        self._hybrid, self._cumulative = [], None
         self._coeffs, self._scales = np.asarray(coeffs, dtype=np.float64), np.ones(len(coeffs))
         return self
 

@@ -267,117 +267,26 @@ def calc_xtx_xty(model: _ffi.Model, datasets: Sequence[Dataset], precision: int 
 
 
 def solver_ridge(xtx: np.ndarray, xty: np.ndarray, alphas: Sequence[float]) -> np.ndarray:
-    """Coefficients (F x n_alpha); a failed factorisation gives a column of 1e30."""
+    """Coefficients (F x n_alpha) of (xtx + alpha I) c = xty for every alpha,
+    all alphas factored together on the device; a failed factorisation gives
+    a column of 1e30.  xty may also be F x n_alpha: one right-hand side per
+    alpha (the corrections of iterative refinement)."""
     F = xtx.shape[0]
     a = np.ascontiguousarray(np.asarray(alphas, dtype=np.float64))
     A = np.asfortranarray(xtx, dtype=np.float64)
-    b = np.ascontiguousarray(xty, dtype=np.float64)
+    b = np.asfortranarray(xty, dtype=np.float64)
     coefs = np.zeros((F, len(a)), order="F")
     info = np.zeros(len(a), dtype=np.int32)
     p = _ffi._p
-    _ffi.check(_ffi.lib().pg_solve_ridge(F, p(A, C.c_double), p(b, C.c_double), p(a, C.c_double), len(a),
-                                         p(coefs, C.c_double), p(info, C.c_int)))
+    if b.ndim == 1:
+        _ffi.check(_ffi.lib().pg_solve_ridge(F, p(A, C.c_double), p(b, C.c_double), p(a, C.c_double), len(a),
+                                             p(coefs, C.c_double), p(info, C.c_int)))
+    else:
+        if b.shape != (F, len(a)):
+            raise ValueError("xty must be F or F x n_alpha")
+        _ffi.check(_ffi.lib().pg_solve_ridge_rhs(F, p(A, C.c_double), p(b, C.c_double), p(a, C.c_double), len(a),
+                                                 p(coefs, C.c_double), p(info, C.c_int)))
     return np.asarray(coefs), info
-
-
-class RidgeFactor:
-    """Device Cholesky factor of xtx + alpha I, applied repeatedly (pg_ridge_factor_*)."""
-
-    def __init__(self, xtx: np.ndarray, alpha: float):
-        self.F = xtx.shape[0]
-        A = np.asfortranarray(xtx, dtype=np.float64)
-        h = _ffi._vp()
-        info = C.c_int()
-        _ffi.check(_ffi.lib().pg_ridge_factor_create(self.F, _ffi._p(A, C.c_double), float(alpha), C.byref(h),
-                                                     C.byref(info)))
-        self._h = h
-        self.info = info.value
-
-    def solve(self, rhs: np.ndarray) -> np.ndarray:
-        b = np.asfortranarray(np.atleast_2d(np.asarray(rhs, dtype=np.float64).T).T)
-        x = np.zeros_like(b, order="F")
-        _ffi.check(_ffi.lib().pg_ridge_factor_solve(self._h, _ffi._p(b, C.c_double), b.shape[1],
-                                                    _ffi._p(x, C.c_double)))
-        return x.reshape(np.shape(rhs))
-
-    def __del__(self):
-        h = getattr(self, "_h", None)
-        if h is not None and h.value and _ffi._lib is not None:
-            _ffi._lib.pg_ridge_factor_destroy(h)
-            self._h = None
-
-
-def normal_matvec(gram: "GramAccumulator", batches: Sequence["DeviceBatch"], v: np.ndarray) -> np.ndarray:
-    """X^T X v (FP64 sums over rows regenerated on the device), v F x k, k <= 16."""
-    v = np.asfortranarray(np.atleast_2d(np.asarray(v, dtype=np.float64).T).T)
-    out = np.zeros_like(v, order="F")
-    for b in batches:
-        o = np.zeros_like(v, order="F")
-        _ffi.check(_ffi.lib().pg_batch_normal_matvec(gram._h, b.handle, _ffi._p(v, C.c_double), v.shape[1],
-                                                     _ffi._p(o, C.c_double)))
-        out += o
-    return out
-
-
-def ridge_pcg(xtx_mixed: np.ndarray, xty: np.ndarray, alphas: np.ndarray, matvec, zero_ids,
-              max_iter: int = 60, rtol: float = 1e-10, factor=None, return_residuals: bool = False):
-    """Solve (A + alpha I) c = b for every alpha by conjugate gradients whose
-    products A p come from `matvec` (exact FP64 sums over the rows) and whose
-    preconditioner is the device Cholesky factor of the mixed-precision
-    matrix, shifted by the smallest tau (0, then 1e-9 ... 1e-2 of its mean
-    diagonal) that makes it positive definite.  The mixed Gram's rounding is
-    larger than small alphas, so it cannot be solved directly; this keeps it
-    only as the preconditioner.  `factor(matrix, shift)` builds the
-    preconditioner (default: `RidgeFactor`, on the device).  Returns (coefs
-    F x n_alpha, iterations, shift per alpha), and the final relative residual
-    norm per alpha with return_residuals."""
-    factor = RidgeFactor if factor is None else factor
-    F = xtx_mixed.shape[0]
-    na = len(alphas)
-    dmean = float(np.mean(np.diag(xtx_mixed)))
-    facs, taus = [], []
-    for a in alphas:
-        for t in [0.0] + [dmean * 10.0 ** e for e in range(-9, -1)]:
-            f = factor(xtx_mixed, a + t)
-            if f.info == 0:
-                break
-        facs.append(f)
-        taus.append(t)
-    mask = np.ones(F)
-    mask[zero_ids] = 0.0
-    b = (xty * mask)[:, None] * np.ones((1, na))
-
-    def apply_a(p):
-        return (matvec(p * mask[:, None]) + p * alphas[None, :]) * mask[:, None]
-
-    def precond(r):
-        return np.stack([facs[k].solve(r[:, k]) for k in range(na)], axis=1) * mask[:, None]
-
-    x = precond(b)
-    r = b - apply_a(x)
-    z = precond(r)
-    p = z.copy()
-    rz = np.einsum("ij,ij->j", r, z)
-    bn = np.linalg.norm(b, axis=0)
-    it = 0
-    active = np.ones(na, dtype=bool)
-    for it in range(1, max_iter + 1):
-        q = apply_a(p)
-        pq = np.einsum("ij,ij->j", p, q)
-        step = np.where(active & (pq > 0), rz / np.where(pq > 0, pq, 1.0), 0.0)
-        x += p * step[None, :]
-        r -= q * step[None, :]
-        active &= np.linalg.norm(r, axis=0) > rtol * bn
-        if not active.any():
-            break
-        z = precond(r)
-        rz_new = np.einsum("ij,ij->j", r, z)
-        beta = np.where(active, rz_new / np.where(rz != 0, rz, 1.0), 0.0)
-        p = z + p * beta[None, :]
-        rz = rz_new
-    if return_residuals:
-        return x, it, np.array(taus), np.linalg.norm(r, axis=0) / np.where(bn > 0, bn, 1.0)
-    return x, it, np.array(taus)
 
 
 def compute_rmse_seq(coefs_array, data_xy: DataXY, check_singular=False, error_threshold=1e6):
@@ -425,9 +334,8 @@ class FitResult:
     rmse_train_array: np.ndarray = field(repr=False, default=None)
     rmse_test_array: np.ndarray = field(repr=False, default=None)
     info: np.ndarray = field(repr=False, default=None)
-    cg_iterations: int = 0                 # conjugate-gradient iterations (mixed path)
-    shifts: np.ndarray = field(repr=False, default=None)  # preconditioner shift per alpha
-    fp64_fallback: bool = False            # mixed path: CG did not converge, FP64 Gram solved directly
+    cg_iterations: int = 0                 # conjugate-gradient iterations (fit_cg)
+    refine_sweeps: int = 0                 # iterative-refinement sweeps (fit)
 
     @property
     def scaled_coeffs(self):
@@ -438,7 +346,7 @@ class FitResult:
 def _assemble(model: _ffi.Model, train: Sequence[Dataset], precision: int, weight_stress: float,
               scales=None, min_energy=None, zero_ids=None):
     """Training batches on the device, their Gram (one pass) and the scaled
-    normal equations: (batches, gram, xtx, xty, scales, zero_ids, min_energy)."""
+    normal equations: (batches, gram, DataXY)."""
     min_e = get_min_energy(train) if min_energy is None else min_energy
     tb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in train]
     gram = GramAccumulator(model, precision)
@@ -454,23 +362,20 @@ def _assemble(model: _ffi.Model, train: Sequence[Dataset], precision: int, weigh
     xtx /= scales[:, None]
     xtx /= scales[None, :]
     xty /= scales
-    return tb, gram, xtx, xty, scales, zero_ids, min_e
+    return tb, gram, DataXY(xtx, xty, yty, int(n_rows), scales, zero_ids, min_e, xe_sum, xe_sq)
 
 
-def _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info, n_iter, shifts):
-    """Residual RMSEs on the training and test batches and the best alpha (FitResult)."""
-    _, sq, n_tr = batch_residual(gram, tb, coefs / scales[:, None])
-    rmse_train = np.sqrt(sq.sum(axis=0) / n_tr)
-    if np.all(rmse_train > 1e6):
-        raise RuntimeError("Matrix (X.T @ X + alpha * I) may be singular. "
-                           "This singularity issue might be reduced by increasing "
-                           "the value of alpha (the magnitude of the penalty term).")
-    vb = [DeviceBatch(model, d, min_e, precision, weight_stress) for d in test]
-    _, sq, n_te = batch_residual(gram, vb, coefs / scales[:, None])
+def _select(model, gram, xy: DataXY, test, coefs, alphas, precision, weight_stress, info, n_iter=0, sweeps=0):
+    """Training RMSEs from the Gram (compute_rmse_seq, with the reference's
+    singularity check), test RMSEs from residuals over the test rows, and the
+    alpha of the smallest test RMSE (get_best_model): a FitResult."""
+    rmse_train = compute_rmse_seq(coefs, xy, check_singular=True)
+    vb = [DeviceBatch(model, d, xy.min_energy, precision, weight_stress) for d in test]
+    _, sq, n_te = batch_residual(gram, vb, coefs / xy.scales[:, None])
     rmse_test = np.sqrt(sq.sum(axis=0) / n_te)
     idx = int(np.argmin(rmse_test))
-    return FitResult(coefs[:, idx], scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
-                     coefs, rmse_train, rmse_test, info, n_iter, shifts)
+    return FitResult(coefs[:, idx], xy.scales, float(alphas[idx]), float(rmse_train[idx]), float(rmse_test[idx]),
+                     coefs, rmse_train, rmse_test, info, n_iter, sweeps)
 
 
 def solver_cg(xtx: np.ndarray, xty: np.ndarray, alpha: float = 1e-3, coef0: Optional[np.ndarray] = None,
@@ -508,16 +413,16 @@ def fit_cg(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset],
     selection as `fit`."""
     model = model or _ffi.Model(params_dict)
     alphas = np.asarray(alphas, dtype=np.float64)
-    tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
+    tb, gram, xy = _assemble(model, train, precision, weight_stress)
     if max_iter is None:
         max_iter = max(model.n_features * 3, 50000)
-    coefs, c0, n_iter = np.zeros((len(xty), len(alphas))), None, 0
+    coefs, c0, n_iter = np.zeros((len(xy.xty), len(alphas))), None, 0
     for k in reversed(range(len(alphas))):
-        c0, it = solver_cg(xtx, xty, float(alphas[k]), c0, gtol, max_iter)
+        c0, it = solver_cg(xy.xtx, xy.xty, float(alphas[k]), c0, gtol, max_iter)
         coefs[:, k] = c0
         n_iter += it
-    return _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress,
-                   np.zeros(len(alphas), dtype=np.int32), n_iter, np.zeros(len(alphas)))
+    return _select(model, gram, xy, test, coefs, alphas, precision, weight_stress,
+                   np.zeros(len(alphas), dtype=np.int32), n_iter=n_iter)
 
 
 def fit_learning_curve(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset],
@@ -534,17 +439,17 @@ def fit_learning_curve(params_dict: dict, train: Sequence[Dataset], test: Sequen
         raise RuntimeError("Number of training datasets must be one for learning curve.")
     model = _ffi.Model(params_dict)
     full = train[0]
-    _, _, _, _, scales, zero_ids, min_e = _assemble(model, [full], precision, weight_stress)
+    _, _, full_xy = _assemble(model, [full], precision, weight_stress)
     n_train = len(full)
     step = max(n_train // 10, 1)
     log = []
     for n in range(step, n_train + 1, step):
         sub = full.slice(0, n)
-        tb, gram, xtx, xty, sc, _, _ = _assemble(model, [sub], precision, weight_stress, scales=scales,
-                                                 min_energy=min_e, zero_ids=zero_ids)
-        coefs, info = solver_ridge(xtx, xty, alphas)
-        best = _select(model, gram, tb, test, coefs, sc, np.asarray(alphas, dtype=np.float64), min_e, precision,
-                       weight_stress, info, 0, np.zeros(len(alphas)))
+        tb, gram, xy = _assemble(model, [sub], precision, weight_stress, scales=full_xy.scales,
+                                 min_energy=full_xy.min_energy, zero_ids=full_xy.zero_ids)
+        coefs, info = solver_ridge(xy.xtx, xy.xty, alphas)
+        best = _select(model, gram, xy, test, coefs, np.asarray(alphas, dtype=np.float64), precision,
+                       weight_stress, info)
         acc = PolymlpEvalAccuracy(params_dict, best.scaled_coeffs, precision=precision)
         for d in test:
             log.append([n, acc.compute_error_single(d, log_energy=False)])
@@ -552,47 +457,27 @@ def fit_learning_curve(params_dict: dict, train: Sequence[Dataset], test: Sequen
 
 
 def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], alphas: Sequence[float],
-        precision: int = _ffi.PG_MIXED, model: Optional[_ffi.Model] = None, refine: Optional[int] = None,
-        weight_stress: float = 0.1, fp64_fallback: bool = False) -> FitResult:
+        precision: int = _ffi.PG_MIXED, model: Optional[_ffi.Model] = None, refine: int = 0,
+        weight_stress: float = 0.1) -> FitResult:
     """GPU counterpart of fit() (src/pypolymlp/mlp_dev/standard/fit.py:12-60).
 
-    The Gram is assembled once (mixed or FP64).  FP64: the ridge systems are
-    solved directly (device Cholesky, as posv).  Mixed: the mixed Gram only
-    preconditions a conjugate-gradient solve whose matrix products are FP64
-    sums over freshly generated rows (`refine` caps the iterations; default
-    60, stopping at a relative residual of 1e-10).  With fp64_fallback, when an
-    alpha's residual is still above 1e-8 after the cap (an ill-conditioned
-    normal matrix, where the mixed Gram needs a large shift to factor and
-    preconditions small alphas weakly), the FP64 Gram is assembled in one more
-    pass and solved directly (FitResult.fp64_fallback); each CG iteration costs
-    a pass over the rows, so this bounds the cost.  RMSEs are computed from
-    residuals (weighted rows, as the reference's Gram-based formula defines
-    them)."""
+    One pass over the training rows assembles the Gram (PG_MIXED: FP32 rows
+    and the tensor-core Gram of those rows, accurate to ~1e-12; PG_FP64: FP64
+    rows and an FP64 Gram), then the ridge systems of all alphas are solved
+    directly on the device (Cholesky, as posv).  `refine` > 0 adds that many
+    iterative-refinement sweeps c += (A + alpha I)^-1 (X^T (y - X c) - alpha c),
+    each with the residual from a fresh pass over the training rows (the rows
+    at the same precision; the direct solve already matches them, so the
+    default is none).  Training RMSEs come from the Gram and test RMSEs from
+    residuals over the test rows; the best alpha has the smallest test RMSE."""
     model = model or _ffi.Model(params_dict)
-    if refine is None:
-        refine = 60 if precision == _ffi.PG_MIXED else 0
     alphas = np.asarray(alphas, dtype=np.float64)
-    tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
-    n_iter, shifts = 0, np.zeros(len(alphas))
-    if precision == _ffi.PG_FP64 and not refine:
-        coefs, info = solver_ridge(xtx, xty, alphas)
-    else:
-        # The mixed Gram preconditions a conjugate-gradient solve whose
-        # products X^T X p are exact FP64 sums over freshly generated rows.
-        def matvec(v):
-            return normal_matvec(gram, tb, v / scales[:, None]) / scales[:, None]
-
-        coefs, n_iter, shifts, resid = ridge_pcg(xtx, xty, alphas, matvec, zero_ids, max_iter=max(1, refine),
-                                                 return_residuals=True)
-        info = np.zeros(len(alphas), dtype=np.int32)
-        if fp64_fallback and precision == _ffi.PG_MIXED and np.any(resid > 1e-8):
-            del tb, gram
-            precision = _ffi.PG_FP64
-            tb, gram, xtx, xty, scales, zero_ids, min_e = _assemble(model, train, precision, weight_stress)
-            coefs, info = solver_ridge(xtx, xty, alphas)
-            res = _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info,
-                          n_iter, shifts)
-            res.fp64_fallback = True
-            return res
-    return _select(model, gram, tb, test, coefs, scales, alphas, min_e, precision, weight_stress, info, n_iter,
-                   shifts)
+    tb, gram, xy = _assemble(model, train, precision, weight_stress)
+    coefs, info = solver_ridge(xy.xtx, xy.xty, alphas)
+    for _ in range(int(refine)):
+        xtr, _, _ = batch_residual(gram, tb, coefs / xy.scales[:, None])
+        r = xtr / xy.scales[:, None] - coefs * alphas[None, :]
+        r[xy.zero_ids] = 0.0
+        dc, info = solver_ridge(xy.xtx, np.asfortranarray(r), alphas)
+        coefs = np.where(info[None, :] == 0, coefs + dc, 1e30)
+    return _select(model, gram, xy, test, coefs, alphas, precision, weight_stress, info, sweeps=int(refine))

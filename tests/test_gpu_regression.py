@@ -1,10 +1,11 @@
 """GPU regression assembly and ridge solve against the CPU pipeline
 (oracle X + numpy X^T X + LAPACK posv).
 
-Tolerances: FP64 Gram 1e-12 relative to max|X^T X|; mixed (BF16x3 products,
-FP32 partial sums flushed to FP64 every 8192 rows) 1e-5 relative; ridge
-coefficients of the FP64 path 1e-8 relative to max|c|; the fitted energy
-RMSE of the mixed path within 0.05 meV/atom of the FP64 oracle fit.
+Tolerances: FP64 Gram 1e-12 relative to max|X^T X|; mixed (FP32 rows, their
+Gram from fixed-point BF16 slices) 1e-4 relative, the FP32 rounding of the
+rows; ridge coefficients 1e-8 relative to max|c| for every alpha (all alphas
+factored together); the fitted energy and force RMSEs of the mixed path
+within 0.05 meV/atom and 1 meV/A of the FP64 fit.
 """
 
 import numpy as np
@@ -49,7 +50,7 @@ def test_gram_fp64_and_mixed_match_cpu():
     assert abs(g64.y_sq_norm - ref.y_sq_norm) <= 1e-12 * ref.y_sq_norm
     assert g64.total_n_data == ref.total_n_data
     g32 = calc_xtx_xty(m, train, precision=_ffi.PG_MIXED, batch_size=7)
-    # dominated by the FP32 rounding of the (cancelling) force-row sums, not by the split
+    # the FP32 rounding of the (cancelling) force-row sums; the Gram of those rows is exact to ~1e-12
     assert np.abs(g32.xtx - ref.xtx).max() / scale < 1e-4
     # symmetric up to the rounding of the two-sided column scaling
     assert np.abs(g64.xtx - g64.xtx.T).max() <= 1e-14 * scale
@@ -59,15 +60,35 @@ def test_ridge_solve_matches_posv():
     from pypolymlp_gb300.regression import solver_ridge
 
     rng = np.random.default_rng(0)
-    for F in (5, 64, 130, 300):
+    for F, n_alpha in ((5, 3), (64, 3), (130, 3), (300, 8), (1100, 8)):
         B = rng.normal(size=(F + 20, F))
         A = B.T @ B
         b = rng.normal(size=F)
-        alphas = [1e-3, 1e-2, 1e-1]
+        alphas = list(10.0 ** np.linspace(-4, 0, n_alpha))
         ref = solver_ridge_cpu(A, b, alphas)
         got, info = solver_ridge(A, b, alphas)
         assert (info == 0).all()
-        assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-8
+        for k in range(n_alpha):
+            assert np.abs(got[:, k] - ref[:, k]).max() / np.abs(ref[:, k]).max() < 1e-8, (F, k)
+
+
+def test_ridge_solve_per_alpha_rhs_and_failures():
+    """One right-hand side per alpha (pg_solve_ridge_rhs), and a failed
+    factorisation of one alpha leaves the others intact."""
+    from pypolymlp_gb300.regression import solver_ridge
+
+    rng = np.random.default_rng(1)
+    F = 200
+    B = rng.normal(size=(F + 5, F))
+    A = B.T @ B - 30.0 * np.eye(F)          # indefinite until alpha exceeds ~30 - lambda_min
+    rhs = np.asfortranarray(rng.normal(size=(F, 3)))
+    alphas = [1e-3, 100.0, 1000.0]
+    got, info = solver_ridge(A, rhs, alphas)
+    assert info[0] != 0 and np.all(got[:, 0] == 1e30)
+    for k in (1, 2):
+        assert info[k] == 0
+        want = np.linalg.solve(A + alphas[k] * np.eye(F), rhs[:, k])
+        assert np.abs(got[:, k] - want).max() <= 1e-9 * np.abs(want).max()
 
 
 def test_ridge_singular_gives_1e30():
@@ -100,10 +121,10 @@ def _energy_force_rmse(params, coefs_unscaled, datasets):
 
 def test_fit_mixed_vs_fp64_rmse():
     """End-to-end fit.  FP64 GPU path: test RMSEs of every alpha equal the CPU
-    pipeline's (Gram formula, LAPACK posv) to 1e-6.  Mixed path (BF16x3 Gram as
-    the preconditioner of a conjugate-gradient solve with FP64 normal-matrix
-    products): the selected model's energy RMSE within 0.05 meV/atom and force
-    RMSE within 1 meV/A of the FP64 fit."""
+    pipeline's (Gram formula, LAPACK posv) to 1e-6.  Mixed path (FP32 rows,
+    tensor-core Gram, direct solve): the selected model's energy RMSE within
+    0.05 meV/atom and force RMSE within 1 meV/A of the FP64 fit, with and
+    without one iterative-refinement sweep."""
     from pypolymlp_gb300 import _ffi
     from pypolymlp_gb300.regression import compute_rmse_seq, fit
 
@@ -116,14 +137,15 @@ def test_fit_mixed_vs_fp64_rmse():
     rmse_ref = compute_rmse_seq(coefs, ref_test)
     r64 = fit(p, train, test, alphas, precision=_ffi.PG_FP64)
     np.testing.assert_allclose(r64.rmse_test_array, rmse_ref, rtol=1e-6)
-    r32 = fit(p, train, test, alphas, precision=_ffi.PG_MIXED)
     e64, f64 = _energy_force_rmse(p, r64.scaled_coeffs, test)
-    e32, f32 = _energy_force_rmse(p, r32.scaled_coeffs, test)
     print(f"fp64: alpha {r64.alpha} rmse_test {r64.rmse_test_array}; E {e64 * 1e3:.4f} meV/atom F {f64 * 1e3:.3f} meV/A")
-    print(f"mixed: alpha {r32.alpha} rmse_test {r32.rmse_test_array}; E {e32 * 1e3:.4f} meV/atom F {f32 * 1e3:.3f} meV/A"
-          f"; cg iterations {r32.cg_iterations}, shifts {r32.shifts}")
-    assert abs(e32 - e64) < 0.05e-3, (e32, e64)
-    assert abs(f32 - f64) < 1e-3, (f32, f64)
+    for refine in (0, 1):
+        r32 = fit(p, train, test, alphas, precision=_ffi.PG_MIXED, refine=refine)
+        e32, f32 = _energy_force_rmse(p, r32.scaled_coeffs, test)
+        print(f"mixed (refine {refine}): alpha {r32.alpha} rmse_test {r32.rmse_test_array}; "
+              f"E {e32 * 1e3:.4f} meV/atom F {f32 * 1e3:.3f} meV/A")
+        assert abs(e32 - e64) < 0.05e-3, (refine, e32, e64)
+        assert abs(f32 - f64) < 1e-3, (refine, f32, f64)
 
 
 def test_fit_cg_matches_direct_solve():

@@ -1,10 +1,9 @@
 """pg_solve_ridge_noalloc: the ridge solve for callers that cannot allocate.
 
 Some callers of this library cannot allocate GPU memory when they need a
-solve - a server or framework whose own allocator owns the device, or code
-running while a CUDA stream is captured.  They own the input and output
-buffers; the entry point keeps its factor workspace in a fixed array inside
-the library.  This test drives it through the C ABI with device buffers the
+solve - a server or framework whose own allocator owns the device's memory.
+They own the input and output buffers; the entry point keeps its factor
+workspace in a fixed array inside the library.  This test drives it through the C ABI with device buffers the
 test allocates (with torch), and checks it against pg_solve_ridge, the
 allocating entry point, on two calls in a row: the second call must not be
 disturbed by what the first left in the shared array.  It lives in its own
@@ -46,7 +45,8 @@ def _noalloc(A, b, alpha):
 def test_noalloc_matches_allocating_solve_twice():
     from pypolymlp_gb300.regression import solver_ridge
 
-    cases = [(_spd(700, 1), 1e-2), (_spd(300, 2), 1e-3)]  # a large call, then a smaller one
+    # the largest size the fixed array holds, then a smaller call after it
+    cases = [(_spd(1024, 1), 1e-2), (_spd(700, 3), 1e-2), (_spd(300, 2), 1e-3)]
     for (A, b), alpha in cases:
         ref, info_ref = solver_ridge(A, b, [alpha])
         got, info = _noalloc(A, b, alpha)
