@@ -117,6 +117,29 @@ int pg_features_x(pg_model* m, const pg_structures* st, const int64_t* e_row,
                   int precision);
 
 /*
+ * The CUDA stream (a cudaStream_t, passed as void*) on which the calling
+ * host thread's later calls issue their device work; NULL (the default) is
+ * the legacy default stream.  Per host thread, as the reference's objects are
+ * used one per thread (pybind11_mlp.cpp holds the GIL).  Every entry point
+ * returns once its results are on the host, so the stream orders the
+ * library's work against the caller's own work on it.  The allocation-free
+ * solve (pg_solve_ridge_noalloc) always uses the legacy default stream.  No
+ * reference counterpart (the reference has no device work).
+ */
+int pg_set_stream(void* stream);
+int pg_get_stream(void** stream);
+
+/*
+ * Work figures of a model, for roofline accounting (no reference
+ * counterpart): atom types, largest l, radial functions per type pair,
+ * k0_pair[a * n_type + b] = a_nlm heads (m <= 0 entries) of a centre of type
+ * a over its type-b neighbours (n_type^2; NULL to skip) and n_terms[a] =
+ * product terms of the feature values and their adjoint for type a (n_type;
+ * NULL to skip).
+ */
+int pg_model_work(const pg_model* m, int* n_type, int* max_l, int* n_radial, int* k0_pair, int64_t* n_terms);
+
+/*
  * Fused regression assembly: X rows are generated on the device, weighted,
  * and summed into X^T X, X^T y, y^T y and the column sums of the (unweighted)
  * energy rows, without X leaving the GPU.  Replaces the sequential loop of

@@ -45,6 +45,8 @@ def lib():
             L = C.CDLL(LIB_PATH)
             L.pg_last_error.argtypes = [C.c_char_p, C.c_size_t]
             L.pg_device_count.argtypes = [_ip]
+            L.pg_set_stream.argtypes = [_vp]
+            L.pg_get_stream.argtypes = [C.POINTER(_vp)]
             L.pg_model_create.argtypes = [_vp, C.POINTER(_vp)]
             L.pg_model_destroy.argtypes = [_vp]
             L.pg_model_n_features.argtypes = [_vp, _ip]
@@ -67,6 +69,7 @@ def lib():
                 ("pg_profile_read", [C.c_char_p, C.c_size_t, _dp, _ip, C.c_int, _ip]),
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
                 ("pg_solve_ridge_rhs", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
+                ("pg_model_work", [_vp, _ip, _ip, _ip, _ip, _i64p]),
                 ("pg_solve_ridge_noalloc", [C.c_int, _vp, _vp, C.c_double, _vp, _ip]),
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),
@@ -89,6 +92,37 @@ def device_count() -> int:
     n = C.c_int()
     check(lib().pg_device_count(C.byref(n)))
     return n.value
+
+
+def set_stream(stream=None):
+    """Issue the calling thread's later library calls on `stream`: a
+    torch.cuda.Stream, a raw cudaStream_t handle (int), or None for the legacy
+    default stream (pg_set_stream).  Every call still returns with its results
+    on the host; the stream orders its device work against the caller's."""
+    h = 0 if stream is None else int(getattr(stream, "cuda_stream", stream))
+    check(lib().pg_set_stream(_vp(h)))
+
+
+def get_stream() -> int:
+    """The raw cudaStream_t handle of the calling thread (0: legacy default)."""
+    h = _vp()
+    check(lib().pg_get_stream(C.byref(h)))
+    return int(h.value or 0)
+
+
+class on_stream:
+    """Context manager: library calls of this thread on `stream`, then back."""
+
+    def __init__(self, stream):
+        self.stream = stream
+
+    def __enter__(self):
+        self.prev = get_stream()
+        set_stream(self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        set_stream(self.prev)
 
 
 def require_device():
@@ -140,6 +174,19 @@ class Model:
                                   _p(s_row, C.c_int64), _p(out, C.c_double), C.c_int64(out.shape[0]),
                                   int(precision)))
         return out
+
+    def work(self):
+        """{n_type, max_l, n_radial, k0_pair (n_type x n_type heads), n_terms (per type)}."""
+        L = lib()
+        nt, ml, nr = C.c_int(), C.c_int(), C.c_int()
+        check(L.pg_model_work(self._h, C.byref(nt), C.byref(ml), C.byref(nr), C.POINTER(C.c_int)(),
+                              C.POINTER(C.c_int64)()))
+        k0 = np.zeros(nt.value * nt.value, np.int32)
+        terms = np.zeros(nt.value, np.int64)
+        check(L.pg_model_work(self._h, C.byref(nt), C.byref(ml), C.byref(nr), _p(k0, C.c_int),
+                              _p(terms, C.c_int64)))
+        return {"n_type": nt.value, "max_l": ml.value, "n_radial": nr.value,
+                "k0_pair": k0.reshape(nt.value, nt.value), "n_terms": terms}
 
     def feature_attrs(self):
         L = lib()

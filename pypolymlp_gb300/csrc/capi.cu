@@ -19,6 +19,9 @@ namespace pg {
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
+static thread_local cudaStream_t g_stream = nullptr;
+cudaStream_t current_stream() { return g_stream; }
+
 // ------------------------------------------------------------ profiler
 namespace {
 struct ProfRec {
@@ -353,8 +356,7 @@ void DeviceBatch::stage(const pg_structures* st, int s_begin, int s_end, double 
 
 void DeviceBatch::host_offsets() {
     nb_off.assign(n_atoms + 1, 0);
-    PG_CUDA(cudaMemcpy(nb_off.data(), d_nb_off.as<long long>(), sizeof(long long) * (n_atoms + 1),
-                       cudaMemcpyDeviceToHost));
+    copy_d2h(nb_off.data(), d_nb_off.as<long long>(), sizeof(long long) * (n_atoms + 1));
 }
 
 DevBatch DeviceBatch::view(double cutoff) const {
@@ -395,7 +397,7 @@ Model::Model(const pg_feature_params* p)
     dev64.build(flat, true);
     dev32.build(flat, false);
     s_missing.alloc(sizeof(int));
-    PG_CUDA(cudaMemset(s_missing.as<void>(), 0, sizeof(int)));
+    zero_async(s_missing.as<void>(), sizeof(int));
     max_k = max_k0 = 1;
     for (const auto& ft : flat.types) {
         max_k = std::max(max_k, ft.K);
@@ -530,9 +532,9 @@ void Model::batch_rows(DeviceBatch& b, const long long* d_e_row, const long long
 // batches until read here, after the work that fed it has completed.
 void Model::check_mirrors() {
     int missing = 0;
-    PG_CUDA(cudaMemcpy(&missing, s_missing.as<int>(), sizeof(int), cudaMemcpyDeviceToHost));
+    copy_d2h(&missing, s_missing.as<int>(), sizeof(int));
     if (missing) {
-        PG_CUDA(cudaMemset(s_missing.as<void>(), 0, sizeof(int)));
+        zero_async(s_missing.as<void>(), sizeof(int));
         throw std::runtime_error("internal: neighbour list is not symmetric");
     }
 }
@@ -598,6 +600,18 @@ int pg_last_error(char* buf, size_t len) {
         buf[len - 1] = 0;
     }
     return 0;
+}
+
+int pg_set_stream(void* stream) {
+    g_stream = static_cast<cudaStream_t>(stream);
+    return 0;
+}
+
+int pg_get_stream(void** stream) {
+    return guarded([&] {
+        if (!stream) throw std::runtime_error("null argument");
+        *stream = static_cast<void*>(g_stream);
+    });
 }
 
 int pg_device_count(int* count) {
@@ -681,6 +695,26 @@ int pg_model_feature_attrs(const pg_model* m, int* n_linear, int* radial_ids, in
     });
 }
 
+int pg_model_work(const pg_model* m, int* n_type, int* max_l, int* n_radial, int* k0_pair, int64_t* n_terms) {
+    return guarded([&] {
+        if (!m || !n_type || !max_l || !n_radial) throw std::runtime_error("null argument");
+        const pg::FlatModel& fm = m->m->flat;
+        *n_type = fm.n_type;
+        *max_l = fm.maxl;
+        *n_radial = fm.n_fn_max;
+        for (int a = 0; a < fm.n_type; ++a) {
+            const pg::FlatType& T = fm.types[a];
+            if (k0_pair)
+                for (int b = 0; b < fm.n_type; ++b) {
+                    const int tp = fm.type_pairs[a * fm.n_type + b];
+                    k0_pair[a * fm.n_type + b] =
+                        (tp >= 0 && tp + 1 < (int)T.tp_head_off.size()) ? T.tp_head_off[tp + 1] - T.tp_head_off[tp] : 0;
+                }
+            if (n_terms) n_terms[a] = (int64_t)T.val_terms.size() + (int64_t)T.g_terms.size();
+        }
+    });
+}
+
 int pg_feature_attrs(const pg_feature_params* fp, int* n_linear, int* radial_ids, int* gtinv_ids,
                      int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,
                      int* n_poly_values, int* poly_offsets, int* poly_values, int* type_pairs) {
@@ -703,7 +737,7 @@ int pg_features_x(pg_model* mh, const pg_structures* st, const int64_t* e_row, c
         Model& m = *mh->m;
         const bool fp64 = precision == PG_FP64;
         const int F = m.flat.n_features;
-        cudaStream_t stream = 0;
+        cudaStream_t stream = current_stream();
         const auto batches = m.plan_batches(st, fp64, device_batch_bytes());
         DeviceBatch b;
         DevBuf Xd, X64, d_e, d_f, d_s;
@@ -833,15 +867,15 @@ int pg_neighbor_list(const pg_structures* st, int structure, double cutoff, int 
         if (half) throw std::runtime_error("half lists are built by the evaluator; use half = 0");
         if (structure < 0 || structure >= st->n_st) throw std::runtime_error("structure index out of range");
         DeviceBatch b;
-        b.stage(st, structure, structure + 1, cutoff, 0);
+        b.stage(st, structure, structure + 1, cutoff, current_stream());
         b.host_offsets();
         *n_entries = b.n_pairs;
         if (!offsets) return;
         for (int i = 0; i <= b.n_atoms; ++i) offsets[i] = (int)b.nb_off[i];
         std::vector<int> nj(b.n_pairs);
         if (b.n_pairs) {
-            PG_CUDA(cudaMemcpy(nj.data(), b.d_nb_j.as<int>(), sizeof(int) * b.n_pairs, cudaMemcpyDeviceToHost));
-            PG_CUDA(cudaMemcpy(diffs, b.d_nb_d.as<double>(), sizeof(double) * 3 * b.n_pairs, cudaMemcpyDeviceToHost));
+            copy_d2h(nj.data(), b.d_nb_j.as<int>(), sizeof(int) * b.n_pairs);
+            copy_d2h(diffs, b.d_nb_d.as<double>(), sizeof(double) * 3 * b.n_pairs);
         }
         for (long long k = 0; k < b.n_pairs; ++k) neighbors[k] = nj[k];  // batch holds one structure: local ids
     });

@@ -265,7 +265,7 @@ struct Evaluator {
     std::vector<DevBuf> bufs;
     EvalTables et{};
     DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_vir, s_g, s_mirror, s_missing, d_E, d_S, d_F;
-    cudaStream_t stream = 0;
+    cudaStream_t stream = current_stream();
 
     Evaluator(const pg_feature_params* fp, const double* coeffs, int n, int prec) : precision(prec) {
         m = std::make_unique<Model>(fp);
@@ -446,6 +446,7 @@ int pg_eval_run(pg_eval* eh, const pg_structures* st, double* energy, double* fo
     return guarded([&] {
         if (!eh || !st || !energy || !forces || !stress) throw std::runtime_error("null argument");
         Evaluator& ev = *eh->e;
+        ev.stream = current_stream();
         const bool fp64 = ev.precision == PG_FP64;
         DeviceBatch b;
         long long a = 0;

@@ -273,7 +273,7 @@ struct Gram {
     int n_tiles64 = 0;
     double yty = 0;
     long long n_rows_total = 0;
-    cudaStream_t stream = 0;
+    cudaStream_t stream = current_stream();
 
     Gram(Model* mm, int prec) : m(mm), precision(prec), F(mm->flat.n_features) {
         G.alloc((size_t)F * F * sizeof(double));
@@ -392,12 +392,14 @@ int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int
         if (!x || !xtx || n_rows < 0 || n_features <= 0 || ld < n_rows) throw std::runtime_error("bad arguments");
         if (precision != PG_FP64 && precision != PG_MIXED) throw std::runtime_error("unknown precision");
         const int F = n_features;
-        cudaStream_t st = 0;
+        cudaStream_t st = current_stream();
         DevBuf X64((size_t)std::max<int64_t>(1, n_rows) * F * 8), G((size_t)F * F * 8);
-        PG_CUDA(cudaMemset(G.as<void>(), 0, G.bytes()));
-        if (n_rows > 0)
-            PG_CUDA(cudaMemcpy2D(X64.as<void>(), (size_t)n_rows * 8, x, (size_t)ld * 8, (size_t)n_rows * 8, F,
-                                 cudaMemcpyHostToDevice));
+        zero_async(G.as<void>(), G.bytes());
+        if (n_rows > 0) {
+            PG_CUDA(cudaMemcpy2DAsync(X64.as<void>(), (size_t)n_rows * 8, x, (size_t)ld * 8, (size_t)n_rows * 8, F,
+                                      cudaMemcpyHostToDevice, st));
+            PG_CUDA(cudaStreamSynchronize(st));
+        }
         if (n_rows > 0 && precision == PG_FP64) {
             const int nt = (F + kS64 - 1) / kS64;
             std::vector<int2> t;
@@ -417,7 +419,7 @@ int pg_gram_xtx(const double* x, int64_t n_rows, int n_features, int64_t ld, int
         dim3 grid((F + 255) / 256, F);
         pg_symmetrize<<<grid, 256, 0, st>>>(G.as<double>(), F);
         PG_CUDA(cudaGetLastError());
-        PG_CUDA(cudaMemcpy(xtx, G.as<double>(), (size_t)F * F * 8, cudaMemcpyDeviceToHost));
+        copy_d2h(xtx, G.as<double>(), (size_t)F * F * 8);
     });
 }
 
@@ -443,6 +445,7 @@ int pg_gram_destroy(pg_gram* g) {
 int pg_gram_reset(pg_gram* g) {
     return guarded([&] {
         if (!g) throw std::runtime_error("null gram");
+        g->g->stream = current_stream();
         g->g->reset();
     });
 }
@@ -452,6 +455,7 @@ int pg_gram_accumulate(pg_gram* gh, const pg_structures* st, const int64_t* e_ro
     return guarded([&] {
         if (!gh || !st || !e_row || !f_row || !s_row || !w || !y) throw std::runtime_error("null argument");
         Gram& g = *gh->g;
+        g.stream = current_stream();
         auto parts = prepare_batches(*g.m, st, e_row, f_row, s_row, n_rows, w, y, g.precision == PG_FP64);
         for (auto& P : parts) g.accumulate(*P);
         PG_CUDA(cudaStreamSynchronize(g.stream));
@@ -473,7 +477,7 @@ int pg_batch_create(pg_model* mh, const pg_structures* st, const int64_t* e_row,
             delete h;
             throw;
         }
-        PG_CUDA(cudaDeviceSynchronize());
+        PG_CUDA(cudaStreamSynchronize(current_stream()));
         *out = h;
     });
 }
@@ -485,6 +489,7 @@ int pg_batch_destroy(pg_batch* b) {
 int pg_gram_accumulate_batch(pg_gram* gh, pg_batch* b) {
     return guarded([&] {
         if (!gh || !b) throw std::runtime_error("null argument");
+        gh->g->stream = current_stream();
         for (auto& P : b->parts) gh->g->accumulate(*P);
     });
 }
@@ -495,11 +500,12 @@ int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef,
         if (!gh || !b || !coefs || n_coef < 1) throw std::runtime_error("bad arguments");
         if (n_coef > kMaxCoef) throw std::runtime_error("at most 16 coefficient vectors per residual pass");
         Gram& g = *gh->g;
+        g.stream = current_stream();
         const int F = g.F;
         DevBuf C((size_t)F * n_coef * 8), XtR((size_t)F * n_coef * 8), SQ((size_t)3 * n_coef * 8), R;
-        PG_CUDA(cudaMemcpy(C.as<void>(), coefs, (size_t)F * n_coef * 8, cudaMemcpyHostToDevice));
-        PG_CUDA(cudaMemset(XtR.as<void>(), 0, XtR.bytes()));
-        PG_CUDA(cudaMemset(SQ.as<void>(), 0, SQ.bytes()));
+        copy_h2d(C.as<void>(), coefs, (size_t)F * n_coef * 8);
+        zero_async(XtR.as<void>(), XtR.bytes());
+        zero_async(SQ.as<void>(), SQ.bytes());
         long long rows = 0;
         for (auto& P : b->parts) {
             g.residual(*P, C.as<double>(), n_coef, XtR.as<double>(), SQ.as<double>(), R);
@@ -507,8 +513,8 @@ int pg_batch_residual(pg_gram* gh, pg_batch* b, const double* coefs, int n_coef,
         }
         PG_CUDA(cudaStreamSynchronize(g.stream));
         g.m->check_mirrors();
-        if (xtr) PG_CUDA(cudaMemcpy(xtr, XtR.as<double>(), (size_t)F * n_coef * 8, cudaMemcpyDeviceToHost));
-        if (sq) PG_CUDA(cudaMemcpy(sq, SQ.as<double>(), (size_t)3 * n_coef * 8, cudaMemcpyDeviceToHost));
+        if (xtr) copy_d2h(xtr, XtR.as<double>(), (size_t)F * n_coef * 8);
+        if (sq) copy_d2h(sq, SQ.as<double>(), (size_t)3 * n_coef * 8);
         if (n_rows) *n_rows = rows;
     });
 }
@@ -518,6 +524,7 @@ int pg_gram_result(pg_gram* gh, double* xtx, double* xty, double* yty, double* x
     return guarded([&] {
         if (!gh) throw std::runtime_error("null gram");
         Gram& g = *gh->g;
+        g.stream = current_stream();
         const int F = g.F;
         dim3 grid((F + 255) / 256, F);
         pg_symmetrize<<<grid, 256, 0, g.stream>>>(g.G.as<double>(), F);
@@ -525,11 +532,10 @@ int pg_gram_result(pg_gram* gh, double* xtx, double* xty, double* yty, double* x
         PG_CUDA(cudaStreamSynchronize(g.stream));
         g.m->check_mirrors();
         gram_tc_check(g.tc);
-        if (xtx) PG_CUDA(cudaMemcpy(xtx, g.G.as<double>(), (size_t)F * F * sizeof(double), cudaMemcpyDeviceToHost));
-        if (xty) PG_CUDA(cudaMemcpy(xty, g.xty.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
-        if (xe_sum) PG_CUDA(cudaMemcpy(xe_sum, g.xe_sum.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
-        if (xe_sq_sum)
-            PG_CUDA(cudaMemcpy(xe_sq_sum, g.xe_sq.as<double>(), F * sizeof(double), cudaMemcpyDeviceToHost));
+        if (xtx) copy_d2h(xtx, g.G.as<double>(), (size_t)F * F * sizeof(double));
+        if (xty) copy_d2h(xty, g.xty.as<double>(), F * sizeof(double));
+        if (xe_sum) copy_d2h(xe_sum, g.xe_sum.as<double>(), F * sizeof(double));
+        if (xe_sq_sum) copy_d2h(xe_sq_sum, g.xe_sq.as<double>(), F * sizeof(double));
         if (yty) *yty = g.yty;
         if (n_rows_total) *n_rows_total = g.n_rows_total;
     });

@@ -486,7 +486,7 @@ void gram_tc_accumulate(const float* X, long long ld, long long rows, int F, dou
     S.E.reserve((size_t)n_seg * F * sizeof(int));
     if (S.err.bytes() == 0) {  // cumulative until gram_tc_check reads it
         S.err.alloc(sizeof(int));
-        PG_CUDA(cudaMemset(S.err.as<void>(), 0, sizeof(int)));
+        zero_async(S.err.as<void>(), sizeof(int));
     }
     // work units: upper tiles x row splits, split-major (tiles of one split share rows in L2)
     if (S.F != F || S.rows != rows) {
@@ -538,9 +538,9 @@ void gram_tc_accumulate(const float* X, long long ld, long long rows, int F, dou
 void gram_tc_check(GramTcScratch& S) {
     if (S.err.bytes() == 0) return;
     int e = 0;
-    PG_CUDA(cudaMemcpy(&e, S.err.as<int>(), sizeof(int), cudaMemcpyDeviceToHost));
+    copy_d2h(&e, S.err.as<int>(), sizeof(int));
     if (e) {
-        PG_CUDA(cudaMemset(S.err.as<void>(), 0, sizeof(int)));
+        zero_async(S.err.as<void>(), sizeof(int));
         throw std::runtime_error("tensor-core Gram timed out waiting on its pipeline");
     }
 }

@@ -18,6 +18,10 @@ namespace pg {
 
 void set_last_error(const std::string& msg);
 
+// The stream every entry point issues its work on: the calling thread's
+// stream set by pg_set_stream (default: the legacy default stream).
+cudaStream_t current_stream();
+
 #define PG_CUDA(call)                                                                                     \
     do {                                                                                                  \
         cudaError_t e_ = (call);                                                                          \
@@ -86,10 +90,29 @@ class DevBuf {
     size_t n_ = 0;
 };
 
+// Copies on the current stream that return when the data have arrived (the
+// host side may be freed or read right after).
+inline void copy_h2d(void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    const cudaStream_t st = current_stream();
+    PG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+}
+inline void copy_d2h(void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    const cudaStream_t st = current_stream();
+    PG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+}
+// Zero device memory, ordered on the current stream.
+inline void zero_async(void* dst, size_t bytes) {
+    if (bytes) PG_CUDA(cudaMemsetAsync(dst, 0, bytes, current_stream()));
+}
+
 template <class V>
 void upload(DevBuf& b, const std::vector<V>& v) {
     b.alloc(v.size() * sizeof(V));
-    if (!v.empty()) PG_CUDA(cudaMemcpy(b.as<void>(), v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+    copy_h2d(b.as<void>(), v.data(), v.size() * sizeof(V));
 }
 
 // Model uploaded to the device for one precision.

@@ -232,7 +232,7 @@ void ridge_batched(int F, const double* xtx, const double* rhs, long long rhs_st
     if (F <= 0 || !xtx || !rhs || !alphas || !coefs || !info || n_alpha < 0) throw std::runtime_error("bad arguments");
     if ((size_t)F * sizeof(double) > kSolveMaxSmem) throw std::runtime_error("n_features too large for the solver");
     if (n_alpha == 0) return;
-    cudaStream_t st = 0;
+    cudaStream_t st = current_stream();
     const size_t ff = (size_t)F * F * sizeof(double);
     // as many alphas per group as half the free memory holds
     size_t free_b = 0, total_b = 0;

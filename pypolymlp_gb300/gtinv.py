@@ -7,8 +7,8 @@ for each order k = 1..order the invariants of that order whose largest l is at
 most l_max[k-2] (0 for k = 1) are kept, in table order; the m combination of
 each term is returned as lm indices l*l + l + m.  The tables themselves are the
 reference's invariant basis (version 1: orders 1-6, version 2: orders 1-2),
-stored in data/gtinv_v{version}.npz (written by data/make_gtinv_tables.py; the
-layout is described there).  Errors follow polymlp_gtinv_data.cpp:34-40: an
+stored in data/gtinv_v{version}.npz (written by tests/golden/make_gtinv_tables.py;
+the layout is described there).  Errors follow polymlp_gtinv_data.cpp:34-40: an
 order above the version's largest table or an unknown version raise
 ValueError; a missing table raises RuntimeError.
 """

@@ -22,6 +22,7 @@ column sums in one call.
 from __future__ import annotations
 
 import ctypes as C
+import time
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -336,6 +337,7 @@ class FitResult:
     info: np.ndarray = field(repr=False, default=None)
     cg_iterations: int = 0                 # conjugate-gradient iterations (fit_cg)
     refine_sweeps: int = 0                 # iterative-refinement sweeps (fit)
+    timings: dict = field(repr=False, default=None)  # fit: wall seconds of its phases, training rows
 
     @property
     def scaled_coeffs(self):
@@ -472,12 +474,19 @@ def fit(params_dict: dict, train: Sequence[Dataset], test: Sequence[Dataset], al
     residuals over the test rows; the best alpha has the smallest test RMSE."""
     model = model or _ffi.Model(params_dict)
     alphas = np.asarray(alphas, dtype=np.float64)
+    t0 = time.perf_counter()
     tb, gram, xy = _assemble(model, train, precision, weight_stress)
+    t1 = time.perf_counter()
     coefs, info = solver_ridge(xy.xtx, xy.xty, alphas)
+    t2 = time.perf_counter()
     for _ in range(int(refine)):
         xtr, _, _ = batch_residual(gram, tb, coefs / xy.scales[:, None])
         r = xtr / xy.scales[:, None] - coefs * alphas[None, :]
         r[xy.zero_ids] = 0.0
         dc, info = solver_ridge(xy.xtx, np.asfortranarray(r), alphas)
         coefs = np.where(info[None, :] == 0, coefs + dc, 1e30)
-    return _select(model, gram, xy, test, coefs, alphas, precision, weight_stress, info, sweeps=int(refine))
+    t3 = time.perf_counter()
+    res = _select(model, gram, xy, test, coefs, alphas, precision, weight_stress, info, sweeps=int(refine))
+    res.timings = {"assemble_s": t1 - t0, "solve_s": t2 - t1, "refine_s": t3 - t2,
+                   "select_s": time.perf_counter() - t3, "train_rows": xy.total_n_data}
+    return res

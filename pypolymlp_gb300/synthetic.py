@@ -116,17 +116,22 @@ def binary_set(n_struct=5000, seed=2, n_min=64, n_max=128):
 
 
 def _min_dist_ok(frac, axis, dmin):
-    cart = frac @ axis.T
-    n = len(cart)
+    """Whether every pair (minimum image) is at least dmin apart.  Atoms are
+    added one at a time and the check stops at the first close pair: random
+    cells of this family almost always have one, early."""
+    n = len(frac)
     if n < 2:
         return True
-    d = cart[:, None, :] - cart[None, :, :]
-    inv = np.linalg.inv(axis)
-    f = d @ inv.T
-    f -= np.round(f)
-    d = f @ axis.T
-    r = np.sqrt((d ** 2).sum(-1)) + np.eye(n) * 1e9
-    return r.min() >= dmin
+    cart = frac @ axis.T
+    inv_t = np.linalg.inv(axis).T
+    for k in range(1, n):
+        d = cart[:k] - cart[k]
+        f = d @ inv_t
+        f -= np.round(f)
+        d = f @ axis.T
+        if np.einsum("ij,ij->i", d, d).min() < dmin * dmin:
+            return False
+    return True
 
 
 def ternary_set(n_struct=20000, seed=3, n_range=None, n_types=3, sigma=0.2):

@@ -93,6 +93,27 @@ def x_signature(x, seed=12345, n_proj=16, n_sample=4096):
             "sample": x.reshape(-1, order="F")[idx], "colmax": np.abs(x).max(axis=0)}
 
 
+def write_potential_model(p, sets, force_dataset, tag):
+    """X of several datasets with mixed force flags in PotentialModel's row
+    layout (PyModel::set_index), computed by the reference build."""
+    from pypolymlp_gb300.abi import row_layout_datasets
+
+    axis, pos, types = [], [], []
+    for ss in sets:
+        axis += list(ss.axis)
+        pos += list(ss.positions)
+        types += list(ss.types)
+    st = Structures(axis, pos, types)
+    n_st_dataset = [len(ss.types) for ss in sets]
+    e, f, s, n, fbegin, sbegin, n_data = row_layout_datasets(n_st_dataset, force_dataset, st.n_atoms)
+    x = ref.features_x(p, st, e, f, s, n)
+    sig = x_signature(x)
+    np.savez_compressed(os.path.join(HERE, f"x_{tag}.npz"), params=to_json(p), axis=st.axis, positions=st.positions,
+                        types=st.types, n_atoms=st.n_atoms, shape=np.array(x.shape), n_st_dataset=n_st_dataset,
+                        force_dataset=np.array(force_dataset), fbegin=fbegin, sbegin=sbegin, n_data=n_data, **sig)
+    print("wrote", tag, x.shape)
+
+
 def write_eval(p, coeffs, sset, tag):
     st = Structures(sset.axis, sset.positions, sset.types)
     e, f, s = ref.evaluate(p, coeffs, st)
@@ -113,6 +134,11 @@ def main():
     write_x("pair", pair, syn.binary_set(2, seed=7, n_min=16, n_max=32), "pair_mt2_p3")
     tri = syn.ternary_set(3, seed=3, n_range=(8, 40))
     write_x("cfg3", params("cfg3"), tri, "cfg3")
+    # the order-4 ternary model (F = 21,945) on two cells of its own family
+    write_x("cfg5p", params("cfg5p"), syn.ternary_set(2, seed=5, n_range=(32, 40)), "cfg5p")
+    # PotentialModel: three datasets, the middle one without forces
+    write_potential_model(params("cfg2"), [syn.binary_set(2, seed=11), syn.binary_set(3, seed=12),
+                                           syn.binary_set(1, seed=13)], [True, False, True], "potential_model")
     rng = np.random.default_rng(42)
     p2 = params("cfg2")
     c2 = rng.normal(size=ref.n_features(p2)) * 1e-3

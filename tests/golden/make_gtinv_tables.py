@@ -3,7 +3,9 @@
 The tables are the reference's invariant basis (version 1: orders 1-6,
 version 2: orders 1-2), read in full through the reference's own reader
 `Readgtinv` (src/pypolymlp/cxx/src/polymlp/polymlp_read_gtinv.cpp:12) built
-under oracle/_ref from the sources in /root/reference (make -C oracle ref).
+under oracle/_ref from the reference's sources (make -C oracle ref; the
+checkout is $PYPOLYMLP_REFERENCE, default /root/reference).  The tables are
+written to pypolymlp_gb300/data/.
 Asking for every order with an unbounded l_max returns every entry of the
 reference's tables, in their order; `pypolymlp_gb300.gtinv` then screens them
 by l_max as Readgtinv does.  The basis has to be the reference's: the
@@ -22,7 +24,8 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
 
 from oracle import ref  # noqa: E402
 
@@ -53,7 +56,7 @@ def tables(version):
 
 def main():
     for version in MAX_ORDER:
-        path = os.path.join(HERE, f"gtinv_v{version}.npz")
+        path = os.path.join(REPO, "pypolymlp_gb300", "data", f"gtinv_v{version}.npz")
         np.savez_compressed(path, **tables(version))
         print("wrote", path, os.path.getsize(path), "bytes")
 

@@ -1,6 +1,7 @@
 """Known-answer fixtures from the reference's own property tests.
 
-Run where the reference tree is available (it reads /root/reference):
+Run where the reference tree is available ($PYPOLYMLP_REFERENCE, default
+/root/reference):
 
     python tests/golden/make_known_answers.py
 
@@ -38,11 +39,13 @@ import sys
 
 import numpy as np
 
+REF_ROOT = os.environ.get("PYPOLYMLP_REFERENCE", "/root/reference")
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
-REF = "/root/reference/tests/test_calc"
+REF = REF_ROOT + "/tests/test_calc"
 OUT = os.path.join(HERE, "known_answers")
 
 # id: (test file, function, potentials, POSCAR, forces layout, stress unit)
@@ -145,7 +148,7 @@ def _x_asserts(fn):
 def function_answers():
     """Radial functions and Y_lm of tests/test_cxx/test_functions.py: the inputs and
     the asserted values (test_get_fn, test_get_ylm sums, test_get_ylm_2 tables)."""
-    path = "/root/reference/tests/test_cxx/test_functions.py"
+    path = REF_ROOT + "/tests/test_cxx/test_functions.py"
     out = {}
     fn = _function(path, "test_get_fn")
     call = next(n for n in ast.walk(fn) if isinstance(n, ast.Call) and getattr(n.func, "id", "") == "get_fn")
@@ -175,7 +178,7 @@ def function_answers():
 def gtinv_answers():
     """Invariant-table requests of tests/test_cxx/test_gtinv.py and their asserted
     values: (kind, index path, expected, approx) per assert."""
-    tree = ast.parse(open("/root/reference/tests/test_cxx/test_gtinv.py").read())
+    tree = ast.parse(open(REF_ROOT + "/tests/test_cxx/test_gtinv.py").read())
     out = {}
     for fn in tree.body:
         if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
@@ -255,7 +258,7 @@ def param_answers():
     reference sources with its compiled module stubbed out (not used by them)."""
     import types
 
-    sys.path.insert(0, "/root/reference/src")
+    sys.path.insert(0, REF_ROOT + "/src")
     stub = types.ModuleType("pypolymlp.cxx.lib")
     stub.libmlpcpp = None
     sys.modules.setdefault("pypolymlp.cxx.lib", stub)
@@ -283,8 +286,8 @@ def param_answers():
 
 
 VASP_FILES = {
-    "vasprun-00001-MgO.xml": "/root/reference/tests/files/vasprun-00001-MgO.xml",
-    "vasprun-00002-MgO.xml": "/root/reference/tests/files/vasprun-00002-MgO.xml",
+    "vasprun-00001-MgO.xml": REF_ROOT + "/tests/files/vasprun-00001-MgO.xml",
+    "vasprun-00002-MgO.xml": REF_ROOT + "/tests/files/vasprun-00002-MgO.xml",
     "vasprun-train1-00001.xml.polymlp": "data-vasp-MgO/vaspruns/train1/vasprun-00001.xml.polymlp",
     "vasprun-test1-00010.xml.polymlp": "data-vasp-MgO/vaspruns/test1/vasprun-00010.xml.polymlp",
 }
@@ -296,7 +299,7 @@ def vasp_answers():
     module stubbed out) of a few files, copied alongside."""
     import types
 
-    sys.path.insert(0, "/root/reference/src")
+    sys.path.insert(0, REF_ROOT + "/src")
     stub = types.ModuleType("pypolymlp.cxx.lib")
     stub.libmlpcpp = None
     sys.modules.setdefault("pypolymlp.cxx.lib", stub)
@@ -327,8 +330,8 @@ def api_answers():
     copied (as api.<name>)."""
     out = {}
     for fname, pot in API_TESTS.items():
-        tree = ast.parse(open(os.path.join("/root/reference/tests/test_cxx", fname)).read())
-        shutil.copyfile(os.path.join("/root/reference/tests/files", pot), os.path.join(OUT, "api." + pot))
+        tree = ast.parse(open(os.path.join(REF_ROOT + "/tests/test_cxx", fname)).read())
+        shutil.copyfile(os.path.join(REF_ROOT + "/tests/files", pot), os.path.join(OUT, "api." + pot))
         for fn in tree.body:
             if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_compute"):
                 continue
@@ -347,7 +350,7 @@ def api_answers():
     return out
 
 
-FIT_DIR = "/root/reference/tests/test_mlp_dev_api"
+FIT_DIR = REF_ROOT + "/tests/test_mlp_dev_api"
 EV_TO_KBAR = 1602.1766208
 
 
@@ -505,7 +508,7 @@ def _neighbor_expr(node):
 def neighbor_answers():
     out = {}
     for fname, poscar in NEIGHBOR_TESTS.items():
-        tree = ast.parse(open(os.path.join("/root/reference/tests/test_cxx", fname)).read())
+        tree = ast.parse(open(os.path.join(REF_ROOT + "/tests/test_cxx", fname)).read())
         for fn in tree.body:
             if not isinstance(fn, ast.FunctionDef) or not fn.name.startswith("test_"):
                 continue
@@ -530,7 +533,7 @@ def neighbor_answers():
                                    "approx": approx})
             if checks:
                 out[f"{fname}::{fn.name}"] = {"structure": poscar, "checks": checks}
-        shutil.copyfile(os.path.join("/root/reference/tests/files", poscar), os.path.join(OUT, poscar))
+        shutil.copyfile(os.path.join(REF_ROOT + "/tests/files", poscar), os.path.join(OUT, poscar))
     return out
 
 

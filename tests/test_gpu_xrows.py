@@ -35,7 +35,7 @@ def _colrel(x, ref):
     return float((np.abs(x - ref) / scale).max())
 
 
-@pytest.mark.parametrize("name", ["x_cfg1.npz", "x_cfg2.npz", "x_cfg3.npz", "x_pair_mt2_p3.npz"])
+@pytest.mark.parametrize("name", ["x_cfg1.npz", "x_cfg2.npz", "x_cfg3.npz", "x_cfg5p.npz", "x_pair_mt2_p3.npz"])
 def test_fp64_rows_match_reference_signature(name):
     from pypolymlp_gb300 import _ffi
 
@@ -54,6 +54,10 @@ CASES = {
                            gtinv_maxl=(2,)), lambda: syn.binary_set(2, seed=35, n_min=16, n_max=40)),
     "unary_order4": (dict(n_type=1, cutoff=6.0, model_type=2, max_p=2, gaussian_params2=(0, 5, 5), gtinv_order=4,
                           gtinv_maxl=(8, 8, 2)), lambda: syn.fcc_set(2, seed=33)),
+    # the order-4 ternary model of the large fit (F = 21,945, rc 8 A)
+    "ternary_order4_rc8": (dict(n_type=3, cutoff=8.0, model_type=3, max_p=2, gaussian_params2=(0, 5, 4),
+                                gtinv_order=4, gtinv_maxl=(8, 8, 2)),
+                           lambda: syn.ternary_set(2, seed=36, n_range=(24, 40))),
     "pair_mt2_p3": (dict(n_type=2, cutoff=6.0, model_type=2, max_p=3, feature_type="pair",
                          gaussian_params2=(0, 5, 6)), lambda: syn.binary_set(2, seed=34, n_min=16, n_max=40)),
 }

@@ -12,7 +12,7 @@ from conftest import assert_signature, load_golden
 from oracle import oracle, ref
 from pypolymlp_gb300.abi import row_layout
 
-X_CASES = ["x_cfg1.npz", "x_cfg2.npz", "x_cfg3.npz", "x_pair_mt2_p3.npz"]
+X_CASES = ["x_cfg1.npz", "x_cfg2.npz", "x_cfg3.npz", "x_cfg5p.npz", "x_pair_mt2_p3.npz"]
 
 
 @pytest.mark.parametrize("name", X_CASES)
