@@ -250,6 +250,29 @@ int pg_eval_run(pg_eval* e, const pg_structures* st, double* energy, double* for
                 double* stress);
 
 /*
+ * Repeated evaluation of the same atoms at new positions (molecular dynamics,
+ * the ASE calculator's loop, calculator/utils/ase_calculator.py:63, and the
+ * autograd wrapper).  pg_eval_bind stages the structures once and builds
+ * their neighbour lists with cutoff + skin; pg_eval_update takes the atoms'
+ * new Cartesian positions (same order as bound, sum(n_atoms) x 3) and only
+ * refreshes the kept entries' displacements, unless some atom has moved more
+ * than skin / 2 since the lists were built, when it rebuilds them (*rebuilt =
+ * 1).  The cell, atom counts and types stay those bound.
+ * pg_eval_bound_energy: energies only (no pair gradients: the forward pass of
+ * E); pg_eval_bound_run: energies, forces and stresses (recomputing a_nlm:
+ * the backward pass).  Results equal pg_eval_run's on the same positions up
+ * to summation order.  pg_eval_workspace_bytes: device bytes the evaluator
+ * holds (lists, a_nlm, adjoint and per-pair gradients; no per-atom
+ * derivative arrays).  No reference counterpart (the reference rebuilds its
+ * neighbour list per call).
+ */
+int pg_eval_bind(pg_eval* e, const pg_structures* st, double skin);
+int pg_eval_update(pg_eval* e, const double* positions, int* rebuilt);
+int pg_eval_bound_energy(pg_eval* e, double* energy);
+int pg_eval_bound_run(pg_eval* e, double* energy, double* forces, double* stress);
+int pg_eval_workspace_bytes(const pg_eval* e, int64_t* bytes);
+
+/*
  * Per-kernel timing with CUDA events on the launching stream.  pg_profile_read
  * synchronises the device and returns, per kernel name, the summed launch
  * durations (ms) and launch counts recorded since the previous read; names are

@@ -74,6 +74,11 @@ def lib():
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),
                 ("pg_eval_run", [_vp, _vp, _dp, _dp, _dp]),
+                ("pg_eval_bind", [_vp, _vp, C.c_double]),
+                ("pg_eval_update", [_vp, _dp, _ip]),
+                ("pg_eval_bound_energy", [_vp, _dp]),
+                ("pg_eval_bound_run", [_vp, _dp, _dp, _dp]),
+                ("pg_eval_workspace_bytes", [_vp, _i64p]),
             ]:
                 if hasattr(L, name):
                     getattr(L, name).argtypes = args
@@ -280,3 +285,35 @@ class Evaluator:
         check(lib().pg_eval_run(self._h, C.cast(st.ref(), _vp), _p(e, C.c_double), _p(f, C.c_double),
                                 _p(s, C.c_double)))
         return e, f, s
+
+    # -- bound structures: neighbour lists kept across position updates --------
+    def bind(self, st: Structures, skin: float = 0.5):
+        """Stage `st` for repeated evaluation with lists built at cutoff + skin."""
+        check(lib().pg_eval_bind(self._h, C.cast(st.ref(), _vp), float(skin)))
+        self._bound = (st.n_st, int(st.n_atoms.sum()), st)
+
+    def update(self, positions) -> bool:
+        """New Cartesian positions (sum N x 3) of the bound atoms; True if the
+        neighbour lists were rebuilt."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        if pos.shape[0] != self._bound[1]:
+            raise ValueError("positions do not match the bound atoms")
+        r = C.c_int()
+        check(lib().pg_eval_update(self._h, _p(pos, C.c_double), C.byref(r)))
+        return bool(r.value)
+
+    def bound_energy(self):
+        e = np.zeros(self._bound[0])
+        check(lib().pg_eval_bound_energy(self._h, _p(e, C.c_double)))
+        return e
+
+    def bound_run(self):
+        n_st, n_at, _ = self._bound
+        e, f, s = np.zeros(n_st), np.zeros((n_at, 3)), np.zeros((n_st, 6))
+        check(lib().pg_eval_bound_run(self._h, _p(e, C.c_double), _p(f, C.c_double), _p(s, C.c_double)))
+        return e, f, s
+
+    def workspace_bytes(self) -> int:
+        n = C.c_int64()
+        check(lib().pg_eval_workspace_bytes(self._h, C.byref(n)))
+        return int(n.value)

@@ -141,7 +141,9 @@ class _Model:
 
     def __init__(self, params: dict, coeffs, precision: int):
         self.params = params
-        self.prop = _properties.PotentialPropertiesFast(params, np.asarray(coeffs, dtype=np.float64), precision)
+        self.coeffs = np.asarray(coeffs, dtype=np.float64)
+        self.precision = precision
+        self.prop = _properties.PotentialPropertiesFast(params, self.coeffs, precision)
 
     def eval_multiple(self, structures: Sequence[PolymlpStructure]):
         n_st = len(structures)

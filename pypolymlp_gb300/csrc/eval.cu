@@ -21,6 +21,8 @@
 // half-list collection, up to summation order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <memory>
 
 #include "kernels.h"
@@ -266,6 +268,15 @@ struct Evaluator {
     EvalTables et{};
     DevBuf d_aoff, s_Anc, s_Aadj, s_E, s_vir, s_g, s_mirror, s_missing, d_E, d_S, d_F;
     cudaStream_t stream = current_stream();
+    // Structures bound for repeated evaluation (molecular dynamics): one
+    // batch whose neighbour lists are built with cutoff + skin and kept; new
+    // positions only refresh the displacements of the kept entries (the
+    // kernels drop entries beyond the cutoff), until some atom has moved more
+    // than skin / 2 since the lists were built.
+    std::unique_ptr<DeviceBatch> bound;
+    double skin = 0.0;
+    std::vector<int> bound_n_atoms, bound_types;
+    std::vector<double> bound_axis, bound_ref, bound_shift, bound_pos;
 
     Evaluator(const pg_feature_params* fp, const double* coeffs, int n, int prec) : precision(prec) {
         m = std::make_unique<Model>(fp);
@@ -330,11 +341,15 @@ struct Evaluator {
         }
     }
 
+    // energy_only: E per structure without the pair gradients (forces and
+    // stress are not written); lists_ready: the batch's neighbour lists are
+    // current (a bound batch).
     template <typename T>
-    void run_batch(DeviceBatch& b, double* energy, double* forces, double* stress) {
+    void run_batch(DeviceBatch& b, double* energy, double* forces, double* stress, bool energy_only = false,
+                   bool lists_ready = false) {
         const DeviceModel& dmod = sizeof(T) == 8 ? m->dev64 : m->dev32;
         const DevModel& M = dmod.dm;
-        b.build_neighbors(m->flat.cutoff, stream);
+        if (!lists_ready) b.build_neighbors(m->flat.cutoff, stream);
         const DevBatch B = b.view(m->flat.cutoff);
         AtomOffsets off;
         m->atom_offsets(b, off);
@@ -369,6 +384,17 @@ struct Evaluator {
                                                                    reinterpret_cast<cplx<T>*>(s_Aadj.as<void>()),
                                                                    s_E.as<double>());
             }
+            if (energy_only) {
+                PG_CUDA(cudaMemsetAsync(s_vir.as<void>(), 0, sizeof(double) * 6 * b.n_atoms, stream));
+                ProfScope ps("pg_eval_reduce", stream);
+                pg_eval_reduce<<<b.n_st, 256, 0, stream>>>(b.d_st_atom_off.as<int>(), s_E.as<double>(),
+                                                           s_vir.as<double>(), d_E.as<double>(), d_S.as<double>());
+                PG_CUDA(cudaGetLastError());
+                PG_CUDA(cudaMemcpyAsync(energy, d_E.as<double>(), sizeof(double) * b.n_st, cudaMemcpyDeviceToHost,
+                                        stream));
+                PG_CUDA(cudaStreamSynchronize(stream));
+                return;
+            }
             const int threads = 256, nw = threads / 32;
             const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
             const size_t sm2 = (size_t)m->max_k0 * 2 * sizeof(T) + 16 +
@@ -399,6 +425,12 @@ struct Evaluator {
             PG_CUDA(cudaMemsetAsync(d_S.as<void>(), 0, sizeof(double) * 6 * b.n_st, stream));
         }
         PG_CUDA(cudaGetLastError());
+        if (energy_only) {  // no atoms
+            PG_CUDA(cudaMemcpyAsync(energy, d_E.as<double>(), sizeof(double) * b.n_st, cudaMemcpyDeviceToHost,
+                                    stream));
+            PG_CUDA(cudaStreamSynchronize(stream));
+            return;
+        }
         int missing = 0;
         PG_CUDA(cudaMemcpyAsync(&missing, s_missing.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, stream));
         PG_CUDA(cudaMemcpyAsync(energy, d_E.as<double>(), sizeof(double) * b.n_st, cudaMemcpyDeviceToHost, stream));
@@ -411,6 +443,73 @@ struct Evaluator {
     }
 
     static const int* d_types(const DeviceBatch& b) { return b.d_types.as<int>(); }
+
+    // Bind structures: stage them and build lists with cutoff + skin.
+    void bind(const pg_structures* st, double skin_) {
+        if (!(skin_ >= 0.0) || !std::isfinite(skin_)) throw std::runtime_error("skin must be finite and >= 0");
+        const bool fp64 = precision == PG_FP64;
+        if (m->plan_batches(st, fp64, device_batch_bytes()).size() != 1)
+            throw std::runtime_error("bound structures must fit one device batch");
+        long long n_tot = 0;
+        for (int s = 0; s < st->n_st; ++s) n_tot += st->n_atoms[s];
+        auto b = std::make_unique<DeviceBatch>();
+        b->upload_structures(st, 0, st->n_st, m->flat.cutoff + skin_);
+        b->build_neighbors(m->flat.cutoff + skin_, stream);
+        bound_n_atoms.assign(st->n_atoms, st->n_atoms + st->n_st);
+        bound_types.assign(st->types, st->types + n_tot);
+        bound_axis.assign(st->axis, st->axis + 9 * (size_t)st->n_st);
+        bound_ref.assign(st->positions, st->positions + 3 * n_tot);
+        bound_shift.resize(3 * n_tot);
+        for (size_t q = 0; q < bound_shift.size(); ++q) bound_shift[q] = b->pos[q] - bound_ref[q];
+        bound_pos = b->pos;
+        skin = skin_;
+        bound = std::move(b);
+    }
+
+    // New Cartesian positions of the bound atoms (same order); returns whether
+    // the lists were rebuilt.
+    bool update(const double* positions) {
+        if (!bound) throw std::runtime_error("no structures are bound (pg_eval_bind)");
+        const size_t n3 = bound_ref.size();
+        double d2max = 0.0;
+        for (size_t a = 0; a < n3; a += 3) {
+            double d2 = 0.0;
+            for (int c = 0; c < 3; ++c) {
+                const double d = positions[a + c] - bound_ref[a + c];
+                d2 += d * d;
+            }
+            if (!std::isfinite(d2)) throw std::runtime_error("non-finite position");
+            d2max = std::max(d2max, d2);
+        }
+        if (d2max > 0.25 * skin * skin) {
+            pg_structures st{(int)bound_n_atoms.size(), bound_n_atoms.data(), bound_axis.data(), positions,
+                             bound_types.data()};
+            bind(&st, skin);
+            return true;
+        }
+        for (size_t q = 0; q < n3; ++q) bound_pos[q] = positions[q] + bound_shift[q];
+        copy_h2d(bound->d_pos.as<void>(), bound_pos.data(), n3 * sizeof(double));
+        const DevBatch B = bound->view(m->flat.cutoff + skin);
+        launch_nb_refresh(B, bound->d_nb_off.as<long long>(), bound->d_keys.as<long long>(), bound->d_nb_j.as<int>(),
+                          bound->d_nb_d.as<double>(), bound->d_nb_df.as<float4>(), stream);
+        PG_CUDA(cudaGetLastError());
+        return false;
+    }
+
+    void run_bound(double* energy, double* forces, double* stress, bool energy_only) {
+        if (!bound) throw std::runtime_error("no structures are bound (pg_eval_bind)");
+        if (precision == PG_FP64) run_batch<double>(*bound, energy, forces, stress, energy_only, true);
+        else run_batch<float>(*bound, energy, forces, stress, energy_only, true);
+    }
+
+    size_t workspace_bytes() const {
+        size_t n = d_aoff.bytes() + s_Anc.bytes() + s_Aadj.bytes() + s_E.bytes() + s_vir.bytes() + s_g.bytes() +
+                   s_mirror.bytes() + s_missing.bytes() + d_E.bytes() + d_S.bytes() + d_F.bytes();
+        if (bound)
+            n += bound->d_nb_j.bytes() + bound->d_nb_d.bytes() + bound->d_nb_df.bytes() + bound->d_keys.bytes() +
+                 bound->d_nb_off.bytes() + bound->d_pos.bytes();
+        return n;
+    }
 };
 
 }  // namespace pg
@@ -440,6 +539,46 @@ int pg_eval_create(const pg_feature_params* fp, const double* coeffs, int n_coef
 
 int pg_eval_destroy(pg_eval* e) {
     return guarded([&] { delete e; });
+}
+
+int pg_eval_bind(pg_eval* eh, const pg_structures* st, double skin) {
+    return guarded([&] {
+        if (!eh || !st) throw std::runtime_error("null argument");
+        eh->e->stream = current_stream();
+        eh->e->bind(st, skin);
+    });
+}
+
+int pg_eval_update(pg_eval* eh, const double* positions, int* rebuilt) {
+    return guarded([&] {
+        if (!eh || !positions) throw std::runtime_error("null argument");
+        eh->e->stream = current_stream();
+        const bool r = eh->e->update(positions);
+        if (rebuilt) *rebuilt = r ? 1 : 0;
+    });
+}
+
+int pg_eval_bound_energy(pg_eval* eh, double* energy) {
+    return guarded([&] {
+        if (!eh || !energy) throw std::runtime_error("null argument");
+        eh->e->stream = current_stream();
+        eh->e->run_bound(energy, nullptr, nullptr, true);
+    });
+}
+
+int pg_eval_bound_run(pg_eval* eh, double* energy, double* forces, double* stress) {
+    return guarded([&] {
+        if (!eh || !energy || !forces || !stress) throw std::runtime_error("null argument");
+        eh->e->stream = current_stream();
+        eh->e->run_bound(energy, forces, stress, false);
+    });
+}
+
+int pg_eval_workspace_bytes(const pg_eval* eh, int64_t* bytes) {
+    return guarded([&] {
+        if (!eh || !bytes) throw std::runtime_error("null argument");
+        *bytes = (int64_t)eh->e->workspace_bytes();
+    });
 }
 
 int pg_eval_run(pg_eval* eh, const pg_structures* st, double* energy, double* forces, double* stress) {

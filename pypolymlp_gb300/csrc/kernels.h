@@ -75,6 +75,10 @@ constexpr int kMaxTypePairs = 64;
 void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st);
 void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, float4* nb_df, long long* keys,
                     bool any_cl, cudaStream_t st);
+// Displacements of the existing list entries (keys[q] = entry q's neighbour and
+// translation) from the batch's current positions.
+void launch_nb_refresh(const DevBatch& B, const long long* off, const long long* keys, int* nb_j, double* nb_d,
+                       float4* nb_df, cudaStream_t st);
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
                  const long long* a_off, void* A, int max_k0, cudaStream_t st);

@@ -231,7 +231,7 @@ __global__ void pg_nb_disp(DevBatch B, const long long* offsets, const long long
 // Cell-list atoms: sort the candidate keys (block per atom, bitonic in shared
 // memory) into the reference's (j, t) order and write the list entries, with
 // the displacement recomputed exactly as the neighbour test forms it.
-__global__ void pg_nb_order(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d,
+__global__ void pg_nb_order(DevBatch B, const long long* offsets, long long* keys, int* nb_j, double* nb_d,
                             float4* nb_df) {
     __shared__ long long sk[kCellListMaxPairs];
     const int i = blockIdx.x;
@@ -261,7 +261,24 @@ __global__ void pg_nb_order(DevBatch B, const long long* offsets, const long lon
             }
             __syncthreads();
         }
-    for (int q = threadIdx.x; q < m; q += blockDim.x) write_entry(B, i, a0, t0, nt, sk[q], o0 + q, nb_j, nb_d, nb_df);
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        write_entry(B, i, a0, t0, nt, sk[q], o0 + q, nb_j, nb_d, nb_df);
+        keys[o0 + q] = sk[q];  // entry q's key, for later refreshes of its displacement
+    }
+}
+
+// Displacements of every list entry from its key, after the positions have
+// moved (the evaluator's neighbour-list reuse; one warp per atom).
+__global__ void pg_nb_refresh(DevBatch B, const long long* offsets, const long long* keys, int* nb_j, double* nb_d,
+                              float4* nb_df) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= B.n_atoms) return;
+    const int s = B.atom_st[i];
+    const int a0 = B.st_atom_off[s];
+    const int t0 = B.st_trans_off[s], nt = B.st_trans_off[s + 1] - t0;
+    for (long long q = offsets[i] + lane; q < offsets[i + 1]; q += 32)
+        write_entry(B, i, a0, t0, nt, keys[q], q, nb_j, nb_d, nb_df);
 }
 
 // ---------------------------------------------------------------- K2 a_nlm
@@ -1046,6 +1063,13 @@ void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* 
     pg_nb_fill<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, keys);
     if (any_cl) pg_nb_order<<<B.n_atoms, 256, 0, st>>>(B, off, keys, nb_j, nb_d, nb_df);
     pg_nb_disp<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, keys, nb_j, nb_d, nb_df);
+}
+
+void launch_nb_refresh(const DevBatch& B, const long long* off, const long long* keys, int* nb_j, double* nb_d,
+                       float4* nb_df, cudaStream_t st) {
+    const int threads = 256, warps = threads / 32;
+    if (B.n_atoms > 0)
+        pg_nb_refresh<<<(B.n_atoms + warps - 1) / warps, threads, 0, st>>>(B, off, keys, nb_j, nb_d, nb_df);
 }
 
 template <typename T>

@@ -197,7 +197,8 @@ def test_ase_calculator_reproduces_reference_known_answers(on_oracle):
                                      [st.types[i] for i in perm])
     atoms = _FakeAtoms(shuffled)
     assert ase_atoms_to_structure(atoms).elements == ["Mg", "O"] * 4
-    ase_calc = PolymlpASECalculator(pot=_pots(case)[0])
+    # the per-call path (the GPU test covers the bound path that keeps neighbour lists)
+    ase_calc = PolymlpASECalculator(pot=_pots(case)[0], reuse_neighbors=False)
     e = ase_calc.get_potential_energy(atoms)
     assert e == pytest.approx(case["energy"], **case["energy_tol"])
     f = ase_calc.get_forces(atoms)
