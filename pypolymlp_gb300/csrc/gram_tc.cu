@@ -382,26 +382,35 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     mbar_arrive(smem_u32(&acce_bar));
                 }
                 if (gi < F) {
+                    // eight columns at a time: their partial sums are loaded
+                    // together (one L2 round trip), then updated and stored
 #pragma unroll
-                    for (int k2 = 0; k2 < 32; ++k2) {
-                        const int gj = tj * kTcTile + (int)col + k2;
-                        if (gj < F && gi <= gj) {
+                    for (int k0 = 0; k0 < 32; k0 += 8) {
+                        float oh[8], ol[8];
+                        int ex[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int gj = tj * kTcTile + (int)col + k0 + u;
+                            const bool in = gj < F && gi <= gj;
                             const size_t idx = (size_t)gj * F + gi;
-                            const int k = ea + Es[gj];
-                            const float sa = ldexpf(sv[k2], k), ta = ldexpf(tv[k2], k);
-                            float h, l;
-                            if (seg == 0) {
-                                h = __fadd_rn(sa, ta);
-                                l = __fsub_rn(ta, __fsub_rn(h, sa));
-                            } else {
+                            ex[u] = in ? __ldg(Es + gj) : 0;
+                            oh[u] = (in && seg > 0) ? __ldcg(ph + idx) : 0.f;
+                            ol[u] = (in && seg > 0) ? __ldcg(pl + idx) : 0.f;
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const int gj = tj * kTcTile + (int)col + k0 + u;
+                            if (gj < F && gi <= gj) {
+                                const size_t idx = (size_t)gj * F + gi;
+                                const int k = ea + ex[u];
+                                const float sa = ldexpf(sv[k0 + u], k), ta = ldexpf(tv[k0 + u], k);
                                 float x, y;
-                                two_sum(ph[idx], sa, x, y);
-                                y = __fadd_rn(y, __fadd_rn(pl[idx], ta));
-                                h = __fadd_rn(x, y);
-                                l = __fsub_rn(y, __fsub_rn(h, x));
+                                two_sum(oh[u], sa, x, y);
+                                y = __fadd_rn(y, __fadd_rn(ol[u], ta));
+                                const float h = __fadd_rn(x, y);
+                                __stcg(ph + idx, h);
+                                __stcg(pl + idx, __fsub_rn(y, __fsub_rn(h, x)));
                             }
-                            ph[idx] = h;
-                            pl[idx] = l;
                         }
                     }
                 }
