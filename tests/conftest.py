@@ -12,6 +12,16 @@ if REPO not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built extension")
+    config.addinivalue_line("markers", "slow: CPU check of minutes; runs with PYPOLYMLP_SLOW=1")
+
+
+def pytest_collection_modifyitems(config, items):
+    if os.environ.get("PYPOLYMLP_SLOW") == "1":
+        return
+    skip = pytest.mark.skip(reason="slow CPU check (set PYPOLYMLP_SLOW=1 to run it)")
+    for item in items:
+        if "slow" in item.keywords:
+            item.add_marker(skip)
 
 
 def load_golden(name):

@@ -400,6 +400,11 @@ FIT_CASES = {
                      "_check_errors_single_dataset_MgO", ["train1", "test1"]),
     "gtinv_multi": ("polymlp.in.vasp.multi.MgO", "test_mlp_devel_multiple_datasets",
                     "_check_errors_multiple_datasets_MgO", ["train1", "train2", "test1", "test2"]),
+    # a hybrid of three gtinv models fitted together (5,736 features); the datasets,
+    # alphas and atomic energies come from the first input file
+    "hybrid_single": (["infile-hybrid-MgO/polymlp1_hybrid.in", "infile-hybrid-MgO/polymlp2_hybrid.in",
+                       "infile-hybrid-MgO/polymlp3_hybrid.in"], "test_mlp_devel_hybrid_single_dataset",
+                      "_check_errors_hybrid_single_dataset_MgO", ["train1", "test1"]),
 }
 FIT_DATA = "data-vasp-MgO/vaspruns/{}/vasprun-*.xml.polymlp"
 
@@ -430,9 +435,12 @@ def fit_known_answers():
 
     cases, arrays = {}, {}
     test_src = os.path.join(FIT_DIR, "test_mlp_devel_vasp.py")
-    for cid, (infile, test_fn, helper, names) in FIT_CASES.items():
-        inp = _read_input(os.path.join(FIT_DIR, infile))
-        shutil.copyfile(os.path.join(FIT_DIR, infile), os.path.join(OUT, infile))
+    for cid, (infiles, test_fn, helper, names) in FIT_CASES.items():
+        infiles = [infiles] if isinstance(infiles, str) else infiles
+        inps = [_read_input(os.path.join(FIT_DIR, f)) for f in infiles]
+        for f in infiles:
+            shutil.copyfile(os.path.join(FIT_DIR, f), os.path.join(OUT, os.path.basename(f)))
+        inp = inps[0]
         elements = inp["elements"]
         atom_e = np.array([float(v) for v in inp["atomic_energy"]])
         for tag in names:
@@ -452,19 +460,27 @@ def fit_known_answers():
         n_features = next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
                           if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
         a0, a1, na = (float(v) for v in inp["reg_alpha_params"])
-        st = {"n_type": int(inp["n_type"][0]), "elements": elements, "feature_type": inp["feature_type"][0],
-              "cutoff": float(inp["cutoff"][0]), "model_type": int(inp["model_type"][0]),
-              "max_p": int(inp["max_p"][0]), "gaussian_params1": [float(v) for v in inp["gaussian_params1"]],
-              "gaussian_params2": [float(v) for v in inp["gaussian_params2"]],
-              "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features,
-              "include_stress": inp.get("include_stress", ["True"])[0].lower() in ("true", "1")}
-        if st["feature_type"] == "gtinv":
-            st["gtinv_order"] = int(inp["gtinv_order"][0])
-            st["gtinv_maxl"] = [int(v) for v in inp["gtinv_maxl"]]
+
+        def settings(one):
+            st = {"n_type": int(one["n_type"][0]), "elements": one["elements"],
+                  "feature_type": one["feature_type"][0], "cutoff": float(one["cutoff"][0]),
+                  "model_type": int(one["model_type"][0]), "max_p": int(one["max_p"][0]),
+                  "gaussian_params1": [float(v) for v in one["gaussian_params1"]],
+                  "gaussian_params2": [float(v) for v in one["gaussian_params2"]],
+                  "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features,
+                  "include_stress": inp.get("include_stress", ["True"])[0].lower() in ("true", "1")}
+            if st["feature_type"] == "gtinv":
+                st["gtinv_order"] = int(one["gtinv_order"][0])
+                st["gtinv_maxl"] = [int(v) for v in one["gtinv_maxl"]]
+            return st
+
+        st = settings(inp)
         cases[cid] = {"test": f"tests/test_mlp_dev_api/test_mlp_devel_vasp.py::{test_fn}", "settings": st,
                       "train": [n for n in names if n.startswith("train")],
                       "test_sets": [n for n in names if n.startswith("test")],
                       "errors": _fit_errors(_function(test_src, helper), names), "data": "fit_MgO.npz"}
+        if len(inps) > 1:
+            cases[cid]["models"] = [settings(one) for one in inps]
         print(cid, cases[cid]["errors"])
     np.savez_compressed(os.path.join(OUT, "fit_MgO.npz"), **arrays)
     with open(os.path.join(OUT, "known_fit.json"), "w") as f:
