@@ -155,9 +155,12 @@ class Pypolymlp:
         (core/parser_polymlp_params.py, parser_infile.py:15-30, dataset.py:119-140):
         model keys as `set_params` takes them, `distance A B d1 d2 ...` lines,
         `atomic_energy`, `reg_alpha_params`, `include_force` / `include_stress`,
-        and `train_data` / `test_data` / `data` lines "glob [include_force [weight]]"
-        (files sorted; `data` split by the reference's rule; the dataset is named by
-        its glob, `prefix` is prepended to it)."""
+        and `train_data` / `test_data` / `data` / `data_md` lines "glob [include_force
+        [weight]]" (files sorted; `data` split by file with the reference's rule
+        into "Train_<glob>" and "Test_<glob>", `data_md` - one MD vasprun.xml - split
+        by step the same way, parser_polymlp_params.py:253-284, dataset.py:142-205;
+        other datasets are named by their glob; `prefix` is prepended to the
+        path)."""
         import glob
 
         from pypolymlp_gb300.io_vasp import split_train_test
@@ -214,8 +217,16 @@ class Pypolymlp:
                 self._test.append(self._vasp_dataset(files, name, force, stress, weight))
             elif tag == "data":
                 tr, te = split_train_test(files, train_ratio)
-                self._train.append(self._vasp_dataset(tr, name, force, stress, weight))
-                self._test.append(self._vasp_dataset(te, name, force, stress, weight))
+                self._train.append(self._vasp_dataset(tr, "Train_" + name, force, stress, weight))
+                self._test.append(self._vasp_dataset(te, "Test_" + name, force, stress, weight))
+            elif tag == "data_md":
+                from pypolymlp_gb300.io_vasp import parse_properties_from_vaspruns, split_ids_train_test
+
+                sts, (e, f, st6) = parse_properties_from_vaspruns(files, verbose=self._verbose)
+                tr, te = split_ids_train_test(len(sts), train_ratio)
+                for ids, nm, out in ((tr, "Train_" + name, self._train), (te, "Test_" + name, self._test)):
+                    out.append(self._dataset([sts[i] for i in ids], e[ids], [f[i] for i in ids], st6[ids], nm,
+                                             force, stress, weight))
         return self
 
     def _dataset(self, structures, energies, forces, stresses, name, include_force=None, include_stress=None,

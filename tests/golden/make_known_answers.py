@@ -408,6 +408,40 @@ FIT_CASES = {
 }
 FIT_DATA = "data-vasp-MgO/vaspruns/{}/vasprun-*.xml.polymlp"
 
+# fits whose `data` lines the reference splits itself ("automatic division": the
+# sorted files of glob "*N", i.e. testN then trainN, split by split_train_test):
+# case -> (input file, test function, error helper or None (asserts inline),
+# helper argument names, the file groups in sorted order, force flag per group)
+AUTO_CASES = {
+    "gtinv_single_auto": ("polymlp.in.vasp.single.auto.MgO", "test_mlp_devel_single_dataset_autodiv",
+                          "_check_errors_single_dataset_MgO_auto", ["train1", "test1"],
+                          [["test1", "train1"]], [True]),
+    "gtinv_multi_auto": ("polymlp.in.vasp.multi.auto.MgO", "test_mlp_devel_multiple_datasets_autodiv", None, None,
+                         [["test1", "train1"], ["test2", "train2"]], [True, True]),
+    "gtinv_multi_auto_selective": ("polymlp.in.vasp.multi.auto.selective.MgO",
+                                   "test_mlp_devel_multiple_datasets_autodiv_selective", None, None,
+                                   [["test1", "train1"], ["test2", "train2"]], [True, False]),
+}
+# one MD vasprun.xml split by step (data_md): case -> (input, test, helper, names, file)
+MD_CASES = {"md_Cu": ("polymlp.in.vasp.md.Cu", "test_mlp_devel_md", "_check_errors_md_Cu", ["train", "test"],
+                      "data-vasp-md-Cu/vasprun.xml")}
+
+
+def _inline_errors(fn):
+    """{tag: {quantity: {value, abs}}} of asserts `error_<tag>[q] == approx(v, abs=a)`
+    written in a test function itself."""
+    expected = {}
+    for node in ast.walk(fn):
+        if isinstance(node, ast.Assert) and isinstance(node.test, ast.Compare) and \
+                isinstance(node.test.left, ast.Subscript) and isinstance(node.test.left.value, ast.Name):
+            var = node.test.left.value.id
+            if not var.startswith("error_"):
+                continue
+            call = node.test.comparators[0]
+            expected.setdefault(var[len("error_"):], {})[ast.literal_eval(node.test.left.slice)] = {
+                "value": ast.literal_eval(call.args[0]), **{k.arg: ast.literal_eval(k.value) for k in call.keywords}}
+    return expected
+
 
 def _fit_errors(fn, names):
     """{dataset name: {quantity: {value, abs}}} of an error-check helper whose
@@ -481,6 +515,43 @@ def fit_known_answers():
                       "errors": _fit_errors(_function(test_src, helper), names), "data": "fit_MgO.npz"}
         if len(inps) > 1:
             cases[cid]["models"] = [settings(one) for one in inps]
+        print(cid, cases[cid]["errors"])
+    def plain_settings(inp, n_features):
+        a0, a1, na = (float(v) for v in inp["reg_alpha_params"])
+        st = {"n_type": int(inp["n_type"][0]), "elements": inp["elements"], "feature_type": inp["feature_type"][0],
+              "cutoff": float(inp["cutoff"][0]), "model_type": int(inp["model_type"][0]),
+              "max_p": int(inp["max_p"][0]), "gaussian_params1": [float(v) for v in inp["gaussian_params1"]],
+              "gaussian_params2": [float(v) for v in inp["gaussian_params2"]],
+              "alphas": list(np.logspace(a0, a1, int(na))), "n_features": n_features,
+              "include_stress": inp.get("include_stress", ["True"])[0].lower() in ("true", "1"),
+              "atomic_energy": [float(v) for v in inp["atomic_energy"]]}
+        if st["feature_type"] == "gtinv":
+            st["gtinv_order"] = int(inp["gtinv_order"][0])
+            st["gtinv_maxl"] = [int(v) for v in inp["gtinv_maxl"]]
+        return st
+
+    def n_features_of(fit):
+        return next(ast.literal_eval(n.comparators[0]) for n in ast.walk(fit)
+                    if isinstance(n, ast.Compare) and getattr(n.left, "attr", "") == "n_features")
+
+    for cid, (infile, test_fn, helper, names, groups, forces) in AUTO_CASES.items():
+        inp = _read_input(os.path.join(FIT_DIR, infile))
+        shutil.copyfile(os.path.join(FIT_DIR, infile), os.path.join(OUT, infile))
+        fit = _function(test_src, test_fn)
+        errors = _fit_errors(_function(test_src, helper), names) if helper else _inline_errors(fit)
+        cases[cid] = {"test": f"tests/test_mlp_dev_api/test_mlp_devel_vasp.py::{test_fn}",
+                      "settings": plain_settings(inp, n_features_of(fit)), "auto": {"groups": groups, "force": forces},
+                      "errors": errors, "data": "fit_MgO.npz"}
+        print(cid, cases[cid]["errors"])
+    for cid, (infile, test_fn, helper, names, md_file) in MD_CASES.items():
+        inp = _read_input(os.path.join(FIT_DIR, infile))
+        shutil.copyfile(os.path.join(FIT_DIR, infile), os.path.join(OUT, infile))
+        os.makedirs(os.path.join(OUT, os.path.dirname(md_file)), exist_ok=True)
+        shutil.copyfile(os.path.join(FIT_DIR, md_file), os.path.join(OUT, md_file))
+        fit = _function(test_src, test_fn)
+        cases[cid] = {"test": f"tests/test_mlp_dev_api/test_mlp_devel_vasp.py::{test_fn}",
+                      "settings": plain_settings(inp, n_features_of(fit)), "input": infile, "md_file": md_file,
+                      "errors": _fit_errors(_function(test_src, helper), names)}
         print(cid, cases[cid]["errors"])
     np.savez_compressed(os.path.join(OUT, "fit_MgO.npz"), **arrays)
     with open(os.path.join(OUT, "known_fit.json"), "w") as f:

@@ -29,9 +29,32 @@ def _cases():
 
 
 def _datasets(case):
-    """(training datasets, test datasets) of a case, named as in its error table."""
+    """(training datasets, test datasets) of a case, named as in its error table.
+    Automatic division ("auto"): each group's files in sorted order (testN, then
+    trainN) form one dataset, split as the reference's split_train_test splits
+    files, into trainN and testN."""
     z = np.load(os.path.join(KA, case["data"]))
     stress = case["settings"]["include_stress"]
+    if "auto" in case:
+        from pypolymlp_gb300.io_vasp import split_ids_train_test
+
+        train, test = [], []
+        for g, (tags, force) in enumerate(zip(case["auto"]["groups"], case["auto"]["force"]), start=1):
+            parts = []
+            for tag in tags:
+                n = z[f"{tag}_n_atoms"]
+                offs = np.concatenate([[0], np.cumsum(n)])
+                for i in range(len(n)):
+                    sl = slice(offs[i], offs[i + 1])
+                    parts.append((z[f"{tag}_axis"][i], z[f"{tag}_positions"][sl], z[f"{tag}_types"][sl],
+                                  z[f"{tag}_energies"][i], z[f"{tag}_forces"][sl], z[f"{tag}_stresses"][i]))
+            tr, te = split_ids_train_test(len(parts), 0.9)
+            for ids, name, out in ((tr, f"train{g}", train), (te, f"test{g}", test)):
+                sel = [parts[i] for i in ids]
+                out.append(Dataset([p[0] for p in sel], [p[1] for p in sel], [p[2] for p in sel],
+                                   np.array([p[3] for p in sel]), [p[4] for p in sel], np.array([p[5] for p in sel]),
+                                   include_force=force, include_stress=stress and force, name=name))
+        return train, test
 
     def one(tag):
         n = z[f"{tag}_n_atoms"]
@@ -84,15 +107,22 @@ def cpu_errors(p, coeffs, datasets):
     return errors
 
 
-def _single_cases():
-    return sorted(k for k, c in _cases().items() if "models" not in c)
+def _single_cases(slow_auto=False):
+    """One-model fits from the npz data; with slow_auto the automatic-division
+    cases carry the slow mark (minutes on the CPU)."""
+    out = []
+    for k, c in sorted(_cases().items()):
+        if "models" in c or "md_file" in c:
+            continue
+        out.append(pytest.param(k, marks=pytest.mark.slow) if slow_auto and "auto" in c else k)
+    return out
 
 
 def _hybrid_cases():
     return sorted(k for k, c in _cases().items() if "models" in c)
 
 
-@pytest.mark.parametrize("name", _single_cases())
+@pytest.mark.parametrize("name", _single_cases(slow_auto=True))
 def test_cpu_pipeline_reproduces_reference_fit_errors(name):
     from oracle import oracle
 
@@ -117,7 +147,7 @@ def _gpu_fit_errors(name, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["pair_single"])
+@pytest.mark.parametrize("name", _single_cases())
 def test_gpu_fit_reproduces_reference_fit_errors(name):
     from pypolymlp_gb300 import _ffi
 

@@ -258,3 +258,37 @@ def test_hybrid_front_end_fits_saves_and_reloads(monkeypatch, tmp_path):
     err, _ = prediction_errors(d, e, f, s)
     for k in ("energy", "force", "stress"):
         assert err[k] == pytest.approx(train_err["data1"][k], rel=1e-9)
+
+
+def _md_front_end():
+    """The reference's MD fit (test_mlp_devel_vasp.py::test_mlp_devel_md): Cu, 225
+    features, one MD vasprun.xml whose steps the parameter file's data_md line
+    splits into Train_ and Test_ datasets."""
+    from test_known_fit import KA, _cases
+
+    case = _cases()["md_Cu"]
+    pm = Pypolymlp().load_parameter_file(f"{KA}/{case['input']}", prefix=KA)
+    return pm, case
+
+
+def _check_md(pm, case):
+    from test_known_fit import _check as check_errors
+
+    train, test = pm.errors
+    name = case["md_file"]
+    check_errors({"train": train["Train_" + name], "test": test["Test_" + name]}, case["errors"])
+
+
+def test_front_end_md_fit_reproduces_reference_fit_errors(on_oracle):
+    pm, case = _md_front_end()
+    assert pm.n_features == case["settings"]["n_features"]
+    assert [d.name for d in pm.train] == ["Train_" + case["md_file"]]
+    pm.run()
+    _check_md(pm, case)
+
+
+@pytest.mark.gpu
+def test_gpu_front_end_md_fit_reproduces_reference_fit_errors():
+    pm, case = _md_front_end()
+    pm.run()
+    _check_md(pm, case)
