@@ -73,6 +73,8 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         for (int tp = 0; tp < fm.n_tp; ++tp)
             dm.max_k0tp = std::max(dm.max_k0tp, ft.tp_head_off[tp + 1] - ft.tp_head_off[tp]);
     }
+    // the stride of the group vectors: a multiple of 4, so that stage B reads them as vectors
+    dm.max_lin = (dm.max_lin + 3) & ~3;
     const int F = fm.n_features;
     const size_t smem_limit = 227 * 1024;
     if (rows_pairs_smem_bytes(dm, fp64) > smem_limit)

@@ -149,7 +149,7 @@ __device__ __forceinline__ void load_full_a(const DevType& ty, const cplx<T>* A,
 
 struct DevModel {
     int n_type, n_tp, F, n_fn_max, maxl, n_ylm, gtinv;
-    int max_k0, max_lin;  // largest K0 and n_lin over the centre types (shared-memory layouts)
+    int max_k0, max_lin;  // largest K0 and n_lin (rounded up to a multiple of 4) over the centre types
     int max_k0tp;         // largest number of heads of one type pair
     double cutoff;
     const int* type_pairs;

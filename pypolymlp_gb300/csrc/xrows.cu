@@ -790,6 +790,23 @@ __device__ __forceinline__ void prod_col_add(const ProdCol& pc, const T* src, co
     }
 }
 
+// Four consecutive values from a 16-byte-aligned address (FP32: one float4;
+// FP64: two double2).
+__device__ __forceinline__ void load_vec4(const float* p, float (&v)[4]) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+}
+__device__ __forceinline__ void load_vec4(const double* p, double (&v)[4]) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
@@ -849,28 +866,31 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
             ProdCol pc;
             const bool has_pc = fuse && (int)threadIdx.x < ty.n_prod && prod_col(ty, ipos, nnz, threadIdx.x, pc);
             T pv[3] = {0, 0, 0};
+            // thread = S consecutive positions of a slab, read as one vector per
+            // Cartesian component (the group vectors' stride NL is a multiple of 4)
             for (int slab = 0; slab < nnz; slab += S * blockDim.x) {
+                const int xb = slab + S * (int)threadIdx.x;
                 T acc[S][3];
 #pragma unroll
                 for (int m = 0; m < S; ++m) acc[m][0] = acc[m][1] = acc[m][2] = (T)0;
-#pragma unroll 2
+#pragma unroll 4
                 for (int k = 0; k < n; ++k) {
                     const long long q = sb + s_list[k];
                     const T* src = Dp + (size_t)q * 3 * NL;
+                    if (xb < nnz) {
 #pragma unroll
-                    for (int m = 0; m < S; ++m) {
-                        const int x = slab + threadIdx.x + m * blockDim.x;
-                        if (x < nnz) {
-                            acc[m][0] += src[x];
-                            acc[m][1] += src[NL + x];
-                            acc[m][2] += src[2 * NL + x];
+                        for (int c = 0; c < 3; ++c) {
+                            T v[S];
+                            load_vec4(src + (size_t)c * NL + xb, v);
+#pragma unroll
+                            for (int m = 0; m < S; ++m) acc[m][c] += v[m];
                         }
                     }
                     if (has_pc) prod_col_add(pc, src, D + d_off[nb_j[q]], NL, pv);
                 }
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
-                    const int x = slab + threadIdx.x + m * blockDim.x;
+                    const int x = xb + m;
                     if (x >= nnz) continue;
                     const int col = ty.lin_col[perm[x]];
                     if (col < 0) continue;
@@ -957,68 +977,121 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     }
 }
 
-// Energy and stress rows: block per (structure, kEsCols columns), kEsSlices
-// threads per column, each summing every kEsSlices-th centre of the structure
-// (long sums: FP64, or float-float in the FP32 kernel); the slices' sums are
-// then added in slice order:
+// Energy and stress rows, block per structure:
 //   X[e_row, col] = sum_i poly_col(d(i)),
 //   X[s_row + q, col] = -sum_i sum_{k in col} w_k,col(i) DS[i][3+q][k].
-constexpr int kEsCols = 64, kEsSlices = 4;
+// A linear column (one feature k, w = 1) is a plain sum over the structure's
+// atoms of its centre type: thread = features k, t + 256 r (r < kEsFeat) held
+// in registers while the atoms go by, so that each atom's feature and DS rows
+// are read together by the block (contiguous features, DS rows at the
+// features' positions of each type pair).  Product columns: thread = column,
+// weights from the atom's features.  Every sum runs over the atoms in order in
+// a long accumulator (FP64, or float-float in the FP32 kernel) and is added to
+// X (zeroed per batch) type by type, since a column can belong to the features
+// of several centre types (those of a type pair): deterministic.
+constexpr int kEsThreads = 256, kEsFeat = 4, kEsTpl = 3;  // positions of up to kEsTpl type pairs in registers
 template <typename T>
-__global__ void __launch_bounds__(kEsCols * kEsSlices) pg_rows_es(DevModel M, DevBatch B, const long long* d_off,
-                                                                  const T* D, const long long* s_off, const T* DS,
-                                                                  const long long* e_row, const long long* f_row,
-                                                                  const long long* s_row, T* X, long long ld) {
-    __shared__ LongSum<T> s_part[kEsSlices - 1][7][kEsCols];
+__global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D,
+                                                         const long long* s_off, const T* DS, const long long* e_row,
+                                                         const long long* f_row, const long long* s_row, T* X,
+                                                         long long ld) {
     const int s = blockIdx.x;
-    const int cl = threadIdx.x % kEsCols, slice = threadIdx.x / kEsCols;
-    const int col = blockIdx.y * kEsCols + cl;
-    const bool force = f_row[s] >= 0;
-    LongSum<T> acc[7];
-    for (int gi = B.st_atom_off[s] + slice; col < M.F && gi < B.st_atom_off[s + 1]; gi += kEsSlices) {
-        const DevType& ty = M.types[B.types[gi]];
-        int4 ci;
-        unpack_col(ty.col_pack[col], ci.x, ci.y, ci.z, ci.w);
-        if (ci.w == 0) continue;
-        const T* Di = D + d_off[gi];
-        T w0 = 1, w1 = 0, w2 = 0, e;
-        if (ci.w == 1) {
-            e = Di[ci.x];
-        } else if (ci.w == 2) {
-            w0 = Di[ci.y];
-            w1 = Di[ci.x];
-            e = Di[ci.x] * Di[ci.y];
-        } else {
-            w0 = Di[ci.y] * Di[ci.z];
-            w1 = Di[ci.x] * Di[ci.z];
-            w2 = Di[ci.x] * Di[ci.y];
-            e = Di[ci.x] * Di[ci.y] * Di[ci.z];
-        }
-        acc[0].add(e);
-        if (!force) continue;
-        const int nl = ty.n_lin;
-        for (int l = 0; l < ty.n_tpl; ++l) {  // virial vectors per type pair, by position
-            const T* ds = DS + s_off[gi] + (size_t)l * 9 * nl + 3 * (size_t)nl;
-            const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
-            const int x0 = ip[ci.x], x1 = ci.w > 1 ? ip[ci.y] : 0, x2 = ci.w > 2 ? ip[ci.z] : 0;
+    const bool force = f_row[s] >= 0 && s_row[s] >= 0;
+    const int a0 = B.st_atom_off[s], a1 = B.st_atom_off[s + 1];
+    T* xe = X + e_row[s];
+    T* xs = force ? X + s_row[s] : nullptr;
+    for (int tc = 0; tc < M.n_type; ++tc) {
+        const DevType& ty = M.types[tc];
+        const int nl = ty.n_lin, ntpl = ty.n_tpl;
+        // ---- linear columns
+        for (int kb = 0; kb < nl; kb += kEsThreads * kEsFeat) {
+            LongSum<T> acc[kEsFeat][7];
+            int kk[kEsFeat], xpos[kEsFeat][kEsTpl];
 #pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                T v = w0 * ds[(size_t)q * nl + x0];
-                if (ci.w > 1) v += w1 * ds[(size_t)q * nl + x1];
-                if (ci.w > 2) v += w2 * ds[(size_t)q * nl + x2];
-                acc[1 + q].add(-v);
+            for (int r = 0; r < kEsFeat; ++r) {
+                kk[r] = kb + threadIdx.x + r * kEsThreads;
+#pragma unroll
+                for (int l = 0; l < kEsTpl; ++l)
+                    xpos[r][l] = (kk[r] < nl && l < ntpl) ? ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + kk[r]] : 0;
+            }
+            for (int i = a0; i < a1; ++i) {
+                if (B.types[i] != tc) continue;
+                const T* Di = D + d_off[i];
+                const T* dsi = DS + s_off[i] + 3 * (size_t)nl;
+#pragma unroll
+                for (int r = 0; r < kEsFeat; ++r) {
+                    if (kk[r] >= nl) continue;
+                    acc[r][0].add(Di[kk[r]]);
+                    if (!force) continue;
+                    T v[6] = {0, 0, 0, 0, 0, 0};
+                    for (int l = 0; l < ntpl; ++l) {
+                        int x = 0;
+#pragma unroll
+                        for (int u = 0; u < kEsTpl; ++u)
+                            if (u == l) x = xpos[r][u];
+                        if (l >= kEsTpl) x = ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + kk[r]];
+                        const T* ds = dsi + (size_t)l * 9 * nl + x;
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) v[q] += ds[(size_t)q * nl];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) acc[r][1 + q].add(-v[q]);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kEsFeat; ++r) {
+                if (kk[r] >= nl) continue;
+                const int col = ty.lin_col[kk[r]];
+                if (col < 0) continue;
+                xe[(size_t)col * ld] += (T)acc[r][0].value();
+                if (force)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) xs[(size_t)col * ld + q] += (T)acc[r][1 + q].value();
             }
         }
+        // ---- product columns
+        for (int p = threadIdx.x; p < ty.n_prod; p += kEsThreads) {
+            const int col = ty.prod_col[p];
+            int k0, k1, k2, w;
+            unpack_col(ty.col_pack[col], k0, k1, k2, w);
+            LongSum<T> acc[7];
+            for (int i = a0; i < a1; ++i) {
+                if (B.types[i] != tc) continue;
+                const T* Di = D + d_off[i];
+                T w0, w1, w2 = 0, e;
+                if (w == 2) {
+                    w0 = Di[k1];
+                    w1 = Di[k0];
+                    e = Di[k0] * Di[k1];
+                } else {
+                    w0 = Di[k1] * Di[k2];
+                    w1 = Di[k0] * Di[k2];
+                    w2 = Di[k0] * Di[k1];
+                    e = Di[k0] * Di[k1] * Di[k2];
+                }
+                acc[0].add(e);
+                if (!force) continue;
+                const T* dsi = DS + s_off[i] + 3 * (size_t)nl;
+                for (int l = 0; l < ntpl; ++l) {
+                    const T* ds = dsi + (size_t)l * 9 * nl;
+                    const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
+                    const int x0 = ip[k0], x1 = ip[k1], x2 = w > 2 ? ip[k2] : 0;
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        T v = w0 * ds[(size_t)q * nl + x0] + w1 * ds[(size_t)q * nl + x1];
+                        if (w > 2) v += w2 * ds[(size_t)q * nl + x2];
+                        acc[1 + q].add(-v);
+                    }
+                }
+            }
+            xe[(size_t)col * ld] += (T)acc[0].value();
+            if (force)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) xs[(size_t)col * ld + q] += (T)acc[1 + q].value();
+        }
+        // a column shared by several centre types receives their sums type by type
+        __syncthreads();
     }
-    if (slice > 0)
-        for (int q = 0; q < 7; ++q) s_part[slice - 1][q][cl] = acc[q];
-    __syncthreads();
-    if (slice > 0 || col >= M.F) return;
-    for (int r = 0; r < kEsSlices - 1; ++r)
-        for (int q = 0; q < 7; ++q) acc[q].merge(s_part[r][q][cl]);
-    X[(size_t)col * ld + e_row[s]] = (T)acc[0].value();
-    if (force && s_row[s] >= 0)
-        for (int q = 0; q < 6; ++q) X[(size_t)col * ld + s_row[s] + q] = (T)acc[1 + q].value();
 }
 
 // ------------------------------------------------------------ prefix sums
@@ -1130,8 +1203,8 @@ template <typename T>
 void launch_rows_es(const DevModel& M, const DevBatch& B, const long long* d_off, const T* D, const long long* s_off,
                     const T* DS, const long long* e_row, const long long* f_row, const long long* s_row, T* X,
                     long long ld, cudaStream_t st) {
-    dim3 grid(B.n_st, (M.F + kEsCols - 1) / kEsCols);
-    pg_rows_es<T><<<grid, kEsCols * kEsSlices, 0, st>>>(M, B, d_off, D, s_off, DS, e_row, f_row, s_row, X, ld);
+    if (B.n_st > 0)
+        pg_rows_es<T><<<B.n_st, kEsThreads, 0, st>>>(M, B, d_off, D, s_off, DS, e_row, f_row, s_row, X, ld);
 }
 
 template void launch_anlm<double>(const DevModel&, const DevBatch&, const long long*, const int*, const double*,
