@@ -69,7 +69,7 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
     dm.max_k0 = dm.max_lin = dm.max_k0tp = 1;
     for (const auto& ft : fm.types) {
         dm.max_k0 = std::max(dm.max_k0, ft.K0);
-        dm.max_lin = std::max(dm.max_lin, ft.n_lin);
+        dm.max_lin = std::max(dm.max_lin, ft.n_pos);
         for (int tp = 0; tp < fm.n_tp; ++tp)
             dm.max_k0tp = std::max(dm.max_k0tp, ft.tp_head_off[tp + 1] - ft.tp_head_off[tp]);
     }
@@ -130,23 +130,16 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.n_prod = (int)prod.size();
         d.lin_col = (const int*)up(lin);
         d.prod_col = (const int*)up(prod);
-        std::vector<int> tnk(ft.tp_heads.size());
-        for (int tp = 0; tp < fm.n_tp; ++tp)
-            for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q) {
-                const int h = ft.tp_heads[q];
-                if (ft.head_nid[h] > 255 || ft.head_key[h] > (1 << 22))
-                    throw std::runtime_error("model too large for the packed head indices");
-                tnk[ft.tp_head_off[tp] + ft.tp_head_row[q]] = ft.head_nid[h] | (ft.head_key[h] << 8);
-            }
-        d.tp_head_nk = (const int*)up(tnk);
         d.n_groups = ft.n_groups;
+        d.n_pos = ft.n_pos;
         d.lay_size = ft.lay_size;
         d.n_tpl = (int)ft.tpl_tp.size();
-        d.lay_hpos = (const int*)up(ft.lay_hpos);
+        d.lay_key = (const int*)up(ft.lay_key);
         d.lay_grp_base = (const int*)up(ft.lay_grp_base);
         d.lay_grp_cnt = (const int*)up(ft.lay_grp_cnt);
         d.tp_perm = (const int*)up(ft.tp_perm);
         d.tp_ipos = (const int*)up(ft.tp_ipos);
+        d.tp_pos_nid = (const int*)up(ft.tp_pos_nid);
         d.tp_nnz = (const int*)up(ft.tp_nnz);
         d.tpl = (const int*)up(ft.tpl);
         d.tpl_tp = (const int*)up(ft.tpl_tp);
@@ -407,10 +400,9 @@ Model::Model(const pg_feature_params* p)
     }
 }
 
-// Per-atom storage offsets (a_nlm, features, adjoint entries) of a staged batch.
 // Per-atom storage offsets of a staged batch: a_nlm (K0), features (n_lin),
 // adjoint entries in the X-row layout (lay_size), self/virial vectors
-// (9 x n_lin per type pair of the centre type).
+// (9 x n_pos feature positions per type pair of the centre type).
 void Model::atom_offsets(const DeviceBatch& b, AtomOffsets& o) const {
     o.a_off.resize(b.n_atoms);
     o.d_off.resize(b.n_atoms);
@@ -426,7 +418,7 @@ void Model::atom_offsets(const DeviceBatch& b, AtomOffsets& o) const {
         o.a_tot += ft.K0;
         o.d_tot += ft.n_lin;
         o.g_tot += ft.lay_size;
-        o.s_tot += 9LL * ft.n_lin * (long long)ft.tpl_tp.size();
+        o.s_tot += 9LL * ft.n_pos * (long long)ft.tpl_tp.size();
     }
 }
 
@@ -435,12 +427,12 @@ size_t Model::bytes_per_atom(bool fp64, double mean_pairs) const {
     size_t mx = 0;
     for (const auto& ft : flat.types) {
         // a_nlm, features, self/virial vectors (9 per feature) and G
-        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts * (1 + 9 * ft.tpl_tp.size()) +
+        const size_t b = (size_t)ft.K0 * 16 + (size_t)ft.n_lin * ts + (size_t)ft.n_pos * ts * 9 * ft.tpl_tp.size() +
                          (size_t)ft.lay_size * 2 * ts;
         mx = std::max(mx, b);
     }
     size_t max_lin = 1;
-    for (const auto& ft : flat.types) max_lin = std::max<size_t>(max_lin, ft.n_lin);
+    for (const auto& ft : flat.types) max_lin = std::max<size_t>(max_lin, ft.n_pos);
     // per pair: index, key, FP64 and FP32 displacements, mirror, group slot, order and
     // the pair derivatives (3 per feature); X rows
     return mx + (size_t)(mean_pairs * (72.0 + 3.0 * max_lin * ts)) + (size_t)flat.n_features * 3 * ts;

@@ -68,11 +68,11 @@ struct DevType {
     int n_prod;                // columns that are products of two or three features of this type
     const int *lin_col, *prod_col;  // per feature: its linear column (-1: none); the product columns
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
-    const int* tp_head_nk;     // per gradient-tile row of a type pair (tp_head_off order): radial index | Y_lm index << 8
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
-    int n_groups, lay_size, n_tpl;
-    const int *lay_hpos, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
-    const int* tp_nnz;  // per type pair: feature positions with entries (the first ones)
+    int n_groups, lay_size, n_tpl, n_pos;  // n_pos: feature positions per type pair (host/flat_tables.h)
+    const int *lay_key, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
+    const int* tp_pos_nid;  // per type pair and position: the radial function of the feature's entries
+    const int* tp_nnz;      // per type pair: feature positions with entries (the first ones)
     // adjoint terms in X-row slot order: slot s owns terms slot_toff[s] ..
     // slot_toff[s + 1]; per term the full a ids (16 bits each, two per word in
     // x, y, z), n | conj << 8 in w, and its coefficient (T of the model; the
@@ -149,7 +149,7 @@ __device__ __forceinline__ void load_full_a(const DevType& ty, const cplx<T>* A,
 
 struct DevModel {
     int n_type, n_tp, F, n_fn_max, maxl, n_ylm, gtinv;
-    int max_k0, max_lin;  // largest K0 and n_lin (rounded up to a multiple of 4) over the centre types
+    int max_k0, max_lin;  // largest K0 and feature-position count n_pos (a multiple of 4) over the centre types
     int max_k0tp;         // largest number of heads of one type pair
     double cutoff;
     const int* type_pairs;

@@ -20,83 +20,6 @@ FlatTerm make_term(double coeff, const std::vector<int>& ids, int conj) {
     return t;
 }
 
-// Rows of the head-space gradient tile for the nh heads of one type pair.
-// The force-row contraction reads, per rank of a 32-feature group, the rows of
-// the heads that the group's entries of that rank name; row r sits in
-// shared-memory bank set r mod 8, so heads read together should have distinct
-// rows mod 8 (same head: broadcast, no conflict).  `ranks` lists the distinct
-// heads (0..nh-1) read together.  Greedy colouring (most-read heads first,
-// each to the class that least raises the ranks' largest class), then one
-// pass of pairwise swaps that lower the sum over ranks of the largest class;
-// class c gets rows c, c + 8, ...  Returns the row of each head.
-std::vector<int> colour_head_rows(int nh, const std::vector<std::vector<int>>& ranks) {
-    constexpr int kC = 8;
-    std::vector<std::vector<int>> ranks_of(nh);
-    for (size_t r = 0; r < ranks.size(); ++r)
-        for (int u : ranks[r]) ranks_of[u].push_back((int)r);
-    std::vector<std::array<int, kC>> cls(ranks.size());
-    for (auto& a : cls) a.fill(0);
-    auto largest = [&](int r) { return *std::max_element(cls[r].begin(), cls[r].end()); };
-    std::vector<int> cap(kC, 0), col(nh, 0), order(nh);
-    for (int u = 0; u < nh; ++u) {
-        cap[u % kC]++;
-        order[u] = u;
-    }
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return ranks_of[a].size() > ranks_of[b].size(); });
-    for (int u : order) {
-        long best = -1;
-        int bc = 0;
-        for (int c = 0; c < kC; ++c) {
-            if (cap[c] == 0) continue;
-            long cost = 0;
-            for (int r : ranks_of[u]) cost += (cls[r][c] + 1 > largest(r) ? 16 : 0) + cls[r][c];
-            if (best < 0 || cost < best) {
-                best = cost;
-                bc = c;
-            }
-        }
-        col[u] = bc;
-        cap[bc]--;
-        for (int r : ranks_of[u]) cls[r][bc]++;
-    }
-    auto move = [&](int u, int from, int to) {
-        for (int r : ranks_of[u]) {
-            cls[r][from]--;
-            cls[r][to]++;
-        }
-    };
-    std::vector<int> touched;
-    for (int a = 0; a < nh; ++a)
-        for (int b = a + 1; b < nh; ++b) {
-            const int ca = col[a], cb = col[b];
-            if (ca == cb || ranks_of[a].empty()) continue;
-            touched.assign(ranks_of[a].begin(), ranks_of[a].end());
-            touched.insert(touched.end(), ranks_of[b].begin(), ranks_of[b].end());
-            std::sort(touched.begin(), touched.end());
-            touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
-            long before = 0, after = 0;
-            for (int r : touched) before += largest(r);
-            move(a, ca, cb);
-            move(b, cb, ca);
-            for (int r : touched) after += largest(r);
-            if (after < before) {
-                col[a] = cb;
-                col[b] = ca;
-            } else {
-                move(a, cb, ca);
-                move(b, ca, cb);
-            }
-        }
-    std::vector<int> next(kC), row(nh);
-    for (int c = 0; c < kC; ++c) next[c] = c;
-    for (int u = 0; u < nh; ++u) {
-        row[u] = next[col[u]];
-        next[col[u]] += kC;
-    }
-    return row;
-}
-
 }  // namespace
 
 FlatModel flatten_model(const ModelTables& mt) {
@@ -273,64 +196,97 @@ FlatModel flatten_model(const ModelTables& mt) {
         // X-row entry layout by type pair (see flat_tables.h)
         {
             const int ntp = mt.n_type_pairs, nl = ft.n_lin;
-            ft.n_groups = (nl + 31) / 32;
-            std::vector<int> hpos_of(ft.K0, 0);
-            for (int tp = 0; tp < ntp; ++tp)
-                for (int q = ft.tp_head_off[tp]; q < ft.tp_head_off[tp + 1]; ++q)
-                    hpos_of[ft.tp_heads[q]] = q - ft.tp_head_off[tp];
-            ft.tp_perm.assign((size_t)ntp * nl, 0);
+            // per type pair: the key sequence of every feature, the features in
+            // layout order and the bundles (two features with equal keys, or one)
+            std::vector<std::vector<std::vector<int>>> keys(ntp, std::vector<std::vector<int>>(nl));
+            std::vector<std::vector<std::array<int, 2>>> bundles(ntp);
+            std::vector<std::vector<int>> rest(ntp);  // features without entries of tp
+            ft.n_groups = 0;
+            ft.n_pos = 0;
+            for (int tp = 0; tp < ntp; ++tp) {
+                for (int k = 0; k < nl; ++k) {
+                    const int e0 = ft.ent_tp_off[(size_t)k * (ntp + 1) + tp];
+                    const int e1 = ft.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1];
+                    for (int e = e0; e < e1; ++e) {
+                        const int h = ft.ent_head[e];
+                        if (ft.head_nid[h] != ft.head_nid[ft.ent_head[e0]])
+                            throw std::runtime_error("internal: a feature mixes radial functions within a type pair");
+                        keys[tp][k].push_back(ft.head_key[h]);
+                    }
+                }
+                const auto& kt = keys[tp];
+                std::vector<int> order(nl);
+                for (int k = 0; k < nl; ++k) order[k] = k;
+                std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                    if (kt[a].size() != kt[b].size()) return kt[a].size() > kt[b].size();
+                    return kt[a] < kt[b];
+                });
+                for (size_t q = 0; q < order.size();) {
+                    const int k = order[q];
+                    if (kt[k].empty()) {
+                        rest[tp].push_back(k);
+                        ++q;
+                    } else if (q + 1 < order.size() && kt[order[q + 1]] == kt[k]) {
+                        bundles[tp].push_back({k, order[q + 1]});
+                        q += 2;
+                    } else {
+                        bundles[tp].push_back({k, -1});
+                        ++q;
+                    }
+                }
+                const int ng = ((int)bundles[tp].size() + 31) / 32;
+                ft.n_groups = std::max(ft.n_groups, ng);
+                ft.n_pos = std::max(ft.n_pos, 64 * ng + (int)rest[tp].size());
+            }
+            ft.n_pos = std::max(4, (ft.n_pos + 3) & ~3);
+            const int np = ft.n_pos, ng = ft.n_groups;
+            ft.tp_perm.assign((size_t)ntp * np, -1);
             ft.tp_ipos.assign((size_t)ntp * nl, 0);
-            ft.lay_grp_base.assign((size_t)ntp * ft.n_groups, 0);
-            ft.lay_grp_cnt.assign((size_t)ntp * ft.n_groups, 0);
+            ft.tp_pos_nid.assign((size_t)ntp * np, 0);
+            ft.lay_grp_base.assign((size_t)ntp * ng, 0);
+            ft.lay_grp_cnt.assign((size_t)ntp * ng, 0);
             ft.tp_nnz.assign(ntp, 0);
             ft.tpl.assign(ntp, -1);
-            ft.tp_head_row.assign(ft.tp_heads.size(), 0);
             for (int tp = 0; tp < ntp; ++tp) {
                 if (ft.tp_head_off[tp + 1] > ft.tp_head_off[tp]) {
                     ft.tpl[tp] = (int)ft.tpl_tp.size();
                     ft.tpl_tp.push_back(tp);
                 }
-                auto cnt = [&](int k) {
-                    return ft.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1] - ft.ent_tp_off[(size_t)k * (ntp + 1) + tp];
+                const auto& kt = keys[tp];
+                const auto& bt = bundles[tp];
+                const int ngt = ((int)bt.size() + 31) / 32;
+                auto place = [&](int k, int x) {
+                    ft.tp_perm[(size_t)tp * np + x] = k;
+                    ft.tp_ipos[(size_t)tp * nl + k] = x;
+                    if (!kt[k].empty())
+                        ft.tp_pos_nid[(size_t)tp * np + x] =
+                            ft.head_nid[ft.ent_head[ft.ent_tp_off[(size_t)k * (ntp + 1) + tp]]];
                 };
-                std::vector<int> order(nl);
-                for (int k = 0; k < nl; ++k) order[k] = k;
-                std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt(a) > cnt(b); });
-                for (int x = 0; x < nl; ++x) {
-                    ft.tp_perm[(size_t)tp * nl + x] = order[x];
-                    ft.tp_ipos[(size_t)tp * nl + order[x]] = x;
-                    if (cnt(order[x]) > 0) ft.tp_nnz[tp] = x + 1;
+                for (size_t t = 0; t < bt.size(); ++t) {
+                    const int x = 64 * (int)(t / 32) + (int)(t % 32);
+                    place(bt[t][0], x);
+                    if (bt[t][1] >= 0) place(bt[t][1], x + 32);
                 }
-                const size_t tp_base = ft.lay_ent.size();
-                std::vector<std::vector<int>> ranks;
-                for (int g = 0; g < ft.n_groups; ++g) {
-                    const int c = cnt(order[32 * g]);
-                    ft.lay_grp_base[(size_t)tp * ft.n_groups + g] = (int)ft.lay_ent.size();
-                    ft.lay_grp_cnt[(size_t)tp * ft.n_groups + g] = c;
+                for (size_t q = 0; q < rest[tp].size(); ++q) place(rest[tp][q], 64 * ngt + (int)q);
+                ft.tp_nnz[tp] = 64 * ngt;
+                for (int g = 0; g < ngt; ++g) {
+                    const int c = (int)kt[bt[32 * g][0]].size();
+                    ft.lay_grp_base[(size_t)tp * ng + g] = (int)ft.lay_ent.size();
+                    ft.lay_grp_cnt[(size_t)tp * ng + g] = c;
                     for (int r = 0; r < c; ++r) {
-                        std::vector<int> heads;
-                        for (int l = 0; l < 32; ++l) {
-                            const int x = 32 * g + l;
-                            int e = -1;
-                            if (x < nl && r < cnt(order[x])) e = ft.ent_tp_off[(size_t)order[x] * (ntp + 1) + tp] + r;
-                            ft.lay_ent.push_back(e);
-                            ft.lay_hpos.push_back(e >= 0 ? hpos_of[ft.ent_head[e]] : 0);
-                            if (e >= 0) heads.push_back(hpos_of[ft.ent_head[e]]);
-                        }
-                        std::sort(heads.begin(), heads.end());
-                        heads.erase(std::unique(heads.begin(), heads.end()), heads.end());
-                        ranks.push_back(std::move(heads));
+                        // a zero entry names the key of lane 0's entry (same address: a broadcast)
+                        const int key0 = kt[bt[32 * g][0]][r];
+                        for (int half = 0; half < 2; ++half)
+                            for (int l = 0; l < 32; ++l) {
+                                const size_t t = 32 * (size_t)g + l;
+                                const int k = t < bt.size() ? bt[t][half] : -1;
+                                int e = -1;
+                                if (k >= 0 && r < (int)kt[k].size()) e = ft.ent_tp_off[(size_t)k * (ntp + 1) + tp] + r;
+                                const int k0 = t < bt.size() ? bt[t][0] : -1;
+                                ft.lay_ent.push_back(e);
+                                ft.lay_key.push_back((k0 >= 0 && r < (int)kt[k0].size()) ? kt[k0][r] : key0);
+                            }
                     }
-                }
-                // head -> row of the gradient tile; a zero entry reads the row of
-                // its rank's first entry (lane 0 holds the group's largest feature)
-                const int q0 = ft.tp_head_off[tp], nh = ft.tp_head_off[tp + 1] - q0;
-                const std::vector<int> row = colour_head_rows(nh, ranks);
-                for (int q = 0; q < nh; ++q) ft.tp_head_row[q0 + q] = row[q];
-                for (size_t s = tp_base; s < ft.lay_ent.size(); s += 32) {
-                    const int first = row[ft.lay_hpos[s]];
-                    for (int l = 0; l < 32; ++l)
-                        ft.lay_hpos[s + l] = ft.lay_ent[s + l] >= 0 ? row[ft.lay_hpos[s + l]] : first;
                 }
             }
             ft.lay_size = (int)ft.lay_ent.size();

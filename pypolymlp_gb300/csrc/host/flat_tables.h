@@ -55,21 +55,31 @@ struct FlatType {
     // (up to two) other features whose product weights d(col)/d(d_k); -1 = none
     std::vector<int> kcol_off, kcol_col, kcol_o1, kcol_o2;
     // X-row layout of the adjoint entries, per type pair tp of this centre
-    // type: the features are ordered by their number of entries of tp
-    // (descending; tp_perm[tp][x] is the feature at position x, tp_ipos the
-    // inverse) and taken 32 at a time (group g = positions 32g .. 32g+31);
-    // group g stores its entries rank-major: slot lay_grp_base[tp][g] + 32 r +
-    // lane holds the r-th entry of the feature at position 32g + lane
-    // (lay_ent = -1 where that feature has fewer entries: a zero entry).
-    // n_groups = ceil(n_lin / 32); lay_grp_cnt[tp][g] = entries of the group's
-    // first (largest) feature.  lay_hpos is the row of the entry's head in the
-    // per-type-pair gradient tile: tp_head_row[q] for the tp_heads entry q, rows
-    // coloured so that the heads one rank reads fall in distinct bank sets; a
-    // zero entry repeats the row of its rank's lane 0.
-    // tp_nnz[tp]: positions with entries of tp (they come first); the
-    // derivatives of the other features by a pair of tp vanish.
-    int n_groups = 0, lay_size = 0;
-    std::vector<int> lay_ent, lay_hpos, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_head_row, tp_nnz;
+    // type.  The entries of feature k by type pair tp all name one radial
+    // function, tp_pos_nid[tp][x] at the feature's position x, so the force
+    // derivative by a pair d of tp factors into
+    //   dd_k/dd = f_n(r) sum_e Re(G_e grad Y_e) + f_n'(r) d/r sum_e Re(G_e Y_e),
+    // sums over the Y_lm keys of the entries.  The features with entries of tp
+    // are ordered by their number of entries (descending), then by their key
+    // sequence, and taken two at a time into bundles of two features with the
+    // same key sequence (or one, when the next feature's keys differ), so that
+    // one table row of a key serves both.  Bundle t = 32 g + l sits in group g,
+    // lane l: its features at positions 64 g + l and 64 g + 32 + l (holes,
+    // tp_perm = -1, where a bundle has one feature or the group is not full).
+    // The features without entries of tp follow at 64 n_g(tp) onwards, and
+    // positions run to n_pos (all type pairs; a multiple of 4); tp_perm[tp][x]
+    // is the feature at position x, tp_ipos[tp][k] the position of feature k.
+    // Group g stores its entries rank-major: slots lay_grp_base[tp][g] + 64 r
+    // + l and + 32 + l hold the r-th entries of the two features of lane l
+    // (lay_ent = -1 for a hole or a feature with fewer entries: a zero entry).
+    // n_groups = the most groups of any type pair; lay_grp_cnt[tp][g] = entries
+    // of the group's first (largest) feature, 0 for groups past the last.
+    // lay_key is the Y_lm key of the lane's entries of the rank (both slots); a
+    // lane past its feature's entries repeats the key of lane 0, so the lanes
+    // of a rank read few distinct keys.  tp_nnz[tp] = 64 n_g(tp): the positions
+    // that can hold derivatives of tp; the others' derivatives vanish.
+    int n_groups = 0, lay_size = 0, n_pos = 0;
+    std::vector<int> lay_ent, lay_key, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_pos_nid, tp_nnz;
     // type pairs with heads for this centre type: local index or -1, and back
     std::vector<int> tpl, tpl_tp;
 };

@@ -464,14 +464,20 @@ __global__ void pg_nb_mirror(int n_atoms, const long long* nb_off, const int* nb
 
 // Stage A.  Block per centre atom i of a force structure; its pairs are taken
 // in chunks of up to NW pairs of one type pair (pairs ordered by type pair,
-// stably, so the images of a neighbour stay consecutive).  Per chunk, warp w
-// builds the basis of pair w and its head-space gradient
-//   H[c][u][w] = d phi_h(d_w) / dd_w,c    (h the u-th head of the type pair),
-// then thread k contracts the adjoint entries of feature k with all pairs of
-// the chunk at once:  dd_k/dd_w,c = sum_e Re(G_e(i) . H[c][u_e][w]).
-// The entries of the centre are stored by type pair, features ordered by
-// their number of entries and interleaved 32 at a time (pg_features_adjoint),
-// so warp = 32 feature positions reads them coalesced with equal loop lengths.
+// stably, so the images of a neighbour stay consecutive).  The entries of
+// feature k by a type pair share one radial function n (host/flat_tables.h),
+// so with phi_h(d) = f_n(r) Y_lm(d/r) the derivative by pair p factors into
+//   dd_k/dd_p,c = f_n(r_p) S_k,c(p) + f_n'(r_p) (d_p,c / r_p) T_k(p),
+//   T_k(p) = sum_e Re(G_e(i) Y_(key e)(p)),  S_k,c(p) = sum_e Re(G_e(i) dY_(key e)(p)/dd_c).
+// Per chunk, warp w builds the basis of pair w into a table of its Y_lm and
+// their gradients (8 values per key) and of its radial functions
+// (f_n, f_n' d_x/r, f_n' d_y/r, f_n' d_z/r); then thread k runs over the
+// entries of feature k once for all pairs of the chunk, reading the table
+// row of the entry's key.  The entries of the centre are stored by type
+// pair, features ordered by their number of entries and then by their key
+// sequence and interleaved 32 at a time (pg_features_adjoint), so warp = 32
+// feature positions reads them coalesced with equal loop lengths and most
+// ranks name one key for all 32 lanes: a shared-memory broadcast.
 // The images of one neighbour j are summed and stored once, at the group slot
 // (the first entry of i in j's list), indexed by feature position, so stage B
 // reads one vector per (centre, target).  The centre's DS vectors are
@@ -479,37 +485,44 @@ __global__ void pg_nb_mirror(int n_atoms, const long long* nb_off, const int* nb
 //   DS[i][tp][c][x]   = sum_{p of tp, j_p != i} dd_k/dd_p,c         (self rows)
 //   DS[i][tp][3+q][x] = sum_{p of tp} d_p,b(q) dd_k/dd_p,a(q)       (virial)
 // with k = perm_tp[x] and (a, b)(q) = (x,x) (y,y) (z,z) (x,y) (y,z) (z,x).
-// H rows (8 complex values: the pairs of a chunk) are read by lanes at random
-// head positions u, so the 16-byte pieces of a row are XOR-swizzled by u to
-// spread them over the shared-memory banks.
-template <typename T>
-__device__ __forceinline__ int h_pos(int u, int w) {
-    return w ^ (u & 7);  // one complex<double> per 16 bytes
+
+// Eight consecutive values of a 16-byte-aligned shared-memory row.
+__device__ __forceinline__ void load_row8(const float* p, float (&v)[8]) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+    v[4] = b.x;
+    v[5] = b.y;
+    v[6] = b.z;
+    v[7] = b.w;
 }
-template <>
-__device__ __forceinline__ int h_pos<float>(int u, int w) {
-    // two complex<float> per 16 bytes; a 64-byte row is half a bank row, so
-    // bit 0 of u picks the half and bits 1-2 the piece: 8 positions in all
-    return (((w >> 1) ^ ((u >> 1) & 3)) << 1) | (w & 1);
-}
-template <typename T>
-__device__ __forceinline__ void load_h8(const cplx<T>* h, int u, cplx<T> (&v)[8]) {
-#pragma unroll
-    for (int w = 0; w < 8; ++w) v[w] = h[h_pos<T>(u, w)];
-}
-template <>
-__device__ __forceinline__ void load_h8<float>(const cplx<float>* h, int u, cplx<float> (&v)[8]) {
-    const float4* p = reinterpret_cast<const float4*>(h);
+__device__ __forceinline__ void load_row8(const double* p, double (&v)[8]) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float4 x = p[q ^ ((u >> 1) & 3)];
-        v[2 * q] = {x.x, x.y};
-        v[2 * q + 1] = {x.z, x.w};
+        const double2 a = reinterpret_cast<const double2*>(p)[q];
+        v[2 * q] = a.x;
+        v[2 * q + 1] = a.y;
     }
+}
+__device__ __forceinline__ void load_row4(const float* p, float (&v)[4]) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+}
+__device__ __forceinline__ void load_row4(const double* p, double (&v)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off,
+__global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off,
                                                               const int* nb_j, const double* nb_d,
                                                               const long long* gslot, const long long* s_off,
                                                               const long long* g_off, const cplx<T>* G,
@@ -518,17 +531,18 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
     static_assert(NW == 8, "the chunk width is 8 pairs");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_wcnt[NW], s_tpoff[kMaxTypePairs + 1];
-    __shared__ int s_q[NW], s_flag[NW];  // pair index; ok | self << 1 | flush << 2 | fresh << 3
+    __shared__ int s_flag[NW];  // ok | self << 1 | flush << 2 | fresh << 3 | first << 4
     __shared__ long long s_slot[NW];
     const int i = blockIdx.x;
     if (f_row[B.atom_st[i]] < 0) return;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nl = ty.n_lin, NL = M.max_lin, HT = M.max_k0tp;
+    const int nl = ty.n_lin, NL = M.max_lin, NY = M.n_ylm, NF = M.n_fn_max;
     const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    cplx<T>* H = reinterpret_cast<cplx<T>*>(smem_raw);  // [3][HT][NW]
-    T* sb = reinterpret_cast<T*>(H + (size_t)3 * HT * NW);
+    T* tab = reinterpret_cast<T*>(smem_raw);  // [NW][NY][8]: Y, dY/dx, dY/dy, dY/dz (re, im)
+    T* rad = tab + (size_t)NW * NY * 8;       // [NW][NF][4]: f, f' x/r, f' y/r, f' z/r
+    T* sb = rad + (size_t)NW * NF * 4;
     T* s_tab = sb + slot * NW;
     T* sd = reinterpret_cast<T*>(
         (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));  // [NW][3]
@@ -558,26 +572,31 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
     }
     if (threadIdx.x == 0) s_tpoff[M.n_tp] = cursor;
     __syncthreads();
-    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
+    const YlmTab<T> ytab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     const cplx<T>* Gi = G + g_off[i];
-    T* dsa = DS + s_off[i];  // [type pair of the centre type][9][n_lin], feature positions of that pair
-    for (int q = threadIdx.x; q < 9 * nl * ty.n_tpl; q += blockDim.x) dsa[q] = (T)0;
+    const int npos = ty.n_pos;
+    T* dsa = DS + s_off[i];  // [type pair of the centre type][9][n_pos], feature positions of that pair
+    for (int q = threadIdx.x; q < 9 * npos * ty.n_tpl; q += blockDim.x) dsa[q] = (T)0;
     for (int tp = 0; tp < M.n_tp; ++tp) {
         const int r_end = s_tpoff[tp + 1];
-        const int q0 = ty.tp_head_off[tp], nh = ty.tp_head_off[tp + 1] - q0;
+        if (ty.tpl[tp] < 0 || r_end == s_tpoff[tp]) continue;  // no heads of tp: zero derivatives
+        const int nfn = M.tp_nfn[tp];
+        const int* pos_nid = ty.tp_pos_nid + (size_t)tp * npos;
         for (int r0 = s_tpoff[tp]; r0 < r_end; r0 += NW) {
             const int n = min(NW, r_end - r0);
-            // ---- bases and head-space gradients of the chunk
+            // ---- basis table of pair w = warp
+            T* tw = tab + (size_t)warp * NY * 8;
+            T* rw = rad + (size_t)warp * NF * 4;
+            bool ok = false;
             if (warp < n) {
                 const long long q = p0 + ord[r0 + warp];
                 T dx, dy, dz, dis;
-                const bool ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
+                ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
                 const int j = nb_j[q];
                 if (lane == 0) {
                     sd[3 * warp] = dx;
                     sd[3 * warp + 1] = dy;
                     sd[3 * warp + 2] = dz;
-                    s_q[warp] = (int)(q - p0);
                     const bool first = q == p0 || nb_j[q - 1] != j;
                     const bool last = q + 1 == p1 || nb_j[q + 1] != j;
                     s_flag[warp] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (last ? 4 : 0) | (first ? 16 : 0);
@@ -587,7 +606,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                     BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
                     warp_radial<T, true>(M, tp, dis, bv, lane);
                     if (M.gtinv) {
-                        warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
+                        warp_ylm<T, true>(M.maxl, M.n_ylm, ytab, dx, dy, dz, dis, bv, lane);
                     } else if (lane == 0) {
                         bv.Y[0] = {(T)1, (T)0};
                         bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
@@ -595,24 +614,33 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                     __syncwarp();
                     const T invr = (T)1 / dis;
                     const T ux = dx * invr, uy = dy * invr, uz = dz * invr;
-                    for (int u = lane; u < nh; u += 32) {
-                        const int nk = ty.tp_head_nk[q0 + u];
-                        const int nid = nk & 0xff, key = nk >> 8;
-                        const T f = bv.fn[nid], fd = bv.fnd[nid];
-                        const cplx<T> y = bv.Y[key];
-                        const cplx<T> yx = bv.dY[key], yy = bv.dY[M.n_ylm + key], yz = bv.dY[2 * M.n_ylm + key];
-                        const int hw = h_pos<T>(u, warp);
-                        H[((size_t)0 * HT + u) * NW + hw] = {f * yx.re + fd * ux * y.re, f * yx.im + fd * ux * y.im};
-                        H[((size_t)1 * HT + u) * NW + hw] = {f * yy.re + fd * uy * y.re, f * yy.im + fd * uy * y.im};
-                        H[((size_t)2 * HT + u) * NW + hw] = {f * yz.re + fd * uz * y.re, f * yz.im + fd * uz * y.im};
+                    for (int u = lane; u < nfn; u += 32) {
+                        const T f = bv.fn[u], fd = bv.fnd[u];
+                        T* o = rw + 4 * u;
+                        o[0] = f;
+                        o[1] = fd * ux;
+                        o[2] = fd * uy;
+                        o[3] = fd * uz;
                     }
-                } else {
-                    for (int u = lane; u < nh; u += 32)
-                        for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + h_pos<T>(u, warp)] = {(T)0, (T)0};
+                    const int ny = M.gtinv ? NY : 1;
+                    for (int u = lane; u < ny; u += 32) {
+                        const cplx<T> y = bv.Y[u], yx = bv.dY[u], yy = bv.dY[NY + u], yz = bv.dY[2 * NY + u];
+                        T* o = tw + 8 * u;
+                        o[0] = y.re;
+                        o[1] = y.im;
+                        o[2] = yx.re;
+                        o[3] = yx.im;
+                        o[4] = yy.re;
+                        o[5] = yy.im;
+                        o[6] = yz.re;
+                        o[7] = yz.im;
+                    }
                 }
-            } else {
-                for (int u = lane; u < nh; u += 32)
-                    for (int c = 0; c < 3; ++c) H[((size_t)c * HT + u) * NW + h_pos<T>(u, warp)] = {(T)0, (T)0};
+            }
+            if (!ok) {
+                // absent or out-of-range pair: a zero table (its derivatives vanish)
+                for (int u = lane; u < NY * 8; u += 32) tw[u] = (T)0;
+                for (int u = lane; u < nfn * 4; u += 32) rw[u] = (T)0;
             }
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -628,36 +656,36 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                 }
             }
             __syncthreads();
-            // ---- contraction of the chunk: warp = group of 32 feature positions,
-            // lane = position; the group's entries are read rank-major (coalesced)
+            // ---- contraction of the chunk: warp = group of 32 bundles, lane =
+            // bundle (two features with the same keys, positions xa and xa + 32);
+            // the group's entries are read rank-major (coalesced) and one table
+            // row per pair and rank serves both features
             {
-                // (a type pair without heads for this centre type contributes zeros and keeps no DS)
-                T* ds = ty.tpl[tp] >= 0 ? dsa + (size_t)ty.tpl[tp] * 9 * nl : nullptr;
+                T* ds = dsa + (size_t)ty.tpl[tp] * 9 * npos;
                 const int ng = ty.n_groups;
                 for (int grp = warp; grp < ng; grp += NW) {
-                    const int x = 32 * grp + lane;
                     const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
-                    // positions without entries of tp: zero derivatives, nothing
+                    // groups past the last of tp: no entries, zero derivatives, nothing
                     // stored (stage B reads positions below tp_nnz only)
                     if (cnt == 0) continue;
-                    T acc[NW][3];
+                    // per pair and feature: T, S_x, S_y, S_z
+                    T acc[NW][2][4];
 #pragma unroll
-                    for (int w = 0; w < NW; ++w) acc[w][0] = acc[w][1] = acc[w][2] = (T)0;
-                    // this position's DS sums so far, loaded before the contraction hides their latency
-                    T sv[9];
+                    for (int w = 0; w < NW; ++w)
 #pragma unroll
-                    for (int v = 0; v < 9; ++v) sv[v] = (ds && x < nl) ? ds[(size_t)v * nl + x] : (T)0;
+                        for (int f = 0; f < 2; ++f) acc[w][f][0] = acc[w][f][1] = acc[w][f][2] = acc[w][f][3] = (T)0;
                     // entries are loaded kPrefetch ranks ahead of the one contracted
-                    constexpr int kPrefetch = 4;
-                    cplx<T> gq[kPrefetch];
-                    int uq[kPrefetch];
+                    constexpr int kPrefetch = 2;
+                    cplx<T> ga[kPrefetch], gb[kPrefetch];
+                    int kq[kPrefetch];
 #pragma unroll
                     for (int s = 0; s < kPrefetch; ++s) {
-                        gq[s] = {(T)0, (T)0};
-                        uq[s] = 0;
+                        ga[s] = gb[s] = {(T)0, (T)0};
+                        kq[s] = 0;
                         if (s < cnt) {
-                            gq[s] = Gi[base + 32 * s + lane];
-                            uq[s] = ty.lay_hpos[base + 32 * s + lane];
+                            ga[s] = Gi[base + 64 * s + lane];
+                            gb[s] = Gi[base + 64 * s + 32 + lane];
+                            kq[s] = ty.lay_key[base + 64 * s + lane];
                         }
                     }
                     for (int r0 = 0; r0 < cnt; r0 += kPrefetch) {
@@ -665,63 +693,79 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows_pairs(DevModel M, DevBat
                         for (int s = 0; s < kPrefetch; ++s) {
                             const int r = r0 + s;
                             if (r >= cnt) break;
-                            const cplx<T> g = gq[s];
-                            const int u = uq[s];
+                            const T are = ga[s].re, aim = -ga[s].im, bre = gb[s].re, bim = -gb[s].im;
+                            const T* row = tab + 8 * kq[s];
                             if (r + kPrefetch < cnt) {
-                                const int sl = base + 32 * (r + kPrefetch) + lane;
-                                gq[s] = Gi[sl];
-                                uq[s] = ty.lay_hpos[sl];
+                                const int sl = base + 64 * (r + kPrefetch) + lane;
+                                ga[s] = Gi[sl];
+                                gb[s] = Gi[sl + 32];
+                                kq[s] = ty.lay_key[sl];
                             }
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) {
-                                cplx<T> h[8];
-                                load_h8<T>(H + ((size_t)c * HT + u) * NW, u, h);
+                            for (int w = 0; w < NW; ++w) {
+                                T v[8];
+                                load_row8(row + (size_t)w * NY * 8, v);
 #pragma unroll
-                                for (int w = 0; w < NW; ++w) acc[w][c] += g.re * h[w].re - g.im * h[w].im;
+                                for (int c = 0; c < 4; ++c) {
+                                    acc[w][0][c] = fma(aim, v[2 * c + 1], fma(are, v[2 * c], acc[w][0][c]));
+                                    acc[w][1][c] = fma(bim, v[2 * c + 1], fma(bre, v[2 * c], acc[w][1][c]));
+                                }
                             }
                         }
                     }
-                    if (x >= nl) continue;
-                    T run0 = 0, run1 = 0, run2 = 0;
+                    // ---- per feature of the bundle: derivatives, image sums, DS sums
 #pragma unroll
-                    for (int w = 0; w < NW; ++w) {
-                        if (w >= n) break;
-                        const int fl = s_flag[w];
-                        const T a0 = acc[w][0], a1 = acc[w][1], a2 = acc[w][2];
-                        if (fl & 1) {
-                            const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
-                            if (!(fl & 2)) {
-                                sv[0] += a0;
-                                sv[1] += a1;
-                                sv[2] += a2;
+                    for (int f = 0; f < 2; ++f) {
+                        const int x = 64 * grp + 32 * f + lane;
+                        const int nid = pos_nid[x];
+                        T sv[9];
+#pragma unroll
+                        for (int v = 0; v < 9; ++v) sv[v] = ds[(size_t)v * npos + x];
+                        T run0 = 0, run1 = 0, run2 = 0;
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) {
+                            if (w >= n) break;
+                            const int fl = s_flag[w];
+                            T rf[4];
+                            load_row4(rad + ((size_t)w * NF + nid) * 4, rf);
+                            const T tk = acc[w][f][0];
+                            const T a0 = fma(rf[0], acc[w][f][1], rf[1] * tk);
+                            const T a1 = fma(rf[0], acc[w][f][2], rf[2] * tk);
+                            const T a2 = fma(rf[0], acc[w][f][3], rf[3] * tk);
+                            if (fl & 1) {
+                                const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
+                                if (!(fl & 2)) {
+                                    sv[0] += a0;
+                                    sv[1] += a1;
+                                    sv[2] += a2;
+                                }
+                                sv[3] = fma(dx, a0, sv[3]);
+                                sv[4] = fma(dy, a1, sv[4]);
+                                sv[5] = fma(dz, a2, sv[5]);
+                                sv[6] = fma(dy, a0, sv[6]);
+                                sv[7] = fma(dz, a1, sv[7]);
+                                sv[8] = fma(dx, a2, sv[8]);
                             }
-                            sv[3] += dx * a0;
-                            sv[4] += dy * a1;
-                            sv[5] += dz * a2;
-                            sv[6] += dy * a0;
-                            sv[7] += dz * a1;
-                            sv[8] += dx * a2;
-                        }
-                        run0 += a0;
-                        run1 += a1;
-                        run2 += a2;
-                        if (fl & 4) {
-                            T* o = Dp + (size_t)s_slot[w] * 3 * NL + x;
-                            if (fl & 8) {
-                                o[0] = run0;
-                                o[NL] = run1;
-                                o[2 * NL] = run2;
-                            } else {
-                                o[0] += run0;
-                                o[NL] += run1;
-                                o[2 * NL] += run2;
+                            run0 += a0;
+                            run1 += a1;
+                            run2 += a2;
+                            if (fl & 4) {
+                                T* o = Dp + (size_t)s_slot[w] * 3 * NL + x;
+                                if (fl & 8) {
+                                    o[0] = run0;
+                                    o[NL] = run1;
+                                    o[2 * NL] = run2;
+                                } else {
+                                    o[0] += run0;
+                                    o[NL] += run1;
+                                    o[2 * NL] += run2;
+                                }
+                                run0 = run1 = run2 = 0;
                             }
-                            run0 = run1 = run2 = 0;
                         }
+#pragma unroll
+                        for (int v = 0; v < 9; ++v) ds[(size_t)v * npos + x] = sv[v];
                     }
-                    if (ds)
-#pragma unroll
-                        for (int v = 0; v < 9; ++v) ds[(size_t)v * nl + x] = sv[v];
                 }
             }
             __syncthreads();
@@ -832,7 +876,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
         const DevType& ty = M.types[tc];
         const int nl = ty.n_lin;
         const int tp = M.type_pairs[tc * M.n_type + tj];
-        const int* perm = ty.tp_perm + (size_t)tp * nl;
+        const int* perm = ty.tp_perm + (size_t)tp * ty.n_pos;
         const int* ipos = ty.tp_ipos + (size_t)tp * nl;
         const int nnz = ty.tp_nnz[tp];  // the group vectors hold positions below nnz; the rest vanish
         if (nnz == 0) continue;
@@ -891,7 +935,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
                     const int x = xb + m;
-                    if (x >= nnz) continue;
+                    if (x >= nnz || perm[x] < 0) continue;  // past the positions with data, or a hole
                     const int col = ty.lin_col[perm[x]];
                     if (col < 0) continue;
                     T* o = X + (size_t)col * ld + r0;
@@ -926,7 +970,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     }
     // self rows: the target as a centre (type tj), its DS self vectors (per type pair, by position)
     const DevType& ty = M.types[tj];
-    const int nl = ty.n_lin;
+    const int nl = ty.n_lin, npos = ty.n_pos;
     const T* Di = D + d_off[gj];
     const T* dsa = DS + s_off[gj];
     for (int k = threadIdx.x; k < nl; k += blockDim.x) {
@@ -934,11 +978,11 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
         if (col < 0) continue;
         T v0 = 0, v1 = 0, v2 = 0;
         for (int l = 0; l < ty.n_tpl; ++l) {
-            const T* ds = dsa + (size_t)l * 9 * nl;
+            const T* ds = dsa + (size_t)l * 9 * npos;
             const int x = ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + k];
             v0 += ds[x];
-            v1 += ds[nl + x];
-            v2 += ds[2 * nl + x];
+            v1 += ds[npos + x];
+            v2 += ds[2 * npos + x];
         }
         T* o = X + (size_t)col * ld + r0;
         o[0] += v0;
@@ -961,13 +1005,13 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
         }
         T v[3] = {0, 0, 0};
         for (int l = 0; l < ty.n_tpl; ++l) {
-            const T* ds = dsa + (size_t)l * 9 * nl;
+            const T* ds = dsa + (size_t)l * 9 * npos;
             const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
             const int x0 = ip[k0], x1 = ip[k1], x2 = w > 2 ? ip[k2] : 0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                v[c] += w0 * ds[(size_t)c * nl + x0] + w1 * ds[(size_t)c * nl + x1];
-                if (w > 2) v[c] += w2 * ds[(size_t)c * nl + x2];
+                v[c] += w0 * ds[(size_t)c * npos + x0] + w1 * ds[(size_t)c * npos + x1];
+                if (w > 2) v[c] += w2 * ds[(size_t)c * npos + x2];
             }
         }
         T* o = X + (size_t)col * ld + r0;
@@ -1002,7 +1046,7 @@ __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B,
     T* xs = force ? X + s_row[s] : nullptr;
     for (int tc = 0; tc < M.n_type; ++tc) {
         const DevType& ty = M.types[tc];
-        const int nl = ty.n_lin, ntpl = ty.n_tpl;
+        const int nl = ty.n_lin, ntpl = ty.n_tpl, npos = ty.n_pos;
         // ---- linear columns
         for (int kb = 0; kb < nl; kb += kEsThreads * kEsFeat) {
             LongSum<T> acc[kEsFeat][7];
@@ -1017,7 +1061,7 @@ __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B,
             for (int i = a0; i < a1; ++i) {
                 if (B.types[i] != tc) continue;
                 const T* Di = D + d_off[i];
-                const T* dsi = DS + s_off[i] + 3 * (size_t)nl;
+                const T* dsi = DS + s_off[i] + 3 * (size_t)npos;
 #pragma unroll
                 for (int r = 0; r < kEsFeat; ++r) {
                     if (kk[r] >= nl) continue;
@@ -1030,9 +1074,9 @@ __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B,
                         for (int u = 0; u < kEsTpl; ++u)
                             if (u == l) x = xpos[r][u];
                         if (l >= kEsTpl) x = ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + kk[r]];
-                        const T* ds = dsi + (size_t)l * 9 * nl + x;
+                        const T* ds = dsi + (size_t)l * 9 * npos + x;
 #pragma unroll
-                        for (int q = 0; q < 6; ++q) v[q] += ds[(size_t)q * nl];
+                        for (int q = 0; q < 6; ++q) v[q] += ds[(size_t)q * npos];
                     }
 #pragma unroll
                     for (int q = 0; q < 6; ++q) acc[r][1 + q].add(-v[q]);
@@ -1071,15 +1115,15 @@ __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B,
                 }
                 acc[0].add(e);
                 if (!force) continue;
-                const T* dsi = DS + s_off[i] + 3 * (size_t)nl;
+                const T* dsi = DS + s_off[i] + 3 * (size_t)npos;
                 for (int l = 0; l < ntpl; ++l) {
-                    const T* ds = dsi + (size_t)l * 9 * nl;
+                    const T* ds = dsi + (size_t)l * 9 * npos;
                     const int* ip = ty.tp_ipos + (size_t)ty.tpl_tp[l] * nl;
                     const int x0 = ip[k0], x1 = ip[k1], x2 = w > 2 ? ip[k2] : 0;
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
-                        T v = w0 * ds[(size_t)q * nl + x0] + w1 * ds[(size_t)q * nl + x1];
-                        if (w > 2) v += w2 * ds[(size_t)q * nl + x2];
+                        T v = w0 * ds[(size_t)q * npos + x0] + w1 * ds[(size_t)q * npos + x1];
+                        if (w > 2) v += w2 * ds[(size_t)q * npos + x2];
                         acc[1 + q].add(-v);
                     }
                 }
@@ -1171,8 +1215,8 @@ size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64) {
     const int nw = kRowsThreads / 32;
     const size_t slot = fp64 ? basis_slot_elems<double>(M.n_fn_max, M.n_ylm, M.maxl)
                              : basis_slot_elems<float>(M.n_fn_max, M.n_ylm, M.maxl);
-    return (size_t)3 * M.max_k0tp * nw * 2 * ts + slot * nw * ts + (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts +
-           16 + (size_t)3 * nw * ts + 16;
+    return (size_t)nw * M.n_ylm * 8 * ts + (size_t)nw * M.n_fn_max * 4 * ts + slot * nw * ts +
+           (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts + 16 + (size_t)3 * nw * ts + 16;
 }
 
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,

@@ -1,100 +1,143 @@
 // Invariants of the host-built X-row layout tables (flat_tables.cpp), checked on
-// the CPU by tests/test_layout_tables.py: the gradient-tile rows of each type
-// pair are a permutation, entries name the row of their head, zero entries
-// repeat their rank's lane-0 row, the positions with entries of a type pair come
-// first (tp_nnz of them), and the colouring does not raise the bank-set load of
-// a rank above the uncoloured order.  Returns 0 and a summary, or 1 and the
-// first violation, in msg.
-#include <algorithm>
+// the CPU by tests/test_layout_tables.py: tp_perm and tp_ipos are inverse (holes
+// aside); the features with entries of a type pair sit below tp_nnz, in bundles
+// (positions 64g + l and 64g + 32 + l) of equal key sequences, with entry counts
+// non-increasing in bundle order; all entries of a feature by one type pair name
+// one radial function, tp_pos_nid at its position; slots hold the r-th entries
+// of their features and name the key of lane l's first feature, or lane 0's
+// past its entries; the slots cover every entry once; and the ranks read few
+// distinct keys (the mean over ranks is reported and bounded by 4).  Returns 0
+// and a summary, or 1 and the first violation, in msg.
 #include <cstdio>
-#include <map>
 #include <set>
 #include <vector>
 
 #include "host/flat_tables.h"
 #include "host/params.h"
 
-namespace {
-
-// largest number of distinct rows of one bank set (row mod 8) among `rows`
-int bank_load(const std::vector<int>& rows) {
-    std::map<int, std::set<int>> cls;
-    for (int r : rows) cls[r % 8].insert(r);
-    int m = 0;
-    for (const auto& kv : cls) m = std::max(m, (int)kv.second.size());
-    return m;
-}
-
-}  // namespace
-
 extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
     using namespace pg;
     const FlatModel fm = flatten_model(build_model_tables(feature_params_from_abi(p)));
     const int ntp = fm.n_tp;
-    long coloured = 0, plain = 0, ranks = 0;
+    long ranks = 0, distinct = 0, slots = 0, entries = 0;
     for (size_t t = 0; t < fm.types.size(); ++t) {
         const FlatType& ft = fm.types[t];
-        const int nl = ft.n_lin, ng = ft.n_groups;
+        const int nl = ft.n_lin, ng = ft.n_groups, np = ft.n_pos;
+        if (np < nl || np % 4) {
+            snprintf(msg, n_msg, "type %zu: n_pos %d for %d features", t, np, nl);
+            return 1;
+        }
+        std::vector<int> seen(ft.ent_head.size(), 0);
         for (int tp = 0; tp < ntp; ++tp) {
-            const int q0 = ft.tp_head_off[tp], nh = ft.tp_head_off[tp + 1] - q0;
-            std::vector<int> pos_of(ft.K0, -1), row_of(ft.K0, -1), seen(nh, 0);
-            for (int q = 0; q < nh; ++q) {
-                const int r = ft.tp_head_row[q0 + q];
-                if (r < 0 || r >= nh || seen[r]++) {
-                    snprintf(msg, n_msg, "type %zu tp %d: head rows are not a permutation", t, tp);
-                    return 1;
-                }
-                pos_of[ft.tp_heads[q0 + q]] = q;
-                row_of[ft.tp_heads[q0 + q]] = r;
-            }
-            auto cnt = [&](int k) {
-                return ft.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1] - ft.ent_tp_off[(size_t)k * (ntp + 1) + tp];
-            };
-            int nnz = 0;
-            for (int x = 0; x < nl; ++x)
-                if (cnt(ft.tp_perm[(size_t)tp * nl + x]) > 0) nnz = x + 1;
-            for (int x = 0; x < nnz; ++x)
-                if (cnt(ft.tp_perm[(size_t)tp * nl + x]) == 0) {
-                    snprintf(msg, n_msg, "type %zu tp %d: a position without entries before the last with", t, tp);
-                    return 1;
-                }
-            if (nnz != ft.tp_nnz[tp]) {
-                snprintf(msg, n_msg, "type %zu tp %d: tp_nnz %d, expected %d", t, tp, ft.tp_nnz[tp], nnz);
+            auto e0 = [&](int k) { return ft.ent_tp_off[(size_t)k * (ntp + 1) + tp]; };
+            auto cnt = [&](int k) { return k < 0 ? 0 : ft.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1] - e0(k); };
+            auto key = [&](int k, int r) { return ft.head_key[ft.ent_head[e0(k) + r]]; };
+            const int* perm = ft.tp_perm.data() + (size_t)tp * np;
+            const int nnz = ft.tp_nnz[tp];
+            if (nnz % 64 || nnz > np) {
+                snprintf(msg, n_msg, "type %zu tp %d: tp_nnz %d", t, tp, nnz);
                 return 1;
             }
-            for (int g = 0; g < ng; ++g) {
-                const int base = ft.lay_grp_base[(size_t)tp * ng + g], c = ft.lay_grp_cnt[(size_t)tp * ng + g];
-                for (int r = 0; r < c; ++r) {
-                    std::vector<int> rows_c, rows_p;
-                    const int s0 = base + 32 * r;
-                    if (ft.lay_ent[s0] < 0) {
-                        snprintf(msg, n_msg, "type %zu tp %d group %d rank %d: lane 0 holds no entry", t, tp, g, r);
+            std::vector<int> hits(nl, 0);
+            for (int x = 0; x < np; ++x) {
+                const int k = perm[x];
+                if (k < 0) continue;
+                if (k >= nl || hits[k]++ || ft.tp_ipos[(size_t)tp * nl + k] != x) {
+                    snprintf(msg, n_msg, "type %zu tp %d: position %d and feature %d disagree", t, tp, x, k);
+                    return 1;
+                }
+                if ((cnt(k) > 0) != (x < nnz)) {
+                    snprintf(msg, n_msg, "type %zu tp %d: feature %d with %d entries at position %d (nnz %d)", t,
+                             tp, k, cnt(k), x, nnz);
+                    return 1;
+                }
+                for (int e = e0(k); e < e0(k) + cnt(k); ++e)
+                    if (ft.head_nid[ft.ent_head[e]] != ft.tp_pos_nid[(size_t)tp * np + x]) {
+                        snprintf(msg, n_msg, "type %zu tp %d feature %d: entry %d names radial %d, position %d", t,
+                                 tp, k, e, ft.head_nid[ft.ent_head[e]], ft.tp_pos_nid[(size_t)tp * np + x]);
                         return 1;
                     }
-                    for (int l = 0; l < 32; ++l) {
-                        const int e = ft.lay_ent[s0 + l];
-                        const int want = e >= 0 ? row_of[ft.ent_head[e]] : ft.lay_hpos[s0];
-                        if (ft.lay_hpos[s0 + l] != want) {
-                            snprintf(msg, n_msg, "type %zu tp %d group %d rank %d lane %d: row %d, expected %d", t,
-                                     tp, g, r, l, ft.lay_hpos[s0 + l], want);
+            }
+            for (int k = 0; k < nl; ++k)
+                if (hits[k] != 1) {
+                    snprintf(msg, n_msg, "type %zu tp %d: feature %d at %d positions", t, tp, k, hits[k]);
+                    return 1;
+                }
+            int prev = 1 << 30;
+            for (int g = 0; g < ng; ++g) {
+                const int base = ft.lay_grp_base[(size_t)tp * ng + g], c = ft.lay_grp_cnt[(size_t)tp * ng + g];
+                if (64 * g >= nnz) {
+                    if (c != 0) {
+                        snprintf(msg, n_msg, "type %zu tp %d group %d past tp_nnz has entries", t, tp, g);
+                        return 1;
+                    }
+                    continue;
+                }
+                if (c != cnt(perm[64 * g])) {
+                    snprintf(msg, n_msg, "type %zu tp %d group %d: count %d is not lane 0's", t, tp, g, c);
+                    return 1;
+                }
+                for (int l = 0; l < 32; ++l) {
+                    const int ka = perm[64 * g + l], kb = perm[64 * g + 32 + l];
+                    if (kb >= 0 && (ka < 0 || cnt(ka) != cnt(kb))) {
+                        snprintf(msg, n_msg, "type %zu tp %d group %d lane %d: bundle partner unlike", t, tp, g, l);
+                        return 1;
+                    }
+                    for (int r = 0; kb >= 0 && r < cnt(kb); ++r)
+                        if (key(ka, r) != key(kb, r)) {
+                            snprintf(msg, n_msg, "type %zu tp %d group %d lane %d: bundle keys differ", t, tp, g, l);
                             return 1;
                         }
-                        if (e >= 0) {
-                            rows_c.push_back(row_of[ft.ent_head[e]]);
-                            rows_p.push_back(pos_of[ft.ent_head[e]]);
+                    if (ka >= 0) {
+                        if (cnt(ka) > prev) {
+                            snprintf(msg, n_msg, "type %zu tp %d group %d lane %d: counts not descending", t, tp, g, l);
+                            return 1;
                         }
+                        prev = cnt(ka);
                     }
-                    coloured += bank_load(rows_c);
-                    plain += bank_load(rows_p);
+                }
+                for (int r = 0; r < c; ++r) {
+                    const int s0 = base + 64 * r;
+                    std::set<int> keys;
+                    for (int h = 0; h < 2; ++h)
+                        for (int l = 0; l < 32; ++l) {
+                            const int k = perm[64 * g + 32 * h + l], ka = perm[64 * g + l];
+                            const int e = ft.lay_ent[s0 + 32 * h + l];
+                            const int want_e = r < cnt(k) ? e0(k) + r : -1;
+                            if (e != want_e) {
+                                snprintf(msg, n_msg, "type %zu tp %d group %d rank %d slot %d: entry %d, expected %d",
+                                         t, tp, g, r, 32 * h + l, e, want_e);
+                                return 1;
+                            }
+                            const int want = r < cnt(ka) ? key(ka, r) : ft.lay_key[s0];
+                            if (ft.lay_key[s0 + 32 * h + l] != want) {
+                                snprintf(msg, n_msg, "type %zu tp %d group %d rank %d slot %d: key %d, expected %d",
+                                         t, tp, g, r, 32 * h + l, ft.lay_key[s0 + 32 * h + l], want);
+                                return 1;
+                            }
+                            if (e >= 0) {
+                                seen[e]++;
+                                ++entries;
+                            }
+                            if (h == 0) keys.insert(want);
+                        }
+                    distinct += (long)keys.size();
+                    slots += 64;
                     ++ranks;
                 }
             }
         }
+        for (size_t e = 0; e < seen.size(); ++e)
+            if (seen[e] != 1) {
+                snprintf(msg, n_msg, "type %zu: entry %zu is in %d slots", t, e, seen[e]);
+                return 1;
+            }
     }
-    if (coloured > plain) {
-        snprintf(msg, n_msg, "colouring raised the bank-set load: %ld > %ld over %ld ranks", coloured, plain, ranks);
+    if (ranks > 0 && distinct > 4 * ranks) {
+        snprintf(msg, n_msg, "ranks read %.2f distinct keys on average", (double)distinct / ranks);
         return 1;
     }
-    snprintf(msg, n_msg, "ranks %ld, bank-set load coloured %ld, uncoloured %ld", ranks, coloured, plain);
+    snprintf(msg, n_msg, "ranks %ld, distinct keys per rank %.2f, slot efficiency %.3f", ranks,
+             ranks ? (double)distinct / ranks : 0.0, slots ? (double)entries / slots : 0.0);
     return 0;
 }

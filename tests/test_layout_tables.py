@@ -39,3 +39,4 @@ def test_layout_tables(checker, kw):
     msg = C.create_string_buffer(512)
     rc = checker.check_layout(C.cast(fp.ref(), C.c_void_p), msg, 512)
     assert rc == 0, msg.value.decode()
+    print(msg.value.decode())
