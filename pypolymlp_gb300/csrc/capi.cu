@@ -77,7 +77,7 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
     dm.max_lin = (dm.max_lin + 3) & ~3;
     const int F = fm.n_features;
     const size_t smem_limit = 227 * 1024;
-    if (rows_pairs_smem_bytes(dm, fp64) > smem_limit)
+    if (rows_pairs_smem_bytes(dm, fp64, rows_pairs_chunk(dm, fp64)) > smem_limit)
         throw std::runtime_error("model too large for the pg_rows_pairs shared-memory layout");
     if (fm.n_tp > kMaxTypePairs) throw std::runtime_error("at most 64 type pairs are supported");
     dm.type_pairs = (const int*)up(fm.type_pairs);

@@ -427,4 +427,147 @@ __device__ __noinline__ void warp_ylm(int maxl, int n_ylm, const YlmTab<T>& tab,
     }
 }
 
+// One radial function q of type pair tp and its derivative at distance r, in
+// the operation order of warp_radial (for one thread).
+template <typename T>
+__device__ __forceinline__ void radial_one(const DevModel& M, int tp, int q, T r, T& fn, T& fnd) {
+    const T rc = model_cutoff<T>(M);
+    const T v1 = (T)kPiD / rc;
+    const T v2 = v1 * r;
+    const T fc = (T)0.5 * (cos(v2) + (T)1.0);
+    const T fcd = (T)-0.5 * v1 * sin(v2);
+    const T beta = model_beta<T>(M, tp * M.n_fn_max + q);
+    const T mu = model_mu<T>(M, tp * M.n_fn_max + q);
+    const T x = r - mu;
+    const T bf = exp(-beta * x * x);
+    fn = bf * fc;
+    fnd = (T)-2.0 * beta * x * bf * fc + bf * fcd;
+}
+
+// Direction terms of Y_lm shared by the columns of one pair.
+template <typename T>
+struct YlmDir {
+    T ct, st, cp, sp, invr;
+};
+template <typename T>
+__device__ __forceinline__ YlmDir<T> ylm_dir(T x, T y, T z, T r) {
+    YlmDir<T> d;
+    d.ct = z / r;
+    const T rho = hypot(x, y);
+    d.cp = rho > (T)0 ? x / rho : (T)1;
+    d.sp = rho > (T)0 ? y / rho : (T)0;
+    d.st = sqrt((T)1 - d.ct * d.ct);
+    d.invr = (T)1 / r;
+    return d;
+}
+
+// Column m' = mp of Y_lm (keys (l, -mp), l = mp .. L, at row l(l+1)/2 + l - mp
+// of `rows`, 8 values per row: Y, dY/dx, dY/dy, dY/dz as (re, im)) for one
+// thread.  The same recursion and constants as warp_ylm (the normalised
+// associated Legendre recursion of polymlp_spherical_harmonics.cpp:27-209),
+// run down column mp, with the Q recursion of column mp + 1 in lock step for
+// the theta derivative, so that no (l, m) scratch table is needed.
+template <typename T>
+__device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, const YlmDir<T>& d, T* rows) {
+    const T s2pi = (T)0.39894228040143267794;
+    const T sq3 = (T)1.7320508075688772935, sq32 = (T)1.2247448713915890491;
+    const T h = (T)0.5 * (T)1.41421356237309504880;
+    const T ct = d.ct, st = d.st, cp = d.cp, sp = d.sp, invr = d.invr;
+    // diagonals P_mp,mp, Q_mp,mp and Q_mp+1,mp+1
+    T pmm, qmm;
+    if (mp == 0) {
+        pmm = s2pi;
+        qmm = 0;
+    } else {
+        pmm = -st * sq32 * s2pi;
+        qmm = -sq32 * s2pi;
+        for (int l = 2; l <= mp; ++l) {
+            const T c1 = tab.C1[l] * st;
+            pmm = c1 * pmm;
+            qmm = c1 * qmm;
+        }
+    }
+    T qn_mm = 0;  // Q_mp+1,mp+1
+    if (mp + 1 <= L) qn_mm = (mp + 1 == 1) ? -sq32 * s2pi : (tab.C1[mp + 1] * st) * qmm;
+    // cos(mp phi), sin(mp phi) by the Chebyshev recurrence
+    T cs = 1, c2 = cp, sn = 0, s2 = -sp;
+    {
+        const T tc = (T)2 * c2;
+        for (int q = 1; q <= mp; ++q) {
+            const T s = tc * sn - s2, c = tc * cs - c2;
+            c2 = cs;
+            cs = c;
+            s2 = sn;
+            sn = s;
+        }
+    }
+    const T sign = (mp & 1) ? (T)-1 : (T)1;
+    const cplx<T> common = {cs * h * invr, sn * h * invr};
+    T p1 = 0, p2 = 0, q1 = 0, q2 = 0;     // column mp: values at l - 1, l - 2
+    T n1 = 0, n2 = 0;                     // column mp + 1 (Q only)
+    for (int l = mp; l <= L; ++l) {
+        T p, q, qn;
+        if (l == mp) {
+            p = pmm;
+            q = qmm;
+            qn = 0;
+        } else if (l == mp + 1) {
+            if (mp == 0) {
+                p = ct * sq3 * s2pi;
+                q = 0;
+            } else {
+                const T c2m = tab.C2[mp] * ct;
+                p = c2m * p1;
+                q = c2m * q1;
+            }
+            qn = qn_mm;
+        } else {
+            const T alm = tab.A[lmi(l, mp)], blm = tab.B[lmi(l, mp)];
+            p = alm * (ct * p1 + blm * p2);
+            q = alm * (ct * q1 + blm * q2);
+            if (l == mp + 2) {
+                qn = (tab.C2[mp + 1] * ct) * n1;
+            } else {
+                const T aln = tab.A[lmi(l, mp + 1)], bln = tab.B[lmi(l, mp + 1)];
+                qn = aln * (ct * n1 + bln * n2);
+            }
+        }
+        p2 = p1;
+        p1 = p;
+        q2 = q1;
+        q1 = q;
+        n2 = n1;
+        n1 = qn;
+        T* o = rows + 8 * (l * (l + 1) / 2 + l - mp);
+        if (mp == 0) {
+            const T qv = (l == 0) ? (T)0 : qn;
+            const T c0 = qv * st * invr * tab.D0[l];
+            o[0] = p * h;
+            o[1] = 0;
+            o[2] = c0 * ct * cp;
+            o[3] = 0;
+            o[4] = c0 * ct * sp;
+            o[5] = 0;
+            o[6] = -c0 * st;
+            o[7] = 0;
+        } else {
+            const T tmp = sign * p * h;
+            T dth = (T)mp * ct * q;
+            if (mp != l) dth += tab.D1[lmi(l, mp)] * qn * st;
+            const T dph = (T)mp * q;
+            const cplx<T> ax = cmul(common, cplx<T>{dth * ct * cp, -dph * sp});
+            const cplx<T> ay = cmul(common, cplx<T>{dth * ct * sp, dph * cp});
+            const cplx<T> az = {-common.re * dth * st, -common.im * dth * st};
+            o[0] = tmp * cs;
+            o[1] = -(tmp * sn);
+            o[2] = sign * ax.re;
+            o[3] = -sign * ax.im;
+            o[4] = sign * ay.re;
+            o[5] = -sign * ay.im;
+            o[6] = sign * az.re;
+            o[7] = -sign * az.im;
+        }
+    }
+}
+
 }  // namespace pg

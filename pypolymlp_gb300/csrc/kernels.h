@@ -71,6 +71,7 @@ constexpr int kCellListMaxPairs = 4096;  // per atom, for the in-block ordering
 
 constexpr int kRowsThreads = 256;  // threads of pg_rows / pg_rows_pairs blocks
 constexpr int kMaxTypePairs = 64;
+constexpr int kMaxSuperChunk = 32;  // pairs per stage-A super-chunk (at most)
 
 void launch_nb_count(const DevBatch& B, int* counts, int* max_cl, cudaStream_t st);
 void launch_nb_fill(const DevBatch& B, const long long* off, int* nb_j, double* nb_d, float4* nb_df, long long* keys,
@@ -87,7 +88,8 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st);
 void launch_exclusive_scan(const int* counts, int n, long long* offsets, long long* total, cudaStream_t st);
-size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64);
+size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64, int ps);
+int rows_pairs_chunk(const DevModel& M, bool fp64);
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,
                       long long* gslot, int* missing, cudaStream_t st);
 template <typename T>

@@ -462,26 +462,29 @@ __global__ void pg_nb_mirror(int n_atoms, const long long* nb_off, const int* nb
     }
 }
 
-// Stage A.  Block per centre atom i of a force structure; its pairs are taken
-// in chunks of up to NW pairs of one type pair (pairs ordered by type pair,
-// stably, so the images of a neighbour stay consecutive).  The entries of
-// feature k by a type pair share one radial function n (host/flat_tables.h),
-// so with phi_h(d) = f_n(r) Y_lm(d/r) the derivative by pair p factors into
+// Stage A.  Block per centre atom i of a force structure; its pairs are
+// ordered by type pair (stably, so the images of a neighbour stay
+// consecutive).  The entries of feature k by a type pair share one radial
+// function n (host/flat_tables.h), so with phi_h(d) = f_n(r) Y_lm(d/r) the
+// derivative by pair p factors into
 //   dd_k/dd_p,c = f_n(r_p) S_k,c(p) + f_n'(r_p) (d_p,c / r_p) T_k(p),
 //   T_k(p) = sum_e Re(G_e(i) Y_(key e)(p)),  S_k,c(p) = sum_e Re(G_e(i) dY_(key e)(p)/dd_c).
-// Per chunk, warp w builds the basis of pair w into a table of its Y_lm and
-// their gradients (8 values per key) and of its radial functions
-// (f_n, f_n' d_x/r, f_n' d_y/r, f_n' d_z/r); then thread k runs over the
-// entries of feature k once for all pairs of the chunk, reading the table
-// row of the entry's key.  The entries of the centre are stored by type
-// pair, features ordered by their number of entries and then by their key
-// sequence and interleaved 32 at a time (pg_features_adjoint), so warp = 32
-// feature positions reads them coalesced with equal loop lengths and most
-// ranks name one key for all 32 lanes: a shared-memory broadcast.
+// The pairs of one type pair are taken up to `ps` at a time (a super-chunk):
+// the block builds their bases at once into shared memory, a table of the
+// Y_lm and their gradients (8 values per key; thread = pair and two Legendre
+// columns, ylm_column) and of the radial functions (f_n, f_n' d_x/r,
+// f_n' d_y/r, f_n' d_z/r; thread = pair and n).  Then each warp takes groups
+// of 32 bundles (lane = two features with the same key sequence) and runs
+// over the group's entries once per NW pairs of the super-chunk, one table
+// row per pair and rank serving both features.  The entries of the centre are
+// stored by type pair, rank-major in groups (pg_features_adjoint), so the
+// lanes read them coalesced with equal loop lengths and most ranks name one
+// key for all 32 lanes: a shared-memory broadcast.
 // The images of one neighbour j are summed and stored once, at the group slot
 // (the first entry of i in j's list), indexed by feature position, so stage B
 // reads one vector per (centre, target).  The centre's DS vectors are
-// accumulated per type pair, also by feature position:
+// accumulated per type pair, also by feature position, in registers over a
+// super-chunk:
 //   DS[i][tp][c][x]   = sum_{p of tp, j_p != i} dd_k/dd_p,c         (self rows)
 //   DS[i][tp][3+q][x] = sum_{p of tp} d_p,b(q) dd_k/dd_p,a(q)       (virial)
 // with k = perm_tp[x] and (a, b)(q) = (x,x) (y,y) (z,z) (x,y) (y,z) (z,x).
@@ -522,30 +525,26 @@ __device__ __forceinline__ void load_row4(const double* p, double (&v)[4]) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off,
-                                                              const int* nb_j, const double* nb_d,
-                                                              const long long* gslot, const long long* s_off,
-                                                              const long long* g_off, const cplx<T>* G,
-                                                              const long long* f_row, int* order, T* Dp, T* DS) {
+__global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
+    pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
+                  const long long* gslot, const long long* s_off, const long long* g_off, const cplx<T>* G,
+                  const long long* f_row, int* order, T* Dp, T* DS, int ps) {
     constexpr int NW = kRowsThreads / 32;
-    static_assert(NW == 8, "the chunk width is 8 pairs");
+    static_assert(NW == 8, "a contraction step takes 8 pairs");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_wcnt[NW], s_tpoff[kMaxTypePairs + 1];
-    __shared__ int s_flag[NW];  // ok | self << 1 | flush << 2 | fresh << 3 | first << 4
-    __shared__ long long s_slot[NW];
+    __shared__ int s_flag[kMaxSuperChunk];  // ok | self << 1 | flush << 2 | fresh << 3 | first << 4
+    __shared__ long long s_slot[kMaxSuperChunk];
     const int i = blockIdx.x;
     if (f_row[B.atom_st[i]] < 0) return;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nl = ty.n_lin, NL = M.max_lin, NY = M.n_ylm, NF = M.n_fn_max;
-    const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    T* tab = reinterpret_cast<T*>(smem_raw);  // [NW][NY][8]: Y, dY/dx, dY/dy, dY/dz (re, im)
-    T* rad = tab + (size_t)NW * NY * 8;       // [NW][NF][4]: f, f' x/r, f' y/r, f' z/r
-    T* sb = rad + (size_t)NW * NF * 4;
-    T* s_tab = sb + slot * NW;
-    T* sd = reinterpret_cast<T*>(
-        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));  // [NW][3]
+    const int NL = M.max_lin, NY = M.n_ylm, NF = M.n_fn_max, L = M.maxl;
+    T* tab = reinterpret_cast<T*>(smem_raw);  // [ps][NY][8]: Y, dY/dx, dY/dy, dY/dz (re, im)
+    T* rad = tab + (size_t)ps * NY * 8;       // [ps][NF][4]: f, f' x/r, f' y/r, f' z/r
+    T* geo = rad + (size_t)ps * NF * 4;       // [ps][4]: d_x, d_y, d_z
+    T* s_tab = geo + (size_t)ps * 4;
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     const long long p0 = nb_off[i], p1 = nb_off[i + 1];
     const int np = (int)(p1 - p0);
@@ -577,97 +576,110 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_
     const int npos = ty.n_pos;
     T* dsa = DS + s_off[i];  // [type pair of the centre type][9][n_pos], feature positions of that pair
     for (int q = threadIdx.x; q < 9 * npos * ty.n_tpl; q += blockDim.x) dsa[q] = (T)0;
+    const int tpp = kRowsThreads / ps;  // threads per pair building the Y_lm table
     for (int tp = 0; tp < M.n_tp; ++tp) {
         const int r_end = s_tpoff[tp + 1];
         if (ty.tpl[tp] < 0 || r_end == s_tpoff[tp]) continue;  // no heads of tp: zero derivatives
         const int nfn = M.tp_nfn[tp];
         const int* pos_nid = ty.tp_pos_nid + (size_t)tp * npos;
-        for (int r0 = s_tpoff[tp]; r0 < r_end; r0 += NW) {
-            const int n = min(NW, r_end - r0);
-            // ---- basis table of pair w = warp
-            T* tw = tab + (size_t)warp * NY * 8;
-            T* rw = rad + (size_t)warp * NF * 4;
-            bool ok = false;
-            if (warp < n) {
-                const long long q = p0 + ord[r0 + warp];
+        T* ds = dsa + (size_t)ty.tpl[tp] * 9 * npos;
+        for (int sc0 = s_tpoff[tp]; sc0 < r_end; sc0 += ps) {
+            const int nsc = min(ps, r_end - sc0);
+            const int nsc8 = (nsc + NW - 1) / NW * NW;  // whole contraction steps; pairs past nsc are zero
+            // ---- bases of the super-chunk; pair flags
+            for (int p = threadIdx.x; p < nsc; p += blockDim.x) {
+                const long long q = p0 + ord[sc0 + p];
                 T dx, dy, dz, dis;
-                ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
+                const bool ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
                 const int j = nb_j[q];
-                if (lane == 0) {
-                    sd[3 * warp] = dx;
-                    sd[3 * warp + 1] = dy;
-                    sd[3 * warp + 2] = dz;
-                    const bool first = q == p0 || nb_j[q - 1] != j;
-                    const bool last = q + 1 == p1 || nb_j[q + 1] != j;
-                    s_flag[warp] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (last ? 4 : 0) | (first ? 16 : 0);
-                    s_slot[warp] = gslot[q];
-                }
+                geo[4 * p] = dx;
+                geo[4 * p + 1] = dy;
+                geo[4 * p + 2] = dz;
+                geo[4 * p + 3] = 0;
+                const bool first = q == p0 || nb_j[q - 1] != j;
+                const bool last = q + 1 == p1 || nb_j[q + 1] != j;
+                s_flag[p] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (last ? 4 : 0) | (first ? 16 : 0);
+                s_slot[p] = gslot[q];
+            }
+            for (int it = threadIdx.x; it < nsc8 * nfn; it += blockDim.x) {
+                const int p = it / nfn, n = it - p * nfn;
+                T* o = rad + ((size_t)p * NF + n) * 4;
+                T dx = 0, dy = 0, dz = 0, dis = 1;
+                const bool ok = p < nsc && pair_geometry<T>(M, B, nb_d, p0 + ord[sc0 + p], dx, dy, dz, dis);
                 if (ok) {
-                    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
-                    warp_radial<T, true>(M, tp, dis, bv, lane);
-                    if (M.gtinv) {
-                        warp_ylm<T, true>(M.maxl, M.n_ylm, ytab, dx, dy, dz, dis, bv, lane);
-                    } else if (lane == 0) {
-                        bv.Y[0] = {(T)1, (T)0};
-                        bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
-                    }
-                    __syncwarp();
+                    T f, fd;
+                    radial_one<T>(M, tp, n, dis, f, fd);
                     const T invr = (T)1 / dis;
-                    const T ux = dx * invr, uy = dy * invr, uz = dz * invr;
-                    for (int u = lane; u < nfn; u += 32) {
-                        const T f = bv.fn[u], fd = bv.fnd[u];
-                        T* o = rw + 4 * u;
-                        o[0] = f;
-                        o[1] = fd * ux;
-                        o[2] = fd * uy;
-                        o[3] = fd * uz;
-                    }
-                    const int ny = M.gtinv ? NY : 1;
-                    for (int u = lane; u < ny; u += 32) {
-                        const cplx<T> y = bv.Y[u], yx = bv.dY[u], yy = bv.dY[NY + u], yz = bv.dY[2 * NY + u];
-                        T* o = tw + 8 * u;
-                        o[0] = y.re;
-                        o[1] = y.im;
-                        o[2] = yx.re;
-                        o[3] = yx.im;
-                        o[4] = yy.re;
-                        o[5] = yy.im;
-                        o[6] = yz.re;
-                        o[7] = yz.im;
-                    }
+                    o[0] = f;
+                    o[1] = fd * (dx * invr);
+                    o[2] = fd * (dy * invr);
+                    o[3] = fd * (dz * invr);
+                } else {
+                    o[0] = o[1] = o[2] = o[3] = (T)0;
                 }
             }
-            if (!ok) {
-                // absent or out-of-range pair: a zero table (its derivatives vanish)
-                for (int u = lane; u < NY * 8; u += 32) tw[u] = (T)0;
-                for (int u = lane; u < nfn * 4; u += 32) rw[u] = (T)0;
+            for (int p = threadIdx.x / tpp; p < nsc8; p += kRowsThreads / tpp) {
+                const int t = threadIdx.x - (threadIdx.x / tpp) * tpp;
+                T* rows = tab + (size_t)p * NY * 8;
+                T dx = 0, dy = 0, dz = 0, dis = 1;
+                const bool ok = p < nsc && pair_geometry<T>(M, B, nb_d, p0 + ord[sc0 + p], dx, dy, dz, dis);
+                if (!M.gtinv) {
+                    if (t == 0)
+                        for (int v = 0; v < 8; ++v) rows[v] = (v == 0 && ok) ? (T)1 : (T)0;
+                    continue;
+                }
+                const YlmDir<T> dir = ylm_dir<T>(dx, dy, dz, dis);
+                // columns a and L - a: about (L + 2) / 2 keys per thread
+                for (int a = t; 2 * a <= L; a += tpp)
+                    for (int side = 0; side < 2; ++side) {
+                        const int mp = side ? L - a : a;
+                        if (side && mp == a) break;
+                        if (ok) {
+                            ylm_column<T>(mp, L, ytab, dir, rows);
+                        } else {
+                            for (int l = mp; l <= L; ++l)
+                                for (int v = 0; v < 8; ++v) rows[8 * (l * (l + 1) / 2 + l - mp) + v] = (T)0;
+                        }
+                    }
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                // where to store the running image sums: at a group's last image or
-                // the chunk's end; "fresh" when the group's first image is in this chunk
-                int seg = 0;
-                for (int w = 0; w < n; ++w) {
-                    int fl = s_flag[w];
-                    const bool flush = (fl & 4) || w == n - 1;
-                    if (s_flag[seg] & 16) fl |= 8;
-                    s_flag[w] = (fl & ~4) | (flush ? 4 : 0);
-                    if (flush) seg = w + 1;
+                // per step of NW pairs, where to store the running image sums: at a
+                // group's last image or the step's end; "fresh" when the group's
+                // first image is in this step
+                for (int s0 = 0; s0 < nsc; s0 += NW) {
+                    const int n = min(NW, nsc - s0);
+                    int seg = s0;
+                    for (int w = s0; w < s0 + n; ++w) {
+                        int fl = s_flag[w];
+                        const bool flush = (fl & 4) || w == s0 + n - 1;
+                        if (s_flag[seg] & 16) fl |= 8;
+                        s_flag[w] = (fl & ~4) | (flush ? 4 : 0);
+                        if (flush) seg = w + 1;
+                    }
                 }
             }
             __syncthreads();
-            // ---- contraction of the chunk: warp = group of 32 bundles, lane =
-            // bundle (two features with the same keys, positions xa and xa + 32);
-            // the group's entries are read rank-major (coalesced) and one table
-            // row per pair and rank serves both features
-            {
-                T* ds = dsa + (size_t)ty.tpl[tp] * 9 * npos;
-                const int ng = ty.n_groups;
-                for (int grp = warp; grp < ng; grp += NW) {
-                    const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
-                    // groups past the last of tp: no entries, zero derivatives, nothing
-                    // stored (stage B reads positions below tp_nnz only)
-                    if (cnt == 0) continue;
+            // ---- contraction: warp = group of 32 bundles, lane = bundle (two
+            // features with the same keys, positions xa and xa + 32); the group's
+            // entries are read rank-major (coalesced) and one table row per pair
+            // and rank serves both features
+            const int ng = ty.n_groups;
+            for (int grp = warp; grp < ng; grp += NW) {
+                const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
+                // groups past the last of tp: no entries, zero derivatives, nothing
+                // stored (stage B reads positions below tp_nnz only)
+                if (cnt == 0) continue;
+                const int xa = 64 * grp + lane;
+                const int nid[2] = {pos_nid[xa], pos_nid[xa + 32]};
+                // the DS sums of both features, over the super-chunk
+                T sv[2][9];
+#pragma unroll
+                for (int f = 0; f < 2; ++f)
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) sv[f][v] = ds[(size_t)v * npos + xa + 32 * f];
+                for (int s0 = 0; s0 < nsc; s0 += NW) {
+                    const T* tab0 = tab + (size_t)s0 * NY * 8;
                     // per pair and feature: T, S_x, S_y, S_z
                     T acc[NW][2][4];
 #pragma unroll
@@ -694,7 +706,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_
                             const int r = r0 + s;
                             if (r >= cnt) break;
                             const T are = ga[s].re, aim = -ga[s].im, bre = gb[s].re, bim = -gb[s].im;
-                            const T* row = tab + 8 * kq[s];
+                            const T* row = tab0 + 8 * kq[s];
                             if (r + kPrefetch < cnt) {
                                 const int sl = base + 64 * (r + kPrefetch) + lane;
                                 ga[s] = Gi[sl];
@@ -714,43 +726,40 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_
                         }
                     }
                     // ---- per feature of the bundle: derivatives, image sums, DS sums
+                    const int n = min(NW, nsc - s0);
 #pragma unroll
                     for (int f = 0; f < 2; ++f) {
-                        const int x = 64 * grp + 32 * f + lane;
-                        const int nid = pos_nid[x];
-                        T sv[9];
-#pragma unroll
-                        for (int v = 0; v < 9; ++v) sv[v] = ds[(size_t)v * npos + x];
+                        const int x = xa + 32 * f;
                         T run0 = 0, run1 = 0, run2 = 0;
 #pragma unroll
                         for (int w = 0; w < NW; ++w) {
                             if (w >= n) break;
-                            const int fl = s_flag[w];
-                            T rf[4];
-                            load_row4(rad + ((size_t)w * NF + nid) * 4, rf);
+                            const int pw = s0 + w;
+                            const int fl = s_flag[pw];
+                            T rf[4], dg[4];
+                            load_row4(rad + ((size_t)pw * NF + nid[f]) * 4, rf);
+                            load_row4(geo + 4 * pw, dg);
                             const T tk = acc[w][f][0];
                             const T a0 = fma(rf[0], acc[w][f][1], rf[1] * tk);
                             const T a1 = fma(rf[0], acc[w][f][2], rf[2] * tk);
                             const T a2 = fma(rf[0], acc[w][f][3], rf[3] * tk);
-                            if (fl & 1) {
-                                const T dx = sd[3 * w], dy = sd[3 * w + 1], dz = sd[3 * w + 2];
-                                if (!(fl & 2)) {
-                                    sv[0] += a0;
-                                    sv[1] += a1;
-                                    sv[2] += a2;
-                                }
-                                sv[3] = fma(dx, a0, sv[3]);
-                                sv[4] = fma(dy, a1, sv[4]);
-                                sv[5] = fma(dz, a2, sv[5]);
-                                sv[6] = fma(dy, a0, sv[6]);
-                                sv[7] = fma(dz, a1, sv[7]);
-                                sv[8] = fma(dx, a2, sv[8]);
+                            // (an out-of-range pair has a zero table: its terms vanish)
+                            if (!(fl & 2)) {
+                                sv[f][0] += a0;
+                                sv[f][1] += a1;
+                                sv[f][2] += a2;
                             }
+                            sv[f][3] = fma(dg[0], a0, sv[f][3]);
+                            sv[f][4] = fma(dg[1], a1, sv[f][4]);
+                            sv[f][5] = fma(dg[2], a2, sv[f][5]);
+                            sv[f][6] = fma(dg[1], a0, sv[f][6]);
+                            sv[f][7] = fma(dg[2], a1, sv[f][7]);
+                            sv[f][8] = fma(dg[0], a2, sv[f][8]);
                             run0 += a0;
                             run1 += a1;
                             run2 += a2;
                             if (fl & 4) {
-                                T* o = Dp + (size_t)s_slot[w] * 3 * NL + x;
+                                T* o = Dp + (size_t)s_slot[pw] * 3 * NL + x;
                                 if (fl & 8) {
                                     o[0] = run0;
                                     o[NL] = run1;
@@ -763,10 +772,12 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1) pg_rows_
                                 run0 = run1 = run2 = 0;
                             }
                         }
-#pragma unroll
-                        for (int v = 0; v < 9; ++v) ds[(size_t)v * npos + x] = sv[v];
                     }
                 }
+#pragma unroll
+                for (int f = 0; f < 2; ++f)
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) ds[(size_t)v * npos + xa + 32 * f] = sv[f][v];
             }
             __syncthreads();
         }
@@ -1210,13 +1221,19 @@ void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long lo
                                                          reinterpret_cast<cplx<T>*>(G));
 }
 
-size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64) {
+// Pairs per stage-A super-chunk: 32, or fewer (16, 8) where the tables of 32
+// pairs would not leave room for two blocks per SM (FP32) or one (FP64).
+int rows_pairs_chunk(const DevModel& M, bool fp64) {
+    const size_t budget = fp64 ? 200 * 1024 : 110 * 1024;
+    int ps = kMaxSuperChunk;
+    while (ps > 8 && rows_pairs_smem_bytes(M, fp64, ps) > budget) ps /= 2;
+    return ps;
+}
+
+size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64, int ps) {
     const size_t ts = fp64 ? 8 : 4;
-    const int nw = kRowsThreads / 32;
-    const size_t slot = fp64 ? basis_slot_elems<double>(M.n_fn_max, M.n_ylm, M.maxl)
-                             : basis_slot_elems<float>(M.n_fn_max, M.n_ylm, M.maxl);
-    return (size_t)nw * M.n_ylm * 8 * ts + (size_t)nw * M.n_fn_max * 4 * ts + slot * nw * ts +
-           (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts + 16 + (size_t)3 * nw * ts + 16;
+    return (size_t)ps * M.n_ylm * 8 * ts + (size_t)ps * M.n_fn_max * 4 * ts + (size_t)ps * 4 * ts +
+           (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts;
 }
 
 void launch_nb_mirror(int n_atoms, const long long* nb_off, const int* nb_j, const double* nb_d, long long* mirror,
@@ -1230,10 +1247,12 @@ template <typename T>
 void launch_rows_pairs(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
                        const double* nb_d, const long long* gslot, const long long* s_off, const long long* g_off,
                        const void* G, const long long* f_row, int* order, T* Dp, T* DS, cudaStream_t st) {
-    const size_t smem = rows_pairs_smem_bytes(M, sizeof(T) == 8);
+    const int ps = rows_pairs_chunk(M, sizeof(T) == 8);
+    const size_t smem = rows_pairs_smem_bytes(M, sizeof(T) == 8, ps);
     PG_CUDA(cudaFuncSetAttribute(pg_rows_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pg_rows_pairs<T><<<B.n_atoms, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, nb_d, gslot, s_off, g_off,
-                                                           reinterpret_cast<const cplx<T>*>(G), f_row, order, Dp, DS);
+                                                           reinterpret_cast<const cplx<T>*>(G), f_row, order, Dp, DS,
+                                                           ps);
 }
 
 template <typename T>
