@@ -137,6 +137,8 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.lay_key = (const int*)up(ft.lay_key);
         d.lay_grp_base = (const int*)up(ft.lay_grp_base);
         d.lay_grp_cnt = (const int*)up(ft.lay_grp_cnt);
+        d.lay_sched = (const int*)up(ft.lay_sched);
+        d.n_rounds = ft.n_rounds;
         d.tp_perm = (const int*)up(ft.tp_perm);
         d.tp_ipos = (const int*)up(ft.tp_ipos);
         d.tp_pos_nid = (const int*)up(ft.tp_pos_nid);

@@ -70,6 +70,8 @@ struct DevType {
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
     int n_groups, lay_size, n_tpl, n_pos;  // n_pos: feature positions per type pair (host/flat_tables.h)
+    int n_rounds;                          // rounds of the stage-A group schedule lay_sched
+    const int* lay_sched;
     const int *lay_key, *lay_grp_base, *lay_grp_cnt, *tp_perm, *tp_ipos, *tpl, *tpl_tp;
     const int* tp_pos_nid;  // per type pair and position: the radial function of the feature's entries
     const int* tp_nnz;      // per type pair: feature positions with entries (the first ones)

@@ -290,6 +290,30 @@ FlatModel flatten_model(const ModelTables& mt) {
                 }
             }
             ft.lay_size = (int)ft.lay_ent.size();
+            // warp schedule of the groups: longest first, each to the least-loaded
+            // warp (a group costs its ranks plus about three ranks of epilogue)
+            std::vector<std::vector<std::vector<int>>> lists(ntp, std::vector<std::vector<int>>(kLayWarps));
+            ft.n_rounds = 0;
+            for (int tp = 0; tp < ntp; ++tp) {
+                std::vector<int> gs;
+                for (int g = 0; g < ng; ++g)
+                    if (ft.lay_grp_cnt[(size_t)tp * ng + g] > 0) gs.push_back(g);
+                std::stable_sort(gs.begin(), gs.end(), [&](int a, int b) {
+                    return ft.lay_grp_cnt[(size_t)tp * ng + a] > ft.lay_grp_cnt[(size_t)tp * ng + b];
+                });
+                std::vector<int> load(kLayWarps, 0);
+                for (int g : gs) {
+                    const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+                    load[w] += ft.lay_grp_cnt[(size_t)tp * ng + g] + 3;
+                    lists[tp][w].push_back(g);
+                    ft.n_rounds = std::max(ft.n_rounds, (int)lists[tp][w].size());
+                }
+            }
+            ft.lay_sched.assign((size_t)ntp * ft.n_rounds * kLayWarps, -1);
+            for (int tp = 0; tp < ntp; ++tp)
+                for (int w = 0; w < kLayWarps; ++w)
+                    for (size_t k = 0; k < lists[tp][w].size(); ++k)
+                        ft.lay_sched[((size_t)tp * ft.n_rounds + k) * kLayWarps + w] = lists[tp][w][k];
         }
     }
     // Legendre / Y_lm constants, computed in IEEE double with the reference's

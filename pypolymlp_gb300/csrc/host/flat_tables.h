@@ -14,6 +14,7 @@
 namespace pg {
 
 constexpr int kMaxOrder = 6;  // gtinv order supported by the reference tables
+constexpr int kLayWarps = 8;  // warps of a stage-A block (the contraction's group schedule)
 
 // One product term: coeff * prod(a[ids[0..n)]) (ids: full local ids).
 struct FlatTerm {
@@ -78,8 +79,11 @@ struct FlatType {
     // lane past its feature's entries repeats the key of lane 0, so the lanes
     // of a rank read few distinct keys.  tp_nnz[tp] = 64 n_g(tp): the positions
     // that can hold derivatives of tp; the others' derivatives vanish.
-    int n_groups = 0, lay_size = 0, n_pos = 0;
-    std::vector<int> lay_ent, lay_key, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_pos_nid, tp_nnz;
+    // lay_sched[tp][k][w] (n_rounds x kLayWarps per type pair): the k-th group
+    // of warp w in stage A, or -1; longest groups first, each to the
+    // least-loaded warp.
+    int n_groups = 0, lay_size = 0, n_pos = 0, n_rounds = 0;
+    std::vector<int> lay_ent, lay_key, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_pos_nid, tp_nnz, lay_sched;
     // type pairs with heads for this centre type: local index or -1, and back
     std::vector<int> tpl, tpl_tp;
 };

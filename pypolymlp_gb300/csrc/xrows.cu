@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
     static_assert(NW == 8, "a contraction step takes 8 pairs");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_wcnt[NW], s_tpoff[kMaxTypePairs + 1];
-    __shared__ int s_flag[kMaxSuperChunk];  // ok | self << 1 | flush << 2 | fresh << 3 | first << 4
+    __shared__ int s_flag[kMaxSuperChunk];  // ok | self << 1 | flush << 2 | fresh << 3
     __shared__ long long s_slot[kMaxSuperChunk];
     const int i = blockIdx.x;
     if (f_row[B.atom_st[i]] < 0) return;
@@ -586,7 +586,10 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
         for (int sc0 = s_tpoff[tp]; sc0 < r_end; sc0 += ps) {
             const int nsc = min(ps, r_end - sc0);
             const int nsc8 = (nsc + NW - 1) / NW * NW;  // whole contraction steps; pairs past nsc are zero
-            // ---- bases of the super-chunk; pair flags
+            // ---- bases of the super-chunk; pair flags: per step of NW pairs, the
+            // running image sums are stored at a group's last image or the step's
+            // end ("flush"), and stored rather than added when the group's first
+            // image is in this step ("fresh"; runs of images are contiguous)
             for (int p = threadIdx.x; p < nsc; p += blockDim.x) {
                 const long long q = p0 + ord[sc0 + p];
                 T dx, dy, dz, dis;
@@ -596,9 +599,18 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                 geo[4 * p + 1] = dy;
                 geo[4 * p + 2] = dz;
                 geo[4 * p + 3] = 0;
-                const bool first = q == p0 || nb_j[q - 1] != j;
+                const int step = p / NW * NW;
                 const bool last = q + 1 == p1 || nb_j[q + 1] != j;
-                s_flag[p] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (last ? 4 : 0) | (first ? 16 : 0);
+                const bool flush = last || p == min(step + NW, nsc) - 1;
+                bool fresh = false;
+                for (int v = p; v >= step; --v) {
+                    const long long qv = p0 + ord[sc0 + v];
+                    if (qv == p0 || nb_j[qv - 1] != nb_j[qv]) {
+                        fresh = true;
+                        break;
+                    }
+                }
+                s_flag[p] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (flush ? 4 : 0) | (fresh ? 8 : 0);
                 s_slot[p] = gslot[q];
             }
             for (int it = threadIdx.x; it < nsc8 * nfn; it += blockDim.x) {
@@ -643,33 +655,18 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                     }
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                // per step of NW pairs, where to store the running image sums: at a
-                // group's last image or the step's end; "fresh" when the group's
-                // first image is in this step
-                for (int s0 = 0; s0 < nsc; s0 += NW) {
-                    const int n = min(NW, nsc - s0);
-                    int seg = s0;
-                    for (int w = s0; w < s0 + n; ++w) {
-                        int fl = s_flag[w];
-                        const bool flush = (fl & 4) || w == s0 + n - 1;
-                        if (s_flag[seg] & 16) fl |= 8;
-                        s_flag[w] = (fl & ~4) | (flush ? 4 : 0);
-                        if (flush) seg = w + 1;
-                    }
-                }
-            }
-            __syncthreads();
             // ---- contraction: warp = group of 32 bundles, lane = bundle (two
             // features with the same keys, positions xa and xa + 32); the group's
             // entries are read rank-major (coalesced) and one table row per pair
             // and rank serves both features
             const int ng = ty.n_groups;
-            for (int grp = warp; grp < ng; grp += NW) {
+            static_assert(NW == kLayWarps, "the group schedule is laid out for the block's warps");
+            for (int k = 0; k < ty.n_rounds; ++k) {
+                // groups past the last of tp have no entries and are not scheduled:
+                // zero derivatives, nothing stored (stage B reads positions below tp_nnz only)
+                const int grp = ty.lay_sched[((size_t)tp * ty.n_rounds + k) * NW + warp];
+                if (grp < 0) continue;
                 const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
-                // groups past the last of tp: no entries, zero derivatives, nothing
-                // stored (stage B reads positions below tp_nnz only)
-                if (cnt == 0) continue;
                 const int xa = 64 * grp + lane;
                 const int nid[2] = {pos_nid[xa], pos_nid[xa + 32]};
                 // the DS sums of both features, over the super-chunk

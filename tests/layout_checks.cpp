@@ -6,7 +6,8 @@
 // one radial function, tp_pos_nid at its position; slots hold the r-th entries
 // of their features and name the key of lane l's first feature, or lane 0's
 // past its entries; the slots cover every entry once; and the ranks read few
-// distinct keys (the mean over ranks is reported and bounded by 4).  Returns 0
+// distinct keys (the mean over ranks is reported and bounded by 4); the warp
+// schedule names every group with entries once.  Returns 0
 // and a summary, or 1 and the first violation, in msg.
 #include <cstdio>
 #include <set>
@@ -61,6 +62,19 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
             for (int k = 0; k < nl; ++k)
                 if (hits[k] != 1) {
                     snprintf(msg, n_msg, "type %zu tp %d: feature %d at %d positions", t, tp, k, hits[k]);
+                    return 1;
+                }
+            std::vector<int> sched(ng, 0);
+            for (int q = 0; q < ft.n_rounds * kLayWarps; ++q) {
+                const int g = ft.lay_sched[(size_t)tp * ft.n_rounds * kLayWarps + q];
+                if (g >= ng || (g >= 0 && sched[g]++)) {
+                    snprintf(msg, n_msg, "type %zu tp %d: schedule entry %d names group %d", t, tp, q, g);
+                    return 1;
+                }
+            }
+            for (int g = 0; g < ng; ++g)
+                if (sched[g] != (ft.lay_grp_cnt[(size_t)tp * ng + g] > 0 ? 1 : 0)) {
+                    snprintf(msg, n_msg, "type %zu tp %d: group %d scheduled %d times", t, tp, g, sched[g]);
                     return 1;
                 }
             int prev = 1 << 30;
