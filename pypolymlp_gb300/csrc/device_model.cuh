@@ -463,14 +463,14 @@ __device__ __forceinline__ YlmDir<T> ylm_dir(T x, T y, T z, T r) {
     return d;
 }
 
-// Column m' = mp of Y_lm (keys (l, -mp), l = mp .. L, at row l(l+1)/2 + l - mp
-// of `rows`, 8 values per row: Y, dY/dx, dY/dy, dY/dz as (re, im)) for one
+// Column m' = mp of Y_lm (keys (l, -mp), l = mp .. L; key k = l(l+1)/2 + l - mp
+// at rows + ks k, 8 values: Y, dY/dx, dY/dy, dY/dz as (re, im)) for one
 // thread.  The same recursion and constants as warp_ylm (the normalised
 // associated Legendre recursion of polymlp_spherical_harmonics.cpp:27-209),
 // run down column mp, with the Q recursion of column mp + 1 in lock step for
 // the theta derivative, so that no (l, m) scratch table is needed.
 template <typename T>
-__device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, const YlmDir<T>& d, T* rows) {
+__device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, const YlmDir<T>& d, T* rows, int ks) {
     const T s2pi = (T)0.39894228040143267794;
     const T sq3 = (T)1.7320508075688772935, sq32 = (T)1.2247448713915890491;
     const T h = (T)0.5 * (T)1.41421356237309504880;
@@ -540,7 +540,7 @@ __device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, con
         q1 = q;
         n2 = n1;
         n1 = qn;
-        T* o = rows + 8 * (l * (l + 1) / 2 + l - mp);
+        T* o = rows + (size_t)ks * (l * (l + 1) / 2 + l - mp);
         if (mp == 0) {
             const T qv = (l == 0) ? (T)0 : qn;
             const T c0 = qv * st * invr * tab.D0[l];

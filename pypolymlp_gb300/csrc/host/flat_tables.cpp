@@ -263,9 +263,9 @@ FlatModel flatten_model(const ModelTables& mt) {
                             ft.head_nid[ft.ent_head[ft.ent_tp_off[(size_t)k * (ntp + 1) + tp]]];
                 };
                 for (size_t t = 0; t < bt.size(); ++t) {
-                    const int x = 64 * (int)(t / 32) + (int)(t % 32);
+                    const int x = 64 * (int)(t / 32) + 2 * (int)(t % 32);
                     place(bt[t][0], x);
-                    if (bt[t][1] >= 0) place(bt[t][1], x + 32);
+                    if (bt[t][1] >= 0) place(bt[t][1], x + 1);
                 }
                 for (size_t q = 0; q < rest[tp].size(); ++q) place(rest[tp][q], 64 * ngt + (int)q);
                 ft.tp_nnz[tp] = 64 * ngt;

@@ -65,7 +65,7 @@ struct FlatType {
     // sequence, and taken two at a time into bundles of two features with the
     // same key sequence (or one, when the next feature's keys differ), so that
     // one table row of a key serves both.  Bundle t = 32 g + l sits in group g,
-    // lane l: its features at positions 64 g + l and 64 g + 32 + l (holes,
+    // lane l: its features at positions 64 g + 2 l and 64 g + 2 l + 1 (holes,
     // tp_perm = -1, where a bundle has one feature or the group is not full).
     // The features without entries of tp follow at 64 n_g(tp) onwards, and
     // positions run to n_pos (all type pairs; a multiple of 4); tp_perm[tp][x]

@@ -524,6 +524,24 @@ __device__ __forceinline__ void load_row4(const double* p, double (&v)[4]) {
     v[3] = b.y;
 }
 
+// Two consecutive values at an 8- (FP32) or 16-byte (FP64) aligned address.
+__device__ __forceinline__ void load_pair(const float* p, float (&v)[2]) {
+    const float2 a = *reinterpret_cast<const float2*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+}
+__device__ __forceinline__ void load_pair(const double* p, double (&v)[2]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+}
+__device__ __forceinline__ void store_pair(float* p, const float (&v)[2]) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+}
+__device__ __forceinline__ void store_pair(double* p, const double (&v)[2]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
     pg_rows_pairs(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j, const double* nb_d,
@@ -541,9 +559,14 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
     const DevType& ty = M.types[t1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int NL = M.max_lin, NY = M.n_ylm, NF = M.n_fn_max, L = M.maxl;
-    T* tab = reinterpret_cast<T*>(smem_raw);  // [ps][NY][8]: Y, dY/dx, dY/dy, dY/dz (re, im)
-    T* rad = tab + (size_t)ps * NY * 8;       // [ps][NF][4]: f, f' x/r, f' y/r, f' z/r
-    T* geo = rad + (size_t)ps * NF * 4;       // [ps][4]: d_x, d_y, d_z
+    // Y_lm table [key][pair][8] (Y, dY/dx, dY/dy, dY/dz as re, im): the rows of
+    // the pairs of a step sit at fixed offsets from their key's row; the key
+    // stride is padded by 16 or 32 bytes so that lanes reading different keys
+    // of one pair hit different banks
+    const int KS = ps * 8 + 4;
+    T* tab = reinterpret_cast<T*>(smem_raw);  // [NY][KS]
+    T* rad = tab + (size_t)NY * KS;           // [ps][NF][4]: f, f' x/r, f' y/r, f' z/r
+    T* geo = rad + (size_t)ps * NF * 4;       // [ps][4]: d_x, d_y, d_z, 0 for an image of the centre (else 1)
     T* s_tab = geo + (size_t)ps * 4;
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     const long long p0 = nb_off[i], p1 = nb_off[i + 1];
@@ -598,7 +621,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                 geo[4 * p] = dx;
                 geo[4 * p + 1] = dy;
                 geo[4 * p + 2] = dz;
-                geo[4 * p + 3] = 0;
+                geo[4 * p + 3] = j == i ? (T)0 : (T)1;
                 const int step = p / NW * NW;
                 const bool last = q + 1 == p1 || nb_j[q + 1] != j;
                 const bool flush = last || p == min(step + NW, nsc) - 1;
@@ -632,7 +655,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
             }
             for (int p = threadIdx.x / tpp; p < nsc8; p += kRowsThreads / tpp) {
                 const int t = threadIdx.x - (threadIdx.x / tpp) * tpp;
-                T* rows = tab + (size_t)p * NY * 8;
+                T* rows = tab + (size_t)p * 8;
                 T dx = 0, dy = 0, dz = 0, dis = 1;
                 const bool ok = p < nsc && pair_geometry<T>(M, B, nb_d, p0 + ord[sc0 + p], dx, dy, dz, dis);
                 if (!M.gtinv) {
@@ -647,16 +670,16 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                         const int mp = side ? L - a : a;
                         if (side && mp == a) break;
                         if (ok) {
-                            ylm_column<T>(mp, L, ytab, dir, rows);
+                            ylm_column<T>(mp, L, ytab, dir, rows, KS);
                         } else {
                             for (int l = mp; l <= L; ++l)
-                                for (int v = 0; v < 8; ++v) rows[8 * (l * (l + 1) / 2 + l - mp) + v] = (T)0;
+                                for (int v = 0; v < 8; ++v) rows[(size_t)KS * (l * (l + 1) / 2 + l - mp) + v] = (T)0;
                         }
                     }
             }
             __syncthreads();
             // ---- contraction: warp = group of 32 bundles, lane = bundle (two
-            // features with the same keys, positions xa and xa + 32); the group's
+            // features with the same keys, positions xa and xa + 1); the group's
             // entries are read rank-major (coalesced) and one table row per pair
             // and rank serves both features
             const int ng = ty.n_groups;
@@ -667,16 +690,14 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                 const int grp = ty.lay_sched[((size_t)tp * ty.n_rounds + k) * NW + warp];
                 if (grp < 0) continue;
                 const int base = ty.lay_grp_base[tp * ng + grp], cnt = ty.lay_grp_cnt[tp * ng + grp];
-                const int xa = 64 * grp + lane;
-                const int nid[2] = {pos_nid[xa], pos_nid[xa + 32]};
+                const int xa = 64 * grp + 2 * lane;
+                const int nid0 = pos_nid[xa], nid1 = pos_nid[xa + 1];
                 // the DS sums of both features, over the super-chunk
-                T sv[2][9];
+                T sv[9][2];
 #pragma unroll
-                for (int f = 0; f < 2; ++f)
-#pragma unroll
-                    for (int v = 0; v < 9; ++v) sv[f][v] = ds[(size_t)v * npos + xa + 32 * f];
+                for (int v = 0; v < 9; ++v) load_pair(ds + (size_t)v * npos + xa, sv[v]);
                 for (int s0 = 0; s0 < nsc; s0 += NW) {
-                    const T* tab0 = tab + (size_t)s0 * NY * 8;
+                    const T* tab0 = tab + (size_t)s0 * 8;
                     // per pair and feature: T, S_x, S_y, S_z
                     T acc[NW][2][4];
 #pragma unroll
@@ -703,7 +724,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                             const int r = r0 + s;
                             if (r >= cnt) break;
                             const T are = ga[s].re, aim = -ga[s].im, bre = gb[s].re, bim = -gb[s].im;
-                            const T* row = tab0 + 8 * kq[s];
+                            const T* row = tab0 + (size_t)KS * kq[s];
                             if (r + kPrefetch < cnt) {
                                 const int sl = base + 64 * (r + kPrefetch) + lane;
                                 ga[s] = Gi[sl];
@@ -713,7 +734,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
 #pragma unroll
                             for (int w = 0; w < NW; ++w) {
                                 T v[8];
-                                load_row8(row + (size_t)w * NY * 8, v);
+                                load_row8(row + 8 * w, v);
 #pragma unroll
                                 for (int c = 0; c < 4; ++c) {
                                     acc[w][0][c] = fma(aim, v[2 * c + 1], fma(are, v[2 * c], acc[w][0][c]));
@@ -722,59 +743,59 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
                             }
                         }
                     }
-                    // ---- per feature of the bundle: derivatives, image sums, DS sums
+                    // ---- per pair: derivatives of both features, image sums, DS sums
+                    // (an out-of-range pair has a zero table: its terms vanish)
                     const int n = min(NW, nsc - s0);
+                    T run[3][2] = {{0, 0}, {0, 0}, {0, 0}};
 #pragma unroll
-                    for (int f = 0; f < 2; ++f) {
-                        const int x = xa + 32 * f;
-                        T run0 = 0, run1 = 0, run2 = 0;
+                    for (int w = 0; w < NW; ++w) {
+                        if (w >= n) break;
+                        const int pw = s0 + w;
+                        const int fl = s_flag[pw];
+                        T dg[4], r0v[4], r1v[4];
+                        load_row4(geo + 4 * pw, dg);
+                        load_row4(rad + ((size_t)pw * NF + nid0) * 4, r0v);
+                        load_row4(rad + ((size_t)pw * NF + nid1) * 4, r1v);
+                        T a[3][2];
 #pragma unroll
-                        for (int w = 0; w < NW; ++w) {
-                            if (w >= n) break;
-                            const int pw = s0 + w;
-                            const int fl = s_flag[pw];
-                            T rf[4], dg[4];
-                            load_row4(rad + ((size_t)pw * NF + nid[f]) * 4, rf);
-                            load_row4(geo + 4 * pw, dg);
-                            const T tk = acc[w][f][0];
-                            const T a0 = fma(rf[0], acc[w][f][1], rf[1] * tk);
-                            const T a1 = fma(rf[0], acc[w][f][2], rf[2] * tk);
-                            const T a2 = fma(rf[0], acc[w][f][3], rf[3] * tk);
-                            // (an out-of-range pair has a zero table: its terms vanish)
-                            if (!(fl & 2)) {
-                                sv[f][0] += a0;
-                                sv[f][1] += a1;
-                                sv[f][2] += a2;
-                            }
-                            sv[f][3] = fma(dg[0], a0, sv[f][3]);
-                            sv[f][4] = fma(dg[1], a1, sv[f][4]);
-                            sv[f][5] = fma(dg[2], a2, sv[f][5]);
-                            sv[f][6] = fma(dg[1], a0, sv[f][6]);
-                            sv[f][7] = fma(dg[2], a1, sv[f][7]);
-                            sv[f][8] = fma(dg[0], a2, sv[f][8]);
-                            run0 += a0;
-                            run1 += a1;
-                            run2 += a2;
-                            if (fl & 4) {
-                                T* o = Dp + (size_t)s_slot[pw] * 3 * NL + x;
+                        for (int c = 0; c < 3; ++c) {
+                            a[c][0] = fma(r0v[0], acc[w][0][1 + c], r0v[1 + c] * acc[w][0][0]);
+                            a[c][1] = fma(r1v[0], acc[w][1][1 + c], r1v[1 + c] * acc[w][1][0]);
+                        }
+#pragma unroll
+                        for (int f = 0; f < 2; ++f) {
+                            sv[0][f] = fma(dg[3], a[0][f], sv[0][f]);
+                            sv[1][f] = fma(dg[3], a[1][f], sv[1][f]);
+                            sv[2][f] = fma(dg[3], a[2][f], sv[2][f]);
+                            sv[3][f] = fma(dg[0], a[0][f], sv[3][f]);
+                            sv[4][f] = fma(dg[1], a[1][f], sv[4][f]);
+                            sv[5][f] = fma(dg[2], a[2][f], sv[5][f]);
+                            sv[6][f] = fma(dg[1], a[0][f], sv[6][f]);
+                            sv[7][f] = fma(dg[2], a[1][f], sv[7][f]);
+                            sv[8][f] = fma(dg[0], a[2][f], sv[8][f]);
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) run[c][f] += a[c][f];
+                        }
+                        if (fl & 4) {
+                            T* o = Dp + (size_t)s_slot[pw] * 3 * NL + xa;
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) {
                                 if (fl & 8) {
-                                    o[0] = run0;
-                                    o[NL] = run1;
-                                    o[2 * NL] = run2;
+                                    store_pair(o + (size_t)c * NL, run[c]);
                                 } else {
-                                    o[0] += run0;
-                                    o[NL] += run1;
-                                    o[2 * NL] += run2;
+                                    T old[2];
+                                    load_pair(o + (size_t)c * NL, old);
+                                    old[0] += run[c][0];
+                                    old[1] += run[c][1];
+                                    store_pair(o + (size_t)c * NL, old);
                                 }
-                                run0 = run1 = run2 = 0;
+                                run[c][0] = run[c][1] = (T)0;
                             }
                         }
                     }
                 }
 #pragma unroll
-                for (int f = 0; f < 2; ++f)
-#pragma unroll
-                    for (int v = 0; v < 9; ++v) ds[(size_t)v * npos + xa + 32 * f] = sv[f][v];
+                for (int v = 0; v < 9; ++v) store_pair(ds + (size_t)v * npos + xa, sv[v]);
             }
             __syncthreads();
         }
@@ -1229,7 +1250,7 @@ int rows_pairs_chunk(const DevModel& M, bool fp64) {
 
 size_t rows_pairs_smem_bytes(const DevModel& M, bool fp64, int ps) {
     const size_t ts = fp64 ? 8 : 4;
-    return (size_t)ps * M.n_ylm * 8 * ts + (size_t)ps * M.n_fn_max * 4 * ts + (size_t)ps * 4 * ts +
+    return (size_t)M.n_ylm * (ps * 8 + 4) * ts + (size_t)ps * M.n_fn_max * 4 * ts + (size_t)ps * 4 * ts +
            (size_t)ylm_table_size(M.n_ylm, M.maxl) * ts;
 }
 

@@ -1,7 +1,7 @@
 // Invariants of the host-built X-row layout tables (flat_tables.cpp), checked on
 // the CPU by tests/test_layout_tables.py: tp_perm and tp_ipos are inverse (holes
 // aside); the features with entries of a type pair sit below tp_nnz, in bundles
-// (positions 64g + l and 64g + 32 + l) of equal key sequences, with entry counts
+// (positions 64g + 2l and 64g + 2l + 1) of equal key sequences, with entry counts
 // non-increasing in bundle order; all entries of a feature by one type pair name
 // one radial function, tp_pos_nid at its position; slots hold the r-th entries
 // of their features and name the key of lane l's first feature, or lane 0's
@@ -92,7 +92,7 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
                     return 1;
                 }
                 for (int l = 0; l < 32; ++l) {
-                    const int ka = perm[64 * g + l], kb = perm[64 * g + 32 + l];
+                    const int ka = perm[64 * g + 2 * l], kb = perm[64 * g + 2 * l + 1];
                     if (kb >= 0 && (ka < 0 || cnt(ka) != cnt(kb))) {
                         snprintf(msg, n_msg, "type %zu tp %d group %d lane %d: bundle partner unlike", t, tp, g, l);
                         return 1;
@@ -115,7 +115,7 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
                     std::set<int> keys;
                     for (int h = 0; h < 2; ++h)
                         for (int l = 0; l < 32; ++l) {
-                            const int k = perm[64 * g + 32 * h + l], ka = perm[64 * g + l];
+                            const int k = perm[64 * g + 2 * l + h], ka = perm[64 * g + 2 * l];
                             const int e = ft.lay_ent[s0 + 32 * h + l];
                             const int want_e = r < cnt(k) ? e0(k) + r : -1;
                             if (e != want_e) {
