@@ -63,6 +63,7 @@
 #include <mutex>
 #include <vector>
 
+#include "async.cuh"
 #include "kernels.h"
 
 namespace pg {
@@ -77,46 +78,10 @@ constexpr int kTcThreads = 320;
 constexpr int kTcEpiThreads = 256;
 constexpr uint32_t kTcOpBytes = kTcTile * kTcK * 2;   // 8 KB per operand (slice x 128 features x 32 rows)
 constexpr uint32_t kTcStageBytes = 2 * kTcSlices * kTcOpBytes;  // 64 KB per stage
-constexpr long long kTcWaitCycles = 4000000000LL;     // about 2 s at 2 GHz
 constexpr size_t kTcSmem = (size_t)kTcStages * kTcStageBytes + 1024;
 constexpr int kTcSplitThreads = 256;                  // pg_split_fx4: 4 rows per thread
 
 // ---------------------------------------------------------------- helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t a) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Wait for the phase of the given parity; false on abort or after the deadline.
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_flag) {
-    const long long t0 = clock64();
-    while (!mbar_try(a, parity)) {
-        if (*abort_flag) return false;
-        if (clock64() - t0 > kTcWaitCycles) {
-            *abort_flag = 1;
-            return false;
-        }
-    }
-    return true;
-}
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t mbar) {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
@@ -269,7 +234,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         mbar_init(smem_u32(&accf_bar), 1);
         mbar_init(smem_u32(&acce_bar), kTcEpiThreads);
         mbar_init(smem_u32(&done_bar), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),

@@ -899,6 +899,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
     // first pair, so a group that crosses a segment is taken in the first one
     constexpr int kSeg = 2048;
     __shared__ int s_list[kSeg];
+    __shared__ long long s_doff[kSeg];  // d_off of each group's centre (its features weight the product columns)
     __shared__ int s_wcnt[kRowsThreads / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int tc = 0; tc < M.n_type; ++tc) {
@@ -915,8 +916,9 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
             for (long long w0 = sb; w0 < se; w0 += blockDim.x) {
                 const long long q = w0 + threadIdx.x;
                 bool head = false;
+                int gi = 0;
                 if (q < se) {
-                    const int gi = nb_j[q];
+                    gi = nb_j[q];
                     head = gi != gj && (q == q0 || nb_j[q - 1] != gi) && B.types[gi] == tc;
                 }
                 const unsigned m = __ballot_sync(0xffffffffu, head);
@@ -927,7 +929,11 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                     before += w < warp ? s_wcnt[w] : 0;
                     total += s_wcnt[w];
                 }
-                if (head) s_list[n + before + __popc(m & ((1u << lane) - 1u))] = (int)(q - sb);
+                if (head) {
+                    const int k = n + before + __popc(m & ((1u << lane) - 1u));
+                    s_list[k] = (int)(q - sb);
+                    s_doff[k] = d_off[gi];
+                }
                 n += total;
                 __syncthreads();
             }
@@ -959,7 +965,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                             for (int m = 0; m < S; ++m) acc[m][c] += v[m];
                         }
                     }
-                    if (has_pc) prod_col_add(pc, src, D + d_off[nb_j[q]], NL, pv);
+                    if (has_pc) prod_col_add(pc, src, D + s_doff[k], NL, pv);
                 }
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
@@ -985,7 +991,7 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
                 T v[3] = {0, 0, 0};
                 for (int k = 0; k < n; ++k) {
                     const long long q = sb + s_list[k];
-                    prod_col_add(pc, Dp + (size_t)q * 3 * NL, D + d_off[nb_j[q]], NL, v);
+                    prod_col_add(pc, Dp + (size_t)q * 3 * NL, D + s_doff[k], NL, v);
                 }
                 T* o = X + (size_t)pc.col * ld + r0;
                 o[0] -= v[0];
