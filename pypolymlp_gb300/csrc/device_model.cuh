@@ -464,12 +464,13 @@ __device__ __forceinline__ YlmDir<T> ylm_dir(T x, T y, T z, T r) {
 }
 
 // Column m' = mp of Y_lm (keys (l, -mp), l = mp .. L; key k = l(l+1)/2 + l - mp
-// at rows + ks k, 8 values: Y, dY/dx, dY/dy, dY/dz as (re, im)) for one
-// thread.  The same recursion and constants as warp_ylm (the normalised
-// associated Legendre recursion of polymlp_spherical_harmonics.cpp:27-209),
-// run down column mp, with the Q recursion of column mp + 1 in lock step for
-// the theta derivative, so that no (l, m) scratch table is needed.
-template <typename T>
+// at rows + ks k: with DERIV 8 values, Y, dY/dx, dY/dy, dY/dz as (re, im);
+// else Y alone) for one thread.  The same recursion and constants as warp_ylm
+// (the normalised associated Legendre recursion of
+// polymlp_spherical_harmonics.cpp:27-209), run down column mp, with the Q
+// recursion of column mp + 1 in lock step for the theta derivative, so that
+// no (l, m) scratch table is needed.
+template <typename T, bool DERIV = true>
 __device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, const YlmDir<T>& d, T* rows, int ks) {
     const T s2pi = (T)0.39894228040143267794;
     const T sq3 = (T)1.7320508075688772935, sq32 = (T)1.2247448713915890491;
@@ -541,6 +542,12 @@ __device__ __noinline__ void ylm_column(int mp, int L, const YlmTab<T>& tab, con
         n2 = n1;
         n1 = qn;
         T* o = rows + (size_t)ks * (l * (l + 1) / 2 + l - mp);
+        if (!DERIV) {
+            const T tmp = mp == 0 ? p * h : sign * p * h;
+            o[0] = mp == 0 ? tmp : tmp * cs;
+            o[1] = mp == 0 ? (T)0 : -(tmp * sn);
+            continue;
+        }
         if (mp == 0) {
             const T qv = (l == 0) ? (T)0 : qn;
             const T c0 = qv * st * invr * tab.D0[l];

@@ -283,35 +283,39 @@ __global__ void pg_nb_refresh(DevBatch B, const long long* offsets, const long l
 
 // ---------------------------------------------------------------- K2 a_nlm
 // Block per centre atom, pairs taken one type pair at a time: the pairs of
-// that type pair are compacted into a list (256 at a time), warps compute the
-// basis of one pair each (8 pairs per chunk), then every thread adds the
-// chunk's fn * Y into the heads of that type pair it owns: a partial sum over
-// the chunk in T, added to the FP64 total once per chunk.
+// that type pair are compacted into a list (256 at a time) and taken up to 32
+// at a time (a super-chunk).  The block builds their bases at once into
+// shared memory (thread = pair and two Legendre columns, ylm_column, or pair
+// and radial functions): Y_lm [pair][key] and f_n [pair][n].  Then every
+// thread adds f_n Y_lm over the super-chunk's pairs into the heads of that
+// type pair it owns: partial sums over 8 pairs in T, each added to the long
+// (FP64, or float-float) total.
+constexpr int kAnlmChunk = 32;  // pairs per a_nlm super-chunk
 template <typename T>
 __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const long long* nb_off, const int* nb_j,
                                                const double* nb_d, const long long* a_off, cplx<T>* A) {
-    constexpr int NW = 8;
+    constexpr int NW = 8, PS = kAnlmChunk, TPP = 256 / PS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int s_list[256], s_wcnt[NW], s_ok[NW];
+    __shared__ int s_list[256], s_wcnt[NW];
     const int i = blockIdx.x;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    T* sb = reinterpret_cast<T*>(smem_raw);
+    const int NY = M.n_ylm, NF = M.n_fn_max, L = M.maxl;
     // per head: running sums of the real and imaginary parts (16 bytes)
-    LongSum<T>* acc = reinterpret_cast<LongSum<T>*>(
-        (reinterpret_cast<uintptr_t>(sb + slot * NW) + 15) & ~uintptr_t(15));
-    T* s_tab = reinterpret_cast<T*>(acc + 2 * (size_t)ty.K0);
+    LongSum<T>* acc = reinterpret_cast<LongSum<T>*>(smem_raw);
+    cplx<T>* Yt = reinterpret_cast<cplx<T>*>(acc + 2 * (size_t)ty.K0);  // [PS][NY]
+    T* rad = reinterpret_cast<T*>(Yt + (size_t)PS * NY);                // [PS][NF]
+    T* s_tab = rad + (size_t)PS * NF;
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
     for (int h = threadIdx.x; h < 2 * ty.K0; h += blockDim.x) acc[h] = LongSum<T>();
     const long long p0 = nb_off[i];
     const int np = (int)(nb_off[i + 1] - p0);
-    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
     for (int tp = 0; tp < M.n_tp; ++tp) {
         const int q0 = ty.tp_head_off[tp], nh = ty.tp_head_off[tp + 1] - q0;
         if (nh == 0) continue;  // the type pair is not one of this centre type's
+        const int nfn = M.tp_nfn[tp];
         for (int r0 = 0; r0 < np; r0 += 256) {
             // compact the pairs of tp among r0 .. r0 + 255, in list order
             const int r = r0 + threadIdx.x;
@@ -326,38 +330,56 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
             }
             if (f) s_list[before + __popc(m & ((1u << lane) - 1u))] = r;
             __syncthreads();
-            for (int k0 = 0; k0 < c; k0 += NW) {
-                const int n = min(NW, c - k0);
-                if (warp < n) {
-                    const long long k = p0 + s_list[k0 + warp];
-                    T dx, dy, dz, dis;
-                    const bool ok = pair_geometry<T>(M, B, nb_d, k, dx, dy, dz, dis);
-                    if (lane == 0) s_ok[warp] = ok;
-                    if (ok) {
-                        warp_radial<T, false>(M, tp, dis, bv, lane);
-                        if (M.gtinv) {
-                            warp_ylm<T, false>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
-                        } else if (lane == 0) {
-                            bv.Y[0] = {(T)1, (T)0};
-                        }
+            for (int k0 = 0; k0 < c; k0 += PS) {
+                const int n = min(PS, c - k0);
+                // bases: thread t of pair p builds Legendre columns (a, L - a) for
+                // a = t, t + TPP, .. (2a <= L), then radial functions t, t + TPP, ..
+                {
+                    const int p = threadIdx.x / TPP, t = threadIdx.x % TPP;
+                    T dx = 0, dy = 0, dz = 0, dis = 1;
+                    const bool ok = p < n && pair_geometry<T>(M, B, nb_d, p0 + s_list[k0 + p], dx, dy, dz, dis);
+                    T* rows = reinterpret_cast<T*>(Yt + (size_t)p * NY);
+                    if (M.gtinv) {
+                        const YlmDir<T> dir = ylm_dir<T>(dx, dy, dz, dis);
+                        for (int a = t; 2 * a <= L; a += TPP)
+                            for (int side = 0; side < 2; ++side) {
+                                const int mp = side ? L - a : a;
+                                if (side && mp == a) break;
+                                if (ok) {
+                                    ylm_column<T, false>(mp, L, tab, dir, rows, 2);
+                                } else {
+                                    for (int l = mp; l <= L; ++l) {
+                                        rows[2 * (l * (l + 1) / 2 + l - mp)] = (T)0;
+                                        rows[2 * (l * (l + 1) / 2 + l - mp) + 1] = (T)0;
+                                    }
+                                }
+                            }
+                    } else if (t == 0) {
+                        rows[0] = ok ? (T)1 : (T)0;
+                        rows[1] = (T)0;
+                    }
+                    for (int q = t; q < nfn; q += TPP) {
+                        T fn = 0, fnd;
+                        if (ok) radial_one<T>(M, tp, q, dis, fn, fnd);
+                        rad[p * NF + q] = fn;
                     }
                 }
                 __syncthreads();
                 for (int q = threadIdx.x; q < nh; q += blockDim.x) {
                     const int h = ty.tp_heads[q0 + q];
                     const int nid = ty.head_nid[h], key = ty.head_key[h];
-                    T px = 0, py = 0;
-                    for (int w = 0; w < n; ++w) {
-                        if (!s_ok[w]) continue;
-                        BasisView<T> v = basis_view<T>(sb + slot * w, M.n_fn_max, M.n_ylm, M.maxl);
-                        const T fw = v.fn[nid];
-                        if (!(fw >= (T)1e-20)) continue;
-                        const cplx<T> y = v.Y[key];
-                        px += fw * y.re;
-                        py += fw * y.im;
+                    for (int w0 = 0; w0 < n; w0 += 8) {
+                        T px = 0, py = 0;
+                        for (int w = w0; w < min(n, w0 + 8); ++w) {
+                            const T fw = rad[w * NF + nid];
+                            if (!(fw >= (T)1e-20)) continue;
+                            const cplx<T> y = Yt[(size_t)w * NY + key];
+                            px += fw * y.re;
+                            py += fw * y.im;
+                        }
+                        acc[2 * h].add(px);
+                        acc[2 * h + 1].add(py);
                     }
-                    acc[2 * h].add(px);
-                    acc[2 * h + 1].add(py);
                 }
                 __syncthreads();
             }
@@ -1227,10 +1249,9 @@ void launch_nb_refresh(const DevBatch& B, const long long* off, const long long*
 template <typename T>
 void launch_anlm(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j, const double* nb_d,
                  const long long* a_off, void* A, int max_k0, cudaStream_t st) {
-    const int threads = 256, nw = threads / 32;
-    const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    const size_t smem = slot * nw * sizeof(T) + 16 + (size_t)max_k0 * sizeof(double2) +
-                        ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
+    const int threads = 256;
+    const size_t smem = (size_t)max_k0 * 2 * sizeof(LongSum<T>) + (size_t)kAnlmChunk * M.n_ylm * sizeof(cplx<T>) +
+                        (size_t)kAnlmChunk * M.n_fn_max * sizeof(T) + ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
     PG_CUDA(cudaFuncSetAttribute(pg_anlm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pg_anlm<T><<<B.n_atoms, threads, smem, st>>>(M, B, nb_off, nb_j, nb_d, a_off, reinterpret_cast<cplx<T>*>(A));
 }
