@@ -174,6 +174,21 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         } else {
             d.tcoef = up(std::vector<float>(tcoef.begin(), tcoef.end()));
         }
+        // feature-value terms in the same packed form (feature k owns val_off[k] ..)
+        std::vector<int4> vcode;
+        std::vector<double> vcoef;
+        for (const FlatTerm& t : ft.val_terms) {
+            int id[6] = {0, 0, 0, 0, 0, 0};
+            for (int r = 0; r < t.n; ++r) id[r] = t.ids[r];
+            vcode.push_back(make_int4(id[0] | (id[1] << 16), id[2] | (id[3] << 16), id[4] | (id[5] << 16), t.n));
+            vcoef.push_back(t.coeff);
+        }
+        d.vcode = (const int4*)up(vcode);
+        if (fp64) {
+            d.vcoef = up(vcoef);
+        } else {
+            d.vcoef = up(std::vector<float>(vcoef.begin(), vcoef.end()));
+        }
     }
 }
 

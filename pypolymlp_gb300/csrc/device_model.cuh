@@ -82,6 +82,9 @@ struct DevType {
     const int* slot_toff;
     const int4* tcode;
     const void* tcoef;
+    // feature-value terms packed like tcode (val_off order), coefficients in T
+    const int4* vcode;
+    const void* vcoef;
 };
 
 // Feature values d_k = sum_q coeff_q Re(prod a[ids_q]) of one centre, one
@@ -114,9 +117,13 @@ __device__ __forceinline__ void warp_feature_values(const DevType& ty, const cpl
 
 // Product of the a ids of a packed term (ids 16 bits each, two per word in x,
 // y, z; n in the low byte of w), in the order of term_product.
+// Products of two and three factors (nearly all terms of the gtinv models up
+// to order 4) take their own short paths.
 template <typename T>
 __device__ __forceinline__ cplx<T> packed_term_product(const int4 c4, const cplx<T>* a) {
     const int n = c4.w & 0xff;
+    if (n == 2) return cmul(a[c4.x & 0xffff], a[(c4.x >> 16) & 0xffff]);
+    if (n == 3) return cmul(cmul(a[c4.x & 0xffff], a[(c4.x >> 16) & 0xffff]), a[c4.y & 0xffff]);
     const int id[6] = {c4.x & 0xffff, (c4.x >> 16) & 0xffff, c4.y & 0xffff,
                        (c4.y >> 16) & 0xffff, c4.z & 0xffff, (c4.z >> 16) & 0xffff};
     cplx<T> p = {(T)1, (T)0};

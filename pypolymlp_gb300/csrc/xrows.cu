@@ -390,23 +390,60 @@ __global__ void __launch_bounds__(256) pg_anlm(DevModel M, DevBatch B, const lon
 }
 
 // ----------------------------------------------- K4 features and adjoint G
+// Block per centre.  Windowed warp sums: a warp evaluates kAdjWin terms of its
+// 32 outputs at a time (all lanes, whatever output a term belongs to; the
+// packed codes and coefficients of the window are requested together, so that
+// their L2 latency overlaps), then each lane adds its own output's terms from
+// the window, in list order.  (A rank of 32 adjoint slots holds about 130
+// terms in the binary l_max 8 model: 128-term windows in FP32; the FP64 kernel,
+// with its slower products, gains from 256.)
 template <typename T>
-__global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_off, const cplx<T>* A,
-                                    const long long* d_off, T* D, const long long* g_off, cplx<T>* G) {
+constexpr int adj_win() { return sizeof(T) == 4 ? 128 : 256; }
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) pg_features_adjoint(DevModel M, DevBatch B, const long long* a_off,
+                                                           const cplx<T>* A, const long long* d_off, T* D,
+                                                           const long long* g_off, cplx<T>* G) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NW = 8, kWin = adj_win<T>(), kU = kWin / 32;
     const int i = blockIdx.x;
     const int t1 = B.types[i];
     const DevType& ty = M.types[t1];
     cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw);
+    cplx<T>* s_v = a + ty.K;  // [NW][kWin]
     load_full_a<T>(ty, A + a_off[i], a);
     __syncthreads();
-    // windowed warp sums (see kTermWin): feature values, then adjoint entries
-    constexpr int NW = 8, kWin = kTermWin;
-    __shared__ cplx<T> s_v[NW][kWin];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    warp_feature_values<T>(ty, a, D + d_off[i], s_v[warp], warp, NW, lane);
-    // adjoint entries in the X-row layout (rank-major groups of 32 features
-    // per type pair; padding slots hold zero), warp per rank of 32 slots
+    cplx<T>* win = s_v + (size_t)warp * kWin;
+    // feature values d_k = sum_q coeff_q Re(prod a[ids_q])
+    const int nl = ty.n_lin;
+    const T* vcoef = reinterpret_cast<const T*>(ty.vcoef);
+    T* Di = D + d_off[i];
+    for (int k0 = 32 * warp; k0 < nl; k0 += 32 * NW) {
+        const int k = k0 + lane;
+        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, nl)];
+        const int ms = k < nl ? ty.val_off[k] : te, me = k < nl ? ty.val_off[k + 1] : te;
+        T v = 0;
+        for (int w0 = tb; w0 < te; w0 += kWin) {
+            int4 c4[kU];
+            T cf[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int t = min(w0 + 32 * u + lane, te - 1);
+                c4[u] = ty.vcode[t];
+                cf[u] = vcoef[t];
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (w0 + 32 * u + lane < te) win[32 * u + lane].re = cf[u] * packed_term_product<T>(c4[u], a).re;
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kWin);
+            for (int t = lo; t < hi; ++t) v += win[t - w0].re;
+            __syncwarp();
+        }
+        if (k < nl) Di[k] = v;
+    }
+    // adjoint entries in the X-row layout (rank-major groups of bundles per
+    // type pair; padding slots hold zero), warp per rank of 32 slots
     cplx<T>* Gi = G + g_off[i];
     const T* coef = reinterpret_cast<const T*>(ty.tcoef);
     for (int rk = warp; rk < ty.lay_size / 32; rk += NW) {
@@ -415,22 +452,26 @@ __global__ void pg_features_adjoint(DevModel M, DevBatch B, const long long* a_o
         const int ms = ty.slot_toff[slot], me = ty.slot_toff[slot + 1];
         cplx<T> g = {(T)0, (T)0};
         for (int w0 = tb; w0 < te; w0 += kWin) {
+            int4 c4[kU];
+            T cf[kU];
 #pragma unroll
-            for (int u = 0; u < kWin / 32; ++u) {
-                const int t = w0 + 32 * u + lane;
-                if (t < te) {
-                    const int4 c4 = ty.tcode[t];
-                    const T cf = coef[t];
-                    const cplx<T> p = packed_term_product<T>(c4, a);
-                    cplx<T> v = {cf * p.re, cf * p.im};
-                    if (c4.w >> 8) v.im = -v.im;
-                    s_v[warp][32 * u + lane] = v;
-                }
+            for (int u = 0; u < kU; ++u) {
+                const int t = min(w0 + 32 * u + lane, te - 1);
+                c4[u] = ty.tcode[t];
+                cf[u] = coef[t];
             }
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (w0 + 32 * u + lane < te) {
+                    const cplx<T> p = packed_term_product<T>(c4[u], a);
+                    cplx<T> v = {cf[u] * p.re, cf[u] * p.im};
+                    if (c4[u].w >> 8) v.im = -v.im;
+                    win[32 * u + lane] = v;
+                }
             __syncwarp();
             const int lo = max(ms, w0), hi = min(me, w0 + kWin);
             for (int t = lo; t < hi; ++t) {
-                const cplx<T> v = s_v[warp][t - w0];
+                const cplx<T> v = win[t - w0];
                 g.re += v.re;
                 g.im += v.im;
             }
@@ -631,73 +672,83 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
         for (int sc0 = s_tpoff[tp]; sc0 < r_end; sc0 += ps) {
             const int nsc = min(ps, r_end - sc0);
             const int nsc8 = (nsc + NW - 1) / NW * NW;  // whole contraction steps; pairs past nsc are zero
-            // ---- bases of the super-chunk; pair flags: per step of NW pairs, the
-            // running image sums are stored at a group's last image or the step's
-            // end ("flush"), and stored rather than added when the group's first
-            // image is in this step ("fresh"; runs of images are contiguous)
-            for (int p = threadIdx.x; p < nsc; p += blockDim.x) {
-                const long long q = p0 + ord[sc0 + p];
-                T dx, dy, dz, dis;
-                const bool ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
-                const int j = nb_j[q];
-                geo[4 * p] = dx;
-                geo[4 * p + 1] = dy;
-                geo[4 * p + 2] = dz;
-                geo[4 * p + 3] = j == i ? (T)0 : (T)1;
-                const int step = p / NW * NW;
-                const bool last = q + 1 == p1 || nb_j[q + 1] != j;
-                const bool flush = last || p == min(step + NW, nsc) - 1;
-                bool fresh = false;
-                for (int v = p; v >= step; --v) {
-                    const long long qv = p0 + ord[sc0 + v];
-                    if (qv == p0 || nb_j[qv - 1] != nb_j[qv]) {
-                        fresh = true;
-                        break;
-                    }
-                }
-                s_flag[p] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (flush ? 4 : 0) | (fresh ? 8 : 0);
-                s_slot[p] = gslot[q];
-            }
-            for (int it = threadIdx.x; it < nsc8 * nfn; it += blockDim.x) {
-                const int p = it / nfn, n = it - p * nfn;
-                T* o = rad + ((size_t)p * NF + n) * 4;
+            // ---- bases of the super-chunk, thread t of pair p (tpp threads a pair):
+            // threads 0 .. ny-1 build Legendre columns (a, L - a), a = t, t + tpp,
+            // .. (2a <= L); the others the radial functions and the pair's flags.
+            // Per step of NW pairs, the running image sums are stored at a
+            // group's last image or the step's end ("flush"), and stored rather
+            // than added when the group's first image is in this step ("fresh";
+            // runs of images are contiguous).
+            {
+                const int p = threadIdx.x / tpp, t = threadIdx.x - (threadIdx.x / tpp) * tpp;
+                const int ny = M.gtinv ? min(tpp, L / 2 + 1) : 1;
+                const int nfree = tpp - ny;
                 T dx = 0, dy = 0, dz = 0, dis = 1;
-                const bool ok = p < nsc && pair_geometry<T>(M, B, nb_d, p0 + ord[sc0 + p], dx, dy, dz, dis);
-                if (ok) {
-                    T f, fd;
-                    radial_one<T>(M, tp, n, dis, f, fd);
-                    const T invr = (T)1 / dis;
-                    o[0] = f;
-                    o[1] = fd * (dx * invr);
-                    o[2] = fd * (dy * invr);
-                    o[3] = fd * (dz * invr);
-                } else {
-                    o[0] = o[1] = o[2] = o[3] = (T)0;
+                bool ok = false;
+                long long q = p0;
+                if (p < nsc) {
+                    q = p0 + ord[sc0 + p];
+                    ok = pair_geometry<T>(M, B, nb_d, q, dx, dy, dz, dis);
                 }
-            }
-            for (int p = threadIdx.x / tpp; p < nsc8; p += kRowsThreads / tpp) {
-                const int t = threadIdx.x - (threadIdx.x / tpp) * tpp;
-                T* rows = tab + (size_t)p * 8;
-                T dx = 0, dy = 0, dz = 0, dis = 1;
-                const bool ok = p < nsc && pair_geometry<T>(M, B, nb_d, p0 + ord[sc0 + p], dx, dy, dz, dis);
-                if (!M.gtinv) {
-                    if (t == 0)
-                        for (int v = 0; v < 8; ++v) rows[v] = (v == 0 && ok) ? (T)1 : (T)0;
-                    continue;
-                }
-                const YlmDir<T> dir = ylm_dir<T>(dx, dy, dz, dis);
-                // columns a and L - a: about (L + 2) / 2 keys per thread
-                for (int a = t; 2 * a <= L; a += tpp)
-                    for (int side = 0; side < 2; ++side) {
-                        const int mp = side ? L - a : a;
-                        if (side && mp == a) break;
-                        if (ok) {
-                            ylm_column<T>(mp, L, ytab, dir, rows, KS);
-                        } else {
-                            for (int l = mp; l <= L; ++l)
-                                for (int v = 0; v < 8; ++v) rows[(size_t)KS * (l * (l + 1) / 2 + l - mp) + v] = (T)0;
+                if (p < nsc && t == tpp - 1) {
+                    const int j = nb_j[q];
+                    geo[4 * p] = dx;
+                    geo[4 * p + 1] = dy;
+                    geo[4 * p + 2] = dz;
+                    geo[4 * p + 3] = j == i ? (T)0 : (T)1;
+                    const int step = p / NW * NW;
+                    const bool last = q + 1 == p1 || nb_j[q + 1] != j;
+                    const bool flush = last || p == min(step + NW, nsc) - 1;
+                    bool fresh = false;
+                    for (int v = p; v >= step; --v) {
+                        const long long qv = p0 + ord[sc0 + v];
+                        if (qv == p0 || nb_j[qv - 1] != nb_j[qv]) {
+                            fresh = true;
+                            break;
                         }
                     }
+                    s_flag[p] = (ok ? 1 : 0) | (j == i ? 2 : 0) | (flush ? 4 : 0) | (fresh ? 8 : 0);
+                    s_slot[p] = gslot[q];
+                }
+                if (p < nsc8) {
+                    T* rows = tab + (size_t)p * 8;
+                    if (!M.gtinv) {
+                        if (t == 0)
+                            for (int v = 0; v < 8; ++v) rows[v] = (v == 0 && ok) ? (T)1 : (T)0;
+                    } else if (t < ny) {
+                        const YlmDir<T> dir = ylm_dir<T>(dx, dy, dz, dis);
+                        for (int a = t; 2 * a <= L; a += ny)
+                            for (int side = 0; side < 2; ++side) {
+                                const int mp = side ? L - a : a;
+                                if (side && mp == a) break;
+                                if (ok) {
+                                    ylm_column<T>(mp, L, ytab, dir, rows, KS);
+                                } else {
+                                    for (int l = mp; l <= L; ++l)
+                                        for (int v = 0; v < 8; ++v) rows[(size_t)KS * (l * (l + 1) / 2 + l - mp) + v] = (T)0;
+                                }
+                            }
+                    }
+                    // radial functions n of this thread: the free threads share them
+                    // (all threads when none is free)
+                    const int r0t = nfree > 0 ? t - ny : t, rstep = nfree > 0 ? nfree : tpp;
+                    if (r0t >= 0) {
+                        const T invr = (T)1 / dis;
+                        for (int n = r0t; n < nfn; n += rstep) {
+                            T* o = rad + ((size_t)p * NF + n) * 4;
+                            if (ok) {
+                                T f, fd;
+                                radial_one<T>(M, tp, n, dis, f, fd);
+                                o[0] = f;
+                                o[1] = fd * (dx * invr);
+                                o[2] = fd * (dy * invr);
+                                o[3] = fd * (dz * invr);
+                            } else {
+                                o[0] = o[1] = o[2] = o[3] = (T)0;
+                            }
+                        }
+                    }
+                }
             }
             __syncthreads();
             // ---- contraction: warp = group of 32 bundles, lane = bundle (two
@@ -1260,7 +1311,7 @@ template <typename T>
 void launch_features_adjoint(const DevModel& M, const DevBatch& B, const long long* a_off, const void* A,
                              const long long* d_off, T* D, const long long* g_off, void* G, int max_k,
                              cudaStream_t st) {
-    const size_t smem = (size_t)max_k * sizeof(cplx<T>);
+    const size_t smem = ((size_t)max_k + 8 * adj_win<T>()) * sizeof(cplx<T>);
     PG_CUDA(cudaFuncSetAttribute(pg_features_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pg_features_adjoint<T><<<B.n_atoms, 256, smem, st>>>(M, B, a_off, reinterpret_cast<const cplx<T>*>(A), d_off, D, g_off,
                                                          reinterpret_cast<cplx<T>*>(G));
