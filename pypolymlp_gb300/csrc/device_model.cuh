@@ -87,34 +87,6 @@ struct DevType {
     const void* vcoef;
 };
 
-// Feature values d_k = sum_q coeff_q Re(prod a[ids_q]) of one centre, one
-// warp per 32 consecutive features (windowed warp sums over val_terms).
-template <typename T>
-__device__ __forceinline__ void warp_feature_values(const DevType& ty, const cplx<T>* a, T* out, cplx<T>* s_v,
-                                                    int warp, int n_warps, int lane) {
-    for (int k0 = 32 * warp; k0 < ty.n_lin; k0 += 32 * n_warps) {
-        const int k = k0 + lane;
-        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, ty.n_lin)];
-        const int ms = k < ty.n_lin ? ty.val_off[k] : te, me = k < ty.n_lin ? ty.val_off[k + 1] : te;
-        T v = 0;
-        for (int w0 = tb; w0 < te; w0 += kTermWin) {
-#pragma unroll
-            for (int u = 0; u < kTermWin / 32; ++u) {
-                const int t = w0 + 32 * u + lane;
-                if (t < te) {
-                    const FlatTerm& f = ty.val_terms[t];
-                    s_v[32 * u + lane].re = (T)f.coeff * term_product_real<T>(f, a);
-                }
-            }
-            __syncwarp();
-            const int lo = max(ms, w0), hi = min(me, w0 + kTermWin);
-            for (int t = lo; t < hi; ++t) v += s_v[t - w0].re;
-            __syncwarp();
-        }
-        if (k < ty.n_lin) out[k] = v;
-    }
-}
-
 // Product of the a ids of a packed term (ids 16 bits each, two per word in x,
 // y, z; n in the low byte of w), in the order of term_product.
 // Products of two and three factors (nearly all terms of the gtinv models up
@@ -132,6 +104,40 @@ __device__ __forceinline__ cplx<T> packed_term_product(const int4 c4, const cplx
     for (int q = 1; q < 6; ++q)
         if (q < n) p = cmul(p, a[id[q]]);
     return p;
+}
+
+// Feature values d_k = sum_q coeff_q Re(prod a[ids_q]) of one centre, one
+// warp per 32 consecutive features (windowed warp sums over the packed value
+// terms vcode/vcoef; a window's codes are requested together).
+template <typename T>
+__device__ __forceinline__ void warp_feature_values(const DevType& ty, const cplx<T>* a, T* out, cplx<T>* s_v,
+                                                    int warp, int n_warps, int lane) {
+    constexpr int kU = kTermWin / 32;
+    const T* vcoef = reinterpret_cast<const T*>(ty.vcoef);
+    for (int k0 = 32 * warp; k0 < ty.n_lin; k0 += 32 * n_warps) {
+        const int k = k0 + lane;
+        const int tb = ty.val_off[k0], te = ty.val_off[min(k0 + 32, ty.n_lin)];
+        const int ms = k < ty.n_lin ? ty.val_off[k] : te, me = k < ty.n_lin ? ty.val_off[k + 1] : te;
+        T v = 0;
+        for (int w0 = tb; w0 < te; w0 += kTermWin) {
+            int4 c4[kU];
+            T cf[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int t = min(w0 + 32 * u + lane, te - 1);
+                c4[u] = ty.vcode[t];
+                cf[u] = vcoef[t];
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (w0 + 32 * u + lane < te) s_v[32 * u + lane].re = cf[u] * packed_term_product<T>(c4[u], a).re;
+            __syncwarp();
+            const int lo = max(ms, w0), hi = min(me, w0 + kTermWin);
+            for (int t = lo; t < hi; ++t) v += s_v[t - w0].re;
+            __syncwarp();
+        }
+        if (k < ty.n_lin) out[k] = v;
+    }
 }
 
 template <typename T>

@@ -118,18 +118,27 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
         const int ms = h < ty.K0 ? et.head_toff[h] : te, me = h < ty.K0 ? et.head_toff[h + 1] : te;
         T re = 0, im = 0;
         for (int w0 = tb; w0 < te; w0 += kTermWin) {
+            // the window's codes, features and coefficients are requested together
+            constexpr int kU = kTermWin / 32;
+            int4 c4[kU];
+            int tk[kU];
+            T cf[kU];
 #pragma unroll
-            for (int u = 0; u < kTermWin / 32; ++u) {
-                const int t = w0 + 32 * u + lane;
-                if (t < te) {
-                    const int4 c4 = et.htcode[t];
-                    const T c = beta[et.htk[t]] * hcoef[t];
-                    const cplx<T> p = packed_term_product<T>(c4, a);
+            for (int u = 0; u < kU; ++u) {
+                const int t = min(w0 + 32 * u + lane, te - 1);
+                c4[u] = et.htcode[t];
+                tk[u] = et.htk[t];
+                cf[u] = hcoef[t];
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (w0 + 32 * u + lane < te) {
+                    const T c = beta[tk[u]] * cf[u];
+                    const cplx<T> p = packed_term_product<T>(c4[u], a);
                     cplx<T> v = {c * p.re, c * p.im};
-                    if (c4.w >> 8) v.im = -v.im;
+                    if (c4[u].w >> 8) v.im = -v.im;
                     s_v[warp][32 * u + lane] = v;
                 }
-            }
             __syncwarp();
             const int lo = max(ms, w0), hi = min(me, w0 + kTermWin);
             for (int t = lo; t < hi; ++t) {
