@@ -11,7 +11,7 @@
 //                      the coefficients, E_i, and the folded adjoint
 //                      A_i[h] = sum_e beta_k(e) G_e (no G stored)
 //   pg_eval_pairs      per pair image p = (i -> j, d): g_p = Re(A_i . dphi(d)/dd),
-//                      one warp per pair with the shared pair basis
+//                      32 pairs at a time with their bases built together
 //   pg_nb_mirror       index of the mirror image (j -> i, -d) of every pair
 //                      (exact: -d is bit-identical; xrows.cu)
 //   pg_eval_gather     F_b = sum_{q in list(b)} (g_q - g_mirror(q))   (no atomics)
@@ -151,70 +151,123 @@ __global__ void pg_eval_adjoint(DevModel M, EvalTables ET, const int* types, con
     }
 }
 
-// One block per centre atom; warps take its pair images.
+// One block per centre atom; its pair images taken 32 at a time.  With
+// phi_h = f_n(r) Y_lm and the adjoint regrouped by Y_lm key,
+//   g_p = sum_key Re(B_key . dY_key/dd) + (d/r) sum_key Re(C_key . Y_key),
+//   B_key = sum_n A[tp, n, key] f_n(r),  C_key = sum_n A[tp, n, key] f_n'(r),
+// so a pair costs about 4 K0(tp) + 16 n_ylm multiply-adds.  The block builds
+// the chunk's bases at once (thread = pair and two Legendre columns,
+// ylm_column, or pair and radial functions) into shared memory; then the 8
+// threads of a pair take every 8th key and sum over the radial functions, and
+// their partial sums are added by shuffles (16 threads a pair in FP64).
+// pairs per chunk: 32 (FP32), 16 (FP64, so that two blocks fit an SM)
 template <typename T>
-__global__ void pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long long* nb_off, const int* nb_j,
-                              const double* nb_d, const long long* a_off, const cplx<T>* Aadj, double* g_out) {
+constexpr int eval_chunk() { return sizeof(T) == 4 ? 32 : 16; }
+template <typename T>
+__global__ void __launch_bounds__(256) pg_eval_pairs(DevModel M, EvalTables ET, DevBatch B, const long long* nb_off,
+                                                     const int* nb_j, const double* nb_d, const long long* a_off,
+                                                     const cplx<T>* Aadj, double* g_out) {
+    constexpr int PS = eval_chunk<T>(), TPP = 256 / PS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int i = blockIdx.x;
     const int t1 = B.types[i];
-    const DevType& ty = M.types[t1];
     const EvalType& et = ET.types[t1];
-    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    cplx<T>* A = reinterpret_cast<cplx<T>*>(smem_raw);
-    T* s_tab = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(A + ty.K0) + 15) & ~uintptr_t(15));
-    const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-    T* sb = reinterpret_cast<T*>(
-        (reinterpret_cast<uintptr_t>(s_tab + ylm_table_size(M.n_ylm, M.maxl)) + 15) & ~uintptr_t(15));
+    const int NY = M.n_ylm, NF = M.n_fn_max, L = M.maxl;
+    cplx<T>* Akn = reinterpret_cast<cplx<T>*>(smem_raw);        // [n_tp][NY][NF]: the adjoint by (key, n)
+    T* tab = reinterpret_cast<T*>(Akn + (size_t)M.n_tp * NY * NF);  // [PS][NY][8]: Y, dY/dx, dY/dy, dY/dz
+    T* rad = tab + (size_t)PS * NY * 8;                             // [PS][NF][2]: f, f'
+    T* s_tab = rad + (size_t)PS * NF * 2;
     const cplx<T>* Ai = Aadj + a_off[i];
-    // the adjoint in type-pair head order (tp_heads), read by consecutive lanes below
-    for (int q = threadIdx.x; q < ty.K0; q += blockDim.x) A[q] = Ai[et.tp_heads[q]];
+    for (int q = threadIdx.x; q < M.n_tp * NY * NF; q += blockDim.x) Akn[q] = {(T)0, (T)0};
     load_ylm_tab<T>(M.ylm_tab, s_tab, M.n_ylm, M.maxl);
     __syncthreads();
-    const YlmTab<T> tab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
-    BasisView<T> bv = basis_view<T>(sb + slot * warp, M.n_fn_max, M.n_ylm, M.maxl);
-    for (long long k = nb_off[i] + warp; k < nb_off[i + 1]; k += nw) {
-        T dx, dy, dz, dis;
-        const bool ok = pair_geometry<T>(M, B, nb_d, k, dx, dy, dz, dis);
-        double gx = 0.0, gy = 0.0, gz = 0.0;
+    for (int tp = 0; tp < M.n_tp; ++tp)
+        for (int q = et.tp_head_off[tp] + threadIdx.x; q < et.tp_head_off[tp + 1]; q += blockDim.x) {
+            const int nk = et.tp_head_nk[q];
+            Akn[((size_t)tp * NY + (nk >> 8)) * NF + (nk & 0xff)] = Ai[et.tp_heads[q]];
+        }
+    const YlmTab<T> ytab = ylm_tab_view<T>(s_tab, M.n_ylm, M.maxl);
+    const int p = threadIdx.x / TPP, t = threadIdx.x - (threadIdx.x / TPP) * TPP;
+    const int ny = M.gtinv ? min(TPP, L / 2 + 1) : 1;
+    const int nfree = TPP - ny;
+    const long long pe = nb_off[i + 1];
+    for (long long k0 = nb_off[i]; k0 < pe; k0 += PS) {
+        const int n = (int)min((long long)PS, pe - k0);
+        T dx = 0, dy = 0, dz = 0, dis = 1;
+        bool ok = false;
+        int tp = 0;
+        if (p < n) {
+            ok = pair_geometry<T>(M, B, nb_d, k0 + p, dx, dy, dz, dis);
+            tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k0 + p]]];
+        }
+        const int nfn = M.tp_nfn[tp];
+        __syncthreads();  // the previous chunk's tables are read
+        // ---- bases (threads 0 .. ny-1 of a pair: Legendre columns; the others: radial functions)
         if (ok) {
-            const int tp = M.type_pairs[t1 * M.n_type + B.types[nb_j[k]]];
-            warp_radial<T, true>(M, tp, dis, bv, lane);
-            if (M.gtinv) {
-                warp_ylm<T, true>(M.maxl, M.n_ylm, tab, dx, dy, dz, dis, bv, lane);
-            } else if (lane == 0) {
-                bv.Y[0] = {(T)1, (T)0};
-                bv.dY[0] = bv.dY[1] = bv.dY[2] = {(T)0, (T)0};
+            T* rows = tab + (size_t)p * NY * 8;
+            if (!M.gtinv) {
+                if (t == 0)
+                    for (int v = 0; v < 8; ++v) rows[v] = v == 0 ? (T)1 : (T)0;
+            } else if (t < ny) {
+                const YlmDir<T> dir = ylm_dir<T>(dx, dy, dz, dis);
+                for (int a = t; 2 * a <= L; a += ny)
+                    for (int side = 0; side < 2; ++side) {
+                        const int mp = side ? L - a : a;
+                        if (side && mp == a) break;
+                        ylm_column<T>(mp, L, ytab, dir, rows, 8);
+                    }
             }
-            __syncwarp();
-            T s0 = 0, sx = 0, sy = 0, sz = 0;
-            for (int q = et.tp_head_off[tp] + lane; q < et.tp_head_off[tp + 1]; q += 32) {
-                const int nk = et.tp_head_nk[q];
-                const int nid = nk & 0xff, key = nk >> 8;
-                const cplx<T> g = A[q];
-                const T f = bv.fn[nid];
-                s0 += bv.fnd[nid] * creal_mul(g, bv.Y[key]);
-                sx += f * creal_mul(g, bv.dY[key]);
-                sy += f * creal_mul(g, bv.dY[M.n_ylm + key]);
-                sz += f * creal_mul(g, bv.dY[2 * M.n_ylm + key]);
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                s0 += __shfl_down_sync(0xffffffffu, s0, o);
-                sx += __shfl_down_sync(0xffffffffu, sx, o);
-                sy += __shfl_down_sync(0xffffffffu, sy, o);
-                sz += __shfl_down_sync(0xffffffffu, sz, o);
-            }
-            const T sc = s0 / dis;
-            gx = (double)(sc * dx + sx);
-            gy = (double)(sc * dy + sy);
-            gz = (double)(sc * dz + sz);
+            const int r0t = nfree > 0 ? t - ny : t, rstep = nfree > 0 ? nfree : TPP;
+            if (r0t >= 0)
+                for (int q = r0t; q < nfn; q += rstep) {
+                    T f, fd;
+                    radial_one<T>(M, tp, q, dis, f, fd);
+                    rad[((size_t)p * NF + q) * 2] = f;
+                    rad[((size_t)p * NF + q) * 2 + 1] = fd;
+                }
         }
-        if (lane == 0) {
-            g_out[3 * k] = gx;
-            g_out[3 * k + 1] = gy;
-            g_out[3 * k + 2] = gz;
+        __syncthreads();
+        // ---- g_p: thread t of pair p takes keys t, t + TPP, ..
+        T s0 = 0, sx = 0, sy = 0, sz = 0;
+        if (ok) {
+            const T* rp = rad + (size_t)p * NF * 2;
+            for (int key = t; key < NY; key += TPP) {
+                const cplx<T>* ak = Akn + ((size_t)tp * NY + key) * NF;
+                T bre = 0, bim = 0, cre = 0, cim = 0;
+                for (int q = 0; q < nfn; ++q) {
+                    const cplx<T> av = ak[q];
+                    const T f = rp[2 * q], fd = rp[2 * q + 1];
+                    bre += av.re * f;
+                    bim += av.im * f;
+                    cre += av.re * fd;
+                    cim += av.im * fd;
+                }
+                const T* row = tab + ((size_t)p * NY + key) * 8;
+                s0 += cre * row[0] - cim * row[1];
+                sx += bre * row[2] - bim * row[3];
+                sy += bre * row[4] - bim * row[5];
+                sz += bre * row[6] - bim * row[7];
+            }
         }
-        __syncwarp();
+#pragma unroll
+        for (int o = 1; o < TPP; o <<= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        }
+        if (t == 0 && p < n) {
+            double gx = 0.0, gy = 0.0, gz = 0.0;
+            if (ok) {
+                const T sc = s0 / dis;
+                gx = (double)(sc * dx + sx);
+                gy = (double)(sc * dy + sy);
+                gz = (double)(sc * dz + sz);
+            }
+            g_out[3 * (k0 + p)] = gx;
+            g_out[3 * (k0 + p) + 1] = gy;
+            g_out[3 * (k0 + p) + 2] = gz;
+        }
     }
 }
 
@@ -404,10 +457,11 @@ struct Evaluator {
                 PG_CUDA(cudaStreamSynchronize(stream));
                 return;
             }
-            const int threads = 256, nw = threads / 32;
-            const size_t slot = basis_slot_elems<T>(M.n_fn_max, M.n_ylm, M.maxl);
-            const size_t sm2 = (size_t)m->max_k0 * 2 * sizeof(T) + 16 +
-                               (size_t)ylm_table_size(M.n_ylm, M.maxl) * sizeof(T) + 16 + slot * nw * sizeof(T);
+            const int threads = 256;
+            const size_t sm2 = (size_t)M.n_tp * M.n_ylm * M.n_fn_max * sizeof(cplx<T>) +
+                               (size_t)eval_chunk<T>() * M.n_ylm * 8 * sizeof(T) +
+                               (size_t)eval_chunk<T>() * M.n_fn_max * 2 * sizeof(T) +
+                               (size_t)ylm_table_size(M.n_ylm, M.maxl) * sizeof(T);
             PG_CUDA(cudaFuncSetAttribute(pg_eval_pairs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
             {
                 ProfScope ps("pg_eval_pairs", stream);
