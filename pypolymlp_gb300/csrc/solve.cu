@@ -10,9 +10,12 @@
 // A = L L^T (lower, column-major, block 64):
 //   pg_chol_diag    factor the diagonal block in shared memory,
 //   pg_chol_panel   panel rows below it: L21 = A21 L11^-T (one thread per row),
-//   pg_chol_update  trailing update A22 -= L21 L21^T (64 x 64 lower tiles,
-//                   the tile of a block decoded from its index).
-// The triangular solves L z = b and L^T x = z run in one block per alpha.
+//   pg_chol_update  trailing update A22 -= L21 L21^T (128 x 128 lower tiles,
+//                   8 x 8 outputs a thread; the tile of a block decoded from
+//                   its index).
+// The triangular solves L z = b and L^T x = z run in one block per alpha up to
+// F = 4,096, above that blocked (64 columns at a time, the updates over many
+// blocks).
 // A non-positive or non-finite pivot sets info = column + 1 and stops that
 // alpha's factorisation; its solution is filled with 1e30.
 #include <cuda_runtime.h>
@@ -102,9 +105,17 @@ __global__ void pg_chol_panel(double* A, int F, int k, const int* info) {
     if (row >= F) return;
     double x[kCB];
     for (int j = 0; j < b; ++j) {
-        double v = A[(size_t)(k + j) * F + row];
-        for (int p = 0; p < j; ++p) v -= x[p] * L[j][p];
-        x[j] = v / L[j][j];
+        // four interleaved partial sums: a quarter of the dependent chain
+        double v0 = A[(size_t)(k + j) * F + row], v1 = 0.0, v2 = 0.0, v3 = 0.0;
+        int p = 0;
+        for (; p + 4 <= j; p += 4) {
+            v0 -= x[p] * L[j][p];
+            v1 -= x[p + 1] * L[j][p + 1];
+            v2 -= x[p + 2] * L[j][p + 2];
+            v3 -= x[p + 3] * L[j][p + 3];
+        }
+        for (; p < j; ++p) v0 -= x[p] * L[j][p];
+        x[j] = ((v0 + v1) + (v2 + v3)) / L[j][j];
     }
     for (int j = 0; j < b; ++j) A[(size_t)(k + j) * F + row] = x[j];
 }
@@ -118,10 +129,17 @@ __device__ __forceinline__ void lower_tile(int t, int& ti, int& tj) {
     tj = t - i * (i + 1) / 2;
 }
 
-// A22 -= L21 L21^T over the lower triangle of matrix blockIdx.y; block x = tile index.
-__global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, const int* info) {
-    __shared__ double Pi[kCB][kCB + 1];
-    __shared__ double Pj[kCB][kCB + 1];
+// A22 -= L21 L21^T over the lower triangle of matrix blockIdx.y; block x =
+// index of a lower 128 x 128 tile.  The two 128-row panels of L21 (width <=
+// kCB) sit in shared memory k-major; thread (ty, tx) of 16 x 16 accumulates
+// the 8 x 8 outputs rows ty + 16u, columns tx + 16v (strided, so that a warp's
+// loads of a k row are consecutive).
+constexpr int kUT = 128;  // update tile
+constexpr size_t kUpdSmem = 2 * (size_t)kCB * kUT * sizeof(double);
+__global__ void __launch_bounds__(256, 1) pg_chol_update(double* A, int F, int k, const int* info) {
+    extern __shared__ double upd[];  // Pi[kCB][kUT], Pj[kCB][kUT]
+    double* Pi = upd;
+    double* Pj = upd + kCB * kUT;
     const int mi = blockIdx.y;
     if (info[mi] != 0) return;
     A += (size_t)mi * F * F;
@@ -129,32 +147,36 @@ __global__ void __launch_bounds__(256) pg_chol_update(double* A, int F, int k, c
     const int s0 = k + b;
     int ti, tj;
     lower_tile(blockIdx.x, ti, tj);
-    const int i0 = s0 + ti * kCB, j0 = s0 + tj * kCB;
-    for (int q = threadIdx.x; q < kCB * kCB; q += 256) {
-        const int r = q % kCB, p = q / kCB;
-        Pi[r][p] = (i0 + r < F && p < b) ? A[(size_t)(k + p) * F + i0 + r] : 0.0;
-        Pj[r][p] = (j0 + r < F && p < b) ? A[(size_t)(k + p) * F + j0 + r] : 0.0;
+    const int i0 = s0 + ti * kUT, j0 = s0 + tj * kUT;
+    for (int q = threadIdx.x; q < kCB * kUT; q += 256) {
+        const int r = q % kUT, p = q / kUT;
+        Pi[p * kUT + r] = (i0 + r < F && p < b) ? A[(size_t)(k + p) * F + i0 + r] : 0.0;
+        Pj[p * kUT + r] = (j0 + r < F && p < b) ? A[(size_t)(k + p) * F + j0 + r] : 0.0;
     }
     __syncthreads();
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4] = {};
-    for (int p = 0; p < b; ++p) {
-        double a[4], c[4];
+    double acc[8][8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            a[u] = Pi[ty * 4 + u][p];
-            c[u] = Pj[tx * 4 + u][p];
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = 0.0;
+    for (int p = 0; p < b; ++p) {
+        double a[8], c[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            a[u] = Pi[p * kUT + ty + 16 * u];
+            c[u] = Pj[p * kUT + tx + 16 * u];
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 8; ++u)
 #pragma unroll
-            for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], c[v], acc[u][v]);
+            for (int v = 0; v < 8; ++v) acc[u][v] = fma(a[u], c[v], acc[u][v]);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 8; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            const int i = i0 + ty * 4 + u, j = j0 + tx * 4 + v;
+        for (int v = 0; v < 8; ++v) {
+            const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
             if (i < F && j < F && j <= i) A[(size_t)j * F + i] -= acc[u][v];
         }
 }
@@ -203,34 +225,130 @@ __global__ void pg_chol_solve(const double* L, int F, const double* b, long long
 // d_info (n ints, zeroed by the caller) receives each status.  No host
 // synchronisation: the launches are queued on st.
 void cholesky_device(double* A, int F, int n, int* d_info, cudaStream_t st) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        PG_CUDA(cudaFuncSetAttribute(pg_chol_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdSmem));
+    });
     for (int k = 0; k < F; k += kCB) {
         pg_chol_diag<<<n, 256, 0, st>>>(A, F, k, d_info);
         const int b = std::min(kCB, F - k);
         const int rest = F - k - b;
         if (rest <= 0) break;
         pg_chol_panel<<<dim3((unsigned)((rest + 127) / 128), (unsigned)n), 128, 0, st>>>(A, F, k, d_info);
-        const int nt = (rest + kCB - 1) / kCB;
-        pg_chol_update<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)n), 256, 0, st>>>(A, F, k, d_info);
+        const int nt = (rest + kUT - 1) / kUT;
+        pg_chol_update<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)n), 256, kUpdSmem, st>>>(A, F, k, d_info);
     }
     PG_CUDA(cudaGetLastError());
 }
 
+// Blocked triangular solves for large F (many blocks, x in global memory):
+// per diagonal block of kTB columns, one block per matrix solves the block
+// with the 64 x 64 triangle in shared memory, then a matrix-vector update of
+// the rest of x spreads over many blocks.  Forward L z = b, then backward
+// L^T x = z, in place in x (blockIdx.y or blockIdx.x = the matrix).
+constexpr int kTB = 64;
+__global__ void pg_trsv_diag(const double* L, int F, int k0, double* x, const int* info, int backward) {
+    __shared__ double S[kTB][kTB + 1];
+    __shared__ double xs[kTB];
+    const int mi = blockIdx.x;
+    if (info[mi] != 0) return;
+    L += (size_t)mi * F * F;
+    x += (size_t)mi * F;
+    const int tb = min(kTB, F - k0), t = threadIdx.x;
+    for (int q = t; q < tb * tb; q += blockDim.x) {
+        const int r = q % tb, c = q / tb;
+        S[r][c] = L[(size_t)(k0 + c) * F + k0 + r];
+    }
+    double v = t < tb ? x[k0 + t] : 0.0;
+    __syncthreads();
+    if (!backward) {
+        for (int j = 0; j < tb; ++j) {
+            if (t == j) xs[j] = v / S[j][j];
+            __syncthreads();
+            if (t > j && t < tb) v -= S[t][j] * xs[j];
+        }
+    } else {
+        for (int j = tb - 1; j >= 0; --j) {
+            if (t == j) xs[j] = v / S[j][j];
+            __syncthreads();
+            if (t < j) v -= S[j][t] * xs[j];
+        }
+    }
+    if (t < tb) x[k0 + t] = xs[t];
+}
+// forward: x[r] -= sum_c L[r, k0 + c] x[k0 + c] for r >= k0 + tb;
+// backward: x[r] -= sum_c L[k0 + c, r] x[k0 + c] for r < k0.
+__global__ void pg_trsv_update(const double* L, int F, int k0, double* x, const int* info, int backward) {
+    __shared__ double xs[kTB];
+    const int mi = blockIdx.y;
+    if (info[mi] != 0) return;
+    L += (size_t)mi * F * F;
+    x += (size_t)mi * F;
+    const int tb = min(kTB, F - k0);
+    if (threadIdx.x < tb) xs[threadIdx.x] = x[k0 + threadIdx.x];
+    __syncthreads();
+    const int r = (backward ? 0 : k0 + tb) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (backward ? r >= k0 : r >= F) return;
+    double s0 = 0.0, s1 = 0.0;
+    if (!backward) {
+        int c = 0;
+        for (; c + 2 <= tb; c += 2) {
+            s0 += L[(size_t)(k0 + c) * F + r] * xs[c];
+            s1 += L[(size_t)(k0 + c + 1) * F + r] * xs[c + 1];
+        }
+        if (c < tb) s0 += L[(size_t)(k0 + c) * F + r] * xs[c];
+    } else {
+        const double* row = L + (size_t)r * F + k0;
+        int c = 0;
+        for (; c + 2 <= tb; c += 2) {
+            s0 += row[c] * xs[c];
+            s1 += row[c + 1] * xs[c + 1];
+        }
+        if (c < tb) s0 += row[c] * xs[c];
+    }
+    x[r] -= s0 + s1;
+}
+__global__ void pg_trsv_init(int F, const double* b, long long b_stride, double* x, const int* info) {
+    const int mi = blockIdx.y;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= F) return;
+    x[(size_t)mi * F + r] = info[mi] != 0 ? 1e30 : b[(size_t)mi * b_stride + r];
+}
+
+// Up to kSolveOneBlockF one block per matrix (F-vector in shared memory, no
+// launch per block column); above it the blocked solves.
+constexpr int kSolveOneBlockF = 4096;
 void chol_solve_device(const double* L, int F, int n, const double* b, long long b_stride, double* x,
                        const int* d_info, cudaStream_t st) {
-    const size_t smem = (size_t)F * sizeof(double);
-    PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pg_chol_solve<<<n, 1024, smem, st>>>(L, F, b, b_stride, x, d_info);
+    if (F <= kSolveOneBlockF) {
+        const size_t smem = (size_t)F * sizeof(double);
+        PG_CUDA(cudaFuncSetAttribute(pg_chol_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        pg_chol_solve<<<n, 1024, smem, st>>>(L, F, b, b_stride, x, d_info);
+        PG_CUDA(cudaGetLastError());
+        return;
+    }
+    const unsigned rows = (unsigned)((F + 255) / 256);
+    pg_trsv_init<<<dim3(rows, (unsigned)n), 256, 0, st>>>(F, b, b_stride, x, d_info);
+    for (int k0 = 0; k0 < F; k0 += kTB) {
+        pg_trsv_diag<<<n, kTB, 0, st>>>(L, F, k0, x, d_info, 0);
+        const int rest = F - k0 - std::min(kTB, F - k0);
+        if (rest > 0)
+            pg_trsv_update<<<dim3((unsigned)((rest + 255) / 256), (unsigned)n), 256, 0, st>>>(L, F, k0, x, d_info, 0);
+    }
+    for (int k0 = (F - 1) / kTB * kTB; k0 >= 0; k0 -= kTB) {
+        pg_trsv_diag<<<n, kTB, 0, st>>>(L, F, k0, x, d_info, 1);
+        if (k0 > 0)
+            pg_trsv_update<<<dim3((unsigned)((k0 + 255) / 256), (unsigned)n), 256, 0, st>>>(L, F, k0, x, d_info, 1);
+    }
     PG_CUDA(cudaGetLastError());
 }
 
-constexpr size_t kSolveMaxSmem = 200 * 1024;  // the triangular solves keep one F-vector in shared memory
 
 // (A + alpha_a I) x_a = rhs_a for every alpha: rhs is F x n_alpha with
 // rhs_stride F (one right-hand side per alpha) or 0 (the same for all).
 void ridge_batched(int F, const double* xtx, const double* rhs, long long rhs_stride, const double* alphas,
                    int n_alpha, double* coefs, int* info) {
     if (F <= 0 || !xtx || !rhs || !alphas || !coefs || !info || n_alpha < 0) throw std::runtime_error("bad arguments");
-    if ((size_t)F * sizeof(double) > kSolveMaxSmem) throw std::runtime_error("n_features too large for the solver");
     if (n_alpha == 0) return;
     cudaStream_t st = current_stream();
     const size_t ff = (size_t)F * F * sizeof(double);

@@ -274,7 +274,12 @@ def solver_ridge(xtx: np.ndarray, xty: np.ndarray, alphas: Sequence[float]) -> n
     alpha (the corrections of iterative refinement)."""
     F = xtx.shape[0]
     a = np.ascontiguousarray(np.asarray(alphas, dtype=np.float64))
-    A = np.asfortranarray(xtx, dtype=np.float64)
+    # xtx is symmetric: a row-major FP64 array is passed as its (equal)
+    # transpose, without a column-major copy (3.9 GB at F = 21,945)
+    if xtx.dtype == np.float64 and xtx.flags.c_contiguous:
+        A = xtx.T
+    else:
+        A = np.asfortranarray(xtx, dtype=np.float64)
     b = np.asfortranarray(xty, dtype=np.float64)
     coefs = np.zeros((F, len(a)), order="F")
     info = np.zeros(len(a), dtype=np.int32)

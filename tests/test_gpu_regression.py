@@ -72,6 +72,26 @@ def test_ridge_solve_matches_posv():
             assert np.abs(got[:, k] - ref[:, k]).max() / np.abs(ref[:, k]).max() < 1e-8, (F, k)
 
 
+def test_ridge_solve_blocked_triangular_matches_posv():
+    """Above F = 4,096 the triangular solves run blocked over many blocks:
+    against posv for two alphas, and a third alpha that makes the shifted
+    matrix indefinite gives 1e30 while the others stay intact."""
+    from pypolymlp_gb300.regression import solver_ridge
+
+    rng = np.random.default_rng(3)
+    F = 4500
+    B = rng.normal(size=(F + 400, F))
+    A = B.T @ B
+    b = rng.normal(size=F)
+    alphas = [1e-2, 1.0]
+    ref = solver_ridge_cpu(A, b, alphas)
+    got, info = solver_ridge(A, b, alphas + [-1e9])
+    assert info[0] == 0 and info[1] == 0 and info[2] != 0
+    for k in range(2):
+        assert np.abs(got[:, k] - ref[:, k]).max() / np.abs(ref[:, k]).max() < 1e-8, k
+    assert np.all(got[:, 2] == 1e30)
+
+
 def test_ridge_solve_per_alpha_rhs_and_failures():
     """One right-hand side per alpha (pg_solve_ridge_rhs), and a failed
     factorisation of one alpha leaves the others intact."""
