@@ -77,11 +77,11 @@ MODELS = {
 
 
 # DRAM traffic of pg_rows_pairs per X row, from one ncu capture (binary model,
-# mixed precision, 20 structures, 5,552 rows: dram__bytes_read.sum 0.188 GB +
-# dram__bytes_write.sum 1.275 GB).  The kernel's traffic is the group vectors it
+# mixed precision, 20 structures, 5,552 rows: dram__bytes_read.sum 0.282 GB +
+# dram__bytes_write.sum 1.497 GB).  The kernel's traffic is the group vectors it
 # writes, which grow with the pair images, in proportion to the rows; the bench
 # line scales it to a launch by the rows the launch processes.
-NCU_ROWS_PAIRS_BYTES_PER_ROW = {"cfg2": 1.463456e9 / 5552}
+NCU_ROWS_PAIRS_BYTES_PER_ROW = {"cfg2": (0.282137 + 1.496542) * 1e9 / 5552}
 
 
 def log(*a):
@@ -546,6 +546,24 @@ def main():
                 "note": f"algorithmic bytes = F x {tb} B written + F x {tb} B read per X row (the X tile); "
                         f"peak {peak_kind} copy bandwidth; traffic = ncu DRAM bytes per X row of the kernel "
                         f"(one ncu capture of 20 structures) x rows per launch"}
+    if "pg_rows_pairs" in prof and precision == _ffi.PG_MIXED:
+        # stage A against the FP32 CUDA cores: per neighbour pair of a force
+        # structure, 16 flops per adjoint entry of its type pair (T and S_x,y,z:
+        # four complex-real products) and 30 per linear feature with entries
+        # (the chain rule f S + f' d/r T and the self/virial sums)
+        xw = model.xrow_work()
+        pc = batch.pair_counts(model.work()["n_type"]).astype(np.float64)
+        a_flops = float(np.sum(pc * (16.0 * xw["n_entries"] + 30.0 * xw["n_positions"])))
+        ams, an = prof["pg_rows_pairs"]
+        a_ach = a_flops / (ams / 1e3) / 1e12
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        roof.setdefault("stage_a_fp32", {
+            "kernel": "pg_rows_pairs", "bound": "fp32 cuda cores", "achieved": a_ach, "peak": fp32_peak,
+            "unit": "TFLOP/s", "frac": a_ach / fp32_peak, "pairs_per_step": int(pc.sum()),
+            "flops_per_step": a_flops,
+            "note": "16 flops per (adjoint entry, pair) + 30 per (linear feature with entries, pair), entries of "
+                    "the pair's type pair; peak nominal (152 SMs x 128 lanes x 2 flops x 2,070 MHz; no FP32 "
+                    "peak is measured)"})
     if "pg_gram_tc" in prof and not dname.startswith("pg_gram"):
         gms, gn = prof["pg_gram_tc"]
         g_ach = F * (F + 1) * rows_per_step / (gms / 1e3) / 1e12

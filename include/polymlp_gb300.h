@@ -140,6 +140,14 @@ int pg_get_stream(void** stream);
 int pg_model_work(const pg_model* m, int* n_type, int* max_l, int* n_radial, int* k0_pair, int64_t* n_terms);
 
 /*
+ * Force-row work of a model, for roofline accounting (no reference
+ * counterpart): per centre type a and neighbour type b (n_type^2 each),
+ * n_entries = adjoint entries by that type pair (the stage-A contraction per
+ * pair) and n_positions = linear features with such entries.
+ */
+int pg_model_xrow_work(const pg_model* m, int* n_entries, int* n_positions);
+
+/*
  * Fused regression assembly: X rows are generated on the device, weighted,
  * and summed into X^T X, X^T y, y^T y and the column sums of the (unweighted)
  * energy rows, without X leaving the GPU.  Replaces the sequential loop of
@@ -170,6 +178,12 @@ int pg_batch_create(pg_model* m, const pg_structures* st, const int64_t* e_row, 
                     const int64_t* s_row, int64_t n_rows, const double* w, const double* y, int precision,
                     pg_batch** out);
 int pg_batch_destroy(pg_batch* b);
+/*
+ * Neighbour pairs of the force structures of a batch by centre type and
+ * neighbour type (counts[a * n_type + b], n_type^2 entries), from the
+ * neighbour lists of its last pg_gram_accumulate_batch (zero before).
+ */
+int pg_batch_pair_counts(pg_batch* b, int n_type, int64_t* counts);
 int pg_gram_accumulate_batch(pg_gram* g, pg_batch* b);
 /*
  * X^T X of one host block X (n_rows x n_features, column-major, leading

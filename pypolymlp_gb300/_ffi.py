@@ -70,6 +70,8 @@ def lib():
                 ("pg_solve_ridge", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
                 ("pg_solve_ridge_rhs", [C.c_int, _dp, _dp, _dp, C.c_int, _dp, _ip]),
                 ("pg_model_work", [_vp, _ip, _ip, _ip, _ip, _i64p]),
+                ("pg_model_xrow_work", [_vp, _ip, _ip]),
+                ("pg_batch_pair_counts", [_vp, C.c_int, _i64p]),
                 ("pg_solve_ridge_noalloc", [C.c_int, _vp, _vp, C.c_double, _vp, _ip]),
                 ("pg_eval_create", [_vp, _dp, C.c_int, C.c_int, C.POINTER(_vp)]),
                 ("pg_eval_destroy", [_vp]),
@@ -192,6 +194,15 @@ class Model:
                               _p(terms, C.c_int64)))
         return {"n_type": nt.value, "max_l": ml.value, "n_radial": nr.value,
                 "k0_pair": k0.reshape(nt.value, nt.value), "n_terms": terms}
+
+    def xrow_work(self):
+        """{n_entries, n_positions}: per (centre type, neighbour type) the adjoint
+        entries and the linear features with entries of that type pair."""
+        n = self.work()["n_type"]
+        ne = np.zeros(n * n, np.int32)
+        npos = np.zeros(n * n, np.int32)
+        check(lib().pg_model_xrow_work(self._h, _p(ne, C.c_int), _p(npos, C.c_int)))
+        return {"n_entries": ne.reshape(n, n), "n_positions": npos.reshape(n, n)}
 
     def feature_attrs(self):
         L = lib()

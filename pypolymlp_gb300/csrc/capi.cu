@@ -726,6 +726,28 @@ int pg_model_work(const pg_model* m, int* n_type, int* max_l, int* n_radial, int
     });
 }
 
+int pg_model_xrow_work(const pg_model* m, int* n_entries, int* n_positions) {
+    return guarded([&] {
+        if (!m || !n_entries || !n_positions) throw std::runtime_error("null argument");
+        const pg::FlatModel& fm = m->m->flat;
+        const int nt = fm.n_type, ntp = fm.n_tp;
+        for (int a = 0; a < nt; ++a) {
+            const pg::FlatType& T = fm.types[a];
+            for (int b = 0; b < nt; ++b) {
+                const int tp = fm.type_pairs[a * nt + b];
+                int ne = 0, np = 0;
+                for (int k = 0; tp >= 0 && k < T.n_lin; ++k) {
+                    const int c = T.ent_tp_off[(size_t)k * (ntp + 1) + tp + 1] - T.ent_tp_off[(size_t)k * (ntp + 1) + tp];
+                    ne += c;
+                    np += c > 0;
+                }
+                n_entries[a * nt + b] = ne;
+                n_positions[a * nt + b] = np;
+            }
+        }
+    });
+}
+
 int pg_feature_attrs(const pg_feature_params* fp, int* n_linear, int* radial_ids, int* gtinv_ids,
                      int* n_tcomb_values, int* tcomb_offsets, int* tcomb_values, int* n_poly,
                      int* n_poly_values, int* poly_offsets, int* poly_values, int* type_pairs) {

@@ -486,6 +486,28 @@ int pg_batch_destroy(pg_batch* b) {
     return guarded([&] { delete b; });
 }
 
+int pg_batch_pair_counts(pg_batch* b, int n_type, int64_t* counts) {
+    return guarded([&] {
+        if (!b || !counts || n_type <= 0) throw std::runtime_error("bad arguments");
+        std::fill(counts, counts + (size_t)n_type * n_type, (int64_t)0);
+        for (auto& P : b->parts) {
+            const DeviceBatch& B = P->b;
+            if (B.n_pairs <= 0 || B.n_atoms <= 0) continue;
+            std::vector<long long> off(B.n_atoms + 1), f(B.n_st);
+            std::vector<int> nb((size_t)B.n_pairs);
+            copy_d2h(off.data(), B.d_nb_off.as<long long>(), off.size() * sizeof(long long));
+            copy_d2h(nb.data(), B.d_nb_j.as<int>(), nb.size() * sizeof(int));
+            copy_d2h(f.data(), P->d_f.as<long long>(), f.size() * sizeof(long long));
+            for (int i = 0; i < B.n_atoms; ++i) {
+                if (f[B.atom_st[i]] < 0) continue;
+                const int a = B.types[i];
+                if (a < 0 || a >= n_type) throw std::runtime_error("atom type out of range");
+                for (long long q = off[i]; q < off[i + 1]; ++q) counts[a * n_type + B.types[nb[q]]]++;
+            }
+        }
+    });
+}
+
 int pg_gram_accumulate_batch(pg_gram* gh, pg_batch* b) {
     return guarded([&] {
         if (!gh || !b) throw std::runtime_error("null argument");

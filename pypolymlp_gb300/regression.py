@@ -207,6 +207,13 @@ class DeviceBatch:
     def handle(self):
         return self._h
 
+    def pair_counts(self, n_type: int) -> np.ndarray:
+        """Neighbour pairs of the force structures by (centre type, neighbour
+        type), from the lists of the last accumulation (zeros before)."""
+        out = np.zeros(n_type * n_type, np.int64)
+        _ffi.check(_ffi.lib().pg_batch_pair_counts(self._h, int(n_type), _ffi._p(out, C.c_int64)))
+        return out.reshape(n_type, n_type)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value and _ffi._lib is not None:

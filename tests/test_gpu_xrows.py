@@ -145,3 +145,33 @@ def test_neighbor_list_bit_exact_cell_list():
         np.testing.assert_array_equal(go, oo)
         np.testing.assert_array_equal(gj, oj)
         np.testing.assert_array_equal(gd, od)
+
+
+def test_xrow_work_and_pair_counts():
+    """The roofline inputs of the bench: adjoint entries and positions per
+    (centre type, neighbour type) of the binary l_max (8, 4) model (4,345
+    entries and 957 features with entries for every type pair), and a staged
+    batch's pair counts by type pair, which add up to its neighbour lists."""
+    from pypolymlp_gb300 import _ffi
+    from pypolymlp_gb300.regression import DeviceBatch, GramAccumulator, Dataset, get_min_energy
+
+    p = make_params_dict(n_type=2, cutoff=7.0, model_type=3, max_p=2, gaussian_params2=(0.0, 5.0, 10),
+                         gtinv_order=3, gtinv_maxl=(8, 4))
+    m = _model(p)
+    w = m.xrow_work()
+    assert (w["n_entries"] == 4345).all() and (w["n_positions"] == 957).all()
+    ss = syn.binary_set(6, seed=3)
+    syn.morse_labels(ss, syn.morse_D(2), rc=7.0)
+    d = Dataset.from_structure_set(ss)
+    b = DeviceBatch(m, d, get_min_energy([d]), _ffi.PG_MIXED)
+    assert b.pair_counts(2).sum() == 0  # no lists before an accumulation
+    g = GramAccumulator(m, _ffi.PG_MIXED)
+    g.accumulate_batch(b)
+    pc = b.pair_counts(2)
+    st = Structures(ss.axis, ss.positions, ss.types)
+    want = np.zeros((2, 2), np.int64)
+    for s in range(st.n_st):
+        offs, nb, _ = _ffi.neighbor_list(st, s, 7.0)
+        t = np.asarray(ss.types[s])
+        np.add.at(want, (np.repeat(t, np.diff(offs)), t[nb]), 1)
+    np.testing.assert_array_equal(pc, want)
