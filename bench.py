@@ -320,9 +320,13 @@ def fit_bench(params, data, args):
     offs = np.concatenate([[0], np.cumsum(test.total_n_atoms)])
     out = {"workload": f"{k} training / {n - k} test structures of the X^T X workload", "alphas": alphas}
     for name, prec in (("mixed", _ffi.PG_MIXED), ("fp64", _ffi.PG_FP64)):
+        _ffi.profile_enable(True)
+        _ffi.profile_read()
         t0 = time.time()
         res = fit(params, [train], [test], alphas, precision=prec)
         wall = time.time() - t0
+        prof = _ffi.profile_read()
+        _ffi.profile_enable(False)
         ev = _ffi.Evaluator(params, res.scaled_coeffs, _ffi.PG_FP64)
         e, f, s = ev.run(st)
         err, _ = prediction_errors(test, e, [f[offs[i]:offs[i + 1]] for i in range(len(test))], s)
@@ -330,7 +334,16 @@ def fit_bench(params, data, args):
         out[name] = {"seconds": wall, "phases_s": {k2: v for k2, v in tm.items() if k2.endswith("_s")},
                      "xtx_rows_per_s": tm["train_rows"] / tm["assemble_s"], "alpha": res.alpha,
                      "rmse_energy_meV_atom": err["energy"] * 1e3, "rmse_force_meV_A": err["force"] * 1e3,
-                     "rmse_test_selected": res.rmse_test}
+                     "rmse_test_selected": res.rmse_test,
+                     "kernels_ms": {k2: v[0] for k2, v in prof.items()}}
+        if "pg_syrk_f64" in prof:
+            # the FP64 Gram (the judge path) against the nominal FP64 rate
+            F = len(res.scaled_coeffs)
+            ach = F * (F + 1) * tm["train_rows"] / (prof["pg_syrk_f64"][0] / 1e3) / 1e12
+            out[name]["gram_fp64_roofline"] = {"kernel": "pg_syrk_f64", "bound": "fp64", "achieved": ach,
+                                               "peak": 1.25, "unit": "TFLOP/s", "frac": ach / 1.25,
+                                               "note": "F(F+1) flops per training row; peak nominal (no FP64 "
+                                                       "peak is measured)"}
         log(f"fit {name}: {wall:.1f}s, alpha {res.alpha}, E {err['energy'] * 1e3:.4f} meV/atom, "
             f"F {err['force'] * 1e3:.3f} meV/A")
     m, d = out["mixed"], out["fp64"]
@@ -381,6 +394,7 @@ def cfg5_bench(args):
     t0 = time.time()
     coefs, info = solver_ridge(A, xty / sc, [1e-3])
     solve_s = time.time() - t0
+    solve_tf = (F ** 3 / 3.0 + 2.0 * F * F) / solve_s / 1e12
     return {"workload": workload.replace("50000 structures", f"{len(data)} structures") + f", F = {F}",
             "rows": int(batch.n_rows), "rows_per_s": batch.n_rows / dt, "seconds": dt,
             "gram": {"ms": gms, "achieved": g_ach, "unit": "TFLOP/s", "peak": bf16_tf / 13.0,
@@ -388,8 +402,9 @@ def cfg5_bench(args):
                      "note": f"F(F+1) flops per X row; peak = {peak_kind} bf16 dense / 13 (slice products)"},
             "kernels": {k2: {"ms": v[0], "launches": v[1]} for k2, v in prof.items()},
             "solve": {"n_features": F, "alphas": 1, "seconds": solve_s, "info": int(info[0]),
+                      "achieved": solve_tf, "peak": 1.25, "unit": "TFLOP/s", "frac": solve_tf / 1.25,
                       "note": "Cholesky of the column-scaled Gram + 1e-3 I and two triangular solves, FP64, "
-                              "host copies included"}}
+                              "host copies included; F^3/3 + 2F^2 flops against the nominal FP64 rate"}}
 
 
 def run_reference(args):
@@ -564,6 +579,17 @@ def main():
             "note": "16 flops per (adjoint entry, pair) + 30 per (linear feature with entries, pair), entries of "
                     "the pair's type pair; peak nominal (152 SMs x 128 lanes x 2 flops x 2,070 MHz; no FP32 "
                     "peak is measured)"})
+    if "pg_nb_count" in prof and "pg_nb_fill" in prof:
+        # the neighbour search against HBM, SURVEY's per-atom bytes: 28 per list
+        # entry (int32 neighbour + 3 x FP64 displacement) + 36 per atom
+        npairs = int(batch.pair_counts(model.work()["n_type"]).sum())
+        n_at = int(sum(data.total_n_atoms))
+        nb_s = (prof["pg_nb_count"][0] + prof["pg_nb_fill"][0]) / 1e3
+        nb_gbs = (28.0 * npairs + 36.0 * n_at) / nb_s / 1e9
+        roof["neighbours"] = {"kernels": ["pg_nb_count", "pg_nb_fill"], "bound": "hbm", "achieved": nb_gbs,
+                              "peak": hbm_gbs, "unit": "GB/s", "frac": nb_gbs / hbm_gbs,
+                              "note": "28 B per list entry + 36 B per atom; the search itself (candidates x "
+                                      "translations per atom) is compute, so the fraction is low"}
     if "pg_gram_tc" in prof and not dname.startswith("pg_gram"):
         gms, gn = prof["pg_gram_tc"]
         g_ach = F * (F + 1) * rows_per_step / (gms / 1e3) / 1e12
