@@ -1133,15 +1133,18 @@ __global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, 
 //   X[e_row, col] = sum_i poly_col(d(i)),
 //   X[s_row + q, col] = -sum_i sum_{k in col} w_k,col(i) DS[i][3+q][k].
 // A linear column (one feature k, w = 1) is a plain sum over the structure's
-// atoms of its centre type: thread = features k, t + 256 r (r < kEsFeat) held
-// in registers while the atoms go by, so that each atom's feature and DS rows
-// are read together by the block (contiguous features, DS rows at the
-// features' positions of each type pair).  Product columns: thread = column,
-// weights from the atom's features.  Every sum runs over the atoms in order in
-// a long accumulator (FP64, or float-float in the FP32 kernel) and is added to
-// X (zeroed per batch) type by type, since a column can belong to the features
-// of several centre types (those of a type pair): deterministic.
-constexpr int kEsThreads = 256, kEsFeat = 4, kEsTpl = 3;  // positions of up to kEsTpl type pairs in registers
+// atoms of its centre type: energies with thread = features k, t + 256 r
+// (r < kEsFeat) held in registers while the atoms go by (each atom's feature
+// row read contiguously); stresses per type pair of the centre type with
+// thread = feature positions x, t + 256 r (the DS rows are stored by position
+// and read contiguously; partial sums over four atoms in T), each position's
+// sum added to its feature's column.
+// Product columns: thread = column, weights from the atom's features.  Every
+// sum runs over the atoms in order in a long accumulator (FP64, or float-float
+// in the FP32 kernel) and is added to X (zeroed per batch) type pair by type
+// pair and type by type, since a column can belong to the features of several
+// centre types (those of a type pair): deterministic.
+constexpr int kEsThreads = 256, kEsFeat = 4;
 template <typename T>
 __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B, const long long* d_off, const T* D,
                                                          const long long* s_off, const T* DS, const long long* e_row,
@@ -1155,50 +1158,77 @@ __global__ void __launch_bounds__(kEsThreads) pg_rows_es(DevModel M, DevBatch B,
     for (int tc = 0; tc < M.n_type; ++tc) {
         const DevType& ty = M.types[tc];
         const int nl = ty.n_lin, ntpl = ty.n_tpl, npos = ty.n_pos;
-        // ---- linear columns
+        // ---- linear columns: energies
         for (int kb = 0; kb < nl; kb += kEsThreads * kEsFeat) {
-            LongSum<T> acc[kEsFeat][7];
-            int kk[kEsFeat], xpos[kEsFeat][kEsTpl];
+            LongSum<T> acc[kEsFeat];
+            int kk[kEsFeat];
 #pragma unroll
-            for (int r = 0; r < kEsFeat; ++r) {
-                kk[r] = kb + threadIdx.x + r * kEsThreads;
-#pragma unroll
-                for (int l = 0; l < kEsTpl; ++l)
-                    xpos[r][l] = (kk[r] < nl && l < ntpl) ? ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + kk[r]] : 0;
-            }
+            for (int r = 0; r < kEsFeat; ++r) kk[r] = kb + threadIdx.x + r * kEsThreads;
             for (int i = a0; i < a1; ++i) {
                 if (B.types[i] != tc) continue;
                 const T* Di = D + d_off[i];
-                const T* dsi = DS + s_off[i] + 3 * (size_t)npos;
 #pragma unroll
-                for (int r = 0; r < kEsFeat; ++r) {
-                    if (kk[r] >= nl) continue;
-                    acc[r][0].add(Di[kk[r]]);
-                    if (!force) continue;
-                    T v[6] = {0, 0, 0, 0, 0, 0};
-                    for (int l = 0; l < ntpl; ++l) {
-                        int x = 0;
-#pragma unroll
-                        for (int u = 0; u < kEsTpl; ++u)
-                            if (u == l) x = xpos[r][u];
-                        if (l >= kEsTpl) x = ty.tp_ipos[(size_t)ty.tpl_tp[l] * nl + kk[r]];
-                        const T* ds = dsi + (size_t)l * 9 * npos + x;
-#pragma unroll
-                        for (int q = 0; q < 6; ++q) v[q] += ds[(size_t)q * npos];
-                    }
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) acc[r][1 + q].add(-v[q]);
-                }
+                for (int r = 0; r < kEsFeat; ++r)
+                    if (kk[r] < nl) acc[r].add(Di[kk[r]]);
             }
 #pragma unroll
             for (int r = 0; r < kEsFeat; ++r) {
                 if (kk[r] >= nl) continue;
                 const int col = ty.lin_col[kk[r]];
-                if (col < 0) continue;
-                xe[(size_t)col * ld] += (T)acc[r][0].value();
-                if (force)
+                if (col >= 0) xe[(size_t)col * ld] += (T)acc[r].value();
+            }
+        }
+        // ---- linear columns: stresses, type pair by type pair (positions past
+        // tp_nnz hold no derivatives)
+        for (int l = 0; force && l < ntpl; ++l) {
+            __syncthreads();  // the previous type pair's additions to a column are done
+            const int tp = ty.tpl_tp[l];
+            const int nnz = ty.tp_nnz[tp];
+            const int* perm = ty.tp_perm + (size_t)tp * npos;
+            for (int xb = 0; xb < nnz; xb += kEsThreads * kEsFeat) {
+                // partial sums over kEsRun atoms in T, each added to the long sum
+                constexpr int kEsRun = 4;
+                LongSum<T> acc[kEsFeat][6];
+                T part[kEsFeat][6];
 #pragma unroll
-                    for (int q = 0; q < 6; ++q) xs[(size_t)col * ld + q] += (T)acc[r][1 + q].value();
+                for (int r = 0; r < kEsFeat; ++r)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) part[r][q] = (T)0;
+                int run = 0;
+                for (int i = a0; i < a1; ++i) {
+                    if (B.types[i] != tc) continue;
+                    const T* ds = DS + s_off[i] + ((size_t)l * 9 + 3) * npos;
+#pragma unroll
+                    for (int r = 0; r < kEsFeat; ++r) {
+                        const int x = xb + threadIdx.x + r * kEsThreads;
+                        if (x < nnz)
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) part[r][q] -= ds[(size_t)q * npos + x];
+                    }
+                    if (++run == kEsRun) {
+                        run = 0;
+#pragma unroll
+                        for (int r = 0; r < kEsFeat; ++r)
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) {
+                                acc[r][q].add(part[r][q]);
+                                part[r][q] = (T)0;
+                            }
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < kEsFeat; ++r)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) acc[r][q].add(part[r][q]);
+#pragma unroll
+                for (int r = 0; r < kEsFeat; ++r) {
+                    const int x = xb + threadIdx.x + r * kEsThreads;
+                    if (x >= nnz || perm[x] < 0) continue;
+                    const int col = ty.lin_col[perm[x]];
+                    if (col < 0) continue;
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) xs[(size_t)col * ld + q] += (T)acc[r][q].value();
+                }
             }
         }
         // ---- product columns
