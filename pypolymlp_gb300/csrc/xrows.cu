@@ -954,7 +954,7 @@ __device__ __forceinline__ void load_vec4(const double* p, double (&v)[4]) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRowsThreads) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
+__global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
                                                         const T* Dp, const long long* s_off, const T* DS,
                                                         const long long* f_row, T* X, long long ld) {
