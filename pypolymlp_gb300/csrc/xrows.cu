@@ -888,7 +888,10 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
 // same pass over the groups when one slab covers the positions, else in a
 // pass of their own.  The self rows add the centre's DS vectors to its own
 // type's columns.  Every X element has one owner thread per type, and types
-// are taken in order, so the sums are deterministic.
+// are taken in order, so the sums are deterministic.  When the three rows of
+// j (F x 3 values) fit in shared memory, they are summed there and written to
+// X once at the end (plain stores, no read-modify-write of X); else each
+// contribution is added to X in place, in the same order.
 __device__ __forceinline__ void unpack_col(int2 c, int& k0, int& k1, int& k2, int& w) {
     k0 = c.x & 0xffff;
     k1 = (c.x >> 16) & 0xffff;
@@ -953,7 +956,26 @@ __device__ __forceinline__ void load_vec4(const double* p, double (&v)[4]) {
     v[3] = b.y;
 }
 
-template <typename T>
+// Rows r0 .. r0 + 2 of column col of X (or of the block's copy s_x when SROW)
+// minus v (plus v when add).
+template <bool SROW, typename T>
+__device__ __forceinline__ void sub_row3(T* s_x, T* X, long long ld, long long r0, int col, const T (&v)[3],
+                                         bool add = false) {
+    const T sg = add ? (T)1 : (T)-1;
+    if (SROW) {
+        T* o = s_x + 3 * col;
+        o[0] += sg * v[0];
+        o[1] += sg * v[1];
+        o[2] += sg * v[2];
+    } else {
+        T* o = X + (size_t)col * ld + r0;
+        o[0] += sg * v[0];
+        o[1] += sg * v[1];
+        o[2] += sg * v[2];
+    }
+}
+
+template <typename T, bool SROW>
 __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
                                                         const T* Dp, const long long* s_off, const T* DS,
@@ -970,10 +992,17 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
     // the groups of j's list (runs of one neighbour i != j) of one centre type,
     // listed kSeg pairs of the list at a time: a group's vector sits at its
     // first pair, so a group that crosses a segment is taken in the first one
-    constexpr int kSeg = 2048;
+    constexpr int kSeg = 1024;
     __shared__ int s_list[kSeg];
     __shared__ long long s_doff[kSeg];  // d_off of each group's centre (its features weight the product columns)
     __shared__ int s_wcnt[kRowsThreads / 32];
+    // the three rows of j by column ([col][3]) when SROW
+    extern __shared__ __align__(16) unsigned char s_x_raw[];
+    T* s_x = reinterpret_cast<T*>(s_x_raw);
+    if (SROW) {
+        for (int q = threadIdx.x; q < 3 * M.F; q += blockDim.x) s_x[q] = (T)0;
+        __syncthreads();
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int tc = 0; tc < M.n_type; ++tc) {
         const DevType& ty = M.types[tc];
@@ -1046,18 +1075,10 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                     if (x >= nnz || perm[x] < 0) continue;  // past the positions with data, or a hole
                     const int col = ty.lin_col[perm[x]];
                     if (col < 0) continue;
-                    T* o = X + (size_t)col * ld + r0;
-                    o[0] -= acc[m][0];
-                    o[1] -= acc[m][1];
-                    o[2] -= acc[m][2];
+                    sub_row3<SROW>(s_x, X, ld, r0, col, acc[m]);
                 }
             }
-            if (has_pc) {
-                T* o = X + (size_t)pc.col * ld + r0;
-                o[0] -= pv[0];
-                o[1] -= pv[1];
-                o[2] -= pv[2];
-            }
+            if (has_pc) sub_row3<SROW>(s_x, X, ld, r0, pc.col, pv);
             // product columns, own pass
             for (int p = threadIdx.x; !fuse && p < ty.n_prod; p += blockDim.x) {
                 if (!prod_col(ty, ipos, nnz, p, pc)) continue;
@@ -1066,10 +1087,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                     const long long q = sb + s_list[k];
                     prod_col_add(pc, Dp + (size_t)q * 3 * NL, D + s_doff[k], NL, v);
                 }
-                T* o = X + (size_t)pc.col * ld + r0;
-                o[0] -= v[0];
-                o[1] -= v[1];
-                o[2] -= v[2];
+                sub_row3<SROW>(s_x, X, ld, r0, pc.col, v);
             }
             // before the list is rebuilt; a column shared by several types is
             // also updated type by type
@@ -1092,10 +1110,8 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
             v1 += ds[npos + x];
             v2 += ds[2 * npos + x];
         }
-        T* o = X + (size_t)col * ld + r0;
-        o[0] += v0;
-        o[1] += v1;
-        o[2] += v2;
+        const T v[3] = {v0, v1, v2};
+        sub_row3<SROW>(s_x, X, ld, r0, col, v, true);
     }
     __syncthreads();
     for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
@@ -1122,10 +1138,16 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                 if (w > 2) v[c] += w2 * ds[(size_t)c * npos + x2];
             }
         }
-        T* o = X + (size_t)col * ld + r0;
-        o[0] += v[0];
-        o[1] += v[1];
-        o[2] += v[2];
+        sub_row3<SROW>(s_x, X, ld, r0, col, v, true);
+    }
+    if (SROW) {
+        __syncthreads();
+        for (int col = threadIdx.x; col < M.F; col += blockDim.x) {
+            T* o = X + (size_t)col * ld + r0;
+            o[0] = s_x[3 * col];
+            o[1] = s_x[3 * col + 1];
+            o[2] = s_x[3 * col + 2];
+        }
     }
 }
 
@@ -1385,7 +1407,16 @@ template <typename T>
 void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, const int* nb_j,
                  const long long* d_off, const T* D, const T* Dp, const long long* s_off, const T* DS,
                  const long long* f_row, T* X, long long ld, cudaStream_t st) {
-    pg_rows<T><<<B.n_atoms, kRowsThreads, 0, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X, ld);
+    // the three rows of a target in shared memory when they fit beside the lists
+    // at the kernel's occupancy (FP32: five blocks an SM; FP64: one)
+    const size_t rows3 = 3 * sizeof(T) * (size_t)M.F;
+    if (rows3 <= (sizeof(T) == 4 ? 31 * 1024 + 512 : 200 * 1024)) {
+        PG_CUDA(cudaFuncSetAttribute(pg_rows<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows3));
+        pg_rows<T, true><<<B.n_atoms, kRowsThreads, rows3, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X,
+                                                                 ld);
+    } else {
+        pg_rows<T, false><<<B.n_atoms, kRowsThreads, 0, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X, ld);
+    }
 }
 
 template <typename T>
