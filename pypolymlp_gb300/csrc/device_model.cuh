@@ -67,6 +67,15 @@ struct DevType {
     const int2* col_pack;      // per column: k0 | k1 << 16, k2 | count << 16 (its up to three linear features)
     int n_prod;                // columns that are products of two or three features of this type
     const int *lin_col, *prod_col;  // per feature: its linear column (-1: none); the product columns
+    // Force rows of the product columns when all are products of two features
+    // (prod_q): per type pair tp of this centre type, prod_qn[tp] (<= the row
+    // kernel's block size) roles, one per (column, differentiated feature k with
+    // data in tp): prod_q[tp][t] = {position of k, the other feature (weight),
+    // column, phase | 2 * (square column)}.  A role sums weight x group-vector
+    // value over the centres; phase 0 and 1 roles of a column are added apart.
+    int prod_qok;
+    const int* prod_qn;
+    const int4* prod_q;
     const int *tp_head_off, *tp_heads;  // heads of each type pair (CSR over type pairs)
     // X-row layout of the adjoint entries by type pair (host/flat_tables.h)
     int n_groups, lay_size, n_tpl, n_pos;  // n_pos: feature positions per type pair (host/flat_tables.h)

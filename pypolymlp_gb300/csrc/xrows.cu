@@ -975,7 +975,7 @@ __device__ __forceinline__ void sub_row3(T* s_x, T* X, long long ld, long long r
     }
 }
 
-template <typename T, bool SROW>
+template <typename T, bool SROW, bool QP>
 __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(DevModel M, DevBatch B, const long long* nb_off,
                                                         const int* nb_j, const long long* d_off, const T* D,
                                                         const T* Dp, const long long* s_off, const T* DS,
@@ -1039,13 +1039,24 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                 n += total;
                 __syncthreads();
             }
-            // linear columns: sum of the group vectors.  When one slab covers
+            // linear columns: sum of the group vectors.  Product columns of two
+            // features: thread = role (column, differentiated feature with data
+            // in tp), summed in the same pass over the groups (first slab) and
+            // added to the column in two phases.  Otherwise, when one slab covers
             // the positions and a thread per product column suffices, the
-            // product columns are gathered in the same pass over the groups,
-            // while the group vector is in L1; else in a pass of their own.
-            const bool fuse = nnz <= S * (int)blockDim.x && ty.n_prod <= (int)blockDim.x;
+            // product columns are gathered in the same pass, while the group
+            // vector is in L1; else in a pass of their own.
+            // (QP: all centre types have such roles, chosen at launch)
+            constexpr bool qp = QP;
+            const int qn = qp ? ty.prod_qn[tp] : 0;
+            const bool has_q = (int)threadIdx.x < qn;
+            // the role's position and weight feature; its column and phase are read after the pass
+            int2 qr = make_int2(0, 0);
+            if (has_q) qr = *reinterpret_cast<const int2*>(ty.prod_q + (size_t)tp * kRowsThreads + threadIdx.x);
+            T qv[3] = {0, 0, 0};
+            const bool fuse = qp || (nnz <= S * (int)blockDim.x && ty.n_prod <= (int)blockDim.x);
             ProdCol pc;
-            const bool has_pc = fuse && (int)threadIdx.x < ty.n_prod && prod_col(ty, ipos, nnz, threadIdx.x, pc);
+            const bool has_pc = !qp && fuse && (int)threadIdx.x < ty.n_prod && prod_col(ty, ipos, nnz, threadIdx.x, pc);
             T pv[3] = {0, 0, 0};
             // thread = S consecutive positions of a slab, read as one vector per
             // Cartesian component (the group vectors' stride NL is a multiple of 4)
@@ -1068,6 +1079,11 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                         }
                     }
                     if (has_pc) prod_col_add(pc, src, D + s_doff[k], NL, pv);
+                    if (has_q && slab == 0) {
+                        const T wq = D[s_doff[k] + qr.y];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) qv[c] += wq * src[(size_t)c * NL + qr.x];
+                    }
                 }
 #pragma unroll
                 for (int m = 0; m < S; ++m) {
@@ -1079,6 +1095,20 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
                 }
             }
             if (has_pc) sub_row3<SROW>(s_x, X, ld, r0, pc.col, pv);
+            if (qp) {
+                // roles of phase 0, then of phase 1 (the second feature of a
+                // column): one writer per column at a time; a square column's
+                // one role counts twice
+                int2 cw = make_int2(0, 0);
+                if (has_q) cw = reinterpret_cast<const int2*>(ty.prod_q + (size_t)tp * kRowsThreads + threadIdx.x)[1];
+                if (has_q && (cw.y & 1) == 0) {
+                    const T m = (cw.y & 2) ? (T)2 : (T)1;
+                    const T v[3] = {m * qv[0], m * qv[1], m * qv[2]};
+                    sub_row3<SROW>(s_x, X, ld, r0, cw.x, v);
+                }
+                __syncthreads();
+                if (has_q && (cw.y & 1) == 1) sub_row3<SROW>(s_x, X, ld, r0, cw.x, qv);
+            }
             // product columns, own pass
             for (int p = threadIdx.x; !fuse && p < ty.n_prod; p += blockDim.x) {
                 if (!prod_col(ty, ipos, nnz, p, pc)) continue;
@@ -1142,11 +1172,11 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
     }
     if (SROW) {
         __syncthreads();
-        for (int col = threadIdx.x; col < M.F; col += blockDim.x) {
-            T* o = X + (size_t)col * ld + r0;
-            o[0] = s_x[3 * col];
-            o[1] = s_x[3 * col + 1];
-            o[2] = s_x[3 * col + 2];
+        // three consecutive threads a column: a warp's stores cover about ten
+        // columns' 12-byte runs
+        for (int q = threadIdx.x; q < 3 * M.F; q += blockDim.x) {
+            const int col = q / 3;
+            X[(size_t)col * ld + r0 + (q - 3 * col)] = s_x[q];
         }
     }
 }
@@ -1410,13 +1440,17 @@ void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, 
     // the three rows of a target in shared memory when they fit beside the lists
     // at the kernel's occupancy (FP32: five blocks an SM; FP64: one)
     const size_t rows3 = 3 * sizeof(T) * (size_t)M.F;
-    if (rows3 <= (sizeof(T) == 4 ? 31 * 1024 + 512 : 200 * 1024)) {
-        PG_CUDA(cudaFuncSetAttribute(pg_rows<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows3));
-        pg_rows<T, true><<<B.n_atoms, kRowsThreads, rows3, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X,
-                                                                 ld);
-    } else {
-        pg_rows<T, false><<<B.n_atoms, kRowsThreads, 0, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X, ld);
-    }
+    const bool srow = rows3 <= (sizeof(T) == 4 ? 31 * 1024 + 512 : 200 * 1024);
+    bool qp = true;
+    for (int t = 0; t < M.n_type; ++t) qp = qp && M.types[t].prod_qok;
+    auto go = [&](auto kernel, size_t smem) {
+        PG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<B.n_atoms, kRowsThreads, smem, st>>>(M, B, nb_off, nb_j, d_off, D, Dp, s_off, DS, f_row, X, ld);
+    };
+    if (srow)
+        qp ? go(pg_rows<T, true, true>, rows3) : go(pg_rows<T, true, false>, rows3);
+    else
+        qp ? go(pg_rows<T, false, true>, 0) : go(pg_rows<T, false, false>, 0);
 }
 
 template <typename T>
