@@ -1124,12 +1124,43 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
             __syncthreads();
         }
     }
-    // self rows: the target as a centre (type tj), its DS self vectors (per type pair, by position)
+    // self rows: the target as a centre (type tj), its DS self vectors (per type
+    // pair, by position).  With product roles (QP): per type pair, thread =
+    // position for the linear columns (contiguous DS reads), then thread = role
+    // for the product columns (phases apart); else thread = feature / column.
     const DevType& ty = M.types[tj];
     const int nl = ty.n_lin, npos = ty.n_pos;
     const T* Di = D + d_off[gj];
     const T* dsa = DS + s_off[gj];
-    for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    if (QP) {
+        for (int l = 0; l < ty.n_tpl; ++l) {
+            const int tpl = ty.tpl_tp[l];
+            const int* pm = ty.tp_perm + (size_t)tpl * npos;
+            const T* ds = dsa + (size_t)l * 9 * npos;
+            for (int x = threadIdx.x; x < ty.tp_nnz[tpl]; x += blockDim.x) {
+                const int k = pm[x];
+                if (k < 0) continue;
+                const int col = ty.lin_col[k];
+                if (col < 0) continue;
+                const T v[3] = {ds[x], ds[npos + x], ds[2 * npos + x]};
+                sub_row3<SROW>(s_x, X, ld, r0, col, v, true);
+            }
+            const bool has_q = (int)threadIdx.x < ty.prod_qn[tpl];
+            int4 qr = make_int4(0, 0, 0, 0);
+            T v[3] = {0, 0, 0};
+            if (has_q) {
+                qr = ty.prod_q[(size_t)tpl * kRowsThreads + threadIdx.x];
+                const T wq = ((qr.w & 2) ? (T)2 : (T)1) * Di[qr.y];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[c] = wq * ds[(size_t)c * npos + qr.x];
+            }
+            if (has_q && (qr.w & 1) == 0) sub_row3<SROW>(s_x, X, ld, r0, qr.z, v, true);
+            __syncthreads();
+            if (has_q && (qr.w & 1) == 1) sub_row3<SROW>(s_x, X, ld, r0, qr.z, v, true);
+            __syncthreads();
+        }
+    }
+    for (int k = threadIdx.x; !QP && k < nl; k += blockDim.x) {
         const int col = ty.lin_col[k];
         if (col < 0) continue;
         T v0 = 0, v1 = 0, v2 = 0;
@@ -1144,7 +1175,7 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
         sub_row3<SROW>(s_x, X, ld, r0, col, v, true);
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < ty.n_prod; p += blockDim.x) {
+    for (int p = threadIdx.x; !QP && p < ty.n_prod; p += blockDim.x) {
         const int col = ty.prod_col[p];
         int k0, k1, k2, w;
         unpack_col(ty.col_pack[col], k0, k1, k2, w);
