@@ -20,6 +20,59 @@ FlatTerm make_term(double coeff, const std::vector<int>& ids, int conj) {
     return t;
 }
 
+// Depth-first packing of the costs (taken in descending order) into nb bins of
+// capacity cap; bins of equal load are tried once per item.  False when none
+// exists or after `budget` nodes.
+bool pack_dfs(const std::vector<int>& cost, const std::vector<int>& order, size_t t, int cap, std::vector<int>& load,
+              std::vector<int>& bin, long& budget) {
+    if (t == order.size()) return true;
+    if (--budget < 0) return false;
+    const int i = order[t];
+    for (size_t b = 0; b < load.size(); ++b) {
+        if (load[b] + cost[i] > cap) continue;
+        bool seen = false;
+        for (size_t e = 0; e < b && !seen; ++e) seen = load[e] == load[b];
+        if (seen) continue;
+        load[b] += cost[i];
+        bin[i] = (int)b;
+        if (pack_dfs(cost, order, t + 1, cap, load, bin, budget)) return true;
+        load[b] -= cost[i];
+    }
+    return false;
+}
+
+// Bins (warps) for the costs (groups) with a small largest load: longest first
+// to the least-loaded bin, then an exact search for each smaller largest load
+// down to the lower bound (bounded in nodes; the best packing found is kept).
+std::vector<int> pack_groups(const std::vector<int>& cost, int nb) {
+    std::vector<int> order(cost.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<int> bin(cost.size(), 0), load(nb, 0);
+    for (int i : order) {
+        const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[b] += cost[i];
+        bin[i] = b;
+    }
+    int best = *std::max_element(load.begin(), load.end());
+    long total = 0;
+    int top = 0;
+    for (int c : cost) {
+        total += c;
+        top = std::max(top, c);
+    }
+    const int lower = std::max(top, (int)((total + nb - 1) / nb));
+    for (int cap = lower; cap < best; ++cap) {
+        std::vector<int> l2(nb, 0), b2(cost.size(), 0);
+        long budget = 200000;
+        if (pack_dfs(cost, order, 0, cap, l2, b2, budget)) {
+            bin = b2;
+            break;
+        }
+    }
+    return bin;
+}
+
 }  // namespace
 
 FlatModel flatten_model(const ModelTables& mt) {
@@ -290,8 +343,8 @@ FlatModel flatten_model(const ModelTables& mt) {
                 }
             }
             ft.lay_size = (int)ft.lay_ent.size();
-            // warp schedule of the groups: longest first, each to the least-loaded
-            // warp (a group costs its ranks plus about three ranks of epilogue)
+            // warp schedule of the groups (a group costs its ranks plus about
+            // three ranks of epilogue): the smallest largest warp load found
             std::vector<std::vector<std::vector<int>>> lists(ntp, std::vector<std::vector<int>>(kLayWarps));
             ft.n_rounds = 0;
             for (int tp = 0; tp < ntp; ++tp) {
@@ -301,13 +354,11 @@ FlatModel flatten_model(const ModelTables& mt) {
                 std::stable_sort(gs.begin(), gs.end(), [&](int a, int b) {
                     return ft.lay_grp_cnt[(size_t)tp * ng + a] > ft.lay_grp_cnt[(size_t)tp * ng + b];
                 });
-                std::vector<int> load(kLayWarps, 0);
-                for (int g : gs) {
-                    const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-                    load[w] += ft.lay_grp_cnt[(size_t)tp * ng + g] + 3;
-                    lists[tp][w].push_back(g);
-                    ft.n_rounds = std::max(ft.n_rounds, (int)lists[tp][w].size());
-                }
+                std::vector<int> cost;
+                for (int g : gs) cost.push_back(ft.lay_grp_cnt[(size_t)tp * ng + g] + 3);
+                const std::vector<int> wof = pack_groups(cost, kLayWarps);
+                for (size_t q = 0; q < gs.size(); ++q) lists[tp][wof[q]].push_back(gs[q]);
+                for (int w = 0; w < kLayWarps; ++w) ft.n_rounds = std::max(ft.n_rounds, (int)lists[tp][w].size());
             }
             ft.lay_sched.assign((size_t)ntp * ft.n_rounds * kLayWarps, -1);
             for (int tp = 0; tp < ntp; ++tp)
