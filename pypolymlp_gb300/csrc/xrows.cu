@@ -1046,7 +1046,9 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 5 : 1) pg_rows(
             // the positions and a thread per product column suffices, the
             // product columns are gathered in the same pass, while the group
             // vector is in L1; else in a pass of their own.
-            // (QP: all centre types have such roles, chosen at launch)
+            // (QP: all centre types have such roles and the rows are in shared
+            // memory, chosen at launch: in X itself, the roles' and positions'
+            // separate adds would each be a read-modify-write of X)
             constexpr bool qp = QP;
             const int qn = qp ? ty.prod_qn[tp] : 0;
             const bool has_q = (int)threadIdx.x < qn;
@@ -1472,7 +1474,7 @@ void launch_rows(const DevModel& M, const DevBatch& B, const long long* nb_off, 
     // at the kernel's occupancy (FP32: five blocks an SM; FP64: one)
     const size_t rows3 = 3 * sizeof(T) * (size_t)M.F;
     const bool srow = rows3 <= (sizeof(T) == 4 ? 31 * 1024 + 512 : 200 * 1024);
-    bool qp = true;
+    bool qp = srow;
     for (int t = 0; t < M.n_type; ++t) qp = qp && M.types[t].prod_qok;
     auto go = [&](auto kernel, size_t smem) {
         PG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
