@@ -81,7 +81,7 @@ MODELS = {
 # dram__bytes_write.sum 1.497 GB).  The kernel's traffic is the group vectors it
 # writes, which grow with the pair images, in proportion to the rows; the bench
 # line scales it to a launch by the rows the launch processes.
-NCU_ROWS_PAIRS_BYTES_PER_ROW = {"cfg2": (0.282137 + 1.496542) * 1e9 / 5552}
+NCU_ROWS_PAIRS_BYTES_PER_ROW = {"cfg2": (0.291940 + 1.483896) * 1e9 / 5552}
 
 
 def log(*a):
