@@ -130,39 +130,11 @@ void DeviceModel::build(const FlatModel& fm, bool fp64) {
         d.n_prod = (int)prod.size();
         d.lin_col = (const int*)up(lin);
         d.prod_col = (const int*)up(prod);
-        {
-            // product-column roles per type pair (stage B), when every product
-            // column is a product of two features and the roles fit a block
-            bool ok = true;
-            for (int c : prod) ok = ok && ft.col_ncomp[c] == 2;
-            std::vector<int> qn(fm.n_tp, 0);
-            std::vector<int4> q((size_t)fm.n_tp * kRowsThreads, make_int4(0, 0, 0, 0));
-            for (int tp = 0; ok && tp < fm.n_tp; ++tp) {
-                const int nnz = ft.tp_nnz[tp];
-                const int* ipos = ft.tp_ipos.data() + (size_t)tp * ft.n_lin;
-                std::vector<int4> r;
-                for (int c : prod) {
-                    const int k0 = ft.comp_k[(size_t)c * 3], k1 = ft.comp_k[(size_t)c * 3 + 1];
-                    if (k0 == k1) {
-                        if (ipos[k0] < nnz) r.push_back(make_int4(ipos[k0], k0, c, 2));
-                    } else {
-                        if (ipos[k0] < nnz) r.push_back(make_int4(ipos[k0], k1, c, 0));
-                        if (ipos[k1] < nnz) r.push_back(make_int4(ipos[k1], k0, c, 1));
-                    }
-                }
-                if ((int)r.size() > kRowsThreads) {
-                    ok = false;
-                    break;
-                }
-                // by position: the lanes of a warp read few distinct group-vector values
-                std::stable_sort(r.begin(), r.end(), [](const int4& a, const int4& b) { return a.x < b.x; });
-                qn[tp] = (int)r.size();
-                std::copy(r.begin(), r.end(), q.begin() + (size_t)tp * kRowsThreads);
-            }
-            d.prod_qok = ok ? 1 : 0;
-            d.prod_qn = (const int*)up(qn);
-            d.prod_q = (const int4*)up(q);
-        }
+        // product-column roles of stage B (host tables: 4 ints a role)
+        static_assert(kRowRoles == kRowsThreads, "a stage-B thread per product-column role");
+        d.prod_qok = ft.prod_qok;
+        d.prod_qn = (const int*)up(ft.prod_qn);
+        d.prod_q = (const int4*)up(ft.prod_q);
         d.n_groups = ft.n_groups;
         d.n_pos = ft.n_pos;
         d.lay_size = ft.lay_size;

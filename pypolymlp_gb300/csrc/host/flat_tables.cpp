@@ -365,6 +365,42 @@ FlatModel flatten_model(const ModelTables& mt) {
                 for (int w = 0; w < kLayWarps; ++w)
                     for (size_t k = 0; k < lists[tp][w].size(); ++k)
                         ft.lay_sched[((size_t)tp * ft.n_rounds + k) * kLayWarps + w] = lists[tp][w][k];
+            // product-column roles of stage B
+            {
+                const int F = (int)ft.col_ncomp.size();
+                bool ok = true;
+                for (int c = 0; c < F; ++c) ok = ok && ft.col_ncomp[c] <= 2;
+                ft.prod_qn.assign(ntp, 0);
+                ft.prod_q.assign((size_t)ntp * kRowRoles * 4, 0);
+                for (int tp = 0; ok && tp < ntp; ++tp) {
+                    const int nnz = ft.tp_nnz[tp];
+                    const int* ipos = ft.tp_ipos.data() + (size_t)tp * nl;
+                    std::vector<std::array<int, 4>> r;
+                    for (int c = 0; c < F; ++c) {
+                        if (ft.col_ncomp[c] != 2) continue;
+                        const int k0 = ft.comp_k[(size_t)c * 3], k1 = ft.comp_k[(size_t)c * 3 + 1];
+                        if (k0 == k1) {
+                            if (ipos[k0] < nnz) r.push_back({ipos[k0], k0, c, 2});
+                        } else {
+                            if (ipos[k0] < nnz) r.push_back({ipos[k0], k1, c, 0});
+                            if (ipos[k1] < nnz) r.push_back({ipos[k1], k0, c, 1});
+                        }
+                    }
+                    if ((int)r.size() > kRowRoles) {
+                        ok = false;
+                        break;
+                    }
+                    // by position: the lanes of a warp read few distinct group-vector values
+                    std::stable_sort(r.begin(), r.end(), [](const std::array<int, 4>& a, const std::array<int, 4>& b) {
+                        return a[0] < b[0];
+                    });
+                    ft.prod_qn[tp] = (int)r.size();
+                    for (size_t t = 0; t < r.size(); ++t)
+                        for (int v = 0; v < 4; ++v) ft.prod_q[((size_t)tp * kRowRoles + t) * 4 + v] = r[t][v];
+                }
+                ft.prod_qok = ok ? 1 : 0;
+                if (!ok) std::fill(ft.prod_qn.begin(), ft.prod_qn.end(), 0);
+            }
         }
     }
     // Legendre / Y_lm constants, computed in IEEE double with the reference's

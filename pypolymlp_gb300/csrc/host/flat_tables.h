@@ -15,6 +15,7 @@ namespace pg {
 
 constexpr int kMaxOrder = 6;  // gtinv order supported by the reference tables
 constexpr int kLayWarps = 8;  // warps of a stage-A block (the contraction's group schedule)
+constexpr int kRowRoles = 256;  // threads of a stage-B block: the most product-column roles of a type pair
 
 // One product term: coeff * prod(a[ids[0..n)]) (ids: full local ids).
 struct FlatTerm {
@@ -80,10 +81,19 @@ struct FlatType {
     // of a rank read few distinct keys.  tp_nnz[tp] = 64 n_g(tp): the positions
     // that can hold derivatives of tp; the others' derivatives vanish.
     // lay_sched[tp][k][w] (n_rounds x kLayWarps per type pair): the k-th group
-    // of warp w in stage A, or -1; longest groups first, each to the
-    // least-loaded warp.
+    // of warp w in stage A, or -1; the packing with the smallest largest warp
+    // load found (a group costs its ranks + 3).
     int n_groups = 0, lay_size = 0, n_pos = 0, n_rounds = 0;
     std::vector<int> lay_ent, lay_key, lay_grp_base, lay_grp_cnt, tp_perm, tp_ipos, tp_pos_nid, tp_nnz, lay_sched;
+    // Product-column roles of stage B (prod_qok: every product column of this
+    // type is a product of two features and each type pair has at most
+    // kRowRoles roles).  Per type pair tp, prod_qn[tp] roles, one per (column,
+    // differentiated feature k with a position below tp_nnz):
+    // prod_q[(tp * kRowRoles + t) * 4 + {0,1,2,3}] = {position of k, the other
+    // feature (the weight), column, phase | 2 * (square column)}, by position.
+    // A column's phase-0 role is its first feature's, phase 1 its second's.
+    int prod_qok = 0;
+    std::vector<int> prod_qn, prod_q;
     // type pairs with heads for this centre type: local index or -1, and back
     std::vector<int> tpl, tpl_tp;
 };

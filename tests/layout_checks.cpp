@@ -7,7 +7,9 @@
 // of their features and name the key of lane l's first feature, or lane 0's
 // past its entries; the slots cover every entry once; and the ranks read few
 // distinct keys (the mean over ranks is reported and bounded by 4); the warp
-// schedule names every group with entries once.  Returns 0
+// schedule names every group with entries once; the product-column roles of
+// stage B cover each (column, differentiated feature with data) once, one role
+// per column and phase, by position.  Returns 0
 // and a summary, or 1 and the first violation, in msg.
 #include <cstdio>
 #include <set>
@@ -20,7 +22,7 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
     using namespace pg;
     const FlatModel fm = flatten_model(build_model_tables(feature_params_from_abi(p)));
     const int ntp = fm.n_tp;
-    long ranks = 0, distinct = 0, slots = 0, entries = 0;
+    long ranks = 0, distinct = 0, slots = 0, entries = 0, roles = 0, role_types = 0;
     for (size_t t = 0; t < fm.types.size(); ++t) {
         const FlatType& ft = fm.types[t];
         const int nl = ft.n_lin, ng = ft.n_groups, np = ft.n_pos;
@@ -146,12 +148,61 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
                 snprintf(msg, n_msg, "type %zu: entry %zu is in %d slots", t, e, seen[e]);
                 return 1;
             }
+        // product-column roles of stage B: with prod_qok, every (column of two
+        // features, differentiated feature with data in tp) has one role naming
+        // its position and the other feature, a column has at most one role per
+        // phase, and the roles run by position
+        const int F = (int)ft.col_ncomp.size();
+        bool two = true;
+        for (int c = 0; c < F; ++c) two = two && ft.col_ncomp[c] <= 2;
+        if (ft.prod_qok && !two) {
+            snprintf(msg, n_msg, "type %zu: product roles with a column of three features", t);
+            return 1;
+        }
+        for (int tp = 0; ft.prod_qok && tp < ntp; ++tp) {
+            const int nq = ft.prod_qn[tp], nnz = ft.tp_nnz[tp];
+            const int* ipos = ft.tp_ipos.data() + (size_t)tp * nl;
+            if (nq > kRowRoles) {
+                snprintf(msg, n_msg, "type %zu tp %d: %d roles", t, tp, nq);
+                return 1;
+            }
+            std::set<std::pair<int, int>> want, got, phase_col;
+            for (int c = 0; c < F; ++c) {
+                if (ft.col_ncomp[c] != 2) continue;
+                const int k0 = ft.comp_k[(size_t)c * 3], k1 = ft.comp_k[(size_t)c * 3 + 1];
+                if (ipos[k0] < nnz) want.insert({c, k0});
+                if (ipos[k1] < nnz) want.insert({c, k1});
+            }
+            int prev = -1;
+            for (int q = 0; q < nq; ++q) {
+                const int* r = ft.prod_q.data() + ((size_t)tp * kRowRoles + q) * 4;
+                const int x = r[0], kw = r[1], c = r[2], ph = r[3] & 1, sq = r[3] >> 1;
+                const int k = x >= 0 && x < np ? ft.tp_perm[(size_t)tp * np + x] : -1;
+                const bool col_ok = c >= 0 && c < F && ft.col_ncomp[c] == 2;
+                const int k0 = col_ok ? ft.comp_k[(size_t)c * 3] : -2, k1 = col_ok ? ft.comp_k[(size_t)c * 3 + 1] : -2;
+                const bool pair_ok = col_ok && ((ph == 0 && k == k0 && kw == k1) || (ph == 1 && k == k1 && kw == k0));
+                if (x >= nnz || k < 0 || !pair_ok || sq != (k0 == k1 ? 1 : 0) || (sq && ph) || x < prev ||
+                    !got.insert({c, k}).second || !phase_col.insert({c, ph}).second) {
+                    snprintf(msg, n_msg, "type %zu tp %d: role %d (position %d, weight %d, column %d, flags %d)", t, tp,
+                             q, x, kw, c, r[3]);
+                    return 1;
+                }
+                prev = x;
+            }
+            if (got != want) {
+                snprintf(msg, n_msg, "type %zu tp %d: %zu roles, %zu expected", t, tp, got.size(), want.size());
+                return 1;
+            }
+            roles += nq;
+        }
+        role_types += ft.prod_qok;
     }
     if (ranks > 0 && distinct > 4 * ranks) {
         snprintf(msg, n_msg, "ranks read %.2f distinct keys on average", (double)distinct / ranks);
         return 1;
     }
-    snprintf(msg, n_msg, "ranks %ld, distinct keys per rank %.2f, slot efficiency %.3f", ranks,
-             ranks ? (double)distinct / ranks : 0.0, slots ? (double)entries / slots : 0.0);
+    snprintf(msg, n_msg, "ranks %ld, distinct keys per rank %.2f, slot efficiency %.3f, product roles %ld (%ld of %zu types)",
+             ranks, ranks ? (double)distinct / ranks : 0.0, slots ? (double)entries / slots : 0.0, roles, role_types,
+             fm.types.size());
     return 0;
 }

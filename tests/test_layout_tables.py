@@ -33,7 +33,9 @@ def checker(tmp_path_factory):
          gtinv_maxl=(6, 4)),
     dict(n_type=1, cutoff=6.0, model_type=2, max_p=2, gaussian_params2=(0.0, 5.0, 8), gtinv_order=2,
          gtinv_maxl=(4,)),
-], ids=["binary", "ternary", "unary"])
+    dict(n_type=2, cutoff=6.0, model_type=2, max_p=3, gaussian_params2=(0.0, 5.0, 6), gtinv_order=2,
+         gtinv_maxl=(4,)),
+], ids=["binary", "ternary", "unary", "binary_p3"])
 def test_layout_tables(checker, kw):
     fp = FeatureParams(make_params_dict(**kw))
     msg = C.create_string_buffer(512)
