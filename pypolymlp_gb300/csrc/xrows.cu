@@ -883,15 +883,19 @@ __global__ void __launch_bounds__(kRowsThreads, sizeof(T) == 4 ? 2 : 1)
 // d_a d_b (d_c) receives -sum_i (d_b dd_a + d_a dd_b ...) with centre i's
 // features as weights.  The groups of one centre type are listed in shared
 // memory first; the linear part is a coalesced column sum of their vectors
-// over the positions with entries (each thread owns S positions per slab);
-// the product columns (a few hundred, thread per column) are gathered in the
-// same pass over the groups when one slab covers the positions, else in a
-// pass of their own.  The self rows add the centre's DS vectors to its own
-// type's columns.  Every X element has one owner thread per type, and types
-// are taken in order, so the sums are deterministic.  When the three rows of
-// j (F x 3 values) fit in shared memory, they are summed there and written to
-// X once at the end (plain stores, no read-modify-write of X); else each
-// contribution is added to X in place, in the same order.
+// over the positions with entries (each thread owns S positions per slab).
+// When the three rows of j (F x 3 values) fit in shared memory (SROW), they
+// are summed there and written to X once at the end (plain stores, no
+// read-modify-write of X), and the product columns of two features are
+// summed by role (QP: thread = (column, differentiated feature with data),
+// weight x group-vector value, in the same pass over the groups; the two
+// roles of a column are added in separate phases).  Otherwise each
+// contribution is added to X in place and the product columns are gathered
+// per column (thread per column) in the same pass when one slab covers the
+// positions, else in a pass of their own.  The self rows add the centre's DS
+// vectors to its own type's columns.  Every X element has one writer at a
+// time (per type, per phase), and types and phases are taken in order, so
+// the sums are deterministic.
 __device__ __forceinline__ void unpack_col(int2 c, int& k0, int& k1, int& k2, int& w) {
     k0 = c.x & 0xffff;
     k1 = (c.x >> 16) & 0xffff;
