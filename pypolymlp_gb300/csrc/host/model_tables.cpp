@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <set>
 #include <stdexcept>
+#include <utility>
 
 namespace pg {
 namespace {
@@ -38,6 +39,55 @@ bool type_in_all_pairs(const std::vector<int>& tps, const std::vector<std::vecto
 }
 
 // All sequences of length r over [0, n) in lexicographic order.
+// Keys ascending, each with the sum of its values in the order given (as an
+// ordered map's operator[] += would give).
+template <typename K>
+std::vector<std::pair<K, double>> merge_keys(std::vector<std::pair<K, double>> v) {
+    std::stable_sort(v.begin(), v.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<std::pair<K, double>> out;
+    for (auto& e : v) {
+        if (out.empty() || out.back().first != e.first) out.push_back({std::move(e.first), 0.0});
+        out.back().second += e.second;
+    }
+    return out;
+}
+
+// Up to six ints, ordered and compared as a std::vector<int> of them would be
+// (lexicographically, a prefix first): the keys of one feature term.
+struct SmallKey {
+    static constexpr size_t kCap = 6;
+    std::array<int, kCap> v{};
+    int n = 0;
+    void push(int x) { v[n++] = x; }
+    void sort() {  // insertion sort: at most six values
+        for (int i = 1; i < n; ++i) {
+            const int x = v[i];
+            int j = i - 1;
+            for (; j >= 0 && v[j] > x; --j) v[j + 1] = v[j];
+            v[j + 1] = x;
+        }
+    }
+    SmallKey erase(int i) const {
+        SmallKey k;
+        for (int j = 0; j < n; ++j)
+            if (j != i) k.push(v[j]);
+        return k;
+    }
+    std::vector<int> vec() const { return std::vector<int>(v.begin(), v.begin() + n); }
+    bool operator<(const SmallKey& o) const {
+        return std::lexicographical_compare(v.begin(), v.begin() + n, o.v.begin(), o.v.begin() + o.n);
+    }
+    bool operator==(const SmallKey& o) const { return n == o.n && std::equal(v.begin(), v.begin() + n, o.v.begin()); }
+    bool operator!=(const SmallKey& o) const { return !(*this == o); }
+};
+
+// Ascending distinct keys (as an ordered set's iteration).
+std::vector<std::vector<int>> sorted_unique(std::vector<std::vector<int>> v) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+}
+
 void all_sequences(int n, int r, std::vector<int>& cur, std::vector<std::vector<int>>& out) {
     if ((int)cur.size() == r) {
         out.push_back(cur);
@@ -56,9 +106,25 @@ struct Builder {
     int n_fn = 0;
     std::vector<std::vector<int>> n_to_tp;
     std::vector<std::vector<int>> tpn_to_n_id;
-    std::map<std::array<int, 3>, int> nlmtp_to_global;       // (n, lm, tp) -> global
-    std::map<std::pair<int, int>, int> global_to_local;      // (global, type) -> local
+    // (n, lm, tp) -> global and (global, type) -> local, dense (-1: none)
+    std::vector<int> nlmtp_global, global_local;
     std::vector<int> global_to_global_conj;
+
+    int& nlmtp_to_global(int n, int lm, int tp) {
+        return nlmtp_global[((size_t)n * mt.n_lm + lm) * mt.n_type_pairs + tp];
+    }
+    int nlmtp_at(int n, int lm, int tp) {
+        if (n < 0 || n >= n_fn || lm < 0 || lm >= mt.n_lm || tp < 0 || tp >= mt.n_type_pairs ||
+            nlmtp_to_global(n, lm, tp) < 0)
+            throw std::runtime_error("internal: no order parameter for (n, lm, tp)");
+        return nlmtp_to_global(n, lm, tp);
+    }
+    int& global_to_local(int g, int t) { return global_local[(size_t)g * fp.n_type + t]; }
+    int local_at(int g, int t) {
+        if (g < 0 || (size_t)g * fp.n_type >= global_local.size() || global_to_local(g, t) < 0)
+            throw std::runtime_error("internal: no local index for (global, type)");
+        return global_to_local(g, t);
+    }
     std::vector<std::vector<int>> comb1_indices, comb2_indices, comb3_indices;
 
     explicit Builder(const FeatureParams& f) : fp(f) { mt.fp = f; }
@@ -102,6 +168,7 @@ struct Builder {
                 a.global_id = gid++;
                 global.push_back(a);
             }
+        global_local.assign(global.size() * fp.n_type, -1);
         for (const auto& a : global) {
             const int t1 = mt.tp_to_types[a.tp][0], t2 = mt.tp_to_types[a.tp][1];
             const int l1 = (int)mt.types[t1].ntp.size(), l2 = (int)mt.types[t2].ntp.size();
@@ -109,13 +176,13 @@ struct Builder {
             b.ilocal_id = l1;
             b.jlocal_id = l2;
             mt.types[t1].ntp.push_back(b);
-            global_to_local[{a.global_id, t1}] = l1;
+            global_to_local(a.global_id, t1) = l1;
             if (t1 != t2) {
                 Ntp c = a;
                 c.ilocal_id = l2;
                 c.jlocal_id = l1;
                 mt.types[t2].ntp.push_back(c);
-                global_to_local[{a.global_id, t2}] = l2;
+                global_to_local(a.global_id, t2) = l2;
             }
         }
         // linear features: one per ntp, in global ntp order (polymlp_features_utils.cpp:25)
@@ -129,7 +196,7 @@ struct Builder {
             for (int q = 0; q < (t1 == t2 ? 1 : 2); ++q) {
                 const int t = q == 0 ? t1 : t2;
                 auto& tt = mt.types[t];
-                const int loc = global_to_local[{a.global_id, t}];
+                const int loc = local_at(a.global_id, t);
                 tt.value_terms.push_back({Term{1.0, {loc}}});
                 tt.deriv_terms.push_back({DerivTerm{1.0, loc, {}}});
                 tt.feature_order.push_back(1);
@@ -203,6 +270,7 @@ struct Builder {
 
         std::vector<Nlmtp> global;
         int gid = 0;
+        nlmtp_global.assign((size_t)n_fn * mt.n_lm * mt.n_type_pairs, -1);
         for (int n = 0; n < n_fn; ++n) {
             const auto& tp_n = n_to_tp[n];
             for (int lm = 0; lm < mt.n_lm; ++lm) {
@@ -222,7 +290,7 @@ struct Builder {
                     a.tp = tp;
                     a.global_id = gid;
                     a.global_conj_id = gid - conj_subtract;
-                    nlmtp_to_global[{n, lm, tp}] = gid;
+                    nlmtp_to_global(n, lm, tp) = gid;
                     global.push_back(a);
                     ++gid;
                 }
@@ -230,6 +298,7 @@ struct Builder {
         }
         global_to_global_conj.resize(global.size());
         for (const auto& a : global) global_to_global_conj[a.global_id] = a.global_conj_id;
+        global_local.assign(global.size() * fp.n_type, -1);
 
         for (const auto& a : global) {
             const int t1 = mt.tp_to_types[a.tp][0], t2 = mt.tp_to_types[a.tp][1];
@@ -243,7 +312,7 @@ struct Builder {
             b.jlocal_noconj_id = nc2;
             T1.full.push_back(b);
             if (!a.conj) T1.noconj.push_back(b);
-            global_to_local[{a.global_id, t1}] = l1;
+            global_to_local(a.global_id, t1) = l1;
             if (t1 != t2) {
                 Nlmtp c = a;
                 c.ilocal_id = l2;
@@ -251,12 +320,12 @@ struct Builder {
                 c.jlocal_noconj_id = nc1;
                 T2.full.push_back(c);
                 if (!a.conj) T2.noconj.push_back(c);
-                global_to_local[{a.global_id, t2}] = l2;
+                global_to_local(a.global_id, t2) = l2;
             }
         }
         for (int t = 0; t < fp.n_type; ++t) {
-            for (auto& a : mt.types[t].full) a.ilocal_conj_id = global_to_local.at({a.global_conj_id, t});
-            for (auto& a : mt.types[t].noconj) a.ilocal_conj_id = global_to_local.at({a.global_conj_id, t});
+            for (auto& a : mt.types[t].full) a.ilocal_conj_id = local_at(a.global_conj_id, t);
+            for (auto& a : mt.types[t].noconj) a.ilocal_conj_id = local_at(a.global_conj_id, t);
         }
     }
 
@@ -377,12 +446,6 @@ struct Builder {
                     }
     }
 
-    std::vector<int> locals_of(const std::vector<int>& globals, int t) {
-        std::vector<int> out;
-        out.reserve(globals.size());
-        for (int g : globals) out.push_back(global_to_local.at({g, t}));
-        return out;
-    }
 
     // polymlp_features_utils.cpp:48-132: linear gtinv features of each type,
     // with the representative (id or conjugate-id) product used for values.
@@ -391,41 +454,50 @@ struct Builder {
             const auto& tp_comb = mt.tp_combs[lt.order][lt.tp_comb_id];
             const auto& lm_list = fp.lm_array.at(lt.lm_comb_id);
             const auto& coeffs = fp.lm_coeffs.at(lt.lm_comb_id);
+            if (lm_list.empty()) throw std::runtime_error("internal: an invariant without terms");
             for (int t : lt.type1) {
-                std::vector<Term> feat, feat_rep;
+                // per term: its globals g1 (sorted), the conjugate's g2 (sorted),
+                // the representative min(g1, g2), and their local indices
+                std::vector<std::pair<SmallKey, double>> vm;
+                std::vector<std::pair<std::pair<int, SmallKey>, double>> dm;
+                vm.reserve(lm_list.size());
+                dm.reserve(lm_list.size() * lm_list[0].size());
+                auto& pd = prod_deriv_keys[t];
                 for (size_t i = 0; i < lm_list.size(); ++i) {
-                    std::vector<int> g1;
-                    for (size_t k = 0; k < lm_list[i].size(); ++k)
-                        g1.push_back(nlmtp_to_global.at({lt.n, lm_list[i][k], tp_comb[k]}));
-                    std::sort(g1.begin(), g1.end());
-                    std::vector<int> g2;
-                    for (int g : g1) g2.push_back(global_to_global_conj[g]);
-                    std::sort(g2.begin(), g2.end());
-                    const auto& rep = std::min(g1, g2);
-                    feat.push_back(Term{coeffs[i], locals_of(g1, t)});
-                    feat_rep.push_back(Term{coeffs[i], locals_of(rep, t)});
+                    if (lm_list[i].size() > SmallKey::kCap) throw std::runtime_error("gtinv order must be 1..6");
+                    SmallKey g1, g2, l1, lr;
+                    for (size_t k = 0; k < lm_list[i].size(); ++k) g1.push(nlmtp_at(lt.n, lm_list[i][k], tp_comb[k]));
+                    g1.sort();
+                    for (int k = 0; k < g1.n; ++k) g2.push(global_to_global_conj[g1.v[k]]);
+                    g2.sort();
+                    const SmallKey& r = (g2 < g1) ? g2 : g1;
+                    for (int k = 0; k < g1.n; ++k) {
+                        l1.push(local_at(g1.v[k], t));
+                        lr.push(local_at(r.v[k], t));
+                    }
+                    vm.push_back({lr, coeffs[i]});
+                    for (int k = 0; k < l1.n; ++k) {
+                        dm.push_back({{l1.v[k], l1.erase(k)}, coeffs[i]});
+                        pd.push_back(l1.erase(k));
+                    }
                 }
                 auto& tt = mt.types[t];
-                tt.feature_order.push_back((int)feat[0].ids.size());
+                tt.feature_order.push_back((int)lm_list[0].size());
                 // merge identical representative products (mapped features)
-                std::map<std::vector<int>, double> vm;
-                for (const auto& s : feat_rep) vm[s.ids] += s.coeff;
                 std::vector<Term> vterms;
-                for (const auto& kv : vm) vterms.push_back(Term{kv.second, kv.first});
-                tt.value_terms.push_back(vterms);
+                for (const auto& kv : merge_keys(std::move(vm))) vterms.push_back(Term{kv.second, kv.first.vec()});
+                tt.value_terms.push_back(std::move(vterms));
                 // derivative terms merged by (head, rest), sorted by head then rest
-                std::map<std::pair<int, std::vector<int>>, double> dm;
-                for (const auto& s : feat)
-                    for (size_t i = 0; i < s.ids.size(); ++i) dm[{s.ids[i], erase_one(s.ids, i)}] += s.coeff;
                 std::vector<DerivTerm> dterms;
-                for (const auto& kv : dm) dterms.push_back(DerivTerm{kv.second, kv.first.first, kv.first.second});
-                tt.deriv_terms.push_back(dterms);
-                raw_features[t].push_back(feat);
+                for (const auto& kv : merge_keys(std::move(dm)))
+                    dterms.push_back(DerivTerm{kv.second, kv.first.first, kv.first.second.vec()});
+                tt.deriv_terms.push_back(std::move(dterms));
             }
         }
     }
 
-    std::vector<std::vector<std::vector<Term>>> raw_features;  // [type][feature] non-merged terms
+    // per type: the erase-one keys of every (unmerged) feature term (prod_deriv candidates)
+    std::vector<std::vector<SmallKey>> prod_deriv_keys;
 
     void finalize_types() {
         for (int t = 0; t < fp.n_type; ++t) {
@@ -443,19 +515,20 @@ struct Builder {
                                            {map1.at(mt.comb3[i][0]), map1.at(mt.comb3[i][1]),
                                             map1.at(mt.comb3[i][2])}});
             // prod_deriv keys: every erase-one key of every term (features.cpp:92)
-            std::set<std::vector<int>> pd;
             if (fp.gtinv) {
-                for (const auto& feat : raw_features[t])
-                    for (const auto& s : feat)
-                        for (size_t i = 0; i < s.ids.size(); ++i) pd.insert(erase_one(s.ids, i));
+                auto& pd = prod_deriv_keys[t];
+                std::sort(pd.begin(), pd.end());
+                pd.erase(std::unique(pd.begin(), pd.end()), pd.end());
+                tt.prod_deriv.clear();
+                for (const auto& k : pd) tt.prod_deriv.push_back(k.vec());
             } else {
-                if (!tt.ntp.empty()) pd.insert(std::vector<int>{});
+                tt.prod_deriv.clear();
+                if (!tt.ntp.empty()) tt.prod_deriv.push_back(std::vector<int>{});
             }
-            tt.prod_deriv.assign(pd.begin(), pd.end());
-            std::set<std::vector<int>> pf;
+            std::vector<std::vector<int>> pf;
             for (const auto& p : tt.poly)
-                for (size_t i = 0; i < p.local_ids.size(); ++i) pf.insert(erase_one(p.local_ids, i));
-            tt.prod_features.assign(pf.begin(), pf.end());
+                for (size_t i = 0; i < p.local_ids.size(); ++i) pf.push_back(erase_one(p.local_ids, i));
+            tt.prod_features = sorted_unique(std::move(pf));
             if (tt.lin_index.size() != tt.value_terms.size())
                 throw std::runtime_error("internal: feature count mismatch");
         }
@@ -470,7 +543,7 @@ ModelTables build_model_tables(const FeatureParams& fp) {
     if ((int)fp.cond.size() != fp.n_type) throw std::runtime_error("pair_params_conditional has wrong shape");
     Builder b(fp);
     b.type_pairs();
-    b.raw_features.assign(fp.n_type, {});
+    b.prod_deriv_keys.assign(fp.n_type, {});
     if (fp.gtinv) {
         b.gtinv_maps();
         b.gtinv_linear_terms();
