@@ -7,11 +7,14 @@
 // of their features and name the key of lane l's first feature, or lane 0's
 // past its entries; the slots cover every entry once; and the ranks read few
 // distinct keys (the mean over ranks is reported and bounded by 4); the warp
-// schedule names every group with entries once; the product-column roles of
+// schedule names every group with entries once, its largest warp load no
+// worse than longest-first; the product-column roles of
 // stage B cover each (column, differentiated feature with data) once, one role
 // per column and phase, by position.  Returns 0
 // and a summary, or 1 and the first violation, in msg.
+#include <algorithm>
 #include <cstdio>
+#include <functional>
 #include <set>
 #include <vector>
 
@@ -22,7 +25,7 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
     using namespace pg;
     const FlatModel fm = flatten_model(build_model_tables(feature_params_from_abi(p)));
     const int ntp = fm.n_tp;
-    long ranks = 0, distinct = 0, slots = 0, entries = 0, roles = 0, role_types = 0;
+    long ranks = 0, distinct = 0, slots = 0, entries = 0, roles = 0, role_types = 0, sched_load = 0, lpt_load = 0;
     for (size_t t = 0; t < fm.types.size(); ++t) {
         const FlatType& ft = fm.types[t];
         const int nl = ft.n_lin, ng = ft.n_groups, np = ft.n_pos;
@@ -79,6 +82,26 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
                     snprintf(msg, n_msg, "type %zu tp %d: group %d scheduled %d times", t, tp, g, sched[g]);
                     return 1;
                 }
+            // the largest warp load (a group costs its ranks + 3) is no worse than
+            // longest-first to the least-loaded warp
+            {
+                std::vector<int> load(kLayWarps, 0), lpt(kLayWarps, 0), cost;
+                for (int q = 0; q < ft.n_rounds * kLayWarps; ++q) {
+                    const int g = ft.lay_sched[(size_t)tp * ft.n_rounds * kLayWarps + q];
+                    if (g >= 0) load[q % kLayWarps] += ft.lay_grp_cnt[(size_t)tp * ng + g] + 3;
+                }
+                for (int g = 0; g < ng; ++g)
+                    if (ft.lay_grp_cnt[(size_t)tp * ng + g] > 0) cost.push_back(ft.lay_grp_cnt[(size_t)tp * ng + g] + 3);
+                std::sort(cost.begin(), cost.end(), std::greater<int>());
+                for (int c : cost) *std::min_element(lpt.begin(), lpt.end()) += c;
+                const int ms = *std::max_element(load.begin(), load.end()), ml = *std::max_element(lpt.begin(), lpt.end());
+                if (ms > ml) {
+                    snprintf(msg, n_msg, "type %zu tp %d: largest warp load %d, longest-first %d", t, tp, ms, ml);
+                    return 1;
+                }
+                sched_load += ms;
+                lpt_load += ml;
+            }
             int prev = 1 << 30;
             for (int g = 0; g < ng; ++g) {
                 const int base = ft.lay_grp_base[(size_t)tp * ng + g], c = ft.lay_grp_cnt[(size_t)tp * ng + g];
@@ -201,8 +224,10 @@ extern "C" int check_layout(const pg_feature_params* p, char* msg, int n_msg) {
         snprintf(msg, n_msg, "ranks read %.2f distinct keys on average", (double)distinct / ranks);
         return 1;
     }
-    snprintf(msg, n_msg, "ranks %ld, distinct keys per rank %.2f, slot efficiency %.3f, product roles %ld (%ld of %zu types)",
+    snprintf(msg, n_msg,
+             "ranks %ld, distinct keys per rank %.2f, slot efficiency %.3f, product roles %ld (%ld of %zu types), "
+             "largest warp loads %ld (longest-first %ld)",
              ranks, ranks ? (double)distinct / ranks : 0.0, slots ? (double)entries / slots : 0.0, roles, role_types,
-             fm.types.size());
+             fm.types.size(), sched_load, lpt_load);
     return 0;
 }
