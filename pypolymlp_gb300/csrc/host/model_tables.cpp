@@ -476,10 +476,7 @@ struct Builder {
                         lr.push(local_at(r.v[k], t));
                     }
                     vm.push_back({lr, coeffs[i]});
-                    for (int k = 0; k < l1.n; ++k) {
-                        dm.push_back({{l1.v[k], l1.erase(k)}, coeffs[i]});
-                        pd.push_back(l1.erase(k));
-                    }
+                    for (int k = 0; k < l1.n; ++k) dm.push_back({{l1.v[k], l1.erase(k)}, coeffs[i]});
                 }
                 auto& tt = mt.types[t];
                 tt.feature_order.push_back((int)lm_list[0].size());
@@ -488,9 +485,16 @@ struct Builder {
                 for (const auto& kv : merge_keys(std::move(vm))) vterms.push_back(Term{kv.second, kv.first.vec()});
                 tt.value_terms.push_back(std::move(vterms));
                 // derivative terms merged by (head, rest), sorted by head then rest
+                // (the rests are the erase-one keys of the feature's terms: prod_deriv
+                // candidates, distinct per feature)
                 std::vector<DerivTerm> dterms;
-                for (const auto& kv : merge_keys(std::move(dm)))
+                const size_t pd0 = pd.size();
+                for (const auto& kv : merge_keys(std::move(dm))) {
                     dterms.push_back(DerivTerm{kv.second, kv.first.first, kv.first.second.vec()});
+                    pd.push_back(kv.first.second);
+                }
+                std::sort(pd.begin() + pd0, pd.end());
+                pd.erase(std::unique(pd.begin() + pd0, pd.end()), pd.end());
                 tt.deriv_terms.push_back(std::move(dterms));
             }
         }
